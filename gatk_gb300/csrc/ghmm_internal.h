@@ -1,0 +1,83 @@
+// ghmm_internal.h -- device-side data layout shared by the kernels (kernels.cu) and the host runtime
+// (runtime.cpp).  Plain C structs: pointers are device addresses.
+#pragma once
+
+#include <cstdint>
+
+namespace ghmm {
+
+// Column-stream byte of a haplotype base (one per haplotype column, haplotypes of a region back to
+// back): bits 0-3 base mask (A=1 C=2 G=4 T=8 N=15), bit 6 first column of a haplotype, bit 7 last.
+constexpr uint8_t kColFirst = 0x40;
+constexpr uint8_t kColLast = 0x80;
+constexpr int kMaxK32 = 8;      // FP32 kernel: rows per lane (strip = 32*K rows)
+constexpr int kMaxK64 = 4;      // FP64 kernel: rows per lane
+constexpr int kMaxReadLen = 1 << 20;
+constexpr int kMaxHapLen = 1 << 20;
+
+// Device lookup tables (QualityUtils / PairHMMModel restated on the host, uploaded once per context).
+struct DevTables {
+    const float *err_f;     // [256] 10^(-q/10)
+    const float *prob_f;    // [256] 1 - 10^(-q/10)
+    const float *err3_f;    // [256] 10^(-q/10) / 3
+    const float *m2m_f;     // [128*128] matchToMatchProb(ins, del), row = ins
+    const double *err_d;
+    const double *prob_d;
+    const double *err3_d;
+    const double *m2m_d;
+};
+
+// Read-pair task of the FP32 pass: two reads of one region (b < 0: single read) against the
+// haplotypes [hap_begin, hap_end) of that region, in K-row-per-lane strips.
+struct F32Task {
+    int32_t read_a, read_b;
+    int32_t hap_begin, hap_end;
+    int32_t region;
+    int16_t nstrips, k;
+    int32_t pad_a, pad_b;  // dummy rows on top of strip 0 (strip rows * nstrips - read length)
+};
+
+// One (read, haplotype) pair for the FP64 kernel.
+struct PairRef {
+    int32_t read, hap;
+};
+
+struct DevBatch {
+    // reads: five planes, byte offsets
+    const uint8_t *bases, *quals, *ins, *dels, *gcp;
+    const int64_t *read_off;
+    // haplotypes
+    const uint8_t *hap_bases;   // raw bytes
+    const uint8_t *hap_code;    // column-stream codes (same indexing as hap_bases)
+    const int64_t *hap_off;
+    const float *hap_init_f;    // 2^120 / H
+    const double *hap_init_d;   // 2^1020 / H
+    // regions
+    const int64_t *region_read_off, *region_hap_off, *out_off;
+    const int32_t *read_region; // region of each read
+    double *out;
+    // FP32 tasks (all buckets, contiguous per K)
+    const F32Task *tasks;
+    // FP64 queue: entries [0, n_direct) filled by the host, the rest appended by the FP32 pass
+    PairRef *rerun;
+    int32_t *counters;          // [0] FP32 task cursor (per launch), [1] rerun tail, [2] FP64 cursor, [3] error flag
+    int64_t rerun_capacity;
+    // strip-boundary scratch of multi-strip FP32 tasks: per resident warp, max_cols float2 x 3
+    float2 *scratch32;
+    int64_t scratch32_cols;
+    double *scratch64;          // FP64 multi-strip boundary: per resident warp, max_hap_len x 3 doubles
+    int64_t scratch64_cols;
+};
+
+// Kernel launchers (kernels.cu).  All return cudaError_t as int.
+int launch_fp32_bucket(const DevTables &t, const DevBatch &b, int k, int task_begin, int task_count, int grid,
+                       int block, int counter_slot, cudaStream_t s);
+int launch_fp64_queue(const DevTables &t, const DevBatch &b, int grid, int block, cudaStream_t s);
+int launch_plain_region(const DevTables &t, const DevBatch &b, int region, int n_reads, int n_haps, int max_read_len,
+                        cudaStream_t s);
+constexpr int kPlainMaxRead = 1024;
+int fp32_kernel_occupancy(int k, int block, int *blocks_per_sm);
+int fp64_kernel_occupancy(int block, int *blocks_per_sm);
+int measure_peaks_device(int sm_count, double *fp32, double *fp32x2, double *fp64, cudaStream_t s);
+
+}  // namespace ghmm

@@ -1,0 +1,672 @@
+// kernels.cu -- sm_103a kernels of the GB300 PairHMM.
+//
+// The recurrence is LoglessPairHMM's (src/main/java/org/broadinstitute/hellbender/utils/pairhmm/
+// LoglessPairHMM.java:47-67): for matrix row i (read position i-1) and column j (haplotype position j-1),
+//   M(i,j) = prior(i,j) * (M(i-1,j-1)*MM_i + I(i-1,j-1)*IM_i + D(i-1,j-1)*IM_i)
+//   I(i,j) = M(i-1,j)*MI_i + I(i-1,j)*II_i
+//   D(i,j) = M(i,j-1)*MD_i + D(i,j-1)*DD_i
+// with D(0,j) = scale/H, every other row-0 and column-0 entry 0, and
+// log10 L = log10(sum_j M(R,j) + I(R,j)) - log10(scale).
+//
+// Three kernels:
+//  * fp32_bucket_kernel<K, MULTI>: the batched FP32 forward.  One warp runs a read-pair task: two reads of
+//    one region, packed into the .x/.y halves of float2 so every cell update is a packed FFMA2/FMUL2/FADD2,
+//    against all (or a chunk of) the region's haplotypes streamed back to back.  Lane l owns K consecutive
+//    rows; at step s it computes column c = s - l, receiving the row above from lane l-1 by __shfl_up_sync
+//    (an anti-diagonal wavefront).  Reads are padded at the top with "dummy" rows that reproduce the row-0
+//    boundary, so the last read row always sits in lane 31's last slot.  Reads longer than 32*K rows run
+//    as several strips whose boundary row goes through per-warp global scratch.  Rows are pre-scaled so a
+//    cell costs 7 FMA-pipe operations instead of 8:  I^ = I*IM_{i+1},  D^ = D*IM_{i+1}  (IM_{R+1} = 1):
+//       M  = prior * fma(M_diag, MM, I^_diag + D^_diag)
+//       I^ = fma(I^_up, II*IM_{i+1}/IM_i, M_up * MI*IM_{i+1})
+//       D^ = fma(D^_left, DD, M_left * MD*IM_{i+1})
+//    Scale 2^120; a sum below GHMM_FP32_RERUN_THRESHOLD (or not finite) queues the pair for FP64.
+//  * fp64_queue_kernel<K>: the FP64 wavefront (one pair per warp, scale 2^1020, unscaled rows so any
+//    gap-continuation penalty, including 0, is exact), used for reruns and double-precision mode.
+//  * plain_fp64_kernel: the plain form, one pair per thread block sweeping anti-diagonals through shared
+//    memory with a block barrier per diagonal, Java's operation order, one launch per region.
+#include <cuda_runtime.h>
+#include <cfloat>
+#include <cstdint>
+
+#include "../../include/ghmm.h"
+#include "ghmm_internal.h"
+
+namespace ghmm {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+// log10(2^120) and log10(2^1020)
+constexpr double kLog10Scale32 = 36.12359947967774;
+constexpr double kLog10Scale64 = 307.0505955772608;
+
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 zero2() { return make_float2(0.f, 0.f); }
+
+__device__ __forceinline__ float2 shfl_up2(float2 v) {
+    return make_float2(__shfl_up_sync(kFull, v.x, 1), __shfl_up_sync(kFull, v.y, 1));
+}
+
+__device__ __forceinline__ uint32_t base_code(uint8_t b) {
+    switch (b) {
+        case 'A': return 1u;
+        case 'C': return 2u;
+        case 'G': return 4u;
+        case 'T': return 8u;
+        case 'N': return 15u;
+        default: return 0u;
+    }
+}
+
+// Per-row coefficients of one read half (see header comment); dummy rows reproduce the row-0 boundary.
+struct RowCoef {
+    float pm, pe, mm, mi, ii, md, dd;
+    uint32_t code;
+};
+
+__device__ __forceinline__ RowCoef row_coef(const DevTables &T, const DevBatch &B, int64_t off, int R, int p) {
+    RowCoef c;
+    if (p < 0 || p >= R) {
+        c.pm = c.pe = 0.f;
+        c.mm = c.mi = c.ii = c.md = 0.f;
+        c.dd = 1.f;
+        c.code = 0u;
+        return c;
+    }
+    const uint8_t base = B.bases[off + p], q = B.quals[off + p];
+    const uint8_t ins = B.ins[off + p], del = B.dels[off + p], gcp = B.gcp[off + p];
+    const float tim = __ldg(T.prob_f + gcp);
+    const float timn = (p + 1 < R) ? __ldg(T.prob_f + B.gcp[off + p + 1]) : 1.f;
+    c.pm = __ldg(T.prob_f + q);
+    c.pe = (base == 'N') ? c.pm : __ldg(T.err3_f + q);
+    c.mm = __ldg(T.m2m_f + ins * 128 + del);
+    c.mi = __ldg(T.err_f + ins) * timn;
+    c.md = __ldg(T.err_f + del) * timn;
+    const float tii = __ldg(T.err_f + gcp);
+    c.ii = tii * timn / tim;
+    c.dd = tii;
+    c.code = base_code(base);
+    return c;
+}
+
+__device__ __forceinline__ void emit_fp32(const DevBatch &B, float sum, int read, int hap, int64_t out_index) {
+    if (sum >= GHMM_FP32_RERUN_THRESHOLD && sum <= FLT_MAX) {
+        B.out[out_index] = log10((double)sum) - kLog10Scale32;
+    } else {
+        const int idx = atomicAdd(&B.counters[1], 1);
+        if ((int64_t)idx < B.rerun_capacity) {
+            B.rerun[idx].read = read;
+            B.rerun[idx].hap = hap;
+        } else {
+            atomicExch(&B.counters[3], 1);
+        }
+    }
+}
+
+}  // namespace
+
+template <int K, bool MULTI>
+__global__ void __launch_bounds__(128) fp32_bucket_kernel(DevTables T, DevBatch B, int task_begin, int task_count,
+                                                          int counter_slot) {
+    constexpr int S = 32 * K;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    float2 *scratch = nullptr;
+    if (MULTI) scratch = B.scratch32 + warp_global * B.scratch32_cols * 3;
+    const float2 nl0 = lane ? make_float2(1.f, 1.f) : zero2();
+
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&B.counters[counter_slot], 1);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= task_count) break;
+        const F32Task task = B.tasks[task_begin + t];
+        const int ra = task.read_a, rb = task.read_b;
+        const int64_t off_a = B.read_off[ra];
+        const int len_a = (int)(B.read_off[ra + 1] - off_a);
+        int64_t off_b = 0;
+        int len_b = 0;
+        if (rb >= 0) {
+            off_b = B.read_off[rb];
+            len_b = (int)(B.read_off[rb + 1] - off_b);
+        }
+        const int region = task.region;
+        const int64_t hap0 = B.region_hap_off[region];
+        const int nh = (int)(B.region_hap_off[region + 1] - hap0);
+        const int64_t rr0 = B.region_read_off[region];
+        const int64_t out_a = B.out_off[region] + (int64_t)(ra - rr0) * nh - hap0;
+        const int64_t out_b = B.out_off[region] + (int64_t)(rb - rr0) * nh - hap0;
+        const int64_t col0 = B.hap_off[task.hap_begin];
+        const int ncols = (int)(B.hap_off[task.hap_end] - col0);
+        const uint8_t *stream = B.hap_code + col0;
+        float2 tim1;
+        tim1.x = __ldg(T.prob_f + B.gcp[off_a]);
+        tim1.y = rb >= 0 ? __ldg(T.prob_f + B.gcp[off_b]) : 0.f;
+        const int nstrips = MULTI ? task.nstrips : 1;
+
+        for (int strip = 0; strip < nstrips; ++strip) {
+            float2 pm[K], pe[K], cmm[K], cmi[K], cii[K], cmd[K], cdd[K];
+            uint32_t rc[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int slot = strip * S + lane * K + k;
+                const RowCoef a = row_coef(T, B, off_a, len_a, slot - task.pad_a);
+                const RowCoef b = row_coef(T, B, off_b, rb >= 0 ? len_b : 0, slot - task.pad_b);
+                pm[k] = make_float2(a.pm, b.pm);
+                pe[k] = make_float2(a.pe, b.pe);
+                cmm[k] = make_float2(a.mm, b.mm);
+                cmi[k] = make_float2(a.mi, b.mi);
+                cii[k] = make_float2(a.ii, b.ii);
+                cmd[k] = make_float2(a.md, b.md);
+                cdd[k] = make_float2(a.dd, b.dd);
+                rc[k] = a.code | (b.code << 8);
+            }
+            float2 Mp[K], Ip[K], Dp[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) Mp[k] = Ip[k] = Dp[k] = zero2();
+            float2 gM = zero2(), gI = zero2(), gD = zero2();  // row above, previous column (diagonal)
+            float2 bnd = zero2();                               // lane 0, strip 0: row-0 D^ boundary
+            float2 acc = zero2();
+            int hap = task.hap_begin - 1;
+            const bool last_strip = (strip == nstrips - 1);
+            float2 nxM = zero2(), nxI = zero2(), nxD = zero2();  // prefetched strip boundary (MULTI, lane 0)
+            if (MULTI && strip > 0 && lane == 0 && ncols > 0) {
+                nxM = scratch[0];
+                nxI = scratch[1];
+                nxD = scratch[2];
+            }
+            const int nsteps = ncols + 31;
+            for (int s = 0; s < nsteps; ++s) {
+                const int c = s - lane;
+                const bool valid = (c >= 0) && (c < ncols);
+                const uint32_t code = valid ? (uint32_t)__ldg(stream + c) : 0u;
+                if (code & kColFirst) {
+                    ++hap;
+                    const float init = __ldg(B.hap_init_f + hap);
+                    const float2 X = make_float2(init * tim1.x, init * tim1.y);
+#pragma unroll
+                    for (int k = 0; k < K; ++k) {
+                        const int slot = lane * K + k;
+                        Mp[k] = Ip[k] = zero2();
+                        Dp[k] = make_float2((strip == 0 && slot < task.pad_a) ? X.x : 0.f,
+                                            (strip == 0 && slot < task.pad_b) ? X.y : 0.f);
+                    }
+                    gM = gI = zero2();
+                    gD = make_float2((strip == 0 && lane * K - 1 < task.pad_a) ? X.x : 0.f,
+                                     (strip == 0 && lane * K - 1 < task.pad_b) ? X.y : 0.f);
+                    if (lane == 0 && strip == 0) bnd = X;
+                    acc = zero2();
+                }
+                // row above at this column: lane l-1's last row (computed last step) or the boundary
+                float2 uM = shfl_up2(Mp[K - 1]);
+                float2 uI = shfl_up2(Ip[K - 1]);
+                float2 uD = shfl_up2(Dp[K - 1]);
+                if (MULTI && strip > 0) {
+                    const float2 bM = nxM, bI = nxI, bD = nxD;
+                    if (lane == 0 && c + 1 < ncols) {
+                        nxM = scratch[3 * (c + 1) + 0];
+                        nxI = scratch[3 * (c + 1) + 1];
+                        nxD = scratch[3 * (c + 1) + 2];
+                    }
+                    uM = fma2(uM, nl0, bM);
+                    uI = fma2(uI, nl0, bI);
+                    uD = fma2(uD, nl0, bD);
+                } else {
+                    uM = mul2(uM, nl0);
+                    uI = mul2(uI, nl0);
+                    uD = fma2(uD, nl0, bnd);
+                }
+                const uint32_t hc2 = (code & 15u) * 0x0101u;
+                // pass 1 (bottom-up so the row above is still the previous column): M and D^
+#pragma unroll
+                for (int k = K - 1; k >= 0; --k) {
+                    const float2 dM = k ? Mp[k - 1] : gM;
+                    const float2 dI = k ? Ip[k - 1] : gI;
+                    const float2 dD = k ? Dp[k - 1] : gD;
+                    const uint32_t m = rc[k] & hc2;
+                    float2 pr;
+                    pr.x = (m & 0x00ffu) ? pm[k].x : pe[k].x;
+                    pr.y = (m & 0xff00u) ? pm[k].y : pe[k].y;
+                    const float2 Mn = mul2(pr, fma2(dM, cmm[k], add2(dI, dD)));
+                    const float2 Dn = fma2(Dp[k], cdd[k], mul2(Mp[k], cmd[k]));
+                    Mp[k] = Mn;
+                    Dp[k] = Dn;
+                }
+                // pass 2 (top-down): I^ from the row above at this column
+                float2 aM = uM, aI = uI;
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    const float2 In = fma2(aI, cii[k], mul2(aM, cmi[k]));
+                    Ip[k] = In;
+                    aM = Mp[k];
+                    aI = In;
+                }
+                gM = uM;
+                gI = uI;
+                gD = uD;
+                if (last_strip) {
+                    acc = add2(acc, add2(Mp[K - 1], Ip[K - 1]));
+                    if (lane == 31 && (code & kColLast)) {
+                        emit_fp32(B, acc.x, ra, hap, out_a + hap);
+                        if (rb >= 0) emit_fp32(B, acc.y, rb, hap, out_b + hap);
+                    }
+                } else if (MULTI && lane == 31 && valid) {
+                    scratch[3 * c + 0] = Mp[K - 1];
+                    scratch[3 * c + 1] = Ip[K - 1];
+                    scratch[3 * c + 2] = Dp[K - 1];
+                }
+            }
+            if (MULTI) __syncwarp();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// FP64 wavefront, one (read, haplotype) pair per warp, K rows per lane, strips of 32*K rows.
+template <int K>
+__global__ void __launch_bounds__(128) fp64_queue_kernel(DevTables T, DevBatch B) {
+    constexpr int S = 32 * K;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    double *scratch = B.scratch64 + warp_global * B.scratch64_cols * 3;
+    const int total = min(B.counters[1], (int)B.rerun_capacity);
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&B.counters[2], 1);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= total) break;
+        const PairRef pr = B.rerun[t];
+        const int read = pr.read, hap = pr.hap;
+        const int64_t roff = B.read_off[read];
+        const int R = (int)(B.read_off[read + 1] - roff);
+        const int64_t hoff = B.hap_off[hap];
+        const int H = (int)(B.hap_off[hap + 1] - hoff);
+        const int region = B.read_region[read];
+        const int64_t nh = B.region_hap_off[region + 1] - B.region_hap_off[region];
+        const int64_t out_index = B.out_off[region] + (int64_t)(read - B.region_read_off[region]) * nh +
+                                  (hap - B.region_hap_off[region]);
+        if (R == 0 || H == 0) {
+            if (lane == 0) B.out[out_index] = -INFINITY;
+            continue;
+        }
+        if (H > B.scratch64_cols && R > S) {
+            if (lane == 0) atomicExch(&B.counters[3], 2);
+            continue;
+        }
+        const double init = B.hap_init_d[hap];
+        const int nstrips = (R + S - 1) / S;
+        const int pad = nstrips * S - R;
+        const uint8_t *hb = B.hap_bases + hoff;
+        double acc = 0.0;
+        for (int strip = 0; strip < nstrips; ++strip) {
+            double pm[K], pe[K], tmm[K], tim[K], tmi[K], tii[K], tmd[K];
+            uint32_t rbase[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int p = strip * S + lane * K + k - pad;
+                if (p < 0) {
+                    pm[k] = pe[k] = 0.0;
+                    tmm[k] = tim[k] = tmi[k] = tii[k] = tmd[k] = 0.0;
+                    rbase[k] = 0x100u;  // matches nothing
+                } else {
+                    const uint8_t base = B.bases[roff + p], q = B.quals[roff + p];
+                    const uint8_t ins = B.ins[roff + p], del = B.dels[roff + p], gcp = B.gcp[roff + p];
+                    pm[k] = __ldg(T.prob_d + q);
+                    pe[k] = base == 'N' ? pm[k] : __ldg(T.err3_d + q);
+                    tmm[k] = __ldg(T.m2m_d + ins * 128 + del);
+                    tim[k] = __ldg(T.prob_d + gcp);
+                    tmi[k] = __ldg(T.err_d + ins);
+                    tii[k] = __ldg(T.err_d + gcp);
+                    tmd[k] = __ldg(T.err_d + del);
+                    rbase[k] = base;
+                }
+            }
+            double Mp[K], Ip[K], Dp[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const bool dummy = (strip == 0) && (lane * K + k < pad);
+                Mp[k] = Ip[k] = 0.0;
+                Dp[k] = dummy ? init : 0.0;
+            }
+            // DD of dummy rows is 1 so their D stays at the row-0 value
+            double tdd[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) tdd[k] = ((strip == 0) && (lane * K + k < pad)) ? 1.0 : tii[k];
+            double gM = 0.0, gI = 0.0;
+            double gD = ((strip == 0) && (lane * K - 1 < pad)) ? init : 0.0;
+            const double bnd = (strip == 0) ? init : 0.0;
+            const bool last_strip = strip == nstrips - 1;
+            double nxM = 0.0, nxI = 0.0, nxD = 0.0;
+            if (strip > 0 && lane == 0) {
+                nxM = scratch[0];
+                nxI = scratch[1];
+                nxD = scratch[2];
+            }
+            const int nsteps = H + 31;
+            for (int s = 0; s < nsteps; ++s) {
+                const int c = s - lane;
+                const bool valid = c >= 0 && c < H;
+                const uint32_t y = valid ? (uint32_t)__ldg(hb + c) : 0x200u;
+                const bool yn = (y == 'N');
+                if (c == 0) {  // column-0 boundary (lanes compute ahead of their first column)
+#pragma unroll
+                    for (int k = 0; k < K; ++k) {
+                        Mp[k] = Ip[k] = 0.0;
+                        Dp[k] = ((strip == 0) && (lane * K + k < pad)) ? init : 0.0;
+                    }
+                    gM = gI = 0.0;
+                    gD = ((strip == 0) && (lane * K - 1 < pad)) ? init : 0.0;
+                }
+                double uM = __shfl_up_sync(kFull, Mp[K - 1], 1);
+                double uI = __shfl_up_sync(kFull, Ip[K - 1], 1);
+                double uD = __shfl_up_sync(kFull, Dp[K - 1], 1);
+                if (lane == 0) {
+                    if (strip == 0) {
+                        uM = 0.0;
+                        uI = 0.0;
+                        uD = bnd;
+                    } else {
+                        uM = nxM;
+                        uI = nxI;
+                        uD = nxD;
+                        if (c + 1 < H) {
+                            nxM = scratch[3 * (c + 1) + 0];
+                            nxI = scratch[3 * (c + 1) + 1];
+                            nxD = scratch[3 * (c + 1) + 2];
+                        }
+                    }
+                }
+#pragma unroll
+                for (int k = K - 1; k >= 0; --k) {
+                    const double dM = k ? Mp[k - 1] : gM;
+                    const double dI = k ? Ip[k - 1] : gI;
+                    const double dD = k ? Dp[k - 1] : gD;
+                    const double prior = (rbase[k] == y || yn) ? pm[k] : pe[k];
+                    const double Mn = prior * fma(dM, tmm[k], (dI + dD) * tim[k]);
+                    const double Dn = fma(Dp[k], tdd[k], Mp[k] * tmd[k]);
+                    Mp[k] = Mn;
+                    Dp[k] = Dn;
+                }
+                double aM = uM, aI = uI;
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    const double In = fma(aI, tii[k], aM * tmi[k]);
+                    Ip[k] = In;
+                    aM = Mp[k];
+                    aI = In;
+                }
+                gM = uM;
+                gI = uI;
+                gD = uD;
+                if (valid && lane == 31) {
+                    if (last_strip) {
+                        acc += Mp[K - 1] + Ip[K - 1];
+                    } else {
+                        scratch[3 * c + 0] = Mp[K - 1];
+                        scratch[3 * c + 1] = Ip[K - 1];
+                        scratch[3 * c + 2] = Dp[K - 1];
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        if (lane == 31) B.out[out_index] = log10(acc) - kLog10Scale64;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Plain FP64 form: one (read, haplotype) pair per 256-thread block; thread t owns rows t+1+256m (m<4);
+// three rolling anti-diagonals of M, I, D in shared memory; one barrier per diagonal; Java's order of
+// operations (no fused multiply-add), so the sums equal the FP64 oracle's.
+constexpr int kPlainThreads = 256;
+constexpr int kPlainRows = 4;
+
+__global__ void __launch_bounds__(kPlainThreads) plain_fp64_kernel(DevTables T, DevBatch B, int region, int nh) {
+    extern __shared__ double sm[];
+    const int pair = blockIdx.x;
+    const int64_t read = B.region_read_off[region] + pair / nh;
+    const int64_t hap = B.region_hap_off[region] + pair % nh;
+    const int64_t roff = B.read_off[read];
+    const int R = (int)(B.read_off[read + 1] - roff);
+    const int64_t hoff = B.hap_off[hap];
+    const int H = (int)(B.hap_off[hap + 1] - hoff);
+    const int64_t out_index = B.out_off[region] + pair;
+    if (R == 0 || H == 0) {
+        if (threadIdx.x == 0) B.out[out_index] = -INFINITY;
+        return;
+    }
+    const int W = R + 1;
+    double *Mb = sm, *Ib = sm + 3 * W, *Db = sm + 6 * W;  // [3][W] each
+    const double init = B.hap_init_d[hap];
+    double t_mm[kPlainRows], t_im[kPlainRows], t_mi[kPlainRows], t_ii[kPlainRows], t_md[kPlainRows];
+    double p_m[kPlainRows], p_e[kPlainRows];
+    uint8_t xb[kPlainRows];
+#pragma unroll
+    for (int m = 0; m < kPlainRows; ++m) {
+        const int i = threadIdx.x + 1 + m * kPlainThreads;
+        if (i <= R) {
+            const int p = i - 1;
+            const uint8_t q = B.quals[roff + p], ins = B.ins[roff + p], del = B.dels[roff + p];
+            const uint8_t gcp = B.gcp[roff + p];
+            t_mm[m] = T.m2m_d[ins * 128 + del];
+            t_im[m] = T.prob_d[gcp];
+            t_mi[m] = T.err_d[ins];
+            t_ii[m] = T.err_d[gcp];
+            t_md[m] = T.err_d[del];
+            p_m[m] = T.prob_d[q];
+            p_e[m] = T.err3_d[q];
+            xb[m] = B.bases[roff + p];
+        } else {
+            t_mm[m] = t_im[m] = t_mi[m] = t_ii[m] = t_md[m] = p_m[m] = p_e[m] = 0.0;
+            xb[m] = 0;
+        }
+    }
+    for (int b = 0; b < 3; ++b)
+        for (int i = threadIdx.x; i < W; i += kPlainThreads) {
+            Mb[b * W + i] = 0.0;
+            Ib[b * W + i] = 0.0;
+            Db[b * W + i] = (i == 0) ? init : 0.0;
+        }
+    __syncthreads();
+    double sum = 0.0;
+    for (int d = 2; d <= R + H; ++d) {
+        const int cur = d % 3, p1 = (d + 2) % 3, p2 = (d + 1) % 3;
+#pragma unroll
+        for (int m = 0; m < kPlainRows; ++m) {
+            const int i = threadIdx.x + 1 + m * kPlainThreads;
+            if (i > R) continue;
+            const int j = d - i;
+            if (j == 0) {  // column-0 boundary
+                Mb[cur * W + i] = 0.0;
+                Ib[cur * W + i] = 0.0;
+                Db[cur * W + i] = 0.0;
+                continue;
+            }
+            if (j < 1 || j > H) continue;
+            const uint8_t y = B.hap_bases[hoff + j - 1];
+            const double prior = (xb[m] == y || xb[m] == 'N' || y == 'N') ? p_m[m] : p_e[m];
+            const double mdiag = Mb[p2 * W + i - 1], idiag = Ib[p2 * W + i - 1], ddiag = Db[p2 * W + i - 1];
+            const double mup = Mb[p1 * W + i - 1], iup = Ib[p1 * W + i - 1];
+            const double mleft = Mb[p1 * W + i], dleft = Db[p1 * W + i];
+            const double mv = __dmul_rn(prior, __dadd_rn(__dadd_rn(__dmul_rn(mdiag, t_mm[m]), __dmul_rn(idiag, t_im[m])),
+                                                         __dmul_rn(ddiag, t_im[m])));
+            const double iv = __dadd_rn(__dmul_rn(mup, t_mi[m]), __dmul_rn(iup, t_ii[m]));
+            const double dv = __dadd_rn(__dmul_rn(mleft, t_md[m]), __dmul_rn(dleft, t_ii[m]));
+            Mb[cur * W + i] = mv;
+            Ib[cur * W + i] = iv;
+            Db[cur * W + i] = dv;
+            if (i == R) sum = __dadd_rn(sum, __dadd_rn(mv, iv));
+        }
+        __syncthreads();
+    }
+    if ((int)threadIdx.x == (R - 1) % kPlainThreads) B.out[out_index] = log10(sum) - kLog10Scale64;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// FP32 / FP64 pipe peak probes: register-resident chains, 8 independent per thread.
+template <int N>
+__global__ void peak_ffma_kernel(float *out, int iters, float x, float y) {
+    float a[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) a[i] = threadIdx.x * 1e-7f + i;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) a[i] = fmaf(a[i], x, y);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < N; ++i) s += a[i];
+    if (s == 12345.678f) out[threadIdx.x] = s;
+}
+
+template <int N>
+__global__ void peak_ffma2_kernel(float *out, int iters, float x, float y) {
+    float2 a[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) a[i] = make_float2(threadIdx.x * 1e-7f + i, threadIdx.x * 2e-7f + i);
+    const float2 xx = make_float2(x, x), yy = make_float2(y, y);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) a[i] = __ffma2_rn(a[i], xx, yy);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < N; ++i) s += a[i].x + a[i].y;
+    if (s == 12345.678f) out[threadIdx.x] = s;
+}
+
+template <int N>
+__global__ void peak_dfma_kernel(double *out, int iters, double x, double y) {
+    double a[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) a[i] = threadIdx.x * 1e-7 + i;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) a[i] = fma(a[i], x, y);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) s += a[i];
+    if (s == 12345.678) out[threadIdx.x] = s;
+}
+
+// ---------------------------------------------------------------------------------------------------
+template <int K, bool MULTI>
+static int launch_fp32_k(const DevTables &t, const DevBatch &b, int task_begin, int task_count, int grid, int block,
+                         int slot, cudaStream_t s) {
+    fp32_bucket_kernel<K, MULTI><<<grid, block, 0, s>>>(t, b, task_begin, task_count, slot);
+    return (int)cudaGetLastError();
+}
+
+int launch_fp32_bucket(const DevTables &t, const DevBatch &b, int k, int task_begin, int task_count, int grid,
+                       int block, int slot, cudaStream_t s) {
+    // k encodes rows per lane in the low 4 bits and the multi-strip flag in bit 4
+    const bool multi = (k & 16) != 0;
+    switch (k & 15) {
+#define GHMM_CASE(KK)                                                                                   \
+    case KK:                                                                                            \
+        return multi ? launch_fp32_k<KK, true>(t, b, task_begin, task_count, grid, block, slot, s)      \
+                     : launch_fp32_k<KK, false>(t, b, task_begin, task_count, grid, block, slot, s);
+        GHMM_CASE(1)
+        GHMM_CASE(2)
+        GHMM_CASE(3)
+        GHMM_CASE(4)
+        GHMM_CASE(5)
+        GHMM_CASE(6)
+        GHMM_CASE(7)
+        GHMM_CASE(8)
+#undef GHMM_CASE
+        default:
+            return (int)cudaErrorInvalidValue;
+    }
+}
+
+int fp32_kernel_occupancy(int k, int block, int *blocks_per_sm) {
+    const bool multi = (k & 16) != 0;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (k & 15) {
+#define GHMM_OCC(KK)                                                                                              \
+    case KK:                                                                                                      \
+        e = multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fp32_bucket_kernel<KK, true>, block, 0) \
+                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fp32_bucket_kernel<KK, false>, block, 0); \
+        break;
+        GHMM_OCC(1)
+        GHMM_OCC(2)
+        GHMM_OCC(3)
+        GHMM_OCC(4)
+        GHMM_OCC(5)
+        GHMM_OCC(6)
+        GHMM_OCC(7)
+        GHMM_OCC(8)
+#undef GHMM_OCC
+        default:
+            break;
+    }
+    return (int)e;
+}
+
+int launch_fp64_queue(const DevTables &t, const DevBatch &b, int grid, int block, cudaStream_t s) {
+    fp64_queue_kernel<kMaxK64><<<grid, block, 0, s>>>(t, b);
+    return (int)cudaGetLastError();
+}
+
+int fp64_kernel_occupancy(int block, int *blocks_per_sm) {
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fp64_queue_kernel<kMaxK64>, block, 0);
+}
+
+// Shared memory: three diagonals of M, I, D over R+1 rows, sized by the region's longest read.
+int launch_plain_region(const DevTables &t, const DevBatch &b, int region, int n_reads, int n_haps,
+                              int max_read_len, cudaStream_t s) {
+    if (n_reads <= 0 || n_haps <= 0) return 0;
+    const size_t smem = sizeof(double) * 9 * (size_t)(max_read_len + 1);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(plain_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+    }
+    plain_fp64_kernel<<<n_reads * n_haps, kPlainThreads, smem, s>>>(t, b, region, n_haps);
+    return (int)cudaGetLastError();
+}
+
+int measure_peaks_device(int sm_count, double *fp32, double *fp32x2, double *fp64, cudaStream_t s) {
+    float *fo = nullptr;
+    double *dout = nullptr;
+    if (cudaMalloc(&fo, 1024 * sizeof(float)) != cudaSuccess) return (int)cudaErrorMemoryAllocation;
+    if (cudaMalloc(&dout, 1024 * sizeof(double)) != cudaSuccess) {
+        cudaFree(fo);
+        return (int)cudaErrorMemoryAllocation;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int block = 256, grid = sm_count * 8;
+    constexpr int N = 8;
+    const double threads = (double)grid * block;
+    float ms = 0.f;
+    int err = 0;
+    auto timeit = [&](auto launch, int iters, double flops_per_iter_thread, double *res) {
+        launch(iters / 8);  // warm-up
+        cudaEventRecord(e0, s);
+        launch(iters);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (res) *res = threads * iters * flops_per_iter_thread / (ms * 1e-3) / 1e12;
+        if (cudaGetLastError() != cudaSuccess) err = 1;
+    };
+    timeit([&](int it) { peak_ffma_kernel<N><<<grid, block, 0, s>>>(fo, it, 0.999999f, 1e-6f); }, 1 << 16,
+           2.0 * N, fp32);
+    timeit([&](int it) { peak_ffma2_kernel<N><<<grid, block, 0, s>>>(fo, it, 0.999999f, 1e-6f); }, 1 << 15,
+           4.0 * N, fp32x2);
+    timeit([&](int it) { peak_dfma_kernel<N><<<grid, block, 0, s>>>(dout, it, 0.999999, 1e-6); }, 1 << 11,
+           2.0 * N, fp64);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(fo);
+    cudaFree(dout);
+    return err ? (int)cudaErrorLaunchFailure : 0;
+}
+
+}  // namespace ghmm

@@ -1,0 +1,153 @@
+"""ctypes binding of libghmm.so (include/ghmm.h, ghmm_synth.h, ghmm_calib.h).
+
+The library is the product: there is no Python or CPU fallback.  ``lib()`` builds it in-tree if it
+is missing and raises if that fails; compute calls raise ``GhmmError`` with the library's message
+when the device is absent or a call fails.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+
+from . import build as _build
+
+GHMM_OK = 0
+GHMM_ERR_ARG = 1
+GHMM_ERR_STATE = 2
+GHMM_ERR_CUDA = 3
+GHMM_ERR_UNSUPPORTED = 4
+GHMM_ERR_RESULT = 5
+GHMM_ERR_NOMEM = 6
+GHMM_ERR_TIMEOUT = 7
+
+MODE_FP32_RERUN = 0
+MODE_FP64 = 1
+MODE_PLAIN_FP64 = 2
+
+FP32_RERUN_THRESHOLD = 1e-28
+
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_f64p = ctypes.POINTER(ctypes.c_double)
+_f32p = ctypes.POINTER(ctypes.c_float)
+
+
+class GhmmError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class Args(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("max_threads", ctypes.c_int32),
+                ("use_double_precision", ctypes.c_int32), ("flags", ctypes.c_int32)]
+
+
+class Read(ctypes.Structure):
+    _fields_ = [("bases", _u8p), ("quals", _u8p), ("ins_gop", _u8p), ("del_gop", _u8p), ("gcp", _u8p),
+                ("length", ctypes.c_int32)]
+
+
+class Hap(ctypes.Structure):
+    _fields_ = [("bases", _u8p), ("length", ctypes.c_int32)]
+
+
+class Region(ctypes.Structure):
+    _fields_ = [("reads", ctypes.POINTER(Read)), ("n_reads", ctypes.c_int32), ("haps", ctypes.POINTER(Hap)),
+                ("n_haps", ctypes.c_int32)]
+
+
+class Flat(ctypes.Structure):
+    _fields_ = [("n_regions", ctypes.c_int64), ("region_read_off", _i64p), ("region_hap_off", _i64p),
+                ("read_off", _i64p), ("bases", _u8p), ("quals", _u8p), ("ins_gop", _u8p), ("del_gop", _u8p),
+                ("gcp", _u8p), ("hap_off", _i64p), ("hap_bases", _u8p), ("out_off", _i64p)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("n_pairs", ctypes.c_int64), ("n_cells", ctypes.c_int64), ("n_rerun", ctypes.c_int64),
+                ("n_fp64_direct", ctypes.c_int64), ("n_tasks_fp32", ctypes.c_int64), ("n_launches", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("ms_fp32", ctypes.c_double), ("ms_fp64", ctypes.c_double),
+                ("ms_plain", ctypes.c_double), ("ms_total", ctypes.c_double), ("h2d_bytes", ctypes.c_int64),
+                ("d2h_bytes", ctypes.c_int64)]
+
+
+class SynthArrays(ctypes.Structure):
+    _fields_ = [("n_regions", ctypes.c_int64), ("n_reads", ctypes.c_int64), ("n_haps", ctypes.c_int64),
+                ("read_bytes", ctypes.c_int64), ("hap_bytes", ctypes.c_int64), ("n_out", ctypes.c_int64),
+                ("region_read_off", _i64p), ("region_hap_off", _i64p), ("read_off", _i64p), ("hap_off", _i64p),
+                ("out_off", _i64p), ("bases", _u8p), ("quals", _u8p), ("ins", _u8p), ("dels", _u8p), ("gcp", _u8p),
+                ("hap_bases", _u8p)]
+
+
+# Every exported symbol and its signature (restype, argtypes).  The tests check that the library
+# exports exactly the functions the public headers declare.
+_SIGS = {
+    "ghmm_load": (ctypes.c_int, []),
+    "ghmm_initialize": (ctypes.c_int, [ctypes.POINTER(Args), ctypes.POINTER(ctypes.c_void_p)]),
+    "ghmm_compute_likelihoods": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Read), ctypes.c_int32,
+                                                ctypes.POINTER(Hap), ctypes.c_int32, _f64p]),
+    "ghmm_done": (ctypes.c_int, [ctypes.c_void_p]),
+    "ghmm_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
+    "ghmm_compute_regions": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Region), ctypes.c_int32, _f64p]),
+    "ghmm_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Region), ctypes.c_int32,
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "ghmm_batch_create_flat": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Flat), ctypes.POINTER(ctypes.c_void_p)]),
+    "ghmm_batch_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    "ghmm_batch_results": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _f64p]),
+    "ghmm_batch_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    "ghmm_batch_destroy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "ghmm_compute_flat": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Flat), _f64p]),
+    "ghmm_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "ghmm_measure_peaks": (ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p]),
+    "ghmm_debug_tables": (ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p]),
+    "ghmm_synth_default_regions": (ctypes.c_int64, [ctypes.c_int32]),
+    "ghmm_synth_generate": (ctypes.c_int, [ctypes.c_int32, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
+                                           ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+    "ghmm_synth_view": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SynthArrays)]),
+    "ghmm_synth_free": (None, [ctypes.c_void_p]),
+    "ghmm_str_analyze": (ctypes.c_int, [_u8p, ctypes.c_int32, ctypes.c_int32, _i32p, _i32p, _i32p]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Load libghmm.so (building it in-tree first if needed)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build()
+            L = ctypes.CDLL(path)
+            for name, (res, args) in _SIGS.items():
+                f = getattr(L, name, None)
+                if f is None:
+                    raise ImportError(f"{path} does not export {name}")
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+def last_error(ctx) -> str:
+    buf = ctypes.create_string_buffer(1024)
+    lib().ghmm_last_error(ctx, buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(code: int, ctx=None):
+    if code != GHMM_OK:
+        raise GhmmError(code, last_error(ctx))
+
+
+def device_available() -> bool:
+    return bool(lib().ghmm_load())

@@ -1,0 +1,223 @@
+"""Host-side mirror of GATK's PairHMM plugin interface for the CUDA_LOGLESS implementation.
+
+Reference interface (paths inside the GATK repository):
+  PairHMM.Implementation, makeNewHMM(PairHMMNativeArguments)   utils/pairhmm/PairHMM.java:40-109
+  VectorLoglessPairHMM (the JNI-backed implementation this mirrors):
+      constructor: load() else HardwareFeatureException         utils/pairhmm/VectorLoglessPairHMM.java:57-82
+      initialize(haplotypes, perSampleReadList, maxR, maxH)     :89-102
+      computeLog10Likelihoods(matrix, processedReads, imputator) :108-159
+      close()                                                   :163-168
+  PairHMMNativeArguments {maxNumberOfThreads, useDoublePrecision} (HC/PairHMMNativeArgumentCollection.java:11-23)
+
+Every computation goes through libghmm.so on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+from dataclasses import dataclass
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import native
+from .workload import Workload
+
+
+class HardwareFeatureException(RuntimeError):
+    """UserException.HardwareFeatureException: the accelerated implementation is not available."""
+
+
+@dataclass
+class PairHMMNativeArguments:
+    max_number_of_threads: int = 0
+    use_double_precision: bool = False
+    device: int = 0
+
+
+class Implementation(enum.Enum):
+    """The PairHMM.Implementation constant this package adds (CUDA_LOGLESS)."""
+
+    CUDA_LOGLESS = "CUDA_LOGLESS"
+
+    def make_new_hmm(self, args: PairHMMNativeArguments | None = None) -> "CudaLoglessPairHMM":
+        return CudaLoglessPairHMM(args)
+
+
+def _u8(x) -> np.ndarray:
+    if isinstance(x, (bytes, bytearray)):
+        return np.frombuffer(bytes(x), dtype=np.uint8)
+    return np.ascontiguousarray(np.asarray(x, dtype=np.uint8))
+
+
+class _Context:
+    def __init__(self, args: PairHMMNativeArguments):
+        L = native.lib()
+        if not L.ghmm_load():
+            raise HardwareFeatureException("Machine does not support the CUDA PairHMM (no compute capability 10.3 GPU).")
+        a = native.Args(args.device, args.max_number_of_threads, int(args.use_double_precision), 0)
+        h = ctypes.c_void_p()
+        rc = L.ghmm_initialize(ctypes.byref(a), ctypes.byref(h))
+        if rc == native.GHMM_ERR_UNSUPPORTED:
+            raise HardwareFeatureException(native.last_error(None))
+        native.check(rc, None)
+        self.h = h
+        self.L = L
+
+    def close(self):
+        if self.h:
+            self.L.ghmm_done(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CudaLoglessPairHMM:
+    """PairHMM backed by the GB300 kernels (VectorLoglessPairHMM's contract).
+
+    ``initialize`` stores the haplotypes; ``compute_log10_likelihoods`` takes the processed reads as
+    (bases, quals, insertion GOP, deletion GOP, GCP) tuples and returns the read-major log10
+    likelihood array (also kept as ``get_log_likelihood_array()``).
+    """
+
+    def __init__(self, args: PairHMMNativeArguments | None = None):
+        self.args = args or PairHMMNativeArguments()
+        self._ctx = _Context(self.args)
+        self._haps: list[np.ndarray] = []
+        self._last: np.ndarray | None = None
+
+    # PairHMM.initialize(List<Haplotype>, Map, int, int)
+    def initialize(self, haplotypes: Sequence, per_sample_reads=None, read_max_length: int = 0,
+                   haplotype_max_length: int = 0) -> None:
+        self._haps = [_u8(h) for h in haplotypes]
+
+    # PairHMM.computeLog10Likelihoods(LikelihoodMatrix, List<GATKRead>, PairHMMInputScoreImputator)
+    def compute_log10_likelihoods(self, reads: Iterable[Sequence]) -> np.ndarray | None:
+        reads = [tuple(_u8(x) for x in r) for r in reads]
+        if not reads:  # PairHMM.java:199-201: nothing to do
+            return None
+        for r in reads:
+            if len(r) != 5 or any(len(x) != len(r[0]) for x in r):
+                raise ValueError("each read needs bases, quals, ins, del and gcp arrays of equal length")
+        nr, nh = len(reads), len(self._haps)
+        rs = (native.Read * nr)()
+        for i, (b, q, ins, dl, g) in enumerate(reads):
+            rs[i] = native.Read(b.ctypes.data_as(native._u8p), q.ctypes.data_as(native._u8p),
+                                ins.ctypes.data_as(native._u8p), dl.ctypes.data_as(native._u8p),
+                                g.ctypes.data_as(native._u8p), len(b))
+        hs = (native.Hap * max(nh, 1))()
+        for i, h in enumerate(self._haps):
+            hs[i] = native.Hap(h.ctypes.data_as(native._u8p), len(h))
+        out = np.empty(nr * nh, dtype=np.float64)
+        rc = self._ctx.L.ghmm_compute_likelihoods(self._ctx.h, rs, nr, hs, nh, out.ctypes.data_as(native._f64p))
+        if rc == native.GHMM_ERR_ARG:
+            raise ValueError(native.last_error(self._ctx.h))
+        native.check(rc, self._ctx.h)
+        self._last = out
+        return out
+
+    def get_log_likelihood_array(self) -> np.ndarray | None:
+        return self._last
+
+    def close(self) -> None:
+        self._ctx.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Engine:
+    """Batched, device-resident use of the kernels (the batcher): one context, many regions."""
+
+    def __init__(self, device: int = 0, max_threads: int = 0, use_double_precision: bool = False):
+        self._ctx = _Context(PairHMMNativeArguments(max_threads, use_double_precision, device))
+        self.L = self._ctx.L
+
+    @property
+    def handle(self):
+        return self._ctx.h
+
+    def stream_handle(self) -> int:
+        return int(self.L.ghmm_stream(self._ctx.h) or 0)
+
+    def compute(self, wl: Workload, via_regions: bool = False) -> np.ndarray:
+        """Upload + forward + download (host buffers in, host results out)."""
+        out = np.empty(wl.n_pairs, dtype=np.float64)
+        if via_regions:
+            regs = wl.as_regions()
+            rc = self.L.ghmm_compute_regions(self._ctx.h, regs, wl.n_regions, out.ctypes.data_as(native._f64p))
+        else:
+            f = wl.as_flat()
+            rc = self.L.ghmm_compute_flat(self._ctx.h, ctypes.byref(f), out.ctypes.data_as(native._f64p))
+        native.check(rc, self._ctx.h)
+        return out
+
+    def batch(self, wl: Workload, via_regions: bool = False) -> "Batch":
+        return Batch(self, wl, via_regions)
+
+    def measure_peaks(self):
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        native.check(self.L.ghmm_measure_peaks(self._ctx.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+                     self._ctx.h)
+        return {"fp32_tflops": a.value, "fp32x2_tflops": b.value, "fp64_tflops": c.value}
+
+    def debug_tables(self):
+        err = np.zeros(256)
+        prob = np.zeros(256)
+        m2m = np.zeros(128 * 128)
+        native.check(self.L.ghmm_debug_tables(self._ctx.h, err.ctypes.data_as(native._f64p),
+                                              prob.ctypes.data_as(native._f64p), m2m.ctypes.data_as(native._f64p)),
+                     self._ctx.h)
+        return err, prob, m2m.reshape(128, 128)
+
+    def close(self):
+        self._ctx.close()
+
+
+class Batch:
+    """A device-resident batch: inputs uploaded once; forward() reruns the kernels on them."""
+
+    def __init__(self, engine: Engine, wl: Workload, via_regions: bool = False):
+        self.engine = engine
+        self.wl = wl
+        h = ctypes.c_void_p()
+        if via_regions:
+            regs = wl.as_regions()
+            rc = engine.L.ghmm_batch_create(engine.handle, regs, wl.n_regions, ctypes.byref(h))
+        else:
+            f = wl.as_flat()
+            rc = engine.L.ghmm_batch_create_flat(engine.handle, ctypes.byref(f), ctypes.byref(h))
+        native.check(rc, engine.handle)
+        self.h = h
+
+    def forward(self, mode: int = native.MODE_FP32_RERUN) -> None:
+        native.check(self.engine.L.ghmm_batch_forward(self.engine.handle, self.h, mode), self.engine.handle)
+
+    def results(self) -> np.ndarray:
+        out = np.empty(self.wl.n_pairs, dtype=np.float64)
+        native.check(self.engine.L.ghmm_batch_results(self.engine.handle, self.h, out.ctypes.data_as(native._f64p)),
+                     self.engine.handle)
+        return out
+
+    def stats(self) -> dict:
+        s = native.Stats()
+        native.check(self.engine.L.ghmm_batch_stats(self.engine.handle, self.h, ctypes.byref(s)), self.engine.handle)
+        return {k: getattr(s, k) for k, _ in native.Stats._fields_ if k != "reserved"}
+
+    def close(self):
+        if self.h:
+            self.engine.L.ghmm_batch_destroy(self.engine.handle, self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

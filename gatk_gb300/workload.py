@@ -1,0 +1,198 @@
+"""Flat workloads: regions of reads and haplotypes laid out as contiguous planes.
+
+``Workload`` is the in-memory form every entry point shares: the synthetic generator
+(``generate``), the batch uploader (``as_flat``) and the test oracle all read the same arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import native
+
+# seeds of the five synthetic workloads
+DEFAULT_SEEDS = {0: 0, 1: 1, 2: 2, 3: 3, 4: 4}
+
+
+@dataclass
+class Workload:
+    region_read_off: np.ndarray  # int64 [G+1]
+    region_hap_off: np.ndarray   # int64 [G+1]
+    read_off: np.ndarray         # int64 [NR+1]
+    bases: np.ndarray            # uint8 planes
+    quals: np.ndarray
+    ins: np.ndarray
+    dels: np.ndarray
+    gcp: np.ndarray
+    hap_off: np.ndarray          # int64 [NH+1]
+    hap_bases: np.ndarray        # uint8
+    out_off: np.ndarray          # int64 [G+1]
+    _keep: list = field(default_factory=list, repr=False)
+
+    @property
+    def n_regions(self) -> int:
+        return len(self.region_read_off) - 1
+
+    @property
+    def n_reads(self) -> int:
+        return len(self.read_off) - 1
+
+    @property
+    def n_haps(self) -> int:
+        return len(self.hap_off) - 1
+
+    @property
+    def n_pairs(self) -> int:
+        return int(self.out_off[-1])
+
+    def read_lengths(self) -> np.ndarray:
+        return np.diff(self.read_off)
+
+    def hap_lengths(self) -> np.ndarray:
+        return np.diff(self.hap_off)
+
+    def cells(self) -> int:
+        rl = self.read_lengths()
+        hl = self.hap_lengths()
+        tot = 0
+        for g in range(self.n_regions):
+            r0, r1 = self.region_read_off[g], self.region_read_off[g + 1]
+            h0, h1 = self.region_hap_off[g], self.region_hap_off[g + 1]
+            tot += int(rl[r0:r1].sum()) * int(hl[h0:h1].sum())
+        return tot
+
+    def cells_per_region(self) -> np.ndarray:
+        rl = np.concatenate([[0], np.cumsum(self.read_lengths())])
+        hl = np.concatenate([[0], np.cumsum(self.hap_lengths())])
+        sr = rl[self.region_read_off[1:]] - rl[self.region_read_off[:-1]]
+        sh = hl[self.region_hap_off[1:]] - hl[self.region_hap_off[:-1]]
+        return sr.astype(np.int64) * sh.astype(np.int64)
+
+    def pair_index(self):
+        """Global (read, haplotype) index of every output slot, read-major per region."""
+        pr = np.empty(self.n_pairs, dtype=np.int64)
+        ph = np.empty(self.n_pairs, dtype=np.int64)
+        for g in range(self.n_regions):
+            r0, r1 = int(self.region_read_off[g]), int(self.region_read_off[g + 1])
+            h0, h1 = int(self.region_hap_off[g]), int(self.region_hap_off[g + 1])
+            o = int(self.out_off[g])
+            nr, nh = r1 - r0, h1 - h0
+            pr[o:o + nr * nh] = np.repeat(np.arange(r0, r1), nh)
+            ph[o:o + nr * nh] = np.tile(np.arange(h0, h1), nr)
+        return pr, ph
+
+    def read(self, r: int):
+        a, b = int(self.read_off[r]), int(self.read_off[r + 1])
+        return (self.bases[a:b], self.quals[a:b], self.ins[a:b], self.dels[a:b], self.gcp[a:b])
+
+    def hap(self, h: int):
+        return self.hap_bases[int(self.hap_off[h]):int(self.hap_off[h + 1])]
+
+    def subset(self, g0: int, g1: int) -> "Workload":
+        """Regions [g0, g1) as a self-contained workload."""
+        r0, r1 = int(self.region_read_off[g0]), int(self.region_read_off[g1])
+        h0, h1 = int(self.region_hap_off[g0]), int(self.region_hap_off[g1])
+        b0, b1 = int(self.read_off[r0]), int(self.read_off[r1])
+        c0, c1 = int(self.hap_off[h0]), int(self.hap_off[h1])
+        return Workload(
+            region_read_off=self.region_read_off[g0:g1 + 1] - r0,
+            region_hap_off=self.region_hap_off[g0:g1 + 1] - h0,
+            read_off=self.read_off[r0:r1 + 1] - b0,
+            bases=self.bases[b0:b1].copy(), quals=self.quals[b0:b1].copy(), ins=self.ins[b0:b1].copy(),
+            dels=self.dels[b0:b1].copy(), gcp=self.gcp[b0:b1].copy(),
+            hap_off=self.hap_off[h0:h1 + 1] - c0, hap_bases=self.hap_bases[c0:c1].copy(),
+            out_off=self.out_off[g0:g1 + 1] - self.out_off[g0])
+
+    def as_flat(self) -> native.Flat:
+        p = lambda a, t: a.ctypes.data_as(t)
+        f = native.Flat(self.n_regions, p(self.region_read_off, native._i64p), p(self.region_hap_off, native._i64p),
+                        p(self.read_off, native._i64p), p(self.bases, native._u8p), p(self.quals, native._u8p),
+                        p(self.ins, native._u8p), p(self.dels, native._u8p), p(self.gcp, native._u8p),
+                        p(self.hap_off, native._i64p), p(self.hap_bases, native._u8p), p(self.out_off, native._i64p))
+        return f
+
+    def as_regions(self):
+        """ghmm_region array with per-read pointers into the planes (the JNI-shaped input)."""
+        NR, NH, G = self.n_reads, self.n_haps, self.n_regions
+        assert ctypes.sizeof(native.Read) == 48 and ctypes.sizeof(native.Hap) == 16
+        assert ctypes.sizeof(native.Region) == 32
+        rd = np.zeros(max(NR, 1), dtype=[("p", "<u8", (5,)), ("len", "<i4"), ("pad", "<i4")])
+        o = self.read_off[:-1].astype(np.uint64)
+        for k, plane in enumerate((self.bases, self.quals, self.ins, self.dels, self.gcp)):
+            rd["p"][:NR, k] = np.uint64(plane.ctypes.data) + o
+        rd["len"][:NR] = np.diff(self.read_off)
+        hp = np.zeros(max(NH, 1), dtype=[("p", "<u8"), ("len", "<i4"), ("pad", "<i4")])
+        hp["p"][:NH] = np.uint64(self.hap_bases.ctypes.data) + self.hap_off[:-1].astype(np.uint64)
+        hp["len"][:NH] = np.diff(self.hap_off)
+        rg = np.zeros(max(G, 1), dtype=[("reads", "<u8"), ("n_reads", "<i4"), ("pad0", "<i4"), ("haps", "<u8"),
+                                        ("n_haps", "<i4"), ("pad1", "<i4")])
+        rg["reads"][:G] = np.uint64(rd.ctypes.data) + self.region_read_off[:-1].astype(np.uint64) * np.uint64(48)
+        rg["n_reads"][:G] = np.diff(self.region_read_off)
+        rg["haps"][:G] = np.uint64(hp.ctypes.data) + self.region_hap_off[:-1].astype(np.uint64) * np.uint64(16)
+        rg["n_haps"][:G] = np.diff(self.region_hap_off)
+        self._keep.append((rd, hp, rg))
+        return rg.ctypes.data_as(ctypes.POINTER(native.Region))
+
+
+def generate(workload: int, regions: int | None = None, seed: int | None = None, region_begin: int = 0,
+             threads: int = 0) -> Workload:
+    """Synthetic workload `workload` (0-4), regions [region_begin, region_begin + regions)."""
+    L = native.lib()
+    if seed is None:
+        seed = DEFAULT_SEEDS[workload]
+    if regions is None:
+        regions = int(L.ghmm_synth_default_regions(workload))
+    h = ctypes.c_void_p()
+    rc = L.ghmm_synth_generate(workload, seed, region_begin, region_begin + regions, threads, ctypes.byref(h))
+    if rc != 0:
+        raise ValueError(f"ghmm_synth_generate failed for workload {workload}")
+    try:
+        a = native.SynthArrays()
+        L.ghmm_synth_view(h, ctypes.byref(a))
+
+        def cp(ptr, n, dt):
+            if n == 0:
+                return np.zeros(0, dtype=dt)
+            return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dt, copy=True)
+
+        G, NR, NH = a.n_regions, a.n_reads, a.n_haps
+        return Workload(
+            region_read_off=cp(a.region_read_off, G + 1, np.int64), region_hap_off=cp(a.region_hap_off, G + 1, np.int64),
+            read_off=cp(a.read_off, NR + 1, np.int64), bases=cp(a.bases, a.read_bytes, np.uint8),
+            quals=cp(a.quals, a.read_bytes, np.uint8), ins=cp(a.ins, a.read_bytes, np.uint8),
+            dels=cp(a.dels, a.read_bytes, np.uint8), gcp=cp(a.gcp, a.read_bytes, np.uint8),
+            hap_off=cp(a.hap_off, NH + 1, np.int64), hap_bases=cp(a.hap_bases, a.hap_bytes, np.uint8),
+            out_off=cp(a.out_off, G + 1, np.int64))
+    finally:
+        L.ghmm_synth_free(h)
+
+
+def from_pairs(regions) -> Workload:
+    """Build a workload from Python data: regions = [(haps, reads)], haps = [bytes], reads =
+    [(bases, quals, ins, dels, gcp)] with byte strings or uint8 arrays (Phred values)."""
+    rro, rho, ro, ho, oo = [0], [0], [0], [0], [0]
+    planes = [[], [], [], [], []]
+    hb = []
+    for haps, reads in regions:
+        for h in haps:
+            h = bytes(h)
+            hb.append(np.frombuffer(h, dtype=np.uint8))
+            ho.append(ho[-1] + len(h))
+        for rd in reads:
+            arrs = [np.asarray(bytearray(x) if isinstance(x, (bytes, bytearray)) else x, dtype=np.uint8) for x in rd]
+            n = len(arrs[0])
+            if any(len(x) != n for x in arrs):
+                raise ValueError("read arrays must have equal lengths")
+            for k in range(5):
+                planes[k].append(arrs[k])
+            ro.append(ro[-1] + n)
+        rro.append(rro[-1] + len(reads))
+        rho.append(rho[-1] + len(haps))
+        oo.append(oo[-1] + len(reads) * len(haps))
+    cat = lambda xs: np.concatenate(xs).astype(np.uint8) if xs else np.zeros(0, dtype=np.uint8)
+    return Workload(region_read_off=np.array(rro, dtype=np.int64), region_hap_off=np.array(rho, dtype=np.int64),
+                    read_off=np.array(ro, dtype=np.int64), bases=cat(planes[0]), quals=cat(planes[1]),
+                    ins=cat(planes[2]), dels=cat(planes[3]), gcp=cat(planes[4]), hap_off=np.array(ho, dtype=np.int64),
+                    hap_bases=cat(hb), out_off=np.array(oo, dtype=np.int64))

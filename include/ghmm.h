@@ -1,0 +1,173 @@
+/*
+ * ghmm.h -- C-ABI of the GB300-native PairHMM (CUDA_LOGLESS) for GATK's read-likelihood step.
+ *
+ * The entry points mirror the native PairHMM binding GATK calls through JNI:
+ *   org.broadinstitute.gatk.nativebindings.pairhmm.PairHMMNativeBinding (gatk-native-bindings 1.1.0),
+ *   used by src/main/java/org/broadinstitute/hellbender/utils/pairhmm/VectorLoglessPairHMM.java:57-168:
+ *     boolean load(File)                                   -> ghmm_load          (VectorLoglessPairHMM.java:63,71)
+ *     void initialize(PairHMMNativeArguments)              -> ghmm_initialize    (VectorLoglessPairHMM.java:81)
+ *     void computeLikelihoods(ReadDataHolder[], HaplotypeDataHolder[], double[])
+ *                                                          -> ghmm_compute_likelihoods (VectorLoglessPairHMM.java:138)
+ *     void done()                                          -> ghmm_done          (VectorLoglessPairHMM.java:164)
+ * ReadDataHolder {readBases, readQuals, insertionGOP, deletionGOP, overallGCP} (VectorLoglessPairHMM.java:122-127)
+ * maps to ghmm_read; HaplotypeDataHolder {haplotypeBases} (:97-98) maps to ghmm_hap.
+ *
+ * Results are log10 likelihoods, read-major: out[r * n_haps + h] (VectorLoglessPairHMM.java:131,147-148),
+ * with the semantics of LoglessPairHMM (LoglessPairHMM.java:20-68): an FP32 wavefront with a 2^120-scaled
+ * initial condition, and an FP64 rerun (2^1020 scale) for every pair whose FP32 sum falls below
+ * GHMM_FP32_RERUN_THRESHOLD or is not finite.
+ *
+ * Ownership: callers own every input array and `out`; the library copies inputs into its own
+ * staging buffers during the call and keeps no caller pointer after it returns.  `out` is fully
+ * written before a successful return.
+ * Errors: every call returns a status code (GHMM_OK = 0); ghmm_last_error gives the message.
+ * Threading: a context is used by one caller thread at a time; separate contexts are independent
+ * (each owns its own CUDA stream and buffers), as GATK creates one PairHMM per likelihood engine
+ * (HC/PairHMMLikelihoodCalculationEngine.java:145) and one engine per Spark partition.
+ */
+#ifndef GHMM_H
+#define GHMM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The JNI layer maps ERR_UNSUPPORTED to UserException.HardwareFeatureException,
+ * ERR_ARG to IllegalArgumentException, ERR_STATE to IllegalStateException, and the rest to
+ * GATKException (PairHMM.java:284-306, VectorLoglessPairHMM.java:63-79). */
+#define GHMM_OK 0
+#define GHMM_ERR_ARG 1         /* invalid argument (lengths, quality bytes out of range, NULL) */
+#define GHMM_ERR_STATE 2       /* context not initialised / already done */
+#define GHMM_ERR_CUDA 3        /* CUDA runtime error */
+#define GHMM_ERR_UNSUPPORTED 4 /* no usable sm_103 GPU */
+#define GHMM_ERR_RESULT 5      /* a likelihood was > 0 or NaN (PairHMM.java:305-306) */
+#define GHMM_ERR_NOMEM 6       /* device or pinned host allocation failed */
+#define GHMM_ERR_TIMEOUT 7     /* a bounded device-side wait ran out */
+
+/* FP32 scaled-sum threshold below which a pair is recomputed in FP64.  The FP32 sum carries the
+ * 2^120 scale, so 1e-28 means log10 L < -64.1; cells on the dominant alignment path are then still
+ * ten decades above FLT_MIN (1.18e-38), where gradual underflow would start to cost precision. */
+#define GHMM_FP32_RERUN_THRESHOLD 1e-28f
+
+/* Forward modes for ghmm_batch_forward. */
+#define GHMM_MODE_FP32_RERUN 0 /* batched FP32 wavefront + FP64 rerun of underflowing pairs (default) */
+#define GHMM_MODE_FP64 1       /* every pair in the FP64 wavefront kernel (useDoublePrecision) */
+#define GHMM_MODE_PLAIN_FP64 2 /* plain FP64 kernel, one pair per thread block, one launch per region */
+
+/* Mirrors PairHMMNativeArguments {maxNumberOfThreads, useDoublePrecision}
+ * (HC/PairHMMNativeArgumentCollection.java:11-23) plus the device to use. */
+typedef struct ghmm_args {
+    int32_t device;               /* CUDA device ordinal */
+    int32_t max_threads;          /* host threads used to marshal inputs (<= 0: all cores) */
+    int32_t use_double_precision; /* nonzero: every pair in FP64 (GHMM_MODE_FP64) */
+    int32_t flags;                /* reserved, must be 0 */
+} ghmm_args;
+
+/* ReadDataHolder: five arrays of `length` bytes; quals are Phred values (not +33). */
+typedef struct ghmm_read {
+    const uint8_t *bases;
+    const uint8_t *quals;
+    const uint8_t *ins_gop;
+    const uint8_t *del_gop;
+    const uint8_t *gcp;
+    int32_t length;
+} ghmm_read;
+
+/* HaplotypeDataHolder */
+typedef struct ghmm_hap {
+    const uint8_t *bases;
+    int32_t length;
+} ghmm_hap;
+
+/* One active region: its reads against its haplotypes (one computeLikelihoods call). */
+typedef struct ghmm_region {
+    const ghmm_read *reads;
+    int32_t n_reads;
+    const ghmm_hap *haps;
+    int32_t n_haps;
+} ghmm_region;
+
+/* The same inputs already laid out as flat planes (int64 offsets), as ghmm_synth produces. */
+typedef struct ghmm_flat {
+    int64_t n_regions;
+    const int64_t *region_read_off; /* [n_regions+1] */
+    const int64_t *region_hap_off;  /* [n_regions+1] */
+    const int64_t *read_off;        /* [n_reads+1] byte offsets into the five planes */
+    const uint8_t *bases, *quals, *ins_gop, *del_gop, *gcp;
+    const int64_t *hap_off;         /* [n_haps+1] byte offsets into hap_bases */
+    const uint8_t *hap_bases;
+    const int64_t *out_off;         /* [n_regions+1] read-major block offsets into out */
+} ghmm_flat;
+
+typedef struct ghmm_ctx ghmm_ctx;
+typedef struct ghmm_batch ghmm_batch;
+
+/* Per-batch statistics (filled by ghmm_batch_stats after ghmm_batch_forward). */
+typedef struct ghmm_stats {
+    int64_t n_pairs;          /* read x haplotype pairs */
+    int64_t n_cells;          /* sum over pairs of read_len * hap_len */
+    int64_t n_rerun;          /* pairs recomputed in FP64 after the FP32 pass */
+    int64_t n_fp64_direct;    /* pairs sent to FP64 directly (gcp 0, non-ACGTN bytes, FP64 mode) */
+    int64_t n_tasks_fp32;     /* warp tasks of the FP32 pass */
+    int32_t n_launches;       /* kernels launched by the last forward */
+    int32_t reserved;
+    double ms_fp32;           /* device time of the FP32 launches (CUDA events), last forward */
+    double ms_fp64;           /* device time of the FP64 rerun / FP64-mode launches */
+    double ms_plain;          /* device time of the plain FP64 launches */
+    double ms_total;          /* device time of the whole forward */
+    int64_t h2d_bytes;        /* host-to-device bytes of the last upload + forward */
+    int64_t d2h_bytes;        /* device-to-host bytes of the last forward + results */
+} ghmm_stats;
+
+/* PairHMMNativeBinding.load: 1 if a usable GPU (compute capability 10.3) is present, else 0. */
+int ghmm_load(void);
+
+/* PairHMMNativeBinding.initialize: create a context on args->device. */
+int ghmm_initialize(const ghmm_args *args, ghmm_ctx **ctx);
+
+/* PairHMMNativeBinding.computeLikelihoods: out[r * n_haps + h] for one region (read-major). */
+int ghmm_compute_likelihoods(ghmm_ctx *ctx, const ghmm_read *reads, int32_t n_reads, const ghmm_hap *haps,
+                             int32_t n_haps, double *out);
+
+/* PairHMMNativeBinding.done: release the context. */
+int ghmm_done(ghmm_ctx *ctx);
+
+/* Message of the last failed call on ctx (or of the last failed ghmm_initialize when ctx is NULL). */
+int ghmm_last_error(const ghmm_ctx *ctx, char *buf, size_t buf_len);
+
+/* Batcher: many regions in one call (regions of HaplotypeCallerEngine.callRegion batched together).
+ * out receives each region's read-major block back to back, in region order. */
+int ghmm_compute_regions(ghmm_ctx *ctx, const ghmm_region *regions, int32_t n_regions, double *out);
+
+/* Device-resident batches: marshal + upload once, run the forward many times, download. */
+int ghmm_batch_create(ghmm_ctx *ctx, const ghmm_region *regions, int32_t n_regions, ghmm_batch **batch);
+int ghmm_batch_create_flat(ghmm_ctx *ctx, const ghmm_flat *flat, ghmm_batch **batch);
+int ghmm_batch_forward(ghmm_ctx *ctx, ghmm_batch *batch, int32_t mode);
+int ghmm_batch_results(ghmm_ctx *ctx, ghmm_batch *batch, double *out);
+int ghmm_batch_stats(ghmm_ctx *ctx, const ghmm_batch *batch, ghmm_stats *stats);
+int ghmm_batch_destroy(ghmm_ctx *ctx, ghmm_batch *batch);
+
+/* Flat inputs straight from host memory to results (upload + forward + download in one call). */
+int ghmm_compute_flat(ghmm_ctx *ctx, const ghmm_flat *flat, double *out);
+
+/* The CUDA stream the context launches on (a cudaStream_t), for callers that time or order work. */
+void *ghmm_stream(ghmm_ctx *ctx);
+
+/* Measured FP32 FMA-pipe peak of the device in TFLOP/s (FMA = 2 FLOP): best of a scalar FFMA and a
+ * packed FFMA2 register-resident loop over all SMs, timed with CUDA events.  Also reports the FP64
+ * DFMA peak.  Either output may be NULL. */
+int ghmm_measure_peaks(ghmm_ctx *ctx, double *fp32_tflops, double *fp32x2_tflops, double *fp64_tflops);
+
+/* Debug/test: copy the context's device-side lookup tables back (double versions):
+ * err[256] = 10^(-q/10), prob[256] = 1 - err, m2m[128*128] = matchToMatchProb(ins, del).
+ * With ctx == NULL the host-built tables are returned (no device needed). */
+int ghmm_debug_tables(ghmm_ctx *ctx, double *err, double *prob, double *m2m);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

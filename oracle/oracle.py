@@ -1,0 +1,156 @@
+"""ctypes binding of the FP64 CPU oracle (oracle/pairhmm_oracle.c, oracle/oracle_grad.c).
+
+TEST INFRASTRUCTURE ONLY.  Imported by tests/, by ``__graft_entry__.smoke()`` as the
+checker, and by the cpu_baseline / ``--impl reference`` leg of bench.py.  The product
+package (gatk_gb300) never imports this module.
+
+The C sources restate GATK's LoglessPairHMM / Log10PairHMM / PairHMMModel /
+QualityUtils / MathUtils.JacobianLogTable; the file:line citations are in their
+headers.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (gcc, OpenMP, -ffp-contract=off)."""
+    srcs = [os.path.join(_HERE, f) for f in ("pairhmm_oracle.c", "oracle_grad.c", "Makefile")]
+    if not force and os.path.exists(_LIB_PATH):
+        if os.path.getmtime(_LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
+            return _LIB_PATH
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        L.oracle_logless.restype = ctypes.c_double
+        L.oracle_logless.argtypes = [_u8p, ctypes.c_int, _u8p, _u8p, _u8p, _u8p, _u8p, ctypes.c_int, ctypes.c_int]
+        L.oracle_log10_hmm.restype = ctypes.c_double
+        L.oracle_log10_hmm.argtypes = [_u8p, ctypes.c_int, _u8p, _u8p, _u8p, _u8p, _u8p, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int]
+        L.oracle_approx_log10_sum_log10.restype = ctypes.c_double
+        L.oracle_approx_log10_sum_log10.argtypes = [ctypes.c_double, ctypes.c_double]
+        L.oracle_match_to_match_prob.restype = ctypes.c_double
+        L.oracle_match_to_match_prob.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.oracle_match_to_match_prob_log10.restype = ctypes.c_double
+        L.oracle_match_to_match_prob_log10.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.oracle_qual_to_error_prob.restype = ctypes.c_double
+        L.oracle_qual_to_error_prob.argtypes = [ctypes.c_int]
+        L.oracle_qual_to_prob.restype = ctypes.c_double
+        L.oracle_qual_to_prob.argtypes = [ctypes.c_int]
+        L.oracle_qual_to_trans_probs.restype = None
+        L.oracle_qual_to_trans_probs.argtypes = [_f64p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.oracle_qual_to_trans_probs_log10.restype = None
+        L.oracle_qual_to_trans_probs_log10.argtypes = [_f64p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.oracle_validate_read.restype = ctypes.c_int
+        L.oracle_validate_read.argtypes = [_u8p, _u8p, _u8p, _u8p, ctypes.c_int]
+        L.oracle_compute_regions.restype = ctypes.c_int64
+        L.oracle_compute_regions.argtypes = [ctypes.c_int32, _i64p, _i64p, _i64p, _u8p, _u8p, _u8p, _u8p, _u8p,
+                                             _i64p, _u8p, _i64p, _f64p, ctypes.c_int]
+        L.oracle_compute_pairs.restype = None
+        L.oracle_compute_pairs.argtypes = [ctypes.c_int64, _i64p, _i64p, _i64p, _u8p, _u8p, _u8p, _u8p, _u8p,
+                                           _i64p, _u8p, _f64p, ctypes.c_int]
+        L.oracle_jacobian_size.restype = ctypes.c_int
+        L.oracle_jacobian_value.restype = ctypes.c_double
+        L.oracle_jacobian_value.argtypes = [ctypes.c_int]
+        L.oracle_initial_condition_log10.restype = ctypes.c_double
+        L.oracle_num_threads.restype = ctypes.c_int
+        L.oracle_cont_forward.restype = ctypes.c_double
+        L.oracle_cont_forward.argtypes = [_u8p, ctypes.c_int, _u8p, _u8p, _f64p, _f64p, ctypes.c_int]
+        L.oracle_cont_grad.restype = ctypes.c_double
+        L.oracle_cont_grad.argtypes = [_u8p, ctypes.c_int, _u8p, _u8p, _f64p, _f64p, ctypes.c_int, _f64p, _f64p]
+        _lib = L
+    return _lib
+
+
+def _u8(a) -> np.ndarray:
+    if isinstance(a, (bytes, bytearray)):
+        return np.frombuffer(bytes(a), dtype=np.uint8).copy()
+    return np.ascontiguousarray(np.asarray(a, dtype=np.uint8))
+
+
+def _p(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+def logless(hap, read, quals, ins, dels, gcp, tristate: bool = True) -> float:
+    """LoglessPairHMM log10 likelihood of one pair (FP64)."""
+    h, r, q, i, d, g = (_u8(x) for x in (hap, read, quals, ins, dels, gcp))
+    return lib().oracle_logless(_p(h, _u8p), len(h), _p(r, _u8p), _p(q, _u8p), _p(i, _u8p), _p(d, _u8p),
+                                _p(g, _u8p), len(r), int(tristate))
+
+
+def log10_hmm(hap, read, quals, ins, dels, gcp, tristate: bool = True, exact: bool = True) -> float:
+    """Log10PairHMM (EXACT when exact=True, ORIGINAL otherwise)."""
+    h, r, q, i, d, g = (_u8(x) for x in (hap, read, quals, ins, dels, gcp))
+    return lib().oracle_log10_hmm(_p(h, _u8p), len(h), _p(r, _u8p), _p(q, _u8p), _p(i, _u8p), _p(d, _u8p),
+                                  _p(g, _u8p), len(r), int(tristate), int(exact))
+
+
+def trans_probs(ins: int, dels: int, gcp: int, log10: bool = False) -> np.ndarray:
+    out = np.zeros(6, dtype=np.float64)
+    f = lib().oracle_qual_to_trans_probs_log10 if log10 else lib().oracle_qual_to_trans_probs
+    f(_p(out, _f64p), ins, dels, gcp)
+    return out
+
+
+def compute_workload(wl, threads: int = 0) -> np.ndarray:
+    """All pairs of a flat workload (gatk_gb300.workload.Workload layout), read-major per region."""
+    L = lib()
+    out = np.empty(int(wl.out_off[-1]), dtype=np.float64)
+    L.oracle_compute_regions(wl.n_regions, _p(wl.region_read_off, _i64p), _p(wl.region_hap_off, _i64p),
+                             _p(wl.read_off, _i64p), _p(wl.bases, _u8p), _p(wl.quals, _u8p), _p(wl.ins, _u8p),
+                             _p(wl.dels, _u8p), _p(wl.gcp, _u8p), _p(wl.hap_off, _i64p), _p(wl.hap_bases, _u8p),
+                             _p(wl.out_off, _i64p), _p(out, _f64p), int(threads))
+    return out
+
+
+def compute_pairs(wl, pair_read: np.ndarray, pair_hap: np.ndarray, threads: int = 0) -> np.ndarray:
+    """Selected (read, haplotype) pairs of a flat workload; indices are global read/hap indices."""
+    pr = np.ascontiguousarray(pair_read, dtype=np.int64)
+    ph = np.ascontiguousarray(pair_hap, dtype=np.int64)
+    out = np.empty(len(pr), dtype=np.float64)
+    lib().oracle_compute_pairs(len(pr), _p(pr, _i64p), _p(ph, _i64p), _p(wl.read_off, _i64p), _p(wl.bases, _u8p),
+                               _p(wl.quals, _u8p), _p(wl.ins, _u8p), _p(wl.dels, _u8p), _p(wl.gcp, _u8p),
+                               _p(wl.hap_off, _i64p), _p(wl.hap_bases, _u8p), _p(out, _f64p), int(threads))
+    return out
+
+
+def cont_forward(hap, read, quals, g, c) -> float:
+    h, r, q = (_u8(x) for x in (hap, read, quals))
+    g = np.ascontiguousarray(g, dtype=np.float64)
+    c = np.ascontiguousarray(c, dtype=np.float64)
+    return lib().oracle_cont_forward(_p(h, _u8p), len(h), _p(r, _u8p), _p(q, _u8p), _p(g, _f64p), _p(c, _f64p),
+                                     len(r))
+
+
+def cont_grad(hap, read, quals, g, c):
+    h, r, q = (_u8(x) for x in (hap, read, quals))
+    g = np.ascontiguousarray(g, dtype=np.float64)
+    c = np.ascontiguousarray(c, dtype=np.float64)
+    dg = np.zeros(len(r), dtype=np.float64)
+    dc = np.zeros(len(r), dtype=np.float64)
+    v = lib().oracle_cont_grad(_p(h, _u8p), len(h), _p(r, _u8p), _p(q, _u8p), _p(g, _f64p), _p(c, _f64p), len(r),
+                               _p(dg, _f64p), _p(dc, _f64p))
+    return v, dg, dc
+
+
+def num_threads() -> int:
+    return lib().oracle_num_threads()

@@ -1,0 +1,258 @@
+"""GPU parity of the CUDA path against the FP64 oracle, through the C-ABI (libghmm.so).
+
+Tolerances (|delta log10 L| against LoglessPairHMM in FP64 on the same inputs):
+  FP32 batched path        <= 1e-3 (budget); on the reference's vector test data <= 1e-5, the bar the
+                           reference sets for its native FP32 implementation (VectorPairHMMUnitTest.java:100)
+  FP64 path (reruns/mode)  <= 1e-9
+  plain FP64 kernel        <= 1e-12 (Java's operation order; only the final log10 may differ in the last ulp)
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from gatk_gb300 import native, workload as W
+from gatk_gb300.pairhmm import CudaLoglessPairHMM, Engine, PairHMMNativeArguments
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL32 = 1e-3
+TOL64 = 1e-9
+TOL_PLAIN = 1e-12
+
+
+def _golden_workload(name):
+    rows = load_golden(name)
+    regions = [([h], [(r, q, i, d, g)]) for h, r, q, i, d, g, _ in rows]
+    return W.from_pairs(regions), np.array([float(r[6]) for r in rows]), rows
+
+
+def _oracle_all(wl):
+    return O.compute_workload(wl)
+
+
+def _run(engine, wl, mode):
+    with engine.batch(wl) as b:
+        b.forward(mode)
+        return b.results(), b.stats()
+
+
+@pytest.mark.parametrize("name", ["hc_java_hmmresults.tsv", "vector_pairhmm_testdata.tsv"])
+def test_golden_fp32(engine, name):
+    wl, expected, _ = _golden_workload(name)
+    got, st = _run(engine, wl, native.MODE_FP32_RERUN)
+    ref = _oracle_all(wl)
+    assert np.max(np.abs(got - ref)) <= 1e-5
+    assert np.max(np.abs(got - expected)) <= 1e-5
+    assert st["n_rerun"] == 0
+
+
+@pytest.mark.parametrize("name", ["hc_java_hmmresults.tsv", "vector_pairhmm_testdata.tsv"])
+def test_golden_fp64_and_plain(engine, name):
+    wl, expected, rows = _golden_workload(name)
+    ref = _oracle_all(wl)
+    got64, _ = _run(engine, wl, native.MODE_FP64)
+    assert np.max(np.abs(got64 - ref)) <= TOL64
+    plain, _ = _run(engine, wl, native.MODE_PLAIN_FP64)
+    assert np.max(np.abs(plain - ref)) <= TOL_PLAIN
+    if name.startswith("hc_java"):
+        # the reference's own LOGLESS_CACHING dump matches as printed text
+        assert all("%e" % v == r[6] for v, r in zip(plain, rows))
+
+
+def test_workload0_all_modes(engine):
+    wl = W.generate(0)
+    ref = _oracle_all(wl)
+    got32, st = _run(engine, wl, native.MODE_FP32_RERUN)
+    d = np.abs(got32 - ref)
+    assert d.max() <= TOL32 and np.median(d) <= 1e-5
+    assert st["n_cells"] == wl.cells()
+    got64, _ = _run(engine, wl, native.MODE_FP64)
+    assert np.abs(got64 - ref).max() <= TOL64
+    plain, _ = _run(engine, wl, native.MODE_PLAIN_FP64)
+    assert np.abs(plain - ref).max() <= TOL_PLAIN
+
+
+def test_workload1_subsample(engine):
+    wl = W.generate(1, regions=24)
+    ref = _oracle_all(wl)
+    got, st = _run(engine, wl, native.MODE_FP32_RERUN)
+    d = np.abs(got - ref)
+    assert d.max() <= TOL32, d.max()
+    assert np.median(d) <= 1e-5
+    rerun = st["n_rerun"]
+    if rerun:
+        # pairs the FP32 pass handed to FP64 must be FP64-exact
+        small = ref < -60
+        assert np.abs(got[small] - ref[small]).max() <= TOL64
+
+
+def test_workload2_rerun_path(engine):
+    wl = W.generate(2, regions=2)
+    ref = _oracle_all(wl)
+    got, st = _run(engine, wl, native.MODE_FP32_RERUN)
+    assert st["n_rerun"] > 0
+    d = np.abs(got - ref)
+    # reruns are the underflowing pairs (log10 L below about -64)
+    under = ref < -64.2
+    assert np.abs(got[under] - ref[under]).max() <= TOL64
+    assert d.max() <= TOL32
+
+
+def _single(hap, read, q=30, ins=45, dl=45, gcp=10):
+    n = len(read)
+    arr = lambda v: np.full(n, v, dtype=np.uint8) if np.isscalar(v) else np.asarray(v, dtype=np.uint8)
+    return ([hap], [(read, arr(q), arr(ins), arr(dl), arr(gcp))])
+
+
+def _rand_seq(rng, n):
+    return bytes(rng.choice(list(b"ACGT"), size=n).astype(np.uint8))
+
+
+def test_strip_and_bucket_boundaries(engine):
+    # read lengths around every rows-per-lane bucket edge (32k) and the multi-strip switch (256)
+    rng = np.random.default_rng(7)
+    regions = []
+    for R in [1, 2, 3, 31, 32, 33, 63, 64, 65, 95, 96, 97, 127, 128, 129, 160, 191, 192, 193, 224, 225, 255, 256,
+              257, 300, 511, 512, 513, 700]:
+        hap = _rand_seq(rng, R + 40)
+        read = bytearray(hap[20:20 + R])
+        for k in rng.integers(0, R, size=max(1, R // 50)):
+            read[k] = ord("ACGT"[(b"ACGT".index(read[k]) + 1) % 4])
+        q = rng.integers(20, 41, size=R)
+        regions.append(([hap, _rand_seq(rng, R + 5)], [(bytes(read), q, np.full(R, 45), np.full(R, 45), np.full(R, 10)),
+                                                      (bytes(read[::-1]), q, np.full(R, 40), np.full(R, 43), np.full(R, 10))]))
+    wl = W.from_pairs(regions)
+    ref = _oracle_all(wl)
+    got, _ = _run(engine, wl, native.MODE_FP32_RERUN)
+    under = ref < -64.2
+    assert np.abs(got[~under] - ref[~under]).max() <= TOL32
+    assert np.abs(got[under] - ref[under]).max() <= TOL64
+
+
+def test_odd_reads_short_haps_and_long_reads(engine):
+    rng = np.random.default_rng(11)
+    regions = []
+    for nr in (1, 3, 5):
+        haps = [_rand_seq(rng, int(h)) for h in rng.integers(1, 60, size=3)]
+        reads = []
+        for _ in range(nr):
+            R = int(rng.integers(1, 90))
+            reads.append((_rand_seq(rng, R), rng.integers(10, 41, size=R), np.full(R, 45), np.full(R, 45), np.full(R, 10)))
+        regions.append((haps, reads))
+    wl = W.from_pairs(regions)
+    ref = _oracle_all(wl)
+    got, _ = _run(engine, wl, native.MODE_FP32_RERUN)
+    under = ref < -64.2
+    assert np.abs(got[~under] - ref[~under]).max() <= TOL32
+    if under.any():
+        assert np.abs(got[under] - ref[under]).max() <= TOL64
+
+
+def test_special_bytes_route_to_fp64(engine):
+    # N bases, gap continuation 0 and non-ACGTN bytes: results are exact FP64
+    rng = np.random.default_rng(3)
+    hap = _rand_seq(rng, 80)
+    read = bytearray(hap[10:60])
+    read[5] = ord("N")
+    read_r = bytearray(read)
+    read_r[7] = ord("R")
+    gcp0 = np.full(50, 10)
+    gcp0[20] = 0
+    hapn = bytearray(hap)
+    hapn[30] = ord("N")
+    regions = [
+        _single(hap, bytes(read)),
+        _single(bytes(hapn), bytes(read)),
+        _single(hap, bytes(read_r)),
+        _single(hap, bytes(read), gcp=gcp0),
+        _single(b"ACGTRACGT" + hap[:40], bytes(read)),
+    ]
+    wl = W.from_pairs(regions)
+    ref = _oracle_all(wl)
+    got, st = _run(engine, wl, native.MODE_FP32_RERUN)
+    assert st["n_fp64_direct"] == 3
+    assert np.abs(got[2:] - ref[2:]).max() <= TOL64
+    assert np.abs(got[:2] - ref[:2]).max() <= TOL32
+
+
+def test_empty_read_and_haplotype(engine):
+    wl = W.from_pairs([
+        ([b"ACGTACGT"], [(b"", [], [], [], [])]),
+        ([b""], [(b"ACG", [30, 30, 30], [45] * 3, [45] * 3, [10] * 3)]),
+    ])
+    got, _ = _run(engine, wl, native.MODE_FP32_RERUN)
+    assert np.all(got == -np.inf)
+
+
+def test_quality_out_of_range_is_an_argument_error(engine):
+    for q, ins in ((255, 45), (30, 128)):
+        wl = W.from_pairs([_single(b"ACGTACGT", b"ACGT", q=q, ins=ins)])
+        with pytest.raises(native.GhmmError) as e:
+            engine.compute(wl)
+        assert e.value.code == native.GHMM_ERR_ARG
+
+
+def test_entry_points_agree(engine):
+    wl = W.generate(1, regions=6)
+    a = engine.compute(wl)
+    b = engine.compute(wl, via_regions=True)
+    with engine.batch(wl, via_regions=True) as bt:
+        bt.forward()
+        c = bt.results()
+    assert np.array_equal(a, b) and np.array_equal(a, c)
+
+
+def test_repeated_forward_is_deterministic(engine):
+    wl = W.generate(1, regions=8)
+    with engine.batch(wl) as b:
+        b.forward()
+        x = b.results()
+        b.forward()
+        y = b.results()
+    assert np.array_equal(x, y)
+
+
+def test_pairhmm_interface_known_answer():
+    # PairHMMUnitTest.testLikelihoodsFromHaplotypes (PairHMMUnitTest.java:512-537): 10 A's vs 20 A's
+    hmm = CudaLoglessPairHMM(PairHMMNativeArguments())
+    try:
+        hmm.initialize([b"A" * 20])
+        assert hmm.compute_log10_likelihoods([]) is None
+        la = hmm.compute_log10_likelihoods([(b"A" * 10, [20] * 10, [45] * 10, [45] * 10, [100] * 10)])
+        assert la.shape == (1,)
+        expected = math.log10((20 - 10 + 1) / 20 * (1 - 10 ** -2.0) ** 10)
+        assert abs(la[0] - expected) <= 1e-3
+    finally:
+        hmm.close()
+
+
+def test_pairhmm_interface_read_major_matrix():
+    wl = W.generate(0)
+    haps = [wl.hap(h) for h in range(wl.n_haps)]
+    reads = [wl.read(r) for r in range(wl.n_reads)]
+    with CudaLoglessPairHMM() as hmm:
+        hmm.initialize(haps)
+        la = hmm.compute_log10_likelihoods(reads)
+    ref = _oracle_all(wl)
+    assert la.shape == ref.shape
+    assert np.abs(la - ref).max() <= TOL32
+
+
+def test_double_precision_argument():
+    wl = W.generate(0)
+    e = Engine(use_double_precision=True)
+    try:
+        got = e.compute(wl)
+    finally:
+        e.close()
+    assert np.abs(got - _oracle_all(wl)).max() <= TOL64
+
+
+def test_peaks_are_sane(engine):
+    p = engine.measure_peaks()
+    assert 20 < p["fp32_tflops"] < 200
+    assert 20 < p["fp32x2_tflops"] < 400
+    assert 0 < p["fp64_tflops"] < 100

@@ -1,0 +1,196 @@
+"""CPU tests of the host side: the C-ABI library loads and exports every declared symbol, the synthetic
+generator is deterministic and has the stated shapes, the product's tables equal the oracle's, and the
+STR analyzer matches DragstrReadSTRAnalyzerTest's brute-force definition and empirical case."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from gatk_gb300 import native, workload as W
+from oracle import oracle as O
+
+
+def _declared_functions():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names.update(re.findall(r"\b(ghmm_\w+)\s*\(", src))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    L = native.lib()
+    declared = _declared_functions()
+    assert declared, "no declarations found"
+    for name in declared:
+        assert hasattr(L, name), name
+    assert declared == set(native.exported_symbols())
+
+
+def test_no_gpu_here_reports_unsupported():
+    L = native.lib()
+    if L.ghmm_load():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    a = native.Args(0, 0, 0, 0)
+    assert L.ghmm_initialize(ctypes.byref(a), ctypes.byref(h)) == native.GHMM_ERR_UNSUPPORTED
+    assert native.last_error(None)
+
+
+def test_product_tables_equal_oracle():
+    err = np.zeros(256)
+    prob = np.zeros(256)
+    m2m = np.zeros(128 * 128)
+    p = lambda a: a.ctypes.data_as(native._f64p)
+    assert native.lib().ghmm_debug_tables(None, p(err), p(prob), p(m2m)) == 0
+    for q in range(255):
+        assert err[q] == O.lib().oracle_qual_to_error_prob(q)
+        assert prob[q] == O.lib().oracle_qual_to_prob(q)
+    m2m = m2m.reshape(128, 128)
+    for i in range(128):
+        for j in range(128):
+            assert m2m[i, j] == O.lib().oracle_match_to_match_prob(i, j), (i, j)
+
+
+def test_synth_deterministic_and_shaped():
+    a = W.generate(0)
+    b = W.generate(0)
+    for f in ("bases", "quals", "ins", "dels", "gcp", "hap_bases", "read_off", "hap_off"):
+        assert np.array_equal(getattr(a, f), getattr(b, f))
+    assert a.n_regions == 1 and a.n_haps == 8 and a.n_reads == 64
+    assert set(a.read_lengths()) == {150}
+    assert a.hap_lengths()[0] == 300
+    assert a.quals.min() >= 10 and a.quals.max() <= 40
+    assert set(np.unique(a.ins)) == {45} and set(np.unique(a.gcp)) == {10}
+    assert set(np.unique(a.hap_bases)) <= set(b"ACGT")
+
+
+def test_synth_region_ranges_compose():
+    whole = W.generate(1, regions=40)
+    part = W.generate(1, regions=15, region_begin=25)
+    sub = whole.subset(25, 40)
+    for f in ("bases", "quals", "hap_bases", "read_off", "hap_off", "region_read_off", "out_off"):
+        assert np.array_equal(getattr(sub, f), getattr(part, f)), f
+
+
+def test_synth_workload1_distributions():
+    wl = W.generate(1, regions=300)
+    nh = np.diff(wl.region_hap_off)
+    nr = np.diff(wl.region_read_off)
+    assert nh.min() >= 2 and nh.max() <= 32
+    assert nr.min() >= 1 and nr.max() <= 1000
+    assert 40 < np.median(nr) < 90  # lognormal(4,1): median e^4 = 54.6
+    rl = wl.read_lengths()
+    assert rl.min() >= 100 and rl.max() <= 250
+
+
+def test_synth_workload2_and_3_shapes():
+    w2 = W.generate(2, regions=5)
+    assert w2.read_lengths().min() >= 800 and w2.read_lengths().max() <= 2000
+    assert w2.quals.min() >= 5 and w2.quals.max() <= 25
+    assert w2.ins.min() >= 20 and w2.ins.max() <= 45
+    w3 = W.generate(3)
+    assert w3.n_regions == 512 and w3.n_reads == 4096 and w3.n_pairs == 4096
+    assert set(w3.hap_lengths()) == {300} and set(w3.read_lengths()) == {150}
+
+
+# ---- DRAGstr STR analyzer ----
+def _brute_repeats(seq: bytes, pos: int, period: int) -> int:
+    """DragstrReadSTRAnalyzerTest.calculateExpectedRepeatLength (DragstrReadSTRAnalyzerTest.java:131-168)."""
+    n = len(seq)
+    if period > n:
+        return 0
+    start = max(0, pos - period + 1)
+    best = 0
+    while start <= pos + 1 and start + period <= n:
+        unit = seq[start:start + period]
+        fwd = 1
+        off = start + period
+        while off <= n - period and seq[off:off + period] == unit:
+            fwd += 1
+            off += period
+        bwd = 0
+        off = start - period
+        while off >= 0 and seq[off:off + period] == unit:
+            bwd += 1
+            off -= period
+        cand = fwd + bwd
+        if pos < period - 1 and start == 0:
+            cand = max(1, cand - 1)
+        best = max(best, cand)
+        start += 1
+    return best
+
+
+def _analyze(seq: bytes, max_period: int):
+    n = len(seq)
+    a = np.frombuffer(seq, dtype=np.uint8).copy()
+    bp = np.zeros(n, dtype=np.int32)
+    br = np.zeros(n, dtype=np.int32)
+    allr = np.zeros(max_period * n, dtype=np.int32)
+    p32 = lambda x: x.ctypes.data_as(native._i32p)
+    assert native.lib().ghmm_str_analyze(a.ctypes.data_as(native._u8p), n, max_period, p32(bp), p32(br), p32(allr)) == 0
+    return bp, br, allr.reshape(max_period, n)
+
+
+def test_str_empirical_case():
+    # DragstrReadSTRAnalyzerTest.java:61-66 (hex digits, repeats capped at 20)
+    seq = b"ATTTTTTCAATGTTTACACATTTCCTTCCTCCCTCCCTCCTTCCTTTCCTCCCTTCCTCCCTTCCTCCCTTCCTTCCTGTTTGCTTTATTATTGTATTG"
+    periods = ("1 1 1 1 1 1 1 1 1 1 1 1 1 1 1 2 2 2 2 1 1 1 1 1 1 1 4 4 4 1 1 1 1 1 1 1 1 4 4 4 1 1 1 1 1 1 1 8 8 1 1 1 1 "
+               "8 8 8 8 1 1 1 1 8 8 8 8 1 1 1 1 8 8 8 8 8 1 1 1 4 1 1 1 1 1 1 1 1 1 1 1 1 1 1 1 5 5 1 1 1")
+    repeats = ("6 6 6 6 6 6 6 2 2 2 1 3 3 3 3 2 2 2 2 3 3 3 3 2 2 2 3 3 3 3 3 3 3 3 3 3 3 3 3 3 2 2 2 3 3 3 3 3 3 3 3 3 3 "
+               "3 3 3 3 3 3 3 3 3 3 3 3 3 3 3 3 3 3 3 3 3 2 2 2 2 3 3 3 3 1 3 3 3 3 2 2 2 2 2 2 2 2 2 2 2")
+    ep = [int(x, 16) for x in periods.split()]
+    er = [int(x, 16) for x in repeats.split()]
+    bp, br, _ = _analyze(seq, 8)
+    # the reference checks positions 0..len(expected)-1 (98 of the 99 bases)
+    assert list(bp[:len(ep)]) == ep
+    assert [min(20, x) for x in br[:len(er)]] == er
+
+
+FIXED = [b"TGATTTGCTCTGTCTGCTGCTGCTGCCTTCAGTAGGGTTGCACGCCTGGGCACGCCTGGAAT", b"AGTATACTGAT",
+         b"GTCTATATATATTTTAATTAATTAATTAATTAAATATATTTTCTGCTGCCTTTTGGAT", b"AAAAA", b"A", b"ACGTAGATCTGTAGCACTATCGAGC"]
+
+
+def _random_sequences(n=60, seed=131):
+    # DragstrReadSTRAnalyzerTest.java:171-197 recipe (random bases with induced tandem repeats)
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        length = int(rng.integers(5, 200))
+        b = bytearray(rng.choice(list(b"ACGT"), size=length).astype(np.uint8).tobytes())
+        for pos in range(length):
+            if rng.random() < 1.0 / length:
+                ul = int(rng.integers(1, 11))
+                reps = int(rng.integers(2, 12))
+                unit = rng.choice(list(b"ACGT"), size=ul).astype(np.uint8).tobytes()
+                off = pos
+                for _r in range(reps):
+                    if off >= length - ul:
+                        break
+                    m = min(ul, length - off)
+                    b[off:off + m] = unit[:m]
+                    off += ul
+        out.append(bytes(b))
+    return out
+
+
+@pytest.mark.parametrize("seq", FIXED + _random_sequences())
+def test_str_matches_bruteforce(seq):
+    # DragstrReadSTRAnalyzerTest.testRepeatPeriodAndCount / testRepeatBestPeriodAndCount
+    max_period = max(5, len(seq) // 4)
+    bp, br, allr = _analyze(seq, max_period)
+    for pos in range(len(seq)):
+        exp = [_brute_repeats(seq, pos, p) for p in range(1, max_period + 1)]
+        assert list(allr[:, pos]) == exp, (pos, list(allr[:, pos]), exp)
+        best_p, best_r = 1, exp[0]
+        for p in range(2, max_period + 1):
+            if exp[p - 1] > best_r:
+                best_p, best_r = p, exp[p - 1]
+        assert (bp[pos], br[pos]) == (best_p, best_r)
