@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""PairHMM read-likelihood benchmark on GB300: GCUPS of the batched FP32 + FP64-rerun forward.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload 1]
+
+A step is one forward over the whole workload (default: workload 1, 10,000 synthetic active regions,
+seed 1, ~1.06e12 cells): every read x haplotype pair of every region, FP32 wavefront plus the FP64 rerun
+of every pair whose FP32 result underflows.  `value` is GCUPS (cells / device second) with the inputs
+already resident in HBM, timed with CUDA events on the library's stream; `e2e` is the same metric
+through the JNI-shaped C-ABI call (ghmm_compute_regions) from host buffers: marshalling, H2D copies,
+kernels, D2H of the results and their validation are all inside its timed region.
+
+Beside it the line reports the plain FP64 kernel (one pair per thread block, one launch per region) on a
+subsample, the accuracy of the timed results against the FP64 oracle on the CPU-baseline sample, the
+roofline of the dominant kernel (the FP32 bucket launches) against the FP32 FMA-pipe peak measured in the
+same run, and the FP64 oracle's GCUPS on the host cores.
+
+--impl reference times the reference's algorithm on the host CPU: the FP64 restatement of
+LoglessPairHMM (oracle/, OpenMP over pairs on every host core) on a bounded sample of the same workload;
+GATK's Java and GKL's AVX code cannot run on this machine (no JVM; GKL is x86-only).
+Under torchrun with N > 1 each rank runs its own 10,000 regions on its own GPU (weak scaling; the regions
+are independent so no collective touches the data path); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PairHMM GCUPS, batched FP32 vs plain FP64 on 1 GB300 at |Δlog10 L|≤1e-3"
+FLOP_PER_CELL = 11  # M: add, mul, fma, mul (5); I: fma (3); D: fma (3); FMA counted as 2
+CPU_SAMPLE_CELLS = 2.0e10  # cells of the oracle's timed sample (about 5-15 s on 16 cores)
+PLAIN_SAMPLE_CELLS = 2.0e10  # cells of the plain-FP64-kernel comparison
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock and throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self._t:
+            self._t.join(timeout=5)
+        sm, mx, pw, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+                pw.append(float(parts[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(pw) if pw else None, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(wl, cells_target):
+    """Leading regions of the workload whose cells reach cells_target (the deterministic CPU sample)."""
+    import numpy as np
+
+    cpr = wl.cells_per_region()
+    n = int(np.searchsorted(np.cumsum(cpr), cells_target)) + 1
+    n = max(1, min(n, wl.n_regions))
+    return n, int(cpr[:n].sum())
+
+
+def run_reference(args):
+    """--impl reference: the FP64 oracle (LoglessPairHMM restated in C, OpenMP) on host cores."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from gatk_gb300 import workload as W
+    from oracle import oracle as O
+
+    wl_full = W.generate(args.workload, regions=args.regions)
+    n, cells = cpu_sample(wl_full, args.cpu_cells)
+    sub = wl_full.subset(0, n)
+    threads = O.num_threads()
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        O.compute_workload(sub, threads=0)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    gcups = cells / statistics.mean(times) / 1e9
+    sample = (f"first {n} of {wl_full.n_regions} regions of workload {args.workload} ({cells:.3e} cells, "
+              f"{sub.n_pairs} pairs) per step")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": gcups, "unit": "GCUPS", "higher_is_better": True,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": statistics.mean(times) * 1e3, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (deterministic generator, seed per workload)",
+        "config": workload_config(args, wl_full),
+        "cpu_baseline": {"value": gcups, "unit": "GCUPS", "cores": threads, "kind": "port", "sample": sample,
+                         "host": f"{platform.machine()} x{os.cpu_count()}"},
+        "e2e": {"value": gcups, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("FP64 C restatement of LoglessPairHMM (oracle/pairhmm_oracle.c); GATK's Java LoglessPairHMM needs "
+                 "a JVM and GKL AVX_LOGLESS_CACHING_OMP is x86-only, neither runs on this host"),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(args, wl):
+    names = {0: "config0: 1 region, 8 haps x 64 reads, seed 0",
+             1: "config1: 10,000 active regions, seed 1 (haps U[2,32] of U[200,600] bp, "
+                "reads lognormal(4,1) of U[100,250] bp)",
+             2: "config2: 2,000 long-pair regions, seed 2", 4: "config4 body: config1 distributions, seed 4"}
+    return {"workload": names.get(args.workload, f"workload {args.workload}"), "regions": wl.n_regions,
+            "pairs": wl.n_pairs, "cells": int(wl.cells_per_region().sum()),
+            "l2": f"inputs larger than L2 ({(wl.bases.nbytes * 5 + wl.hap_bases.nbytes) / 1e6:.0f} MB of read and "
+                  f"haplotype bytes vs 129 MB L2)"}
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from gatk_gb300 import native, workload as W
+    from gatk_gb300.pairhmm import Engine
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+    torch.cuda.set_device(local)
+    device = local
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        return float(t.item())
+
+    eng = Engine(device=device)
+    peaks = eng.measure_peaks()
+    # weak scaling: every rank owns its own block of regions of the same distribution
+    n_regions = args.regions or int(native.lib().ghmm_synth_default_regions(args.workload))
+    wl = W.generate(args.workload, regions=n_regions, region_begin=rank * n_regions)
+    cells = int(wl.cells_per_region().sum())
+
+    # ---- device-resident forward (value) ----
+    batch = eng.batch(wl)
+    for _ in range(args.warmup):
+        batch.forward(native.MODE_FP32_RERUN)
+    stream = torch.cuda.ExternalStream(eng.stream_handle(), device=f"cuda:{device}")
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(device)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize(device)
+    ev0.record(stream)
+    st_steps = []
+    for _ in range(args.steps):
+        batch.forward(native.MODE_FP32_RERUN)
+        st_steps.append(batch.stats())
+    ev1.record(stream)
+    torch.cuda.synchronize(device)
+    barrier()
+    clk = clocks.stop()
+    ms_step_local = ev0.elapsed_time(ev1) / args.steps
+    ms_step = max_over_ranks(ms_step_local)
+    total_cells = sum_over_ranks(float(cells))
+    value = total_cells / (ms_step * 1e-3) / 1e9
+    launches = sum(s["n_launches"] for s in st_steps)
+    st = st_steps[-1]
+    ms_fp32 = statistics.mean(s["ms_fp32"] for s in st_steps)
+    ms_fp64 = statistics.mean(s["ms_fp64"] for s in st_steps)
+    results = batch.results()
+    io = batch.stats()  # byte counts of upload + forward + results (what one e2e call moves)
+    rerun_frac = st["n_rerun"] / max(1, st["n_pairs"])
+
+    # ---- e2e through the JNI-shaped C-ABI from host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        regs = wl.as_regions()
+        out = np.empty(wl.n_pairs, dtype=np.float64)
+        L = eng.L
+        for _ in range(max(1, min(args.warmup, 2))):
+            native.check(L.ghmm_compute_regions(eng.handle, regs, wl.n_regions, out.ctypes.data_as(native._f64p)),
+                         eng.handle)
+        barrier()
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        e2e_steps = max(1, min(args.steps, 3))
+        for _ in range(e2e_steps):
+            native.check(L.ghmm_compute_regions(eng.handle, regs, wl.n_regions, out.ctypes.data_as(native._f64p)),
+                         eng.handle)
+        torch.cuda.synchronize(device)
+        dt = (time.perf_counter() - t0) / e2e_steps
+        barrier()
+        dt = max_over_ranks(dt)
+        same = bool(np.array_equal(out, results))
+        e2e = {"value": total_cells / dt / 1e9, "unit": "GCUPS", "ms_per_step": dt * 1e3,
+               "h2d_bytes_per_step": int(io["h2d_bytes"]), "d2h_bytes_per_step": int(io["d2h_bytes"]),
+               "api": "ghmm_compute_regions (per-read pointer arrays, as the JNI binding passes them)",
+               "matches_device_resident_results": same}
+
+    if rank != 0:
+        batch.close()
+        eng.close()
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
+    # ---- accuracy and CPU baseline on the deterministic sample ----
+    from oracle import oracle as O
+
+    n_cpu, cpu_cells = cpu_sample(wl, args.cpu_cells)
+    sub = wl.subset(0, n_cpu)
+    t0 = time.perf_counter()
+    ref = O.compute_workload(sub, threads=0)
+    cpu_dt = time.perf_counter() - t0
+    got = results[:sub.n_pairs]
+    d = np.abs(got - ref)
+    under = ref < -64.2
+    accuracy = {"sample_pairs": int(sub.n_pairs), "max_abs_dlog10": float(d.max()),
+                "median_abs_dlog10": float(np.median(d)),
+                "fp64_rerun_pairs_in_sample": int(under.sum()),
+                "max_abs_dlog10_fp64_reruns": float(d[under].max()) if under.any() else None}
+    cpu_baseline = {"value": cpu_cells / cpu_dt / 1e9, "unit": "GCUPS", "cores": O.num_threads(), "kind": "port",
+                    "sample": f"first {n_cpu} regions of the timed workload ({cpu_cells:.3e} cells, {sub.n_pairs} pairs)",
+                    "host": f"{platform.machine()} x{os.cpu_count()}"}
+
+    # ---- plain FP64 kernel, one pair per block, one launch per region ----
+    n_pl, pl_cells = cpu_sample(wl, args.plain_cells)
+    with eng.batch(wl.subset(0, n_pl)) as pb:
+        pb.forward(native.MODE_PLAIN_FP64)
+        pb.forward(native.MODE_PLAIN_FP64)
+        pst = pb.stats()
+        plain_res = pb.results()
+    plain_gcups = pl_cells / (pst["ms_plain"] * 1e-3) / 1e9
+    plain_vs_ours = float(np.abs(plain_res - results[:len(plain_res)]).max())
+
+    # ---- roofline of the dominant kernel: the FP32 bucket launches of one forward ----
+    direct_cells = 0  # pairs sent straight to FP64 (none in the synthetic workloads)
+    fp32_cells = cells - direct_cells
+    achieved = FLOP_PER_CELL * fp32_cells / (ms_fp32 * 1e-3) / 1e12
+    peak = max(peaks["fp32_tflops"], peaks["fp32x2_tflops"])
+    traffic = read_profile_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (deterministic generator; seeded stand-in for HaplotypeCaller active regions)",
+        "config": workload_config(args, wl),
+        "roofline": {"bound": "fp32_fma_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "fp32_bucket_kernel (all rows-per-lane buckets of one forward)",
+                     "flop_per_cell": FLOP_PER_CELL, "cells_per_launch_set": fp32_cells,
+                     "ms_per_launch_set": ms_fp32,
+                     "peak_source": ("measured in this run: FFMA and FFMA2 register loops over all SMs "
+                                     f"({peaks['fp32_tflops']:.1f} / {peaks['fp32x2_tflops']:.1f} TFLOP/s); "
+                                     "MEASURED_PEAKS.json carries no FP32 figure")},
+        "cpu_baseline": cpu_baseline,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "fp64_rerun": {"pairs": int(st["n_rerun"]), "fraction": rerun_frac, "ms": ms_fp64},
+        "plain_fp64": {"value": plain_gcups, "unit": "GCUPS", "regions": n_pl, "cells": pl_cells,
+                       "launches": int(pst["n_launches"]), "speedup_batched_vs_plain": value / world / plain_gcups,
+                       "max_abs_diff_vs_batched": plain_vs_ours},
+        "accuracy_vs_fp64_oracle": accuracy,
+        "peaks_measured": peaks,
+    }
+    print(json.dumps(line), flush=True)
+    batch.close()
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def read_profile_traffic():
+    """DRAM bytes per launch set of the FP32 kernels from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "fp32_bucket_kernel_workload1.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch_set:"):
+                    return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", type=int, default=1)
+    ap.add_argument("--regions", type=int, default=0, help="regions per rank (0: the workload's full size)")
+    ap.add_argument("--cpu-cells", type=float, default=CPU_SAMPLE_CELLS)
+    ap.add_argument("--plain-cells", type=float, default=PLAIN_SAMPLE_CELLS)
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -183,6 +183,12 @@ __global__ void __launch_bounds__(128) fp32_bucket_kernel(DevTables T, DevBatch 
                 const int c = s - lane;
                 const bool valid = (c >= 0) && (c < ncols);
                 const uint32_t code = valid ? (uint32_t)__ldg(stream + c) : 0u;
+                // row above at this column: lane l-1's last row as computed last step.  Shuffled before
+                // this lane resets its own state at a haplotype start, since lane l+1 still needs the
+                // previous haplotype's last column from it.
+                float2 uM = shfl_up2(Mp[K - 1]);
+                float2 uI = shfl_up2(Ip[K - 1]);
+                float2 uD = shfl_up2(Dp[K - 1]);
                 if (code & kColFirst) {
                     ++hap;
                     const float init = __ldg(B.hap_init_f + hap);
@@ -200,10 +206,7 @@ __global__ void __launch_bounds__(128) fp32_bucket_kernel(DevTables T, DevBatch 
                     if (lane == 0 && strip == 0) bnd = X;
                     acc = zero2();
                 }
-                // row above at this column: lane l-1's last row (computed last step) or the boundary
-                float2 uM = shfl_up2(Mp[K - 1]);
-                float2 uI = shfl_up2(Ip[K - 1]);
-                float2 uD = shfl_up2(Dp[K - 1]);
+                // lane 0 takes the row-0 boundary (strip 0) or the previous strip's last row instead
                 if (MULTI && strip > 0) {
                     const float2 bM = nxM, bI = nxI, bD = nxD;
                     if (lane == 0 && c + 1 < ncols) {

@@ -298,7 +298,7 @@ int64_t oracle_compute_regions(int32_t n_regions, const int64_t *region_read_off
     for (int32_t g = 0; g < n_regions; g++)
         total += (region_read_off[g + 1] - region_read_off[g]) * (region_hap_off[g + 1] - region_hap_off[g]);
 #ifdef _OPENMP
-    if (threads > 0) omp_set_num_threads(threads);
+    omp_set_num_threads(threads > 0 ? threads : omp_get_num_procs());
 #else
     (void)threads;
 #endif
@@ -330,7 +330,7 @@ void oracle_compute_pairs(int64_t n_pairs, const int64_t *pair_read, const int64
                           const uint8_t *gcp, const int64_t *hap_off, const uint8_t *hap_bases, double *out,
                           int threads) {
 #ifdef _OPENMP
-    if (threads > 0) omp_set_num_threads(threads);
+    omp_set_num_threads(threads > 0 ? threads : omp_get_num_procs());
 #else
     (void)threads;
 #endif

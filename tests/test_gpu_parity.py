@@ -21,6 +21,8 @@ pytestmark = pytest.mark.gpu
 TOL32 = 1e-3
 TOL64 = 1e-9
 TOL_PLAIN = 1e-12
+# log10 L below which the FP32 scaled sum (L * 2^120) is under the 1e-28 rerun threshold
+RERUN_LOG10 = math.log10(1e-28) - 120 * math.log10(2)
 
 
 def _golden_workload(name):
@@ -31,6 +33,18 @@ def _golden_workload(name):
 
 def _oracle_all(wl):
     return O.compute_workload(wl)
+
+
+def _absdiff(got, ref):
+    """|got - ref| where equal infinities count as 0 (a pair whose likelihood underflows even the FP64
+    2^1020 scale is -Infinity in LoglessPairHMM too); any other non-finite value is an error."""
+    got = np.asarray(got)
+    ref = np.asarray(ref)
+    same_inf = np.isinf(got) & np.isinf(ref) & (got == ref)
+    with np.errstate(invalid="ignore"):
+        d = np.where(same_inf, 0.0, np.abs(got - ref))
+    assert not np.isnan(d).any(), "non-finite result where the oracle has a finite one"
+    return d
 
 
 def _run(engine, wl, mode):
@@ -44,8 +58,8 @@ def test_golden_fp32(engine, name):
     wl, expected, _ = _golden_workload(name)
     got, st = _run(engine, wl, native.MODE_FP32_RERUN)
     ref = _oracle_all(wl)
-    assert np.max(np.abs(got - ref)) <= 1e-5
-    assert np.max(np.abs(got - expected)) <= 1e-5
+    assert np.max(_absdiff(got, ref)) <= 1e-5
+    assert np.max(_absdiff(got, expected)) <= 1e-5
     assert st["n_rerun"] == 0
 
 
@@ -54,9 +68,9 @@ def test_golden_fp64_and_plain(engine, name):
     wl, expected, rows = _golden_workload(name)
     ref = _oracle_all(wl)
     got64, _ = _run(engine, wl, native.MODE_FP64)
-    assert np.max(np.abs(got64 - ref)) <= TOL64
+    assert np.max(_absdiff(got64, ref)) <= TOL64
     plain, _ = _run(engine, wl, native.MODE_PLAIN_FP64)
-    assert np.max(np.abs(plain - ref)) <= TOL_PLAIN
+    assert np.max(_absdiff(plain, ref)) <= TOL_PLAIN
     if name.startswith("hc_java"):
         # the reference's own LOGLESS_CACHING dump matches as printed text
         assert all("%e" % v == r[6] for v, r in zip(plain, rows))
@@ -66,27 +80,27 @@ def test_workload0_all_modes(engine):
     wl = W.generate(0)
     ref = _oracle_all(wl)
     got32, st = _run(engine, wl, native.MODE_FP32_RERUN)
-    d = np.abs(got32 - ref)
+    d = _absdiff(got32, ref)
     assert d.max() <= TOL32 and np.median(d) <= 1e-5
     assert st["n_cells"] == wl.cells()
     got64, _ = _run(engine, wl, native.MODE_FP64)
-    assert np.abs(got64 - ref).max() <= TOL64
+    assert _absdiff(got64, ref).max() <= TOL64
     plain, _ = _run(engine, wl, native.MODE_PLAIN_FP64)
-    assert np.abs(plain - ref).max() <= TOL_PLAIN
+    assert _absdiff(plain, ref).max() <= TOL_PLAIN
 
 
 def test_workload1_subsample(engine):
     wl = W.generate(1, regions=24)
     ref = _oracle_all(wl)
     got, st = _run(engine, wl, native.MODE_FP32_RERUN)
-    d = np.abs(got - ref)
+    d = _absdiff(got, ref)
     assert d.max() <= TOL32, d.max()
     assert np.median(d) <= 1e-5
     rerun = st["n_rerun"]
     if rerun:
-        # pairs the FP32 pass handed to FP64 must be FP64-exact
-        small = ref < -60
-        assert np.abs(got[small] - ref[small]).max() <= TOL64
+        # pairs the FP32 pass handed to FP64 (scaled sum < 1e-28, i.e. log10 L < -64.12) are FP64-exact
+        small = ref < RERUN_LOG10 - 0.01
+        assert _absdiff(got[small], ref[small]).max() <= TOL64
 
 
 def test_workload2_rerun_path(engine):
@@ -94,10 +108,10 @@ def test_workload2_rerun_path(engine):
     ref = _oracle_all(wl)
     got, st = _run(engine, wl, native.MODE_FP32_RERUN)
     assert st["n_rerun"] > 0
-    d = np.abs(got - ref)
+    d = _absdiff(got, ref)
     # reruns are the underflowing pairs (log10 L below about -64)
-    under = ref < -64.2
-    assert np.abs(got[under] - ref[under]).max() <= TOL64
+    under = ref < RERUN_LOG10 - 0.01
+    assert _absdiff(got[under], ref[under]).max() <= TOL64
     assert d.max() <= TOL32
 
 
@@ -127,9 +141,32 @@ def test_strip_and_bucket_boundaries(engine):
     wl = W.from_pairs(regions)
     ref = _oracle_all(wl)
     got, _ = _run(engine, wl, native.MODE_FP32_RERUN)
-    under = ref < -64.2
-    assert np.abs(got[~under] - ref[~under]).max() <= TOL32
-    assert np.abs(got[under] - ref[under]).max() <= TOL64
+    under = ref < RERUN_LOG10 - 0.01
+    assert _absdiff(got[~under], ref[~under]).max() <= TOL32
+    assert _absdiff(got[under], ref[under]).max() <= TOL64
+
+
+def test_reads_longer_than_haplotypes_across_haplotype_boundaries(engine):
+    # Every haplotype but the last hands the wavefront to the next one mid-warp; reads longer than the
+    # haplotypes make the insertion chain at each haplotype's last column dominate the likelihood.
+    rng = np.random.default_rng(19)
+    regions = []
+    for R, H in ((240, 225), (247, 219), (60, 40), (33, 31), (150, 100), (300, 280)):
+        base = _rand_seq(rng, H)
+        haps = [base, base[:H - 3] + b"ACG", _rand_seq(rng, H - 5)]
+        reads = []
+        for _ in range(3):
+            rd = bytearray(base + _rand_seq(rng, R - H))
+            q = rng.integers(10, 41, size=R)
+            reads.append((bytes(rd), q, np.full(R, 45), np.full(R, 45), np.full(R, 10)))
+        regions.append((haps, reads))
+    wl = W.from_pairs(regions)
+    ref = _oracle_all(wl)
+    got, _ = _run(engine, wl, native.MODE_FP32_RERUN)
+    under = ref < RERUN_LOG10 - 0.01
+    assert _absdiff(got[~under], ref[~under]).max() <= TOL32
+    if under.any():
+        assert _absdiff(got[under], ref[under]).max() <= TOL64
 
 
 def test_odd_reads_short_haps_and_long_reads(engine):
@@ -145,10 +182,10 @@ def test_odd_reads_short_haps_and_long_reads(engine):
     wl = W.from_pairs(regions)
     ref = _oracle_all(wl)
     got, _ = _run(engine, wl, native.MODE_FP32_RERUN)
-    under = ref < -64.2
-    assert np.abs(got[~under] - ref[~under]).max() <= TOL32
+    under = ref < RERUN_LOG10 - 0.01
+    assert _absdiff(got[~under], ref[~under]).max() <= TOL32
     if under.any():
-        assert np.abs(got[under] - ref[under]).max() <= TOL64
+        assert _absdiff(got[under], ref[under]).max() <= TOL64
 
 
 def test_special_bytes_route_to_fp64(engine):
@@ -174,8 +211,8 @@ def test_special_bytes_route_to_fp64(engine):
     ref = _oracle_all(wl)
     got, st = _run(engine, wl, native.MODE_FP32_RERUN)
     assert st["n_fp64_direct"] == 3
-    assert np.abs(got[2:] - ref[2:]).max() <= TOL64
-    assert np.abs(got[:2] - ref[:2]).max() <= TOL32
+    assert _absdiff(got[2:], ref[2:]).max() <= TOL64
+    assert _absdiff(got[:2], ref[:2]).max() <= TOL32
 
 
 def test_empty_read_and_haplotype(engine):
@@ -238,7 +275,7 @@ def test_pairhmm_interface_read_major_matrix():
         la = hmm.compute_log10_likelihoods(reads)
     ref = _oracle_all(wl)
     assert la.shape == ref.shape
-    assert np.abs(la - ref).max() <= TOL32
+    assert _absdiff(la, ref).max() <= TOL32
 
 
 def test_double_precision_argument():
@@ -248,7 +285,7 @@ def test_double_precision_argument():
         got = e.compute(wl)
     finally:
         e.close()
-    assert np.abs(got - _oracle_all(wl)).max() <= TOL64
+    assert _absdiff(got, _oracle_all(wl)).max() <= TOL64
 
 
 def test_peaks_are_sane(engine):
