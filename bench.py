@@ -187,25 +187,20 @@ def run_ours(args):
         if dist is not None:
             dist.barrier()
 
+    from gatk_gb300 import sharding
+
     def max_over_ranks(x: float) -> float:
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return sharding.reduce_max(x, device=f"cuda:{device}")
 
     def sum_over_ranks(x: float) -> float:
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        return float(t.item())
+        return sharding.reduce_sum(x, device=f"cuda:{device}")
 
     eng = Engine(device=device)
     peaks = eng.measure_peaks()
     # weak scaling: every rank owns its own block of regions of the same distribution
     n_regions = args.regions or int(native.lib().ghmm_synth_default_regions(args.workload))
-    wl = W.generate(args.workload, regions=n_regions, region_begin=rank * n_regions)
+    g0, g1 = sharding.block_range(n_regions, rank)
+    wl = W.generate(args.workload, regions=g1 - g0, region_begin=g0)
     cells = int(wl.cells_per_region().sum())
 
     # ---- device-resident forward (value) ----
