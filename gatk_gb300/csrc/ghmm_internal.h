@@ -79,5 +79,7 @@ constexpr int kPlainMaxRead = 1024;
 int fp32_kernel_occupancy(int k, int block, int *blocks_per_sm);
 int fp64_kernel_occupancy(int block, int *blocks_per_sm);
 int measure_peaks_device(int sm_count, double *fp32, double *fp32x2, double *fp64, cudaStream_t s);
+// Message returned by ghmm_last_error(NULL, ...) (runtime.cpp).
+void set_global_error(const char *msg);
 
 }  // namespace ghmm

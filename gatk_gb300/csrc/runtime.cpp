@@ -670,6 +670,11 @@ static int batch_results(ghmm_ctx *ctx, ghmm_batch &b, double *out) {
     return GHMM_OK;
 }
 
+void ghmm::set_global_error(const char *msg) {
+    std::lock_guard<std::mutex> lk(g_init_error_mu);
+    g_init_error = msg ? msg : "";
+}
+
 // -------------------------------------------------------------------------------------------------
 // C-ABI
 extern "C" {

@@ -72,6 +72,17 @@ class Stats(ctypes.Structure):
                 ("d2h_bytes", ctypes.c_int64)]
 
 
+class DevPairs(ctypes.Structure):
+    _fields_ = [("bases", ctypes.c_void_p), ("quals", ctypes.c_void_p), ("ins_gop", ctypes.c_void_p),
+                ("del_gop", ctypes.c_void_p), ("gcp", ctypes.c_void_p), ("read_off", ctypes.c_void_p),
+                ("hap_bases", ctypes.c_void_p), ("hap_off", ctypes.c_void_p), ("pair_read", ctypes.c_void_p),
+                ("pair_hap", ctypes.c_void_p), ("n_pairs", ctypes.c_int64), ("max_hap_len", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+NOALLOC_MAX_HAP_LEN = 2048
+
+
 class SynthArrays(ctypes.Structure):
     _fields_ = [("n_regions", ctypes.c_int64), ("n_reads", ctypes.c_int64), ("n_haps", ctypes.c_int64),
                 ("read_bytes", ctypes.c_int64), ("hap_bytes", ctypes.c_int64), ("n_out", ctypes.c_int64),
@@ -107,6 +118,8 @@ _SIGS = {
     "ghmm_synth_view": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SynthArrays)]),
     "ghmm_synth_free": (None, [ctypes.c_void_p]),
     "ghmm_str_analyze": (ctypes.c_int, [_u8p, ctypes.c_int32, ctypes.c_int32, _i32p, _i32p, _i32p]),
+    "ghmm_forward_pairs_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(DevPairs), ctypes.c_void_p,
+                                                  ctypes.c_void_p]),
 }
 
 _lib = None

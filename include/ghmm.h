@@ -166,6 +166,35 @@ int ghmm_measure_peaks(ghmm_ctx *ctx, double *fp32_tflops, double *fp32x2_tflops
  * With ctx == NULL the host-built tables are returned (no device needed). */
 int ghmm_debug_tables(ghmm_ctx *ctx, double *err, double *prob, double *m2m);
 
+/* ---- No-allocation entry point.  It has no counterpart in the reference. ----
+ * For callers that cannot allocate GPU memory (code running inside another framework's memory pool or
+ * a fixed device-memory budget, or that must not take the synchronisation an allocation implies):
+ * log10 likelihoods of explicit (read, haplotype) pairs whose bytes the caller already holds in device
+ * memory, written to d_out[n_pairs] (device), with the FP64 wavefront kernel.  The call allocates
+ * nothing: its scratch (strip-boundary rows for reads longer than 128 bases, 12 MiB) and its Phred
+ * tables are static device arrays that every GPU which loads the library holds until the process exits.
+ * The first call on a device (made with that device current) resolves the scratch address and fills
+ * the tables, so it should come before any stream capture.  Calls share the scratch array and must not
+ * overlap on the GPU.  Haplotypes longer than GHMM_NOALLOC_MAX_HAP_LEN are rejected with GHMM_ERR_ARG
+ * (max_hap_len is the caller's bound; a longer haplotype found on the device yields NaN for its pair).
+ * Launches on `stream` (a cudaStream_t; NULL is the legacy default stream) and returns without waiting;
+ * error messages come from ghmm_last_error(NULL, ...). */
+#define GHMM_NOALLOC_MAX_HAP_LEN 2048
+#define GHMM_NOALLOC_WARPS 256
+
+typedef struct ghmm_dev_pairs {
+    const uint8_t *bases, *quals, *ins_gop, *del_gop, *gcp; /* device read planes */
+    const int64_t *read_off;                                /* device [n_reads+1] */
+    const uint8_t *hap_bases;                               /* device */
+    const int64_t *hap_off;                                 /* device [n_haps+1] */
+    const int32_t *pair_read, *pair_hap;                    /* device [n_pairs] */
+    int64_t n_pairs;
+    int32_t max_hap_len; /* caller's bound on every haplotype length, <= GHMM_NOALLOC_MAX_HAP_LEN */
+    int32_t reserved;
+} ghmm_dev_pairs;
+
+int ghmm_forward_pairs_noalloc(int32_t device, const ghmm_dev_pairs *pairs, double *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
