@@ -73,6 +73,7 @@ struct DevBatch {
 int launch_fp32_bucket(const DevTables &t, const DevBatch &b, int k, int task_begin, int task_count, int grid,
                        int block, int counter_slot, cudaStream_t s);
 int launch_fp64_queue(const DevTables &t, const DevBatch &b, int grid, int block, cudaStream_t s);
+int launch_finalize_fp32(double *out, int64_t n, int sm_count, cudaStream_t s);
 int launch_plain_region(const DevTables &t, const DevBatch &b, int region, int n_reads, int n_haps, int max_read_len,
                         cudaStream_t s);
 constexpr int kPlainMaxRead = 1024;

@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 #include <cfloat>
 #include <cstdint>
+#include <type_traits>
 
 #include "../../include/ghmm.h"
 #include "ghmm_internal.h"
@@ -92,9 +93,11 @@ __device__ __forceinline__ RowCoef row_coef(const DevTables &T, const DevBatch &
     return c;
 }
 
+// Accepted sums are stored raw (as double); finalize_fp32_kernel turns them into log10 with every lane busy,
+// rather than one lane per warp running the FP64 log10 here on the 1/64-rate FP64 pipe.
 __device__ __forceinline__ void emit_fp32(const DevBatch &B, float sum, int read, int hap, int64_t out_index) {
     if (sum >= GHMM_FP32_RERUN_THRESHOLD && sum <= FLT_MAX) {
-        B.out[out_index] = log10((double)sum) - kLog10Scale32;
+        B.out[out_index] = (double)sum;
     } else {
         const int idx = atomicAdd(&B.counters[1], 1);
         if ((int64_t)idx < B.rerun_capacity) {
@@ -179,32 +182,45 @@ __global__ void __launch_bounds__(128) fp32_bucket_kernel(DevTables T, DevBatch 
                 nxD = scratch[2];
             }
             const int nsteps = ncols + 31;
-            for (int s = 0; s < nsteps; ++s) {
+            // One wavefront step.  CHK steps handle columns outside the stream (lanes that have not started
+            // or have finished), haplotype starts (state reset) and ends (lane 31 emits); they are needed
+            // only in the 32 steps after each haplotype start, where those events fall.  Every other step
+            // runs the check-free form.
+            auto step = [&](const int s, auto chk_tag) {
+                constexpr bool CHK = decltype(chk_tag)::value;
                 const int c = s - lane;
-                const bool valid = (c >= 0) && (c < ncols);
-                const uint32_t code = valid ? (uint32_t)__ldg(stream + c) : 0u;
+                bool valid = true;
+                uint32_t code;
+                if constexpr (CHK) {
+                    valid = (c >= 0) && (c < ncols);
+                    code = valid ? (uint32_t)__ldg(stream + c) : 0u;
+                } else {
+                    code = (uint32_t)__ldg(stream + c);
+                }
                 // row above at this column: lane l-1's last row as computed last step.  Shuffled before
                 // this lane resets its own state at a haplotype start, since lane l+1 still needs the
                 // previous haplotype's last column from it.
                 float2 uM = shfl_up2(Mp[K - 1]);
                 float2 uI = shfl_up2(Ip[K - 1]);
                 float2 uD = shfl_up2(Dp[K - 1]);
-                if (code & kColFirst) {
-                    ++hap;
-                    const float init = __ldg(B.hap_init_f + hap);
-                    const float2 X = make_float2(init * tim1.x, init * tim1.y);
+                if constexpr (CHK) {
+                    if (code & kColFirst) {
+                        ++hap;
+                        const float init = __ldg(B.hap_init_f + hap);
+                        const float2 X = make_float2(init * tim1.x, init * tim1.y);
+                        // dummy rows (global slot < pad) hold the row-0 value X in D^; a pad may reach past
+                        // strip 0 for the shorter read of a pair
+                        const int slot0 = strip * S + lane * K;
 #pragma unroll
-                    for (int k = 0; k < K; ++k) {
-                        const int slot = lane * K + k;
-                        Mp[k] = Ip[k] = zero2();
-                        Dp[k] = make_float2((strip == 0 && slot < task.pad_a) ? X.x : 0.f,
-                                            (strip == 0 && slot < task.pad_b) ? X.y : 0.f);
+                        for (int k = 0; k < K; ++k) {
+                            Mp[k] = Ip[k] = zero2();
+                            Dp[k] = make_float2((slot0 + k < task.pad_a) ? X.x : 0.f, (slot0 + k < task.pad_b) ? X.y : 0.f);
+                        }
+                        gM = gI = zero2();
+                        gD = make_float2((slot0 - 1 < task.pad_a) ? X.x : 0.f, (slot0 - 1 < task.pad_b) ? X.y : 0.f);
+                        if (lane == 0 && strip == 0) bnd = X;
+                        acc = zero2();
                     }
-                    gM = gI = zero2();
-                    gD = make_float2((strip == 0 && lane * K - 1 < task.pad_a) ? X.x : 0.f,
-                                     (strip == 0 && lane * K - 1 < task.pad_b) ? X.y : 0.f);
-                    if (lane == 0 && strip == 0) bnd = X;
-                    acc = zero2();
                 }
                 // lane 0 takes the row-0 boundary (strip 0) or the previous strip's last row instead
                 if (MULTI && strip > 0) {
@@ -252,19 +268,42 @@ __global__ void __launch_bounds__(128) fp32_bucket_kernel(DevTables T, DevBatch 
                 gD = uD;
                 if (last_strip) {
                     acc = add2(acc, add2(Mp[K - 1], Ip[K - 1]));
-                    if (lane == 31 && (code & kColLast)) {
-                        emit_fp32(B, acc.x, ra, hap, out_a + hap);
-                        if (rb >= 0) emit_fp32(B, acc.y, rb, hap, out_b + hap);
+                    if constexpr (CHK) {
+                        if (lane == 31 && (code & kColLast)) {
+                            emit_fp32(B, acc.x, ra, hap, out_a + hap);
+                            if (rb >= 0) emit_fp32(B, acc.y, rb, hap, out_b + hap);
+                        }
                     }
                 } else if (MULTI && lane == 31 && valid) {
                     scratch[3 * c + 0] = Mp[K - 1];
                     scratch[3 * c + 1] = Ip[K - 1];
                     scratch[3 * c + 2] = Dp[K - 1];
                 }
+            };
+            // haplotype boundaries of this task: columns hb(j) = hap_off[hap_begin + j] - col0, hb(n) = ncols
+            const int64_t *hoff = B.hap_off + task.hap_begin;
+            const int nh_task = task.hap_end - task.hap_begin;
+            int s = 0, j = 0;
+            while (s < nsteps) {
+                while (j <= nh_task && (int)(hoff[j] - col0) <= s) ++j;
+                const int window_end = min((int)(hoff[j - 1] - col0) + 32, nsteps);
+                if (s < window_end) {
+                    for (; s < window_end; ++s) step(s, std::true_type{});
+                    continue;
+                }
+                const int next_boundary = (j <= nh_task) ? (int)(hoff[j] - col0) : nsteps;
+                for (; s < next_boundary; ++s) step(s, std::false_type{});
             }
             if (MULTI) __syncwarp();
         }
     }
+}
+
+// Final log10 un-scaling of the FP32 pass, in FP64: out = log10(sum) - log10(2^120).  Runs before the FP64
+// queue kernel, which then overwrites the pairs it recomputes (their slots hold no accepted sum).
+__global__ void finalize_fp32_kernel(double *out, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = log10(out[i]) - kLog10Scale32;
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -613,6 +652,12 @@ int fp32_kernel_occupancy(int k, int block, int *blocks_per_sm) {
 
 int launch_fp64_queue(const DevTables &t, const DevBatch &b, int grid, int block, cudaStream_t s) {
     fp64_queue_kernel<kMaxK64><<<grid, block, 0, s>>>(t, b);
+    return (int)cudaGetLastError();
+}
+
+int launch_finalize_fp32(double *out, int64_t n, int sm_count, cudaStream_t s) {
+    if (n <= 0) return 0;
+    finalize_fp32_kernel<<<sm_count * 4, 256, 0, s>>>(out, n);
     return (int)cudaGetLastError();
 }
 

@@ -32,7 +32,6 @@ constexpr int kBlock = 128;
 constexpr int kWarpsPerBlock = kBlock / 32;
 constexpr int kCounterBase = 8;  // counters[8 + bucket] are per-bucket task cursors
 constexpr int kNumCounters = 64;
-constexpr int kChunkCols = 16384;  // haplotype columns per FP32 task (MULTI tasks: scratch bound)
 
 uint8_t base_code(uint8_t b) {
     switch (b) {
@@ -186,6 +185,7 @@ struct ghmm_ctx {
     void *table_mem = nullptr;
     std::string last_error;
     ghmm_batch scratch_batch;  // reused by the one-shot entry points
+    int max_k = kMaxK32, max_k_multi = kMaxK32, chunk_cols = 16384;
     bool alive = false;
 };
 
@@ -402,17 +402,22 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
         if (h1 == h0 || r1 == r0) continue;
         bool region_fp64 = false;
         for (int64_t h = h0; h < h1; h++) region_fp64 |= (hap_flag[(size_t)h] != 0);
-        std::vector<std::pair<int, int64_t>> groups;  // (key, read)
+        std::vector<std::pair<int64_t, int64_t>> groups;  // ((key, strips, length), read)
         for (int64_t r = r0; r < r1; r++) {
             const int R = (int)(read_off[(size_t)r + 1] - read_off[(size_t)r]);
             if (region_fp64 || (read_flag[(size_t)r] & 1)) {
                 for (int64_t h = h0; h < h1; h++) direct.push_back(PairRef{(int32_t)r, (int32_t)h});
                 continue;
             }
-            int key;
-            if (R <= 32 * kMaxK32) key = (R + 31) / 32;
-            else key = kMaxK32 | 16;
-            groups.emplace_back(key * 100000 + R, r);
+            int key, ns = 1;
+            if (R <= 32 * ctx->max_k) {
+                key = (R + 31) / 32;
+            } else {  // fewest strips of at most max_k_multi rows per lane, then the fewest rows per lane
+                ns = (R + 32 * ctx->max_k_multi - 1) / (32 * ctx->max_k_multi);
+                key = ((R + 32 * ns - 1) / (32 * ns)) | 16;
+            }
+            // reads are paired only within one (rows per lane, strip count) class
+            groups.emplace_back(((int64_t)key * 4096 + ns) * 100000 + R, r);
         }
         std::sort(groups.begin(), groups.end());
         // haplotype chunks
@@ -421,7 +426,7 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
             int64_t a = h0;
             while (a < h1) {
                 int64_t e = a + 1, cols = hap_off[(size_t)a + 1] - hap_off[(size_t)a];
-                while (e < h1 && cols + (hap_off[(size_t)e + 1] - hap_off[(size_t)e]) <= kChunkCols) {
+                while (e < h1 && cols + (hap_off[(size_t)e + 1] - hap_off[(size_t)e]) <= ctx->chunk_cols) {
                     cols += hap_off[(size_t)e + 1] - hap_off[(size_t)e];
                     e++;
                 }
@@ -430,10 +435,11 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
             }
         }
         for (size_t i = 0; i < groups.size();) {
-            const int key = groups[i].first / 100000;
+            const int64_t cls = groups[i].first / 100000;
+            const int key = (int)(cls / 4096);
             const int64_t ra = groups[i].second;
             int64_t rb = -1;
-            if (i + 1 < groups.size() && groups[i + 1].first / 100000 == key) rb = groups[i + 1].second;
+            if (i + 1 < groups.size() && groups[i + 1].first / 100000 == cls) rb = groups[i + 1].second;
             i += (rb >= 0) ? 2 : 1;
             const int K = key & 15;
             const bool multi = (key & 16) != 0;
@@ -633,6 +639,11 @@ static int batch_forward(ghmm_ctx *ctx, ghmm_batch &b, int mode) {
             b.last_launches++;
         }
     }
+    if (mode == GHMM_MODE_FP32_RERUN && b.n_tasks > 0) {
+        int e = launch_finalize_fp32(b.dev.out, b.n_out, ctx->sm_count, s);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "FP32 finalize launch");
+        b.last_launches++;
+    }
     GHMM_CUDA(cudaEventRecord(ev[3], s), "event");
     {
         int e = launch_fp64_queue(ctx->tables, b.dev, b.fp64_grid, kBlock, s);
@@ -750,6 +761,20 @@ int ghmm_initialize(const ghmm_args *args, ghmm_ctx **out) {
     ctx->tables.m2m_d = dt->m2m;
     ctx->alive = true;
     *out = ctx;
+    return GHMM_OK;
+}
+
+int ghmm_set_tuning(ghmm_ctx *ctx, const ghmm_tuning *t) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!t) return fail(ctx, GHMM_ERR_ARG, "NULL tuning");
+    const int mk = t->max_rows_per_lane ? t->max_rows_per_lane : kMaxK32;
+    const int mm = t->max_rows_per_lane_multi ? t->max_rows_per_lane_multi : kMaxK32;
+    const int cc = t->chunk_cols ? t->chunk_cols : 16384;
+    if (mk < 1 || mk > kMaxK32 || mm < 1 || mm > kMaxK32 || cc < 1)
+        return fail(ctx, GHMM_ERR_ARG, "tuning out of range (rows per lane 1..8, chunk_cols >= 1)");
+    ctx->max_k = mk;
+    ctx->max_k_multi = mm;
+    ctx->chunk_cols = cc;
     return GHMM_OK;
 }
 

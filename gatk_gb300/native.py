@@ -44,6 +44,11 @@ class Args(ctypes.Structure):
                 ("use_double_precision", ctypes.c_int32), ("flags", ctypes.c_int32)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("max_rows_per_lane", ctypes.c_int32), ("max_rows_per_lane_multi", ctypes.c_int32),
+                ("chunk_cols", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class Read(ctypes.Structure):
     _fields_ = [("bases", _u8p), ("quals", _u8p), ("ins_gop", _u8p), ("del_gop", _u8p), ("gcp", _u8p),
                 ("length", ctypes.c_int32)]
@@ -99,6 +104,7 @@ _SIGS = {
     "ghmm_compute_likelihoods": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Read), ctypes.c_int32,
                                                 ctypes.POINTER(Hap), ctypes.c_int32, _f64p]),
     "ghmm_done": (ctypes.c_int, [ctypes.c_void_p]),
+    "ghmm_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
     "ghmm_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
     "ghmm_compute_regions": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Region), ctypes.c_int32, _f64p]),
     "ghmm_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Region), ctypes.c_int32,

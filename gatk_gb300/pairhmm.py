@@ -159,6 +159,11 @@ class Engine:
         native.check(rc, self._ctx.h)
         return out
 
+    def set_tuning(self, max_rows_per_lane: int = 0, max_rows_per_lane_multi: int = 0, chunk_cols: int = 0):
+        """FP32 launch shape for batches created afterwards (0 keeps a field's default)."""
+        t = native.Tuning(max_rows_per_lane, max_rows_per_lane_multi, chunk_cols, 0)
+        native.check(self.L.ghmm_set_tuning(self._ctx.h, ctypes.byref(t)), self._ctx.h)
+
     def batch(self, wl: Workload, via_regions: bool = False) -> "Batch":
         return Batch(self, wl, via_regions)
 

@@ -122,6 +122,17 @@ typedef struct ghmm_stats {
     int64_t d2h_bytes;        /* device-to-host bytes of the last forward + results */
 } ghmm_stats;
 
+/* Launch-shape choices of the FP32 pass (the autotuner's knobs; the reference has none besides its thread
+ * count).  A read of R bases runs single-strip with ceil(R/32) rows per lane when that is at most
+ * max_rows_per_lane, otherwise as the fewest strips of at most max_rows_per_lane_multi rows per lane.
+ * Zero fields keep their defaults (8, 8, 16384). */
+typedef struct ghmm_tuning {
+    int32_t max_rows_per_lane;       /* 1..8 */
+    int32_t max_rows_per_lane_multi; /* 1..8 */
+    int32_t chunk_cols;              /* haplotype columns per FP32 task, >= 1 */
+    int32_t reserved;
+} ghmm_tuning;
+
 /* PairHMMNativeBinding.load: 1 if a usable GPU (compute capability 10.3) is present, else 0. */
 int ghmm_load(void);
 
@@ -131,6 +142,9 @@ int ghmm_initialize(const ghmm_args *args, ghmm_ctx **ctx);
 /* PairHMMNativeBinding.computeLikelihoods: out[r * n_haps + h] for one region (read-major). */
 int ghmm_compute_likelihoods(ghmm_ctx *ctx, const ghmm_read *reads, int32_t n_reads, const ghmm_hap *haps,
                              int32_t n_haps, double *out);
+
+/* Set the FP32 launch shape used by batches created after this call (see ghmm_tuning). */
+int ghmm_set_tuning(ghmm_ctx *ctx, const ghmm_tuning *tuning);
 
 /* PairHMMNativeBinding.done: release the context. */
 int ghmm_done(ghmm_ctx *ctx);

@@ -146,6 +146,36 @@ def test_strip_and_bucket_boundaries(engine):
     assert _absdiff(got[under], ref[under]).max() <= TOL64
 
 
+@pytest.mark.parametrize("tuning", [(8, 8), (6, 4), (4, 2), (2, 1), (5, 3)])
+def test_tunings_agree_with_oracle(tuning):
+    # every launch shape (rows per lane, strips) gives the same results; reads of one region cover
+    # several strip counts so pairs of reads with different strip counts would be exposed
+    rng = np.random.default_rng(29)
+    regions = []
+    for _ in range(3):
+        H = int(rng.integers(150, 400))
+        base = _rand_seq(rng, H)
+        haps = [base, base[:H // 2] + b"T" + base[H // 2 + 1:], _rand_seq(rng, H - 7)]
+        reads = []
+        for R in (100, 130, 161, 190, 200, 229, 250, 257, 300):
+            start = int(rng.integers(0, max(1, H - R)))
+            rd = (base[start:start + R] + _rand_seq(rng, R))[:R]
+            reads.append((rd, rng.integers(20, 41, size=R), np.full(R, 45), np.full(R, 45), np.full(R, 10)))
+        regions.append((haps, reads))
+    wl = W.from_pairs(regions)
+    ref = _oracle_all(wl)
+    e = Engine()
+    try:
+        e.set_tuning(*tuning)
+        got, _ = _run(e, wl, native.MODE_FP32_RERUN)
+    finally:
+        e.close()
+    under = ref < RERUN_LOG10 - 0.01
+    assert _absdiff(got[~under], ref[~under]).max() <= TOL32
+    if under.any():
+        assert _absdiff(got[under], ref[under]).max() <= TOL64
+
+
 def test_reads_longer_than_haplotypes_across_haplotype_boundaries(engine):
     # Every haplotype but the last hands the wavefront to the next one mid-warp; reads longer than the
     # haplotypes make the insertion chain at each haplotype's last column dominate the likelihood.
