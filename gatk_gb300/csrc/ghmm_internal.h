@@ -7,7 +7,7 @@
 namespace ghmm {
 
 // Column-stream byte of a haplotype base (one per haplotype column, haplotypes of a region back to
-// back): bits 0-3 base mask (A=1 C=2 G=4 T=8 N=15), bit 6 first column of a haplotype, bit 7 last.
+// back): bits 0-2 base index (A=0 C=1 G=2 T=3 N=4), bit 6 first column of a haplotype, bit 7 last.
 constexpr uint8_t kColFirst = 0x40;
 constexpr uint8_t kColLast = 0x80;
 constexpr int kMaxK32 = 8;      // FP32 kernel: rows per lane (strip = 32*K rows)

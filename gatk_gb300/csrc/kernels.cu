@@ -62,6 +62,11 @@ __device__ __forceinline__ uint32_t base_code(uint8_t b) {
     }
 }
 
+// Haplotype column codes carry a base index (A, C, G, T, N = 0..4); a read base matches index h when its
+// mask shares a bit with kBaseMask[h] (N matches everything).
+constexpr int kBases = 5;
+__device__ __constant__ uint32_t kBaseMask[kBases] = {1u, 2u, 4u, 8u, 15u};
+
 // Per-row coefficients of one read half (see header comment); dummy rows reproduce the row-0 boundary.
 struct RowCoef {
     float pm, pe, mm, mi, ii, md, dd;
@@ -111,11 +116,21 @@ __device__ __forceinline__ void emit_fp32(const DevBatch &B, float sum, int read
 
 }  // namespace
 
+// Blocks of 128 threads the FP32 kernel asks ptxas to fit per SM (register budget 65536 / (128 * n)).
+template <int K>
+struct Fp32MinBlocks {
+    static constexpr int value = K >= 5 ? 3 : 4;
+};
+
 template <int K, bool MULTI>
-__global__ void __launch_bounds__(128) fp32_bucket_kernel(DevTables T, DevBatch B, int task_begin, int task_count,
-                                                          int counter_slot) {
+__global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value)
+    fp32_bucket_kernel(DevTables T, DevBatch B, int task_begin, int task_count, int counter_slot) {
     constexpr int S = 32 * K;
     const int lane = threadIdx.x & 31;
+    // Per-warp prior table in shared memory: prior[k][base][lane] as (read A, read B), base index
+    // A,C,G,T,N = 0..4.  One 64-bit load per row and step replaces two compares and two selects.
+    extern __shared__ float2 prior_smem[];
+    float2 *prior_tbl = prior_smem + (size_t)(threadIdx.x >> 5) * (K * kBases * 32) + lane;
     const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     float2 *scratch = nullptr;
     if (MULTI) scratch = B.scratch32 + warp_global * B.scratch32_cols * 3;
@@ -151,22 +166,26 @@ __global__ void __launch_bounds__(128) fp32_bucket_kernel(DevTables T, DevBatch 
         const int nstrips = MULTI ? task.nstrips : 1;
 
         for (int strip = 0; strip < nstrips; ++strip) {
-            float2 pm[K], pe[K], cmm[K], cmi[K], cii[K], cmd[K], cdd[K];
-            uint32_t rc[K];
+            float2 cmm[K], cmi[K], cii[K], cmd[K], cdd[K];
+            __syncwarp();  // the previous strip's steps have finished reading this warp's table
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 const int slot = strip * S + lane * K + k;
                 const RowCoef a = row_coef(T, B, off_a, len_a, slot - task.pad_a);
                 const RowCoef b = row_coef(T, B, off_b, rb >= 0 ? len_b : 0, slot - task.pad_b);
-                pm[k] = make_float2(a.pm, b.pm);
-                pe[k] = make_float2(a.pe, b.pe);
                 cmm[k] = make_float2(a.mm, b.mm);
                 cmi[k] = make_float2(a.mi, b.mi);
                 cii[k] = make_float2(a.ii, b.ii);
                 cmd[k] = make_float2(a.md, b.md);
                 cdd[k] = make_float2(a.dd, b.dd);
-                rc[k] = a.code | (b.code << 8);
+#pragma unroll
+                for (int h = 0; h < kBases; ++h) {
+                    const uint32_t hm = kBaseMask[h];
+                    prior_tbl[(k * kBases + h) * 32] =
+                        make_float2((a.code & hm) ? a.pm : a.pe, (b.code & hm) ? b.pm : b.pe);
+                }
             }
+            __syncwarp();
             float2 Mp[K], Ip[K], Dp[K];
 #pragma unroll
             for (int k = 0; k < K; ++k) Mp[k] = Ip[k] = Dp[k] = zero2();
@@ -238,17 +257,14 @@ __global__ void __launch_bounds__(128) fp32_bucket_kernel(DevTables T, DevBatch 
                     uI = mul2(uI, nl0);
                     uD = fma2(uD, nl0, bnd);
                 }
-                const uint32_t hc2 = (code & 15u) * 0x0101u;
+                const float2 *pri = prior_tbl + (code & 7u) * 32;
                 // pass 1 (bottom-up so the row above is still the previous column): M and D^
 #pragma unroll
                 for (int k = K - 1; k >= 0; --k) {
                     const float2 dM = k ? Mp[k - 1] : gM;
                     const float2 dI = k ? Ip[k - 1] : gI;
                     const float2 dD = k ? Dp[k - 1] : gD;
-                    const uint32_t m = rc[k] & hc2;
-                    float2 pr;
-                    pr.x = (m & 0x00ffu) ? pm[k].x : pe[k].x;
-                    pr.y = (m & 0xff00u) ? pm[k].y : pe[k].y;
+                    const float2 pr = pri[k * kBases * 32];
                     const float2 Mn = mul2(pr, fma2(dM, cmm[k], add2(dI, dD)));
                     const float2 Dn = fma2(Dp[k], cdd[k], mul2(Mp[k], cmd[k]));
                     Mp[k] = Mn;
@@ -596,10 +612,18 @@ __global__ void peak_dfma_kernel(double *out, int iters, double x, double y) {
 }
 
 // ---------------------------------------------------------------------------------------------------
+static size_t fp32_smem_bytes(int k, int block) { return (size_t)(block / 32) * k * kBases * 32 * sizeof(float2); }
+
 template <int K, bool MULTI>
 static int launch_fp32_k(const DevTables &t, const DevBatch &b, int task_begin, int task_count, int grid, int block,
                          int slot, cudaStream_t s) {
-    fp32_bucket_kernel<K, MULTI><<<grid, block, 0, s>>>(t, b, task_begin, task_count, slot);
+    const size_t smem = fp32_smem_bytes(K, block);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(fp32_bucket_kernel<K, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return (int)e;
+    }
+    fp32_bucket_kernel<K, MULTI><<<grid, block, smem, s>>>(t, b, task_begin, task_count, slot);
     return (int)cudaGetLastError();
 }
 
@@ -632,8 +656,10 @@ int fp32_kernel_occupancy(int k, int block, int *blocks_per_sm) {
     switch (k & 15) {
 #define GHMM_OCC(KK)                                                                                              \
     case KK:                                                                                                      \
-        e = multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fp32_bucket_kernel<KK, true>, block, 0) \
-                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fp32_bucket_kernel<KK, false>, block, 0); \
+        e = multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fp32_bucket_kernel<KK, true>, block,  \
+                                                                  fp32_smem_bytes(KK, block))                          \
+                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fp32_bucket_kernel<KK, false>, block, \
+                                                                  fp32_smem_bytes(KK, block));                         \
         break;
         GHMM_OCC(1)
         GHMM_OCC(2)

@@ -44,6 +44,17 @@ uint8_t base_code(uint8_t b) {
     }
 }
 
+// column-code base index of a haplotype byte (A, C, G, T, N = 0..4; anything else routes to FP64)
+uint8_t base_index(uint8_t b) {
+    switch (b) {
+        case 'A': return 0;
+        case 'C': return 1;
+        case 'G': return 2;
+        case 'T': return 3;
+        default: return 4;
+    }
+}
+
 template <typename T>
 struct DevBuf {
     T *p = nullptr;
@@ -361,8 +372,9 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
             if (H > 0) memcpy(hraw + ofs, sh, (size_t)H);
             uint8_t fl = (H == 0) ? 1 : 0;
             for (int j = 0; j < H; j++) {
-                uint8_t c = base_code(sh[j]);
-                if (c == 0) fl |= 1;
+                const uint8_t m = base_code(sh[j]);
+                if (m == 0) fl |= 1;
+                uint8_t c = base_index(sh[j]);
                 if (j == 0) c |= kColFirst;
                 if (j == H - 1) c |= kColLast;
                 hcode[ofs + j] = c;
