@@ -15,11 +15,17 @@
 //    rows; at step s it computes column c = s - l, receiving the row above from lane l-1 by __shfl_up_sync
 //    (an anti-diagonal wavefront).  Reads are padded at the top with "dummy" rows that reproduce the row-0
 //    boundary, so the last read row always sits in lane 31's last slot.  Reads longer than 32*K rows run
-//    as several strips whose boundary row goes through per-warp global scratch.  Rows are pre-scaled so a
-//    cell costs 7 FMA-pipe operations instead of 8:  I^ = I*IM_{i+1},  D^ = D*IM_{i+1}  (IM_{R+1} = 1):
-//       M  = prior * fma(M_diag, MM, I^_diag + D^_diag)
-//       I^ = fma(I^_up, II*IM_{i+1}/IM_i, M_up * MI*IM_{i+1})
-//       D^ = fma(D^_left, DD, M_left * MD*IM_{i+1})
+//    as several strips whose boundary row goes through per-warp global scratch.  Each row's states are
+//    rescaled so a cell costs 5 FMA-pipe operations instead of 8: with a_0 = 1, a_i = a_{i-1} / MM_i,
+//       M~ = a_i M,   I~ = (a_{i-1} / MI_i) I,   D~ = (a_i / MD_i) D,
+//    the recurrence becomes
+//       M~ = prior * fma(I~_diag, b_i, fma(D~_diag, c_i, M~_diag))
+//       I~ = fma(I~_up, e_i, M~_up)
+//       D~ = fma(D~_left, DD_i, M~_left)
+//    with b_i = IM_i MI_{i-1} / (MM_i MM_{i-1}), c_i = IM_i MD_{i-1} / MM_i, e_i = II_i MI_{i-1} / (MI_i MM_{i-1})
+//    (MM_0 = MI_0 = MD_0 = 1) and  M_R + I_R = (M~_R + I~_R MI_R / MM_R) / a_R.  Only ratios of adjacent rows'
+//    coefficients appear; log2 a_R is summed per read.  Reads whose I~ could outgrow FP32 (steeply rising
+//    insertion penalties) or whose MM is 0 are sent to FP64 by the host.
 //    Scale 2^120; a sum below GHMM_FP32_RERUN_THRESHOLD (or not finite) queues the pair for FP64.
 //  * fp64_queue_kernel<K>: the FP64 wavefront (one pair per warp, scale 2^1020, unscaled rows so any
 //    gap-continuation penalty, including 0, is exact), used for reruns and double-precision mode.
@@ -69,7 +75,7 @@ __device__ __constant__ uint32_t kBaseMask[kBases] = {1u, 2u, 4u, 8u, 15u};
 
 // Per-row coefficients of one read half (see header comment); dummy rows reproduce the row-0 boundary.
 struct RowCoef {
-    float pm, pe, mm, mi, ii, md, dd;
+    float pm, pe, b, c, e, dd, lmm, kappa;
     uint32_t code;
 };
 
@@ -77,32 +83,44 @@ __device__ __forceinline__ RowCoef row_coef(const DevTables &T, const DevBatch &
     RowCoef c;
     if (p < 0 || p >= R) {
         c.pm = c.pe = 0.f;
-        c.mm = c.mi = c.ii = c.md = 0.f;
+        c.b = c.c = c.e = 0.f;
         c.dd = 1.f;
+        c.lmm = c.kappa = 0.f;
         c.code = 0u;
         return c;
     }
     const uint8_t base = B.bases[off + p], q = B.quals[off + p];
     const uint8_t ins = B.ins[off + p], del = B.dels[off + p], gcp = B.gcp[off + p];
-    const float tim = __ldg(T.prob_f + gcp);
-    const float timn = (p + 1 < R) ? __ldg(T.prob_f + B.gcp[off + p + 1]) : 1.f;
+    const float mm = __ldg(T.m2m_f + ins * 128 + del), mi = __ldg(T.err_f + ins), md = __ldg(T.err_f + del);
+    const float im = __ldg(T.prob_f + gcp), ii = __ldg(T.err_f + gcp);
+    float mm_p = 1.f, mi_p = 1.f, md_p = 1.f;
+    if (p > 0) {
+        const uint8_t ins_p = B.ins[off + p - 1], del_p = B.dels[off + p - 1];
+        mm_p = __ldg(T.m2m_f + ins_p * 128 + del_p);
+        mi_p = __ldg(T.err_f + ins_p);
+        md_p = __ldg(T.err_f + del_p);
+    }
     c.pm = __ldg(T.prob_f + q);
     c.pe = (base == 'N') ? c.pm : __ldg(T.err3_f + q);
-    c.mm = __ldg(T.m2m_f + ins * 128 + del);
-    c.mi = __ldg(T.err_f + ins) * timn;
-    c.md = __ldg(T.err_f + del) * timn;
-    const float tii = __ldg(T.err_f + gcp);
-    c.ii = tii * timn / tim;
-    c.dd = tii;
+    c.b = im * mi_p / (mm * mm_p);
+    c.c = im * md_p / mm;
+    c.e = (p > 0) ? ii * mi_p / (mi * mm_p) : 0.f;
+    c.dd = ii;
+    c.lmm = -log2f(mm);
+    c.kappa = mi / mm;
     c.code = base_code(base);
     return c;
 }
 
-// Accepted sums are stored raw (as double); finalize_fp32_kernel turns them into log10 with every lane busy,
-// rather than one lane per warp running the FP64 log10 here on the 1/64-rate FP64 pipe.
-__device__ __forceinline__ void emit_fp32(const DevBatch &B, float sum, int read, int hap, int64_t out_index) {
-    if (sum >= GHMM_FP32_RERUN_THRESHOLD && sum <= FLT_MAX) {
-        B.out[out_index] = (double)sum;
+// log2(GHMM_FP32_RERUN_THRESHOLD) = log2(1e-28)
+constexpr float kLog2Threshold = -93.01398f;
+
+// t = a_R (M_R + I_R) summed over the haplotype (scaled by 2^120), la = log2 a_R.  Accepted sums are stored raw
+// as the float pair (t, la) in the output slot; finalize_fp32_kernel turns them into log10 in FP64 with every lane
+// busy, rather than one lane per warp running the FP64 log10 here on the 1/64-rate FP64 pipe.
+__device__ __forceinline__ void emit_fp32(const DevBatch &B, float t, float la, int read, int hap, int64_t out_index) {
+    if (t > 0.f && t <= FLT_MAX && log2f(t) - la >= kLog2Threshold) {
+        reinterpret_cast<float2 *>(B.out)[out_index] = make_float2(t, la);
     } else {
         const int idx = atomicAdd(&B.counters[1], 1);
         if ((int64_t)idx < B.rerun_capacity) {
@@ -160,24 +178,25 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value)
         const int64_t col0 = B.hap_off[task.hap_begin];
         const int ncols = (int)(B.hap_off[task.hap_end] - col0);
         const uint8_t *stream = B.hap_code + col0;
-        float2 tim1;
-        tim1.x = __ldg(T.prob_f + B.gcp[off_a]);
-        tim1.y = rb >= 0 ? __ldg(T.prob_f + B.gcp[off_b]) : 0.f;
         const int nstrips = MULTI ? task.nstrips : 1;
+        float2 la = zero2();  // log2 a_R of both reads, summed over strips
 
         for (int strip = 0; strip < nstrips; ++strip) {
-            float2 cmm[K], cmi[K], cii[K], cmd[K], cdd[K];
+            float2 cb[K], cc[K], ce[K], cdd[K];
+            float2 kappa = zero2(), lsum = zero2();
             __syncwarp();  // the previous strip's steps have finished reading this warp's table
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 const int slot = strip * S + lane * K + k;
                 const RowCoef a = row_coef(T, B, off_a, len_a, slot - task.pad_a);
                 const RowCoef b = row_coef(T, B, off_b, rb >= 0 ? len_b : 0, slot - task.pad_b);
-                cmm[k] = make_float2(a.mm, b.mm);
-                cmi[k] = make_float2(a.mi, b.mi);
-                cii[k] = make_float2(a.ii, b.ii);
-                cmd[k] = make_float2(a.md, b.md);
+                cb[k] = make_float2(a.b, b.b);
+                cc[k] = make_float2(a.c, b.c);
+                ce[k] = make_float2(a.e, b.e);
                 cdd[k] = make_float2(a.dd, b.dd);
+                lsum.x += a.lmm;
+                lsum.y += b.lmm;
+                if (k == K - 1) kappa = make_float2(a.kappa, b.kappa);
 #pragma unroll
                 for (int h = 0; h < kBases; ++h) {
                     const uint32_t hm = kBaseMask[h];
@@ -185,13 +204,19 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value)
                         make_float2((a.code & hm) ? a.pm : a.pe, (b.code & hm) ? b.pm : b.pe);
                 }
             }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                lsum.x += __shfl_xor_sync(kFull, lsum.x, o);
+                lsum.y += __shfl_xor_sync(kFull, lsum.y, o);
+            }
+            la = add2(la, lsum);
             __syncwarp();
             float2 Mp[K], Ip[K], Dp[K];
 #pragma unroll
             for (int k = 0; k < K; ++k) Mp[k] = Ip[k] = Dp[k] = zero2();
             float2 gM = zero2(), gI = zero2(), gD = zero2();  // row above, previous column (diagonal)
-            float2 bnd = zero2();                               // lane 0, strip 0: row-0 D^ boundary
-            float2 acc = zero2();
+            float2 bnd = zero2();                               // lane 0, strip 0: row-0 D~ boundary
+            float2 accM = zero2(), accI = zero2();
             int hap = task.hap_begin - 1;
             const bool last_strip = (strip == nstrips - 1);
             float2 nxM = zero2(), nxI = zero2(), nxD = zero2();  // prefetched strip boundary (MULTI, lane 0)
@@ -226,7 +251,7 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value)
                     if (code & kColFirst) {
                         ++hap;
                         const float init = __ldg(B.hap_init_f + hap);
-                        const float2 X = make_float2(init * tim1.x, init * tim1.y);
+                        const float2 X = make_float2(init, rb >= 0 ? init : 0.f);
                         // dummy rows (global slot < pad) hold the row-0 value X in D^; a pad may reach past
                         // strip 0 for the shorter read of a pair
                         const int slot0 = strip * S + lane * K;
@@ -238,7 +263,7 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value)
                         gM = gI = zero2();
                         gD = make_float2((slot0 - 1 < task.pad_a) ? X.x : 0.f, (slot0 - 1 < task.pad_b) ? X.y : 0.f);
                         if (lane == 0 && strip == 0) bnd = X;
-                        acc = zero2();
+                        accM = accI = zero2();
                     }
                 }
                 // lane 0 takes the row-0 boundary (strip 0) or the previous strip's last row instead
@@ -265,16 +290,16 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value)
                     const float2 dI = k ? Ip[k - 1] : gI;
                     const float2 dD = k ? Dp[k - 1] : gD;
                     const float2 pr = pri[k * kBases * 32];
-                    const float2 Mn = mul2(pr, fma2(dM, cmm[k], add2(dI, dD)));
-                    const float2 Dn = fma2(Dp[k], cdd[k], mul2(Mp[k], cmd[k]));
+                    const float2 Mn = mul2(pr, fma2(dI, cb[k], fma2(dD, cc[k], dM)));
+                    const float2 Dn = fma2(Dp[k], cdd[k], Mp[k]);
                     Mp[k] = Mn;
                     Dp[k] = Dn;
                 }
-                // pass 2 (top-down): I^ from the row above at this column
+                // pass 2 (top-down): I~ from the row above at this column
                 float2 aM = uM, aI = uI;
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
-                    const float2 In = fma2(aI, cii[k], mul2(aM, cmi[k]));
+                    const float2 In = fma2(aI, ce[k], aM);
                     Ip[k] = In;
                     aM = Mp[k];
                     aI = In;
@@ -283,11 +308,13 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value)
                 gI = uI;
                 gD = uD;
                 if (last_strip) {
-                    acc = add2(acc, add2(Mp[K - 1], Ip[K - 1]));
+                    accM = add2(accM, Mp[K - 1]);
+                    accI = add2(accI, Ip[K - 1]);
                     if constexpr (CHK) {
                         if (lane == 31 && (code & kColLast)) {
-                            emit_fp32(B, acc.x, ra, hap, out_a + hap);
-                            if (rb >= 0) emit_fp32(B, acc.y, rb, hap, out_b + hap);
+                            const float2 t = fma2(kappa, accI, accM);
+                            emit_fp32(B, t.x, la.x, ra, hap, out_a + hap);
+                            if (rb >= 0) emit_fp32(B, t.y, la.y, rb, hap, out_b + hap);
                         }
                     }
                 } else if (MULTI && lane == 31 && valid) {
@@ -315,11 +342,14 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value)
     }
 }
 
-// Final log10 un-scaling of the FP32 pass, in FP64: out = log10(sum) - log10(2^120).  Runs before the FP64
+// Final log10 un-scaling of the FP32 pass, in FP64: out = log10(t) - log10(a_R) - log10(2^120).  Runs before the FP64
 // queue kernel, which then overwrites the pairs it recomputes (their slots hold no accepted sum).
 __global__ void finalize_fp32_kernel(double *out, int64_t n) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = log10(out[i]) - kLog10Scale32;
+    const double log10_2 = 0.30102999566398120;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 v = reinterpret_cast<const float2 *>(out)[i];  // (t, log2 a_R), see emit_fp32
+        out[i] = log10((double)v.x) - (double)v.y * log10_2 - kLog10Scale32;
+    }
 }
 
 // ---------------------------------------------------------------------------------------------------

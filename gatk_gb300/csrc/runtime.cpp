@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -194,6 +195,7 @@ struct ghmm_ctx {
     cudaEvent_t ev[8]{};
     DevTables tables{};
     void *table_mem = nullptr;
+    HostTables *host_tables = nullptr;  // host copy, for routing decisions
     std::string last_error;
     ghmm_batch scratch_batch;  // reused by the one-shot entry points
     int max_k = kMaxK32, max_k_multi = kMaxK32, chunk_cols = 16384;
@@ -323,13 +325,21 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
     std::copy(rho.begin(), rho.end(), o + NR + 1 + NH + 1 + G + 1);
     std::copy(oo.begin(), oo.end(), o + NR + 1 + NH + 1 + 2 * (G + 1));
 
-    // per-read flags: bit0 needs FP64 (gcp 0 or a non-ACGTN base), bit1 invalid quality
+    // per-read flags: bit0 needs FP64, bit1 invalid quality.  FP64 is needed for a gap-continuation
+    // penalty of 0, a non-ACGTN base, a matchToMatch probability of (almost) 0, or when the FP32 kernel's
+    // rescaled insertion state could outgrow FP32 (see kernels.cu: I~ <= G * max M~ with
+    // G_i = 1 + e_i G_{i-1}, and max M~ <= 2^120 / H).
     std::vector<uint8_t> read_flag((size_t)NR, 0), hap_flag((size_t)NH, 0);
     std::vector<int> region_max_read((size_t)G, 0);
+    const HostTables &HT = *ctx->host_tables;
 
     parallel_for(G, threads, [&](int64_t g) {
         int64_t r = rro[(size_t)g];
         int mx = 0;
+        int64_t hmin = INT64_MAX;
+        for (int64_t h = rho[(size_t)g]; h < rho[(size_t)g + 1]; h++)
+            hmin = std::min<int64_t>(hmin, hap_off[(size_t)h + 1] - hap_off[(size_t)h]);
+        const double max_i_scaled = 1e37 * (double)std::max<int64_t>(hmin, 1) / std::ldexp(1.0, 120);
         for (int64_t k = 0; r < rro[(size_t)g + 1]; r++, k++) {
             const int64_t ofs = read_off[(size_t)r];
             const int R = (int)(read_off[(size_t)r + 1] - ofs);
@@ -351,9 +361,21 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                 memcpy(pg + ofs, sg, (size_t)R);
             }
             uint8_t fl = (R == 0) ? 1 : 0;
+            double growth = 1.0;
             for (int i = 0; i < R; i++) {
-                if (sq[i] > kMaxQual || si[i] > 127 || sd[i] > 127 || sg[i] > 127) fl |= 2;
+                if (sq[i] > kMaxQual || si[i] > 127 || sd[i] > 127 || sg[i] > 127) {
+                    fl |= 2;
+                    break;
+                }
                 if (sg[i] == 0 || base_code(sb[i]) == 0) fl |= 1;
+                const double mm = HT.m2m[si[i] * 128 + sd[i]];
+                if (mm < 1e-6) fl |= 1;
+                if (i > 0) {
+                    const double e = HT.err[sg[i]] * HT.err[si[i - 1]] /
+                                     (HT.err[si[i]] * std::max(HT.m2m[si[i - 1] * 128 + sd[i - 1]], 1e-300));
+                    growth = 1.0 + e * growth;
+                    if (growth > max_i_scaled) fl |= 1;
+                }
             }
             read_flag[(size_t)r] = fl;
             b.h_read_region.p[r] = (int32_t)g;
@@ -742,6 +764,7 @@ int ghmm_initialize(const ghmm_args *args, ghmm_ctx **out) {
     ctx->double_precision = a.use_double_precision != 0;
     auto bail = [&](cudaError_t e, const char *what) {
         set_init_error(std::string(what) + ": " + cudaGetErrorString(e));
+        delete ctx->host_tables;
         delete ctx;
         return e == cudaErrorMemoryAllocation ? GHMM_ERR_NOMEM : GHMM_ERR_CUDA;
     };
@@ -760,7 +783,7 @@ int ghmm_initialize(const ghmm_args *args, ghmm_ctx **out) {
         return bail(e, "cudaMalloc tables");
     }
     e = cudaMemcpy(ctx->table_mem, ht, bytes, cudaMemcpyHostToDevice);
-    delete ht;
+    ctx->host_tables = ht;
     if (e != cudaSuccess) return bail(e, "upload tables");
     const HostTables *dt = (const HostTables *)ctx->table_mem;
     ctx->tables.err_f = dt->err_f;
@@ -796,6 +819,7 @@ int ghmm_done(ghmm_ctx *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     ctx->scratch_batch.release();
     if (ctx->table_mem) cudaFree(ctx->table_mem);
+    delete ctx->host_tables;
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

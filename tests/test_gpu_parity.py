@@ -218,6 +218,34 @@ def test_odd_reads_short_haps_and_long_reads(engine):
         assert _absdiff(got[under], ref[under]).max() <= TOL64
 
 
+def test_known_answer_cases_with_anchored_penalties(engine):
+    # PairHMMUnitTest.java:148-199 cases: penalties of 100 everywhere except at the indel, so insertion
+    # penalties rise steeply between neighbouring positions (the FP32 kernel's rescaled insertion state is
+    # bounded on the host and such reads go to FP64 when the bound could exceed FP32's range)
+    ctx = b"ACGTAATGACGATTGCA"
+    regions = []
+    for bq, iq, gcp in ((10, 20, 8), (30, 40, 10), (50, 50, 20)):
+        for size in (2, 5, 10, 35):
+            for ins in (True, False):
+                small, big = b"A", b"A" * size
+                ref, read = (small, big) if ins else (big, small)
+                hap = ctx + ref + ctx
+                rd = ctx + read + ctx
+                n = len(rd)
+                q = np.full(n, 100, dtype=np.uint8)
+                q[len(ctx):len(ctx) + len(read)] = bq
+                g = np.full(n, 100, dtype=np.uint8)
+                g[len(ctx)] = iq
+                c = np.full(n, 100, dtype=np.uint8)
+                c[len(ctx):len(ctx) + len(read)] = gcp
+                regions.append(([hap], [(rd, q, g, g, c)]))
+    wl = W.from_pairs(regions)
+    ref = _oracle_all(wl)
+    got, st = _run(engine, wl, native.MODE_FP32_RERUN)
+    assert np.isfinite(got).all()
+    assert _absdiff(got, ref).max() <= TOL32
+
+
 def test_special_bytes_route_to_fp64(engine):
     # N bases, gap continuation 0 and non-ACGTN bytes: results are exact FP64
     rng = np.random.default_rng(3)
