@@ -4,6 +4,8 @@
 
 #include <cstdint>
 
+#include "../../include/ghmm_calib.h"
+
 namespace ghmm {
 
 // Column-stream byte of a haplotype base (one per haplotype column, haplotypes of a region back to
@@ -80,6 +82,13 @@ constexpr int kPlainMaxRead = 1024;
 int fp32_kernel_occupancy(int k, int block, int *blocks_per_sm);
 int fp64_kernel_occupancy(int block, int *blocks_per_sm);
 int measure_peaks_device(int sm_count, double *fp32, double *fp32x2, double *fp64, cudaStream_t s);
+// Calibration forward/backward (calib.cu).
+int64_t calib_scratch_per_warp(int k, int max_hap_len, bool fp64);
+int calib_grid(int sm_count);
+int calib_block();
+int launch_calib(const DevTables &TB, const ghmm_calib_batch &in, int k, bool backward, bool fp64, void *scratch,
+                 int64_t scratch_bytes_per_warp, double *loglik, const double *weights, float *grad_open,
+                 float *grad_cont, int *need_fp64, int sm_count, cudaStream_t s);
 // Message returned by ghmm_last_error(NULL, ...) (runtime.cpp).
 void set_global_error(const char *msg);
 

@@ -199,6 +199,10 @@ struct ghmm_ctx {
     std::string last_error;
     ghmm_batch scratch_batch;  // reused by the one-shot entry points
     int max_k = kMaxK32, max_k_multi = kMaxK32, chunk_cols = 16384;
+    // calibration scratch (checkpointed fronts per resident warp), FP64-redo flags, unit weights
+    DevBuf<uint8_t> calib_scratch;
+    DevBuf<int> calib_flags;
+    DevBuf<double> calib_ones;
     bool alive = false;
 };
 
@@ -799,6 +803,51 @@ int ghmm_initialize(const ghmm_args *args, ghmm_ctx **out) {
     return GHMM_OK;
 }
 
+// Calibration forward (+ backward): FP32 pass over every pair, then an FP64 pass over the pairs it flagged
+// (precision 0), or an FP64 pass over every pair (precision 1).
+static int calib_run(ghmm_ctx *ctx, const ghmm_calib_batch *in, int precision, const double *weights, double *loglik,
+                     float *gopen, float *gcont, bool backward) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!in || !loglik || (backward && (!gopen || !gcont))) return fail(ctx, GHMM_ERR_ARG, "NULL argument");
+    if (precision < 0 || precision > 1) return fail(ctx, GHMM_ERR_ARG, "precision must be 0 (FP32 + FP64 redo) or 1 (FP64)");
+    if (in->n_pairs < 0) return fail(ctx, GHMM_ERR_ARG, "negative pair count");
+    if (in->n_pairs == 0) return GHMM_OK;
+    if (in->max_read_len < 1 || in->max_read_len > 256)
+        return fail(ctx, GHMM_ERR_ARG, "calibration supports reads of 1..256 bases (max_read_len)");
+    if (in->max_hap_len < 1) return fail(ctx, GHMM_ERR_ARG, "max_hap_len must be >= 1");
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const int k = (in->max_read_len + 31) / 32;
+    const int64_t per_warp = calib_scratch_per_warp(k, in->max_hap_len, true);  // sized for the FP64 pass
+    const int64_t warps = (int64_t)calib_grid(ctx->sm_count) * calib_block() / 32;
+    if (backward) GHMM_CUDA(ctx->calib_scratch.reserve((size_t)(per_warp * warps)), "calibration scratch");
+    GHMM_CUDA(ctx->calib_flags.reserve((size_t)in->n_pairs), "calibration flags");
+    cudaStream_t s = ctx->stream;
+    if (backward && !weights) {
+        GHMM_CUDA(ctx->calib_ones.reserve((size_t)in->n_pairs), "calibration weights");
+        std::vector<double> ones((size_t)in->n_pairs, 1.0);
+        GHMM_CUDA(cudaMemcpyAsync(ctx->calib_ones.p, ones.data(), ones.size() * 8, cudaMemcpyHostToDevice, s), "H2D weights");
+        GHMM_CUDA(cudaStreamSynchronize(s), "H2D weights");
+        weights = ctx->calib_ones.p;
+    }
+    GHMM_CUDA(cudaMemsetAsync(ctx->calib_flags.p, 0, (size_t)in->n_pairs * sizeof(int), s), "clear flags");
+    int *flags = ctx->calib_flags.p;
+    if (precision == 1) {  // flag every pair so the FP64 pass takes all of them
+        std::vector<int> all((size_t)in->n_pairs, 1);
+        GHMM_CUDA(cudaMemcpyAsync(flags, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice, s), "H2D flags");
+        GHMM_CUDA(cudaStreamSynchronize(s), "H2D flags");
+    } else {
+        int e = launch_calib(ctx->tables, *in, k, backward, false, ctx->calib_scratch.p,
+                             calib_scratch_per_warp(k, in->max_hap_len, false), loglik, weights, gopen, gcont, flags,
+                             ctx->sm_count, s);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "calibration FP32 launch");
+    }
+    int e = launch_calib(ctx->tables, *in, k, backward, true, ctx->calib_scratch.p, per_warp, loglik, weights, gopen,
+                         gcont, flags, ctx->sm_count, s);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "calibration FP64 launch");
+    GHMM_CUDA(cudaStreamSynchronize(s), "calibration kernels");
+    return GHMM_OK;
+}
+
 int ghmm_set_tuning(ghmm_ctx *ctx, const ghmm_tuning *t) {
     if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
     if (!t) return fail(ctx, GHMM_ERR_ARG, "NULL tuning");
@@ -818,6 +867,9 @@ int ghmm_done(ghmm_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     ctx->scratch_batch.release();
+    ctx->calib_scratch.release();
+    ctx->calib_flags.release();
+    ctx->calib_ones.release();
     if (ctx->table_mem) cudaFree(ctx->table_mem);
     delete ctx->host_tables;
     for (auto &ev : ctx->ev)
@@ -960,6 +1012,15 @@ int ghmm_compute_flat(ghmm_ctx *ctx, const ghmm_flat *flat, double *out) {
 }
 
 void *ghmm_stream(ghmm_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int ghmm_calib_forward(ghmm_ctx *ctx, const ghmm_calib_batch *batch, int32_t precision, double *d_loglik) {
+    return calib_run(ctx, batch, precision, nullptr, d_loglik, nullptr, nullptr, false);
+}
+
+int ghmm_calib_backward(ghmm_ctx *ctx, const ghmm_calib_batch *batch, int32_t precision, const double *d_weights,
+                        double *d_loglik, float *d_grad_open, float *d_grad_cont) {
+    return calib_run(ctx, batch, precision, d_weights, d_loglik, d_grad_open, d_grad_cont, true);
+}
 
 int ghmm_measure_peaks(ghmm_ctx *ctx, double *fp32, double *fp32x2, double *fp64) {
     if (!ctx || !ctx->alive) return GHMM_ERR_STATE;

@@ -88,6 +88,13 @@ class DevPairs(ctypes.Structure):
 NOALLOC_MAX_HAP_LEN = 2048
 
 
+class CalibBatch(ctypes.Structure):
+    _fields_ = [("bases", ctypes.c_void_p), ("quals", ctypes.c_void_p), ("read_off", ctypes.c_void_p),
+                ("hap_bases", ctypes.c_void_p), ("hap_off", ctypes.c_void_p), ("pair_read", ctypes.c_void_p),
+                ("pair_hap", ctypes.c_void_p), ("gap_open", ctypes.c_void_p), ("gap_cont", ctypes.c_void_p),
+                ("n_pairs", ctypes.c_int64), ("max_read_len", ctypes.c_int32), ("max_hap_len", ctypes.c_int32)]
+
+
 class SynthArrays(ctypes.Structure):
     _fields_ = [("n_regions", ctypes.c_int64), ("n_reads", ctypes.c_int64), ("n_haps", ctypes.c_int64),
                 ("read_bytes", ctypes.c_int64), ("hap_bytes", ctypes.c_int64), ("n_out", ctypes.c_int64),
@@ -124,6 +131,9 @@ _SIGS = {
     "ghmm_synth_view": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SynthArrays)]),
     "ghmm_synth_free": (None, [ctypes.c_void_p]),
     "ghmm_str_analyze": (ctypes.c_int, [_u8p, ctypes.c_int32, ctypes.c_int32, _i32p, _i32p, _i32p]),
+    "ghmm_calib_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CalibBatch), ctypes.c_int32, ctypes.c_void_p]),
+    "ghmm_calib_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CalibBatch), ctypes.c_int32, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "ghmm_forward_pairs_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(DevPairs), ctypes.c_void_p,
                                                   ctypes.c_void_p]),
 }

@@ -1,0 +1,125 @@
+"""Gap-penalty calibration (workload 3: 4,096 read x haplotype pairs around short tandem repeats).
+
+The forward log10 likelihoods and the hand-written backward (calib.cu) are checked against the FP64
+oracle (oracle_grad.c: forward and adjoint gradient over full matrices) and against FP64 central finite
+differences with step 1e-4 computed with the GPU's FP64 forward; the tolerance on the gradient is 1e-3
+relative (scaled by the largest component).
+"""
+import numpy as np
+import pytest
+
+from gatk_gb300 import calibration as C
+from gatk_gb300 import workload as W
+from oracle import oracle as O
+
+
+def test_str_parameter_index_layout():
+    idx = C.str_parameter_index(np.frombuffer(b"ACACACACGTTTTTGA", dtype=np.uint8))
+    assert idx[-1] == -1
+    assert ((idx[:-1] >= 0) & (idx[:-1] < C.MAX_PERIOD * C.MAX_REPEAT)).all()
+    # inside the ACAC... run the best period is 2
+    assert (idx[2:6] // C.MAX_REPEAT == 1).all()
+    # the TTTTT homopolymer: period 1, 5 repeats
+    assert idx[11] == 0 * C.MAX_REPEAT + (5 - 1)
+
+
+def test_default_theta():
+    torch = pytest.importorskip("torch")
+    t = C.default_theta()
+    assert tuple(t.shape) == (8, 20, 2)
+    assert torch.all(t[..., 0] == -4.5)
+    assert abs(float(t[0, 0, 1]) + 1.0) < 1e-6 and abs(float(t[2, 0, 1]) + 0.333) < 1e-6
+
+
+def _oracle_pair(wl, cs, g, c, p, grad=False):
+    pr, ph = wl.pair_index()
+    r, h = int(pr[p]), int(ph[p])
+    a, b = int(wl.read_off[r]), int(wl.read_off[r + 1])
+    args = (wl.hap(h), wl.bases[a:b], wl.quals[a:b], g[a:b].astype(np.float64), c[a:b].astype(np.float64))
+    return O.cont_grad(*args) if grad else O.cont_forward(*args)
+
+
+@pytest.fixture(scope="module")
+def calib():
+    torch = pytest.importorskip("torch")
+    from gatk_gb300.pairhmm import Engine
+
+    e = Engine()
+    wl = W.generate(3)
+    cs = C.CalibrationSet(wl)
+    yield torch, e, wl, cs
+    e.close()
+
+
+@pytest.mark.gpu
+def test_forward_matches_oracle(calib):
+    torch, e, wl, cs = calib
+    theta = C.default_theta()
+    g, c = cs.position_params(theta)
+    ll32 = C.log10_likelihoods(theta, cs, e, precision=0).cpu().numpy()
+    ll64 = C.log10_likelihoods(theta, cs, e, precision=1).cpu().numpy()
+    gn, cn = g.cpu().numpy(), c.cpu().numpy()
+    for p in range(0, cs.n_pairs, 64):
+        ref = _oracle_pair(wl, cs, gn, cn, p)
+        assert abs(ll64[p] - ref) <= 1e-9
+        assert abs(ll32[p] - ref) <= 1e-3
+
+
+@pytest.mark.gpu
+def test_backward_matches_oracle_gradient(calib):
+    torch, e, wl, cs = calib
+    theta = C.default_theta()
+    g, c = cs.position_params(theta)
+    g = g.detach().requires_grad_(True)
+    c = c.detach().requires_grad_(True)
+    fn = C._function() if C._FN is None else C._FN
+    for precision, tol in ((0, 1e-3), (1, 1e-6)):  # gradients are returned as float32
+        g.grad = None
+        c.grad = None
+        ll = fn.apply(g, c, cs, e, precision)
+        ll.sum().backward()
+        gg, gc = g.grad.cpu().numpy(), c.grad.cpu().numpy()
+        gn, cn = g.detach().cpu().numpy(), c.detach().cpu().numpy()
+        pr, _ = wl.pair_index()
+        for p in range(0, cs.n_pairs, 256):  # each read has one pair here, so per-position gradients are per pair
+            _, dg, dc = _oracle_pair(wl, cs, gn, cn, p, grad=True)
+            r = int(pr[p])
+            a, b = int(wl.read_off[r]), int(wl.read_off[r + 1])
+            scale = max(np.abs(dg).max(), np.abs(dc).max())
+            assert np.abs(gg[a:b] - dg).max() <= tol * scale + 1e-9, (p, precision)
+            assert np.abs(gc[a:b] - dc).max() <= tol * scale + 1e-9, (p, precision)
+
+
+@pytest.mark.gpu
+def test_theta_gradient_matches_fp64_central_differences(calib):
+    torch, e, wl, cs = calib
+    theta = C.default_theta().to(cs.device).requires_grad_(True)
+    s = C.log10_likelihoods(theta, cs, e, precision=0).sum()
+    s.backward()
+    grad = theta.grad.detach().cpu().numpy().reshape(-1, 2)
+    # the table entries the reads actually use, most used first
+    used = np.bincount(cs.param_index_np[cs.param_index_np >= 0], minlength=160)
+    order = np.argsort(-used)[:8]
+    h = 1e-4
+    scale = np.abs(grad).max()
+    with torch.no_grad():
+        for k in order:
+            for comp in (0, 1):
+                tp = theta.detach().clone()
+                tm = theta.detach().clone()
+                tp.view(-1, 2)[k, comp] += h
+                tm.view(-1, 2)[k, comp] -= h
+                sp = float(C.log10_likelihoods(tp, cs, e, precision=1).sum())
+                sm = float(C.log10_likelihoods(tm, cs, e, precision=1).sum())
+                # the table is float32: divide by the step actually stored, not by 2h
+                step = float(tp.view(-1, 2)[k, comp].double() - tm.view(-1, 2)[k, comp].double())
+                fd = (sp - sm) / step
+                assert abs(grad[k, comp] - fd) <= 1e-3 * max(abs(fd), 1e-2 * scale), (k, comp, grad[k, comp], fd)
+
+
+@pytest.mark.gpu
+def test_fit_increases_likelihood(calib):
+    torch, e, wl, cs = calib
+    theta, hist = C.fit(cs, e, steps=8, lr=0.05)
+    assert hist[-1] > hist[0]
+    assert torch.isfinite(theta).all()
