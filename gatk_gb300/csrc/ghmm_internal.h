@@ -15,6 +15,9 @@ constexpr uint8_t kColLast = 0x80;
 constexpr int kMaxK32 = 8;      // FP32 kernel: rows per lane (strip = 32*K rows)
 constexpr int kMaxK64 = 4;      // FP64 kernel: rows per lane
 constexpr int kMaxReadLen = 1 << 20;
+constexpr int kNumBucketKeys = 32;       // bucket key = rows per lane (1..8) | 16 for multi-strip
+constexpr int kCounterBucketBase = 8;    // counters[8 + key]: bucket task cursors
+constexpr int kNumCounters = 64;
 constexpr int kMaxHapLen = 1 << 20;
 
 // Device lookup tables (QualityUtils / PairHMMModel restated on the host, uploaded once per context).
@@ -62,7 +65,9 @@ struct DevBatch {
     const F32Task *tasks;
     // FP64 queue: entries [0, n_direct) filled by the host, the rest appended by the FP32 pass
     PairRef *rerun;
-    int32_t *counters;          // [0] FP32 task cursor (per launch), [1] rerun tail, [2] FP64 cursor, [3] error flag
+    int32_t *counters;          // [1] FP64 queue tail, [2] FP64 cursor, [3] error flag, [8 + key] bucket cursors
+    const int32_t *bucket_info; // [key] first task of bucket key, [kNumBucketKeys + key] its task count
+    const int64_t *n_out_dev;   // number of outputs (for the FP64 epilogue)
     int64_t rerun_capacity;
     // strip-boundary scratch of multi-strip FP32 tasks: per resident warp, max_cols float2 x 3
     float2 *scratch32;
@@ -72,10 +77,9 @@ struct DevBatch {
 };
 
 // Kernel launchers (kernels.cu).  All return cudaError_t as int.
-int launch_fp32_bucket(const DevTables &t, const DevBatch &b, int k, int task_begin, int task_count, int grid,
-                       int block, int counter_slot, cudaStream_t s);
+int launch_fp32_bucket(const DevTables &t, const DevBatch &b, int key, int grid, int block, cudaStream_t s);
 int launch_fp64_queue(const DevTables &t, const DevBatch &b, int grid, int block, cudaStream_t s);
-int launch_finalize_fp32(double *out, int64_t n, int sm_count, cudaStream_t s);
+int launch_finalize_fp32(double *out, const int64_t *n_out, int sm_count, cudaStream_t s);
 int launch_plain_region(const DevTables &t, const DevBatch &b, int region, int n_reads, int n_haps, int max_read_len,
                         cudaStream_t s);
 constexpr int kPlainMaxRead = 1024;

@@ -140,9 +140,13 @@ struct Fp32MinBlocks {
     static constexpr int value = K >= 5 ? 3 : 4;
 };
 
+// The bucket's task range and cursor live in device memory (B.bucket_info, B.counters), so the launch
+// arguments do not depend on the batch and a captured CUDA graph can be replayed for every batch.
 template <int K, bool MULTI>
-__global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value)
-    fp32_bucket_kernel(DevTables T, DevBatch B, int task_begin, int task_count, int counter_slot) {
+__global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kernel(DevTables T, DevBatch B) {
+    constexpr int KEY = K | (MULTI ? 16 : 0);
+    const int task_begin = B.bucket_info[KEY], task_count = B.bucket_info[kNumBucketKeys + KEY];
+    const int counter_slot = kCounterBucketBase + KEY;
     constexpr int S = 32 * K;
     const int lane = threadIdx.x & 31;
     // Per-warp prior table in shared memory: prior[k][base][lane] as (read A, read B), base index
@@ -344,7 +348,8 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value)
 
 // Final log10 un-scaling of the FP32 pass, in FP64: out = log10(t) - log10(a_R) - log10(2^120).  Runs before the FP64
 // queue kernel, which then overwrites the pairs it recomputes (their slots hold no accepted sum).
-__global__ void finalize_fp32_kernel(double *out, int64_t n) {
+__global__ void finalize_fp32_kernel(double *out, const int64_t *n_out) {
+    const int64_t n = *n_out;
     const double log10_2 = 0.30102999566398120;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float2 v = reinterpret_cast<const float2 *>(out)[i];  // (t, log2 a_R), see emit_fp32
@@ -645,27 +650,24 @@ __global__ void peak_dfma_kernel(double *out, int iters, double x, double y) {
 static size_t fp32_smem_bytes(int k, int block) { return (size_t)(block / 32) * k * kBases * 32 * sizeof(float2); }
 
 template <int K, bool MULTI>
-static int launch_fp32_k(const DevTables &t, const DevBatch &b, int task_begin, int task_count, int grid, int block,
-                         int slot, cudaStream_t s) {
+static int launch_fp32_k(const DevTables &t, const DevBatch &b, int grid, int block, cudaStream_t s) {
     const size_t smem = fp32_smem_bytes(K, block);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(fp32_bucket_kernel<K, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return (int)e;
     }
-    fp32_bucket_kernel<K, MULTI><<<grid, block, smem, s>>>(t, b, task_begin, task_count, slot);
+    fp32_bucket_kernel<K, MULTI><<<grid, block, smem, s>>>(t, b);
     return (int)cudaGetLastError();
 }
 
-int launch_fp32_bucket(const DevTables &t, const DevBatch &b, int k, int task_begin, int task_count, int grid,
-                       int block, int slot, cudaStream_t s) {
+int launch_fp32_bucket(const DevTables &t, const DevBatch &b, int k, int grid, int block, cudaStream_t s) {
     // k encodes rows per lane in the low 4 bits and the multi-strip flag in bit 4
     const bool multi = (k & 16) != 0;
     switch (k & 15) {
 #define GHMM_CASE(KK)                                                                                   \
     case KK:                                                                                            \
-        return multi ? launch_fp32_k<KK, true>(t, b, task_begin, task_count, grid, block, slot, s)      \
-                     : launch_fp32_k<KK, false>(t, b, task_begin, task_count, grid, block, slot, s);
+        return multi ? launch_fp32_k<KK, true>(t, b, grid, block, s) : launch_fp32_k<KK, false>(t, b, grid, block, s);
         GHMM_CASE(1)
         GHMM_CASE(2)
         GHMM_CASE(3)
@@ -711,9 +713,8 @@ int launch_fp64_queue(const DevTables &t, const DevBatch &b, int grid, int block
     return (int)cudaGetLastError();
 }
 
-int launch_finalize_fp32(double *out, int64_t n, int sm_count, cudaStream_t s) {
-    if (n <= 0) return 0;
-    finalize_fp32_kernel<<<sm_count * 4, 256, 0, s>>>(out, n);
+int launch_finalize_fp32(double *out, const int64_t *n_out, int sm_count, cudaStream_t s) {
+    finalize_fp32_kernel<<<sm_count * 4, 256, 0, s>>>(out, n_out);
     return (int)cudaGetLastError();
 }
 

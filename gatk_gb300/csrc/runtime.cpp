@@ -8,10 +8,14 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <condition_variable>
+#include <deque>
+#include <memory>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -31,8 +35,6 @@ std::string g_init_error;
 
 constexpr int kBlock = 128;
 constexpr int kWarpsPerBlock = kBlock / 32;
-constexpr int kCounterBase = 8;  // counters[8 + bucket] are per-bucket task cursors
-constexpr int kNumCounters = 64;
 
 uint8_t base_code(uint8_t b) {
     switch (b) {
@@ -62,10 +64,12 @@ struct DevBuf {
     size_t cap = 0;
     cudaError_t reserve(size_t n) {
         if (n <= cap && p) return cudaSuccess;
+        // a buffer that has to grow again grows by a quarter more than asked, so that batches of slowly
+        // rising size do not free (and so synchronise the device) every time
+        const size_t want = std::max<size_t>(cap ? std::max(n, cap + cap / 4) : n, 1);
         if (p) cudaFree(p);
         p = nullptr;
         cap = 0;
-        const size_t want = std::max<size_t>(n, 1);
         cudaError_t e = cudaMalloc(&p, want * sizeof(T));
         if (e == cudaSuccess) cap = want;
         return e;
@@ -83,10 +87,10 @@ struct HostBuf {  // pinned
     size_t cap = 0;
     cudaError_t reserve(size_t n) {
         if (n <= cap && p) return cudaSuccess;
+        const size_t want = std::max<size_t>(cap ? std::max(n, cap + cap / 4) : n, 1);
         if (p) cudaFreeHost(p);
         p = nullptr;
         cap = 0;
-        const size_t want = std::max<size_t>(n, 1);
         cudaError_t e = cudaMallocHost(&p, want * sizeof(T));
         if (e == cudaSuccess) cap = want;
         return e;
@@ -104,7 +108,7 @@ int hw_threads(int requested) {
 }
 
 template <typename F>
-void parallel_for(int64_t n, int threads, F f) {
+void parallel_for(int64_t n, int threads, F f, int64_t grain = 64) {
     if (n <= 0) return;
     threads = (int)std::min<int64_t>(threads, n);
     if (threads <= 1) {
@@ -116,9 +120,9 @@ void parallel_for(int64_t n, int threads, F f) {
     for (int t = 0; t < threads; t++)
         pool.emplace_back([&] {
             for (;;) {
-                const int64_t i0 = next.fetch_add(64);
+                const int64_t i0 = next.fetch_add(grain);
                 if (i0 >= n) break;
-                const int64_t i1 = std::min(n, i0 + 64);
+                const int64_t i1 = std::min(n, i0 + grain);
                 for (int64_t i = i0; i < i1; i++) f(i);
             }
         });
@@ -144,7 +148,8 @@ struct ghmm_batch {
     HostBuf<F32Task> h_tasks;
     HostBuf<PairRef> h_direct;
     HostBuf<double> h_out;
-    HostBuf<int32_t> h_counters;
+    HostBuf<int32_t> h_counters;  // [kNumCounters] counters, then [2 * kNumBucketKeys] bucket info
+    HostBuf<int64_t> h_nout;
     // device
     DevBuf<uint8_t> d_planes, d_hap;
     DevBuf<int64_t> d_off;
@@ -154,7 +159,8 @@ struct ghmm_batch {
     DevBuf<F32Task> d_tasks;
     DevBuf<PairRef> d_rerun;
     DevBuf<double> d_out;
-    DevBuf<int32_t> d_counters;
+    DevBuf<int32_t> d_counters;  // same layout as h_counters
+    DevBuf<int64_t> d_nout;
     DevBuf<float2> d_scratch32;
     DevBuf<double> d_scratch64;
     // sizes
@@ -165,6 +171,8 @@ struct ghmm_batch {
     // tasks
     std::vector<Bucket> buckets;
     int64_t n_tasks = 0, n_direct = 0;
+    int64_t cells_direct = 0;  // cells of the pairs sent to FP64 directly
+    double ms_host_copy = 0, ms_host_tasks = 0;  // host time of the last marshal: copy + checks, task building
     int64_t n_direct_fp64mode = 0;
     int64_t scratch32_cols = 0;
     int fp64_grid = 0;
@@ -176,8 +184,25 @@ struct ghmm_batch {
     int64_t upload_bytes = 0, forward_h2d = 0, forward_d2h = 0, results_d2h = 0;
     bool uploaded = false;
     DevBatch dev{};
+    // asynchronous forward: events of the last enqueue, and the captured launch sequence
+    cudaEvent_t ev[5]{};
+    bool events_ready = false;
+    int64_t pending_n_pre = 0;
+    int pending_mode = -1;
+    cudaGraphExec_t graph[2]{};  // captured FP32 phase and FP64 phase
+    std::vector<unsigned char> graph_sig;  // DevBatch bytes, mode, bucket keys and grids the graphs were captured for
 
     void release() {
+        for (auto &g : graph) {
+            if (g) cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+        graph_sig.clear();
+        if (events_ready)
+            for (auto &e : ev) cudaEventDestroy(e);
+        events_ready = false;
+        h_nout.release();
+        d_nout.release();
         h_planes.release(); h_hap.release(); h_off.release(); h_read_region.release(); h_init_f.release();
         h_init_d.release(); h_tasks.release(); h_direct.release(); h_out.release(); h_counters.release();
         d_planes.release(); d_hap.release(); d_off.release(); d_read_region.release(); d_init_f.release();
@@ -203,13 +228,22 @@ struct ghmm_ctx {
     DevBuf<uint8_t> calib_scratch;
     DevBuf<int> calib_flags;
     DevBuf<double> calib_ones;
+    ghmm_queue *pipe = nullptr;      // the queue that pipelines large synchronous calls
+    std::atomic<int> open_queues{0};  // queues of this context not yet destroyed (including pipe)
     bool alive = false;
 };
 
 namespace {
 
+// A queue's worker thread reports into the queue's own message instead of the context's, which belongs to
+// the caller's thread.
+thread_local std::string *t_error_sink = nullptr;
+
 int fail(ghmm_ctx *ctx, int code, const std::string &msg) {
-    if (ctx) ctx->last_error = msg;
+    if (t_error_sink)
+        *t_error_sink = msg;
+    else if (ctx)
+        ctx->last_error = msg;
     return code;
 }
 
@@ -303,6 +337,7 @@ int plan_sizes(ghmm_ctx *ctx, const Source &src, ghmm_batch &b, std::vector<int6
 // -------------------------------------------------------------------------------------------------
 // Marshal inputs into the batch's pinned staging and build tasks.
 static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
+    const auto t_start = std::chrono::steady_clock::now();
     std::vector<int64_t> read_off, hap_off, rro, rho, oo;
     int rc = plan_sizes(ctx, src, b, read_off, hap_off, rro, rho, oo);
     if (rc) return rc;
@@ -316,7 +351,8 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
     GHMM_CUDA(b.h_read_region.reserve((size_t)NR), "pinned read regions");
     GHMM_CUDA(b.h_init_f.reserve((size_t)NH), "pinned init");
     GHMM_CUDA(b.h_init_d.reserve((size_t)NH), "pinned init");
-    GHMM_CUDA(b.h_counters.reserve(kNumCounters), "pinned counters");
+    GHMM_CUDA(b.h_counters.reserve(kNumCounters + 2 * kNumBucketKeys), "pinned counters");
+    GHMM_CUDA(b.h_nout.reserve(1), "pinned output count");
 
     uint8_t *P = b.h_planes.p;
     const int64_t RB = b.read_bytes;
@@ -429,115 +465,157 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
 
     // ---- tasks ----
     // FP32 reads are bucketed by rows per lane K = ceil(R/32) (single strip) or K = 8 with
-    // ceil(R/256) strips, paired within a region and bucket, and split into haplotype chunks.
-    std::vector<std::vector<F32Task>> per_bucket(32);
-    std::vector<std::vector<int64_t>> per_bucket_cost(32);
-    std::vector<PairRef> direct;
-    int64_t max_multi_cols = 0;
-    for (int64_t g = 0; g < G; g++) {
-        const int64_t h0 = rho[(size_t)g], h1 = rho[(size_t)g + 1];
-        const int64_t r0 = rro[(size_t)g], r1 = rro[(size_t)g + 1];
-        if (h1 == h0 || r1 == r0) continue;
-        bool region_fp64 = false;
-        for (int64_t h = h0; h < h1; h++) region_fp64 |= (hap_flag[(size_t)h] != 0);
+    // ceil(R/256) strips, paired within a region and bucket, and split into haplotype chunks.  Regions are
+    // processed in parallel in contiguous parts whose outputs are concatenated in region order, so the
+    // task list is the same for any thread count.
+    const auto t_tasks = std::chrono::steady_clock::now();
+    struct PartOut {
+        std::vector<F32Task> tasks[kNumBucketKeys];
+        std::vector<int64_t> cost[kNumBucketKeys];
+        std::vector<PairRef> direct;
+        int64_t max_multi_cols = 0, cells_direct = 0;
+    };
+    const int64_t n_parts = std::max<int64_t>(1, std::min<int64_t>(G, (int64_t)threads * 4));
+    std::vector<PartOut> parts((size_t)n_parts);
+    const int max_k = ctx->max_k, max_k_multi = ctx->max_k_multi;
+    const int64_t chunk_cols = ctx->chunk_cols;
+    parallel_for(n_parts, threads, [&](int64_t part) {
+        PartOut &po = parts[(size_t)part];
         std::vector<std::pair<int64_t, int64_t>> groups;  // ((key, strips, length), read)
-        for (int64_t r = r0; r < r1; r++) {
-            const int R = (int)(read_off[(size_t)r + 1] - read_off[(size_t)r]);
-            if (region_fp64 || (read_flag[(size_t)r] & 1)) {
-                for (int64_t h = h0; h < h1; h++) direct.push_back(PairRef{(int32_t)r, (int32_t)h});
-                continue;
+        std::vector<std::pair<int64_t, int64_t>> chunks;  // haplotype ranges of one task
+        for (int64_t g = G * part / n_parts; g < G * (part + 1) / n_parts; g++) {
+            const int64_t h0 = rho[(size_t)g], h1 = rho[(size_t)g + 1];
+            const int64_t r0 = rro[(size_t)g], r1 = rro[(size_t)g + 1];
+            if (h1 == h0 || r1 == r0) continue;
+            bool region_fp64 = false;
+            for (int64_t h = h0; h < h1; h++) region_fp64 |= (hap_flag[(size_t)h] != 0);
+            const int64_t region_cols = hap_off[(size_t)h1] - hap_off[(size_t)h0];
+            groups.clear();
+            for (int64_t r = r0; r < r1; r++) {
+                const int R = (int)(read_off[(size_t)r + 1] - read_off[(size_t)r]);
+                if (region_fp64 || (read_flag[(size_t)r] & 1)) {
+                    for (int64_t h = h0; h < h1; h++) po.direct.push_back(PairRef{(int32_t)r, (int32_t)h});
+                    po.cells_direct += (int64_t)R * region_cols;
+                    continue;
+                }
+                int key, ns = 1;
+                if (R <= 32 * max_k) {
+                    key = (R + 31) / 32;
+                } else {  // fewest strips of at most max_k_multi rows per lane, then the fewest rows per lane
+                    ns = (R + 32 * max_k_multi - 1) / (32 * max_k_multi);
+                    key = ((R + 32 * ns - 1) / (32 * ns)) | 16;
+                }
+                // reads are paired only within one (rows per lane, strip count) class
+                groups.emplace_back(((int64_t)key * 4096 + ns) * 100000 + R, r);
             }
-            int key, ns = 1;
-            if (R <= 32 * ctx->max_k) {
-                key = (R + 31) / 32;
-            } else {  // fewest strips of at most max_k_multi rows per lane, then the fewest rows per lane
-                ns = (R + 32 * ctx->max_k_multi - 1) / (32 * ctx->max_k_multi);
-                key = ((R + 32 * ns - 1) / (32 * ns)) | 16;
-            }
-            // reads are paired only within one (rows per lane, strip count) class
-            groups.emplace_back(((int64_t)key * 4096 + ns) * 100000 + R, r);
-        }
-        std::sort(groups.begin(), groups.end());
-        // haplotype chunks
-        std::vector<std::pair<int64_t, int64_t>> chunks;
-        {
-            int64_t a = h0;
-            while (a < h1) {
+            std::sort(groups.begin(), groups.end());
+            chunks.clear();
+            for (int64_t a = h0; a < h1;) {
                 int64_t e = a + 1, cols = hap_off[(size_t)a + 1] - hap_off[(size_t)a];
-                while (e < h1 && cols + (hap_off[(size_t)e + 1] - hap_off[(size_t)e]) <= ctx->chunk_cols) {
+                while (e < h1 && cols + (hap_off[(size_t)e + 1] - hap_off[(size_t)e]) <= chunk_cols) {
                     cols += hap_off[(size_t)e + 1] - hap_off[(size_t)e];
                     e++;
                 }
                 chunks.emplace_back(a, e);
                 a = e;
             }
-        }
-        for (size_t i = 0; i < groups.size();) {
-            const int64_t cls = groups[i].first / 100000;
-            const int key = (int)(cls / 4096);
-            const int64_t ra = groups[i].second;
-            int64_t rb = -1;
-            if (i + 1 < groups.size() && groups[i + 1].first / 100000 == cls) rb = groups[i + 1].second;
-            i += (rb >= 0) ? 2 : 1;
-            const int K = key & 15;
-            const bool multi = (key & 16) != 0;
-            const int S = 32 * K;
-            const int Ra = (int)(read_off[(size_t)ra + 1] - read_off[(size_t)ra]);
-            const int Rb = rb >= 0 ? (int)(read_off[(size_t)rb + 1] - read_off[(size_t)rb]) : 0;
-            const int nstrips = multi ? (std::max(Ra, Rb) + S - 1) / S : 1;
-            for (auto &ch : chunks) {
-                F32Task t;
-                t.read_a = (int32_t)ra;
-                t.read_b = (int32_t)rb;
-                t.hap_begin = (int32_t)ch.first;
-                t.hap_end = (int32_t)ch.second;
-                t.region = (int32_t)g;
-                t.nstrips = (int16_t)nstrips;
-                t.k = (int16_t)K;
-                t.pad_a = nstrips * S - Ra;
-                t.pad_b = rb >= 0 ? nstrips * S - Rb : nstrips * S;
-                const int64_t cols = hap_off[(size_t)ch.second] - hap_off[(size_t)ch.first];
-                if (multi) max_multi_cols = std::max(max_multi_cols, cols);
-                per_bucket[(size_t)key].push_back(t);
-                per_bucket_cost[(size_t)key].push_back((cols + 31) * K * nstrips);
+            for (size_t i = 0; i < groups.size();) {
+                const int64_t cls = groups[i].first / 100000;
+                const int key = (int)(cls / 4096);
+                const int64_t ra = groups[i].second;
+                int64_t rb = -1;
+                if (i + 1 < groups.size() && groups[i + 1].first / 100000 == cls) rb = groups[i + 1].second;
+                i += (rb >= 0) ? 2 : 1;
+                const int K = key & 15;
+                const bool multi = (key & 16) != 0;
+                const int S = 32 * K;
+                const int Ra = (int)(read_off[(size_t)ra + 1] - read_off[(size_t)ra]);
+                const int Rb = rb >= 0 ? (int)(read_off[(size_t)rb + 1] - read_off[(size_t)rb]) : 0;
+                const int nstrips = multi ? (std::max(Ra, Rb) + S - 1) / S : 1;
+                for (auto &ch : chunks) {
+                    F32Task t;
+                    t.read_a = (int32_t)ra;
+                    t.read_b = (int32_t)rb;
+                    t.hap_begin = (int32_t)ch.first;
+                    t.hap_end = (int32_t)ch.second;
+                    t.region = (int32_t)g;
+                    t.nstrips = (int16_t)nstrips;
+                    t.k = (int16_t)K;
+                    t.pad_a = nstrips * S - Ra;
+                    t.pad_b = rb >= 0 ? nstrips * S - Rb : nstrips * S;
+                    const int64_t cols = hap_off[(size_t)ch.second] - hap_off[(size_t)ch.first];
+                    if (multi) po.max_multi_cols = std::max(po.max_multi_cols, cols);
+                    po.tasks[key].push_back(t);
+                    po.cost[key].push_back((cols + 31) * K * nstrips);
+                }
             }
         }
-    }
-    // order each bucket longest first and concatenate
+    }, 1);
+    // buckets in key order, each ordered longest task first (ties keep region order)
     b.buckets.clear();
-    int64_t total_tasks = 0;
-    for (auto &v : per_bucket) total_tasks += (int64_t)v.size();
-    GHMM_CUDA(b.h_tasks.reserve((size_t)total_tasks), "pinned tasks");
-    int64_t pos = 0;
-    for (int key = 1; key < 32; key++) {
-        auto &v = per_bucket[(size_t)key];
-        if (v.empty()) continue;
-        auto &cost = per_bucket_cost[(size_t)key];
-        std::vector<size_t> idx(v.size());
-        std::iota(idx.begin(), idx.end(), 0);
-        std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) { return cost[x] > cost[y]; });
-        for (size_t k = 0; k < idx.size(); k++) b.h_tasks.p[pos + (int64_t)k] = v[idx[k]];
+    int64_t total_tasks = 0, max_multi_cols = 0, n_direct = 0;
+    b.cells_direct = 0;
+    std::vector<int64_t> bucket_pos(kNumBucketKeys + 1, 0);
+    for (int key = 0; key < kNumBucketKeys; key++) {
+        int64_t n = 0;
+        for (auto &po : parts) n += (int64_t)po.tasks[key].size();
+        bucket_pos[(size_t)key + 1] = bucket_pos[(size_t)key] + n;
+    }
+    for (auto &po : parts) {
+        max_multi_cols = std::max(max_multi_cols, po.max_multi_cols);
+        n_direct += (int64_t)po.direct.size();
+        b.cells_direct += po.cells_direct;
+    }
+    total_tasks = bucket_pos[kNumBucketKeys];
+    GHMM_CUDA(b.h_tasks.reserve((size_t)std::max<int64_t>(total_tasks, 1)), "pinned tasks");
+    parallel_for(kNumBucketKeys, threads, [&](int64_t key) {
+        const int64_t n = bucket_pos[(size_t)key + 1] - bucket_pos[(size_t)key];
+        if (n == 0) return;
+        std::vector<std::pair<int64_t, int64_t>> order;  // (-cost, position in region order)
+        order.reserve((size_t)n);
+        std::vector<const F32Task *> src_task;
+        src_task.reserve((size_t)n);
+        for (auto &po : parts)
+            for (size_t i = 0; i < po.tasks[key].size(); i++) {
+                order.emplace_back(-po.cost[key][i], (int64_t)src_task.size());
+                src_task.push_back(&po.tasks[key][i]);
+            }
+        std::sort(order.begin(), order.end());
+        F32Task *dst = b.h_tasks.p + bucket_pos[(size_t)key];
+        for (int64_t i = 0; i < n; i++) dst[i] = *src_task[(size_t)order[(size_t)i].second];
+    }, 1);
+    for (int key = 1; key < kNumBucketKeys; key++) {
+        const int64_t n = bucket_pos[(size_t)key + 1] - bucket_pos[(size_t)key];
+        if (n == 0) continue;
         int bpsm = 0;
         if (fp32_kernel_occupancy(key, kBlock, &bpsm) != 0 || bpsm <= 0) bpsm = 1;
-        const int64_t want = ((int64_t)v.size() + kWarpsPerBlock - 1) / kWarpsPerBlock;
+        const int64_t want = (n + kWarpsPerBlock - 1) / kWarpsPerBlock;
         const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->sm_count * bpsm));
-        b.buckets.push_back(Bucket{key, (int)pos, (int)v.size(), grid});
-        pos += (int64_t)v.size();
+        b.buckets.push_back(Bucket{key, (int)bucket_pos[(size_t)key], (int)n, grid});
     }
     b.n_tasks = total_tasks;
-    b.n_direct = (int64_t)direct.size();
-    GHMM_CUDA(b.h_direct.reserve(direct.size()), "pinned direct pairs");
-    if (!direct.empty()) memcpy(b.h_direct.p, direct.data(), direct.size() * sizeof(PairRef));
+    b.n_direct = n_direct;
+    GHMM_CUDA(b.h_direct.reserve((size_t)std::max<int64_t>(n_direct, 1)), "pinned direct pairs");
+    {
+        int64_t k = 0;
+        for (auto &po : parts) {
+            if (!po.direct.empty()) memcpy(b.h_direct.p + k, po.direct.data(), po.direct.size() * sizeof(PairRef));
+            k += (int64_t)po.direct.size();
+        }
+    }
     b.scratch32_cols = max_multi_cols;
     int bpsm64 = 0;
     if (fp64_kernel_occupancy(kBlock, &bpsm64) != 0 || bpsm64 <= 0) bpsm64 = 1;
     b.fp64_grid = ctx->sm_count * bpsm64;
     b.uploaded = false;
+    const auto t_end = std::chrono::steady_clock::now();
+    b.ms_host_copy = std::chrono::duration<double, std::milli>(t_tasks - t_start).count();
+    b.ms_host_tasks = std::chrono::duration<double, std::milli>(t_end - t_tasks).count();
     return GHMM_OK;
 }
 
 // Allocate device buffers and upload the staged batch.
-static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b) {
+static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
     const int64_t NR = b.n_reads, NH = b.n_haps, G = b.n_regions;
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     GHMM_CUDA(b.d_planes.reserve((size_t)b.read_bytes * 5), "device read planes");
@@ -551,7 +629,8 @@ static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b) {
     const int64_t capacity = std::max<int64_t>(b.n_out, 1);
     GHMM_CUDA(b.d_rerun.reserve((size_t)capacity), "device FP64 queue");
     GHMM_CUDA(b.d_out.reserve((size_t)std::max<int64_t>(b.n_out, 1)), "device output");
-    GHMM_CUDA(b.d_counters.reserve(kNumCounters), "device counters");
+    GHMM_CUDA(b.d_counters.reserve(kNumCounters + 2 * kNumBucketKeys), "device counters");
+    GHMM_CUDA(b.d_nout.reserve(1), "device output count");
     int max_grid_multi = 0;
     for (auto &bk : b.buckets)
         if (bk.key & 16) max_grid_multi = std::max(max_grid_multi, bk.grid);
@@ -560,7 +639,6 @@ static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b) {
     const size_t s64 = (size_t)b.fp64_grid * kWarpsPerBlock * (size_t)std::max(b.max_hap_len, 1) * 3;
     GHMM_CUDA(b.d_scratch64.reserve(s64), "device FP64 strip scratch");
 
-    cudaStream_t s = ctx->stream;
     GHMM_CUDA(cudaMemcpyAsync(b.d_planes.p, b.h_planes.p, (size_t)b.read_bytes * 5, cudaMemcpyHostToDevice, s), "H2D planes");
     GHMM_CUDA(cudaMemcpyAsync(b.d_hap.p, b.h_hap.p, (size_t)b.hap_bytes * 2, cudaMemcpyHostToDevice, s), "H2D haplotypes");
     GHMM_CUDA(cudaMemcpyAsync(b.d_off.p, b.h_off.p, n_off * sizeof(int64_t), cudaMemcpyHostToDevice, s), "H2D offsets");
@@ -595,6 +673,8 @@ static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b) {
     d.tasks = b.d_tasks.p;
     d.rerun = b.d_rerun.p;
     d.counters = b.d_counters.p;
+    d.bucket_info = b.d_counters.p + kNumCounters;
+    d.n_out_dev = b.d_nout.p;
     d.rerun_capacity = capacity;
     d.scratch32 = b.d_scratch32.p;
     d.scratch32_cols = b.scratch32_cols;
@@ -618,6 +698,9 @@ static int fill_fp64_all(ghmm_ctx *ctx, ghmm_batch &b) {
     b.n_direct_fp64mode = k;
     return GHMM_OK;
 }
+
+static int batch_enqueue(ghmm_ctx *ctx, ghmm_batch &b, int mode, cudaStream_t s);
+static int batch_finish(ghmm_ctx *ctx, ghmm_batch &b);
 
 static int batch_forward(ghmm_ctx *ctx, ghmm_batch &b, int mode) {
     if (!b.uploaded) return fail(ctx, GHMM_ERR_STATE, "batch not uploaded");
@@ -650,7 +733,62 @@ static int batch_forward(ghmm_ctx *ctx, ghmm_batch &b, int mode) {
         b.last_rerun = 0;
         return GHMM_OK;
     }
-    // counters: cursors 0, FP64 queue tail = number of pre-queued pairs
+    int rc = batch_enqueue(ctx, b, mode, s);
+    if (rc) return rc;
+    return batch_finish(ctx, b);
+}
+
+// The kernel sequence of one forward in two phases: 0 = FP32 buckets and the FP64 log10 epilogue, 1 = the FP64
+// queue (pre-queued pairs and FP32 underflows).  Their launch arguments depend only on the batch's device
+// pointers, so each phase is captured once into a CUDA graph and replayed while those stay the same; events
+// recorded between the two graph launches time the phases.
+static int batch_phase(ghmm_ctx *ctx, ghmm_batch &b, int phase, cudaStream_t s) {
+    if (phase == 0) {
+        for (auto &bk : b.buckets) {
+            int e = launch_fp32_bucket(ctx->tables, b.dev, bk.key, bk.grid, kBlock, s);
+            if (e) return cuda_fail(ctx, (cudaError_t)e, "FP32 bucket launch");
+        }
+        if (b.n_tasks > 0) {
+            int e = launch_finalize_fp32(b.dev.out, b.dev.n_out_dev, ctx->sm_count, s);
+            if (e) return cuda_fail(ctx, (cudaError_t)e, "FP32 finalize launch");
+        }
+        return GHMM_OK;
+    }
+    int e = launch_fp64_queue(ctx->tables, b.dev, b.fp64_grid, kBlock, s);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "FP64 queue launch");
+    return GHMM_OK;
+}
+
+static int capture_phase(ghmm_ctx *ctx, ghmm_batch &b, int phase, cudaStream_t s, cudaGraphExec_t *out) {
+    GHMM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "graph capture");
+    int rc = batch_phase(ctx, b, phase, s);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph capture");
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph instantiate");
+    return GHMM_OK;
+}
+
+static int kernel_launch_count(const ghmm_batch &b, int mode) {
+    int n = 1;
+    if (mode == GHMM_MODE_FP32_RERUN) n += (int)b.buckets.size() + (b.n_tasks > 0 ? 1 : 0);
+    return n;
+}
+
+// Enqueue a forward on stream s without waiting: control words, FP64 pre-queue, the kernel graph, and the
+// D2H of the counters.  batch_finish waits and reads the outcome.
+static int batch_enqueue(ghmm_ctx *ctx, ghmm_batch &b, int mode, cudaStream_t s) {
+    if (!b.events_ready) {
+        for (auto &e : b.ev) GHMM_CUDA(cudaEventCreate(&e), "cudaEventCreate");
+        b.events_ready = true;
+    }
+    GHMM_CUDA(cudaEventRecord(b.ev[0], s), "event");
     int64_t n_pre = b.n_direct;
     if (mode == GHMM_MODE_FP64) {
         if (b.n_direct_fp64mode != b.n_out) {
@@ -662,44 +800,71 @@ static int batch_forward(ghmm_ctx *ctx, ghmm_batch &b, int mode) {
     if (n_pre > 0)
         GHMM_CUDA(cudaMemcpyAsync(b.d_rerun.p, b.h_direct.p, (size_t)n_pre * sizeof(PairRef), cudaMemcpyHostToDevice, s),
                   "H2D FP64 pairs");
-    b.forward_h2d = n_pre * (int64_t)sizeof(PairRef) + kNumCounters * 4;
-    b.forward_d2h = kNumCounters * 4;
     int32_t *hc = b.h_counters.p;
-    for (int i = 0; i < kNumCounters; i++) hc[i] = 0;
+    for (int i = 0; i < kNumCounters + 2 * kNumBucketKeys; i++) hc[i] = 0;
     hc[1] = (int32_t)n_pre;
-    GHMM_CUDA(cudaMemcpyAsync(b.d_counters.p, hc, kNumCounters * sizeof(int32_t), cudaMemcpyHostToDevice, s), "H2D counters");
-    GHMM_CUDA(cudaEventRecord(ev[2], s), "event");
-    if (mode == GHMM_MODE_FP32_RERUN) {
-        int slot = kCounterBase;
-        for (auto &bk : b.buckets) {
-            int e = launch_fp32_bucket(ctx->tables, b.dev, bk.key, bk.begin, bk.count, bk.grid, kBlock, slot++, s);
-            if (e) return cuda_fail(ctx, (cudaError_t)e, "FP32 bucket launch");
-            b.last_launches++;
+    for (auto &bk : b.buckets) {
+        hc[kNumCounters + bk.key] = bk.begin;
+        hc[kNumCounters + kNumBucketKeys + bk.key] = bk.count;
+    }
+    b.h_nout.p[0] = b.n_out;
+    GHMM_CUDA(cudaMemcpyAsync(b.d_counters.p, hc, (kNumCounters + 2 * kNumBucketKeys) * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, s), "H2D counters");
+    GHMM_CUDA(cudaMemcpyAsync(b.d_nout.p, b.h_nout.p, sizeof(int64_t), cudaMemcpyHostToDevice, s), "H2D output count");
+    b.forward_h2d = n_pre * (int64_t)sizeof(PairRef) + (kNumCounters + 2 * kNumBucketKeys) * 4 + 8;
+    b.forward_d2h = kNumCounters * 4;
+    // the graph signature: everything the captured launches depend on
+    std::vector<unsigned char> sig(sizeof(DevBatch) + 2 * sizeof(int));
+    memcpy(sig.data(), &b.dev, sizeof(DevBatch));
+    memcpy(sig.data() + sizeof(DevBatch), &mode, sizeof(int));
+    const int has_tasks = b.n_tasks > 0;
+    memcpy(sig.data() + sizeof(DevBatch) + sizeof(int), &has_tasks, sizeof(int));
+    for (auto &bk : b.buckets) {
+        const int kg[2] = {bk.key, bk.grid};
+        const unsigned char *k = (const unsigned char *)kg;
+        sig.insert(sig.end(), k, k + sizeof(kg));
+    }
+    if (sig != b.graph_sig) {
+        for (auto &g : b.graph) {
+            if (g) cudaGraphExecDestroy(g);
+            g = nullptr;
         }
+        b.graph_sig.clear();
+        if (mode == GHMM_MODE_FP32_RERUN && (b.n_tasks > 0 || !b.buckets.empty())) {
+            int rc = capture_phase(ctx, b, 0, s, &b.graph[0]);
+            if (rc) return rc;
+        }
+        int rc = capture_phase(ctx, b, 1, s, &b.graph[1]);
+        if (rc) return rc;
+        b.graph_sig = sig;
     }
-    if (mode == GHMM_MODE_FP32_RERUN && b.n_tasks > 0) {
-        int e = launch_finalize_fp32(b.dev.out, b.n_out, ctx->sm_count, s);
-        if (e) return cuda_fail(ctx, (cudaError_t)e, "FP32 finalize launch");
-        b.last_launches++;
-    }
-    GHMM_CUDA(cudaEventRecord(ev[3], s), "event");
-    {
-        int e = launch_fp64_queue(ctx->tables, b.dev, b.fp64_grid, kBlock, s);
-        if (e) return cuda_fail(ctx, (cudaError_t)e, "FP64 queue launch");
-        b.last_launches++;
-    }
-    GHMM_CUDA(cudaEventRecord(ev[4], s), "event");
+    GHMM_CUDA(cudaEventRecord(b.ev[1], s), "event");
+    if (b.graph[0]) GHMM_CUDA(cudaGraphLaunch(b.graph[0], s), "graph launch");
+    GHMM_CUDA(cudaEventRecord(b.ev[2], s), "event");
+    GHMM_CUDA(cudaGraphLaunch(b.graph[1], s), "graph launch");
+    GHMM_CUDA(cudaEventRecord(b.ev[3], s), "event");
     GHMM_CUDA(cudaMemcpyAsync(hc, b.d_counters.p, kNumCounters * sizeof(int32_t), cudaMemcpyDeviceToHost, s), "D2H counters");
-    GHMM_CUDA(cudaStreamSynchronize(s), "forward kernels");
+    GHMM_CUDA(cudaEventRecord(b.ev[4], s), "event");
+    b.pending_n_pre = n_pre;
+    b.pending_mode = mode;
+    b.last_mode = mode;
+    b.last_launches = kernel_launch_count(b, mode);
+    return GHMM_OK;
+}
+
+static int batch_finish(ghmm_ctx *ctx, ghmm_batch &b) {
+    GHMM_CUDA(cudaEventSynchronize(b.ev[4]), "forward kernels");
     float ms = 0;
-    cudaEventElapsedTime(&ms, ev[2], ev[3]);
+    cudaEventElapsedTime(&ms, b.ev[1], b.ev[2]);
     b.ms_fp32 = ms;
-    cudaEventElapsedTime(&ms, ev[3], ev[4]);
+    cudaEventElapsedTime(&ms, b.ev[2], b.ev[3]);
     b.ms_fp64 = ms;
-    cudaEventElapsedTime(&ms, ev[0], ev[4]);
+    cudaEventElapsedTime(&ms, b.ev[0], b.ev[3]);
     b.ms_total = ms;
+    b.ms_plain = 0;
+    const int32_t *hc = b.h_counters.p;
     if (hc[3] != 0) return fail(ctx, GHMM_ERR_CUDA, "device-side queue overflow or scratch bound exceeded");
-    b.last_rerun = (int64_t)hc[1] - n_pre;
+    b.last_rerun = (int64_t)hc[1] - b.pending_n_pre;
     return GHMM_OK;
 }
 
@@ -718,6 +883,392 @@ static int batch_results(ghmm_ctx *ctx, ghmm_batch &b, double *out) {
         }
     return GHMM_OK;
 }
+
+
+// -------------------------------------------------------------------------------------------------
+// Streaming queue: regions are pushed as they arrive and gathered into batches of about batch_cells
+// cells; a worker thread marshals each full batch into one of two slots (pinned + device buffers, one
+// CUDA stream each) and launches it, so the marshal of batch k+1 on the host, the upload of batch k+1
+// and the kernels of batch k overlap, and the two streams fill each other's kernel tails.
+
+struct QueueUnit {
+    // an owned copy of pushed regions, in the flat layout ...
+    std::vector<uint8_t> planes[5];
+    std::vector<uint8_t> hap_bases;
+    std::vector<int64_t> read_off{0}, hap_off{0}, region_read_off{0}, region_hap_off{0};
+    // ... or a borrowed range of a synchronous call's input, which outlives the call
+    bool borrowed = false;
+    Source src;
+    ghmm_flat flat{};
+    std::vector<std::pair<double *, int64_t>> dests;  // output runs in region order
+    int64_t cells = 0, n_out = 0, n_regions = 0;
+
+    void seal_flat() {  // point the flat view at the owned vectors
+        flat = ghmm_flat{};
+        flat.n_regions = n_regions;
+        flat.region_read_off = region_read_off.data();
+        flat.region_hap_off = region_hap_off.data();
+        flat.read_off = read_off.data();
+        flat.bases = planes[0].data();
+        flat.quals = planes[1].data();
+        flat.ins_gop = planes[2].data();
+        flat.del_gop = planes[3].data();
+        flat.gcp = planes[4].data();
+        flat.hap_off = hap_off.data();
+        flat.hap_bases = hap_bases.data();
+        flat.out_off = nullptr;
+        src = Source{};
+        src.flat = &flat;
+        src.n_regions = n_regions;
+    }
+    void drop_inputs() {
+        for (auto &v : planes) std::vector<uint8_t>().swap(v);
+        std::vector<uint8_t>().swap(hap_bases);
+        std::vector<int64_t>().swap(read_off);
+        std::vector<int64_t>().swap(hap_off);
+        std::vector<int64_t>().swap(region_read_off);
+        std::vector<int64_t>().swap(region_hap_off);
+    }
+};
+
+struct ghmm_queue {
+    ghmm_ctx *ctx = nullptr;
+    int64_t batch_cells = 0;
+    int mode = GHMM_MODE_FP32_RERUN;
+    std::unique_ptr<QueueUnit> open;  // filled by push on the caller's thread
+    std::mutex mu;
+    std::condition_variable cv_work, cv_space, cv_done;
+    std::deque<std::unique_ptr<QueueUnit>> ready;
+    int64_t submitted = 0, retired = 0;
+    bool stop = false;
+    int error = GHMM_OK;
+    std::string error_msg;
+    ghmm_queue_info info{};
+    std::thread worker;
+    // worker-owned
+    ghmm_batch slot[2];
+    cudaStream_t stream[2]{};
+    std::unique_ptr<QueueUnit> inflight[2];
+    int64_t inflight_seq[2]{};
+    int64_t seq = 0;
+};
+
+namespace {
+
+constexpr size_t kQueueMaxReady = 2;  // sealed batches waiting for the worker before push blocks
+
+// Copy a finished slot's results to its destinations and check them (PairHMM.java:305-306).
+int queue_deliver(ghmm_ctx *ctx, ghmm_batch &b, const QueueUnit &u, int threads) {
+    const double *src = b.h_out.p;
+    std::atomic<int64_t> bad{-1};
+    std::vector<int64_t> base(u.dests.size() + 1, 0);
+    for (size_t i = 0; i < u.dests.size(); i++) base[i + 1] = base[i] + u.dests[i].second;
+    // blocks of at most 1M results, in parallel
+    std::vector<std::pair<size_t, int64_t>> blocks;
+    for (size_t i = 0; i < u.dests.size(); i++)
+        for (int64_t a = 0; a < u.dests[i].second; a += (1 << 20)) blocks.emplace_back(i, a);
+    parallel_for((int64_t)blocks.size(), threads, [&](int64_t k) {
+        const size_t i = blocks[(size_t)k].first;
+        const int64_t a = blocks[(size_t)k].second, e = std::min<int64_t>(u.dests[i].second, a + (1 << 20));
+        const double *s = src + base[i];
+        double *d = u.dests[i].first;
+        for (int64_t j = a; j < e; j++) {
+            const double v = s[j];
+            d[j] = v;
+            if (!(v <= 0.0)) {
+                int64_t expect = -1;
+                bad.compare_exchange_strong(expect, base[i] + j);
+            }
+        }
+    }, 1);
+    if (bad.load() >= 0) {
+        char msg[160];
+        snprintf(msg, sizeof msg, "PairHMM log10 likelihood %g at output %lld of a queued batch is not a valid log10 probability",
+                 src[bad.load()], (long long)bad.load());
+        return fail(ctx, GHMM_ERR_RESULT, msg);
+    }
+    return GHMM_OK;
+}
+
+// Worker: marshal + upload + launch one unit into slot i (which is free).
+int queue_launch(ghmm_queue *q, int i, QueueUnit &u) {
+    ghmm_ctx *ctx = q->ctx;
+    ghmm_batch &b = q->slot[i];
+    int rc = batch_marshal(ctx, u.src, b);
+    if (rc) return rc;
+    if (b.n_out != u.n_out) return fail(ctx, GHMM_ERR_STATE, "queued batch size mismatch");
+    rc = batch_upload(ctx, b, q->stream[i]);
+    if (rc) return rc;
+    rc = batch_enqueue(ctx, b, q->mode, q->stream[i]);
+    if (rc) return rc;
+    if (b.n_out > 0) {
+        GHMM_CUDA(b.h_out.reserve((size_t)b.n_out), "pinned results");
+        GHMM_CUDA(cudaMemcpyAsync(b.h_out.p, b.d_out.p, (size_t)b.n_out * sizeof(double), cudaMemcpyDeviceToHost,
+                                  q->stream[i]), "D2H results");
+        GHMM_CUDA(cudaEventRecord(b.ev[4], q->stream[i]), "event");
+    }
+    b.results_d2h = b.n_out * 8;
+    return GHMM_OK;
+}
+
+int queue_retire(ghmm_queue *q, int i) {
+    ghmm_ctx *ctx = q->ctx;
+    ghmm_batch &b = q->slot[i];
+    int rc = batch_finish(ctx, b);
+    if (!rc) rc = queue_deliver(ctx, b, *q->inflight[i], hw_threads(ctx->max_threads));
+    std::lock_guard<std::mutex> lk(q->mu);
+    if (!rc) {
+        ghmm_queue_info &in = q->info;
+        in.n_batches++;
+        in.n_launches += b.last_launches;
+        in.n_rerun += b.last_mode == GHMM_MODE_FP32_RERUN ? b.last_rerun : 0;
+        in.n_fp64_direct += b.last_mode == GHMM_MODE_FP64 ? b.n_direct_fp64mode : b.n_direct;
+        in.n_cells_fp64_direct += b.last_mode == GHMM_MODE_FP64 ? b.n_cells : b.cells_direct;
+        in.h2d_bytes += b.upload_bytes + b.forward_h2d;
+        in.d2h_bytes += b.forward_d2h + b.results_d2h;
+        in.ms_fp32 += b.ms_fp32;
+        in.ms_fp64 += b.ms_fp64;
+        in.ms_host_marshal += b.ms_host_copy;
+        in.ms_host_tasks += b.ms_host_tasks;
+    }
+    q->inflight[i].reset();
+    q->retired++;
+    q->cv_done.notify_all();
+    return rc;
+}
+
+void queue_record_error(ghmm_queue *q, int rc, const std::string &msg) {
+    std::lock_guard<std::mutex> lk(q->mu);
+    if (q->error == GHMM_OK) {
+        q->error = rc;
+        q->error_msg = msg;
+    }
+}
+
+void queue_worker(ghmm_queue *q) {
+    std::string err;
+    t_error_sink = &err;
+    cudaSetDevice(q->ctx->device);
+    for (;;) {
+        std::unique_ptr<QueueUnit> u;
+        int oldest = -1;
+        {
+            std::unique_lock<std::mutex> lk(q->mu);
+            for (;;) {
+                if (!q->ready.empty()) {
+                    u = std::move(q->ready.front());
+                    q->ready.pop_front();
+                    q->cv_space.notify_all();
+                    break;
+                }
+                oldest = -1;
+                for (int i = 0; i < 2; i++)
+                    if (q->inflight[i] && (oldest < 0 || q->inflight_seq[i] < q->inflight_seq[oldest])) oldest = i;
+                if (oldest >= 0) {
+                    // nothing to marshal: retire the oldest batch once it is done, polling so that a newly
+                    // sealed batch is taken up while it runs
+                    if (cudaEventQuery(q->slot[oldest].ev[4]) != cudaErrorNotReady) break;
+                    q->cv_work.wait_for(lk, std::chrono::microseconds(200));
+                    oldest = -1;
+                    continue;
+                }
+                if (q->stop) return;
+                q->cv_work.wait(lk);
+            }
+        }
+        if (!u) {  // retire the oldest finished batch
+            int rc = queue_retire(q, oldest);
+            if (rc) queue_record_error(q, rc, err);
+            continue;
+        }
+        int i = q->inflight[0] ? (q->inflight[1] ? -1 : 1) : 0;
+        if (i < 0) {  // both busy: retire the older one and reuse its slot
+            i = q->inflight_seq[0] < q->inflight_seq[1] ? 0 : 1;
+            int rc = queue_retire(q, i);
+            if (rc) queue_record_error(q, rc, err);
+        }
+        bool failed;
+        {
+            std::lock_guard<std::mutex> lk(q->mu);
+            failed = q->error != GHMM_OK;
+        }
+        int rc = failed ? GHMM_OK : queue_launch(q, i, *u);
+        if (failed || rc) {  // after an error the remaining batches are dropped, not computed
+            if (rc) queue_record_error(q, rc, err);
+            std::lock_guard<std::mutex> lk(q->mu);
+            q->retired++;
+            q->cv_done.notify_all();
+            continue;
+        }
+        if (!u->borrowed) u->drop_inputs();
+        q->inflight[i] = std::move(u);
+        q->inflight_seq[i] = ++q->seq;
+    }
+}
+
+// Hand the open unit to the worker (blocks while kQueueMaxReady units already wait).
+void queue_submit(ghmm_queue *q, std::unique_ptr<QueueUnit> u) {
+    if (!u->borrowed) u->seal_flat();
+    std::unique_lock<std::mutex> lk(q->mu);
+    q->cv_space.wait(lk, [&] { return q->ready.size() < kQueueMaxReady || q->error != GHMM_OK; });
+    q->ready.push_back(std::move(u));
+    q->submitted++;
+    q->cv_work.notify_all();
+}
+
+int queue_wait_all(ghmm_queue *q) {
+    std::unique_lock<std::mutex> lk(q->mu);
+    q->cv_done.wait(lk, [&] { return q->retired == q->submitted; });
+    return q->error;
+}
+
+int queue_open(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **out) {
+    auto *q = new ghmm_queue();
+    q->ctx = ctx;
+    q->batch_cells = batch_cells > 0 ? batch_cells : (int64_t)2e11;
+    q->mode = ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN;
+    for (auto &st : q->stream) {
+        cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            for (auto &s2 : q->stream)
+                if (s2) cudaStreamDestroy(s2);
+            delete q;
+            return cuda_fail(ctx, e, "queue stream");
+        }
+    }
+    q->worker = std::thread(queue_worker, q);
+    ctx->open_queues++;
+    *out = q;
+    return GHMM_OK;
+}
+
+void queue_close(ghmm_queue *q) {
+    {
+        std::lock_guard<std::mutex> lk(q->mu);
+        q->stop = true;
+        q->cv_work.notify_all();
+    }
+    q->worker.join();
+    cudaSetDevice(q->ctx->device);
+    for (int i = 0; i < 2; i++) {
+        if (q->stream[i]) cudaStreamSynchronize(q->stream[i]);
+        q->slot[i].release();
+        if (q->stream[i]) cudaStreamDestroy(q->stream[i]);
+    }
+    q->ctx->open_queues--;
+    delete q;
+}
+
+// The error a queue recorded, moved into the context's message on the caller's thread.
+int queue_status(ghmm_queue *q) {
+    std::lock_guard<std::mutex> lk(q->mu);
+    if (q->error != GHMM_OK) q->ctx->last_error = q->error_msg;
+    return q->error;
+}
+
+// Regions [g0, g1) of a synchronous call, borrowed.  out_base points at region g0's first result.
+std::unique_ptr<QueueUnit> borrowed_unit(const Source &src, int64_t g0, int64_t g1, double *out_base, int64_t n_out,
+                                         int64_t cells) {
+    auto u = std::make_unique<QueueUnit>();
+    u->borrowed = true;
+    u->n_regions = g1 - g0;
+    if (src.flat) {
+        u->flat = *src.flat;
+        u->flat.n_regions = g1 - g0;
+        u->flat.region_read_off = src.flat->region_read_off + g0;
+        u->flat.region_hap_off = src.flat->region_hap_off + g0;
+        u->src.flat = &u->flat;
+    } else {
+        u->src.regions = src.regions + g0;
+    }
+    u->src.n_regions = g1 - g0;
+    u->n_out = n_out;
+    u->cells = cells;
+    if (n_out > 0) u->dests.emplace_back(out_base, n_out);
+    return u;
+}
+
+// Large synchronous inputs run as a pipeline of batches through the context's own queue: the first batch
+// is small so that the GPU starts early, later ones grow to a third of the input.
+constexpr int64_t kPipelineMinCells = (int64_t)6e10;
+
+int pipelined_compute(ghmm_ctx *ctx, const Source &src, const std::vector<int64_t> &reg_cells,
+                      const std::vector<int64_t> &reg_out, double *out) {
+    if (!ctx->pipe) {
+        int rc = queue_open(ctx, 0, &ctx->pipe);
+        if (rc) return rc;
+    }
+    ghmm_queue *q = ctx->pipe;
+    {
+        std::lock_guard<std::mutex> lk(q->mu);
+        q->error = GHMM_OK;
+        q->error_msg.clear();
+        q->mode = ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN;
+    }
+    const int64_t G = src.n_regions;
+    int64_t total = 0;
+    for (int64_t g = 0; g < G; g++) total += reg_cells[(size_t)g];
+    int64_t target = std::max<int64_t>(total / 16, 1), g0 = 0;
+    while (g0 < G) {
+        int64_t g1 = g0, c = 0;
+        while (g1 < G && (c < target || g1 == g0)) c += reg_cells[(size_t)g1++];
+        if (G - g1 < 8) {  // do not leave a sliver
+            for (; g1 < G; g1++) c += reg_cells[(size_t)g1];
+        }
+        queue_submit(q, borrowed_unit(src, g0, g1, out + reg_out[(size_t)g0], reg_out[(size_t)g1] - reg_out[(size_t)g0], c));
+        target = std::min(target * 5 / 2, std::max<int64_t>(total / 3, 1));
+        g0 = g1;
+    }
+    int rc = queue_wait_all(q);
+    if (rc) return queue_status(q);
+    return GHMM_OK;
+}
+
+// Per-region cells and output offsets of a region array or flat input; false if a count is negative.
+bool region_sizes(const Source &src, std::vector<int64_t> &cells, std::vector<int64_t> &outo) {
+    const int64_t G = src.n_regions;
+    cells.assign((size_t)G, 0);
+    outo.assign((size_t)G + 1, 0);
+    for (int64_t g = 0; g < G; g++) {
+        int64_t sr = 0, sh = 0, nr, nh;
+        if (src.flat) {
+            const ghmm_flat *f = src.flat;
+            nr = f->region_read_off[g + 1] - f->region_read_off[g];
+            nh = f->region_hap_off[g + 1] - f->region_hap_off[g];
+            if (nr < 0 || nh < 0) return false;
+            sr = f->read_off[f->region_read_off[g + 1]] - f->read_off[f->region_read_off[g]];
+            sh = f->hap_off[f->region_hap_off[g + 1]] - f->hap_off[f->region_hap_off[g]];
+        } else {
+            const ghmm_region &rg = src.regions[g];
+            nr = rg.n_reads;
+            nh = rg.n_haps;
+            if (nr < 0 || nh < 0 || (nr > 0 && !rg.reads) || (nh > 0 && !rg.haps)) return false;
+            for (int32_t r = 0; r < rg.n_reads; r++) sr += std::max(rg.reads[r].length, 0);
+            for (int32_t h = 0; h < rg.n_haps; h++) sh += std::max(rg.haps[h].length, 0);
+        }
+        cells[(size_t)g] = sr * sh;
+        outo[(size_t)g + 1] = outo[(size_t)g] + nr * nh;
+    }
+    return true;
+}
+
+// Synchronous compute of regions or flat input: one batch for small inputs, the pipeline for large ones.
+int compute_sync(ghmm_ctx *ctx, const Source &src, double *out) {
+    std::vector<int64_t> cells, outo;
+    if (!region_sizes(src, cells, outo)) return fail(ctx, GHMM_ERR_ARG, "negative count or NULL array in a region");
+    int64_t total = 0;
+    for (auto c : cells) total += c;
+    if (outo.back() > 0 && !out) return fail(ctx, GHMM_ERR_ARG, "NULL output");
+    if (total >= kPipelineMinCells && src.n_regions >= 4) return pipelined_compute(ctx, src, cells, outo, out);
+    ghmm_batch &b = ctx->scratch_batch;
+    int rc = batch_marshal(ctx, src, b);
+    if (!rc) rc = batch_upload(ctx, b, ctx->stream);
+    if (!rc) rc = batch_forward(ctx, b, ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN);
+    if (!rc) rc = batch_results(ctx, b, out);
+    return rc;
+}
+
+}  // namespace
 
 void ghmm::set_global_error(const char *msg) {
     std::lock_guard<std::mutex> lk(g_init_error_mu);
@@ -851,6 +1402,8 @@ static int calib_run(ghmm_ctx *ctx, const ghmm_calib_batch *in, int precision, c
 int ghmm_set_tuning(ghmm_ctx *ctx, const ghmm_tuning *t) {
     if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
     if (!t) return fail(ctx, GHMM_ERR_ARG, "NULL tuning");
+    if (ctx->open_queues.load() > (ctx->pipe ? 1 : 0))
+        return fail(ctx, GHMM_ERR_STATE, "the tuning cannot change while a queue is open");
     const int mk = t->max_rows_per_lane ? t->max_rows_per_lane : kMaxK32;
     const int mm = t->max_rows_per_lane_multi ? t->max_rows_per_lane_multi : kMaxK32;
     const int cc = t->chunk_cols ? t->chunk_cols : 16384;
@@ -864,7 +1417,11 @@ int ghmm_set_tuning(ghmm_ctx *ctx, const ghmm_tuning *t) {
 
 int ghmm_done(ghmm_ctx *ctx) {
     if (!ctx) return GHMM_ERR_STATE;
+    if (ctx->open_queues.load() > (ctx->pipe ? 1 : 0))
+        return fail(ctx, GHMM_ERR_STATE, "destroy the context's queues before ghmm_done");
     cudaSetDevice(ctx->device);
+    if (ctx->pipe) queue_close(ctx->pipe);
+    ctx->pipe = nullptr;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     ctx->scratch_batch.release();
     ctx->calib_scratch.release();
@@ -896,15 +1453,11 @@ int ghmm_compute_regions(ghmm_ctx *ctx, const ghmm_region *regions, int32_t n_re
     if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
     if (n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad region array");
     if (n_regions == 0) return GHMM_OK;
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     Source src;
     src.regions = regions;
     src.n_regions = n_regions;
-    ghmm_batch &b = ctx->scratch_batch;
-    int rc = batch_marshal(ctx, src, b);
-    if (!rc) rc = batch_upload(ctx, b);
-    if (!rc) rc = batch_forward(ctx, b, ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN);
-    if (!rc) rc = batch_results(ctx, b, out);
-    return rc;
+    return compute_sync(ctx, src, out);
 }
 
 int ghmm_compute_likelihoods(ghmm_ctx *ctx, const ghmm_read *reads, int32_t n_reads, const ghmm_hap *haps,
@@ -923,7 +1476,7 @@ int ghmm_batch_create(ghmm_ctx *ctx, const ghmm_region *regions, int32_t n_regio
     src.regions = regions;
     src.n_regions = n_regions;
     int rc = batch_marshal(ctx, src, *b);
-    if (!rc) rc = batch_upload(ctx, *b);
+    if (!rc) rc = batch_upload(ctx, *b, ctx->stream);
     if (!rc) rc = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? GHMM_OK : fail(ctx, GHMM_ERR_CUDA, "upload");
     if (rc) {
         b->release();
@@ -942,7 +1495,7 @@ int ghmm_batch_create_flat(ghmm_ctx *ctx, const ghmm_flat *flat, ghmm_batch **ou
     src.flat = flat;
     src.n_regions = flat->n_regions;
     int rc = batch_marshal(ctx, src, *b);
-    if (!rc) rc = batch_upload(ctx, *b);
+    if (!rc) rc = batch_upload(ctx, *b, ctx->stream);
     if (!rc) rc = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? GHMM_OK : fail(ctx, GHMM_ERR_CUDA, "upload");
     if (rc) {
         b->release();
@@ -982,6 +1535,8 @@ int ghmm_batch_stats(ghmm_ctx *ctx, const ghmm_batch *b, ghmm_stats *st) {
     st->ms_total = b->ms_total;
     st->h2d_bytes = b->upload_bytes + b->forward_h2d;
     st->d2h_bytes = b->forward_d2h + b->results_d2h;
+    st->ms_host_marshal = b->ms_host_copy;
+    st->ms_host_tasks = b->ms_host_tasks;
     return GHMM_OK;
 }
 
@@ -1000,15 +1555,115 @@ int ghmm_compute_flat(ghmm_ctx *ctx, const ghmm_flat *flat, double *out) {
     if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
     if (!flat || flat->n_regions < 0) return fail(ctx, GHMM_ERR_ARG, "bad arguments");
     if (flat->n_regions == 0) return GHMM_OK;
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     Source src;
     src.flat = flat;
     src.n_regions = flat->n_regions;
-    ghmm_batch &b = ctx->scratch_batch;
-    int rc = batch_marshal(ctx, src, b);
-    if (!rc) rc = batch_upload(ctx, b);
-    if (!rc) rc = batch_forward(ctx, b, ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN);
-    if (!rc) rc = batch_results(ctx, b, out);
-    return rc;
+    return compute_sync(ctx, src, out);
+}
+
+int ghmm_queue_create(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **queue) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!queue || batch_cells < 0) return fail(ctx, GHMM_ERR_ARG, "bad arguments");
+    *queue = nullptr;
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    return queue_open(ctx, batch_cells, queue);
+}
+
+int ghmm_queue_push(ghmm_queue *q, const ghmm_region *regions, int32_t n_regions, double *out) {
+    if (!q) return GHMM_ERR_STATE;
+    ghmm_ctx *ctx = q->ctx;
+    if (int rc = queue_status(q)) return rc;
+    if (n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad region array");
+    // check everything first, so that a rejected push leaves the queue as it was
+    int64_t n_out = 0;
+    for (int32_t g = 0; g < n_regions; g++) {
+        const ghmm_region &rg = regions[g];
+        if (rg.n_reads < 0 || rg.n_haps < 0) return fail(ctx, GHMM_ERR_ARG, "negative read or haplotype count");
+        if ((rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps))
+            return fail(ctx, GHMM_ERR_ARG, "NULL read or haplotype array");
+        for (int32_t r = 0; r < rg.n_reads; r++) {
+            const ghmm_read &rd = rg.reads[r];
+            if (rd.length < 0 || rd.length > kMaxReadLen) return fail(ctx, GHMM_ERR_ARG, "read length out of range");
+            if (rd.length > 0 && (!rd.bases || !rd.quals || !rd.ins_gop || !rd.del_gop || !rd.gcp))
+                return fail(ctx, GHMM_ERR_ARG, "NULL read array");
+            for (int32_t i = 0; i < rd.length; i++)
+                if (rd.quals[i] > kMaxQual || rd.ins_gop[i] > 127 || rd.del_gop[i] > 127 || rd.gcp[i] > 127)
+                    return fail(ctx, GHMM_ERR_ARG,
+                                "quality out of range (base quality must be <= 254; insertion, deletion and gap "
+                                "continuation penalties must be 0..127)");
+        }
+        for (int32_t h = 0; h < rg.n_haps; h++) {
+            const ghmm_hap &hp = rg.haps[h];
+            if (hp.length < 0 || hp.length > kMaxHapLen) return fail(ctx, GHMM_ERR_ARG, "haplotype length out of range");
+            if (hp.length > 0 && !hp.bases) return fail(ctx, GHMM_ERR_ARG, "NULL haplotype bases");
+        }
+        n_out += (int64_t)rg.n_reads * rg.n_haps;
+    }
+    if (n_out > 0 && !out) return fail(ctx, GHMM_ERR_ARG, "NULL output");
+    if (!q->open) q->open = std::make_unique<QueueUnit>();
+    QueueUnit &u = *q->open;
+    for (int32_t g = 0; g < n_regions; g++) {
+        const ghmm_region &rg = regions[g];
+        int64_t sr = 0, sh = 0;
+        for (int32_t r = 0; r < rg.n_reads; r++) {
+            const ghmm_read &rd = rg.reads[r];
+            const uint8_t *src[5] = {rd.bases, rd.quals, rd.ins_gop, rd.del_gop, rd.gcp};
+            for (int p = 0; p < 5; p++) u.planes[p].insert(u.planes[p].end(), src[p], src[p] + rd.length);
+            u.read_off.push_back(u.read_off.back() + rd.length);
+            sr += rd.length;
+        }
+        for (int32_t h = 0; h < rg.n_haps; h++) {
+            const ghmm_hap &hp = rg.haps[h];
+            u.hap_bases.insert(u.hap_bases.end(), hp.bases, hp.bases + hp.length);
+            u.hap_off.push_back(u.hap_off.back() + hp.length);
+            sh += hp.length;
+        }
+        u.region_read_off.push_back(u.region_read_off.back() + rg.n_reads);
+        u.region_hap_off.push_back(u.region_hap_off.back() + rg.n_haps);
+        u.n_regions++;
+        u.cells += sr * sh;
+        std::lock_guard<std::mutex> lk(q->mu);
+        q->info.n_cells += sr * sh;
+    }
+    if (n_out > 0) {
+        if (!u.dests.empty() && u.dests.back().first + u.dests.back().second == out)
+            u.dests.back().second += n_out;  // contiguous with the previous push
+        else
+            u.dests.emplace_back(out, n_out);
+    }
+    u.n_out += n_out;
+    {
+        std::lock_guard<std::mutex> lk(q->mu);
+        q->info.n_regions += n_regions;
+        q->info.n_pairs += n_out;
+    }
+    if (u.cells >= q->batch_cells) queue_submit(q, std::move(q->open));
+    return queue_status(q);
+}
+
+int ghmm_queue_flush(ghmm_queue *q) {
+    if (!q) return GHMM_ERR_STATE;
+    if (q->open && q->open->n_regions > 0) queue_submit(q, std::move(q->open));
+    q->open.reset();
+    queue_wait_all(q);
+    return queue_status(q);
+}
+
+int ghmm_queue_get_info(ghmm_queue *q, ghmm_queue_info *info) {
+    if (!q) return GHMM_ERR_STATE;
+    if (!info) return fail(q->ctx, GHMM_ERR_ARG, "NULL info");
+    std::lock_guard<std::mutex> lk(q->mu);
+    *info = q->info;
+    return GHMM_OK;
+}
+
+int ghmm_queue_destroy(ghmm_queue *q) {
+    if (!q) return GHMM_OK;
+    if (q->open && q->open->n_regions > 0) queue_submit(q, std::move(q->open));
+    queue_wait_all(q);
+    queue_close(q);
+    return GHMM_OK;
 }
 
 void *ghmm_stream(ghmm_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }

@@ -74,7 +74,16 @@ class Stats(ctypes.Structure):
                 ("n_fp64_direct", ctypes.c_int64), ("n_tasks_fp32", ctypes.c_int64), ("n_launches", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("ms_fp32", ctypes.c_double), ("ms_fp64", ctypes.c_double),
                 ("ms_plain", ctypes.c_double), ("ms_total", ctypes.c_double), ("h2d_bytes", ctypes.c_int64),
-                ("d2h_bytes", ctypes.c_int64)]
+                ("d2h_bytes", ctypes.c_int64), ("ms_host_marshal", ctypes.c_double),
+                ("ms_host_tasks", ctypes.c_double)]
+
+
+class QueueInfo(ctypes.Structure):
+    _fields_ = [("n_regions", ctypes.c_int64), ("n_pairs", ctypes.c_int64), ("n_cells", ctypes.c_int64),
+                ("n_cells_fp64_direct", ctypes.c_int64), ("n_rerun", ctypes.c_int64), ("n_fp64_direct", ctypes.c_int64),
+                ("n_batches", ctypes.c_int64), ("n_launches", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64),
+                ("d2h_bytes", ctypes.c_int64), ("ms_fp32", ctypes.c_double), ("ms_fp64", ctypes.c_double),
+                ("ms_host_marshal", ctypes.c_double), ("ms_host_tasks", ctypes.c_double)]
 
 
 class DevPairs(ctypes.Structure):
@@ -123,6 +132,11 @@ _SIGS = {
     "ghmm_batch_destroy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "ghmm_compute_flat": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Flat), _f64p]),
     "ghmm_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "ghmm_queue_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "ghmm_queue_push": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "ghmm_queue_flush": (ctypes.c_int, [ctypes.c_void_p]),
+    "ghmm_queue_get_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(QueueInfo)]),
+    "ghmm_queue_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "ghmm_measure_peaks": (ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p]),
     "ghmm_debug_tables": (ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p]),
     "ghmm_synth_default_regions": (ctypes.c_int64, [ctypes.c_int32]),

@@ -167,6 +167,9 @@ class Engine:
     def batch(self, wl: Workload, via_regions: bool = False) -> "Batch":
         return Batch(self, wl, via_regions)
 
+    def queue(self, batch_cells: int = 0) -> "Queue":
+        return Queue(self, batch_cells)
+
     def measure_peaks(self):
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         native.check(self.L.ghmm_measure_peaks(self._ctx.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
@@ -220,6 +223,67 @@ class Batch:
         if self.h:
             self.engine.L.ghmm_batch_destroy(self.engine.handle, self.h)
             self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Queue:
+    """Streaming queue: push regions one at a time as they arrive; results land in the caller's arrays.
+
+    ``push`` copies the region's inputs before it returns; the output array must stay alive (and is held
+    here) until ``flush`` returns.
+    """
+
+    def __init__(self, engine: Engine, batch_cells: int = 0):
+        self.engine = engine
+        h = ctypes.c_void_p()
+        native.check(engine.L.ghmm_queue_create(engine.handle, int(batch_cells), ctypes.byref(h)), engine.handle)
+        self.h = h
+        self._keep: list = []
+
+    def push_regions(self, regions, n_regions: int, out: np.ndarray, keep=None) -> None:
+        """Push n_regions ghmm_region structs starting at ``regions`` (a ctypes pointer); out is float64."""
+        assert out.dtype == np.float64 and out.flags.c_contiguous
+        rc = self.engine.L.ghmm_queue_push(self.h, ctypes.cast(regions, ctypes.c_void_p), int(n_regions),
+                                           out.ctypes.data if out.size else None)
+        self._keep.append(out)
+        native.check(rc, self.engine.handle)
+
+    def push(self, wl: Workload, out: np.ndarray | None = None) -> np.ndarray:
+        """Push every region of a workload (one push per region); returns the output array."""
+        regs = wl.as_regions()
+        if out is None:
+            out = np.empty(wl.n_pairs, dtype=np.float64)
+        size = ctypes.sizeof(native.Region)
+        base = ctypes.cast(regs, ctypes.c_void_p).value
+        oo = wl.out_off
+        for g in range(wl.n_regions):
+            rc = self.engine.L.ghmm_queue_push(self.h, base + g * size, 1,
+                                               out.ctypes.data + int(oo[g]) * 8 if oo[g + 1] > oo[g] else None)
+            native.check(rc, self.engine.handle)
+        self._keep.append((out, regs))
+        return out
+
+    def flush(self) -> None:
+        rc = self.engine.L.ghmm_queue_flush(self.h)
+        self._keep.clear()
+        native.check(rc, self.engine.handle)
+
+    def info(self) -> dict:
+        i = native.QueueInfo()
+        native.check(self.engine.L.ghmm_queue_get_info(self.h, ctypes.byref(i)), self.engine.handle)
+        return {k: getattr(i, k) for k, _ in native.QueueInfo._fields_}
+
+    def close(self) -> None:
+        if self.h:
+            rc = self.engine.L.ghmm_queue_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+            native.check(rc, self.engine.handle)
 
     def __enter__(self):
         return self

@@ -104,6 +104,7 @@ typedef struct ghmm_flat {
 
 typedef struct ghmm_ctx ghmm_ctx;
 typedef struct ghmm_batch ghmm_batch;
+typedef struct ghmm_queue ghmm_queue;
 
 /* Per-batch statistics (filled by ghmm_batch_stats after ghmm_batch_forward). */
 typedef struct ghmm_stats {
@@ -120,6 +121,8 @@ typedef struct ghmm_stats {
     double ms_total;          /* device time of the whole forward */
     int64_t h2d_bytes;        /* host-to-device bytes of the last upload + forward */
     int64_t d2h_bytes;        /* device-to-host bytes of the last forward + results */
+    double ms_host_marshal;   /* host time of the last marshal: copies into pinned planes, checks, routing */
+    double ms_host_tasks;     /* host time of building and ordering the FP32 warp tasks */
 } ghmm_stats;
 
 /* Launch-shape choices of the FP32 pass (the autotuner's knobs; the reference has none besides its thread
@@ -153,7 +156,9 @@ int ghmm_done(ghmm_ctx *ctx);
 int ghmm_last_error(const ghmm_ctx *ctx, char *buf, size_t buf_len);
 
 /* Batcher: many regions in one call (regions of HaplotypeCallerEngine.callRegion batched together).
- * out receives each region's read-major block back to back, in region order. */
+ * out receives each region's read-major block back to back, in region order.  Inputs of 6e10 cells or
+ * more run as a pipeline of batches (the first small, later ones up to a third of the input) on the
+ * context's internal queue, so that marshalling overlaps the kernels; the results are the same. */
 int ghmm_compute_regions(ghmm_ctx *ctx, const ghmm_region *regions, int32_t n_regions, double *out);
 
 /* Device-resident batches: marshal + upload once, run the forward many times, download. */
@@ -169,6 +174,43 @@ int ghmm_compute_flat(ghmm_ctx *ctx, const ghmm_flat *flat, double *out);
 
 /* The CUDA stream the context launches on (a cudaStream_t), for callers that time or order work. */
 void *ghmm_stream(ghmm_ctx *ctx);
+
+/* Streaming queue: regions enqueued one at a time as they arrive, as HaplotypeCaller produces them.
+ * No counterpart in the reference's binding, whose computeLikelihoods is synchronous per active region
+ * (PH/VectorLoglessPairHMM.java:138, called once per region from HC/HaplotypeCallerEngine.java:734-918
+ * through PairHMMLikelihoodCalculationEngine.computeReadLikelihoods); the queue is what a caller puts in
+ * front of it to batch regions.
+ *   ghmm_queue_create: a queue on ctx; batches are launched once they hold batch_cells cells (0: 2e11).
+ *   ghmm_queue_push:   copy n_regions regions into the open batch before returning, so the caller may
+ *                      reuse its arrays; their read-major results go to out (as ghmm_compute_regions), which
+ *                      must stay valid until ghmm_queue_flush returns.  Input errors are reported by this
+ *                      call and leave the queue unchanged; an error of an earlier batch (a device failure or
+ *                      an invalid result) is returned by every later push and flush.
+ *   ghmm_queue_flush:  launch the open batch and wait until every pushed region's results are in place.
+ *   ghmm_queue_get_info: totals over the queue's finished batches.
+ *   ghmm_queue_destroy: flush, then release the queue (before ghmm_done of its context).
+ * A worker thread marshals and launches full batches on two streams with two buffer slots.  One queue is
+ * driven by one thread at a time; ghmm_set_tuning is refused while a queue is open. */
+typedef struct ghmm_queue_info {
+    int64_t n_regions;            /* regions pushed */
+    int64_t n_pairs;              /* read x haplotype pairs pushed */
+    int64_t n_cells;              /* cells pushed */
+    int64_t n_cells_fp64_direct;  /* cells of finished pairs sent to FP64 directly (the rest ran in FP32) */
+    int64_t n_rerun;              /* finished pairs recomputed in FP64 after the FP32 pass */
+    int64_t n_fp64_direct;        /* finished pairs sent to FP64 directly */
+    int64_t n_batches;            /* batches finished */
+    int64_t n_launches;           /* kernels launched by the finished batches */
+    int64_t h2d_bytes, d2h_bytes; /* bytes copied by the finished batches */
+    double ms_fp32, ms_fp64;      /* summed device time of the two phases (batches on the two streams overlap) */
+    double ms_host_marshal;       /* summed worker time in marshalling copies and checks */
+    double ms_host_tasks;         /* summed worker time in building FP32 tasks */
+} ghmm_queue_info;
+
+int ghmm_queue_create(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **queue);
+int ghmm_queue_push(ghmm_queue *queue, const ghmm_region *regions, int32_t n_regions, double *out);
+int ghmm_queue_flush(ghmm_queue *queue);
+int ghmm_queue_get_info(ghmm_queue *queue, ghmm_queue_info *info);
+int ghmm_queue_destroy(ghmm_queue *queue);
 
 /* Measured FP32 FMA-pipe peak of the device in TFLOP/s (FMA = 2 FLOP): best of a scalar FFMA and a
  * packed FFMA2 register-resident loop over all SMs, timed with CUDA events.  Also reports the FP64
