@@ -1562,6 +1562,83 @@ int ghmm_compute_flat(ghmm_ctx *ctx, const ghmm_flat *flat, double *out) {
     return compute_sync(ctx, src, out);
 }
 
+int ghmm_autotune(ghmm_ctx *ctx, const ghmm_flat *sample, const ghmm_tuning *candidates, int32_t n_candidates,
+                  int32_t reps, ghmm_tuning *best, double *ms) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!sample || sample->n_regions <= 0 || n_candidates < 0 || (n_candidates > 0 && !candidates))
+        return fail(ctx, GHMM_ERR_ARG, "bad arguments");
+    if (ctx->open_queues.load() > (ctx->pipe ? 1 : 0))
+        return fail(ctx, GHMM_ERR_STATE, "the tuning cannot change while a queue is open");
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    std::vector<ghmm_tuning> cand;
+    if (n_candidates > 0) {
+        cand.assign(candidates, candidates + n_candidates);
+    } else {  // the built-in grid: rows per lane of single- and multi-strip reads, haplotype columns per task
+        for (int mk : {8, 6, 4})
+            for (int mm : {8, 6, 4})
+                for (int cc : {16384, 4096}) cand.push_back(ghmm_tuning{mk, mm, cc, 0});
+    }
+    reps = reps > 0 ? reps : 3;
+    const int old_k = ctx->max_k, old_m = ctx->max_k_multi, old_c = ctx->chunk_cols;
+    const int mode = ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN;
+    Source src;
+    src.flat = sample;
+    src.n_regions = sample->n_regions;
+    ghmm_batch tb;
+    int rc = GHMM_OK, best_i = -1;
+    double best_ms = 0;
+    for (size_t i = 0; i < cand.size() && !rc; i++) {
+        const ghmm_tuning &t = cand[i];
+        const int mk = t.max_rows_per_lane ? t.max_rows_per_lane : kMaxK32;
+        const int mm = t.max_rows_per_lane_multi ? t.max_rows_per_lane_multi : kMaxK32;
+        const int cc = t.chunk_cols ? t.chunk_cols : 16384;
+        if (mk < 1 || mk > kMaxK32 || mm < 1 || mm > kMaxK32 || cc < 1) {
+            rc = fail(ctx, GHMM_ERR_ARG, "tuning candidate out of range (rows per lane 1..8, chunk_cols >= 1)");
+            break;
+        }
+        ctx->max_k = mk;
+        ctx->max_k_multi = mm;
+        ctx->chunk_cols = cc;
+        rc = batch_marshal(ctx, src, tb);
+        if (!rc) rc = batch_upload(ctx, tb, ctx->stream);
+        if (!rc) rc = batch_forward(ctx, tb, mode);  // warm-up (graph capture)
+        std::vector<double> times;
+        for (int r = 0; r < reps && !rc; r++) {
+            rc = batch_forward(ctx, tb, mode);
+            times.push_back(tb.ms_total);
+        }
+        if (rc) break;
+        std::sort(times.begin(), times.end());
+        const double med = times[times.size() / 2];
+        if (ms) ms[i] = med;
+        if (best_i < 0 || med < best_ms) {
+            best_i = (int)i;
+            best_ms = med;
+        }
+        cand[i] = ghmm_tuning{mk, mm, cc, 0};
+    }
+    cudaStreamSynchronize(ctx->stream);
+    tb.release();
+    if (rc || best_i < 0) {
+        ctx->max_k = old_k;
+        ctx->max_k_multi = old_m;
+        ctx->chunk_cols = old_c;
+        return rc ? rc : fail(ctx, GHMM_ERR_ARG, "no candidate");
+    }
+    ctx->max_k = cand[(size_t)best_i].max_rows_per_lane;
+    ctx->max_k_multi = cand[(size_t)best_i].max_rows_per_lane_multi;
+    ctx->chunk_cols = cand[(size_t)best_i].chunk_cols;
+    if (best) *best = cand[(size_t)best_i];
+    return GHMM_OK;
+}
+
+int ghmm_get_tuning(ghmm_ctx *ctx, ghmm_tuning *t) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!t) return fail(ctx, GHMM_ERR_ARG, "NULL tuning");
+    *t = ghmm_tuning{ctx->max_k, ctx->max_k_multi, ctx->chunk_cols, 0};
+    return GHMM_OK;
+}
+
 int ghmm_queue_create(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **queue) {
     if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
     if (!queue || batch_cells < 0) return fail(ctx, GHMM_ERR_ARG, "bad arguments");

@@ -121,6 +121,9 @@ _SIGS = {
                                                 ctypes.POINTER(Hap), ctypes.c_int32, _f64p]),
     "ghmm_done": (ctypes.c_int, [ctypes.c_void_p]),
     "ghmm_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
+    "ghmm_get_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
+    "ghmm_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Flat), ctypes.POINTER(Tuning), ctypes.c_int32,
+                                     ctypes.c_int32, ctypes.POINTER(Tuning), _f64p]),
     "ghmm_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
     "ghmm_compute_regions": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Region), ctypes.c_int32, _f64p]),
     "ghmm_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Region), ctypes.c_int32,

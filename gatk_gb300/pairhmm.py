@@ -139,6 +139,8 @@ class Engine:
     def __init__(self, device: int = 0, max_threads: int = 0, use_double_precision: bool = False):
         self._ctx = _Context(PairHMMNativeArguments(max_threads, use_double_precision, device))
         self.L = self._ctx.L
+        self.device = device
+        self.double_precision = use_double_precision
 
     @property
     def handle(self):
@@ -163,6 +165,17 @@ class Engine:
         """FP32 launch shape for batches created afterwards (0 keeps a field's default)."""
         t = native.Tuning(max_rows_per_lane, max_rows_per_lane_multi, chunk_cols, 0)
         native.check(self.L.ghmm_set_tuning(self._ctx.h, ctypes.byref(t)), self._ctx.h)
+
+    def get_tuning(self) -> tuple[int, int, int]:
+        t = native.Tuning()
+        native.check(self.L.ghmm_get_tuning(self._ctx.h, ctypes.byref(t)), self._ctx.h)
+        return t.max_rows_per_lane, t.max_rows_per_lane_multi, t.chunk_cols
+
+    def autotune(self, wl: Workload, **kw) -> dict:
+        """Pick and set the fastest launch shape for workloads shaped like `wl` (gatk_gb300.autotune)."""
+        from . import autotune
+
+        return autotune.autotune(self, wl, device=self.device, **kw)
 
     def batch(self, wl: Workload, via_regions: bool = False) -> "Batch":
         return Batch(self, wl, via_regions)

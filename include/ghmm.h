@@ -148,6 +148,16 @@ int ghmm_compute_likelihoods(ghmm_ctx *ctx, const ghmm_read *reads, int32_t n_re
 
 /* Set the FP32 launch shape used by batches created after this call (see ghmm_tuning). */
 int ghmm_set_tuning(ghmm_ctx *ctx, const ghmm_tuning *tuning);
+int ghmm_get_tuning(ghmm_ctx *ctx, ghmm_tuning *tuning);
+
+/* Autotuner (no counterpart in the reference, which has no launch shape to choose): time every candidate
+ * tuning on a sample of the caller's workload -- marshal with that tuning, one warm-up forward, then the
+ * median device time of reps forwards (0: 3) -- set the fastest on ctx and return it in *best.
+ * candidates NULL / n_candidates 0 selects the built-in grid: max_rows_per_lane {8, 6, 4} x
+ * max_rows_per_lane_multi {8, 6, 4} x chunk_cols {16384, 4096}, in that order; ms (may be NULL) receives
+ * each candidate's median milliseconds.  The sample should hold a few times 1e10 cells. */
+int ghmm_autotune(ghmm_ctx *ctx, const ghmm_flat *sample, const ghmm_tuning *candidates, int32_t n_candidates,
+                  int32_t reps, ghmm_tuning *best, double *ms);
 
 /* PairHMMNativeBinding.done: release the context. */
 int ghmm_done(ghmm_ctx *ctx);
