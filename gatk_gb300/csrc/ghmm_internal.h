@@ -82,7 +82,12 @@ int launch_fp64_queue(const DevTables &t, const DevBatch &b, int grid, int block
 int launch_finalize_fp32(double *out, const int64_t *n_out, int sm_count, cudaStream_t s);
 int launch_plain_region(const DevTables &t, const DevBatch &b, int region, int n_reads, int n_haps, int max_read_len,
                         cudaStream_t s);
-constexpr int kPlainMaxRead = 1024;
+constexpr int kPlainMaxRead = 2048;
+// Rows below each read in the FP32 layout that accumulate the haplotype sum (kernels.cu).
+constexpr int kAccRows = 2;
+// Zero bytes on both sides of the column-code plane, so the FP32 kernel may load a code one step ahead
+// (and lanes that have not started may load before the first column) without leaving the allocation.
+constexpr int kCodePad = 64;
 int fp32_kernel_occupancy(int k, int block, int *blocks_per_sm);
 int fp64_kernel_occupancy(int block, int *blocks_per_sm);
 int measure_peaks_device(int sm_count, double *fp32, double *fp32x2, double *fp64, cudaStream_t s);

@@ -13,8 +13,9 @@
 //    one region, packed into the .x/.y halves of float2 so every cell update is a packed FFMA2/FMUL2/FADD2,
 //    against all (or a chunk of) the region's haplotypes streamed back to back.  Lane l owns K consecutive
 //    rows; at step s it computes column c = s - l, receiving the row above from lane l-1 by __shfl_up_sync
-//    (an anti-diagonal wavefront).  Reads are padded at the top with "dummy" rows that reproduce the row-0
-//    boundary, so the last read row always sits in lane 31's last slot.  Reads longer than 32*K rows run
+//    (an anti-diagonal wavefront).  Each read is followed by two accumulator rows that sum the last row over
+//    the haplotype (row_coef), and padded at the top with "dummy" rows that reproduce the row-0 boundary, so
+//    the accumulator rows always sit in lane 31's last two slots.  Reads longer than 32*K rows run
 //    as several strips whose boundary row goes through per-warp global scratch.  Each row's states are
 //    rescaled so a cell costs 5 FMA-pipe operations instead of 8: with a_0 = 1, a_i = a_{i-1} / MM_i,
 //       M~ = a_i M,   I~ = (a_{i-1} / MI_i) I,   D~ = (a_i / MD_i) D,
@@ -75,18 +76,38 @@ __device__ __constant__ uint32_t kBaseMask[kBases] = {1u, 2u, 4u, 8u, 15u};
 
 // Per-row coefficients of one read half (see header comment); dummy rows reproduce the row-0 boundary.
 struct RowCoef {
-    float pm, pe, b, c, e, dd, lmm, kappa;
+    float pm, pe, b, c, e, dd, lmm;
     uint32_t code;
 };
 
+// Rows p = R and p = R + 1 below a read of R bases are its accumulator rows (kAccRows): row R+1 has prior 0
+// and e = MI_R / MM_R, so I~(R+1, j) = M~(R, j) + (MI_R / MM_R) I~(R, j) = a_R (M + I)(R, j); row R+2 has
+// prior 1, b = 1, c = 0, DD = 1, so M~(R+2, j) = I~(R+1, j-1) and D~(R+2, j) runs the sum over columns.  At a
+// haplotype's last column H the likelihood numerator is D~(R+2, H) + M~(R+2, H) + I~(R+1, H) (sums through
+// columns H-2, H-1 and H), and no per-step accumulation is left in the wavefront.
 __device__ __forceinline__ RowCoef row_coef(const DevTables &T, const DevBatch &B, int64_t off, int R, int p) {
     RowCoef c;
-    if (p < 0 || p >= R) {
+    c.lmm = 0.f;
+    c.code = 0u;
+    if (p < 0 || p > R + 1 || R == 0) {  // dummy row: holds the row-0 boundary
         c.pm = c.pe = 0.f;
         c.b = c.c = c.e = 0.f;
         c.dd = 1.f;
-        c.lmm = c.kappa = 0.f;
-        c.code = 0u;
+        return c;
+    }
+    if (p == R) {  // accumulator row R+1
+        const uint8_t ins = B.ins[off + R - 1], del = B.dels[off + R - 1];
+        c.pm = c.pe = 0.f;
+        c.b = c.c = 0.f;
+        c.e = __ldg(T.err_f + ins) / __ldg(T.m2m_f + ins * 128 + del);
+        c.dd = 0.f;
+        return c;
+    }
+    if (p == R + 1) {  // accumulator row R+2
+        c.pm = c.pe = 1.f;
+        c.b = 1.f;
+        c.c = c.e = 0.f;
+        c.dd = 1.f;
         return c;
     }
     const uint8_t base = B.bases[off + p], q = B.quals[off + p];
@@ -107,7 +128,6 @@ __device__ __forceinline__ RowCoef row_coef(const DevTables &T, const DevBatch &
     c.e = (p > 0) ? ii * mi_p / (mi * mm_p) : 0.f;
     c.dd = ii;
     c.lmm = -log2f(mm);
-    c.kappa = mi / mm;
     c.code = base_code(base);
     return c;
 }
@@ -156,7 +176,6 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
     const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     float2 *scratch = nullptr;
     if (MULTI) scratch = B.scratch32 + warp_global * B.scratch32_cols * 3;
-    const float2 nl0 = lane ? make_float2(1.f, 1.f) : zero2();
 
     for (;;) {
         int t = 0;
@@ -187,7 +206,7 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
 
         for (int strip = 0; strip < nstrips; ++strip) {
             float2 cb[K], cc[K], ce[K], cdd[K];
-            float2 kappa = zero2(), lsum = zero2();
+            float2 lsum = zero2();
             __syncwarp();  // the previous strip's steps have finished reading this warp's table
 #pragma unroll
             for (int k = 0; k < K; ++k) {
@@ -200,7 +219,6 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                 cdd[k] = make_float2(a.dd, b.dd);
                 lsum.x += a.lmm;
                 lsum.y += b.lmm;
-                if (k == K - 1) kappa = make_float2(a.kappa, b.kappa);
 #pragma unroll
                 for (int h = 0; h < kBases; ++h) {
                     const uint32_t hm = kBaseMask[h];
@@ -220,7 +238,6 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
             for (int k = 0; k < K; ++k) Mp[k] = Ip[k] = Dp[k] = zero2();
             float2 gM = zero2(), gI = zero2(), gD = zero2();  // row above, previous column (diagonal)
             float2 bnd = zero2();                               // lane 0, strip 0: row-0 D~ boundary
-            float2 accM = zero2(), accI = zero2();
             int hap = task.hap_begin - 1;
             const bool last_strip = (strip == nstrips - 1);
             float2 nxM = zero2(), nxI = zero2(), nxD = zero2();  // prefetched strip boundary (MULTI, lane 0)
@@ -230,6 +247,9 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                 nxD = scratch[2];
             }
             const int nsteps = ncols + 31;
+            // column code of the next step, loaded one step ahead (the code plane has kCodePad bytes on
+            // both sides, so columns just outside the stream are readable; CHK steps mask them)
+            uint32_t code_next = (uint32_t)__ldg(stream - lane);
             // One wavefront step.  CHK steps handle columns outside the stream (lanes that have not started
             // or have finished), haplotype starts (state reset) and ends (lane 31 emits); they are needed
             // only in the 32 steps after each haplotype start, where those events fall.  Every other step
@@ -238,12 +258,11 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                 constexpr bool CHK = decltype(chk_tag)::value;
                 const int c = s - lane;
                 bool valid = true;
-                uint32_t code;
+                uint32_t code = code_next;
+                code_next = (uint32_t)__ldg(stream + c + 1);
                 if constexpr (CHK) {
                     valid = (c >= 0) && (c < ncols);
-                    code = valid ? (uint32_t)__ldg(stream + c) : 0u;
-                } else {
-                    code = (uint32_t)__ldg(stream + c);
+                    code = valid ? code : 0u;
                 }
                 // row above at this column: lane l-1's last row as computed last step.  Shuffled before
                 // this lane resets its own state at a haplotype start, since lane l+1 still needs the
@@ -267,24 +286,25 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                         gM = gI = zero2();
                         gD = make_float2((slot0 - 1 < task.pad_a) ? X.x : 0.f, (slot0 - 1 < task.pad_b) ? X.y : 0.f);
                         if (lane == 0 && strip == 0) bnd = X;
-                        accM = accI = zero2();
                     }
                 }
                 // lane 0 takes the row-0 boundary (strip 0) or the previous strip's last row instead
+                // (selects on the ALU pipe, not multiplies on the FMA pipe)
                 if (MULTI && strip > 0) {
-                    const float2 bM = nxM, bI = nxI, bD = nxD;
-                    if (lane == 0 && c + 1 < ncols) {
-                        nxM = scratch[3 * (c + 1) + 0];
-                        nxI = scratch[3 * (c + 1) + 1];
-                        nxD = scratch[3 * (c + 1) + 2];
+                    if (lane == 0) {
+                        uM = nxM;
+                        uI = nxI;
+                        uD = nxD;
+                        if (c + 1 < ncols) {
+                            nxM = scratch[3 * (c + 1) + 0];
+                            nxI = scratch[3 * (c + 1) + 1];
+                            nxD = scratch[3 * (c + 1) + 2];
+                        }
                     }
-                    uM = fma2(uM, nl0, bM);
-                    uI = fma2(uI, nl0, bI);
-                    uD = fma2(uD, nl0, bD);
-                } else {
-                    uM = mul2(uM, nl0);
-                    uI = mul2(uI, nl0);
-                    uD = fma2(uD, nl0, bnd);
+                } else if (lane == 0) {
+                    uM = zero2();
+                    uI = zero2();
+                    uD = bnd;
                 }
                 const float2 *pri = prior_tbl + (code & 7u) * 32;
                 // pass 1 (bottom-up so the row above is still the previous column): M and D^
@@ -308,15 +328,14 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                     aM = Mp[k];
                     aI = In;
                 }
+                const float2 i_acc = (K >= 2) ? Ip[K >= 2 ? K - 2 : 0] : uI;  // I~(R+1) at this column
                 gM = uM;
                 gI = uI;
                 gD = uD;
                 if (last_strip) {
-                    accM = add2(accM, Mp[K - 1]);
-                    accI = add2(accI, Ip[K - 1]);
                     if constexpr (CHK) {
                         if (lane == 31 && (code & kColLast)) {
-                            const float2 t = fma2(kappa, accI, accM);
+                            const float2 t = add2(add2(Dp[K - 1], Mp[K - 1]), i_acc);
                             emit_fp32(B, t.x, la.x, ra, hap, out_a + hap);
                             if (rb >= 0) emit_fp32(B, t.y, la.y, rb, hap, out_b + hap);
                         }
@@ -511,12 +530,13 @@ __global__ void __launch_bounds__(128) fp64_queue_kernel(DevTables T, DevBatch B
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Plain FP64 form: one (read, haplotype) pair per 256-thread block; thread t owns rows t+1+256m (m<4);
-// three rolling anti-diagonals of M, I, D in shared memory; one barrier per diagonal; Java's order of
-// operations (no fused multiply-add), so the sums equal the FP64 oracle's.
+// Plain FP64 form: one (read, haplotype) pair per 256-thread block; thread t owns rows t+1+256m (m<ROWS:
+// 4 rows for reads up to 1024 bases, 8 up to 2048); three rolling anti-diagonals of M, I, D in shared
+// memory; one barrier per diagonal; Java's order of operations (no fused multiply-add), so the sums equal
+// the FP64 oracle's.
 constexpr int kPlainThreads = 256;
-constexpr int kPlainRows = 4;
 
+template <int kPlainRows>
 __global__ void __launch_bounds__(kPlainThreads) plain_fp64_kernel(DevTables T, DevBatch B, int region, int nh) {
     extern __shared__ double sm[];
     const int pair = blockIdx.x;
@@ -726,12 +746,18 @@ int fp64_kernel_occupancy(int block, int *blocks_per_sm) {
 int launch_plain_region(const DevTables &t, const DevBatch &b, int region, int n_reads, int n_haps,
                               int max_read_len, cudaStream_t s) {
     if (n_reads <= 0 || n_haps <= 0) return 0;
+    if (max_read_len > kPlainMaxRead) return (int)cudaErrorInvalidValue;
     const size_t smem = sizeof(double) * 9 * (size_t)(max_read_len + 1);
+    const bool wide = max_read_len > 4 * kPlainThreads;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(plain_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = wide ? cudaFuncSetAttribute(plain_fp64_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                             : cudaFuncSetAttribute(plain_fp64_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return (int)e;
     }
-    plain_fp64_kernel<<<n_reads * n_haps, kPlainThreads, smem, s>>>(t, b, region, n_haps);
+    if (wide)
+        plain_fp64_kernel<8><<<n_reads * n_haps, kPlainThreads, smem, s>>>(t, b, region, n_haps);
+    else
+        plain_fp64_kernel<4><<<n_reads * n_haps, kPlainThreads, smem, s>>>(t, b, region, n_haps);
     return (int)cudaGetLastError();
 }
 

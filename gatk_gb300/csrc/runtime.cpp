@@ -140,7 +140,7 @@ struct Bucket {
 struct ghmm_batch {
     // host (pinned) staging
     HostBuf<uint8_t> h_planes;  // 5 planes back to back
-    HostBuf<uint8_t> h_hap;     // raw bytes then codes
+    HostBuf<uint8_t> h_hap;     // raw bytes, kCodePad bytes, codes, kCodePad bytes
     HostBuf<int64_t> h_off;     // read_off | hap_off | region_read_off | region_hap_off | out_off
     HostBuf<int32_t> h_read_region;
     HostBuf<float> h_init_f;
@@ -345,7 +345,7 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
     const int threads = hw_threads(ctx->max_threads);
 
     GHMM_CUDA(b.h_planes.reserve((size_t)b.read_bytes * 5), "pinned read planes");
-    GHMM_CUDA(b.h_hap.reserve((size_t)b.hap_bytes * 2), "pinned haplotypes");
+    GHMM_CUDA(b.h_hap.reserve((size_t)b.hap_bytes * 2 + 2 * kCodePad), "pinned haplotypes");
     const size_t n_off = (size_t)(NR + 1) + (size_t)(NH + 1) + 3 * (size_t)(G + 1);
     GHMM_CUDA(b.h_off.reserve(n_off), "pinned offsets");
     GHMM_CUDA(b.h_read_region.reserve((size_t)NR), "pinned read regions");
@@ -357,7 +357,9 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
     uint8_t *P = b.h_planes.p;
     const int64_t RB = b.read_bytes;
     uint8_t *pb = P, *pq = P + RB, *pi = P + 2 * RB, *pd = P + 3 * RB, *pg = P + 4 * RB;
-    uint8_t *hraw = b.h_hap.p, *hcode = b.h_hap.p + b.hap_bytes;
+    uint8_t *hraw = b.h_hap.p, *hcode = b.h_hap.p + b.hap_bytes + kCodePad;
+    memset(hcode - kCodePad, 0, kCodePad);
+    memset(hcode + b.hap_bytes, 0, kCodePad);
     int64_t *o = b.h_off.p;
     std::copy(read_off.begin(), read_off.end(), o);
     std::copy(hap_off.begin(), hap_off.end(), o + NR + 1);
@@ -498,12 +500,14 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                     po.cells_direct += (int64_t)R * region_cols;
                     continue;
                 }
+                // rows of the layout: the read plus its two accumulator rows (kernels.cu)
+                const int rows = R + kAccRows;
                 int key, ns = 1;
-                if (R <= 32 * max_k) {
-                    key = (R + 31) / 32;
+                if (rows <= 32 * max_k) {
+                    key = (rows + 31) / 32;
                 } else {  // fewest strips of at most max_k_multi rows per lane, then the fewest rows per lane
-                    ns = (R + 32 * max_k_multi - 1) / (32 * max_k_multi);
-                    key = ((R + 32 * ns - 1) / (32 * ns)) | 16;
+                    ns = (rows + 32 * max_k_multi - 1) / (32 * max_k_multi);
+                    key = ((rows + 32 * ns - 1) / (32 * ns)) | 16;
                 }
                 // reads are paired only within one (rows per lane, strip count) class
                 groups.emplace_back(((int64_t)key * 4096 + ns) * 100000 + R, r);
@@ -531,7 +535,7 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                 const int S = 32 * K;
                 const int Ra = (int)(read_off[(size_t)ra + 1] - read_off[(size_t)ra]);
                 const int Rb = rb >= 0 ? (int)(read_off[(size_t)rb + 1] - read_off[(size_t)rb]) : 0;
-                const int nstrips = multi ? (std::max(Ra, Rb) + S - 1) / S : 1;
+                const int nstrips = multi ? (std::max(Ra, Rb) + kAccRows + S - 1) / S : 1;
                 for (auto &ch : chunks) {
                     F32Task t;
                     t.read_a = (int32_t)ra;
@@ -541,8 +545,8 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                     t.region = (int32_t)g;
                     t.nstrips = (int16_t)nstrips;
                     t.k = (int16_t)K;
-                    t.pad_a = nstrips * S - Ra;
-                    t.pad_b = rb >= 0 ? nstrips * S - Rb : nstrips * S;
+                    t.pad_a = nstrips * S - Ra - kAccRows;
+                    t.pad_b = rb >= 0 ? nstrips * S - Rb - kAccRows : nstrips * S;
                     const int64_t cols = hap_off[(size_t)ch.second] - hap_off[(size_t)ch.first];
                     if (multi) po.max_multi_cols = std::max(po.max_multi_cols, cols);
                     po.tasks[key].push_back(t);
@@ -619,7 +623,7 @@ static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
     const int64_t NR = b.n_reads, NH = b.n_haps, G = b.n_regions;
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     GHMM_CUDA(b.d_planes.reserve((size_t)b.read_bytes * 5), "device read planes");
-    GHMM_CUDA(b.d_hap.reserve((size_t)b.hap_bytes * 2), "device haplotypes");
+    GHMM_CUDA(b.d_hap.reserve((size_t)b.hap_bytes * 2 + 2 * kCodePad), "device haplotypes");
     const size_t n_off = (size_t)(NR + 1) + (size_t)(NH + 1) + 3 * (size_t)(G + 1);
     GHMM_CUDA(b.d_off.reserve(n_off), "device offsets");
     GHMM_CUDA(b.d_read_region.reserve((size_t)NR), "device read regions");
@@ -640,7 +644,8 @@ static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
     GHMM_CUDA(b.d_scratch64.reserve(s64), "device FP64 strip scratch");
 
     GHMM_CUDA(cudaMemcpyAsync(b.d_planes.p, b.h_planes.p, (size_t)b.read_bytes * 5, cudaMemcpyHostToDevice, s), "H2D planes");
-    GHMM_CUDA(cudaMemcpyAsync(b.d_hap.p, b.h_hap.p, (size_t)b.hap_bytes * 2, cudaMemcpyHostToDevice, s), "H2D haplotypes");
+    GHMM_CUDA(cudaMemcpyAsync(b.d_hap.p, b.h_hap.p, (size_t)b.hap_bytes * 2 + 2 * kCodePad, cudaMemcpyHostToDevice, s),
+              "H2D haplotypes");
     GHMM_CUDA(cudaMemcpyAsync(b.d_off.p, b.h_off.p, n_off * sizeof(int64_t), cudaMemcpyHostToDevice, s), "H2D offsets");
     if (NR) GHMM_CUDA(cudaMemcpyAsync(b.d_read_region.p, b.h_read_region.p, (size_t)NR * 4, cudaMemcpyHostToDevice, s), "H2D regions");
     if (NH) {
@@ -650,7 +655,7 @@ static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
     if (b.n_tasks)
         GHMM_CUDA(cudaMemcpyAsync(b.d_tasks.p, b.h_tasks.p, (size_t)b.n_tasks * sizeof(F32Task), cudaMemcpyHostToDevice, s), "H2D tasks");
 
-    b.upload_bytes = b.read_bytes * 5 + b.hap_bytes * 2 + (int64_t)n_off * 8 + NR * 4 + NH * 12 +
+    b.upload_bytes = b.read_bytes * 5 + b.hap_bytes * 2 + 2 * kCodePad + (int64_t)n_off * 8 + NR * 4 + NH * 12 +
                      b.n_tasks * (int64_t)sizeof(F32Task);
     DevBatch &d = b.dev;
     const int64_t RB = b.read_bytes;
@@ -661,7 +666,7 @@ static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
     d.gcp = b.d_planes.p + 4 * RB;
     d.read_off = b.d_off.p;
     d.hap_bases = b.d_hap.p;
-    d.hap_code = b.d_hap.p + b.hap_bytes;
+    d.hap_code = b.d_hap.p + b.hap_bytes + kCodePad;
     d.hap_off = b.d_off.p + NR + 1;
     d.hap_init_f = b.d_init_f.p;
     d.hap_init_d = b.d_init_d.p;
@@ -715,7 +720,7 @@ static int batch_forward(ghmm_ctx *ctx, ghmm_batch &b, int mode) {
     b.forward_h2d = b.forward_d2h = 0;
     if (mode == GHMM_MODE_PLAIN_FP64) {
         if (b.max_read_len > kPlainMaxRead)
-            return fail(ctx, GHMM_ERR_ARG, "the plain FP64 kernel supports reads up to 1024 bases");
+            return fail(ctx, GHMM_ERR_ARG, "the plain FP64 kernel supports reads up to 2048 bases");
         const int64_t *o = b.h_off.p;
         const int64_t *rro = o + b.n_reads + 1 + b.n_haps + 1, *rho = rro + b.n_regions + 1;
         for (int64_t g = 0; g < b.n_regions; g++) {

@@ -55,7 +55,7 @@ extern "C" {
 /* Forward modes for ghmm_batch_forward. */
 #define GHMM_MODE_FP32_RERUN 0 /* batched FP32 wavefront + FP64 rerun of underflowing pairs (default) */
 #define GHMM_MODE_FP64 1       /* every pair in the FP64 wavefront kernel (useDoublePrecision) */
-#define GHMM_MODE_PLAIN_FP64 2 /* plain FP64 kernel, one pair per thread block, one launch per region */
+#define GHMM_MODE_PLAIN_FP64 2 /* plain FP64 kernel, one pair per thread block, one launch per region; reads <= 2048 */
 
 /* Mirrors PairHMMNativeArguments {maxNumberOfThreads, useDoublePrecision}
  * (HC/PairHMMNativeArgumentCollection.java:11-23) plus the device to use. */
