@@ -353,11 +353,14 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
             while (s < nsteps) {
                 while (j <= nh_task && (int)(hoff[j] - col0) <= s) ++j;
                 const int window_end = min((int)(hoff[j - 1] - col0) + 32, nsteps);
+                // unrolled by two: the scheduler interleaves one step's I~ chain with the next step's M~ and D~
                 if (s < window_end) {
+#pragma unroll 2
                     for (; s < window_end; ++s) step(s, std::true_type{});
                     continue;
                 }
                 const int next_boundary = (j <= nh_task) ? (int)(hoff[j] - col0) : nsteps;
+#pragma unroll 2
                 for (; s < next_boundary; ++s) step(s, std::false_type{});
             }
             if (MULTI) __syncwarp();
