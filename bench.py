@@ -3,6 +3,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload 1]
     python bench.py --stream [--regions N] [--batch-cells C]     (workload 4 through the streaming queue)
+    python bench.py --calib                                      (workload 3: calibration forward + backward)
 
 A step is one forward over the whole workload (default: workload 1, 10,000 synthetic active regions,
 seed 1, ~1.06e12 cells): every read x haplotype pair of every region, FP32 wavefront plus the FP64 rerun
@@ -460,6 +461,98 @@ def run_stream(args):
     return 0
 
 
+def run_calib(args):
+    """--calib: workload 3 (4,096 read x haplotype pairs around short tandem repeats).  Times the FP32
+    forward and the forward + hand-written backward (ghmm_calib_*, through the torch.autograd.Function) and
+    checks the gradient of sum log10 L with respect to the 8 x 20 x 2 (period, repeat) table against FP64
+    central differences (step 1e-4, FP64 forward on the GPU) and against the FP64 oracle's adjoint."""
+    import numpy as np
+    import torch
+
+    from gatk_gb300 import calibration as C, workload as W
+    from gatk_gb300.pairhmm import Engine
+    from oracle import oracle as O
+
+    eng = Engine()
+    wl = W.generate(3)
+    cs = C.CalibrationSet(wl)
+    cells = int(cs.cells)
+    theta = C.default_theta().to(cs.device)
+
+    def timed(fn, reps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps
+
+    def fwd():
+        with torch.no_grad():
+            C.log10_likelihoods(theta, cs, eng, precision=0)
+
+    def fwd_bwd():
+        t = theta.detach().requires_grad_(True)
+        C.log10_likelihoods(t, cs, eng, precision=0).sum().backward()
+
+    reps = max(args.steps, 10)
+    dt_f = timed(fwd, reps)
+    dt_fb = timed(fwd_bwd, reps)
+    # gradient checks
+    t = theta.detach().requires_grad_(True)
+    C.log10_likelihoods(t, cs, eng, precision=0).sum().backward()
+    grad = t.grad.detach().cpu().numpy().reshape(-1, 2)
+    used = np.bincount(cs.param_index_np[cs.param_index_np >= 0], minlength=160)
+    order = np.argsort(-used)[:8]
+    h = 1e-4
+    scale = np.abs(grad).max()
+    fd_rel = 0.0
+    with torch.no_grad():
+        for k in order:
+            for comp in (0, 1):
+                tp, tm = theta.clone(), theta.clone()
+                tp.view(-1, 2)[k, comp] += h
+                tm.view(-1, 2)[k, comp] -= h
+                sp = float(C.log10_likelihoods(tp, cs, eng, precision=1).sum())
+                sm = float(C.log10_likelihoods(tm, cs, eng, precision=1).sum())
+                step = float(tp.view(-1, 2)[k, comp].double() - tm.view(-1, 2)[k, comp].double())
+                fd = (sp - sm) / step
+                fd_rel = max(fd_rel, abs(grad[k, comp] - fd) / max(abs(fd), 1e-2 * scale))
+    # per-position gradients against the FP64 oracle's adjoint on a sample of pairs
+    g, c = cs.position_params(theta)
+    g = g.detach().requires_grad_(True)
+    c = c.detach().requires_grad_(True)
+    fn = C._function() if C._FN is None else C._FN
+    fn.apply(g, c, cs, eng, 0).sum().backward()
+    gg, gc = g.grad.cpu().numpy(), c.grad.cpu().numpy()
+    gn, cn = g.detach().cpu().numpy(), c.detach().cpu().numpy()
+    pr, ph = wl.pair_index()
+    oracle_rel = 0.0
+    for p in range(0, cs.n_pairs, 128):
+        r, hh = int(pr[p]), int(ph[p])
+        a, b = int(wl.read_off[r]), int(wl.read_off[r + 1])
+        _, dg, dc = O.cont_grad(wl.hap(hh), wl.bases[a:b], wl.quals[a:b], gn[a:b].astype(np.float64),
+                                cn[a:b].astype(np.float64))
+        sc = max(np.abs(dg).max(), np.abs(dc).max())
+        oracle_rel = max(oracle_rel, np.abs(gg[a:b] - dg).max() / sc, np.abs(gc[a:b] - dc).max() / sc)
+    line = {
+        "metric": "PairHMM calibration: FP32 forward + hand-written backward, GCUPS", "value": cells / dt_fb / 1e9,
+        "unit": "GCUPS", "n_gpus": 1, "steps": reps, "warmup": args.warmup, "ms_per_step": dt_fb * 1e3,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic (workload 3: STR regions, seed 3)",
+        "config": {"workload": "config3: 4,096 read x haplotype pairs, 150 bp reads, 300 bp STR haplotypes",
+                   "pairs": cs.n_pairs, "cells": cells, "parameters": "8 x 20 x 2 (period, repeat) log10 table"},
+        "forward_gcups": cells / dt_f / 1e9, "forward_ms": dt_f * 1e3,
+        "gradient_vs_fp64_central_differences": {"max_rel": float(fd_rel), "params": int(len(order) * 2), "step": h,
+                                                 "budget": 1e-3},
+        "gradient_vs_fp64_oracle_adjoint": {"max_rel": float(oracle_rel), "sample_pairs": len(range(0, cs.n_pairs, 128))},
+    }
+    print(json.dumps(line), flush=True)
+    eng.close()
+    return 0
+
+
 def absdiff(got, ref):
     """|got - ref|, where equal infinities count as 0: a pair whose likelihood underflows even the FP64
     2^1020 scale is -Infinity in LoglessPairHMM too."""
@@ -504,6 +597,8 @@ def main():
     ap.add_argument("--stream", action="store_true",
                     help="push the workload one region at a time through the queue (default workload 4)")
     ap.add_argument("--batch-cells", type=float, default=2e11, help="queue batch size in cells (--stream)")
+    ap.add_argument("--calib", action="store_true",
+                    help="time the calibration forward + backward on workload 3 and check its gradient")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -513,6 +608,8 @@ def main():
         return run_reference(args)
     if args.stream:
         return run_stream(args)
+    if args.calib:
+        return run_calib(args)
     return run_ours(args)
 
 

@@ -88,6 +88,8 @@ constexpr int kAccRows = 2;
 // Zero bytes on both sides of the column-code plane, so the FP32 kernel may load a code one step ahead
 // (and lanes that have not started may load before the first column) without leaving the allocation.
 constexpr int kCodePad = 64;
+// Largest insertion-state growth bound G (I~ <= G max M~) the rescaled FP64 tier takes (headroom 2^60).
+constexpr double kMaxGrowth64 = 1e10;
 int fp32_kernel_occupancy(int k, int block, int *blocks_per_sm);
 int fp64_kernel_occupancy(int block, int *blocks_per_sm);
 int measure_peaks_device(int sm_count, double *fp32, double *fp32x2, double *fp64, cudaStream_t s);

@@ -28,8 +28,9 @@
 //    coefficients appear; log2 a_R is summed per read.  Reads whose I~ could outgrow FP32 (steeply rising
 //    insertion penalties) or whose MM is 0 are sent to FP64 by the host.
 //    Scale 2^120; a sum below GHMM_FP32_RERUN_THRESHOLD (or not finite) queues the pair for FP64.
-//  * fp64_queue_kernel<K>: the FP64 wavefront (one pair per warp, scale 2^1020, unscaled rows so any
-//    gap-continuation penalty, including 0, is exact), used for reruns and double-precision mode.
+//  * fp64_queue_kernel<K, RESCALED>: the FP64 wavefront, one pair per warp, used for reruns and
+//    double-precision mode: a rescaled tier (5 DP operations per cell) and an exact unscaled tier (scale
+//    2^1020, LoglessPairHMM's magnitudes) for results near the bottom of the FP64 range.
 //  * plain_fp64_kernel: the plain form, one pair per thread block sweeping anti-diagonals through shared
 //    memory with a block barrier per diagonal, Java's operation order, one launch per region.
 #include <cuda_runtime.h>
@@ -380,20 +381,38 @@ __global__ void finalize_fp32_kernel(double *out, const int64_t *n_out) {
 }
 
 // ---------------------------------------------------------------------------------------------------
-// FP64 wavefront, one (read, haplotype) pair per warp, K rows per lane, strips of 32*K rows.
-template <int K>
+// FP64 wavefront, one (read, haplotype) pair per warp, K rows per lane, strips of 32*K rows, in two tiers.
+//
+// RESCALED (queue 1: host-routed pairs and FP32 underflows): the FP32 kernel's rescaled recurrence in FP64,
+// 5 DP operations per cell instead of 8 (the FP64 pipe runs at 1/64 of the FP32 rate on this part):
+//    M~ = prior * fma(I~_diag, b_i, fma(D~_diag, c_i, M~_diag)),  I~ = fma(I~_up, e_i, M~_up),
+//    D~ = fma(D~_left, DD_i, M~_left),  sum over the haplotype of M~_R + (MI_R / MM_R) I~_R.
+// The scale is S' = 2^960 instead of 2^1020 (headroom for I~ and D~, which carry 1 / MI and 1 / MD), and the
+// initial condition is divided by 2^round(la), la = log2 a_R = sum of -log2 MM_i, so that the last row sits at
+// scale S' like the unscaled recurrence.  Along every contributing path the rescaled states stay above the
+// final sum's magnitude, so a result of log10 L >= kRescaledFloor (well inside the FP64 range at S') is as
+// accurate as the unscaled recurrence; lower or non-finite results go to queue 2.
+//
+// EXACT (queue 2: those, and reads the host marks, e.g. matchToMatch ~ 0): the unscaled recurrence with the
+// reference's 2^1020 initial condition, so it underflows exactly where LoglessPairHMM does.
+constexpr double kLog10Scale64R = 288.9887958374219;  // log10(2^960)
+constexpr double kRescaledFloor = GHMM_FP64_RESCALED_FLOOR;
+
+template <int K, bool RESCALED>
 __global__ void __launch_bounds__(128) fp64_queue_kernel(DevTables T, DevBatch B) {
     constexpr int S = 32 * K;
     const int lane = threadIdx.x & 31;
     const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     double *scratch = B.scratch64 + warp_global * B.scratch64_cols * 3;
-    const int total = min(B.counters[1], (int)B.rerun_capacity);
+    const PairRef *queue = RESCALED ? B.rerun : B.rerun + B.rerun_capacity;
+    const int total = min(B.counters[RESCALED ? 1 : 4], (int)B.rerun_capacity);
+    const int cursor = RESCALED ? 2 : 5;
     for (;;) {
         int t = 0;
-        if (lane == 0) t = atomicAdd(&B.counters[2], 1);
+        if (lane == 0) t = atomicAdd(&B.counters[cursor], 1);
         t = __shfl_sync(kFull, t, 0);
         if (t >= total) break;
-        const PairRef pr = B.rerun[t];
+        const PairRef pr = queue[t];
         const int read = pr.read, hap = pr.hap;
         const int64_t roff = B.read_off[read];
         const int R = (int)(B.read_off[read + 1] - roff);
@@ -411,31 +430,64 @@ __global__ void __launch_bounds__(128) fp64_queue_kernel(DevTables T, DevBatch B
             if (lane == 0) atomicExch(&B.counters[3], 2);
             continue;
         }
-        const double init = B.hap_init_d[hap];
+        // RESCALED: la = log2 a_R, and the initial condition divided by 2^round(la)
+        double la = 0.0, init = B.hap_init_d[hap];
+        if (RESCALED) {
+            for (int p = lane; p < R; p += 32) {
+                const uint8_t ins = B.ins[roff + p], del = B.dels[roff + p];
+                la -= log2(__ldg(T.m2m_d + ins * 128 + del));
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) la += __shfl_xor_sync(kFull, la, o);
+            init = scalbn(init, -60 - (int)rint(la));
+        }
         const int nstrips = (R + S - 1) / S;
         const int pad = nstrips * S - R;
         const uint8_t *hb = B.hap_bases + hoff;
-        double acc = 0.0;
+        double acc = 0.0, kappa = 0.0;
+        if (RESCALED) {
+            const uint8_t ins = B.ins[roff + R - 1], del = B.dels[roff + R - 1];
+            kappa = __ldg(T.err_d + ins) / __ldg(T.m2m_d + ins * 128 + del);
+        }
         for (int strip = 0; strip < nstrips; ++strip) {
-            double pm[K], pe[K], tmm[K], tim[K], tmi[K], tii[K], tmd[K];
+            // per-row coefficients: RESCALED (b, c, e, DD); exact (MM, IM, MI, II, MD)
+            double pm[K], pe[K], c1[K], c2[K], c3[K], c4[K], c5[K];
             uint32_t rbase[K];
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 const int p = strip * S + lane * K + k - pad;
                 if (p < 0) {
                     pm[k] = pe[k] = 0.0;
-                    tmm[k] = tim[k] = tmi[k] = tii[k] = tmd[k] = 0.0;
+                    c1[k] = c2[k] = c3[k] = c5[k] = 0.0;
+                    c4[k] = RESCALED ? 1.0 : 0.0;  // DD = 1 keeps a dummy row's D~ at the row-0 value
                     rbase[k] = 0x100u;  // matches nothing
                 } else {
                     const uint8_t base = B.bases[roff + p], q = B.quals[roff + p];
                     const uint8_t ins = B.ins[roff + p], del = B.dels[roff + p], gcp = B.gcp[roff + p];
                     pm[k] = __ldg(T.prob_d + q);
                     pe[k] = base == 'N' ? pm[k] : __ldg(T.err3_d + q);
-                    tmm[k] = __ldg(T.m2m_d + ins * 128 + del);
-                    tim[k] = __ldg(T.prob_d + gcp);
-                    tmi[k] = __ldg(T.err_d + ins);
-                    tii[k] = __ldg(T.err_d + gcp);
-                    tmd[k] = __ldg(T.err_d + del);
+                    const double mm = __ldg(T.m2m_d + ins * 128 + del), im = __ldg(T.prob_d + gcp);
+                    const double mi = __ldg(T.err_d + ins), ii = __ldg(T.err_d + gcp), md = __ldg(T.err_d + del);
+                    if (RESCALED) {
+                        double mm_p = 1.0, mi_p = 1.0, md_p = 1.0;
+                        if (p > 0) {
+                            const uint8_t ins_p = B.ins[roff + p - 1], del_p = B.dels[roff + p - 1];
+                            mm_p = __ldg(T.m2m_d + ins_p * 128 + del_p);
+                            mi_p = __ldg(T.err_d + ins_p);
+                            md_p = __ldg(T.err_d + del_p);
+                        }
+                        c1[k] = im * mi_p / (mm * mm_p);                  // b
+                        c2[k] = im * md_p / mm;                           // c
+                        c3[k] = (p > 0) ? ii * mi_p / (mi * mm_p) : 0.0;  // e
+                        c4[k] = ii;                                       // DD
+                        c5[k] = 0.0;
+                    } else {
+                        c1[k] = mm;
+                        c2[k] = im;
+                        c3[k] = mi;
+                        c4[k] = ii;
+                        c5[k] = md;
+                    }
                     rbase[k] = base;
                 }
             }
@@ -446,10 +498,10 @@ __global__ void __launch_bounds__(128) fp64_queue_kernel(DevTables T, DevBatch B
                 Mp[k] = Ip[k] = 0.0;
                 Dp[k] = dummy ? init : 0.0;
             }
-            // DD of dummy rows is 1 so their D stays at the row-0 value
+            // exact: DD of dummy rows is 1 so their D stays at the row-0 value
             double tdd[K];
 #pragma unroll
-            for (int k = 0; k < K; ++k) tdd[k] = ((strip == 0) && (lane * K + k < pad)) ? 1.0 : tii[k];
+            for (int k = 0; k < K; ++k) tdd[k] = ((strip == 0) && (lane * K + k < pad)) ? 1.0 : c4[k];
             double gM = 0.0, gI = 0.0;
             double gD = ((strip == 0) && (lane * K - 1 < pad)) ? init : 0.0;
             const double bnd = (strip == 0) ? init : 0.0;
@@ -500,15 +552,21 @@ __global__ void __launch_bounds__(128) fp64_queue_kernel(DevTables T, DevBatch B
                     const double dI = k ? Ip[k - 1] : gI;
                     const double dD = k ? Dp[k - 1] : gD;
                     const double prior = (rbase[k] == y || yn) ? pm[k] : pe[k];
-                    const double Mn = prior * fma(dM, tmm[k], (dI + dD) * tim[k]);
-                    const double Dn = fma(Dp[k], tdd[k], Mp[k] * tmd[k]);
+                    double Mn, Dn;
+                    if (RESCALED) {
+                        Mn = prior * fma(dI, c1[k], fma(dD, c2[k], dM));
+                        Dn = fma(Dp[k], tdd[k], Mp[k]);
+                    } else {
+                        Mn = prior * fma(dM, c1[k], (dI + dD) * c2[k]);
+                        Dn = fma(Dp[k], tdd[k], Mp[k] * c5[k]);
+                    }
                     Mp[k] = Mn;
                     Dp[k] = Dn;
                 }
                 double aM = uM, aI = uI;
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
-                    const double In = fma(aI, tii[k], aM * tmi[k]);
+                    const double In = RESCALED ? fma(aI, c3[k], aM) : fma(aI, c4[k], aM * c3[k]);
                     Ip[k] = In;
                     aM = Mp[k];
                     aI = In;
@@ -518,7 +576,7 @@ __global__ void __launch_bounds__(128) fp64_queue_kernel(DevTables T, DevBatch B
                 gD = uD;
                 if (valid && lane == 31) {
                     if (last_strip) {
-                        acc += Mp[K - 1] + Ip[K - 1];
+                        acc += RESCALED ? fma(kappa, Ip[K - 1], Mp[K - 1]) : Mp[K - 1] + Ip[K - 1];
                     } else {
                         scratch[3 * c + 0] = Mp[K - 1];
                         scratch[3 * c + 1] = Ip[K - 1];
@@ -528,7 +586,23 @@ __global__ void __launch_bounds__(128) fp64_queue_kernel(DevTables T, DevBatch B
             }
             __syncwarp();
         }
-        if (lane == 31) B.out[out_index] = log10(acc) - kLog10Scale64;
+        if (lane == 31) {
+            if (RESCALED) {
+                const double rla = rint(la);
+                const double v = log10(acc) - kLog10Scale64R - (la - rla) * 0.30102999566398120;
+                if (v >= kRescaledFloor && v <= 0.0) {
+                    B.out[out_index] = v;
+                } else {  // too close to the FP64 range at S' (or not finite): the exact tier recomputes it
+                    const int idx = atomicAdd(&B.counters[4], 1);
+                    if ((int64_t)idx < B.rerun_capacity)
+                        B.rerun[B.rerun_capacity + idx] = pr;
+                    else
+                        atomicExch(&B.counters[3], 1);
+                }
+            } else {
+                B.out[out_index] = log10(acc) - kLog10Scale64;
+            }
+        }
     }
 }
 
@@ -732,7 +806,10 @@ int fp32_kernel_occupancy(int k, int block, int *blocks_per_sm) {
 }
 
 int launch_fp64_queue(const DevTables &t, const DevBatch &b, int grid, int block, cudaStream_t s) {
-    fp64_queue_kernel<kMaxK64><<<grid, block, 0, s>>>(t, b);
+    fp64_queue_kernel<kMaxK64, true><<<grid, block, 0, s>>>(t, b);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return (int)e;
+    fp64_queue_kernel<kMaxK64, false><<<grid, block, 0, s>>>(t, b);
     return (int)cudaGetLastError();
 }
 
@@ -742,7 +819,13 @@ int launch_finalize_fp32(double *out, const int64_t *n_out, int sm_count, cudaSt
 }
 
 int fp64_kernel_occupancy(int block, int *blocks_per_sm) {
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fp64_queue_kernel<kMaxK64>, block, 0);
+    // both tiers run on the same grid and scratch: the smaller occupancy of the two
+    int a = 0, b = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, fp64_queue_kernel<kMaxK64, true>, block, 0);
+    if (e != cudaSuccess) return (int)e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fp64_queue_kernel<kMaxK64, false>, block, 0);
+    *blocks_per_sm = a < b ? a : b;
+    return (int)e;
 }
 
 // Shared memory: three diagonals of M, I, D over R+1 rows, sized by the region's longest read.

@@ -146,7 +146,8 @@ struct ghmm_batch {
     HostBuf<float> h_init_f;
     HostBuf<double> h_init_d;
     HostBuf<F32Task> h_tasks;
-    HostBuf<PairRef> h_direct;
+    HostBuf<PairRef> h_direct;    // FP32 mode: pairs routed to FP64, rescaled tier then exact tier
+    HostBuf<PairRef> h_fp64all;   // FP64 mode: every pair, rescaled tier then exact tier
     HostBuf<double> h_out;
     HostBuf<int32_t> h_counters;  // [kNumCounters] counters, then [2 * kNumBucketKeys] bucket info
     HostBuf<int64_t> h_nout;
@@ -170,16 +171,17 @@ struct ghmm_batch {
     std::vector<int> region_max_read;  // for the plain kernel's shared-memory size
     // tasks
     std::vector<Bucket> buckets;
-    int64_t n_tasks = 0, n_direct = 0;
+    int64_t n_tasks = 0, n_direct = 0, n_direct_exact = 0;
     int64_t cells_direct = 0;  // cells of the pairs sent to FP64 directly
     double ms_host_copy = 0, ms_host_tasks = 0;  // host time of the last marshal: copy + checks, task building
-    int64_t n_direct_fp64mode = 0;
+    int64_t n_direct_fp64mode = 0, n_fp64mode_exact = 0;
+    std::vector<uint8_t> read_exact;  // reads whose pairs go to the exact FP64 tier directly
     int64_t scratch32_cols = 0;
     int fp64_grid = 0;
     // last forward
     int last_mode = -1;
     int last_launches = 0;
-    int64_t last_rerun = 0;
+    int64_t last_rerun = 0, last_exact = 0;
     double ms_fp32 = 0, ms_fp64 = 0, ms_plain = 0, ms_total = 0;
     int64_t upload_bytes = 0, forward_h2d = 0, forward_d2h = 0, results_d2h = 0;
     bool uploaded = false;
@@ -204,7 +206,7 @@ struct ghmm_batch {
         h_nout.release();
         d_nout.release();
         h_planes.release(); h_hap.release(); h_off.release(); h_read_region.release(); h_init_f.release();
-        h_init_d.release(); h_tasks.release(); h_direct.release(); h_out.release(); h_counters.release();
+        h_init_d.release(); h_tasks.release(); h_direct.release(); h_fp64all.release(); h_out.release(); h_counters.release();
         d_planes.release(); d_hap.release(); d_off.release(); d_read_region.release(); d_init_f.release();
         d_init_d.release(); d_tasks.release(); d_rerun.release(); d_out.release(); d_counters.release();
         d_scratch32.release(); d_scratch64.release();
@@ -411,12 +413,13 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                 }
                 if (sg[i] == 0 || base_code(sb[i]) == 0) fl |= 1;
                 const double mm = HT.m2m[si[i] * 128 + sd[i]];
-                if (mm < 1e-6) fl |= 1;
+                if (mm < 1e-6) fl |= 1 | 4;  // exact FP64 tier only (the rescaled forms divide by MM)
                 if (i > 0) {
                     const double e = HT.err[sg[i]] * HT.err[si[i - 1]] /
                                      (HT.err[si[i]] * std::max(HT.m2m[si[i - 1] * 128 + sd[i - 1]], 1e-300));
                     growth = 1.0 + e * growth;
                     if (growth > max_i_scaled) fl |= 1;
+                    if (growth > kMaxGrowth64) fl |= 1 | 4;  // the rescaled FP64 tier's headroom is 2^60
                 }
             }
             read_flag[(size_t)r] = fl;
@@ -454,6 +457,9 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                         "quality out of range (base quality must be <= 254; insertion, deletion and gap "
                         "continuation penalties must be 0..127)");
     b.region_max_read = region_max_read;
+    b.read_exact.assign((size_t)NR, 0);
+    for (int64_t r = 0; r < NR; r++) b.read_exact[(size_t)r] = (read_flag[(size_t)r] & 4) ? 1 : 0;
+    b.n_direct_fp64mode = b.n_fp64mode_exact = -1;  // FP64-mode lists are built on first use
     b.max_read_len = 0;
     b.max_hap_len = 0;
     b.n_cells = 0;
@@ -474,7 +480,7 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
     struct PartOut {
         std::vector<F32Task> tasks[kNumBucketKeys];
         std::vector<int64_t> cost[kNumBucketKeys];
-        std::vector<PairRef> direct;
+        std::vector<PairRef> direct, direct_exact;
         int64_t max_multi_cols = 0, cells_direct = 0;
     };
     const int64_t n_parts = std::max<int64_t>(1, std::min<int64_t>(G, (int64_t)threads * 4));
@@ -496,7 +502,8 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
             for (int64_t r = r0; r < r1; r++) {
                 const int R = (int)(read_off[(size_t)r + 1] - read_off[(size_t)r]);
                 if (region_fp64 || (read_flag[(size_t)r] & 1)) {
-                    for (int64_t h = h0; h < h1; h++) po.direct.push_back(PairRef{(int32_t)r, (int32_t)h});
+                    auto &dst = (read_flag[(size_t)r] & 4) ? po.direct_exact : po.direct;
+                    for (int64_t h = h0; h < h1; h++) dst.push_back(PairRef{(int32_t)r, (int32_t)h});
                     po.cells_direct += (int64_t)R * region_cols;
                     continue;
                 }
@@ -557,7 +564,7 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
     }, 1);
     // buckets in key order, each ordered longest task first (ties keep region order)
     b.buckets.clear();
-    int64_t total_tasks = 0, max_multi_cols = 0, n_direct = 0;
+    int64_t total_tasks = 0, max_multi_cols = 0, n_direct = 0, n_direct_exact = 0;
     b.cells_direct = 0;
     std::vector<int64_t> bucket_pos(kNumBucketKeys + 1, 0);
     for (int key = 0; key < kNumBucketKeys; key++) {
@@ -568,6 +575,7 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
     for (auto &po : parts) {
         max_multi_cols = std::max(max_multi_cols, po.max_multi_cols);
         n_direct += (int64_t)po.direct.size();
+        n_direct_exact += (int64_t)po.direct_exact.size();
         b.cells_direct += po.cells_direct;
     }
     total_tasks = bucket_pos[kNumBucketKeys];
@@ -599,12 +607,18 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
     }
     b.n_tasks = total_tasks;
     b.n_direct = n_direct;
-    GHMM_CUDA(b.h_direct.reserve((size_t)std::max<int64_t>(n_direct, 1)), "pinned direct pairs");
+    b.n_direct_exact = n_direct_exact;
+    GHMM_CUDA(b.h_direct.reserve((size_t)std::max<int64_t>(n_direct + n_direct_exact, 1)), "pinned direct pairs");
     {
         int64_t k = 0;
         for (auto &po : parts) {
             if (!po.direct.empty()) memcpy(b.h_direct.p + k, po.direct.data(), po.direct.size() * sizeof(PairRef));
             k += (int64_t)po.direct.size();
+        }
+        for (auto &po : parts) {
+            if (!po.direct_exact.empty())
+                memcpy(b.h_direct.p + k, po.direct_exact.data(), po.direct_exact.size() * sizeof(PairRef));
+            k += (int64_t)po.direct_exact.size();
         }
     }
     b.scratch32_cols = max_multi_cols;
@@ -631,7 +645,7 @@ static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
     GHMM_CUDA(b.d_init_d.reserve((size_t)NH), "device init");
     GHMM_CUDA(b.d_tasks.reserve((size_t)b.n_tasks), "device tasks");
     const int64_t capacity = std::max<int64_t>(b.n_out, 1);
-    GHMM_CUDA(b.d_rerun.reserve((size_t)capacity), "device FP64 queue");
+    GHMM_CUDA(b.d_rerun.reserve((size_t)capacity * 2), "device FP64 queues");
     GHMM_CUDA(b.d_out.reserve((size_t)std::max<int64_t>(b.n_out, 1)), "device output");
     GHMM_CUDA(b.d_counters.reserve(kNumCounters + 2 * kNumBucketKeys), "device counters");
     GHMM_CUDA(b.d_nout.reserve(1), "device output count");
@@ -689,18 +703,25 @@ static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
     return GHMM_OK;
 }
 
-// Direct FP64 pairs: all pairs (FP64 mode) or the host-classified ones.
+// FP64 mode: every (read, hap) pair of every region, read-major; reads marked exact-only go to the exact tier.
 static int fill_fp64_all(ghmm_ctx *ctx, ghmm_batch &b) {
-    // every (read, hap) pair of every region, read-major
-    GHMM_CUDA(b.h_direct.reserve((size_t)std::max<int64_t>(b.n_out, 1)), "pinned FP64 pairs");
+    GHMM_CUDA(b.h_fp64all.reserve((size_t)std::max<int64_t>(b.n_out, 1)), "pinned FP64 pairs");
     const int64_t *o = b.h_off.p;
     const int64_t NR = b.n_reads, NH = b.n_haps, G = b.n_regions;
     const int64_t *rro = o + NR + 1 + NH + 1, *rho = rro + G + 1;
     int64_t k = 0;
+    for (int pass = 0; pass < 2; pass++)
+        for (int64_t g = 0; g < G; g++)
+            for (int64_t r = rro[g]; r < rro[g + 1]; r++) {
+                if ((b.read_exact[(size_t)r] != 0) != (pass == 1)) continue;
+                for (int64_t h = rho[g]; h < rho[g + 1]; h++) b.h_fp64all.p[k++] = PairRef{(int32_t)r, (int32_t)h};
+            }
+    int64_t n_exact = 0;
     for (int64_t g = 0; g < G; g++)
         for (int64_t r = rro[g]; r < rro[g + 1]; r++)
-            for (int64_t h = rho[g]; h < rho[g + 1]; h++) b.h_direct.p[k++] = PairRef{(int32_t)r, (int32_t)h};
-    b.n_direct_fp64mode = k;
+            if (b.read_exact[(size_t)r]) n_exact += rho[g + 1] - rho[g];
+    b.n_fp64mode_exact = n_exact;
+    b.n_direct_fp64mode = k - n_exact;
     return GHMM_OK;
 }
 
@@ -794,20 +815,29 @@ static int batch_enqueue(ghmm_ctx *ctx, ghmm_batch &b, int mode, cudaStream_t s)
         b.events_ready = true;
     }
     GHMM_CUDA(cudaEventRecord(b.ev[0], s), "event");
-    int64_t n_pre = b.n_direct;
+    // pre-queued pairs: queue 1 (rescaled FP64 tier) at d_rerun[0..), queue 2 (exact tier) at d_rerun[cap..)
+    int64_t n_pre = b.n_direct, n_pre_exact = b.n_direct_exact;
+    const PairRef *pre = b.h_direct.p;
     if (mode == GHMM_MODE_FP64) {
-        if (b.n_direct_fp64mode != b.n_out) {
+        if (b.n_direct_fp64mode < 0) {
             int rc = fill_fp64_all(ctx, b);
             if (rc) return rc;
         }
         n_pre = b.n_direct_fp64mode;
+        n_pre_exact = b.n_fp64mode_exact;
+        pre = b.h_fp64all.p;
     }
+    const int64_t cap = b.dev.rerun_capacity;
     if (n_pre > 0)
-        GHMM_CUDA(cudaMemcpyAsync(b.d_rerun.p, b.h_direct.p, (size_t)n_pre * sizeof(PairRef), cudaMemcpyHostToDevice, s),
+        GHMM_CUDA(cudaMemcpyAsync(b.d_rerun.p, pre, (size_t)n_pre * sizeof(PairRef), cudaMemcpyHostToDevice, s),
                   "H2D FP64 pairs");
+    if (n_pre_exact > 0)
+        GHMM_CUDA(cudaMemcpyAsync(b.d_rerun.p + cap, pre + n_pre, (size_t)n_pre_exact * sizeof(PairRef),
+                                  cudaMemcpyHostToDevice, s), "H2D exact FP64 pairs");
     int32_t *hc = b.h_counters.p;
     for (int i = 0; i < kNumCounters + 2 * kNumBucketKeys; i++) hc[i] = 0;
     hc[1] = (int32_t)n_pre;
+    hc[4] = (int32_t)n_pre_exact;
     for (auto &bk : b.buckets) {
         hc[kNumCounters + bk.key] = bk.begin;
         hc[kNumCounters + kNumBucketKeys + bk.key] = bk.count;
@@ -816,7 +846,7 @@ static int batch_enqueue(ghmm_ctx *ctx, ghmm_batch &b, int mode, cudaStream_t s)
     GHMM_CUDA(cudaMemcpyAsync(b.d_counters.p, hc, (kNumCounters + 2 * kNumBucketKeys) * sizeof(int32_t),
                               cudaMemcpyHostToDevice, s), "H2D counters");
     GHMM_CUDA(cudaMemcpyAsync(b.d_nout.p, b.h_nout.p, sizeof(int64_t), cudaMemcpyHostToDevice, s), "H2D output count");
-    b.forward_h2d = n_pre * (int64_t)sizeof(PairRef) + (kNumCounters + 2 * kNumBucketKeys) * 4 + 8;
+    b.forward_h2d = (n_pre + n_pre_exact) * (int64_t)sizeof(PairRef) + (kNumCounters + 2 * kNumBucketKeys) * 4 + 8;
     b.forward_d2h = kNumCounters * 4;
     // the graph signature: everything the captured launches depend on
     std::vector<unsigned char> sig(sizeof(DevBatch) + 2 * sizeof(int));
@@ -870,6 +900,7 @@ static int batch_finish(ghmm_ctx *ctx, ghmm_batch &b) {
     const int32_t *hc = b.h_counters.p;
     if (hc[3] != 0) return fail(ctx, GHMM_ERR_CUDA, "device-side queue overflow or scratch bound exceeded");
     b.last_rerun = (int64_t)hc[1] - b.pending_n_pre;
+    b.last_exact = (int64_t)hc[4];
     return GHMM_OK;
 }
 
@@ -1027,7 +1058,8 @@ int queue_retire(ghmm_queue *q, int i) {
         in.n_batches++;
         in.n_launches += b.last_launches;
         in.n_rerun += b.last_mode == GHMM_MODE_FP32_RERUN ? b.last_rerun : 0;
-        in.n_fp64_direct += b.last_mode == GHMM_MODE_FP64 ? b.n_direct_fp64mode : b.n_direct;
+        in.n_fp64_direct += b.last_mode == GHMM_MODE_FP64 ? b.n_out : b.n_direct + b.n_direct_exact;
+        in.n_fp64_exact += b.last_exact;
         in.n_cells_fp64_direct += b.last_mode == GHMM_MODE_FP64 ? b.n_cells : b.cells_direct;
         in.h2d_bytes += b.upload_bytes + b.forward_h2d;
         in.d2h_bytes += b.forward_d2h + b.results_d2h;
@@ -1530,7 +1562,8 @@ int ghmm_batch_stats(ghmm_ctx *ctx, const ghmm_batch *b, ghmm_stats *st) {
     st->n_pairs = b->n_out;
     st->n_cells = b->n_cells;
     st->n_rerun = b->last_mode == GHMM_MODE_FP32_RERUN ? b->last_rerun : 0;
-    st->n_fp64_direct = b->last_mode == GHMM_MODE_FP64 ? b->n_direct_fp64mode : b->n_direct;
+    st->n_fp64_direct = b->last_mode == GHMM_MODE_FP64 ? b->n_out : b->n_direct + b->n_direct_exact;
+    st->n_fp64_exact = b->last_mode == GHMM_MODE_PLAIN_FP64 ? 0 : b->last_exact;
     st->n_tasks_fp32 = b->n_tasks;
     st->n_launches = b->last_launches;
     st->reserved = 0;

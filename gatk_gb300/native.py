@@ -22,6 +22,7 @@ GHMM_ERR_TIMEOUT = 7
 
 MODE_FP32_RERUN = 0
 MODE_FP64 = 1
+FP64_RESCALED_FLOOR = -500.0  # GHMM_FP64_RESCALED_FLOOR
 MODE_PLAIN_FP64 = 2
 
 FP32_RERUN_THRESHOLD = 1e-28
@@ -75,7 +76,7 @@ class Stats(ctypes.Structure):
                 ("reserved", ctypes.c_int32), ("ms_fp32", ctypes.c_double), ("ms_fp64", ctypes.c_double),
                 ("ms_plain", ctypes.c_double), ("ms_total", ctypes.c_double), ("h2d_bytes", ctypes.c_int64),
                 ("d2h_bytes", ctypes.c_int64), ("ms_host_marshal", ctypes.c_double),
-                ("ms_host_tasks", ctypes.c_double)]
+                ("ms_host_tasks", ctypes.c_double), ("n_fp64_exact", ctypes.c_int64)]
 
 
 class QueueInfo(ctypes.Structure):
@@ -83,7 +84,8 @@ class QueueInfo(ctypes.Structure):
                 ("n_cells_fp64_direct", ctypes.c_int64), ("n_rerun", ctypes.c_int64), ("n_fp64_direct", ctypes.c_int64),
                 ("n_batches", ctypes.c_int64), ("n_launches", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64),
                 ("d2h_bytes", ctypes.c_int64), ("ms_fp32", ctypes.c_double), ("ms_fp64", ctypes.c_double),
-                ("ms_host_marshal", ctypes.c_double), ("ms_host_tasks", ctypes.c_double)]
+                ("ms_host_marshal", ctypes.c_double), ("ms_host_tasks", ctypes.c_double),
+                ("n_fp64_exact", ctypes.c_int64)]
 
 
 class DevPairs(ctypes.Structure):

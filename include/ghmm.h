@@ -52,6 +52,12 @@ extern "C" {
  * ten decades above FLT_MIN (1.18e-38), where gradual underflow would start to cost precision. */
 #define GHMM_FP32_RERUN_THRESHOLD 1e-28f
 
+/* The FP64 path has two tiers: a rescaled recurrence (5 DP operations per cell, scale 2^960) for every pair,
+ * and LoglessPairHMM's unscaled recurrence (scale 2^1020) for pairs whose rescaled result falls below
+ * log10 L = GHMM_FP64_RESCALED_FLOOR or is not finite, so results near the bottom of the FP64 range, and
+ * -Infinity, come out as the reference computes them. */
+#define GHMM_FP64_RESCALED_FLOOR (-500.0)
+
 /* Forward modes for ghmm_batch_forward. */
 #define GHMM_MODE_FP32_RERUN 0 /* batched FP32 wavefront + FP64 rerun of underflowing pairs (default) */
 #define GHMM_MODE_FP64 1       /* every pair in the FP64 wavefront kernel (useDoublePrecision) */
@@ -123,6 +129,8 @@ typedef struct ghmm_stats {
     int64_t d2h_bytes;        /* device-to-host bytes of the last forward + results */
     double ms_host_marshal;   /* host time of the last marshal: copies into pinned planes, checks, routing */
     double ms_host_tasks;     /* host time of building and ordering the FP32 warp tasks */
+    int64_t n_fp64_exact;     /* pairs of the last forward computed by the exact (unscaled, 2^1020) FP64 tier:
+                                 results of the rescaled FP64 tier below log10 L = -500, and host-marked reads */
 } ghmm_stats;
 
 /* Launch-shape choices of the FP32 pass (the autotuner's knobs; the reference has none besides its thread
@@ -214,6 +222,7 @@ typedef struct ghmm_queue_info {
     double ms_fp32, ms_fp64;      /* summed device time of the two phases (batches on the two streams overlap) */
     double ms_host_marshal;       /* summed worker time in marshalling copies and checks */
     double ms_host_tasks;         /* summed worker time in building FP32 tasks */
+    int64_t n_fp64_exact;         /* finished pairs computed by the exact FP64 tier */
 } ghmm_queue_info;
 
 int ghmm_queue_create(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **queue);

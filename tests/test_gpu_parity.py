@@ -351,3 +351,41 @@ def test_peaks_are_sane(engine):
     assert 20 < p["fp32_tflops"] < 200
     assert 20 < p["fp32x2_tflops"] < 400
     assert 0 < p["fp64_tflops"] < 100
+
+
+def test_fp64_tiers_near_the_bottom_of_the_range(engine):
+    # random reads against unrelated haplotypes at low base quality: log10 L from about -150 to below the
+    # FP64 range (-Infinity in LoglessPairHMM too); results below the rescaled tier's floor (-500) come
+    # from the exact tier, and everything matches the oracle to the FP64 bar
+    rng = np.random.default_rng(11)
+    regions = []
+    for R in (150, 250, 350, 450, 550, 650, 800, 1200):
+        hap = _rand_seq(rng, R + 40)
+        regions.append(_single(hap, _rand_seq(rng, R), q=rng.integers(8, 14, size=R)))
+    wl = W.from_pairs(regions)
+    ref = _oracle_all(wl)
+    assert (ref < native.FP64_RESCALED_FLOOR).any() and (ref > native.FP64_RESCALED_FLOOR).any()
+    for mode in (native.MODE_FP32_RERUN, native.MODE_FP64):
+        got, st = _run(engine, wl, mode)
+        finite = np.isfinite(ref) & (ref > -600)
+        assert np.abs(got[finite] - ref[finite]).max() <= TOL64, mode
+        # at the very bottom (subnormal sums) the reference itself is imprecise; only the -Infinity
+        # boundary is compared there
+        deep = ~finite
+        assert np.all((got[deep] == -np.inf) | (got[deep] < -600)), mode
+        assert st["n_fp64_exact"] >= int((ref < native.FP64_RESCALED_FLOOR).sum()), mode
+
+
+def test_steep_insertion_penalties_route_to_the_exact_tier(engine):
+    # insertion penalty jumping 10 -> 127 between neighbours: the rescaled forms' I~ could outgrow their
+    # headroom, so the host sends the read to the exact FP64 tier
+    rng = np.random.default_rng(5)
+    hap = _rand_seq(rng, 120)
+    read = hap[20:90]
+    ins = np.where(np.arange(70) % 2 == 0, 10, 127)
+    wl = W.from_pairs([_single(hap, read, ins=ins), _single(hap, read)])
+    ref = _oracle_all(wl)
+    got, st = _run(engine, wl, native.MODE_FP32_RERUN)
+    assert st["n_fp64_exact"] == 1
+    assert _absdiff(got[:1], ref[:1]).max() <= TOL64
+    assert _absdiff(got[1:], ref[1:]).max() <= TOL32

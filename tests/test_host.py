@@ -33,6 +33,41 @@ def test_library_exports_every_declared_symbol():
     assert declared == set(native.exported_symbols())
 
 
+def test_header_constants_match_the_bindings():
+    src = open(os.path.join(ROOT, "include", "ghmm.h")).read()
+    defs = dict(re.findall(r"#define (GHMM_\w+) \(?([-0-9.e]+)f?\)?", src))
+    for name in ("GHMM_OK", "GHMM_ERR_ARG", "GHMM_ERR_STATE", "GHMM_ERR_CUDA", "GHMM_ERR_UNSUPPORTED",
+                 "GHMM_ERR_RESULT", "GHMM_ERR_NOMEM", "GHMM_ERR_TIMEOUT"):
+        assert int(defs[name]) == getattr(native, name), name
+    assert int(defs["GHMM_MODE_FP32_RERUN"]) == native.MODE_FP32_RERUN
+    assert int(defs["GHMM_MODE_FP64"]) == native.MODE_FP64
+    assert int(defs["GHMM_MODE_PLAIN_FP64"]) == native.MODE_PLAIN_FP64
+    assert float(defs["GHMM_FP64_RESCALED_FLOOR"]) == native.FP64_RESCALED_FLOOR
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    # compile the headers with the host C compiler and compare every struct's size with the ctypes mirror
+    import shutil
+    import subprocess
+
+    cc = shutil.which("cc") or shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"ghmm_args": native.Args, "ghmm_read": native.Read, "ghmm_hap": native.Hap,
+               "ghmm_region": native.Region, "ghmm_flat": native.Flat, "ghmm_stats": native.Stats,
+               "ghmm_tuning": native.Tuning, "ghmm_queue_info": native.QueueInfo,
+               "ghmm_dev_pairs": native.DevPairs, "ghmm_calib_batch": native.CalibBatch}
+    src = tmp_path / "sizes.c"
+    src.write_text('#include <stdio.h>\n#include "ghmm.h"\n#include "ghmm_calib.h"\nint main(void) {\n' +
+                   "".join(f'printf("{n} %zu\\n", sizeof({n}));\n' for n in structs) + "return 0;\n}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    sizes = dict(zip(out[0::2], map(int, out[1::2])))
+    for n, cls in structs.items():
+        assert sizes[n] == ctypes.sizeof(cls), n
+
+
 def test_no_gpu_here_reports_unsupported():
     L = native.lib()
     if L.ghmm_load():
