@@ -84,16 +84,22 @@ class CalibrationSet:
         self.max_read_len = int(wl.read_lengths().max()) if wl.n_reads else 1
         self.max_hap_len = int(wl.hap_lengths().max()) if wl.n_haps else 1
         self.cells = wl.cells()
+        self._ii = None
 
     def position_params(self, theta):
         """(gap_open, gap_cont) per read position from the [8, 20, 2] table (differentiable in theta)."""
         import torch
 
         flat = theta.reshape(-1, 2).to(self.device, torch.float32)
-        ii = self.param_index.clamp(min=0)
-        fixed = self.param_index < 0
-        g = torch.where(fixed, torch.full_like(ii, 0, dtype=torch.float32) + LAST_GAP_OPEN, flat[ii, 0])
-        c = torch.where(fixed, torch.full_like(ii, 0, dtype=torch.float32) + LAST_GAP_CONT, flat[ii, 1])
+        if self._ii is None:
+            self._ii = self.param_index.clamp(min=0)
+            self._fixed = self.param_index < 0
+            self._last = (torch.full_like(self._ii, 0, dtype=torch.float32) + LAST_GAP_OPEN,
+                          torch.full_like(self._ii, 0, dtype=torch.float32) + LAST_GAP_CONT)
+        # index_select: its backward is an index_add over the table (advanced indexing's backward sorts the
+        # 10^5-10^6 positions and costs tens of milliseconds)
+        g = torch.where(self._fixed, self._last[0], torch.index_select(flat[:, 0], 0, self._ii))
+        c = torch.where(self._fixed, self._last[1], torch.index_select(flat[:, 1], 0, self._ii))
         return g.contiguous(), c.contiguous()
 
     def batch(self, gap_open, gap_cont) -> native.CalibBatch:
