@@ -90,17 +90,18 @@ class CalibrationSet:
         """(gap_open, gap_cont) per read position from the [8, 20, 2] table (differentiable in theta)."""
         import torch
 
-        flat = theta.reshape(-1, 2).to(self.device, torch.float32)
+        # gathered in FP64 so that the backward's index_add sums the 10^5-10^6 per-position gradients into the
+        # table in FP64 (index_select's backward is an atomic index_add; advanced indexing's sorts the
+        # positions and costs tens of milliseconds)
+        flat = theta.reshape(-1, 2).to(self.device, torch.float64)
         if self._ii is None:
             self._ii = self.param_index.clamp(min=0)
             self._fixed = self.param_index < 0
-            self._last = (torch.full_like(self._ii, 0, dtype=torch.float32) + LAST_GAP_OPEN,
-                          torch.full_like(self._ii, 0, dtype=torch.float32) + LAST_GAP_CONT)
-        # index_select: its backward is an index_add over the table (advanced indexing's backward sorts the
-        # 10^5-10^6 positions and costs tens of milliseconds)
+            self._last = (torch.full_like(self._ii, 0, dtype=torch.float64) + LAST_GAP_OPEN,
+                          torch.full_like(self._ii, 0, dtype=torch.float64) + LAST_GAP_CONT)
         g = torch.where(self._fixed, self._last[0], torch.index_select(flat[:, 0], 0, self._ii))
         c = torch.where(self._fixed, self._last[1], torch.index_select(flat[:, 1], 0, self._ii))
-        return g.contiguous(), c.contiguous()
+        return g.float().contiguous(), c.float().contiguous()
 
     def batch(self, gap_open, gap_cont) -> native.CalibBatch:
         return native.CalibBatch(self.bases.data_ptr(), self.quals.data_ptr(), self.read_off.data_ptr(),

@@ -170,10 +170,13 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
     const int counter_slot = kCounterBucketBase + KEY;
     constexpr int S = 32 * K;
     const int lane = threadIdx.x & 31;
-    // Per-warp prior table in shared memory: prior[k][base][lane] as (read A, read B), base index
-    // A,C,G,T,N = 0..4.  One 64-bit load per row and step replaces two compares and two selects.
-    extern __shared__ float2 prior_smem[];
-    float2 *prior_tbl = prior_smem + (size_t)(threadIdx.x >> 5) * (K * kBases * 32) + lane;
+    // Per-warp prior table in shared memory: prior[k/2][base][lane] holds rows k and k+1 as (read A, read B,
+    // read A, read B), base index A,C,G,T,N = 0..4.  One 128-bit load per row pair and step replaces four
+    // compares and four selects.
+    constexpr int KP = (K + 1) / 2;  // row pairs
+    extern __shared__ float4 prior_smem4[];
+    float4 *prior_tbl4 = prior_smem4 + (size_t)(threadIdx.x >> 5) * (KP * kBases * 32) + lane;
+    float2 *prior_tbl2 = reinterpret_cast<float2 *>(prior_tbl4);
     const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     float2 *scratch = nullptr;
     if (MULTI) scratch = B.scratch32 + warp_global * B.scratch32_cols * 3;
@@ -223,7 +226,7 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
 #pragma unroll
                 for (int h = 0; h < kBases; ++h) {
                     const uint32_t hm = kBaseMask[h];
-                    prior_tbl[(k * kBases + h) * 32] =
+                    prior_tbl2[((k / 2) * kBases + h) * 64 + (k & 1)] =
                         make_float2((a.code & hm) ? a.pm : a.pe, (b.code & hm) ? b.pm : b.pe);
                 }
             }
@@ -307,14 +310,21 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                     uI = zero2();
                     uD = bnd;
                 }
-                const float2 *pri = prior_tbl + (code & 7u) * 32;
+                const float4 *pri4 = prior_tbl4 + (code & 7u) * 32;
+                float2 prs[2 * KP];
+#pragma unroll
+                for (int kk = 0; kk < KP; ++kk) {
+                    const float4 v = pri4[kk * kBases * 32];
+                    prs[2 * kk] = make_float2(v.x, v.y);
+                    prs[2 * kk + 1] = make_float2(v.z, v.w);
+                }
                 // pass 1 (bottom-up so the row above is still the previous column): M and D^
 #pragma unroll
                 for (int k = K - 1; k >= 0; --k) {
                     const float2 dM = k ? Mp[k - 1] : gM;
                     const float2 dI = k ? Ip[k - 1] : gI;
                     const float2 dD = k ? Dp[k - 1] : gD;
-                    const float2 pr = pri[k * kBases * 32];
+                    const float2 pr = prs[k];
                     const float2 Mn = mul2(pr, fma2(dI, cb[k], fma2(dD, cc[k], dM)));
                     const float2 Dn = fma2(Dp[k], cdd[k], Mp[k]);
                     Mp[k] = Mn;
@@ -354,14 +364,15 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
             while (s < nsteps) {
                 while (j <= nh_task && (int)(hoff[j] - col0) <= s) ++j;
                 const int window_end = min((int)(hoff[j - 1] - col0) + 32, nsteps);
-                // unrolled by two: the scheduler interleaves one step's I~ chain with the next step's M~ and D~
+                // unrolled (4 checked, 16 check-free steps; measured best of 2-32): the scheduler interleaves
+                // one step's I~ chain and shuffles with the following steps' M~ and D~
                 if (s < window_end) {
-#pragma unroll 2
+#pragma unroll 4
                     for (; s < window_end; ++s) step(s, std::true_type{});
                     continue;
                 }
                 const int next_boundary = (j <= nh_task) ? (int)(hoff[j] - col0) : nsteps;
-#pragma unroll 2
+#pragma unroll 16
                 for (; s < next_boundary; ++s) step(s, std::false_type{});
             }
             if (MULTI) __syncwarp();
@@ -744,7 +755,7 @@ __global__ void peak_dfma_kernel(double *out, int iters, double x, double y) {
 }
 
 // ---------------------------------------------------------------------------------------------------
-static size_t fp32_smem_bytes(int k, int block) { return (size_t)(block / 32) * k * kBases * 32 * sizeof(float2); }
+static size_t fp32_smem_bytes(int k, int block) { return (size_t)(block / 32) * ((k + 1) / 2) * kBases * 32 * sizeof(float4); }
 
 template <int K, bool MULTI>
 static int launch_fp32_k(const DevTables &t, const DevBatch &b, int grid, int block, cudaStream_t s) {
