@@ -204,6 +204,7 @@ def run_ours(args):
     g0, g1 = sharding.block_range(n_regions, rank)
     wl = W.generate(args.workload, regions=g1 - g0, region_begin=g0)
     cells = int(wl.cells_per_region().sum())
+    tuning = apply_tuning(args, eng, wl)
 
     # ---- device-resident forward (value) ----
     batch = eng.batch(wl)
@@ -324,6 +325,7 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk,
         "fp64_rerun": {"pairs": int(st["n_rerun"]), "fraction": rerun_frac, "ms": ms_fp64},
+        "tuning": tuning,
         "plain_fp64": {"value": plain_gcups, "unit": "GCUPS", "regions": n_pl, "cells": pl_cells,
                        "launches": int(pst["n_launches"]), "speedup_batched_vs_plain": value / world / plain_gcups,
                        "max_abs_diff_vs_batched": plain_vs_ours},
@@ -553,6 +555,21 @@ def run_calib(args):
     return 0
 
 
+def apply_tuning(args, eng, wl):
+    """--tuning K,KM,C sets the launch shape; --autotune runs the native autotuner on the whole workload
+    (untimed) over the candidates it names.  Returns what was used."""
+    if args.autotune:
+        cands = [tuple(int(x) for x in c.split(",")) for c in args.autotune.split(";")]
+        t = eng.autotune(wl, candidates=cands, use_cache=False, sample_cells=float("inf"))
+        return {"max_rows_per_lane": t["max_rows_per_lane"], "max_rows_per_lane_multi": t["max_rows_per_lane_multi"],
+                "chunk_cols": t["chunk_cols"], "autotune_ms": t["ms"], "autotune_s": t["search_s"]}
+    if args.tuning:
+        k, km, c = (int(x) for x in args.tuning.split(","))
+        eng.set_tuning(k, km, c)
+    k, km, c = eng.get_tuning()
+    return {"max_rows_per_lane": k, "max_rows_per_lane_multi": km, "chunk_cols": c}
+
+
 def absdiff(got, ref):
     """|got - ref|, where equal infinities count as 0: a pair whose likelihood underflows even the FP64
     2^1020 scale is -Infinity in LoglessPairHMM too."""
@@ -597,6 +614,10 @@ def main():
     ap.add_argument("--stream", action="store_true",
                     help="push the workload one region at a time through the queue (default workload 4)")
     ap.add_argument("--batch-cells", type=float, default=2e11, help="queue batch size in cells (--stream)")
+    ap.add_argument("--tuning", default="", help="launch shape K,KM,CHUNK_COLS (rows per lane, multi-strip rows "
+                    "per lane, haplotype columns per task)")
+    ap.add_argument("--autotune", default="", help="autotune over candidates 'K,KM,C;K,KM,C;...' on the whole "
+                    "workload before timing")
     ap.add_argument("--calib", action="store_true",
                     help="time the calibration forward + backward on workload 3 and check its gradient")
     args = ap.parse_args()

@@ -21,7 +21,15 @@ import numpy as np
 from . import native
 from .workload import Workload
 
-SAMPLE_CELLS = 4e10  # cells of the autotuning sample: about 10-15 ms per forward on one GB300
+# Cells of the autotuning sample: about 60 ms per forward on one GB300.  The sample has to carry the
+# workload's load balance as well as its shapes: on workload 1 a 4e10-cell sample preferred 4,096-column
+# tasks (a small batch is dominated by its last tasks), while the whole workload runs fastest with 16,384
+# (271 vs 276 ms for the FP32 launch set).
+SAMPLE_CELLS = 2e11
+# Default candidates (rows per lane single-strip, multi-strip, haplotype columns per task): the shapes that
+# won or came close on workloads 1, 2 and 4.  ghmm_autotune's built-in 18-shape grid is used when the caller
+# passes candidates=[] explicitly.
+DEFAULT_CANDIDATES = [(8, 8, 16384), (8, 8, 8192), (8, 8, 4096), (8, 6, 16384), (8, 4, 16384), (6, 8, 16384)]
 
 
 def cache_path() -> str:
@@ -110,7 +118,7 @@ def _store(path: str, data: dict) -> None:
 
 
 def autotune(engine, wl: Workload, device: int = 0, use_cache: bool = True, candidates=None, reps: int = 3,
-             path: str | None = None) -> dict:
+             path: str | None = None, sample_cells: float = SAMPLE_CELLS) -> dict:
     """Set the fastest tuning for workloads shaped like `wl` on `engine` and return it.
 
     Returns {"max_rows_per_lane", "max_rows_per_lane_multi", "chunk_cols", "cached", "key", "ms"
@@ -123,8 +131,10 @@ def autotune(engine, wl: Workload, device: int = 0, use_cache: bool = True, cand
         t = cache[key]
         engine.set_tuning(t["max_rows_per_lane"], t["max_rows_per_lane_multi"], t["chunk_cols"])
         return dict(t, cached=True, key=key)
-    smp = sample(wl)
+    smp = sample(wl, sample_cells)
     flat = smp.as_flat()
+    if candidates is None:
+        candidates = DEFAULT_CANDIDATES
     if candidates:
         n = len(candidates)
         cand = (native.Tuning * n)(*[native.Tuning(*c, 0) for c in candidates])
