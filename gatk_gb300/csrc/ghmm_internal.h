@@ -92,6 +92,17 @@ constexpr int kCodePad = 64;
 constexpr double kMaxGrowth64 = 1e10;
 int fp32_kernel_occupancy(int k, int block, int *blocks_per_sm);
 int fp64_kernel_occupancy(int block, int *blocks_per_sm);
+
+// Post-likelihood normalisation and filtering (post.cu).
+struct PostArgs {
+    double cap;                   // log10globalReadMismappingRate (< 0)
+    double rate;                  // expected error rate per base
+    double scale;                 // dynamic threshold's K
+    const int32_t *reference_hap; // per region, or nullptr
+    int normalize, symmetric, dynamic;
+};
+int launch_postprocess(const DevBatch &b, int64_t n_reads, const PostArgs &p, uint8_t *keep, int sm_count,
+                       cudaStream_t s);
 int measure_peaks_device(int sm_count, double *fp32, double *fp32x2, double *fp64, cudaStream_t s);
 // Calibration forward/backward (calib.cu).
 int64_t calib_scratch_per_warp(int k, int max_hap_len, bool fp64);

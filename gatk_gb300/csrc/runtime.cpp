@@ -162,6 +162,7 @@ struct ghmm_batch {
     DevBuf<double> d_out;
     DevBuf<int32_t> d_counters;  // same layout as h_counters
     DevBuf<int64_t> d_nout;
+    DevBuf<uint8_t> d_post;  // postprocess: reference haplotype per region, keep flags per read
     DevBuf<float2> d_scratch32;
     DevBuf<double> d_scratch64;
     // sizes
@@ -209,7 +210,7 @@ struct ghmm_batch {
         h_init_d.release(); h_tasks.release(); h_direct.release(); h_fp64all.release(); h_out.release(); h_counters.release();
         d_planes.release(); d_hap.release(); d_off.release(); d_read_region.release(); d_init_f.release();
         d_init_d.release(); d_tasks.release(); d_rerun.release(); d_out.release(); d_counters.release();
-        d_scratch32.release(); d_scratch64.release();
+        d_scratch32.release(); d_scratch64.release(); d_post.release();
     }
 };
 
@@ -1575,6 +1576,39 @@ int ghmm_batch_stats(ghmm_ctx *ctx, const ghmm_batch *b, ghmm_stats *st) {
     st->d2h_bytes = b->forward_d2h + b->results_d2h;
     st->ms_host_marshal = b->ms_host_copy;
     st->ms_host_tasks = b->ms_host_tasks;
+    return GHMM_OK;
+}
+
+int ghmm_batch_postprocess(ghmm_ctx *ctx, ghmm_batch *b, const ghmm_postprocess *pp, uint8_t *keep) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!b || !pp || (b->n_reads > 0 && !keep)) return fail(ctx, GHMM_ERR_ARG, "NULL argument");
+    if (!b->uploaded || b->last_mode < 0) return fail(ctx, GHMM_ERR_STATE, "run a forward on the batch first");
+    const double cap = pp->max_likelihood_difference_cap;
+    if (!(cap < 0.0)) return fail(ctx, GHMM_ERR_ARG, "the minimum reference likelihood fall must be negative");
+    if (!(pp->expected_error_rate_per_base >= 0.0)) return fail(ctx, GHMM_ERR_ARG, "expected error rate must be >= 0");
+    if (b->n_reads == 0) return GHMM_OK;
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t s = ctx->stream;
+    PostArgs p{};
+    p.cap = cap;
+    p.rate = pp->expected_error_rate_per_base;
+    p.scale = pp->read_disqualification_scale;
+    p.normalize = std::isinf(cap) ? 0 : 1;
+    p.symmetric = pp->symmetric ? 1 : 0;
+    p.dynamic = pp->dynamic_disqualification ? 1 : 0;
+    if (pp->reference_hap) {
+        GHMM_CUDA(b->d_post.reserve((size_t)b->n_regions * sizeof(int32_t) + (size_t)b->n_reads), "device post buffers");
+        GHMM_CUDA(cudaMemcpyAsync(b->d_post.p, pp->reference_hap, (size_t)b->n_regions * sizeof(int32_t),
+                                  cudaMemcpyHostToDevice, s), "H2D reference haplotypes");
+        p.reference_hap = reinterpret_cast<const int32_t *>(b->d_post.p);
+    } else {
+        GHMM_CUDA(b->d_post.reserve((size_t)b->n_regions * sizeof(int32_t) + (size_t)b->n_reads), "device post buffers");
+    }
+    uint8_t *d_keep = b->d_post.p + (size_t)b->n_regions * sizeof(int32_t);
+    int e = launch_postprocess(b->dev, b->n_reads, p, d_keep, ctx->sm_count, s);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "postprocess launch");
+    GHMM_CUDA(cudaMemcpyAsync(keep, d_keep, (size_t)b->n_reads, cudaMemcpyDeviceToHost, s), "D2H keep flags");
+    GHMM_CUDA(cudaStreamSynchronize(s), "postprocess");
     return GHMM_OK;
 }
 

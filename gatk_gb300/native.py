@@ -79,6 +79,12 @@ class Stats(ctypes.Structure):
                 ("ms_host_tasks", ctypes.c_double), ("n_fp64_exact", ctypes.c_int64)]
 
 
+class Postprocess(ctypes.Structure):
+    _fields_ = [("max_likelihood_difference_cap", ctypes.c_double), ("symmetric", ctypes.c_int32),
+                ("dynamic_disqualification", ctypes.c_int32), ("expected_error_rate_per_base", ctypes.c_double),
+                ("read_disqualification_scale", ctypes.c_double), ("reference_hap", ctypes.c_void_p)]
+
+
 class QueueInfo(ctypes.Structure):
     _fields_ = [("n_regions", ctypes.c_int64), ("n_pairs", ctypes.c_int64), ("n_cells", ctypes.c_int64),
                 ("n_cells_fp64_direct", ctypes.c_int64), ("n_rerun", ctypes.c_int64), ("n_fp64_direct", ctypes.c_int64),
@@ -135,6 +141,8 @@ _SIGS = {
     "ghmm_batch_results": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _f64p]),
     "ghmm_batch_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Stats)]),
     "ghmm_batch_destroy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "ghmm_batch_postprocess": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Postprocess),
+                                              ctypes.c_void_p]),
     "ghmm_compute_flat": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Flat), _f64p]),
     "ghmm_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
     "ghmm_queue_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),

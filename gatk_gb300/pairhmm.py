@@ -227,6 +227,21 @@ class Batch:
                      self.engine.handle)
         return out
 
+    def postprocess(self, cap: float = -4.5, symmetric: bool = True, reference_hap=None, expected_error_rate: float = 0.02,
+                    dynamic: bool = False, scale: float = 1.0) -> np.ndarray:
+        """Normalise the last forward's likelihoods and flag poorly modelled reads on the device
+        (PairHMMLikelihoodCalculationEngine.computeReadLikelihoods' last two steps); returns keep flags per read.
+        cap is log10globalReadMismappingRate (GATK default -4.5: Phred 45)."""
+        ref = None
+        if reference_hap is not None:
+            ref = np.ascontiguousarray(reference_hap, dtype=np.int32)
+        p = native.Postprocess(float(cap), int(symmetric), int(dynamic), float(expected_error_rate), float(scale),
+                               ref.ctypes.data if ref is not None else None)
+        keep = np.empty(max(self.wl.n_reads, 1), dtype=np.uint8)
+        native.check(self.engine.L.ghmm_batch_postprocess(self.engine.handle, self.h, ctypes.byref(p), keep.ctypes.data),
+                     self.engine.handle)
+        return keep[:self.wl.n_reads]
+
     def stats(self) -> dict:
         s = native.Stats()
         native.check(self.engine.L.ghmm_batch_stats(self.engine.handle, self.h, ctypes.byref(s)), self.engine.handle)

@@ -196,3 +196,34 @@ def from_pairs(regions) -> Workload:
                     read_off=np.array(ro, dtype=np.int64), bases=cat(planes[0]), quals=cat(planes[1]),
                     ins=cat(planes[2]), dels=cat(planes[3]), gcp=cat(planes[4]), hap_off=np.array(ho, dtype=np.int64),
                     hap_bases=cat(hb), out_off=np.array(oo, dtype=np.int64))
+
+
+# PartiallyDeterminedHaplotype flag bits (utils/haplotype/PartiallyDeterminedHaplotype.java:59-66)
+PD_SNP, PD_DEL_START, PD_DEL_END = 1, 2, 4
+PD_BASE_BIT = {ord("A"): 8, ord("C"): 16, ord("G"): 32, ord("T"): 64}
+
+
+def pd_flags(wl: Workload, seed: int = 5, snps_per_hap=(1, 3), dels_per_hap=(0, 2), del_len=(1, 10)) -> np.ndarray:
+    """Partially-determined-haplotype flags for every haplotype of a workload (a byte per haplotype base, parallel
+    to hap_bases), as PartiallyDeterminedHaplotype.getAlternateBases gives them (PartiallyDeterminedHaplotype.java:
+    170-205): an undetermined SNP site carries SNP plus the bit of its alternative base; an undetermined deletion
+    marks its first base DEL_START and its last DEL_END (both on a single-base deletion).  Sites are drawn with a
+    numpy PCG64 stream seeded per haplotype, so the flags are the same on every machine."""
+    out = np.zeros(len(wl.hap_bases), dtype=np.uint8)
+    for h in range(wl.n_haps):
+        a, b = int(wl.hap_off[h]), int(wl.hap_off[h + 1])
+        H = b - a
+        if H < 4:
+            continue
+        rng = np.random.default_rng([seed, h])
+        hb = wl.hap_bases[a:b]
+        for _ in range(int(rng.integers(snps_per_hap[0], snps_per_hap[1] + 1))):
+            j = int(rng.integers(0, H))
+            alts = [c for c in b"ACGT" if c != hb[j]]
+            out[a + j] |= PD_SNP | PD_BASE_BIT[alts[int(rng.integers(0, 3))]]
+        for _ in range(int(rng.integers(dels_per_hap[0], dels_per_hap[1] + 1))):
+            n = int(rng.integers(del_len[0], del_len[1] + 1))
+            j = int(rng.integers(1, max(2, H - n)))
+            out[a + j] |= PD_DEL_START
+            out[a + min(j + n - 1, H - 1)] |= PD_DEL_END
+    return out

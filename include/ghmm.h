@@ -187,6 +187,25 @@ int ghmm_batch_results(ghmm_ctx *ctx, ghmm_batch *batch, double *out);
 int ghmm_batch_stats(ghmm_ctx *ctx, const ghmm_batch *batch, ghmm_stats *stats);
 int ghmm_batch_destroy(ghmm_ctx *ctx, ghmm_batch *batch);
 
+/* The step after the likelihoods, fused on the device over a batch's last forward: per read, every haplotype
+ * likelihood below best + cap is raised to best + cap (AlleleLikelihoods.normalizeLikelihoods,
+ * utils/genotyper/AlleleLikelihoods.java:416-458, best as searchBestAllele :505-540), and reads whose best
+ * likelihood is below their threshold are flagged for removal (filterPoorlyModeledEvidence :1351-1376 with
+ * ReadLikelihoodCalculationEngine.log10MinTrueLikelihood :124-132, or the DRAGEN-GATK dynamic threshold
+ * :106-158), in that order, as PairHMMLikelihoodCalculationEngine.java:200-201 runs them.  The normalised values
+ * replace the batch's results (ghmm_batch_results); keep[r] (n_reads bytes, host) is 1 for a read that stays.
+ * One region is one sample and its haplotypes are the alleles. */
+typedef struct ghmm_postprocess {
+    double max_likelihood_difference_cap; /* log10globalReadMismappingRate: < 0, or -INFINITY to skip normalising */
+    int32_t symmetric;                    /* symmetricallyNormalizeAllelesToReference: the reference may be best */
+    int32_t dynamic_disqualification;     /* dynamicDisqualification: the DRAGEN-GATK read-quality threshold */
+    double expected_error_rate_per_base;  /* expectedErrorRatePerBase (GATK default 0.02), >= 0 */
+    double read_disqualification_scale;   /* readDisqualificationScale (GATK default 1.0) */
+    const int32_t *reference_hap;         /* per region: reference haplotype index within the region or -1; NULL: none */
+} ghmm_postprocess;
+
+int ghmm_batch_postprocess(ghmm_ctx *ctx, ghmm_batch *batch, const ghmm_postprocess *pp, uint8_t *keep);
+
 /* Flat inputs straight from host memory to results (upload + forward + download in one call). */
 int ghmm_compute_flat(ghmm_ctx *ctx, const ghmm_flat *flat, double *out);
 

@@ -27,7 +27,7 @@ _f64p = ctypes.POINTER(ctypes.c_double)
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, OpenMP, -ffp-contract=off)."""
-    srcs = [os.path.join(_HERE, f) for f in ("pairhmm_oracle.c", "oracle_grad.c", "Makefile")]
+    srcs = [os.path.join(_HERE, f) for f in ("pairhmm_oracle.c", "oracle_grad.c", "pdhmm_oracle.c", "Makefile")]
     if not force and os.path.exists(_LIB_PATH):
         if os.path.getmtime(_LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
             return _LIB_PATH
@@ -76,6 +76,12 @@ def lib():
         L.oracle_cont_forward.argtypes = [_u8p, ctypes.c_int, _u8p, _u8p, _f64p, _f64p, ctypes.c_int]
         L.oracle_cont_grad.restype = ctypes.c_double
         L.oracle_cont_grad.argtypes = [_u8p, ctypes.c_int, _u8p, _u8p, _f64p, _f64p, ctypes.c_int, _f64p, _f64p]
+        L.oracle_pd_logless.restype = ctypes.c_double
+        L.oracle_pd_logless.argtypes = [_u8p, _u8p, ctypes.c_int, _u8p, _u8p, _u8p, _u8p, _u8p, ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_int)]
+        L.oracle_pd_compute_pairs.restype = ctypes.c_int64
+        L.oracle_pd_compute_pairs.argtypes = [ctypes.c_int64, _i64p, _i64p, _i64p, _u8p, _u8p, _u8p, _u8p, _u8p,
+                                              _i64p, _u8p, _u8p, _f64p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -154,3 +160,32 @@ def cont_grad(hap, read, quals, g, c):
 
 def num_threads() -> int:
     return lib().oracle_num_threads()
+
+
+def pd_logless(hap, pd, read, quals, ins, dels, gcp) -> float:
+    """LoglessPDPairHMM for one pair (pdhmm_oracle.c); raises ValueError where the reference throws."""
+    h, f, r, q, i, d, g = (_u8(x) for x in (hap, pd, read, quals, ins, dels, gcp))
+    err = ctypes.c_int(0)
+    v = lib().oracle_pd_logless(_p(h, _u8p), _p(f, _u8p), len(h), _p(r, _u8p), _p(q, _u8p), _p(i, _u8p),
+                                _p(d, _u8p), _p(g, _u8p), len(r), ctypes.byref(err))
+    if err.value:
+        raise ValueError("Found unexpected base in alt alleles")
+    return v
+
+
+def pd_compute_workload(wl, hap_pd: np.ndarray, threads: int = 0) -> np.ndarray:
+    """Every pair of a workload whose haplotypes carry PD flags (hap_pd, parallel to hap_bases), read-major."""
+    pr, ph = wl.pair_index()
+    out = np.empty(len(pr), dtype=np.float64)
+    if len(pr) == 0:
+        return out
+    pd = np.ascontiguousarray(hap_pd, dtype=np.uint8)
+    pr = np.ascontiguousarray(pr, dtype=np.int64)
+    ph = np.ascontiguousarray(ph, dtype=np.int64)
+    bad = lib().oracle_pd_compute_pairs(len(pr), _p(pr, _i64p), _p(ph, _i64p), _p(wl.read_off, _i64p),
+                                        _p(wl.bases, _u8p), _p(wl.quals, _u8p), _p(wl.ins, _u8p), _p(wl.dels, _u8p),
+                                        _p(wl.gcp, _u8p), _p(wl.hap_off, _i64p), _p(wl.hap_bases, _u8p),
+                                        _p(pd, _u8p), _p(out, _f64p), threads)
+    if bad:
+        raise ValueError(f"{bad} pairs hit 'Found unexpected base in alt alleles'")
+    return out

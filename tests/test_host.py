@@ -56,7 +56,8 @@ def test_struct_layouts_match_the_header(tmp_path):
     structs = {"ghmm_args": native.Args, "ghmm_read": native.Read, "ghmm_hap": native.Hap,
                "ghmm_region": native.Region, "ghmm_flat": native.Flat, "ghmm_stats": native.Stats,
                "ghmm_tuning": native.Tuning, "ghmm_queue_info": native.QueueInfo,
-               "ghmm_dev_pairs": native.DevPairs, "ghmm_calib_batch": native.CalibBatch}
+               "ghmm_dev_pairs": native.DevPairs, "ghmm_calib_batch": native.CalibBatch,
+               "ghmm_postprocess": native.Postprocess}
     src = tmp_path / "sizes.c"
     src.write_text('#include <stdio.h>\n#include "ghmm.h"\n#include "ghmm_calib.h"\nint main(void) {\n' +
                    "".join(f'printf("{n} %zu\\n", sizeof({n}));\n' for n in structs) + "return 0;\n}\n")

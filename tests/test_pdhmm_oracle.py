@@ -1,0 +1,143 @@
+"""The PD-HMM oracle (oracle/pdhmm_oracle.c) against an independent pure-Python restatement of
+LoglessPDPairHMM.subComputeReadLikelihoodGivenHaplotypeLog10 (LoglessPDPairHMM.java:35-150) on small cases, and
+against the plain LoglessPairHMM oracle where no PD flag is set.  The reference's PD-HMM golden file is a git-lfs
+pointer in this checkout, so these restatements are the pin."""
+import math
+
+import numpy as np
+import pytest
+
+from gatk_gb300 import workload as W
+from oracle import oracle as O
+
+SNP, DS, DE = 1, 2, 4
+BIT = {ord("A"): 8, ord("C"): 16, ord("G"): 32, ord("T"): 64}
+
+
+def _py_pdhmm(hap, pd, read, q, ins, dl, gcp):
+    """Full-matrix transliteration (small cases only)."""
+    R, H = len(read), len(hap)
+    M = [[0.0] * (H + 1) for _ in range(R + 1)]
+    I = [[0.0] * (H + 1) for _ in range(R + 1)]
+    D = [[0.0] * (H + 1) for _ in range(R + 1)]
+    bM = [[0.0] * (H + 1) for _ in range(R + 1)]
+    bI = [[0.0] * (H + 1) for _ in range(R + 1)]
+    bD = [[0.0] * (H + 1) for _ in range(R + 1)]
+    init = 2.0 ** 1020 / H
+    for j in range(H + 1):
+        D[0][j] = init
+    state = 0  # 0 NORMAL, 1 INSIDE_DEL, 2 AFTER_DEL
+    for i in range(1, R + 1):
+        t = np.zeros(6)
+        O.lib().oracle_qual_to_trans_probs(t.ctypes.data_as(O._f64p), int(ins[i - 1]), int(dl[i - 1]), int(gcp[i - 1]))
+        MM, IM, MI, II, MD, DD = t
+        x = read[i - 1]
+        for j in range(1, H + 1):
+            y, f = hap[j - 1], pd[j - 1]
+            pdm = bool(f & SNP) and bool(f & BIT.get(x, 0))
+            m = x == y or x == ord("N") or y == ord("N") or pdm
+            prior = O.lib().oracle_qual_to_prob(int(q[i - 1])) if m else O.lib().oracle_qual_to_error_prob(int(q[i - 1])) / 3.0
+            if state in (0, 1):
+                if state == 0:
+                    bM[i][j], bD[i][j], bI[i][j] = M[i][j - 1], D[i][j - 1], I[i][j - 1]
+                else:
+                    bM[i][j], bD[i][j], bI[i][j] = bM[i][j - 1], bD[i][j - 1], bI[i][j - 1]
+                M[i][j] = prior * (M[i - 1][j - 1] * MM + I[i - 1][j - 1] * IM + D[i - 1][j - 1] * IM)
+                D[i][j] = M[i][j - 1] * MD + D[i][j - 1] * DD
+            else:
+                bM[i][j] = max(bM[i][j - 1], M[i][j - 1])
+                bD[i][j] = max(bD[i][j - 1], D[i][j - 1])
+                bI[i][j] = max(bI[i][j - 1], I[i][j - 1])
+                M[i][j] = prior * (max(bM[i - 1][j - 1], M[i - 1][j - 1]) * MM + max(bI[i - 1][j - 1], I[i - 1][j - 1]) * IM
+                                   + max(bD[i - 1][j - 1], D[i - 1][j - 1]) * IM)
+                D[i][j] = max(bM[i][j - 1], M[i][j - 1]) * MD + max(bD[i][j - 1], D[i][j - 1]) * DD
+            if f & DE:
+                I[i][j] = max(bM[i - 1][j], M[i - 1][j]) * MI + max(bI[i - 1][j], I[i - 1][j]) * II
+            else:
+                I[i][j] = M[i - 1][j] * MI + I[i - 1][j] * II
+            if state == 2:
+                state = 0
+            if f & DS:
+                state = 1
+            if f & DE:
+                state = 2
+    s = 0.0
+    for j in range(1, H + 1):
+        s += M[R][j] + I[R][j]
+    return math.log10(s) - math.log10(2.0 ** 1020)
+
+
+def _case(rng, H=40, R=25, n_snp=2, n_del=1, dl=(1, 6), end_flag=False):
+    hap = rng.choice(list(b"ACGT"), size=H).astype(np.uint8)
+    pd = np.zeros(H, dtype=np.uint8)
+    for _ in range(n_snp):
+        j = int(rng.integers(0, H))
+        alt = [c for c in b"ACGT" if c != hap[j]][int(rng.integers(0, 3))]
+        pd[j] |= SNP | BIT[alt]
+    for _ in range(n_del):
+        n = int(rng.integers(dl[0], dl[1] + 1))
+        j = int(rng.integers(1, H - n))
+        pd[j] |= DS
+        pd[j + n - 1] |= DE
+    if end_flag:
+        pd[H - 1] |= DS if rng.integers(0, 2) else DE
+    off = int(rng.integers(0, H - R + 1))
+    read = hap[off:off + R].copy()
+    for k in range(R):  # a few substitutions, some to the SNP alternative
+        if rng.random() < 0.1:
+            read[k] = rng.choice(list(b"ACGT"))
+    q = rng.integers(10, 41, size=R).astype(np.uint8)
+    ins = rng.integers(20, 46, size=R).astype(np.uint8)
+    dls = rng.integers(20, 46, size=R).astype(np.uint8)
+    g = np.full(R, 10, dtype=np.uint8)
+    return hap, pd, read, q, ins, dls, g
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_c_oracle_matches_python_restatement(seed):
+    rng = np.random.default_rng(seed)
+    case = _case(rng, n_del=1 + seed % 3, end_flag=(seed % 4 == 3))
+    assert O.pd_logless(*case) == _py_pdhmm(*[np.asarray(c) for c in case]) or \
+        abs(O.pd_logless(*case) - _py_pdhmm(*[np.asarray(c) for c in case])) <= 1e-12
+
+
+def test_without_flags_equals_plain_logless():
+    wl = W.generate(0)
+    plain = O.compute_workload(wl)
+    pd = O.pd_compute_workload(wl, np.zeros(len(wl.hap_bases), dtype=np.uint8))
+    assert np.array_equal(plain, pd)
+
+
+def test_flags_change_the_likelihood_and_snp_alt_matches():
+    # a read carrying the SNP alternative: the PD haplotype gives a higher likelihood than the plain one
+    hap = b"ACGTACGTACGTACGTACGTAAAACCCCGGGGTTTT"
+    read = bytearray(hap[5:30])
+    j = 12
+    read[j - 5] = ord("G") if hap[j] != ord("G") else ord("T")
+    pd = np.zeros(len(hap), dtype=np.uint8)
+    pd[j] = SNP | BIT[read[j - 5]]
+    n = len(read)
+    args = ([30] * n, [45] * n, [45] * n, [10] * n)
+    with_pd = O.pd_logless(hap, pd, bytes(read), *args)
+    without = O.pd_logless(hap, np.zeros(len(hap), np.uint8), bytes(read), *args)
+    assert with_pd > without + 1.0
+
+
+def test_unexpected_base_with_snp_flag_raises():
+    hap = b"ACGTACGTACGT"
+    pd = np.zeros(len(hap), dtype=np.uint8)
+    pd[3] = SNP | BIT[ord("A")]
+    with pytest.raises(ValueError):
+        O.pd_logless(hap, pd, b"ACGRAC", [30] * 6, [45] * 6, [45] * 6, [10] * 6)
+
+
+def test_synthetic_flags_are_deterministic_and_well_formed():
+    wl = W.generate(1, regions=30)
+    a = W.pd_flags(wl)
+    b = W.pd_flags(wl)
+    assert np.array_equal(a, b)
+    assert (a & SNP).sum() > 0 and (a & DS).sum() > 0
+    # every SNP flag names an alternative base different from the haplotype base
+    snp = (a & SNP) != 0
+    for k in np.nonzero(snp)[0][:200]:
+        assert not (a[k] & BIT[int(wl.hap_bases[k])]) or bin(int(a[k]) >> 3).count("1") > 1
