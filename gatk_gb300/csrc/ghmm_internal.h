@@ -93,6 +93,17 @@ constexpr double kMaxGrowth64 = 1e10;
 int fp32_kernel_occupancy(int k, int block, int *blocks_per_sm);
 int fp64_kernel_occupancy(int block, int *blocks_per_sm);
 
+// PD-HMM (pd.cu): per haplotype column, the PD flag byte (PartiallyDeterminedHaplotype bits) and the HMM state
+// code: bits 0-1 the state the read's first row uses at this column, bits 2-3 the state of the other rows
+// (0 NORMAL, 1 INSIDE_DEL, 2 AFTER_DEL), bit 4 this column carries DEL_END.
+struct PdPlanes {
+    const uint8_t *flags;
+    const uint8_t *states;
+};
+int pd_kernel_occupancy(int *blocks_per_sm);
+int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int grid, cudaStream_t s);
+constexpr int kPdRowsPerLane = 4;
+
 // Post-likelihood normalisation and filtering (post.cu).
 struct PostArgs {
     double cap;                   // log10globalReadMismappingRate (< 0)

@@ -1,0 +1,261 @@
+// pd.cu -- the partially-determined-haplotype PairHMM (PD-HMM) forward on the GPU.
+//
+// The recurrence is LoglessPDPairHMM's (src/main/java/org/broadinstitute/hellbender/utils/pairhmm/
+// LoglessPDPairHMM.java:35-150): LoglessPairHMM's M/I/D plus three branch matrices bM/bI/bD that carry the state
+// from before an undetermined deletion.  Along a row every column is processed in one of three states, set by the
+// PD flags of the previous column (DEL_START enters INSIDE_DEL, DEL_END enters AFTER_DEL, AFTER_DEL lasts one
+// column):
+//    NORMAL:     bX(i,j) = X(i,j-1)
+//    INSIDE_DEL: bX(i,j) = bX(i,j-1)
+//    AFTER_DEL:  bX(i,j) = max(bX(i,j-1), X(i,j-1)), and M and D read max(bX, X) of their diagonal / left inputs
+// and at a DEL_END column I reads max(bX, X) of the row above.  The state carries from the end of one row to the
+// start of the next, so row 1 and rows >= 2 can see different states at the first columns; the host computes both
+// sequences per haplotype column (pd_attach in runtime.cpp) and the kernel takes row 1's for the read's first row.
+// The prior also matches a read base against an undetermined SNP's alternative (isBasePDMatching, :196-210).
+//
+// Kernel: one (read, haplotype) pair per warp, K rows per lane, the anti-diagonal wavefront of the FP64 kernels in
+// kernels.cu with six values per row, strips of 32*K rows through per-warp scratch (six doubles per column), FP64 at
+// the reference's scale 2^1020.  Steps where no lane of the warp is at an AFTER_DEL or DEL_END column (nearly all)
+// take a path without max(); the rest take the general one.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "ghmm_internal.h"
+
+namespace ghmm {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr double kLog10Scale = 307.0505955772608;  // log10(2^1020)
+constexpr int kPdK = 4;
+constexpr int kPdBlock = 128;
+
+__device__ __forceinline__ uint32_t pd_base_bit(uint32_t x) {
+    switch (x) {
+        case 'A': case 'a': return 8u;
+        case 'C': case 'c': return 16u;
+        case 'G': case 'g': return 32u;
+        case 'T': case 't': return 64u;
+        default: return 0u;
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kPdBlock) pd_fp64_kernel(DevTables T, DevBatch B, PdPlanes P) {
+    constexpr int S = 32 * K;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    double *scratch = B.scratch64 + warp_global * B.scratch64_cols * 6;
+    const int total = min(B.counters[1], (int)B.rerun_capacity);
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&B.counters[2], 1);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= total) break;
+        const PairRef pr = B.rerun[t];
+        const int read = pr.read, hap = pr.hap;
+        const int64_t roff = B.read_off[read];
+        const int R = (int)(B.read_off[read + 1] - roff);
+        const int64_t hoff = B.hap_off[hap];
+        const int H = (int)(B.hap_off[hap + 1] - hoff);
+        const int region = B.read_region[read];
+        const int64_t nh = B.region_hap_off[region + 1] - B.region_hap_off[region];
+        const int64_t out_index = B.out_off[region] + (int64_t)(read - B.region_read_off[region]) * nh +
+                                  (hap - B.region_hap_off[region]);
+        if (R == 0 || H == 0) {
+            if (lane == 0) B.out[out_index] = -INFINITY;
+            continue;
+        }
+        if (H > B.scratch64_cols && R > S) {
+            if (lane == 0) atomicExch(&B.counters[3], 2);
+            continue;
+        }
+        const double init = B.hap_init_d[hap];
+        const int nstrips = (R + S - 1) / S;
+        const int pad = nstrips * S - R;
+        const uint8_t *hb = B.hap_bases + hoff;
+        const uint8_t *hf = P.flags + hoff;
+        const uint8_t *hs = P.states + hoff;
+        double acc = 0.0;
+        for (int strip = 0; strip < nstrips; ++strip) {
+            double pm[K], pe[K], tmm[K], tim[K], tmi[K], tii[K], tmd[K], tdd[K];
+            uint32_t rbase[K], rbit[K];
+            bool first[K], dummy[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int p = strip * S + lane * K + k - pad;
+                dummy[k] = p < 0;
+                first[k] = p == 0;
+                if (p < 0) {
+                    pm[k] = pe[k] = 0.0;
+                    tmm[k] = tim[k] = tmi[k] = tii[k] = tmd[k] = 0.0;
+                    tdd[k] = 1.0;  // a dummy row holds the row-0 D value
+                    rbase[k] = 0x100u;
+                    rbit[k] = 0u;
+                } else {
+                    const uint8_t base = B.bases[roff + p], q = B.quals[roff + p];
+                    const uint8_t ins = B.ins[roff + p], del = B.dels[roff + p], gcp = B.gcp[roff + p];
+                    pm[k] = __ldg(T.prob_d + q);
+                    pe[k] = __ldg(T.err3_d + q);
+                    tmm[k] = __ldg(T.m2m_d + ins * 128 + del);
+                    tim[k] = __ldg(T.prob_d + gcp);
+                    tmi[k] = __ldg(T.err_d + ins);
+                    tii[k] = __ldg(T.err_d + gcp);
+                    tmd[k] = __ldg(T.err_d + del);
+                    tdd[k] = tii[k];
+                    rbase[k] = base;
+                    rbit[k] = pd_base_bit(base);
+                }
+            }
+            double Mp[K], Ip[K], Dp[K], bM[K], bI[K], bD[K];
+            auto reset = [&]() {
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    Mp[k] = Ip[k] = 0.0;
+                    Dp[k] = dummy[k] ? init : 0.0;
+                    bM[k] = bI[k] = bD[k] = 0.0;
+                }
+            };
+            reset();
+            double gM = 0.0, gI = 0.0, gbM = 0.0, gbI = 0.0, gbD = 0.0;
+            const bool above_dummy = (strip == 0) && (lane * K - 1 < pad);
+            double gD = above_dummy ? init : 0.0;
+            const bool last_strip = strip == nstrips - 1;
+            double nx[6] = {0, 0, 0, 0, 0, 0};
+            if (strip > 0 && lane == 0)
+#pragma unroll
+                for (int v = 0; v < 6; ++v) nx[v] = scratch[v];
+            const int nsteps = H + 31;
+            for (int s = 0; s < nsteps; ++s) {
+                const int c = s - lane;
+                const bool valid = c >= 0 && c < H;
+                uint32_t y = 0x200u, f = 0u, st = 0u;
+                if (valid) {
+                    y = __ldg(hb + c);
+                    f = __ldg(hf + c);
+                    st = __ldg(hs + c);
+                }
+                if (c == 0) {  // column-0 boundary: M = I = D = 0 (row 0: D = 2^1020 / H), branches 0
+                    reset();
+                    gM = gI = gbM = gbI = gbD = 0.0;
+                    gD = above_dummy ? init : 0.0;
+                }
+                double u[6];
+                u[0] = __shfl_up_sync(kFull, Mp[K - 1], 1);
+                u[1] = __shfl_up_sync(kFull, Ip[K - 1], 1);
+                u[2] = __shfl_up_sync(kFull, Dp[K - 1], 1);
+                u[3] = __shfl_up_sync(kFull, bM[K - 1], 1);
+                u[4] = __shfl_up_sync(kFull, bI[K - 1], 1);
+                u[5] = __shfl_up_sync(kFull, bD[K - 1], 1);
+                if (lane == 0) {
+                    if (strip == 0) {
+                        u[0] = u[1] = u[3] = u[4] = u[5] = 0.0;
+                        u[2] = init;
+                    } else {
+#pragma unroll
+                        for (int v = 0; v < 6; ++v) u[v] = nx[v];
+                        if (c + 1 < H)
+#pragma unroll
+                            for (int v = 0; v < 6; ++v) nx[v] = scratch[6 * (c + 1) + v];
+                    }
+                }
+                const uint32_t st1 = st & 3u, st2 = (st >> 2) & 3u;
+                const bool del_end = (st & 16u) != 0;
+                const bool yn = (y == 'N');
+                // the general path only when a lane of this warp sits at an AFTER_DEL or DEL_END column
+                const bool special = __any_sync(kFull, valid && (st1 == 2u || st2 == 2u || del_end));
+                // pass 1 (bottom-up, the row above still holds the previous column): branches, M, D
+#pragma unroll
+                for (int k = K - 1; k >= 0; --k) {
+                    const double dM = k ? Mp[k - 1] : gM, dI = k ? Ip[k - 1] : gI, dD = k ? Dp[k - 1] : gD;
+                    const uint32_t sk = first[k] ? st1 : st2;
+                    const bool match = rbase[k] == y || rbase[k] == 'N' || yn || ((f & 1u) && (f & rbit[k]));
+                    const double prior = match ? pm[k] : pe[k];
+                    double Mn, Dn, nbM, nbI, nbD;
+                    if (!special) {
+                        const bool inside = sk == 1u;
+                        nbM = inside ? bM[k] : Mp[k];
+                        nbI = inside ? bI[k] : Ip[k];
+                        nbD = inside ? bD[k] : Dp[k];
+                        Mn = prior * fma(dM, tmm[k], (dI + dD) * tim[k]);
+                        Dn = fma(Dp[k], tdd[k], Mp[k] * tmd[k]);
+                    } else {
+                        const double dbM = k ? bM[k - 1] : gbM, dbI = k ? bI[k - 1] : gbI, dbD = k ? bD[k - 1] : gbD;
+                        if (sk == 2u) {
+                            nbM = fmax(bM[k], Mp[k]);
+                            nbI = fmax(bI[k], Ip[k]);
+                            nbD = fmax(bD[k], Dp[k]);
+                            Mn = prior * fma(fmax(dbM, dM), tmm[k], (fmax(dbI, dI) + fmax(dbD, dD)) * tim[k]);
+                            Dn = fma(fmax(bD[k], Dp[k]), tdd[k], fmax(bM[k], Mp[k]) * tmd[k]);
+                        } else {
+                            const bool inside = sk == 1u;
+                            nbM = inside ? bM[k] : Mp[k];
+                            nbI = inside ? bI[k] : Ip[k];
+                            nbD = inside ? bD[k] : Dp[k];
+                            Mn = prior * fma(dM, tmm[k], (dI + dD) * tim[k]);
+                            Dn = fma(Dp[k], tdd[k], Mp[k] * tmd[k]);
+                        }
+                    }
+                    if (!valid) Mn = Dn = 0.0, nbM = nbI = nbD = 0.0;
+                    Mp[k] = Mn;
+                    Dp[k] = Dn;
+                    bM[k] = nbM;
+                    bI[k] = nbI;
+                    bD[k] = nbD;
+                }
+                // pass 2 (top-down): I from the row above at this column
+                double aM = u[0], aI = u[1], abM = u[3], abI = u[4];
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    double In;
+                    if (special && del_end)
+                        In = fma(fmax(abI, aI), tii[k], fmax(abM, aM) * tmi[k]);
+                    else
+                        In = fma(aI, tii[k], aM * tmi[k]);
+                    if (!valid) In = 0.0;
+                    Ip[k] = In;
+                    aM = Mp[k];
+                    aI = In;
+                    abM = bM[k];
+                    abI = bI[k];
+                }
+                gM = u[0];
+                gI = u[1];
+                gD = u[2];
+                gbM = u[3];
+                gbI = u[4];
+                gbD = u[5];
+                if (valid && lane == 31) {
+                    if (last_strip) {
+                        acc += Mp[K - 1] + Ip[K - 1];
+                    } else {
+                        double *d = scratch + 6 * c;
+                        d[0] = Mp[K - 1];
+                        d[1] = Ip[K - 1];
+                        d[2] = Dp[K - 1];
+                        d[3] = bM[K - 1];
+                        d[4] = bI[K - 1];
+                        d[5] = bD[K - 1];
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        if (lane == 31) B.out[out_index] = log10(acc) - kLog10Scale;
+    }
+}
+
+}  // namespace
+
+int pd_kernel_occupancy(int *blocks_per_sm) {
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pd_fp64_kernel<kPdK>, kPdBlock, 0);
+}
+
+int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int grid, cudaStream_t s) {
+    pd_fp64_kernel<kPdK><<<grid, kPdBlock, 0, s>>>(t, b, p);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace ghmm

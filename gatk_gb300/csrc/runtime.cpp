@@ -163,6 +163,11 @@ struct ghmm_batch {
     DevBuf<int32_t> d_counters;  // same layout as h_counters
     DevBuf<int64_t> d_nout;
     DevBuf<uint8_t> d_post;  // postprocess: reference haplotype per region, keep flags per read
+    // PD-HMM batches: PD flags then state codes per haplotype column (pd.cu)
+    HostBuf<uint8_t> h_pd;
+    DevBuf<uint8_t> d_pd;
+    bool has_pd = false;
+    PdPlanes pd{};
     DevBuf<float2> d_scratch32;
     DevBuf<double> d_scratch64;
     // sizes
@@ -210,7 +215,8 @@ struct ghmm_batch {
         h_init_d.release(); h_tasks.release(); h_direct.release(); h_fp64all.release(); h_out.release(); h_counters.release();
         d_planes.release(); d_hap.release(); d_off.release(); d_read_region.release(); d_init_f.release();
         d_init_d.release(); d_tasks.release(); d_rerun.release(); d_out.release(); d_counters.release();
-        d_scratch32.release(); d_scratch64.release(); d_post.release();
+        d_scratch32.release(); d_scratch64.release(); d_post.release(); h_pd.release(); d_pd.release();
+        has_pd = false;
     }
 };
 
@@ -226,6 +232,7 @@ struct ghmm_ctx {
     HostTables *host_tables = nullptr;  // host copy, for routing decisions
     std::string last_error;
     ghmm_batch scratch_batch;  // reused by the one-shot entry points
+    ghmm_batch pd_batch;       // reused by the one-shot PD-HMM entry points
     int max_k = kMaxK32, max_k_multi = kMaxK32, chunk_cols = 16384;
     // calibration scratch (checkpointed fronts per resident warp), FP64-redo flags, unit weights
     DevBuf<uint8_t> calib_scratch;
@@ -729,8 +736,14 @@ static int fill_fp64_all(ghmm_ctx *ctx, ghmm_batch &b) {
 static int batch_enqueue(ghmm_ctx *ctx, ghmm_batch &b, int mode, cudaStream_t s);
 static int batch_finish(ghmm_ctx *ctx, ghmm_batch &b);
 
+static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b);
+
 static int batch_forward(ghmm_ctx *ctx, ghmm_batch &b, int mode) {
     if (!b.uploaded) return fail(ctx, GHMM_ERR_STATE, "batch not uploaded");
+    if (b.has_pd != (mode == GHMM_MODE_PD))
+        return fail(ctx, GHMM_ERR_ARG, b.has_pd ? "a PD-HMM batch runs in GHMM_MODE_PD only"
+                                                : "GHMM_MODE_PD needs a batch from ghmm_pd_batch_create");
+    if (mode == GHMM_MODE_PD) return batch_forward_pd(ctx, b);
     if (ctx->double_precision && mode == GHMM_MODE_FP32_RERUN) mode = GHMM_MODE_FP64;
     cudaStream_t s = ctx->stream;
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -1308,6 +1321,159 @@ int compute_sync(ghmm_ctx *ctx, const Source &src, double *out) {
 
 }  // namespace
 
+
+// -------------------------------------------------------------------------------------------------
+// PD-HMM batches: the regular marshal over the haplotypes' bases, plus per haplotype column the PD flags and the
+// HMM state codes (PdPlanes), and a forward that runs every pair through pd.cu.
+
+namespace {
+
+// State sequence along one row (LoglessPDPairHMM.java:62-142): the state a column is processed in, then AFTER_DEL
+// ends, DEL_START enters INSIDE_DEL, DEL_END enters AFTER_DEL.  Returns the state after the last column.
+int pd_states(const uint8_t *f, int H, int start, uint8_t *code, int shift) {
+    int st = start;
+    for (int j = 0; j < H; j++) {
+        code[j] |= (uint8_t)(st << shift);
+        if (st == 2) st = 0;
+        if (f[j] & 2) st = 1;
+        if (f[j] & 4) st = 2;
+    }
+    return st;
+}
+
+bool pd_read_base_ok(uint8_t x) {
+    switch (x) {
+        case 'A': case 'C': case 'G': case 'T': case 'a': case 'c': case 'g': case 't': case 'N': return true;
+        default: return false;
+    }
+}
+
+}  // namespace
+
+static int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch &b) {
+    std::vector<ghmm_region> rr((size_t)G);
+    std::vector<std::vector<ghmm_hap>> hh((size_t)G);
+    std::vector<const uint8_t *> pdp;
+    for (int64_t g = 0; g < G; g++) {
+        const ghmm_pd_region &rg = regs[g];
+        if (rg.n_reads < 0 || rg.n_haps < 0 || (rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps))
+            return fail(ctx, GHMM_ERR_ARG, "bad PD region");
+        hh[(size_t)g].resize((size_t)rg.n_haps);
+        for (int32_t h = 0; h < rg.n_haps; h++) {
+            const ghmm_pd_hap &hp = rg.haps[h];
+            if (hp.length > 0 && (!hp.bases || !hp.pd_bases)) return fail(ctx, GHMM_ERR_ARG, "NULL PD haplotype array");
+            hh[(size_t)g][(size_t)h] = ghmm_hap{hp.bases, hp.length};
+            pdp.push_back(hp.pd_bases);
+        }
+        rr[(size_t)g] = ghmm_region{rg.reads, rg.n_reads, hh[(size_t)g].data(), rg.n_haps};
+    }
+    Source src;
+    src.regions = rr.data();
+    src.n_regions = G;
+    int rc = batch_marshal(ctx, src, b);
+    if (rc) return rc;
+    const int64_t NH = b.n_haps, HB = b.hap_bytes;
+    GHMM_CUDA(b.h_pd.reserve((size_t)std::max<int64_t>(2 * HB, 1)), "pinned PD planes");
+    const int64_t *o = b.h_off.p;
+    const int64_t *hap_off = o + b.n_reads + 1;
+    uint8_t *flags = b.h_pd.p, *states = b.h_pd.p + HB;
+    parallel_for(NH, hw_threads(ctx->max_threads), [&](int64_t h) {
+        const int64_t a = hap_off[h];
+        const int H = (int)(hap_off[h + 1] - a);
+        if (H <= 0) return;
+        memcpy(flags + a, pdp[(size_t)h], (size_t)H);
+        uint8_t *code = states + a;
+        memset(code, 0, (size_t)H);
+        const int end1 = pd_states(flags + a, H, 0, code, 0);
+        pd_states(flags + a, H, end1, code, 2);
+        for (int j = 0; j < H; j++)
+            if (flags[a + j] & 4) code[j] |= 16;
+    });
+    // a read base outside ACGTacgtN that meets an undetermined SNP column throws in the reference
+    const int64_t *rro = o + b.n_reads + 1 + NH + 1, *rho = rro + G + 1;
+    const uint8_t *bases = b.h_planes.p;
+    const uint8_t *hraw = b.h_hap.p;
+    for (int64_t g = 0; g < G; g++)
+        for (int64_t r = rro[g]; r < rro[g + 1]; r++)
+            for (int64_t i = o[r]; i < o[r + 1]; i++) {
+                const uint8_t x = bases[i];
+                if (pd_read_base_ok(x)) continue;
+                for (int64_t h = rho[g]; h < rho[g + 1]; h++)
+                    for (int64_t j = hap_off[h]; j < hap_off[h + 1]; j++)
+                        if ((flags[j] & 1) && hraw[j] != x && hraw[j] != 'N')
+                            return fail(ctx, GHMM_ERR_ARG, "Found unexpected base in alt alleles");
+            }
+    b.has_pd = true;
+    return GHMM_OK;
+}
+
+static int pd_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
+    int rc = batch_upload(ctx, b, s);
+    if (rc) return rc;
+    const int64_t HB = b.hap_bytes;
+    GHMM_CUDA(b.d_pd.reserve((size_t)std::max<int64_t>(2 * HB, 1)), "device PD planes");
+    if (HB > 0)
+        GHMM_CUDA(cudaMemcpyAsync(b.d_pd.p, b.h_pd.p, (size_t)(2 * HB), cudaMemcpyHostToDevice, s), "H2D PD planes");
+    b.pd.flags = b.d_pd.p;
+    b.pd.states = b.d_pd.p + HB;
+    b.upload_bytes += 2 * HB;
+    return GHMM_OK;
+}
+
+static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b) {
+    cudaStream_t s = ctx->stream;
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    // every pair, read-major per region
+    GHMM_CUDA(b.h_fp64all.reserve((size_t)std::max<int64_t>(b.n_out, 1)), "pinned PD pairs");
+    const int64_t *o = b.h_off.p;
+    const int64_t *rro = o + b.n_reads + 1 + b.n_haps + 1, *rho = rro + b.n_regions + 1;
+    int64_t k = 0;
+    for (int64_t g = 0; g < b.n_regions; g++)
+        for (int64_t r = rro[g]; r < rro[g + 1]; r++)
+            for (int64_t h = rho[g]; h < rho[g + 1]; h++) b.h_fp64all.p[k++] = PairRef{(int32_t)r, (int32_t)h};
+    int bpsm = 0;
+    if (pd_kernel_occupancy(&bpsm) != 0 || bpsm <= 0) bpsm = 1;
+    const int grid = ctx->sm_count * bpsm;
+    const size_t scr = (size_t)grid * (kBlock / 32) * (size_t)std::max(b.max_hap_len, 1) * 6;
+    GHMM_CUDA(b.d_scratch64.reserve(scr), "device PD strip scratch");
+    b.dev.scratch64 = b.d_scratch64.p;
+    b.dev.scratch64_cols = std::max(b.max_hap_len, 1);
+    if (!b.events_ready) {
+        for (auto &e : b.ev) GHMM_CUDA(cudaEventCreate(&e), "cudaEventCreate");
+        b.events_ready = true;
+    }
+    GHMM_CUDA(cudaEventRecord(b.ev[0], s), "event");
+    if (k > 0)
+        GHMM_CUDA(cudaMemcpyAsync(b.d_rerun.p, b.h_fp64all.p, (size_t)k * sizeof(PairRef), cudaMemcpyHostToDevice, s),
+                  "H2D PD pairs");
+    int32_t *hc = b.h_counters.p;
+    for (int i = 0; i < kNumCounters + 2 * kNumBucketKeys; i++) hc[i] = 0;
+    hc[1] = (int32_t)k;
+    GHMM_CUDA(cudaMemcpyAsync(b.d_counters.p, hc, (kNumCounters + 2 * kNumBucketKeys) * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, s), "H2D counters");
+    GHMM_CUDA(cudaEventRecord(b.ev[1], s), "event");
+    int e = launch_pd(ctx->tables, b.dev, b.pd, grid, s);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "PD-HMM launch");
+    GHMM_CUDA(cudaEventRecord(b.ev[2], s), "event");
+    GHMM_CUDA(cudaMemcpyAsync(hc, b.d_counters.p, kNumCounters * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
+              "D2H counters");
+    GHMM_CUDA(cudaEventRecord(b.ev[3], s), "event");
+    GHMM_CUDA(cudaEventSynchronize(b.ev[3]), "PD-HMM kernel");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, b.ev[1], b.ev[2]);
+    b.ms_fp64 = ms;
+    b.ms_fp32 = b.ms_plain = 0;
+    cudaEventElapsedTime(&ms, b.ev[0], b.ev[3]);
+    b.ms_total = ms;
+    b.last_mode = GHMM_MODE_PD;
+    b.last_launches = 1;
+    b.last_rerun = b.last_exact = 0;
+    b.forward_h2d = k * (int64_t)sizeof(PairRef) + (kNumCounters + 2 * kNumBucketKeys) * 4;
+    b.forward_d2h = kNumCounters * 4;
+    if (hc[3] != 0) return fail(ctx, GHMM_ERR_CUDA, "device-side scratch bound exceeded");
+    return GHMM_OK;
+}
+
 void ghmm::set_global_error(const char *msg) {
     std::lock_guard<std::mutex> lk(g_init_error_mu);
     g_init_error = msg ? msg : "";
@@ -1462,6 +1628,7 @@ int ghmm_done(ghmm_ctx *ctx) {
     ctx->pipe = nullptr;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     ctx->scratch_batch.release();
+    ctx->pd_batch.release();
     ctx->calib_scratch.release();
     ctx->calib_flags.release();
     ctx->calib_ones.release();
@@ -1547,7 +1714,7 @@ int ghmm_batch_create_flat(ghmm_ctx *ctx, const ghmm_flat *flat, ghmm_batch **ou
 int ghmm_batch_forward(ghmm_ctx *ctx, ghmm_batch *b, int32_t mode) {
     if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
     if (!b) return fail(ctx, GHMM_ERR_ARG, "NULL batch");
-    if (mode < 0 || mode > 2) return fail(ctx, GHMM_ERR_ARG, "unknown mode");
+    if (mode < 0 || mode > 3) return fail(ctx, GHMM_ERR_ARG, "unknown mode");
     return batch_forward(ctx, *b, mode);
 }
 
@@ -1709,6 +1876,44 @@ int ghmm_get_tuning(ghmm_ctx *ctx, ghmm_tuning *t) {
     if (!t) return fail(ctx, GHMM_ERR_ARG, "NULL tuning");
     *t = ghmm_tuning{ctx->max_k, ctx->max_k_multi, ctx->chunk_cols, 0};
     return GHMM_OK;
+}
+
+int ghmm_pd_batch_create(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_t n_regions, ghmm_batch **out) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!out || n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad arguments");
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    auto *b = new ghmm_batch();
+    int rc = pd_marshal(ctx, regions, n_regions, *b);
+    if (!rc) rc = pd_upload(ctx, *b, ctx->stream);
+    if (!rc) rc = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? GHMM_OK : fail(ctx, GHMM_ERR_CUDA, "upload");
+    if (rc) {
+        b->release();
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return GHMM_OK;
+}
+
+int ghmm_pd_compute_regions(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_t n_regions, double *out) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad region array");
+    if (n_regions == 0) return GHMM_OK;
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    ghmm_batch &b = ctx->pd_batch;
+    int rc = pd_marshal(ctx, regions, n_regions, b);
+    if (!rc) rc = pd_upload(ctx, b, ctx->stream);
+    if (!rc) rc = batch_forward(ctx, b, GHMM_MODE_PD);
+    if (!rc) rc = batch_results(ctx, b, out);
+    return rc;
+}
+
+int ghmm_pd_compute_likelihoods(ghmm_ctx *ctx, const ghmm_read *reads, int32_t n_reads, const ghmm_pd_hap *haps,
+                                int32_t n_haps, double *out) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (n_reads == 0 || n_haps == 0) return GHMM_OK;
+    ghmm_pd_region r{reads, n_reads, haps, n_haps};
+    return ghmm_pd_compute_regions(ctx, &r, 1, out);
 }
 
 int ghmm_queue_create(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **queue) {

@@ -22,6 +22,7 @@ GHMM_ERR_TIMEOUT = 7
 
 MODE_FP32_RERUN = 0
 MODE_FP64 = 1
+MODE_PD = 3
 FP64_RESCALED_FLOOR = -500.0  # GHMM_FP64_RESCALED_FLOOR
 MODE_PLAIN_FP64 = 2
 
@@ -77,6 +78,16 @@ class Stats(ctypes.Structure):
                 ("ms_plain", ctypes.c_double), ("ms_total", ctypes.c_double), ("h2d_bytes", ctypes.c_int64),
                 ("d2h_bytes", ctypes.c_int64), ("ms_host_marshal", ctypes.c_double),
                 ("ms_host_tasks", ctypes.c_double), ("n_fp64_exact", ctypes.c_int64)]
+
+
+class PdHap(ctypes.Structure):
+    _fields_ = [("bases", ctypes.c_void_p), ("pd_bases", ctypes.c_void_p), ("length", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class PdRegion(ctypes.Structure):
+    _fields_ = [("reads", ctypes.c_void_p), ("n_reads", ctypes.c_int32), ("haps", ctypes.c_void_p),
+                ("n_haps", ctypes.c_int32)]
 
 
 class Postprocess(ctypes.Structure):
@@ -141,6 +152,11 @@ _SIGS = {
     "ghmm_batch_results": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _f64p]),
     "ghmm_batch_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Stats)]),
     "ghmm_batch_destroy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "ghmm_pd_compute_likelihoods": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Read), ctypes.c_int32,
+                                                   ctypes.POINTER(PdHap), ctypes.c_int32, _f64p]),
+    "ghmm_pd_compute_regions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, _f64p]),
+    "ghmm_pd_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                            ctypes.POINTER(ctypes.c_void_p)]),
     "ghmm_batch_postprocess": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Postprocess),
                                               ctypes.c_void_p]),
     "ghmm_compute_flat": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Flat), _f64p]),

@@ -180,6 +180,19 @@ class Engine:
     def batch(self, wl: Workload, via_regions: bool = False) -> "Batch":
         return Batch(self, wl, via_regions)
 
+    def pd_compute(self, wl: Workload, hap_pd: np.ndarray) -> np.ndarray:
+        """PD-HMM log10 likelihoods of every pair (haplotypes with PD flags), host buffers in and out."""
+        from .workload import as_pd_regions
+
+        out = np.empty(max(wl.n_pairs, 1), dtype=np.float64)
+        regs = as_pd_regions(wl, hap_pd)
+        native.check(self.L.ghmm_pd_compute_regions(self._ctx.h, regs, wl.n_regions, out.ctypes.data_as(native._f64p)),
+                     self._ctx.h)
+        return out[:wl.n_pairs]
+
+    def pd_batch(self, wl: Workload, hap_pd: np.ndarray) -> "Batch":
+        return Batch(self, wl, pd=hap_pd)
+
     def queue(self, batch_cells: int = 0) -> "Queue":
         return Queue(self, batch_cells)
 
@@ -205,11 +218,16 @@ class Engine:
 class Batch:
     """A device-resident batch: inputs uploaded once; forward() reruns the kernels on them."""
 
-    def __init__(self, engine: Engine, wl: Workload, via_regions: bool = False):
+    def __init__(self, engine: Engine, wl: Workload, via_regions: bool = False, pd=None):
         self.engine = engine
         self.wl = wl
         h = ctypes.c_void_p()
-        if via_regions:
+        if pd is not None:
+            from .workload import as_pd_regions
+
+            regs = as_pd_regions(wl, pd)
+            rc = engine.L.ghmm_pd_batch_create(engine.handle, regs, wl.n_regions, ctypes.byref(h))
+        elif via_regions:
             regs = wl.as_regions()
             rc = engine.L.ghmm_batch_create(engine.handle, regs, wl.n_regions, ctypes.byref(h))
         else:

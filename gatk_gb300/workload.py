@@ -136,6 +136,26 @@ class Workload:
         return rg.ctypes.data_as(ctypes.POINTER(native.Region))
 
 
+def as_pd_regions(wl: Workload, hap_pd: np.ndarray):
+    """ghmm_pd_region array for a workload whose haplotypes carry PD flags (hap_pd, parallel to hap_bases)."""
+    NR, NH, G = wl.n_reads, wl.n_haps, wl.n_regions
+    wl.as_regions()  # builds the per-read structs (kept alive in wl._keep)
+    rd = wl._keep[-1][0]
+    pd = np.ascontiguousarray(hap_pd, dtype=np.uint8)
+    hp = np.zeros(max(NH, 1), dtype=[("p", "<u8"), ("f", "<u8"), ("len", "<i4"), ("pad", "<i4")])
+    hp["p"][:NH] = np.uint64(wl.hap_bases.ctypes.data) + wl.hap_off[:-1].astype(np.uint64)
+    hp["f"][:NH] = np.uint64(pd.ctypes.data) + wl.hap_off[:-1].astype(np.uint64)
+    hp["len"][:NH] = np.diff(wl.hap_off)
+    rg = np.zeros(max(G, 1), dtype=[("reads", "<u8"), ("n_reads", "<i4"), ("pad0", "<i4"), ("haps", "<u8"),
+                                    ("n_haps", "<i4"), ("pad1", "<i4")])
+    rg["reads"][:G] = np.uint64(rd.ctypes.data) + wl.region_read_off[:-1].astype(np.uint64) * np.uint64(48)
+    rg["n_reads"][:G] = np.diff(wl.region_read_off)
+    rg["haps"][:G] = np.uint64(hp.ctypes.data) + wl.region_hap_off[:-1].astype(np.uint64) * np.uint64(24)
+    rg["n_haps"][:G] = np.diff(wl.region_hap_off)
+    wl._keep.append((pd, hp, rg))
+    return rg.ctypes.data
+
+
 def generate(workload: int, regions: int | None = None, seed: int | None = None, region_begin: int = 0,
              threads: int = 0) -> Workload:
     """Synthetic workload `workload` (0-4), regions [region_begin, region_begin + regions)."""

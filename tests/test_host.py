@@ -42,6 +42,7 @@ def test_header_constants_match_the_bindings():
     assert int(defs["GHMM_MODE_FP32_RERUN"]) == native.MODE_FP32_RERUN
     assert int(defs["GHMM_MODE_FP64"]) == native.MODE_FP64
     assert int(defs["GHMM_MODE_PLAIN_FP64"]) == native.MODE_PLAIN_FP64
+    assert int(defs["GHMM_MODE_PD"]) == native.MODE_PD
     assert float(defs["GHMM_FP64_RESCALED_FLOOR"]) == native.FP64_RESCALED_FLOOR
 
 
@@ -57,7 +58,7 @@ def test_struct_layouts_match_the_header(tmp_path):
                "ghmm_region": native.Region, "ghmm_flat": native.Flat, "ghmm_stats": native.Stats,
                "ghmm_tuning": native.Tuning, "ghmm_queue_info": native.QueueInfo,
                "ghmm_dev_pairs": native.DevPairs, "ghmm_calib_batch": native.CalibBatch,
-               "ghmm_postprocess": native.Postprocess}
+               "ghmm_postprocess": native.Postprocess, "ghmm_pd_hap": native.PdHap, "ghmm_pd_region": native.PdRegion}
     src = tmp_path / "sizes.c"
     src.write_text('#include <stdio.h>\n#include "ghmm.h"\n#include "ghmm_calib.h"\nint main(void) {\n' +
                    "".join(f'printf("{n} %zu\\n", sizeof({n}));\n' for n in structs) + "return 0;\n}\n")

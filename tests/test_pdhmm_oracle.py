@@ -141,3 +141,71 @@ def test_synthetic_flags_are_deterministic_and_well_formed():
     snp = (a & SNP) != 0
     for k in np.nonzero(snp)[0][:200]:
         assert not (a[k] & BIT[int(wl.hap_bases[k])]) or bin(int(a[k]) >> 3).count("1") > 1
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# the GPU PD-HMM kernel (pd.cu) against the oracle
+
+def _pd_workload(regions=6, seed=5):
+    wl = W.generate(1, regions=regions)
+    return wl, W.pd_flags(wl, seed)
+
+
+@pytest.mark.gpu
+def test_gpu_pdhmm_matches_oracle(engine):
+    wl, pd = _pd_workload(8)
+    ref = O.pd_compute_workload(wl, pd)
+    got = engine.pd_compute(wl, pd)
+    assert np.abs(got - ref).max() <= 1e-9
+
+
+@pytest.mark.gpu
+def test_gpu_pdhmm_without_flags_equals_plain(engine):
+    wl = W.generate(1, regions=4)
+    got = engine.pd_compute(wl, np.zeros(len(wl.hap_bases), dtype=np.uint8))
+    ref = O.compute_workload(wl)
+    assert np.abs(got - ref).max() <= 1e-9
+
+
+@pytest.mark.gpu
+def test_gpu_pdhmm_hand_cases_and_long_reads(engine):
+    # deletions at the first and last columns (the state carries into the next row), single-base deletions,
+    # SNP alternatives, and reads longer than one 128-row strip
+    rng = np.random.default_rng(21)
+    regions, pds = [], []
+    for k in range(12):
+        H = int(rng.integers(150, 400))
+        R = int(rng.integers(60, 300))
+        hap, pd, read, q, ins, dls, g = _case(rng, H=H, R=min(R, H - 5), n_snp=3, n_del=1 + k % 3,
+                                               end_flag=(k % 3 == 0))
+        if k % 4 == 1:
+            pd[0] |= DS
+        regions.append(([bytes(hap)], [(bytes(read), q, ins, dls, g)]))
+        pds.append(pd)
+    wl = W.from_pairs(regions)
+    pd = np.concatenate(pds)
+    ref = O.pd_compute_workload(wl, pd)
+    got = engine.pd_compute(wl, pd)
+    assert np.abs(got - ref).max() <= 1e-9
+
+
+@pytest.mark.gpu
+def test_gpu_pdhmm_batch_and_errors(engine):
+    from gatk_gb300 import native
+
+    wl, pd = _pd_workload(3)
+    with engine.pd_batch(wl, pd) as b:
+        b.forward(native.MODE_PD)
+        a = b.results()
+        b.forward(native.MODE_PD)
+        assert np.array_equal(a, b.results())
+        with pytest.raises(native.GhmmError):
+            b.forward(native.MODE_FP32_RERUN)
+    # a read base outside ACGTacgtN meeting an undetermined SNP: the reference throws
+    hap = b"ACGTACGTACGTACGT"
+    f = np.zeros(len(hap), dtype=np.uint8)
+    f[5] = SNP | BIT[ord("A")]
+    bad = W.from_pairs([([hap], [(b"ACGRAC", [30] * 6, [45] * 6, [45] * 6, [10] * 6)])])
+    with pytest.raises(native.GhmmError) as e:
+        engine.pd_compute(bad, f)
+    assert e.value.code == native.GHMM_ERR_ARG
