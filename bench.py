@@ -4,6 +4,7 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload 1]
     python bench.py --stream [--regions N] [--batch-cells C]     (workload 4 through the streaming queue)
     python bench.py --calib                                      (workload 3: calibration forward + backward)
+    python bench.py --pd [--regions N]                           (PD-HMM, DRAGEN-GATK mode)
 
 A step is one forward over the whole workload (default: workload 1, 10,000 synthetic active regions,
 seed 1, ~1.06e12 cells): every read x haplotype pair of every region, FP32 wavefront plus the FP64 rerun
@@ -555,6 +556,78 @@ def run_calib(args):
     return 0
 
 
+def run_pd(args):
+    """--pd: the PD-HMM (LoglessPDPairHMM, DRAGEN-GATK mode) over workload 1's regions with synthetic
+    partially-determined haplotypes (1-3 undetermined SNPs and 0-2 undetermined deletions per haplotype,
+    seeded).  Device-resident GCUPS of the FP64 PD kernel, e2e through ghmm_pd_compute_regions, accuracy and the
+    CPU baseline against the FP64 PD oracle on the leading regions."""
+    import numpy as np
+
+    from gatk_gb300 import native, workload as W
+    from gatk_gb300.pairhmm import Engine
+    from oracle import oracle as O
+
+    eng = Engine()
+    peaks = eng.measure_peaks()
+    n_regions = args.regions or 1000
+    wl = W.generate(1, regions=n_regions)
+    pd = W.pd_flags(wl, 5)
+    cells = int(wl.cells_per_region().sum())
+    batch = eng.pd_batch(wl, pd)
+    for _ in range(args.warmup):
+        batch.forward(native.MODE_PD)
+    clocks = ClockSampler(0)
+    clocks.start()
+    sts = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batch.forward(native.MODE_PD)
+        sts.append(batch.stats())
+    dt_host = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    ms = statistics.mean(s["ms_total"] for s in sts)
+    ms_kernel = statistics.mean(s["ms_fp64"] for s in sts)
+    res = batch.results()
+    io = batch.stats()
+    batch.close()
+    out = eng.pd_compute(wl, pd)  # warm
+    t0 = time.perf_counter()
+    out = eng.pd_compute(wl, pd)
+    dt_e2e = time.perf_counter() - t0
+    n_cpu, cpu_cells = cpu_sample(wl, args.cpu_cells / 4)
+    sub = wl.subset(0, n_cpu)
+    sub_pd = pd[: int(wl.hap_off[int(wl.region_hap_off[n_cpu])])]
+    t1 = time.perf_counter()
+    ref = O.pd_compute_workload(sub, sub_pd)
+    cpu_dt = time.perf_counter() - t1
+    d = absdiff(res[: sub.n_pairs], ref)
+    dp_flop_per_cell = 11  # M: add, mul, fma, mul; I: mul, fma; D: mul, fma (FMA = 2): 8 FP64-pipe operations
+    achieved = dp_flop_per_cell * cells / (ms_kernel * 1e-3) / 1e12
+    line = {
+        "metric": "PD-HMM GCUPS (FP64, partially determined haplotypes) on 1 GB300", "value": cells / (ms * 1e-3) / 1e9,
+        "unit": "GCUPS", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "dtype": "f64", "data": "synthetic (workload 1 regions with seeded PD flags)",
+        "config": {"workload": f"first {n_regions} regions of config1 with 1-3 undetermined SNPs and 0-2 undetermined "
+                               "deletions per haplotype", "regions": n_regions, "pairs": wl.n_pairs, "cells": cells},
+        "roofline": {"bound": "fp64_pipe", "achieved": achieved, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
+                     "frac": achieved / peaks["fp64_tflops"], "flop_per_cell": dp_flop_per_cell,
+                     "kernel": "pd_fp64_kernel<4>"},
+        "e2e": {"value": cells / dt_e2e / 1e9, "unit": "GCUPS", "ms_per_step": dt_e2e * 1e3,
+                "h2d_bytes_per_step": int(io["h2d_bytes"]), "d2h_bytes_per_step": int(io["d2h_bytes"]),
+                "api": "ghmm_pd_compute_regions", "matches_batch": bool(np.array_equal(out, res))},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+        "cpu_baseline": {"value": cpu_cells / cpu_dt / 1e9, "unit": "GCUPS", "cores": O.num_threads(), "kind": "port",
+                         "sample": f"first {n_cpu} regions ({cpu_cells:.3e} cells, {sub.n_pairs} pairs)",
+                         "host": f"{platform.machine()} x{os.cpu_count()}"},
+        "accuracy_vs_fp64_oracle": {"sample_pairs": int(sub.n_pairs), "max_abs_dlog10": float(d.max()),
+                                    "median_abs_dlog10": float(np.median(d))},
+    }
+    print(json.dumps(line), flush=True)
+    eng.close()
+    return 0
+
+
 def apply_tuning(args, eng, wl):
     """--tuning K,KM,C sets the launch shape; --autotune runs the native autotuner on the whole workload
     (untimed) over the candidates it names.  Returns what was used."""
@@ -618,6 +691,7 @@ def main():
                     "per lane, haplotype columns per task)")
     ap.add_argument("--autotune", default="", help="autotune over candidates 'K,KM,C;K,KM,C;...' on the whole "
                     "workload before timing")
+    ap.add_argument("--pd", action="store_true", help="PD-HMM over workload 1 regions with synthetic PD flags")
     ap.add_argument("--calib", action="store_true",
                     help="time the calibration forward + backward on workload 3 and check its gradient")
     args = ap.parse_args()
@@ -631,6 +705,8 @@ def main():
         return run_stream(args)
     if args.calib:
         return run_calib(args)
+    if args.pd:
+        return run_pd(args)
     return run_ours(args)
 
 

@@ -101,8 +101,10 @@ struct PdPlanes {
     const uint8_t *states;
 };
 int pd_kernel_occupancy(int *blocks_per_sm);
-int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int grid, cudaStream_t s);
-constexpr int kPdRowsPerLane = 4;
+int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int k, int begin, int count, int grid,
+              cudaStream_t s);
+constexpr int kPdMaxK = 4;          // PD kernel: rows per lane 1..4
+constexpr int kCounterPdBase = 40;  // counters[40 + K]: PD task cursors (inside the 64 counters, above the buckets)
 
 // Post-likelihood normalisation and filtering (post.cu).
 struct PostArgs {

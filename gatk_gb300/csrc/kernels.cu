@@ -567,7 +567,8 @@ __global__ void __launch_bounds__(128) fp64_queue_kernel(DevTables T, DevBatch B
                     if (RESCALED) {
                         Mn = prior * fma(dI, c1[k], fma(dD, c2[k], dM));
                         Dn = fma(Dp[k], tdd[k], Mp[k]);
-                    } else {
+                    } else {  // the reference's grouping: prior x (M x MM + (I + D) x IM), so results deep in the
+                              // subnormal range round as LoglessPairHMM's do
                         Mn = prior * fma(dM, c1[k], (dI + dD) * c2[k]);
                         Dn = fma(Dp[k], tdd[k], Mp[k] * c5[k]);
                     }

@@ -13,9 +13,9 @@
 // sequences per haplotype column (pd_attach in runtime.cpp) and the kernel takes row 1's for the read's first row.
 // The prior also matches a read base against an undetermined SNP's alternative (isBasePDMatching, :196-210).
 //
-// Kernel: one (read, haplotype) pair per warp, K rows per lane, the anti-diagonal wavefront of the FP64 kernels in
-// kernels.cu with six values per row, strips of 32*K rows through per-warp scratch (six doubles per column), FP64 at
-// the reference's scale 2^1020.  Steps where no lane of the warp is at an AFTER_DEL or DEL_END column (nearly all)
+// Kernel: one (read, haplotype) pair per warp, K rows per lane (K = 1..4, per read the strip height that wastes the
+// fewest padding rows), the anti-diagonal wavefront of the FP64 kernels in kernels.cu with six values per row,
+// strips of 32*K rows through per-warp scratch (six doubles per column), FP64 at the reference's scale 2^1020.  Steps where no lane of the warp is at an AFTER_DEL or DEL_END column (nearly all)
 // take a path without max(); the rest take the general one.
 #include <cuda_runtime.h>
 
@@ -29,7 +29,6 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr double kLog10Scale = 307.0505955772608;  // log10(2^1020)
-constexpr int kPdK = 4;
 constexpr int kPdBlock = 128;
 
 __device__ __forceinline__ uint32_t pd_base_bit(uint32_t x) {
@@ -42,19 +41,21 @@ __device__ __forceinline__ uint32_t pd_base_bit(uint32_t x) {
     }
 }
 
+// Pairs [begin, begin + count) of the batch's pair list, all of whose reads take K rows per lane: the host picks,
+// per read, the strip height 32 K (K = 1..4) that wastes the fewest padding rows.
 template <int K>
-__global__ void __launch_bounds__(kPdBlock) pd_fp64_kernel(DevTables T, DevBatch B, PdPlanes P) {
+__global__ void __launch_bounds__(kPdBlock, 3) pd_fp64_kernel(DevTables T, DevBatch B, PdPlanes P, int begin, int count,
+                                                              int cursor) {
     constexpr int S = 32 * K;
     const int lane = threadIdx.x & 31;
     const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     double *scratch = B.scratch64 + warp_global * B.scratch64_cols * 6;
-    const int total = min(B.counters[1], (int)B.rerun_capacity);
     for (;;) {
         int t = 0;
-        if (lane == 0) t = atomicAdd(&B.counters[2], 1);
+        if (lane == 0) t = atomicAdd(&B.counters[cursor], 1);
         t = __shfl_sync(kFull, t, 0);
-        if (t >= total) break;
-        const PairRef pr = B.rerun[t];
+        if (t >= count) break;
+        const PairRef pr = B.rerun[begin + t];
         const int read = pr.read, hap = pr.hap;
         const int64_t roff = B.read_off[read];
         const int R = (int)(B.read_off[read + 1] - roff);
@@ -80,7 +81,12 @@ __global__ void __launch_bounds__(kPdBlock) pd_fp64_kernel(DevTables T, DevBatch
         const uint8_t *hs = P.states + hoff;
         double acc = 0.0;
         for (int strip = 0; strip < nstrips; ++strip) {
-            double pm[K], pe[K], tmm[K], tim[K], tmi[K], tii[K], tmd[K], tdd[K];
+            // tii doubles as DD (equal for read rows); a dummy row has tii = 1 so its D holds the row-0 value and its
+            // I stays at the (zero) value above it
+            // the prior is folded into M's coefficients: (prior x MM, prior x IM) for a match and a mismatch, so a
+            // cell's M costs one multiply and two fused multiply-adds (this part's FP64 pipe takes a DMUL or DADD
+            // for two DFMAs)
+            double mMM[K], mIM[K], eMM[K], eIM[K], tmi[K], tii[K], tmd[K];
             uint32_t rbase[K], rbit[K];
             bool first[K], dummy[K];
 #pragma unroll
@@ -89,22 +95,23 @@ __global__ void __launch_bounds__(kPdBlock) pd_fp64_kernel(DevTables T, DevBatch
                 dummy[k] = p < 0;
                 first[k] = p == 0;
                 if (p < 0) {
-                    pm[k] = pe[k] = 0.0;
-                    tmm[k] = tim[k] = tmi[k] = tii[k] = tmd[k] = 0.0;
-                    tdd[k] = 1.0;  // a dummy row holds the row-0 D value
+                    mMM[k] = mIM[k] = eMM[k] = eIM[k] = 0.0;
+                    tmi[k] = tmd[k] = 0.0;
+                    tii[k] = 1.0;
                     rbase[k] = 0x100u;
                     rbit[k] = 0u;
                 } else {
                     const uint8_t base = B.bases[roff + p], q = B.quals[roff + p];
                     const uint8_t ins = B.ins[roff + p], del = B.dels[roff + p], gcp = B.gcp[roff + p];
-                    pm[k] = __ldg(T.prob_d + q);
-                    pe[k] = __ldg(T.err3_d + q);
-                    tmm[k] = __ldg(T.m2m_d + ins * 128 + del);
-                    tim[k] = __ldg(T.prob_d + gcp);
+                    const double pm = __ldg(T.prob_d + q), pe = __ldg(T.err3_d + q);
+                    const double mm = __ldg(T.m2m_d + ins * 128 + del), im = __ldg(T.prob_d + gcp);
+                    mMM[k] = pm * mm;
+                    mIM[k] = pm * im;
+                    eMM[k] = pe * mm;
+                    eIM[k] = pe * im;
                     tmi[k] = __ldg(T.err_d + ins);
                     tii[k] = __ldg(T.err_d + gcp);
                     tmd[k] = __ldg(T.err_d + del);
-                    tdd[k] = tii[k];
                     rbase[k] = base;
                     rbit[k] = pd_base_bit(base);
                 }
@@ -172,30 +179,30 @@ __global__ void __launch_bounds__(kPdBlock) pd_fp64_kernel(DevTables T, DevBatch
                     const double dM = k ? Mp[k - 1] : gM, dI = k ? Ip[k - 1] : gI, dD = k ? Dp[k - 1] : gD;
                     const uint32_t sk = first[k] ? st1 : st2;
                     const bool match = rbase[k] == y || rbase[k] == 'N' || yn || ((f & 1u) && (f & rbit[k]));
-                    const double prior = match ? pm[k] : pe[k];
+                    const double cMM = match ? mMM[k] : eMM[k], cIM = match ? mIM[k] : eIM[k];
                     double Mn, Dn, nbM, nbI, nbD;
                     if (!special) {
                         const bool inside = sk == 1u;
                         nbM = inside ? bM[k] : Mp[k];
                         nbI = inside ? bI[k] : Ip[k];
                         nbD = inside ? bD[k] : Dp[k];
-                        Mn = prior * fma(dM, tmm[k], (dI + dD) * tim[k]);
-                        Dn = fma(Dp[k], tdd[k], Mp[k] * tmd[k]);
+                        Mn = fma(dM, cMM, fma(dI, cIM, dD * cIM));
+                        Dn = fma(Dp[k], tii[k], Mp[k] * tmd[k]);
                     } else {
                         const double dbM = k ? bM[k - 1] : gbM, dbI = k ? bI[k - 1] : gbI, dbD = k ? bD[k - 1] : gbD;
                         if (sk == 2u) {
                             nbM = fmax(bM[k], Mp[k]);
                             nbI = fmax(bI[k], Ip[k]);
                             nbD = fmax(bD[k], Dp[k]);
-                            Mn = prior * fma(fmax(dbM, dM), tmm[k], (fmax(dbI, dI) + fmax(dbD, dD)) * tim[k]);
-                            Dn = fma(fmax(bD[k], Dp[k]), tdd[k], fmax(bM[k], Mp[k]) * tmd[k]);
+                            Mn = fma(fmax(dbM, dM), cMM, fma(fmax(dbI, dI), cIM, fmax(dbD, dD) * cIM));
+                            Dn = fma(fmax(bD[k], Dp[k]), tii[k], fmax(bM[k], Mp[k]) * tmd[k]);
                         } else {
                             const bool inside = sk == 1u;
                             nbM = inside ? bM[k] : Mp[k];
                             nbI = inside ? bI[k] : Ip[k];
                             nbD = inside ? bD[k] : Dp[k];
-                            Mn = prior * fma(dM, tmm[k], (dI + dD) * tim[k]);
-                            Dn = fma(Dp[k], tdd[k], Mp[k] * tmd[k]);
+                            Mn = fma(dM, cMM, fma(dI, cIM, dD * cIM));
+                            Dn = fma(Dp[k], tii[k], Mp[k] * tmd[k]);
                         }
                     }
                     if (!valid) Mn = Dn = 0.0, nbM = nbI = nbD = 0.0;
@@ -250,11 +257,34 @@ __global__ void __launch_bounds__(kPdBlock) pd_fp64_kernel(DevTables T, DevBatch
 }  // namespace
 
 int pd_kernel_occupancy(int *blocks_per_sm) {
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pd_fp64_kernel<kPdK>, kPdBlock, 0);
+    // every K variant runs on the same grid and scratch: the smallest occupancy of the four
+    int best = 1 << 30;
+    for (int k = 1; k <= kPdMaxK; ++k) {
+        int n = 0;
+        cudaError_t e;
+        switch (k) {
+            case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pd_fp64_kernel<1>, kPdBlock, 0); break;
+            case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pd_fp64_kernel<2>, kPdBlock, 0); break;
+            case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pd_fp64_kernel<3>, kPdBlock, 0); break;
+            default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pd_fp64_kernel<4>, kPdBlock, 0); break;
+        }
+        if (e != cudaSuccess) return (int)e;
+        best = n < best ? n : best;
+    }
+    *blocks_per_sm = best;
+    return 0;
 }
 
-int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int grid, cudaStream_t s) {
-    pd_fp64_kernel<kPdK><<<grid, kPdBlock, 0, s>>>(t, b, p);
+int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int k, int begin, int count, int grid,
+              cudaStream_t s) {
+    const int cursor = kCounterPdBase + k;
+    switch (k) {
+        case 1: pd_fp64_kernel<1><<<grid, kPdBlock, 0, s>>>(t, b, p, begin, count, cursor); break;
+        case 2: pd_fp64_kernel<2><<<grid, kPdBlock, 0, s>>>(t, b, p, begin, count, cursor); break;
+        case 3: pd_fp64_kernel<3><<<grid, kPdBlock, 0, s>>>(t, b, p, begin, count, cursor); break;
+        case 4: pd_fp64_kernel<4><<<grid, kPdBlock, 0, s>>>(t, b, p, begin, count, cursor); break;
+        default: return (int)cudaErrorInvalidValue;
+    }
     return (int)cudaGetLastError();
 }
 

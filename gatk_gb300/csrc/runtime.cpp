@@ -1423,14 +1423,33 @@ static int pd_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
 static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b) {
     cudaStream_t s = ctx->stream;
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-    // every pair, read-major per region
+    // every pair, grouped by the rows per lane K of its read (the strip height 32 K, K = 1..4, that needs the
+    // fewest rows; ties to the larger K, i.e. fewer strips), read-major per region within a group
     GHMM_CUDA(b.h_fp64all.reserve((size_t)std::max<int64_t>(b.n_out, 1)), "pinned PD pairs");
     const int64_t *o = b.h_off.p;
     const int64_t *rro = o + b.n_reads + 1 + b.n_haps + 1, *rho = rro + b.n_regions + 1;
-    int64_t k = 0;
+    auto pick_k = [](int64_t R) {
+        int best_k = kPdMaxK;
+        int64_t best_rows = INT64_MAX;
+        for (int k = kPdMaxK; k >= 1; --k) {
+            const int64_t rows = ((R + 32 * k - 1) / (32 * k)) * 32 * k;
+            if (rows < best_rows) best_rows = rows, best_k = k;
+        }
+        return best_k;
+    };
+    int64_t kcount[kPdMaxK + 1] = {0};
     for (int64_t g = 0; g < b.n_regions; g++)
-        for (int64_t r = rro[g]; r < rro[g + 1]; r++)
-            for (int64_t h = rho[g]; h < rho[g + 1]; h++) b.h_fp64all.p[k++] = PairRef{(int32_t)r, (int32_t)h};
+        for (int64_t r = rro[g]; r < rro[g + 1]; r++) kcount[pick_k(o[r + 1] - o[r])] += rho[g + 1] - rho[g];
+    int64_t kbegin[kPdMaxK + 2] = {0};
+    for (int kk = 1; kk <= kPdMaxK; kk++) kbegin[kk + 1] = kbegin[kk] + kcount[kk];
+    int64_t kpos[kPdMaxK + 1];
+    for (int kk = 1; kk <= kPdMaxK; kk++) kpos[kk] = kbegin[kk];
+    for (int64_t g = 0; g < b.n_regions; g++)
+        for (int64_t r = rro[g]; r < rro[g + 1]; r++) {
+            const int kk = pick_k(o[r + 1] - o[r]);
+            for (int64_t h = rho[g]; h < rho[g + 1]; h++) b.h_fp64all.p[kpos[kk]++] = PairRef{(int32_t)r, (int32_t)h};
+        }
+    const int64_t k = kbegin[kPdMaxK + 1];
     int bpsm = 0;
     if (pd_kernel_occupancy(&bpsm) != 0 || bpsm <= 0) bpsm = 1;
     const int grid = ctx->sm_count * bpsm;
@@ -1452,8 +1471,13 @@ static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b) {
     GHMM_CUDA(cudaMemcpyAsync(b.d_counters.p, hc, (kNumCounters + 2 * kNumBucketKeys) * sizeof(int32_t),
                               cudaMemcpyHostToDevice, s), "H2D counters");
     GHMM_CUDA(cudaEventRecord(b.ev[1], s), "event");
-    int e = launch_pd(ctx->tables, b.dev, b.pd, grid, s);
-    if (e) return cuda_fail(ctx, (cudaError_t)e, "PD-HMM launch");
+    int launches = 0;
+    for (int kk = kPdMaxK; kk >= 1; --kk) {  // longest strips first
+        if (kcount[kk] == 0) continue;
+        int e = launch_pd(ctx->tables, b.dev, b.pd, kk, (int)kbegin[kk], (int)kcount[kk], grid, s);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "PD-HMM launch");
+        launches++;
+    }
     GHMM_CUDA(cudaEventRecord(b.ev[2], s), "event");
     GHMM_CUDA(cudaMemcpyAsync(hc, b.d_counters.p, kNumCounters * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
               "D2H counters");
@@ -1466,7 +1490,7 @@ static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b) {
     cudaEventElapsedTime(&ms, b.ev[0], b.ev[3]);
     b.ms_total = ms;
     b.last_mode = GHMM_MODE_PD;
-    b.last_launches = 1;
+    b.last_launches = launches;
     b.last_rerun = b.last_exact = 0;
     b.forward_h2d = k * (int64_t)sizeof(PairRef) + (kNumCounters + 2 * kNumBucketKeys) * 4;
     b.forward_d2h = kNumCounters * 4;
