@@ -13,7 +13,9 @@
 //    one region, packed into the .x/.y halves of float2 so every cell update is a packed FFMA2/FMUL2/FADD2,
 //    against all (or a chunk of) the region's haplotypes streamed back to back.  Lane l owns K consecutive
 //    rows; at step s it computes column c = s - l, receiving the row above from lane l-1 by __shfl_up_sync
-//    (an anti-diagonal wavefront).  Each read is followed by two accumulator rows that sum the last row over
+//    (an anti-diagonal wavefront); lane l-1 hands lane l two packed values per step, its row 0's I~ at this
+//    column and the inner sum b I~ + c D~ + M~ of its row 0's next M~, computed with lane l's row-0 coefficients,
+//    instead of three raw states (K >= 2).  Each read is followed by two accumulator rows that sum the last row over
 //    the haplotype (row_coef), and padded at the top with "dummy" rows that reproduce the row-0 boundary, so
 //    the accumulator rows always sit in lane 31's last two slots.  Reads longer than 32*K rows run
 //    as several strips whose boundary row goes through per-warp global scratch.  Each row's states are
@@ -57,6 +59,9 @@ __device__ __forceinline__ float2 zero2() { return make_float2(0.f, 0.f); }
 
 __device__ __forceinline__ float2 shfl_up2(float2 v) {
     return make_float2(__shfl_up_sync(kFull, v.x, 1), __shfl_up_sync(kFull, v.y, 1));
+}
+__device__ __forceinline__ float2 shfl_down2(float2 v) {
+    return make_float2(__shfl_down_sync(kFull, v.x, 1), __shfl_down_sync(kFull, v.y, 1));
 }
 
 __device__ __forceinline__ uint32_t base_code(uint8_t b) {
@@ -236,20 +241,34 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                 lsum.y += __shfl_xor_sync(kFull, lsum.y, o);
             }
             la = add2(la, lsum);
+            // row-0 coefficients of the lane below (lane 31: of the next strip's first row), with which this lane
+            // hands it its row 0's I~ and M~ inner sum instead of three raw states
+            float2 b0n = shfl_down2(cb[0]), c0n = shfl_down2(cc[0]), e0n = shfl_down2(ce[0]);
+            if (lane == 31) {
+                b0n = c0n = e0n = zero2();
+                if (MULTI && strip + 1 < nstrips) {
+                    const int slot = (strip + 1) * S;
+                    const RowCoef a = row_coef(T, B, off_a, len_a, slot - task.pad_a);
+                    const RowCoef b = row_coef(T, B, off_b, rb >= 0 ? len_b : 0, slot - task.pad_b);
+                    b0n = make_float2(a.b, b.b);
+                    c0n = make_float2(a.c, b.c);
+                    e0n = make_float2(a.e, b.e);
+                }
+            }
             __syncwarp();
             float2 Mp[K], Ip[K], Dp[K];
 #pragma unroll
             for (int k = 0; k < K; ++k) Mp[k] = Ip[k] = Dp[k] = zero2();
-            float2 gM = zero2(), gI = zero2(), gD = zero2();  // row above, previous column (diagonal)
-            float2 bnd = zero2();                               // lane 0, strip 0: row-0 D~ boundary
+            float2 gW = zero2();   // row 0's M~ inner sum for this step (from the lane above, one step late)
+            float2 w0 = zero2();   // lane 0, strip 0: the row-0 boundary's inner sum c_0 X
             int hap = task.hap_begin - 1;
             const bool last_strip = (strip == nstrips - 1);
-            float2 nxM = zero2(), nxI = zero2(), nxD = zero2();  // prefetched strip boundary (MULTI, lane 0)
+            float2 nxV = zero2(), nxW = zero2();  // prefetched strip boundary (MULTI, lane 0)
             if (MULTI && strip > 0 && lane == 0 && ncols > 0) {
-                nxM = scratch[0];
-                nxI = scratch[1];
-                nxD = scratch[2];
+                nxV = scratch[0];
+                nxW = scratch[1];
             }
+            float2 sV = zero2(), sW = zero2();  // what this lane hands the lane below at the end of a step
             const int nsteps = ncols + 31;
             // column code of the next step, loaded one step ahead (the code plane has kCodePad bytes on
             // both sides, so columns just outside the stream are readable; CHK steps mask them)
@@ -271,9 +290,8 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                 // row above at this column: lane l-1's last row as computed last step.  Shuffled before
                 // this lane resets its own state at a haplotype start, since lane l+1 still needs the
                 // previous haplotype's last column from it.
-                float2 uM = shfl_up2(Mp[K - 1]);
-                float2 uI = shfl_up2(Ip[K - 1]);
-                float2 uD = shfl_up2(Dp[K - 1]);
+                float2 uV = shfl_up2(sV);  // I~ of this lane's row 0 at this column
+                float2 uW = shfl_up2(sW);  // row 0's M~ inner sum for the next column
                 if constexpr (CHK) {
                     if (code & kColFirst) {
                         ++hap;
@@ -287,28 +305,26 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                             Mp[k] = Ip[k] = zero2();
                             Dp[k] = make_float2((slot0 + k < task.pad_a) ? X.x : 0.f, (slot0 + k < task.pad_b) ? X.y : 0.f);
                         }
-                        gM = gI = zero2();
-                        gD = make_float2((slot0 - 1 < task.pad_a) ? X.x : 0.f, (slot0 - 1 < task.pad_b) ? X.y : 0.f);
-                        if (lane == 0 && strip == 0) bnd = X;
+                        const float2 gD = make_float2((slot0 - 1 < task.pad_a) ? X.x : 0.f,
+                                                      (slot0 - 1 < task.pad_b) ? X.y : 0.f);
+                        gW = mul2(cc[0], gD);
+                        if (lane == 0 && strip == 0) w0 = mul2(cc[0], X);
                     }
                 }
                 // lane 0 takes the row-0 boundary (strip 0) or the previous strip's last row instead
                 // (selects on the ALU pipe, not multiplies on the FMA pipe)
                 if (MULTI && strip > 0) {
                     if (lane == 0) {
-                        uM = nxM;
-                        uI = nxI;
-                        uD = nxD;
+                        uV = nxV;
+                        uW = nxW;
                         if (c + 1 < ncols) {
-                            nxM = scratch[3 * (c + 1) + 0];
-                            nxI = scratch[3 * (c + 1) + 1];
-                            nxD = scratch[3 * (c + 1) + 2];
+                            nxV = scratch[2 * (c + 1) + 0];
+                            nxW = scratch[2 * (c + 1) + 1];
                         }
                     }
                 } else if (lane == 0) {
-                    uM = zero2();
-                    uI = zero2();
-                    uD = bnd;
+                    uV = zero2();
+                    uW = w0;
                 }
                 const float4 *pri4 = prior_tbl4 + (code & 7u) * 32;
                 float2 prs[2 * KP];
@@ -321,28 +337,26 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                 // pass 1 (bottom-up so the row above is still the previous column): M and D^
 #pragma unroll
                 for (int k = K - 1; k >= 0; --k) {
-                    const float2 dM = k ? Mp[k - 1] : gM;
-                    const float2 dI = k ? Ip[k - 1] : gI;
-                    const float2 dD = k ? Dp[k - 1] : gD;
                     const float2 pr = prs[k];
-                    const float2 Mn = mul2(pr, fma2(dI, cb[k], fma2(dD, cc[k], dM)));
+                    float2 Mn;
+                    if (k) {
+                        Mn = mul2(pr, fma2(Ip[k - 1], cb[k], fma2(Dp[k - 1], cc[k], Mp[k - 1])));
+                    } else {
+                        Mn = mul2(pr, gW);
+                    }
                     const float2 Dn = fma2(Dp[k], cdd[k], Mp[k]);
                     Mp[k] = Mn;
                     Dp[k] = Dn;
                 }
-                // pass 2 (top-down): I~ from the row above at this column
-                float2 aM = uM, aI = uI;
+                // pass 2 (top-down): I~ from the row above at this column; row 0's comes from the lane above
+                Ip[0] = uV;
 #pragma unroll
-                for (int k = 0; k < K; ++k) {
-                    const float2 In = fma2(aI, ce[k], aM);
-                    Ip[k] = In;
-                    aM = Mp[k];
-                    aI = In;
-                }
-                const float2 i_acc = (K >= 2) ? Ip[K >= 2 ? K - 2 : 0] : uI;  // I~(R+1) at this column
-                gM = uM;
-                gI = uI;
-                gD = uD;
+                for (int k = 1; k < K; ++k) Ip[k] = fma2(Ip[k - 1], ce[k], Mp[k - 1]);
+                const float2 i_acc = Ip[K >= 2 ? K - 2 : 0];  // I~(R+1) at this column (K >= 2)
+                gW = uW;
+                // hand the lane below its row 0's I~ at this column and M~ inner sum for the next
+                sV = fma2(Ip[K - 1], e0n, Mp[K - 1]);
+                sW = fma2(Ip[K - 1], b0n, fma2(Dp[K - 1], c0n, Mp[K - 1]));
                 if (last_strip) {
                     if constexpr (CHK) {
                         if (lane == 31 && (code & kColLast)) {
@@ -352,9 +366,8 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                         }
                     }
                 } else if (MULTI && lane == 31 && valid) {
-                    scratch[3 * c + 0] = Mp[K - 1];
-                    scratch[3 * c + 1] = Ip[K - 1];
-                    scratch[3 * c + 2] = Dp[K - 1];
+                    scratch[2 * c + 0] = sV;
+                    scratch[2 * c + 1] = sW;
                 }
             };
             // haplotype boundaries of this task: columns hb(j) = hap_off[hap_begin + j] - col0, hb(n) = ncols

@@ -515,14 +515,15 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                     po.cells_direct += (int64_t)R * region_cols;
                     continue;
                 }
-                // rows of the layout: the read plus its two accumulator rows (kernels.cu)
+                // rows of the layout: the read plus its two accumulator rows (kernels.cu); at least 2 rows per lane,
+                // since the accumulator rows must share lane 31
                 const int rows = R + kAccRows;
                 int key, ns = 1;
                 if (rows <= 32 * max_k) {
-                    key = (rows + 31) / 32;
+                    key = std::max(2, (rows + 31) / 32);
                 } else {  // fewest strips of at most max_k_multi rows per lane, then the fewest rows per lane
                     ns = (rows + 32 * max_k_multi - 1) / (32 * max_k_multi);
-                    key = ((rows + 32 * ns - 1) / (32 * ns)) | 16;
+                    key = std::max(2, (rows + 32 * ns - 1) / (32 * ns)) | 16;
                 }
                 // reads are paired only within one (rows per lane, strip count) class
                 groups.emplace_back(((int64_t)key * 4096 + ns) * 100000 + R, r);
