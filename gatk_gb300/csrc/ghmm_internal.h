@@ -106,6 +106,14 @@ int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int k, i
 constexpr int kPdMaxK = 4;          // PD kernel: rows per lane 1..4
 constexpr int kCounterPdBase = 40;  // counters[40 + K]: PD task cursors (inside the 64 counters, above the buckets)
 
+// Read preparation on the device (prep.cu).
+struct PrepArgs {
+    const int32_t *mapq;     // per read
+    uint8_t pcr_cache[24];   // PCR indel model quality per repeat length 0..20
+    int pcr, cap_to_mapq, threshold;
+};
+int launch_prep(const DevBatch &b, int64_t n_reads, const PrepArgs &p, int sm_count, cudaStream_t s);
+
 // Post-likelihood normalisation and filtering (post.cu).
 struct PostArgs {
     double cap;                   // log10globalReadMismappingRate (< 0)

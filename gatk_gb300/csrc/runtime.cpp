@@ -163,6 +163,8 @@ struct ghmm_batch {
     DevBuf<int32_t> d_counters;  // same layout as h_counters
     DevBuf<int64_t> d_nout;
     DevBuf<uint8_t> d_post;  // postprocess: reference haplotype per region, keep flags per read
+    HostBuf<int32_t> h_mapq;  // raw-read batches: mapping quality per read
+    DevBuf<int32_t> d_mapq;
     // PD-HMM batches: PD flags then state codes per haplotype column (pd.cu)
     HostBuf<uint8_t> h_pd;
     DevBuf<uint8_t> d_pd;
@@ -216,6 +218,7 @@ struct ghmm_batch {
         d_planes.release(); d_hap.release(); d_off.release(); d_read_region.release(); d_init_f.release();
         d_init_d.release(); d_tasks.release(); d_rerun.release(); d_out.release(); d_counters.release();
         d_scratch32.release(); d_scratch64.release(); d_post.release(); h_pd.release(); d_pd.release();
+        h_mapq.release(); d_mapq.release();
         has_pd = false;
     }
 };
@@ -1499,6 +1502,90 @@ static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b) {
     return GHMM_OK;
 }
 
+
+// -------------------------------------------------------------------------------------------------
+// Raw reads: the regular marshal over the reads' bases and raw qualities (45 where a read has no BI / BD tag, the
+// constant gap continuation penalty), then prep.cu rewrites the quality planes on the device.  The host's routing
+// checks see the raw qualities; a read whose prepared qualities would make the FP32 or rescaled FP64 forms
+// overflow still ends up exact, because a non-finite sum sends its pair on to the next tier.
+
+namespace {
+
+struct RawView {
+    std::vector<ghmm_region> regions;
+    std::vector<std::vector<ghmm_read>> reads;
+    std::vector<uint8_t> q45, qgcp;  // shared constant planes
+    std::vector<int32_t> mapq;
+};
+
+int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_read_prep *prep, RawView &v) {
+    if (!prep) return fail(ctx, GHMM_ERR_ARG, "NULL read preparation arguments");
+    if (prep->gcp < 1 || prep->gcp > 127) return fail(ctx, GHMM_ERR_ARG, "gap continuation penalty must be 1..127");
+    if (prep->base_quality_threshold < 6 || prep->base_quality_threshold > 127)
+        return fail(ctx, GHMM_ERR_ARG, "base quality threshold must be 6..127 (QualityUtils.MIN_USABLE_Q_SCORE)");
+    if (!(prep->pcr_rate_factor >= 0.0)) return fail(ctx, GHMM_ERR_ARG, "PCR rate factor must be >= 0");
+    int32_t max_len = 0;
+    for (int64_t g = 0; g < G; g++) {
+        const ghmm_raw_region &rg = raw[g];
+        if (rg.n_reads < 0 || rg.n_haps < 0 || (rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps))
+            return fail(ctx, GHMM_ERR_ARG, "bad raw region");
+        for (int32_t r = 0; r < rg.n_reads; r++) {
+            const ghmm_raw_read &rd = rg.reads[r];
+            if (rd.length < 0 || rd.length > kMaxReadLen) return fail(ctx, GHMM_ERR_ARG, "read length out of range");
+            if (rd.length > 0 && (!rd.bases || !rd.quals)) return fail(ctx, GHMM_ERR_ARG, "NULL read array");
+            if (rd.mapping_quality < 0 || rd.mapping_quality > 255) return fail(ctx, GHMM_ERR_ARG, "mapping quality 0..255");
+            max_len = std::max(max_len, rd.length);
+        }
+    }
+    v.q45.assign((size_t)std::max(max_len, 1), 45);
+    v.qgcp.assign((size_t)std::max(max_len, 1), (uint8_t)prep->gcp);
+    v.regions.resize((size_t)G);
+    v.reads.resize((size_t)G);
+    for (int64_t g = 0; g < G; g++) {
+        const ghmm_raw_region &rg = raw[g];
+        auto &rr = v.reads[(size_t)g];
+        rr.resize((size_t)rg.n_reads);
+        for (int32_t r = 0; r < rg.n_reads; r++) {
+            const ghmm_raw_read &rd = rg.reads[r];
+            rr[(size_t)r] = ghmm_read{rd.bases, rd.quals, rd.ins_quals ? rd.ins_quals : v.q45.data(),
+                                      rd.del_quals ? rd.del_quals : v.q45.data(), v.qgcp.data(), rd.length};
+            v.mapq.push_back(rd.mapping_quality);
+        }
+        v.regions[(size_t)g] = ghmm_region{rr.data(), rg.n_reads, rg.haps, rg.n_haps};
+    }
+    return GHMM_OK;
+}
+
+}  // namespace
+
+static int raw_prepare_device(ghmm_ctx *ctx, ghmm_batch &b, const RawView &v, const ghmm_read_prep *prep,
+                              cudaStream_t s) {
+    const int64_t NR = b.n_reads;
+    if (NR == 0) return GHMM_OK;
+    GHMM_CUDA(b.h_mapq.reserve((size_t)NR), "pinned mapping qualities");
+    GHMM_CUDA(b.d_mapq.reserve((size_t)NR), "device mapping qualities");
+    memcpy(b.h_mapq.p, v.mapq.data(), (size_t)NR * sizeof(int32_t));
+    GHMM_CUDA(cudaMemcpyAsync(b.d_mapq.p, b.h_mapq.p, (size_t)NR * sizeof(int32_t), cudaMemcpyHostToDevice, s),
+              "H2D mapping qualities");
+    PrepArgs p{};
+    p.mapq = b.d_mapq.p;
+    p.pcr = prep->pcr_rate_factor != 0.0;
+    p.cap_to_mapq = prep->cap_to_mapq ? 1 : 0;
+    p.threshold = prep->base_quality_threshold;
+    // getErrorModelAdjustedQual (PairHMMLikelihoodCalculationEngine.java:355-358): max(10, fastRound(40 -
+    // exp(repeatLength / (rateFactor pi)) + 1))
+    for (int rl = 0; rl <= 20; rl++) {
+        double d = 40.0;
+        if (p.pcr) d = 40.0 - std::exp((double)rl / (prep->pcr_rate_factor * M_PI)) + 1.0;
+        const int rounded = d > 0.0 ? (int)(d + 0.5) : (int)(d - 0.5);
+        p.pcr_cache[rl] = (uint8_t)std::max(10, rounded);
+    }
+    int e = launch_prep(b.dev, NR, p, ctx->sm_count, s);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "read preparation launch");
+    b.upload_bytes += NR * 4;
+    return GHMM_OK;
+}
+
 void ghmm::set_global_error(const char *msg) {
     std::lock_guard<std::mutex> lk(g_init_error_mu);
     g_init_error = msg ? msg : "";
@@ -1901,6 +1988,67 @@ int ghmm_get_tuning(ghmm_ctx *ctx, ghmm_tuning *t) {
     if (!t) return fail(ctx, GHMM_ERR_ARG, "NULL tuning");
     *t = ghmm_tuning{ctx->max_k, ctx->max_k_multi, ctx->chunk_cols, 0};
     return GHMM_OK;
+}
+
+int ghmm_batch_create_raw(ghmm_ctx *ctx, const ghmm_raw_region *regions, int32_t n_regions, const ghmm_read_prep *prep,
+                          ghmm_batch **out) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!out || n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad arguments");
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    RawView v;
+    int rc = raw_view(ctx, regions, n_regions, prep, v);
+    if (rc) return rc;
+    auto *b = new ghmm_batch();
+    Source src;
+    src.regions = v.regions.data();
+    src.n_regions = n_regions;
+    rc = batch_marshal(ctx, src, *b);
+    if (!rc) rc = batch_upload(ctx, *b, ctx->stream);
+    if (!rc) rc = raw_prepare_device(ctx, *b, v, prep, ctx->stream);
+    if (!rc) rc = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? GHMM_OK : fail(ctx, GHMM_ERR_CUDA, "upload");
+    if (rc) {
+        b->release();
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return GHMM_OK;
+}
+
+int ghmm_batch_read_planes(ghmm_ctx *ctx, const ghmm_batch *b, uint8_t *bases, uint8_t *quals, uint8_t *ins,
+                           uint8_t *dels, uint8_t *gcp) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!b) return fail(ctx, GHMM_ERR_ARG, "NULL batch");
+    if (!b->uploaded) return fail(ctx, GHMM_ERR_STATE, "batch not uploaded");
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    uint8_t *dst[5] = {bases, quals, ins, dels, gcp};
+    for (int k = 0; k < 5; k++)
+        if (dst[k] && b->read_bytes > 0)
+            GHMM_CUDA(cudaMemcpyAsync(dst[k], b->d_planes.p + (size_t)k * b->read_bytes, (size_t)b->read_bytes,
+                                      cudaMemcpyDeviceToHost, ctx->stream), "D2H read planes");
+    GHMM_CUDA(cudaStreamSynchronize(ctx->stream), "D2H read planes");
+    return GHMM_OK;
+}
+
+int ghmm_compute_regions_raw(ghmm_ctx *ctx, const ghmm_raw_region *regions, int32_t n_regions, const ghmm_read_prep *prep,
+                             double *out) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad region array");
+    if (n_regions == 0) return GHMM_OK;
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    RawView v;
+    int rc = raw_view(ctx, regions, n_regions, prep, v);
+    if (rc) return rc;
+    Source src;
+    src.regions = v.regions.data();
+    src.n_regions = n_regions;
+    ghmm_batch &b = ctx->scratch_batch;
+    rc = batch_marshal(ctx, src, b);
+    if (!rc) rc = batch_upload(ctx, b, ctx->stream);
+    if (!rc) rc = raw_prepare_device(ctx, b, v, prep, ctx->stream);
+    if (!rc) rc = batch_forward(ctx, b, ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN);
+    if (!rc) rc = batch_results(ctx, b, out);
+    return rc;
 }
 
 int ghmm_pd_batch_create(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_t n_regions, ghmm_batch **out) {

@@ -80,6 +80,21 @@ class Stats(ctypes.Structure):
                 ("ms_host_tasks", ctypes.c_double), ("n_fp64_exact", ctypes.c_int64)]
 
 
+class RawRead(ctypes.Structure):
+    _fields_ = [("bases", ctypes.c_void_p), ("quals", ctypes.c_void_p), ("ins_quals", ctypes.c_void_p),
+                ("del_quals", ctypes.c_void_p), ("length", ctypes.c_int32), ("mapping_quality", ctypes.c_int32)]
+
+
+class RawRegion(ctypes.Structure):
+    _fields_ = [("reads", ctypes.c_void_p), ("n_reads", ctypes.c_int32), ("haps", ctypes.c_void_p),
+                ("n_haps", ctypes.c_int32)]
+
+
+class ReadPrep(ctypes.Structure):
+    _fields_ = [("base_quality_threshold", ctypes.c_int32), ("cap_to_mapq", ctypes.c_int32),
+                ("pcr_rate_factor", ctypes.c_double), ("gcp", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class PdHap(ctypes.Structure):
     _fields_ = [("bases", ctypes.c_void_p), ("pd_bases", ctypes.c_void_p), ("length", ctypes.c_int32),
                 ("reserved", ctypes.c_int32)]
@@ -152,6 +167,12 @@ _SIGS = {
     "ghmm_batch_results": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _f64p]),
     "ghmm_batch_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Stats)]),
     "ghmm_batch_destroy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "ghmm_compute_regions_raw": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                                ctypes.POINTER(ReadPrep), _f64p]),
+    "ghmm_batch_create_raw": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                             ctypes.POINTER(ReadPrep), ctypes.POINTER(ctypes.c_void_p)]),
+    "ghmm_batch_read_planes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "ghmm_pd_compute_likelihoods": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Read), ctypes.c_int32,
                                                    ctypes.POINTER(PdHap), ctypes.c_int32, _f64p]),
     "ghmm_pd_compute_regions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, _f64p]),

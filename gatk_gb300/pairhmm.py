@@ -180,6 +180,19 @@ class Engine:
     def batch(self, wl: Workload, via_regions: bool = False) -> "Batch":
         return Batch(self, wl, via_regions)
 
+    def compute_raw(self, wl: Workload, mapq, with_indel_quals: bool = True, base_quality_threshold: int = 18,
+                    cap_to_mapq: bool = True, pcr_rate_factor: float = 3.0, gcp: int = 10) -> np.ndarray:
+        """Likelihoods from raw reads, prepared on the device (PairHMMLikelihoodCalculationEngine.modifyReadQualities
+        and the standard imputation); wl.quals are the raw base qualities, wl.ins / wl.dels the BI / BD tags."""
+        from .workload import as_raw_regions
+
+        out = np.empty(max(wl.n_pairs, 1), dtype=np.float64)
+        regs = as_raw_regions(wl, mapq, with_indel_quals)
+        p = native.ReadPrep(int(base_quality_threshold), int(cap_to_mapq), float(pcr_rate_factor), int(gcp), 0)
+        native.check(self.L.ghmm_compute_regions_raw(self._ctx.h, regs, wl.n_regions, ctypes.byref(p),
+                                                     out.ctypes.data_as(native._f64p)), self._ctx.h)
+        return out[:wl.n_pairs]
+
     def pd_compute(self, wl: Workload, hap_pd: np.ndarray) -> np.ndarray:
         """PD-HMM log10 likelihoods of every pair (haplotypes with PD flags), host buffers in and out."""
         from .workload import as_pd_regions
@@ -189,6 +202,11 @@ class Engine:
         native.check(self.L.ghmm_pd_compute_regions(self._ctx.h, regs, wl.n_regions, out.ctypes.data_as(native._f64p)),
                      self._ctx.h)
         return out[:wl.n_pairs]
+
+    def raw_batch(self, wl: Workload, mapq, with_indel_quals: bool = True, base_quality_threshold: int = 18,
+                  cap_to_mapq: bool = True, pcr_rate_factor: float = 3.0, gcp: int = 10) -> "Batch":
+        p = native.ReadPrep(int(base_quality_threshold), int(cap_to_mapq), float(pcr_rate_factor), int(gcp), 0)
+        return Batch(self, wl, raw=(mapq, with_indel_quals, p))
 
     def pd_batch(self, wl: Workload, hap_pd: np.ndarray) -> "Batch":
         return Batch(self, wl, pd=hap_pd)
@@ -218,11 +236,17 @@ class Engine:
 class Batch:
     """A device-resident batch: inputs uploaded once; forward() reruns the kernels on them."""
 
-    def __init__(self, engine: Engine, wl: Workload, via_regions: bool = False, pd=None):
+    def __init__(self, engine: Engine, wl: Workload, via_regions: bool = False, pd=None, raw=None):
         self.engine = engine
         self.wl = wl
         h = ctypes.c_void_p()
-        if pd is not None:
+        if raw is not None:
+            from .workload import as_raw_regions
+
+            mapq, with_indel, prep = raw
+            regs = as_raw_regions(wl, mapq, with_indel)
+            rc = engine.L.ghmm_batch_create_raw(engine.handle, regs, wl.n_regions, ctypes.byref(prep), ctypes.byref(h))
+        elif pd is not None:
             from .workload import as_pd_regions
 
             regs = as_pd_regions(wl, pd)
@@ -259,6 +283,14 @@ class Batch:
         native.check(self.engine.L.ghmm_batch_postprocess(self.engine.handle, self.h, ctypes.byref(p), keep.ctypes.data),
                      self.engine.handle)
         return keep[:self.wl.n_reads]
+
+    def read_planes(self):
+        """The five read planes as the kernels see them: (bases, quals, ins, dels, gcp)."""
+        n = len(self.wl.bases)
+        planes = [np.empty(max(n, 1), dtype=np.uint8) for _ in range(5)]
+        native.check(self.engine.L.ghmm_batch_read_planes(self.engine.handle, self.h, *[p.ctypes.data for p in planes]),
+                     self.engine.handle)
+        return tuple(p[:n] for p in planes)
 
     def stats(self) -> dict:
         s = native.Stats()

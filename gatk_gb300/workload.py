@@ -136,6 +136,32 @@ class Workload:
         return rg.ctypes.data_as(ctypes.POINTER(native.Region))
 
 
+def as_raw_regions(wl: Workload, mapq: np.ndarray, with_indel_quals: bool = True):
+    """ghmm_raw_region array: the workload's bases and base qualities as raw reads with a mapping quality each;
+    the insertion / deletion planes as BI / BD tags, or none (the library's 45) when with_indel_quals is False."""
+    NR, NH, G = wl.n_reads, wl.n_haps, wl.n_regions
+    o = wl.read_off[:-1].astype(np.uint64)
+    rd = np.zeros(max(NR, 1), dtype=[("p", "<u8", (4,)), ("len", "<i4"), ("mapq", "<i4")])
+    rd["p"][:NR, 0] = np.uint64(wl.bases.ctypes.data) + o
+    rd["p"][:NR, 1] = np.uint64(wl.quals.ctypes.data) + o
+    if with_indel_quals:
+        rd["p"][:NR, 2] = np.uint64(wl.ins.ctypes.data) + o
+        rd["p"][:NR, 3] = np.uint64(wl.dels.ctypes.data) + o
+    rd["len"][:NR] = np.diff(wl.read_off)
+    rd["mapq"][:NR] = np.asarray(mapq, dtype=np.int32)
+    hp = np.zeros(max(NH, 1), dtype=[("p", "<u8"), ("len", "<i4"), ("pad", "<i4")])
+    hp["p"][:NH] = np.uint64(wl.hap_bases.ctypes.data) + wl.hap_off[:-1].astype(np.uint64)
+    hp["len"][:NH] = np.diff(wl.hap_off)
+    rg = np.zeros(max(G, 1), dtype=[("reads", "<u8"), ("n_reads", "<i4"), ("pad0", "<i4"), ("haps", "<u8"),
+                                    ("n_haps", "<i4"), ("pad1", "<i4")])
+    rg["reads"][:G] = np.uint64(rd.ctypes.data) + wl.region_read_off[:-1].astype(np.uint64) * np.uint64(40)
+    rg["n_reads"][:G] = np.diff(wl.region_read_off)
+    rg["haps"][:G] = np.uint64(hp.ctypes.data) + wl.region_hap_off[:-1].astype(np.uint64) * np.uint64(16)
+    rg["n_haps"][:G] = np.diff(wl.region_hap_off)
+    wl._keep.append((rd, hp, rg))
+    return rg.ctypes.data
+
+
 def as_pd_regions(wl: Workload, hap_pd: np.ndarray):
     """ghmm_pd_region array for a workload whose haplotypes carry PD flags (hap_pd, parallel to hap_bases)."""
     NR, NH, G = wl.n_reads, wl.n_haps, wl.n_regions

@@ -213,6 +213,47 @@ int ghmm_compute_flat(ghmm_ctx *ctx, const ghmm_flat *flat, double *out);
 /* The CUDA stream the context launches on (a cudaStream_t), for callers that time or order work. */
 void *ghmm_stream(ghmm_ctx *ctx);
 
+/* Reads as they come off the alignment, prepared for the PairHMM on the device: what
+ * PairHMMLikelihoodCalculationEngine.modifyReadQualities does on the host in GATK (HC/PairHMMLikelihoodCalculation
+ * Engine.java:283-322): the PCR indel error model (:331-371, with findTandemRepeatUnits,
+ * HC/ReadLikelihoodCalculationEngine.java:193-253), base qualities capped by the mapping quality, base qualities below
+ * the threshold and insertion / deletion qualities below 6 set to 6; and the standard input-score imputation (a
+ * constant gap continuation penalty; insertion / deletion qualities from the BI / BD tags, or 45 when a read has
+ * none, ReadUtils.java:838-862).  Soft-clip removal stays with the caller (it needs the CIGAR). */
+typedef struct ghmm_raw_read {
+    const uint8_t *bases;
+    const uint8_t *quals;     /* base qualities as read */
+    const uint8_t *ins_quals; /* BI tag, or NULL for 45 */
+    const uint8_t *del_quals; /* BD tag, or NULL for 45 */
+    int32_t length;
+    int32_t mapping_quality;
+} ghmm_raw_read;
+
+typedef struct ghmm_raw_region {
+    const ghmm_raw_read *reads;
+    int32_t n_reads;
+    const ghmm_hap *haps;
+    int32_t n_haps;
+} ghmm_raw_region;
+
+typedef struct ghmm_read_prep {
+    int32_t base_quality_threshold; /* --base-quality-score-threshold (PairHMM.BASE_QUALITY_SCORE_THRESHOLD = 18) */
+    int32_t cap_to_mapq;            /* !disableCapReadQualitiesToMapQ */
+    double pcr_rate_factor;         /* PCRErrorModel: 0 NONE, 1 HOSTILE, 2 AGGRESSIVE, 3 CONSERVATIVE (GATK default) */
+    int32_t gcp;                    /* constant gap continuation penalty (--gcp-hmm, default 10), 1..127 */
+    int32_t reserved;
+} ghmm_read_prep;
+
+/* As ghmm_compute_regions, from raw reads; the preparation runs on the device before the forward. */
+int ghmm_compute_regions_raw(ghmm_ctx *ctx, const ghmm_raw_region *regions, int32_t n_regions, const ghmm_read_prep *prep,
+                             double *out);
+int ghmm_batch_create_raw(ghmm_ctx *ctx, const ghmm_raw_region *regions, int32_t n_regions, const ghmm_read_prep *prep,
+                          ghmm_batch **batch);
+/* Copy a batch's five read planes as the kernels see them (after the device preparation of a raw batch) into
+ * host arrays of n_read_bytes each, reads back to back in batch order; any pointer may be NULL. */
+int ghmm_batch_read_planes(ghmm_ctx *ctx, const ghmm_batch *batch, uint8_t *bases, uint8_t *quals, uint8_t *ins,
+                           uint8_t *dels, uint8_t *gcp);
+
 /* Partially-determined-haplotype PairHMM (PD-HMM), the DRAGEN-GATK mode's likelihood step: LoglessPDPairHMM
  * (PH/LoglessPDPairHMM.java:35-150), whose native binding IntelPDHMM.computeLikelihoods(ReadDataHolder[],
  * HaplotypeDataHolder[], double[]) is called at PH/VectorLoglessPairPDHMM.java:98.  A PD haplotype carries, beside its

@@ -58,7 +58,8 @@ def test_struct_layouts_match_the_header(tmp_path):
                "ghmm_region": native.Region, "ghmm_flat": native.Flat, "ghmm_stats": native.Stats,
                "ghmm_tuning": native.Tuning, "ghmm_queue_info": native.QueueInfo,
                "ghmm_dev_pairs": native.DevPairs, "ghmm_calib_batch": native.CalibBatch,
-               "ghmm_postprocess": native.Postprocess, "ghmm_pd_hap": native.PdHap, "ghmm_pd_region": native.PdRegion}
+               "ghmm_postprocess": native.Postprocess, "ghmm_pd_hap": native.PdHap, "ghmm_pd_region": native.PdRegion,
+               "ghmm_raw_read": native.RawRead, "ghmm_raw_region": native.RawRegion, "ghmm_read_prep": native.ReadPrep}
     src = tmp_path / "sizes.c"
     src.write_text('#include <stdio.h>\n#include "ghmm.h"\n#include "ghmm_calib.h"\nint main(void) {\n' +
                    "".join(f'printf("{n} %zu\\n", sizeof({n}));\n' for n in structs) + "return 0;\n}\n")
