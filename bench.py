@@ -5,6 +5,7 @@
     python bench.py --stream [--regions N] [--batch-cells C]     (workload 4 through the streaming queue)
     python bench.py --calib                                      (workload 3: calibration forward + backward)
     python bench.py --pd [--regions N]                           (PD-HMM, DRAGEN-GATK mode)
+    python bench.py --sw [--regions N]                           (Smith-Waterman realignment to the best haplotype)
 
 A step is one forward over the whole workload (default: workload 1, 10,000 synthetic active regions,
 seed 1, ~1.06e12 cells): every read x haplotype pair of every region, FP32 wavefront plus the FP64 rerun
@@ -628,6 +629,118 @@ def run_pd(args):
     return 0
 
 
+SW_OPS_PER_CELL = 12  # calculateMatrix's inner loop: 5 adds, 6 compares / maxima, the base compare
+
+
+def run_sw(args):
+    """--sw: the step after the likelihoods, AssemblyBasedCallerUtils.realignReadsToTheirBestHaplotype on workload
+    1: every read realigned with Smith-Waterman (ALIGNMENT_TO_BEST_HAPLOTYPE_SW_PARAMETERS, SOFTCLIP, the exact-
+    substring shortcut) against the haplotype its likelihoods favour, ties broken toward the region's first
+    (reference) haplotype.  A step is one ghmm_batch_realign over every read of the workload with the sequences and
+    the PairHMM likelihoods resident on the GPU (cigars come back to the host inside the step).  `value` is GCUPS
+    over the cells of the alignments that ran the score recurrence, per device second; `e2e` is the same alignments
+    through ghmm_sw_align_batch from host buffers (marshal, H2D, kernels, D2H).  The CPU baseline is the C
+    restatement of SmithWatermanJavaAligner on every host core over the leading reads; its cigars and offsets must
+    equal the GPU's."""
+    import ctypes
+
+    import numpy as np
+
+    from gatk_gb300 import native, workload as W
+    from gatk_gb300 import smithwaterman as SWG
+    from gatk_gb300.pairhmm import Batch, Engine
+    from oracle import oracle as O
+
+    eng = Engine()
+    wl = W.generate(1, regions=args.regions or None)
+    n_regions = wl.n_regions
+    batch = Batch(eng, wl)
+    batch.forward()
+    prio = np.zeros(wl.n_haps, dtype=np.float64)
+    prio[wl.region_hap_off[:-1]] = 1.0  # HAPLOTYPE_ALIGNMENT_TIEBREAKING_PRIORITY: reference haplotype, no cigars
+    for _ in range(args.warmup):
+        best, inf, res = SWG.realign_batch(batch, prio)
+    clocks = ClockSampler(0)
+    clocks.start()
+    sts = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        best, inf, res = SWG.realign_batch(batch, prio)
+        sts.append(SWG.sw_stats(eng.L, eng.handle))
+    dt_call = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    st = sts[-1]
+    cells = st["cells"]
+    ms_dev = statistics.mean(x["ms_device"] for x in sts)
+    ms_fwd = statistics.mean(x["ms_forward"] for x in sts)
+    batch.close()
+    # the same (haplotype, read) pairs from host buffers through the batched C-ABI call
+    pairs = np.zeros(wl.n_reads, dtype=[("ref", "<u8"), ("alt", "<u8"), ("ref_len", "<i4"), ("alt_len", "<i4")])
+    region_of = np.repeat(np.arange(wl.n_regions), np.diff(wl.region_read_off))
+    hap = wl.region_hap_off[region_of] + best
+    pairs["ref"] = wl.hap_bases.ctypes.data + wl.hap_off[hap]
+    pairs["ref_len"] = wl.hap_off[hap + 1] - wl.hap_off[hap]
+    pairs["alt"] = wl.bases.ctypes.data + wl.read_off[:-1]
+    pairs["alt_len"] = np.diff(wl.read_off)
+    cap = int(2 * pairs["alt_len"].sum() + 4 * wl.n_reads)
+    res2, off2, start2, len2, ops2 = SWG._result(wl.n_reads, cap)
+    p = SWG.ALIGNMENT_TO_BEST_HAPLOTYPE_SW_PARAMETERS.as_native()
+    pp = ctypes.cast(pairs.ctypes.data, ctypes.POINTER(native.SwPair))
+    for _ in range(2):
+        native.check(eng.L.ghmm_sw_align_batch(eng.handle, pp, wl.n_reads, ctypes.byref(p), native.SW_SOFTCLIP,
+                                               native.SW_SUBSTRING_SHORTCUT, ctypes.byref(res2)), eng.handle)
+    t0 = time.perf_counter()
+    native.check(eng.L.ghmm_sw_align_batch(eng.handle, pp, wl.n_reads, ctypes.byref(p), native.SW_SOFTCLIP,
+                                           native.SW_SUBSTRING_SHORTCUT, ctypes.byref(res2)), eng.handle)
+    dt_e2e = time.perf_counter() - t0
+    st2 = SWG.sw_stats(eng.L, eng.handle)
+    same = (np.array_equal(off2[:wl.n_reads], res.offset) and np.array_equal(len2[:wl.n_reads], res.cigar_len)
+            and np.array_equal(ops2[:res2.cigar_total], res.cigar_ops))
+    # CPU baseline and parity on the leading reads
+    lens = pairs["ref_len"].astype(np.int64) * pairs["alt_len"]
+    n_cpu = int(min(wl.n_reads, np.searchsorted(np.cumsum(lens), args.cpu_cells / 2) + 1))
+    t1 = time.perf_counter()
+    ops_c, start_c, n_c, off_c = O.sw_align_pairs(wl.hap_bases, wl.hap_off[hap[:n_cpu]], pairs["ref_len"][:n_cpu],
+                                                  wl.bases, wl.read_off[:n_cpu], pairs["alt_len"][:n_cpu],
+                                                  (10, -15, -30, -5), native.SW_SOFTCLIP, True)
+    cpu_dt = time.perf_counter() - t1
+    mism = 0
+    for i in range(n_cpu):
+        if off_c[i] != res.offset[i] or not np.array_equal(ops_c[start_c[i]:start_c[i] + n_c[i]], res.ops(i)):
+            mism += 1
+    with SWG.SmithWatermanCudaAligner() as a:
+        peak = a.measure_peak()
+    achieved = SW_OPS_PER_CELL * cells / (ms_fwd * 1e-3) / 1e12
+    line = {
+        "metric": "Smith-Waterman realignment GCUPS (reads to their best haplotype) on 1 GB300",
+        "value": cells / (ms_dev * 1e-3) / 1e9, "unit": "GCUPS", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_dev, "higher_is_better": True, "dtype": "int32",
+        "data": "synthetic (workload 1; best haplotypes from the PairHMM forward)",
+        "config": {"workload": f"config1: {n_regions} regions, every read against its best haplotype",
+                   "reads": int(wl.n_reads), "alignments_with_recurrence": int(st["n_alignments"] - st["n_shortcut"]),
+                   "substring_shortcut": int(st["n_shortcut"]), "cells": int(cells), "chunks": int(st["chunks"]),
+                   "parameters": "ALIGNMENT_TO_BEST_HAPLOTYPE_SW_PARAMETERS (10, -15, -30, -5), SOFTCLIP"},
+        "realign_call_ms": dt_call * 1e3,
+        "alignments_per_s": wl.n_reads / (dt_call),
+        "roofline": {"bound": "int32_alu", "achieved": achieved, "peak": peak, "unit": "Tops/s",
+                     "frac": achieved / peak, "ops_per_cell": SW_OPS_PER_CELL, "kernel": "sw_forward_kernel<K>",
+                     "ms_forward": ms_fwd, "peak_source": "measured in this run: max.s32 register loop over all SMs"},
+        "e2e": {"value": st2["cells"] / dt_e2e / 1e9, "unit": "GCUPS", "ms_per_step": dt_e2e * 1e3,
+                "h2d_bytes_per_step": int(st2["h2d_bytes"]), "d2h_bytes_per_step": int(st2["d2h_bytes"]),
+                "api": "ghmm_sw_align_batch (host pairs, SOFTCLIP, substring shortcut)", "matches_realign": bool(same)},
+        "gpu_launches": int(st["launches"]),
+        "clocks": clk,
+        "cpu_baseline": {"value": float(lens[:n_cpu].sum()) / cpu_dt / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),
+                         "kind": "port", "sample": f"first {n_cpu} reads against their best haplotypes "
+                                                   f"({float(lens[:n_cpu].sum()):.3e} cells)",
+                         "host": f"{platform.machine()} x{os.cpu_count()}"},
+        "parity_vs_oracle": {"sample_reads": n_cpu, "mismatches": mism},
+    }
+    print(json.dumps(line), flush=True)
+    eng.close()
+    return 0 if mism == 0 and same else 1
+
+
 def apply_tuning(args, eng, wl):
     """--tuning K,KM,C sets the launch shape; --autotune runs the native autotuner on the whole workload
     (untimed) over the candidates it names.  Returns what was used."""
@@ -694,6 +807,8 @@ def main():
     ap.add_argument("--pd", action="store_true", help="PD-HMM over workload 1 regions with synthetic PD flags")
     ap.add_argument("--calib", action="store_true",
                     help="time the calibration forward + backward on workload 3 and check its gradient")
+    ap.add_argument("--sw", action="store_true",
+                    help="Smith-Waterman realignment of every workload 1 read to its best haplotype")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -707,6 +822,8 @@ def main():
         return run_calib(args)
     if args.pd:
         return run_pd(args)
+    if args.sw:
+        return run_sw(args)
     return run_ours(args)
 
 

@@ -23,9 +23,9 @@ OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libghmm.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kernels.cu", "noalloc.cu", "calib.cu", "post.cu", "pd.cu", "prep.cu"]
-CPP_SOURCES = ["runtime.cpp", "tables.cpp", "synth.cpp", "str_analyzer.cpp"]
-HEADERS = ["ghmm_internal.h", "tables.h", "str_analyzer.h"]
+CU_SOURCES = ["kernels.cu", "noalloc.cu", "calib.cu", "post.cu", "pd.cu", "prep.cu", "sw.cu"]
+CPP_SOURCES = ["runtime.cpp", "tables.cpp", "synth.cpp", "str_analyzer.cpp", "sw_host.cpp"]
+HEADERS = ["ghmm_internal.h", "tables.h", "str_analyzer.h", "host_util.h"]
 
 
 def nvcc() -> str:

@@ -132,6 +132,56 @@ int calib_block();
 int launch_calib(const DevTables &TB, const ghmm_calib_batch &in, int k, bool backward, bool fp64, void *scratch,
                  int64_t scratch_bytes_per_warp, double *loglik, const double *weights, float *grad_open,
                  float *grad_cont, int *need_fp64, int sm_count, cudaStream_t s);
+// Smith-Waterman (sw.cu).  Overhang strategies (SWOverhangStrategy) and BAM cigar op codes.
+constexpr int kSwSoftclip = 0, kSwIndel = 1, kSwLeadingIndel = 2, kSwIgnore = 3;
+constexpr uint32_t kSwOpM = 0, kSwOpI = 1, kSwOpD = 2, kSwOpS = 4;
+constexpr int kSwMaxK = 8;  // alt columns per lane; longer alts run in strips of 32 * 8 columns
+
+// One alignment: alt against ref.  Offsets index the ref / alt planes and the chunk's buffers.
+struct SwPair {
+    int64_t ref_off, alt_off;
+    int64_t tb_off;       // first traceback word: strips x (ref_len + 31) steps x 32 lanes
+    int64_t edge_off;     // ref_len last-column scores, then alt_len bottom-row scores
+    int64_t slot_off;     // 2 * alt_len + 4 cigar ops, written in reverse by the traceback
+    int64_t scratch_off;  // strip boundary (score, horizontal gap) per ref row 0..ref_len, multi-strip alts only
+    int32_t ref_len, alt_len;
+    int32_t k, pad;       // alt columns per lane
+};
+
+struct SwArgs {
+    const uint8_t *ref_plane, *alt_plane;
+    const SwPair *pairs;  // the chunk's pairs; state / offset / n_ops are indexed like them
+    uint32_t *tb;
+    int *edges;
+    int2 *strip_scratch;
+    uint32_t *slot;
+    int32_t *state;       // 1: solved by the exact-substring shortcut
+    int32_t *offset;      // alignment offset
+    int32_t *n_ops;
+    int *error;           // set when a traceback overruns its slot (cannot happen for valid input)
+    int match, mismatch, open, extend;
+    int strategy, indel_edges, shortcut;
+};
+int launch_sw_forward(const SwArgs &a, int k, const int32_t *tasks, int n_tasks, int *cursor, int grid,
+                      cudaStream_t s);
+int sw_forward_occupancy(int k, int *blocks_per_sm);
+int launch_sw_traceback(const SwArgs &a, int n_pairs, cudaStream_t s);
+// exclusive scan of the chunk's n_ops into starts (offset by *running, which then advances), gather into ops
+int launch_sw_compact(const SwArgs &a, int n_pairs, int64_t *starts, int64_t *running, uint32_t *ops, int64_t ops_cap,
+                      cudaStream_t s);
+
+// Read-to-best-haplotype realignment setup (sw.cu): per read, the best haplotype of its region by
+// AlleleLikelihoods.searchBestAllele with tie-breaking priorities, written into the read's SwPair (ref fields).
+struct SwRealignArgs {
+    const double *priority;  // per batch haplotype, or nullptr
+    SwPair *pairs;           // one per read, alt fields and buffer offsets filled by the host
+    int32_t *best;           // per read: best haplotype's index within its region
+    uint8_t *informative;    // per read: BestAllele.isInformative()
+    int64_t first_read, n_reads;
+};
+int launch_sw_realign_setup(const DevBatch &b, const SwRealignArgs &a, int sm_count, cudaStream_t s);
+// Measured int32 max throughput of the device in Tops/s (sw.cu).
+int measure_int32_peak(int sm_count, double *tops, cudaStream_t s);
 // Message returned by ghmm_last_error(NULL, ...) (runtime.cpp).
 void set_global_error(const char *msg);
 

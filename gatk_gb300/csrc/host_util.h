@@ -1,0 +1,117 @@
+// host_util.h -- host-side helpers shared by the runtime (runtime.cpp) and the Smith-Waterman host code
+// (sw_host.cpp): device and pinned buffers that grow, a thread pool loop, and the context and batch views the
+// Smith-Waterman code needs from the runtime.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdint>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ghmm_internal.h"
+
+struct ghmm_ctx;
+struct ghmm_batch;
+
+namespace ghmm {
+
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t cap = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= cap && p) return cudaSuccess;
+        // a buffer that has to grow again grows by a quarter more than asked, so that batches of slowly
+        // rising size do not free (and so synchronise the device) every time
+        const size_t want = std::max<size_t>(cap ? std::max(n, cap + cap / 4) : n, 1);
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+template <typename T>
+struct HostBuf {  // pinned
+    T *p = nullptr;
+    size_t cap = 0;
+    cudaError_t reserve(size_t n) {
+        if (n <= cap && p) return cudaSuccess;
+        const size_t want = std::max<size_t>(cap ? std::max(n, cap + cap / 4) : n, 1);
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMallocHost(&p, want * sizeof(T));
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+inline int hw_threads(int requested) {
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    return requested > 0 ? std::min(requested, hw) : hw;
+}
+
+template <typename F>
+inline void parallel_for(int64_t n, int threads, F f, int64_t grain = 64) {
+    if (n <= 0) return;
+    threads = (int)std::min<int64_t>(threads, n);
+    if (threads <= 1) {
+        for (int64_t i = 0; i < n; i++) f(i);
+        return;
+    }
+    std::atomic<int64_t> next{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; t++)
+        pool.emplace_back([&] {
+            for (;;) {
+                const int64_t i0 = next.fetch_add(grain);
+                if (i0 >= n) break;
+                const int64_t i1 = std::min(n, i0 + grain);
+                for (int64_t i = i0; i < i1; i++) f(i);
+            }
+        });
+    for (auto &th : pool) th.join();
+}
+
+struct SwEngine;
+void sw_engine_destroy(SwEngine *e);
+
+// What the Smith-Waterman entry points need from a context (runtime.cpp).
+struct CtxInfo {
+    int device = 0, sm_count = 0, threads = 0;
+    cudaStream_t stream = nullptr;
+    SwEngine **sw = nullptr;  // the context's Smith-Waterman buffers, created on first use
+};
+// GHMM_ERR_STATE when the context is NULL or closed.
+int ctx_info(ghmm_ctx *ctx, CtxInfo *info);
+// Records msg as the context's last error and returns code.
+int ctx_fail(ghmm_ctx *ctx, int code, const std::string &msg);
+
+// A batch's device view and host offsets (runtime.cpp): read_off[n_reads + 1], hap_off[n_haps + 1],
+// region_read_off[n_regions + 1], region_hap_off[n_regions + 1], out_off[n_regions + 1], back to back.
+struct BatchInfo {
+    const DevBatch *dev = nullptr;
+    const int64_t *h_off = nullptr;
+    int64_t n_regions = 0, n_reads = 0, n_haps = 0;
+    bool has_results = false;  // uploaded and run at least once
+};
+void batch_info(const ghmm_batch *b, BatchInfo *info);
+
+}  // namespace ghmm

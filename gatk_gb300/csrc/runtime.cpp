@@ -24,6 +24,7 @@
 
 #include "../../include/ghmm.h"
 #include "ghmm_internal.h"
+#include "host_util.h"
 #include "tables.h"
 
 using namespace ghmm;
@@ -56,77 +57,6 @@ uint8_t base_index(uint8_t b) {
         case 'T': return 3;
         default: return 4;
     }
-}
-
-template <typename T>
-struct DevBuf {
-    T *p = nullptr;
-    size_t cap = 0;
-    cudaError_t reserve(size_t n) {
-        if (n <= cap && p) return cudaSuccess;
-        // a buffer that has to grow again grows by a quarter more than asked, so that batches of slowly
-        // rising size do not free (and so synchronise the device) every time
-        const size_t want = std::max<size_t>(cap ? std::max(n, cap + cap / 4) : n, 1);
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
-        if (e == cudaSuccess) cap = want;
-        return e;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-};
-
-template <typename T>
-struct HostBuf {  // pinned
-    T *p = nullptr;
-    size_t cap = 0;
-    cudaError_t reserve(size_t n) {
-        if (n <= cap && p) return cudaSuccess;
-        const size_t want = std::max<size_t>(cap ? std::max(n, cap + cap / 4) : n, 1);
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        cap = 0;
-        cudaError_t e = cudaMallocHost(&p, want * sizeof(T));
-        if (e == cudaSuccess) cap = want;
-        return e;
-    }
-    void release() {
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        cap = 0;
-    }
-};
-
-int hw_threads(int requested) {
-    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-    return requested > 0 ? std::min(requested, hw) : hw;
-}
-
-template <typename F>
-void parallel_for(int64_t n, int threads, F f, int64_t grain = 64) {
-    if (n <= 0) return;
-    threads = (int)std::min<int64_t>(threads, n);
-    if (threads <= 1) {
-        for (int64_t i = 0; i < n; i++) f(i);
-        return;
-    }
-    std::atomic<int64_t> next{0};
-    std::vector<std::thread> pool;
-    for (int t = 0; t < threads; t++)
-        pool.emplace_back([&] {
-            for (;;) {
-                const int64_t i0 = next.fetch_add(grain);
-                if (i0 >= n) break;
-                const int64_t i1 = std::min(n, i0 + grain);
-                for (int64_t i = i0; i < i1; i++) f(i);
-            }
-        });
-    for (auto &th : pool) th.join();
 }
 
 struct Bucket {
@@ -243,6 +173,7 @@ struct ghmm_ctx {
     DevBuf<double> calib_ones;
     ghmm_queue *pipe = nullptr;      // the queue that pipelines large synchronous calls
     std::atomic<int> open_queues{0};  // queues of this context not yet destroyed (including pipe)
+    SwEngine *sw = nullptr;          // Smith-Waterman buffers (sw_host.cpp), created on first use
     bool alive = false;
 };
 
@@ -1744,6 +1675,8 @@ int ghmm_done(ghmm_ctx *ctx) {
     ctx->calib_scratch.release();
     ctx->calib_flags.release();
     ctx->calib_ones.release();
+    sw_engine_destroy(ctx->sw);
+    ctx->sw = nullptr;
     if (ctx->table_mem) cudaFree(ctx->table_mem);
     delete ctx->host_tables;
     for (auto &ev : ctx->ev)
@@ -2236,3 +2169,28 @@ int ghmm_debug_tables(ghmm_ctx *ctx, double *err, double *prob, double *m2m) {
 }
 
 }  // extern "C"
+
+namespace ghmm {
+
+int ctx_info(ghmm_ctx *ctx, CtxInfo *info) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    info->device = ctx->device;
+    info->sm_count = ctx->sm_count;
+    info->threads = hw_threads(ctx->max_threads);
+    info->stream = ctx->stream;
+    info->sw = &ctx->sw;
+    return GHMM_OK;
+}
+
+int ctx_fail(ghmm_ctx *ctx, int code, const std::string &msg) { return fail(ctx, code, msg); }
+
+void batch_info(const ghmm_batch *b, BatchInfo *info) {
+    info->dev = &b->dev;
+    info->h_off = b->h_off.p;
+    info->n_regions = b->n_regions;
+    info->n_reads = b->n_reads;
+    info->n_haps = b->n_haps;
+    info->has_results = b->uploaded && b->last_mode >= 0;
+}
+
+}  // namespace ghmm

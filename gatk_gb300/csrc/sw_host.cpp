@@ -1,0 +1,595 @@
+// sw_host.cpp -- host side of the Smith-Waterman entry points (include/ghmm_sw.h): ghmm_sw_align (the
+// SWAlignerNativeBinding.align mirror), ghmm_sw_align_batch and ghmm_batch_realign.
+//
+// A call flows: validate and marshal (refs deduplicated by address, one pinned plane of refs then alts) -> plan
+// chunks so that each chunk's traceback bits fit the traceback buffer (4 bits per cell, 32-bit words per lane and
+// step) -> one H2D -> per chunk: the score-recurrence kernels by alt columns per lane (8 .. 1, longest refs first),
+// the traceback kernel, the cigar compaction into one device array -> D2H of offsets and counts, then of the ops.
+// The realign path takes its sequences and likelihoods from a PairHMM batch already on the device: the host only
+// sizes each read's buffers by the longest haplotype of its region, and a setup kernel picks the haplotype.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/ghmm.h"
+#include "../../include/ghmm_sw.h"
+#include "ghmm_internal.h"
+#include "host_util.h"
+
+using namespace ghmm;
+
+namespace ghmm {
+
+struct SwEngine {
+    HostBuf<SwPair> h_pairs;
+    DevBuf<SwPair> d_pairs;
+    HostBuf<int32_t> h_tasks;
+    DevBuf<int32_t> d_tasks;
+    HostBuf<uint8_t> h_planes;
+    DevBuf<uint8_t> d_planes;
+    DevBuf<int32_t> d_res;      // state | offset | n_ops | best, n each
+    DevBuf<int64_t> d_starts;
+    DevBuf<uint32_t> d_ops;
+    DevBuf<int64_t> d_counters; // [0] running op total, [1] error flag (as int), then int cursors
+    DevBuf<uint32_t> d_tb;
+    DevBuf<int> d_edges;
+    DevBuf<int2> d_scratch;
+    DevBuf<uint32_t> d_slot;
+    DevBuf<double> d_prio;
+    DevBuf<uint8_t> d_inf;
+    HostBuf<int32_t> h_res;
+    HostBuf<int64_t> h_starts;
+    HostBuf<int64_t> h_counters;
+    HostBuf<uint32_t> h_ops;
+    std::vector<cudaEvent_t> events;
+    ghmm_sw_stats stats{};
+    int64_t tb_budget_words = int64_t(1) << 30;  // 4 GiB of traceback bits per chunk
+
+    cudaEvent_t event(size_t i) {
+        while (events.size() <= i) {
+            cudaEvent_t e = nullptr;
+            cudaEventCreate(&e);
+            events.push_back(e);
+        }
+        return events[i];
+    }
+    void release() {
+        h_pairs.release(); d_pairs.release(); h_tasks.release(); d_tasks.release(); h_planes.release();
+        d_planes.release(); d_res.release(); d_starts.release(); d_ops.release(); d_counters.release();
+        d_tb.release(); d_edges.release(); d_scratch.release(); d_slot.release(); d_prio.release(); d_inf.release();
+        h_res.release(); h_starts.release(); h_counters.release(); h_ops.release();
+        for (auto e : events) cudaEventDestroy(e);
+        events.clear();
+    }
+};
+
+void sw_engine_destroy(SwEngine *e) {
+    if (!e) return;
+    e->release();
+    delete e;
+}
+
+}  // namespace ghmm
+
+namespace {
+
+#define SW_CUDA(call, what)                                             \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return cuda_error(ctx, e_, what);        \
+    } while (0)
+
+int cuda_error(ghmm_ctx *ctx, cudaError_t e, const char *what) {
+    return ctx_fail(ctx, e == cudaErrorMemoryAllocation ? GHMM_ERR_NOMEM : GHMM_ERR_CUDA,
+                    std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+constexpr int kCursorsPerChunk = kSwMaxK + 1;
+
+int sw_k(int alt_len) { return alt_len > 32 * kSwMaxK ? kSwMaxK : (alt_len + 31) / 32; }
+
+struct Chunk {
+    int64_t p0 = 0, p1 = 0;
+    int64_t tb_words = 0, edges = 0, slots = 0, scratch = 0;
+    int64_t task_begin[kSwMaxK + 1]{}, task_count[kSwMaxK + 1]{};
+};
+
+// Buffer offsets (chunk-relative) and alt columns per lane of every pair, chunk boundaries, and per chunk the
+// pairs of each K sorted by decreasing work.  ref_bound[i] sizes pair i's buffers (its ref length, or an upper
+// bound of it when the ref is chosen on the device).
+void plan(SwPair *pairs, const int32_t *ref_bound, int64_t n, int64_t budget_words, std::vector<Chunk> &chunks,
+          int32_t *tasks) {
+    chunks.clear();
+    Chunk c;
+    for (int64_t i = 0; i < n; ++i) {
+        SwPair &P = pairs[i];
+        if (ref_bound[i] <= 0) {  // nothing to align against: no task, no buffers
+            P.k = 1;
+            P.tb_off = P.edge_off = P.slot_off = c.slots;
+            P.scratch_off = -1;
+            c.slots += 2 * (int64_t)P.alt_len + 4;
+            continue;
+        }
+        const int k = sw_k(P.alt_len);
+        const int64_t strips = (P.alt_len + 32 * k - 1) / (32 * k);
+        const int64_t rb = ref_bound[i];
+        const int64_t words = strips * (rb + 31) * 32;
+        if (i > c.p0 && c.tb_words + words > budget_words) {
+            c.p1 = i;
+            chunks.push_back(c);
+            c = Chunk{};
+            c.p0 = i;
+        }
+        P.k = k;
+        P.tb_off = c.tb_words;
+        P.edge_off = c.edges;
+        P.slot_off = c.slots;
+        P.scratch_off = strips > 1 ? c.scratch : -1;
+        c.tb_words += words;
+        c.edges += rb + P.alt_len;
+        c.slots += 2 * (int64_t)P.alt_len + 4;
+        if (strips > 1) c.scratch += rb + 1;
+    }
+    c.p1 = n;
+    if (n > 0) chunks.push_back(c);
+    // tasks: chunk-local pair indices, grouped by K, longest work first
+    int64_t pos = 0;
+    std::vector<int32_t> tmp;
+    for (auto &ch : chunks) {
+        for (int k = kSwMaxK; k >= 1; --k) {
+            tmp.clear();
+            for (int64_t i = ch.p0; i < ch.p1; ++i)
+                if (pairs[i].k == k && ref_bound[i] > 0) tmp.push_back((int32_t)(i - ch.p0));
+            std::stable_sort(tmp.begin(), tmp.end(), [&](int32_t a, int32_t b) {
+                const SwPair &A = pairs[ch.p0 + a], &B = pairs[ch.p0 + b];
+                return (int64_t)ref_bound[ch.p0 + a] * A.alt_len > (int64_t)ref_bound[ch.p0 + b] * B.alt_len;
+            });
+            ch.task_begin[k] = pos;
+            ch.task_count[k] = (int64_t)tmp.size();
+            std::copy(tmp.begin(), tmp.end(), tasks + pos);
+            pos += (int64_t)tmp.size();
+        }
+    }
+}
+
+struct RunIn {
+    const uint8_t *ref_plane, *alt_plane;
+    const ghmm_sw_params *params;
+    int strategy, shortcut;
+    int64_t n;
+    const int32_t *ref_bound;
+    int64_t ops_cap;
+    // realign: device setup before the chunks
+    const BatchInfo *batch = nullptr;
+    const double *priority = nullptr;  // host, per batch haplotype
+};
+
+// Everything after the host pairs are filled: plan, upload, kernels, results into the engine's host buffers.
+// On return h_res holds state | offset | n_ops | best (n each), h_starts the op starts, h_counters[0] the op
+// total, and h_ops the ops.
+int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t plane_bytes,
+        std::vector<uint8_t> *informative) {
+    const int64_t n = in.n;
+    cudaStream_t s = ci.stream;
+    std::vector<Chunk> chunks;
+    SW_CUDA(E.h_tasks.reserve((size_t)std::max<int64_t>(n, 1)), "pinned tasks");
+    plan(E.h_pairs.p, in.ref_bound, n, E.tb_budget_words, chunks, E.h_tasks.p);
+    int64_t max_tb = 0, max_edges = 0, max_slots = 0, max_scratch = 0;
+    for (auto &c : chunks) {
+        max_tb = std::max(max_tb, c.tb_words);
+        max_edges = std::max(max_edges, c.edges);
+        max_slots = std::max(max_slots, c.slots);
+        max_scratch = std::max(max_scratch, c.scratch);
+    }
+    const int64_t n_cursors = 2 + (int64_t)chunks.size() * kCursorsPerChunk;
+    SW_CUDA(E.d_pairs.reserve((size_t)n), "device pairs");
+    SW_CUDA(E.d_tasks.reserve((size_t)n), "device tasks");
+    SW_CUDA(E.d_res.reserve((size_t)n * 4), "device results");
+    SW_CUDA(E.d_starts.reserve((size_t)n), "device cigar starts");
+    SW_CUDA(E.d_ops.reserve((size_t)std::max<int64_t>(in.ops_cap, 1)), "device cigar ops");
+    SW_CUDA(E.d_counters.reserve((size_t)n_cursors), "device counters");
+    SW_CUDA(E.d_tb.reserve((size_t)max_tb), "traceback buffer");
+    SW_CUDA(E.d_edges.reserve((size_t)max_edges), "edge scores");
+    SW_CUDA(E.d_scratch.reserve((size_t)std::max<int64_t>(max_scratch, 1)), "strip scratch");
+    SW_CUDA(E.d_slot.reserve((size_t)max_slots), "cigar slots");
+    SW_CUDA(E.h_res.reserve((size_t)n * 4), "pinned results");
+    SW_CUDA(E.h_starts.reserve((size_t)n), "pinned starts");
+    SW_CUDA(E.h_counters.reserve(2), "pinned counters");
+    if (plane_bytes > 0)
+        SW_CUDA(cudaMemcpyAsync(E.d_planes.p, E.h_planes.p, (size_t)plane_bytes, cudaMemcpyHostToDevice, s),
+                "H2D sequences");
+    SW_CUDA(cudaMemcpyAsync(E.d_pairs.p, E.h_pairs.p, (size_t)n * sizeof(SwPair), cudaMemcpyHostToDevice, s),
+            "H2D pairs");
+    SW_CUDA(cudaMemcpyAsync(E.d_tasks.p, E.h_tasks.p, (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice, s),
+            "H2D tasks");
+    SW_CUDA(cudaMemsetAsync(E.d_counters.p, 0, (size_t)n_cursors * sizeof(int64_t), s), "zero counters");
+    E.stats.h2d_bytes = plane_bytes + n * (int64_t)(sizeof(SwPair) + sizeof(int32_t));
+    int launches = 0;
+    int32_t *d_state = E.d_res.p, *d_offset = E.d_res.p + n, *d_nops = E.d_res.p + 2 * n, *d_best = E.d_res.p + 3 * n;
+    int *d_err = reinterpret_cast<int *>(E.d_counters.p + 1);
+    int *d_cursors = reinterpret_cast<int *>(E.d_counters.p + 2);
+    SW_CUDA(cudaEventRecord(E.event(0), s), "event");
+    if (in.batch) {
+        SwRealignArgs R{};
+        if (in.priority) {
+            SW_CUDA(E.d_prio.reserve((size_t)in.batch->n_haps), "device priorities");
+            SW_CUDA(cudaMemcpyAsync(E.d_prio.p, in.priority, (size_t)in.batch->n_haps * sizeof(double),
+                                    cudaMemcpyHostToDevice, s), "H2D priorities");
+            R.priority = E.d_prio.p;
+            E.stats.h2d_bytes += in.batch->n_haps * (int64_t)sizeof(double);
+        }
+        SW_CUDA(E.d_inf.reserve((size_t)n), "device informative flags");
+        R.pairs = E.d_pairs.p;
+        R.best = d_best;
+        R.informative = E.d_inf.p;
+        R.first_read = 0;
+        R.n_reads = n;
+        const int e = launch_sw_realign_setup(*in.batch->dev, R, ci.sm_count, s);
+        if (e) return cuda_error(ctx, (cudaError_t)e, "realign setup launch");
+        ++launches;
+    }
+    SwArgs A{};
+    A.ref_plane = in.ref_plane;
+    A.alt_plane = in.alt_plane;
+    A.tb = E.d_tb.p;
+    A.edges = E.d_edges.p;
+    A.strip_scratch = E.d_scratch.p;
+    A.slot = E.d_slot.p;
+    A.error = d_err;
+    A.match = in.params->match_value;
+    A.mismatch = in.params->mismatch_penalty;
+    A.open = in.params->gap_open_penalty;
+    A.extend = in.params->gap_extend_penalty;
+    A.strategy = in.strategy;
+    A.indel_edges = (in.strategy == kSwIndel || in.strategy == kSwLeadingIndel) ? 1 : 0;
+    A.shortcut = in.shortcut && (in.strategy == kSwSoftclip || in.strategy == kSwIgnore) ? 1 : 0;
+    int occ[kSwMaxK + 1]{};
+    for (int k = 1; k <= kSwMaxK; ++k) {
+        int b = 0;
+        const int e = sw_forward_occupancy(k, &b);
+        if (e) return cuda_error(ctx, (cudaError_t)e, "occupancy");
+        occ[k] = std::max(b, 1);
+    }
+    size_t ev = 1;
+    std::vector<std::pair<size_t, size_t>> fwd_events;
+    for (size_t c = 0; c < chunks.size(); ++c) {
+        const Chunk &ch = chunks[c];
+        const int64_t cn = ch.p1 - ch.p0;
+        SwArgs a = A;
+        a.pairs = E.d_pairs.p + ch.p0;
+        a.state = d_state + ch.p0;
+        a.offset = d_offset + ch.p0;
+        a.n_ops = d_nops + ch.p0;
+        const size_t e0 = ev++, e1 = ev++;
+        SW_CUDA(cudaEventRecord(E.event(e0), s), "event");
+        for (int k = kSwMaxK; k >= 1; --k) {
+            const int64_t cnt = ch.task_count[k];
+            if (!cnt) continue;
+            const int64_t want = (cnt + 3) / 4;
+            const int grid = (int)std::min<int64_t>(want, (int64_t)occ[k] * ci.sm_count);
+            const int e = launch_sw_forward(a, k, E.d_tasks.p + ch.task_begin[k], (int)cnt,
+                                            d_cursors + c * kCursorsPerChunk + k, grid, s);
+            if (e) return cuda_error(ctx, (cudaError_t)e, "Smith-Waterman forward launch");
+            ++launches;
+        }
+        SW_CUDA(cudaEventRecord(E.event(e1), s), "event");
+        fwd_events.emplace_back(e0, e1);
+        int e = launch_sw_traceback(a, (int)cn, s);
+        if (e) return cuda_error(ctx, (cudaError_t)e, "Smith-Waterman traceback launch");
+        e = launch_sw_compact(a, (int)cn, E.d_starts.p + ch.p0, E.d_counters.p, E.d_ops.p, in.ops_cap, s);
+        if (e) return cuda_error(ctx, (cudaError_t)e, "Smith-Waterman cigar compaction launch");
+        launches += 3;
+    }
+    const size_t ev_end = ev++;
+    SW_CUDA(cudaEventRecord(E.event(ev_end), s), "event");
+    SW_CUDA(cudaMemcpyAsync(E.h_res.p, E.d_res.p, (size_t)n * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
+            "D2H results");
+    SW_CUDA(cudaMemcpyAsync(E.h_starts.p, E.d_starts.p, (size_t)n * sizeof(int64_t), cudaMemcpyDeviceToHost, s),
+            "D2H cigar starts");
+    SW_CUDA(cudaMemcpyAsync(E.h_counters.p, E.d_counters.p, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, s),
+            "D2H counters");
+    if (informative) {
+        informative->resize((size_t)n);
+        SW_CUDA(cudaMemcpyAsync(informative->data(), E.d_inf.p, (size_t)n, cudaMemcpyDeviceToHost, s),
+                "D2H informative flags");
+    }
+    SW_CUDA(cudaStreamSynchronize(s), "Smith-Waterman kernels");
+    E.stats.d2h_bytes = n * (int64_t)(4 * sizeof(int32_t) + sizeof(int64_t)) + 16 + (informative ? n : 0);
+    const int err = (int)(E.h_counters.p[1] & 0xffffffff);
+    if (err == 2) return ctx_fail(ctx, GHMM_ERR_ARG, "cigar_cap too small for the alignments' cigars");
+    if (err) return ctx_fail(ctx, GHMM_ERR_CUDA, "Smith-Waterman traceback overran its buffer");
+    const int64_t total = E.h_counters.p[0];
+    if (total > in.ops_cap) return ctx_fail(ctx, GHMM_ERR_ARG, "cigar_cap too small for the alignments' cigars");
+    SW_CUDA(E.h_ops.reserve((size_t)std::max<int64_t>(total, 1)), "pinned cigar ops");
+    if (total > 0) {
+        SW_CUDA(cudaMemcpyAsync(E.h_ops.p, E.d_ops.p, (size_t)total * sizeof(uint32_t), cudaMemcpyDeviceToHost, s),
+                "D2H cigar ops");
+        SW_CUDA(cudaStreamSynchronize(s), "D2H cigar ops");
+    }
+    E.stats.d2h_bytes += total * (int64_t)sizeof(uint32_t);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, E.event(0), E.event(ev_end));
+    E.stats.ms_device = ms;
+    double fwd = 0;
+    for (auto &fe : fwd_events) {
+        float m = 0;
+        cudaEventElapsedTime(&m, E.event(fe.first), E.event(fe.second));
+        fwd += m;
+    }
+    E.stats.ms_forward = fwd;
+    E.stats.chunks = (int32_t)chunks.size();
+    E.stats.launches = launches;
+    E.stats.n_alignments = n;
+    return GHMM_OK;
+}
+
+int check_params(ghmm_ctx *ctx, const ghmm_sw_params *params, int32_t strategy) {
+    if (!params) return ctx_fail(ctx, GHMM_ERR_ARG, "Smith-Waterman parameters must not be null");
+    if (strategy < GHMM_SW_SOFTCLIP || strategy > GHMM_SW_IGNORE)
+        return ctx_fail(ctx, GHMM_ERR_ARG, "unknown overhang strategy " + std::to_string(strategy));
+    return GHMM_OK;
+}
+
+SwEngine *engine(const CtxInfo &ci) {
+    if (!*ci.sw) *ci.sw = new SwEngine();
+    return *ci.sw;
+}
+
+// results of pairs [0, n) from the engine's host buffers into the caller's arrays
+int deliver(ghmm_ctx *ctx, SwEngine &E, int64_t n, const int32_t *ref_len_of, ghmm_sw_result *res) {
+    const int32_t *state = E.h_res.p, *offset = E.h_res.p + n, *nops = E.h_res.p + 2 * n;
+    const int64_t total = E.h_counters.p[0];
+    int64_t n_short = 0, cells = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        res->alignment_offset[i] = offset[i];
+        res->cigar_start[i] = E.h_starts.p[i];
+        res->cigar_len[i] = nops[i];
+        if (ref_len_of && ref_len_of[i] <= 0) continue;  // not aligned
+        if (state[i] == 1)
+            ++n_short;
+        else if (ref_len_of)
+            cells += (int64_t)ref_len_of[i] * E.h_pairs.p[i].alt_len;
+    }
+    if (total > 0) std::memcpy(res->cigar_ops, E.h_ops.p, (size_t)total * sizeof(uint32_t));
+    res->cigar_total = total;
+    E.stats.n_shortcut = n_short;
+    E.stats.cells = cells;
+    (void)ctx;
+    return GHMM_OK;
+}
+
+int sw_batch(ghmm_ctx *ctx, const CtxInfo &ci, const ghmm_sw_pair *pairs, int64_t n, const ghmm_sw_params *params,
+             int32_t strategy, int32_t flags, ghmm_sw_result *res) {
+    const auto t0 = std::chrono::steady_clock::now();
+    SwEngine &E = *engine(ci);
+    E.stats = ghmm_sw_stats{};
+    for (int64_t i = 0; i < n; ++i) {
+        const ghmm_sw_pair &p = pairs[i];
+        if (!p.ref || !p.alt || p.ref_len <= 0 || p.alt_len <= 0)
+            return ctx_fail(ctx, GHMM_ERR_ARG,
+                            "Non-null, non-empty sequences are required for the Smith-Waterman calculation");
+        if (p.ref_len > GHMM_SW_MAX_LEN || p.alt_len > GHMM_SW_MAX_LEN)
+            return ctx_fail(ctx, GHMM_ERR_ARG, "sequence longer than GHMM_SW_MAX_LEN");
+    }
+    // refs deduplicated by (address, length): a haplotype shared by many reads is copied once
+    std::unordered_map<const uint8_t *, std::pair<int64_t, int32_t>> seen;
+    std::vector<int64_t> ref_off((size_t)n);
+    std::vector<int64_t> uniq;  // pair index of each distinct ref
+    int64_t ref_bytes = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        auto it = seen.find(pairs[i].ref);
+        if (it != seen.end() && it->second.second == pairs[i].ref_len) {
+            ref_off[(size_t)i] = it->second.first;
+            continue;
+        }
+        seen[pairs[i].ref] = {ref_bytes, pairs[i].ref_len};
+        ref_off[(size_t)i] = ref_bytes;
+        uniq.push_back(i);
+        ref_bytes += pairs[i].ref_len;
+    }
+    std::vector<int64_t> alt_off((size_t)n + 1);
+    alt_off[0] = 0;
+    for (int64_t i = 0; i < n; ++i) alt_off[(size_t)i + 1] = alt_off[(size_t)i] + pairs[i].alt_len;
+    const int64_t plane_bytes = ref_bytes + alt_off[(size_t)n];
+    SW_CUDA(cudaSetDevice(ci.device), "cudaSetDevice");
+    SW_CUDA(E.h_planes.reserve((size_t)plane_bytes), "pinned sequences");
+    SW_CUDA(E.d_planes.reserve((size_t)plane_bytes), "device sequences");
+    SW_CUDA(E.h_pairs.reserve((size_t)n), "pinned pairs");
+    uint8_t *hp = E.h_planes.p;
+    parallel_for((int64_t)uniq.size(), ci.threads, [&](int64_t u) {
+        const int64_t i = uniq[(size_t)u];
+        std::memcpy(hp + ref_off[(size_t)i], pairs[i].ref, (size_t)pairs[i].ref_len);
+    });
+    parallel_for(n, ci.threads, [&](int64_t i) {
+        std::memcpy(hp + ref_bytes + alt_off[(size_t)i], pairs[i].alt, (size_t)pairs[i].alt_len);
+        SwPair &P = E.h_pairs.p[i];
+        P = SwPair{};
+        P.ref_off = ref_off[(size_t)i];
+        P.alt_off = alt_off[(size_t)i];
+        P.ref_len = pairs[i].ref_len;
+        P.alt_len = pairs[i].alt_len;
+    });
+    std::vector<int32_t> ref_len((size_t)n);
+    for (int64_t i = 0; i < n; ++i) ref_len[(size_t)i] = pairs[i].ref_len;
+    RunIn in{};
+    in.ref_plane = E.d_planes.p;
+    in.alt_plane = E.d_planes.p + ref_bytes;
+    in.params = params;
+    in.strategy = strategy;
+    in.shortcut = (flags & GHMM_SW_SUBSTRING_SHORTCUT) ? 1 : 0;
+    in.n = n;
+    in.ref_bound = ref_len.data();
+    in.ops_cap = res->cigar_cap;
+    int rc = run(ctx, ci, E, in, plane_bytes, nullptr);
+    if (rc) return rc;
+    rc = deliver(ctx, E, n, ref_len.data(), res);
+    E.stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+bool valid_result(const ghmm_sw_result *r) {
+    return r && r->alignment_offset && r->cigar_start && r->cigar_len && (r->cigar_ops || r->cigar_cap == 0) &&
+           r->cigar_cap >= 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t ghmm_sw_cigar_bound(const ghmm_sw_pair *pairs, int32_t n_pairs) {
+    if (!pairs || n_pairs <= 0) return 0;
+    int64_t b = 0;
+    for (int32_t i = 0; i < n_pairs; ++i) b += 2 * (int64_t)std::max(pairs[i].alt_len, 0) + 4;
+    return b;
+}
+
+int ghmm_sw_align_batch(ghmm_ctx *ctx, const ghmm_sw_pair *pairs, int32_t n_pairs, const ghmm_sw_params *params,
+                        int32_t strategy, int32_t flags, ghmm_sw_result *result) {
+    CtxInfo ci;
+    if (ctx_info(ctx, &ci)) return GHMM_ERR_STATE;
+    if (n_pairs < 0 || (n_pairs > 0 && (!pairs || !valid_result(result))))
+        return ctx_fail(ctx, GHMM_ERR_ARG, "NULL argument");
+    int rc = check_params(ctx, params, strategy);
+    if (rc) return rc;
+    if (n_pairs == 0) {
+        if (result) result->cigar_total = 0;
+        return GHMM_OK;
+    }
+    return sw_batch(ctx, ci, pairs, n_pairs, params, strategy, flags, result);
+}
+
+int ghmm_sw_align(ghmm_ctx *ctx, const uint8_t *ref, int32_t ref_len, const uint8_t *alt, int32_t alt_len,
+                  const ghmm_sw_params *params, int32_t strategy, char *cigar, int32_t cigar_cap,
+                  int32_t *alignment_offset) {
+    CtxInfo ci;
+    if (ctx_info(ctx, &ci)) return GHMM_ERR_STATE;
+    if (!cigar || cigar_cap <= 0 || !alignment_offset) return ctx_fail(ctx, GHMM_ERR_ARG, "NULL argument");
+    int rc = check_params(ctx, params, strategy);
+    if (rc) return rc;
+    if (!ref || !alt || ref_len <= 0 || alt_len <= 0)
+        return ctx_fail(ctx, GHMM_ERR_ARG, "Non-null, non-empty sequences are required for the Smith-Waterman calculation");
+    ghmm_sw_pair p{ref, alt, ref_len, alt_len};
+    std::vector<uint32_t> ops((size_t)2 * alt_len + 4);
+    int32_t off = 0, len = 0;
+    int64_t start = 0;
+    ghmm_sw_result r{&off, &start, &len, ops.data(), (int64_t)ops.size(), 0};
+    rc = sw_batch(ctx, ci, &p, 1, params, strategy, 0, &r);
+    if (rc) return rc;
+    // TextCigarCodec.encode: length then operator per element, "*" for none
+    static const char kOps[] = "MIDNSHP=X";
+    std::string text;
+    for (int32_t q = 0; q < len; ++q) {
+        const uint32_t o = ops[(size_t)(start + q)];
+        text += std::to_string(o >> 4);
+        text += kOps[o & 15u];
+    }
+    if (text.empty()) text = "*";
+    if ((int64_t)text.size() + 1 > cigar_cap) return ctx_fail(ctx, GHMM_ERR_ARG, "cigar buffer too small");
+    std::memcpy(cigar, text.c_str(), text.size() + 1);
+    *alignment_offset = off;
+    return GHMM_OK;
+}
+
+int ghmm_batch_realign(ghmm_ctx *ctx, ghmm_batch *batch, const double *hap_priority, const ghmm_sw_params *params,
+                       int32_t *best_hap, uint8_t *informative, ghmm_sw_result *result) {
+    CtxInfo ci;
+    if (ctx_info(ctx, &ci)) return GHMM_ERR_STATE;
+    if (!batch || !params) return ctx_fail(ctx, GHMM_ERR_ARG, "NULL argument");
+    BatchInfo bi;
+    batch_info(batch, &bi);
+    if (!bi.has_results) return ctx_fail(ctx, GHMM_ERR_STATE, "run a forward on the batch first");
+    const int64_t n = bi.n_reads;
+    if (n > 0 && (!best_hap || !informative || !valid_result(result)))
+        return ctx_fail(ctx, GHMM_ERR_ARG, "NULL argument");
+    if (n == 0) {
+        if (result) result->cigar_total = 0;
+        return GHMM_OK;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    SwEngine &E = *engine(ci);
+    E.stats = ghmm_sw_stats{};
+    SW_CUDA(cudaSetDevice(ci.device), "cudaSetDevice");
+    const int64_t NR = n, NH = bi.n_haps, G = bi.n_regions;
+    const int64_t *read_off = bi.h_off, *hap_off = read_off + NR + 1, *rro = hap_off + NH + 1, *rho = rro + G + 1;
+    SW_CUDA(E.h_pairs.reserve((size_t)n), "pinned pairs");
+    // buffers of each read sized by the longest haplotype of its region; reads of regions without haplotypes
+    // get no alignment (the setup kernel marks them, the forward skips them through an empty task list)
+    std::vector<int32_t> bound((size_t)n);
+    for (int64_t g = 0; g < G; ++g) {
+        int32_t hmax = 0;
+        for (int64_t h = rho[g]; h < rho[g + 1]; ++h) hmax = std::max<int32_t>(hmax, (int32_t)(hap_off[h + 1] - hap_off[h]));
+        for (int64_t r = rro[g]; r < rro[g + 1]; ++r) {
+            SwPair &P = E.h_pairs.p[r];
+            P = SwPair{};
+            P.alt_off = read_off[r];
+            P.alt_len = (int32_t)(read_off[r + 1] - read_off[r]);
+            P.ref_len = 0;
+            bound[(size_t)r] = hmax;
+        }
+    }
+    for (int64_t r = 0; r < n; ++r)
+        if (E.h_pairs.p[r].alt_len <= 0)
+            return ctx_fail(ctx, GHMM_ERR_ARG,
+                            "Non-null, non-empty sequences are required for the Smith-Waterman calculation");
+    RunIn in{};
+    in.ref_plane = bi.dev->hap_bases;
+    in.alt_plane = bi.dev->bases;
+    in.params = params;
+    in.strategy = kSwSoftclip;
+    in.shortcut = 1;
+    in.n = n;
+    in.ref_bound = bound.data();
+    in.ops_cap = result->cigar_cap;
+    in.batch = &bi;
+    in.priority = hap_priority;
+    std::vector<uint8_t> inf;
+    int rc = run(ctx, ci, E, in, 0, &inf);
+    if (rc) return rc;
+    const int32_t *best = E.h_res.p + 3 * n;
+    std::vector<int32_t> ref_len((size_t)n);
+    // the chosen haplotype's length per read, for the cell count
+    for (int64_t r = 0, g = 0; r < n; ++r) {
+        best_hap[r] = best[r];
+        informative[r] = inf[(size_t)r];
+        while (rro[g + 1] <= r) ++g;
+        const int64_t h = rho[g] + best[r];
+        ref_len[(size_t)r] = best[r] < 0 ? 0 : (int32_t)(hap_off[h + 1] - hap_off[h]);
+    }
+    rc = deliver(ctx, E, n, ref_len.data(), result);
+    E.stats.d2h_bytes += n * (int64_t)sizeof(int32_t);
+    E.stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int ghmm_sw_set_traceback_budget(ghmm_ctx *ctx, int64_t bytes) {
+    CtxInfo ci;
+    if (ctx_info(ctx, &ci)) return GHMM_ERR_STATE;
+    engine(ci)->tb_budget_words = std::max<int64_t>(bytes, int64_t(1) << 20) / 4;
+    return GHMM_OK;
+}
+
+int ghmm_sw_measure_peak(ghmm_ctx *ctx, double *int32_tops) {
+    CtxInfo ci;
+    if (ctx_info(ctx, &ci)) return GHMM_ERR_STATE;
+    if (!int32_tops) return ctx_fail(ctx, GHMM_ERR_ARG, "NULL argument");
+    SW_CUDA(cudaSetDevice(ci.device), "cudaSetDevice");
+    const int e = measure_int32_peak(ci.sm_count, int32_tops, ci.stream);
+    if (e) return cuda_error(ctx, (cudaError_t)e, "int32 peak loop");
+    return GHMM_OK;
+}
+
+int ghmm_sw_last_stats(ghmm_ctx *ctx, ghmm_sw_stats *stats) {
+    CtxInfo ci;
+    if (ctx_info(ctx, &ci)) return GHMM_ERR_STATE;
+    if (!stats) return ctx_fail(ctx, GHMM_ERR_ARG, "NULL argument");
+    *stats = *ci.sw ? (*ci.sw)->stats : ghmm_sw_stats{};
+    return GHMM_OK;
+}
+
+}  // extern "C"

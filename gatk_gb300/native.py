@@ -1,4 +1,4 @@
-"""ctypes binding of libghmm.so (include/ghmm.h, ghmm_synth.h, ghmm_calib.h).
+"""ctypes binding of libghmm.so (include/ghmm.h, ghmm_sw.h, ghmm_synth.h, ghmm_calib.h).
 
 The library is the product: there is no Python or CPU fallback.  ``lib()`` builds it in-tree if it
 is missing and raises if that fails; compute calls raise ``GhmmError`` with the library's message
@@ -146,6 +146,36 @@ class SynthArrays(ctypes.Structure):
                 ("hap_bases", _u8p)]
 
 
+# Smith-Waterman (include/ghmm_sw.h)
+SW_SOFTCLIP, SW_INDEL, SW_LEADING_INDEL, SW_IGNORE = 0, 1, 2, 3
+SW_SUBSTRING_SHORTCUT = 1
+CIGAR_M, CIGAR_I, CIGAR_D, CIGAR_S = 0, 1, 2, 4
+SW_MAX_LEN = 1 << 20
+
+
+class SwParams(ctypes.Structure):
+    _fields_ = [("match_value", ctypes.c_int32), ("mismatch_penalty", ctypes.c_int32),
+                ("gap_open_penalty", ctypes.c_int32), ("gap_extend_penalty", ctypes.c_int32)]
+
+
+class SwPair(ctypes.Structure):
+    _fields_ = [("ref", ctypes.c_void_p), ("alt", ctypes.c_void_p), ("ref_len", ctypes.c_int32),
+                ("alt_len", ctypes.c_int32)]
+
+
+class SwResult(ctypes.Structure):
+    _fields_ = [("alignment_offset", ctypes.c_void_p), ("cigar_start", ctypes.c_void_p),
+                ("cigar_len", ctypes.c_void_p), ("cigar_ops", ctypes.c_void_p), ("cigar_cap", ctypes.c_int64),
+                ("cigar_total", ctypes.c_int64)]
+
+
+class SwStats(ctypes.Structure):
+    _fields_ = [("n_alignments", ctypes.c_int64), ("n_shortcut", ctypes.c_int64), ("cells", ctypes.c_int64),
+                ("chunks", ctypes.c_int32), ("launches", ctypes.c_int32), ("ms_device", ctypes.c_double),
+                ("ms_forward", ctypes.c_double), ("ms_total", ctypes.c_double), ("h2d_bytes", ctypes.c_int64),
+                ("d2h_bytes", ctypes.c_int64)]
+
+
 # Every exported symbol and its signature (restype, argtypes).  The tests check that the library
 # exports exactly the functions the public headers declare.
 _SIGS = {
@@ -200,6 +230,17 @@ _SIGS = {
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "ghmm_forward_pairs_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(DevPairs), ctypes.c_void_p,
                                                   ctypes.c_void_p]),
+    "ghmm_sw_align": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+                                     ctypes.POINTER(SwParams), ctypes.c_int32, ctypes.c_char_p, ctypes.c_int32, _i32p]),
+    "ghmm_sw_cigar_bound": (ctypes.c_int64, [ctypes.POINTER(SwPair), ctypes.c_int32]),
+    "ghmm_sw_align_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SwPair), ctypes.c_int32,
+                                           ctypes.POINTER(SwParams), ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.POINTER(SwResult)]),
+    "ghmm_batch_realign": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(SwParams),
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(SwResult)]),
+    "ghmm_sw_last_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SwStats)]),
+    "ghmm_sw_set_traceback_budget": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
+    "ghmm_sw_measure_peak": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
 }
 
 _lib = None

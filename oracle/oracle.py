@@ -1,12 +1,12 @@
-"""ctypes binding of the FP64 CPU oracle (oracle/pairhmm_oracle.c, oracle/oracle_grad.c).
+"""ctypes binding of the CPU oracle (oracle/pairhmm_oracle.c, oracle_grad.c, pdhmm_oracle.c, sw_oracle.c).
 
 TEST INFRASTRUCTURE ONLY.  Imported by tests/, by ``__graft_entry__.smoke()`` as the
 checker, and by the cpu_baseline / ``--impl reference`` leg of bench.py.  The product
 package (gatk_gb300) never imports this module.
 
 The C sources restate GATK's LoglessPairHMM / Log10PairHMM / PairHMMModel /
-QualityUtils / MathUtils.JacobianLogTable; the file:line citations are in their
-headers.
+QualityUtils / MathUtils.JacobianLogTable, LoglessPDPairHMM and SmithWatermanJavaAligner;
+the file:line citations are in their headers.
 """
 from __future__ import annotations
 
@@ -27,7 +27,8 @@ _f64p = ctypes.POINTER(ctypes.c_double)
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, OpenMP, -ffp-contract=off)."""
-    srcs = [os.path.join(_HERE, f) for f in ("pairhmm_oracle.c", "oracle_grad.c", "pdhmm_oracle.c", "Makefile")]
+    srcs = [os.path.join(_HERE, f) for f in ("pairhmm_oracle.c", "oracle_grad.c", "pdhmm_oracle.c", "sw_oracle.c",
+                                            "Makefile")]
     if not force and os.path.exists(_LIB_PATH):
         if os.path.getmtime(_LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
             return _LIB_PATH
@@ -82,6 +83,14 @@ def lib():
         L.oracle_pd_compute_pairs.restype = ctypes.c_int64
         L.oracle_pd_compute_pairs.argtypes = [ctypes.c_int64, _i64p, _i64p, _i64p, _u8p, _u8p, _u8p, _u8p, _u8p,
                                               _i64p, _u8p, _u8p, _f64p, ctypes.c_int]
+        _i32p = ctypes.POINTER(ctypes.c_int32)
+        _u32p = ctypes.POINTER(ctypes.c_uint32)
+        L.sw_oracle_align.restype = ctypes.c_int
+        L.sw_oracle_align.argtypes = [_u8p, ctypes.c_int, _u8p, ctypes.c_int, _i32p, ctypes.c_int, ctypes.c_int, _u32p,
+                                      ctypes.c_int, _i32p, _i32p]
+        L.sw_oracle_align_batch.restype = ctypes.c_int
+        L.sw_oracle_align_batch.argtypes = [ctypes.c_int64, _u8p, _i64p, _i32p, _u8p, _i64p, _i32p, _i32p, ctypes.c_int,
+                                            ctypes.c_int, _u32p, _i64p, _i32p, _i32p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -189,3 +198,49 @@ def pd_compute_workload(wl, hap_pd: np.ndarray, threads: int = 0) -> np.ndarray:
     if bad:
         raise ValueError(f"{bad} pairs hit 'Found unexpected base in alt alleles'")
     return out
+
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+
+
+def sw_align(ref, alt, params, strategy: int, shortcut: bool = True):
+    """Smith-Waterman of alt against ref (sw_oracle.c): (BAM-encoded cigar ops as a list, alignment offset)."""
+    r, a = _u8(ref), _u8(alt)
+    prm = np.ascontiguousarray(params, dtype=np.int32)
+    ops = np.zeros(2 * len(a) + 4, dtype=np.uint32)
+    n_ops, off = ctypes.c_int32(0), ctypes.c_int32(0)
+    st = lib().sw_oracle_align(_p(r, _u8p), len(r), _p(a, _u8p), len(a), _p(prm, _i32p), strategy, int(shortcut),
+                               _p(ops, _u32p), len(ops), ctypes.byref(n_ops), ctypes.byref(off))
+    if st != 0:
+        raise ValueError(f"sw_oracle_align status {st}")
+    return [int(x) for x in ops[:n_ops.value]], off.value
+
+
+def sw_align_pairs(ref_plane, ref_off, ref_len, alt_plane, alt_off, alt_len, params, strategy: int,
+                   shortcut: bool = True, threads: int = 0):
+    """Many alignments over all host threads: (ops, ops_start, n_ops, offset); pair p's BAM-encoded ops are
+    ops[ops_start[p]:ops_start[p] + n_ops[p]]."""
+    n = len(ref_off)
+    ref_plane, alt_plane = _u8(ref_plane), _u8(alt_plane)
+    ref_off = np.ascontiguousarray(ref_off, dtype=np.int64)
+    alt_off = np.ascontiguousarray(alt_off, dtype=np.int64)
+    ref_len = np.ascontiguousarray(ref_len, dtype=np.int32)
+    alt_len = np.ascontiguousarray(alt_len, dtype=np.int32)
+    prm = np.ascontiguousarray(params, dtype=np.int32)
+    cap = 2 * alt_len.astype(np.int64) + 4
+    start = np.zeros(n, dtype=np.int64)
+    if n > 1:
+        start[1:] = np.cumsum(cap)[:-1]
+    ops = np.zeros(int(cap.sum()) if n else 1, dtype=np.uint32)
+    n_ops = np.zeros(n, dtype=np.int32)
+    off = np.zeros(n, dtype=np.int32)
+    if n == 0:
+        return ops, start, n_ops, off
+    st = lib().sw_oracle_align_batch(n, _p(ref_plane, _u8p), _p(ref_off, _i64p), _p(ref_len, _i32p),
+                                     _p(alt_plane, _u8p), _p(alt_off, _i64p), _p(alt_len, _i32p), _p(prm, _i32p),
+                                     strategy, int(shortcut), _p(ops, _u32p), _p(start, _i64p), _p(n_ops, _i32p),
+                                     _p(off, _i32p), threads)
+    if st != 0:
+        raise ValueError(f"sw_oracle_align_batch status {st}")
+    return ops, start, n_ops, off

@@ -1,11 +1,13 @@
 """CPU restatement of the step after the likelihoods: normalisation and poorly-modelled-read filtering.
 
-TEST INFRASTRUCTURE ONLY (the oracle for ghmm_batch_postprocess).  Plain numpy/Python loops over a
+TEST INFRASTRUCTURE ONLY (the oracle for ghmm_batch_postprocess and for the haplotype ghmm_batch_realign
+picks).  Plain numpy/Python loops over a
 workload's read-major blocks, following (paths inside the GATK repository):
 
   AlleleLikelihoods.normalizeLikelihoods / normalizeLikelihoodsPerEvidence
       src/main/java/org/broadinstitute/hellbender/utils/genotyper/AlleleLikelihoods.java:416-458
-  AlleleLikelihoods.searchBestAllele                                                  :505-540
+  AlleleLikelihoods.searchBestAllele                                                  :505-560
+  AlleleLikelihoods.bestAllelesBreakingTies, BestAllele.isInformative                 :1062-1075, 1269-1282
   AlleleLikelihoods.maximumLikelihoodOverAllAlleles                                   :1198-1208
   AlleleLikelihoods.filterPoorlyModeledEvidence                                       :1351-1376
   ReadLikelihoodCalculationEngine.log10MinTrueLikelihood                              tools/walkers/haplotypecaller/
@@ -51,6 +53,41 @@ def best_allele(values, reference: int, can_be_reference: bool) -> float:
         if values[a] > best:
             best = values[a]
     return best
+
+
+LOG_10_INFORMATIVE_THRESHOLD = 0.2  # AlleleLikelihoods.java:38
+
+
+def best_allele_breaking_ties(values, priorities=None):
+    """searchBestAllele(sample, read, canBeReference = true, priorities) (AlleleLikelihoods.java:505-560) as
+    bestAllelesBreakingTies calls it (:1062-1075): (best index, BestAllele.isInformative() (:1269-1282))."""
+    n = len(values)
+    if n == 0:
+        return -1, False
+    best, second = 0, 0
+    best_l, second_l = values[0], -math.inf
+    for a in range(1, n):
+        c = values[a]
+        if c > best_l:
+            second, best, second_l, best_l = best, a, best_l, c
+        elif c > second_l:
+            second, second_l = a, c
+    thr = LOG_10_INFORMATIVE_THRESHOLD
+    if priorities is not None and best_l - second_l < thr:
+        best_p, second_p = priorities[best], priorities[second]
+        for a in range(n):
+            c = values[a]
+            if a == best or best_l - c > thr:
+                continue
+            cp = priorities[a]
+            if cp > best_p:
+                second, best, second_p, best_p = best, a, best_p, cp
+            elif cp > second_p:
+                second, second_p = a, cp
+    best_l = values[best]
+    second_l = values[second] if second != best else -math.inf
+    confidence = 0.0 if best_l == second_l else best_l - second_l
+    return best, confidence > thr
 
 
 def min_true_likelihood(read_len: int, rate: float, cap: bool) -> float:

@@ -44,6 +44,16 @@ def test_header_constants_match_the_bindings():
     assert int(defs["GHMM_MODE_PLAIN_FP64"]) == native.MODE_PLAIN_FP64
     assert int(defs["GHMM_MODE_PD"]) == native.MODE_PD
     assert float(defs["GHMM_FP64_RESCALED_FLOOR"]) == native.FP64_RESCALED_FLOOR
+    sw = open(os.path.join(ROOT, "include", "ghmm_sw.h")).read()
+    swd = dict(re.findall(r"#define (GHMM_\w+) \(?([-0-9]+)", sw))
+    assert int(swd["GHMM_SW_SOFTCLIP"]) == native.SW_SOFTCLIP
+    assert int(swd["GHMM_SW_INDEL"]) == native.SW_INDEL
+    assert int(swd["GHMM_SW_LEADING_INDEL"]) == native.SW_LEADING_INDEL
+    assert int(swd["GHMM_SW_IGNORE"]) == native.SW_IGNORE
+    assert int(swd["GHMM_SW_SUBSTRING_SHORTCUT"]) == native.SW_SUBSTRING_SHORTCUT
+    for op in "MIDS":
+        assert int(swd[f"GHMM_CIGAR_{op}"]) == getattr(native, f"CIGAR_{op}")
+    assert "#define GHMM_SW_MAX_LEN (1 << 20)" in sw and native.SW_MAX_LEN == 1 << 20
 
 
 def test_struct_layouts_match_the_header(tmp_path):
@@ -59,9 +69,12 @@ def test_struct_layouts_match_the_header(tmp_path):
                "ghmm_tuning": native.Tuning, "ghmm_queue_info": native.QueueInfo,
                "ghmm_dev_pairs": native.DevPairs, "ghmm_calib_batch": native.CalibBatch,
                "ghmm_postprocess": native.Postprocess, "ghmm_pd_hap": native.PdHap, "ghmm_pd_region": native.PdRegion,
-               "ghmm_raw_read": native.RawRead, "ghmm_raw_region": native.RawRegion, "ghmm_read_prep": native.ReadPrep}
+               "ghmm_raw_read": native.RawRead, "ghmm_raw_region": native.RawRegion, "ghmm_read_prep": native.ReadPrep,
+               "ghmm_sw_params": native.SwParams, "ghmm_sw_pair": native.SwPair, "ghmm_sw_result": native.SwResult,
+               "ghmm_sw_stats": native.SwStats}
     src = tmp_path / "sizes.c"
-    src.write_text('#include <stdio.h>\n#include "ghmm.h"\n#include "ghmm_calib.h"\nint main(void) {\n' +
+    src.write_text('#include <stdio.h>\n#include "ghmm.h"\n#include "ghmm_calib.h"\n#include "ghmm_sw.h"\n'
+                   'int main(void) {\n' +
                    "".join(f'printf("{n} %zu\\n", sizeof({n}));\n' for n in structs) + "return 0;\n}\n")
     exe = tmp_path / "sizes"
     subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
