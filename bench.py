@@ -721,13 +721,15 @@ def run_sw(args):
                    "substring_shortcut": int(st["n_shortcut"]), "cells": int(cells), "chunks": int(st["chunks"]),
                    "parameters": "ALIGNMENT_TO_BEST_HAPLOTYPE_SW_PARAMETERS (10, -15, -30, -5), SOFTCLIP"},
         "realign_call_ms": dt_call * 1e3,
+        "realign_host_ms": statistics.mean(x["ms_host"] for x in sts),
         "alignments_per_s": wl.n_reads / (dt_call),
         "roofline": {"bound": "int32_alu", "achieved": achieved, "peak": peak, "unit": "Tops/s",
                      "frac": achieved / peak, "ops_per_cell": SW_OPS_PER_CELL, "kernel": "sw_forward_kernel<K>",
                      "ms_forward": ms_fwd, "peak_source": "measured in this run: max.s32 register loop over all SMs"},
         "e2e": {"value": st2["cells"] / dt_e2e / 1e9, "unit": "GCUPS", "ms_per_step": dt_e2e * 1e3,
                 "h2d_bytes_per_step": int(st2["h2d_bytes"]), "d2h_bytes_per_step": int(st2["d2h_bytes"]),
-                "api": "ghmm_sw_align_batch (host pairs, SOFTCLIP, substring shortcut)", "matches_realign": bool(same)},
+                "api": "ghmm_sw_align_batch (host pairs, SOFTCLIP, substring shortcut)", "matches_realign": bool(same),
+                "host_ms": st2["ms_host"], "device_ms": st2["ms_device"]},
         "gpu_launches": int(st["launches"]),
         "clocks": clk,
         "cpu_baseline": {"value": float(lens[:n_cpu].sum()) / cpu_dt / 1e9, "unit": "GCUPS", "cores": os.cpu_count(),

@@ -136,12 +136,15 @@ int launch_calib(const DevTables &TB, const ghmm_calib_batch &in, int k, bool ba
 constexpr int kSwSoftclip = 0, kSwIndel = 1, kSwLeadingIndel = 2, kSwIgnore = 3;
 constexpr uint32_t kSwOpM = 0, kSwOpI = 1, kSwOpD = 2, kSwOpS = 4;
 constexpr int kSwMaxK = 8;  // alt columns per lane; longer alts run in strips of 32 * 8 columns
+// Row stride of the last-column lane's scores in the edge array: K rounded up to whole int4s.
+#define kSwRowStride(k) ((((k) + 3) / 4) * 4)
 
 // One alignment: alt against ref.  Offsets index the ref / alt planes and the chunk's buffers.
 struct SwPair {
     int64_t ref_off, alt_off;
     int64_t tb_off;       // first traceback word: strips x (ref_len + 31) steps x 32 lanes
-    int64_t edge_off;     // ref_len last-column scores, then alt_len bottom-row scores
+    int64_t edge_off;     // ref_len rows of the last-column lane's kSwRowStride(k) scores, then alt_len bottom-row
+                          // scores (a multiple of 4 ints, so the rows are int4-aligned)
     int64_t slot_off;     // 2 * alt_len + 4 cigar ops, written in reverse by the traceback
     int64_t scratch_off;  // strip boundary (score, horizontal gap) per ref row 0..ref_len, multi-strip alts only
     int32_t ref_len, alt_len;
@@ -161,6 +164,7 @@ struct SwArgs {
     int *error;           // set when a traceback overruns its slot (cannot happen for valid input)
     int match, mismatch, open, extend;
     int strategy, indel_edges, shortcut;
+    int clamp;            // apply MATRIX_MIN_CUTOFF (0 when the scores provably never reach it)
 };
 int launch_sw_forward(const SwArgs &a, int k, const int32_t *tasks, int n_tasks, int *cursor, int grid,
                       cudaStream_t s);

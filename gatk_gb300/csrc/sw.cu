@@ -32,6 +32,7 @@ constexpr int kSwCutoff = -100000000;       // MATRIX_MIN_CUTOFF (int) -1.0e8
 constexpr int kSwLowInit = INT32_MIN / 2;   // lowInitValue = Integer.MIN_VALUE / 2
 
 __device__ __forceinline__ int wadd(int a, int b) { return (int)((unsigned)a + (unsigned)b); }
+__device__ __forceinline__ int wsub(int a, int b) { return (int)((unsigned)a - (unsigned)b); }
 
 // top row / left column of the score matrix: 0, or gap open + (k - 1) gap extends for INDEL and LEADING_INDEL
 __device__ __forceinline__ int edge_init(const SwArgs &A, int64_t k) {
@@ -56,98 +57,157 @@ __device__ int warp_last_index_of(const uint8_t *ref, int n, const uint8_t *alt,
     return -1;
 }
 
+// bits |= mask when a > b (a >= b): one compare and one predicated OR
+__device__ __forceinline__ void or_if_gt(uint32_t &bits, int a, int b, uint32_t mask) {
+    asm("{\n\t.reg .pred p;\n\tsetp.gt.s32 p, %1, %2;\n\t@p or.b32 %0, %0, %3;\n\t}"
+        : "+r"(bits)
+        : "r"(a), "r"(b), "r"(mask));
+}
+__device__ __forceinline__ void or_if_ge(uint32_t &bits, int a, int b, uint32_t mask) {
+    asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %1, %2;\n\t@p or.b32 %0, %0, %3;\n\t}"
+        : "+r"(bits)
+        : "r"(a), "r"(b), "r"(mask));
+}
+
+// What one lane needs across the steps of a strip.
+struct StripCtx {
+    const uint8_t *ref;
+    uint32_t *tb;          // this lane's traceback word of step 0 (words of a step are 32 apart)
+    int *lastrow;          // the lane holding the alt's last column: its K scores + open per row (kSwRowStride ints)
+    const int2 *strip_in;  // lane 0 after the first strip: (score, horizontal gap) of the previous strip's last column
+    int2 *strip_out;       // lane 31 before the last strip
+    int n, open, ext;
+    int match_o, mismatch_o;  // match / mismatch minus the gap open penalty (scores are carried as H + open)
+    bool inject;           // lane 0 of the first strip: the matrix's left edge
+    bool indel_edges;
+    bool owns_last;
+};
+
 template <int K>
-__device__ __forceinline__ void sw_strip(const SwArgs &A, const SwPair &P, int p, int s, int nstrips) {
+struct LaneState {
+    uint8_t b[K];   // alt bases of the lane's columns
+    int hup[K];     // H[i-1][j] + open before a step, H[i][j] + open after it
+    int bv[K];      // best vertical gap of each column
+    int hdiag;      // H[i-1][first column - 1] + open
+    int send_h, send_b;
+    uint8_t a_next;
+};
+
+// One anti-diagonal step of one lane: row i = t - lane + 1 over the lane's K columns.  CHECK: some lanes of the
+// warp are outside the matrix this step (the first and last 31 steps of a strip).  Scores travel as H + open: the
+// one add per cell then serves as the next row's vertical gap opening and the next column's horizontal one, and
+// the diagonal adds the score minus open.  Every sum is the Java one modulo 2^32.
+template <int K, bool CLAMP, bool CHECK>
+__device__ __forceinline__ void sw_step(const StripCtx &C, LaneState<K> &L, int t, int lane) {
+    const int i = t - lane + 1;
+    const bool active = !CHECK || (i >= 1 && i <= C.n);
+    const uint8_t a = L.a_next;
+    L.a_next = C.ref[min(max(i, 0), C.n - 1)];  // the next step's row is i + 1, whose base is ref[i]
+    int h_left = __shfl_up_sync(0xffffffffu, L.send_h, 1);
+    int bh = __shfl_up_sync(0xffffffffu, L.send_b, 1);
+    if (lane == 0) {
+        if (C.inject) {
+            h_left = wadd(C.indel_edges && i > 0 ? (int)((unsigned)C.open + (unsigned)(i - 1) * (unsigned)C.ext) : 0,
+                          C.open);
+            bh = kSwLowInit;
+        } else if (active) {
+            const int2 v = C.strip_in[i];
+            h_left = v.x;
+            bh = v.y;
+        }
+    }
+    if (!active) return;
+    uint32_t bits = 0;
+    int hd = L.hdiag;
+    int hl = h_left;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int diag = wadd(hd, a == L.b[k] ? C.match_o : C.mismatch_o);
+        const int bvk = wadd(L.bv[k], C.ext), pv = L.hup[k];
+        const int v = max(bvk, pv);
+        const int bhk = wadd(bh, C.ext), ph = hl;
+        const int h = max(bhk, ph);
+        const int g = max(h, v);
+        int hn = max(diag, g);
+        if (CLAMP) hn = max(hn, kSwCutoff);
+        or_if_gt(bits, g, diag, 1u << (4 * k));  // not diagonal: diag < max(right, down)
+        or_if_ge(bits, h, v, 2u << (4 * k));     // right >= down
+        or_if_gt(bits, pv, bvk, 4u << (4 * k));  // vertical gap opened here
+        or_if_gt(bits, ph, bhk, 8u << (4 * k));  // horizontal gap opened here
+        const int hno = wadd(hn, C.open);
+        L.bv[k] = v;
+        bh = h;
+        hd = L.hup[k];
+        L.hup[k] = hno;
+        hl = hno;
+    }
+    C.tb[(int64_t)t * 32] = bits;
+    if (C.owns_last) {
+        int4 *row = reinterpret_cast<int4 *>(C.lastrow + (int64_t)(i - 1) * kSwRowStride(K));
+#pragma unroll
+        for (int q = 0; q < K; q += 4)
+            row[q / 4] = make_int4(L.hup[q], q + 1 < K ? L.hup[q + 1 < K ? q + 1 : 0] : 0,
+                                   q + 2 < K ? L.hup[q + 2 < K ? q + 2 : 0] : 0,
+                                   q + 3 < K ? L.hup[q + 3 < K ? q + 3 : 0] : 0);
+    }
+    if (C.strip_out && lane == 31) C.strip_out[i] = make_int2(hl, bh);
+    L.send_h = hl;
+    L.send_b = bh;
+    L.hdiag = h_left;
+}
+
+template <int K, bool CLAMP>
+__device__ __forceinline__ void sw_strip(const SwArgs &A, const SwPair &P, int s, int nstrips) {
     const int lane = threadIdx.x & 31;
     const int n = P.ref_len, m = P.alt_len;
     const int col0 = s * 32 * K;               // alt columns of this strip: col0+1 .. col0+32K (1-based)
     const int jbase = col0 + lane * K;         // this lane's columns: jbase+1 .. jbase+K
-    const uint8_t *ref = A.ref_plane + P.ref_off;
     const uint8_t *alt = A.alt_plane + P.alt_off;
-    const int match = A.match, mismatch = A.mismatch, open = A.open, ext = A.extend;
     const bool last_strip = s == nstrips - 1;
-    // which of this lane's columns is the alt's last one (the end-cell scan reads that column)
-    const int km = (m - 1) - jbase;            // in [0, K) on the owning lane of the last strip
-    const bool owns_last = last_strip && km >= 0 && km < K;
-
-    uint8_t b[K];
-    int hup[K], bv[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const int j = jbase + k + 1;
-        b[k] = j <= m ? alt[j - 1] : 0;
-        hup[k] = edge_init(A, j);
-        bv[k] = kSwLowInit;
-    }
-    int hdiag = edge_init(A, jbase);           // H[i-1][jbase] for the lane's first active row
+    StripCtx C;
+    C.ref = A.ref_plane + P.ref_off;
+    C.n = n;
+    C.open = A.open;
+    C.ext = A.extend;
+    C.match_o = wsub(A.match, A.open);
+    C.mismatch_o = wsub(A.mismatch, A.open);
+    C.inject = s == 0;
+    C.indel_edges = A.indel_edges != 0;
+    const int km = (m - 1) - jbase;            // the alt's last column, on its lane in the last strip
+    C.owns_last = last_strip && km >= 0 && km < K;
     const int64_t steps = (int64_t)n + 31;
-    uint32_t *tb = A.tb + P.tb_off + (int64_t)s * steps * 32 + lane;
-    int *lastcol = A.edges + P.edge_off;       // H[i][m] at lastcol[i-1]
-    int2 *strip_in = s > 0 ? A.strip_scratch + P.scratch_off : nullptr;
-    int2 *strip_out = !last_strip ? A.strip_scratch + P.scratch_off : nullptr;
-    int send_h = 0, send_b = kSwLowInit;
-    uint8_t a_next = ref[min(max(0 - lane, 0), n - 1)];
-    for (int64_t t = 0; t < steps; ++t) {
-        const int i = (int)t - lane + 1;       // this lane's row this step (1-based)
-        const bool active = i >= 1 && i <= n;
-        const uint8_t a = a_next;
-        a_next = ref[min(max(i, 0), n - 1)];   // the next step's row is i + 1, whose ref base is ref[i]
-        int h_left = __shfl_up_sync(0xffffffffu, send_h, 1);
-        int bh = __shfl_up_sync(0xffffffffu, send_b, 1);
-        if (lane == 0) {
-            if (s == 0) {
-                h_left = edge_init(A, i);
-                bh = kSwLowInit;
-            } else if (active) {
-                const int2 v = strip_in[i];
-                h_left = v.x;
-                bh = v.y;
-            }
-        }
-        if (active) {
-            uint32_t bits = 0;
-            int hd = hdiag;
-            int hl = h_left;
-            int hm = 0;
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                const int diag = wadd(hd, a == b[k] ? match : mismatch);
-                bool ext_v, ext_h, right_ge_down, diag_ge;
-                const int v = __vibmax_s32(wadd(bv[k], ext), wadd(hup[k], open), &ext_v);
-                const int h = __vibmax_s32(wadd(bh, ext), wadd(hl, open), &ext_h);
-                const int g = __vibmax_s32(h, v, &right_ge_down);
-                int hn = __vibmax_s32(diag, g, &diag_ge);
-                hn = max(hn, kSwCutoff);
-                bv[k] = v;
-                bh = h;
-                hd = hup[k];
-                hup[k] = hn;
-                hl = hn;
-                if (!diag_ge) bits |= 1u << (4 * k);
-                if (right_ge_down) bits |= 2u << (4 * k);
-                if (!ext_v) bits |= 4u << (4 * k);
-                if (!ext_h) bits |= 8u << (4 * k);
-                if (k == km) hm = hn;
-            }
-            tb[t * 32] = bits;
-            if (owns_last) lastcol[i - 1] = hm;
-            if (strip_out && lane == 31) strip_out[i] = make_int2(hl, bh);
-            send_h = hl;
-            send_b = bh;
-            hdiag = h_left;
-        }
-    }
-    // the lanes finish on row n: their scores are the bottom row
-    int *bottom = A.edges + P.edge_off + n;    // H[n][j] at bottom[j-1]
+    C.tb = A.tb + P.tb_off + (int64_t)s * steps * 32 + lane;
+    C.lastrow = A.edges + P.edge_off;
+    C.strip_in = s > 0 ? A.strip_scratch + P.scratch_off : nullptr;
+    C.strip_out = !last_strip ? A.strip_scratch + P.scratch_off : nullptr;
+    LaneState<K> L;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const int j = jbase + k + 1;
-        if (j <= m) bottom[j - 1] = hup[k];
+        L.b[k] = j <= m ? alt[j - 1] : 0;
+        L.hup[k] = wadd(edge_init(A, j), A.open);
+        L.bv[k] = kSwLowInit;
+    }
+    L.hdiag = wadd(edge_init(A, jbase), A.open);  // H[0][jbase] + open
+    L.send_h = 0;
+    L.send_b = kSwLowInit;
+    L.a_next = C.ref[min(max(0 - lane, 0), n - 1)];
+    int t = 0;
+    for (; t < 31; ++t) sw_step<K, CLAMP, true>(C, L, t, lane);
+#pragma unroll 4
+    for (; t < n; ++t) sw_step<K, CLAMP, false>(C, L, t, lane);  // every lane inside the matrix
+    for (; t < n + 31; ++t) sw_step<K, CLAMP, true>(C, L, t, lane);
+    // the lanes finish on row n: their scores are the bottom row
+    int *bottom = A.edges + P.edge_off + (int64_t)n * kSwRowStride(K);  // H[n][j] + open at bottom[j-1]
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int j = jbase + k + 1;
+        if (j <= m) bottom[j - 1] = L.hup[k];
     }
     __syncwarp();
 }
 
-template <int K>
+template <int K, bool CLAMP>
 __global__ void __launch_bounds__(128) sw_forward_kernel(SwArgs A, const int32_t *tasks, int n_tasks, int *cursor) {
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -170,7 +230,7 @@ __global__ void __launch_bounds__(128) sw_forward_kernel(SwArgs A, const int32_t
         }
         if (lane == 0) A.state[p] = 0;
         const int nstrips = (P.alt_len + 32 * K - 1) / (32 * K);
-        for (int s = 0; s < nstrips; ++s) sw_strip<K>(A, P, p, s, nstrips);
+        for (int s = 0; s < nstrips; ++s) sw_strip<K, CLAMP>(A, P, s, nstrips);
     }
 }
 
@@ -202,7 +262,9 @@ __global__ void sw_traceback_kernel(SwArgs A, int n_pairs) {
         return;
     }
     const int K = P.k;
-    const int *lastcol = A.edges + P.edge_off, *bottom = lastcol + n;
+    const int stride = kSwRowStride(K);
+    const int km = (m - 1) % (32 * K) % K;  // the last column's place among its lane's columns
+    const int *lastcol = A.edges + P.edge_off + km, *bottom = A.edges + P.edge_off + (int64_t)n * stride;
     int p1 = 0, p2 = 0;
     int maxscore = INT32_MIN;
     int segment = 0;
@@ -212,7 +274,7 @@ __global__ void sw_traceback_kernel(SwArgs A, int n_pairs) {
     } else {
         p2 = m;
         for (int i = 1; i <= n; ++i) {
-            const int sc = lastcol[i - 1];
+            const int sc = wsub(lastcol[(int64_t)(i - 1) * stride], A.open);  // stored as H + open
             if (sc >= maxscore) {
                 p1 = i;
                 maxscore = sc;
@@ -220,7 +282,7 @@ __global__ void sw_traceback_kernel(SwArgs A, int n_pairs) {
         }
         if (A.strategy != kSwLeadingIndel) {
             for (int j = 1; j <= m; ++j) {
-                const int sc = bottom[j - 1];
+                const int sc = wsub(bottom[j - 1], A.open);
                 const int dn = n - j < 0 ? j - n : n - j, dc = p1 - p2 < 0 ? p2 - p1 : p1 - p2;
                 if (sc > maxscore || (sc == maxscore && dn < dc)) {
                     p1 = n;
@@ -455,8 +517,13 @@ int launch_sw_forward(const SwArgs &a, int k, const int32_t *tasks, int n_tasks,
                       cudaStream_t s) {
     if (n_tasks <= 0) return 0;
     switch (k) {
-#define GHMM_SW_CASE(KK) \
-    case KK: sw_forward_kernel<KK><<<grid, 128, 0, s>>>(a, tasks, n_tasks, cursor); break;
+#define GHMM_SW_CASE(KK)                                                                         \
+    case KK:                                                                                     \
+        if (a.clamp)                                                                             \
+            sw_forward_kernel<KK, true><<<grid, 128, 0, s>>>(a, tasks, n_tasks, cursor);         \
+        else                                                                                     \
+            sw_forward_kernel<KK, false><<<grid, 128, 0, s>>>(a, tasks, n_tasks, cursor);        \
+        break;
         GHMM_SW_CASE(1)
         GHMM_SW_CASE(2)
         GHMM_SW_CASE(3)
@@ -474,8 +541,9 @@ int launch_sw_forward(const SwArgs &a, int k, const int32_t *tasks, int n_tasks,
 int sw_forward_occupancy(int k, int *blocks_per_sm) {
     cudaError_t e = cudaErrorInvalidValue;
     switch (k) {
-#define GHMM_SW_OCC(KK) \
-    case KK: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sw_forward_kernel<KK>, 128, 0); break;
+#define GHMM_SW_OCC(KK)                                                                                     \
+    case KK: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sw_forward_kernel<KK, false>, 128, 0); \
+        break;
         GHMM_SW_OCC(1)
         GHMM_SW_OCC(2)
         GHMM_SW_OCC(3)

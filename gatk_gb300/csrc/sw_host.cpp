@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -49,7 +50,8 @@ struct SwEngine {
     HostBuf<uint32_t> h_ops;
     std::vector<cudaEvent_t> events;
     ghmm_sw_stats stats{};
-    int64_t tb_budget_words = int64_t(1) << 30;  // 4 GiB of traceback bits per chunk
+    int stats_clamp = 0;
+    int64_t tb_budget_words = 0;  // traceback words per chunk; 0: chosen on first use
 
     cudaEvent_t event(size_t i) {
         while (events.size() <= i) {
@@ -132,30 +134,56 @@ void plan(SwPair *pairs, const int32_t *ref_bound, int64_t n, int64_t budget_wor
         P.slot_off = c.slots;
         P.scratch_off = strips > 1 ? c.scratch : -1;
         c.tb_words += words;
-        c.edges += rb + P.alt_len;
+        c.edges += (rb * kSwRowStride(k) + P.alt_len + 3) / 4 * 4;  // int4-aligned rows
         c.slots += 2 * (int64_t)P.alt_len + 4;
         if (strips > 1) c.scratch += rb + 1;
     }
     c.p1 = n;
     if (n > 0) chunks.push_back(c);
-    // tasks: chunk-local pair indices, grouped by K, longest work first
+    // tasks: chunk-local pair indices, grouped by K, longest ref first (a stable counting sort on the ref length:
+    // the alt lengths within one K differ by less than 32 columns per lane)
     int64_t pos = 0;
-    std::vector<int32_t> tmp;
+    std::vector<int32_t> count, by_k[kSwMaxK + 1];
     for (auto &ch : chunks) {
+        for (auto &v : by_k) v.clear();
+        for (int64_t i = ch.p0; i < ch.p1; ++i)
+            if (ref_bound[i] > 0) by_k[pairs[i].k].push_back((int32_t)(i - ch.p0));
         for (int k = kSwMaxK; k >= 1; --k) {
-            tmp.clear();
-            for (int64_t i = ch.p0; i < ch.p1; ++i)
-                if (pairs[i].k == k && ref_bound[i] > 0) tmp.push_back((int32_t)(i - ch.p0));
-            std::stable_sort(tmp.begin(), tmp.end(), [&](int32_t a, int32_t b) {
-                const SwPair &A = pairs[ch.p0 + a], &B = pairs[ch.p0 + b];
-                return (int64_t)ref_bound[ch.p0 + a] * A.alt_len > (int64_t)ref_bound[ch.p0 + b] * B.alt_len;
-            });
+            const std::vector<int32_t> &v = by_k[k];
             ch.task_begin[k] = pos;
-            ch.task_count[k] = (int64_t)tmp.size();
-            std::copy(tmp.begin(), tmp.end(), tasks + pos);
-            pos += (int64_t)tmp.size();
+            ch.task_count[k] = (int64_t)v.size();
+            int32_t kmax = 0;
+            for (int32_t q : v) kmax = std::max(kmax, ref_bound[ch.p0 + q]);
+            count.assign((size_t)kmax + 2, 0);
+            for (int32_t q : v) ++count[(size_t)(kmax - ref_bound[ch.p0 + q])];  // descending: longest first
+            int32_t run = 0;
+            for (auto &c : count) {
+                const int32_t x = c;
+                c = run;
+                run += x;
+            }
+            for (int32_t q : v) tasks[pos + count[(size_t)(kmax - ref_bound[ch.p0 + q])]++] = q;
+            pos += (int64_t)v.size();
         }
     }
+}
+
+// Whether any score of these alignments can reach MATRIX_MIN_CUTOFF (or wrap): along the diagonal every score is
+// at least the matrix edge it starts from plus min(0, match, mismatch) per cell, and with every quantity far inside
+// the int32 range no add wraps.  When that lower bound stays above the cutoff, the clamp never acts.
+bool needs_clamp(const ghmm_sw_params &p, int strategy, int64_t max_ref, int64_t max_alt) {
+    const int64_t mag = std::llabs((int64_t)p.match_value) + std::llabs((int64_t)p.mismatch_penalty) +
+                        std::llabs((int64_t)p.gap_open_penalty) + std::llabs((int64_t)p.gap_extend_penalty);
+    const int64_t len = max_ref + max_alt + 2;
+    if (mag * len >= (int64_t(1) << 29)) return true;
+    int64_t edge_min = 0;
+    if (strategy == kSwIndel || strategy == kSwLeadingIndel) {
+        const int64_t L = std::max(max_ref, max_alt);
+        edge_min = std::min<int64_t>({0, (int64_t)p.gap_open_penalty,
+                                      (int64_t)p.gap_open_penalty + (L - 1) * p.gap_extend_penalty});
+    }
+    const int64_t worst = std::min<int64_t>({0, (int64_t)p.match_value, (int64_t)p.mismatch_penalty});
+    return edge_min + worst * std::min(max_ref, max_alt) <= -100000000;
 }
 
 struct RunIn {
@@ -168,6 +196,7 @@ struct RunIn {
     // realign: device setup before the chunks
     const BatchInfo *batch = nullptr;
     const double *priority = nullptr;  // host, per batch haplotype
+    std::chrono::steady_clock::time_point t0;  // start of the call
 };
 
 // Everything after the host pairs are filled: plan, upload, kernels, results into the engine's host buffers.
@@ -214,6 +243,7 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
     int32_t *d_state = E.d_res.p, *d_offset = E.d_res.p + n, *d_nops = E.d_res.p + 2 * n, *d_best = E.d_res.p + 3 * n;
     int *d_err = reinterpret_cast<int *>(E.d_counters.p + 1);
     int *d_cursors = reinterpret_cast<int *>(E.d_counters.p + 2);
+    E.stats.ms_host = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - in.t0).count();
     SW_CUDA(cudaEventRecord(E.event(0), s), "event");
     if (in.batch) {
         SwRealignArgs R{};
@@ -249,6 +279,15 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
     A.strategy = in.strategy;
     A.indel_edges = (in.strategy == kSwIndel || in.strategy == kSwLeadingIndel) ? 1 : 0;
     A.shortcut = in.shortcut && (in.strategy == kSwSoftclip || in.strategy == kSwIgnore) ? 1 : 0;
+    {
+        int64_t max_ref = 0, max_alt = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            max_ref = std::max<int64_t>(max_ref, in.ref_bound[i]);
+            max_alt = std::max<int64_t>(max_alt, E.h_pairs.p[i].alt_len);
+        }
+        A.clamp = needs_clamp(*in.params, in.strategy, max_ref, max_alt) ? 1 : 0;
+        E.stats_clamp = A.clamp;
+    }
     int occ[kSwMaxK + 1]{};
     for (int k = 1; k <= kSwMaxK; ++k) {
         int b = 0;
@@ -338,7 +377,15 @@ int check_params(ghmm_ctx *ctx, const ghmm_sw_params *params, int32_t strategy) 
 
 SwEngine *engine(const CtxInfo &ci) {
     if (!*ci.sw) *ci.sw = new SwEngine();
-    return *ci.sw;
+    SwEngine *e = *ci.sw;
+    if (e->tb_budget_words == 0) {  // 16 GiB, or a quarter of the free device memory
+        size_t free_b = 0, total_b = 0;
+        int64_t budget = int64_t(16) << 30;
+        if (cudaSetDevice(ci.device) == cudaSuccess && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+            budget = std::min<int64_t>(budget, (int64_t)(free_b / 4));
+        e->tb_budget_words = std::max<int64_t>(budget, int64_t(1) << 20) / 4;
+    }
+    return e;
 }
 
 // results of pairs [0, n) from the engine's host buffers into the caller's arrays
@@ -379,6 +426,7 @@ int sw_batch(ghmm_ctx *ctx, const CtxInfo &ci, const ghmm_sw_pair *pairs, int64_
     }
     // refs deduplicated by (address, length): a haplotype shared by many reads is copied once
     std::unordered_map<const uint8_t *, std::pair<int64_t, int32_t>> seen;
+    seen.reserve((size_t)std::min<int64_t>(n, 1 << 20));
     std::vector<int64_t> ref_off((size_t)n);
     std::vector<int64_t> uniq;  // pair index of each distinct ref
     int64_t ref_bytes = 0;
@@ -426,6 +474,7 @@ int sw_batch(ghmm_ctx *ctx, const CtxInfo &ci, const ghmm_sw_pair *pairs, int64_
     in.n = n;
     in.ref_bound = ref_len.data();
     in.ops_cap = res->cigar_cap;
+    in.t0 = t0;
     int rc = run(ctx, ci, E, in, plane_bytes, nullptr);
     if (rc) return rc;
     rc = deliver(ctx, E, n, ref_len.data(), res);
@@ -548,6 +597,7 @@ int ghmm_batch_realign(ghmm_ctx *ctx, ghmm_batch *batch, const double *hap_prior
     in.ops_cap = result->cigar_cap;
     in.batch = &bi;
     in.priority = hap_priority;
+    in.t0 = t0;
     std::vector<uint8_t> inf;
     int rc = run(ctx, ci, E, in, 0, &inf);
     if (rc) return rc;

@@ -173,7 +173,7 @@ class SwStats(ctypes.Structure):
     _fields_ = [("n_alignments", ctypes.c_int64), ("n_shortcut", ctypes.c_int64), ("cells", ctypes.c_int64),
                 ("chunks", ctypes.c_int32), ("launches", ctypes.c_int32), ("ms_device", ctypes.c_double),
                 ("ms_forward", ctypes.c_double), ("ms_total", ctypes.c_double), ("h2d_bytes", ctypes.c_int64),
-                ("d2h_bytes", ctypes.c_int64)]
+                ("d2h_bytes", ctypes.c_int64), ("ms_host", ctypes.c_double)]
 
 
 # Every exported symbol and its signature (restype, argtypes).  The tests check that the library

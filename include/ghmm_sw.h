@@ -101,6 +101,7 @@ typedef struct ghmm_sw_stats {
     double ms_forward;     /* summed time of the score-recurrence kernels */
     double ms_total;       /* wall time of the call */
     int64_t h2d_bytes, d2h_bytes;
+    double ms_host;        /* host time before the first launch: checks, marshalling, chunk and task planning */
 } ghmm_sw_stats;
 
 /* SWAlignerNativeBinding.align: the cigar as text into cigar[cigar_cap] (NUL-terminated; GHMM_ERR_ARG when
@@ -127,7 +128,8 @@ int ghmm_batch_realign(ghmm_ctx *ctx, ghmm_batch *batch, const double *hap_prior
 
 int ghmm_sw_last_stats(ghmm_ctx *ctx, ghmm_sw_stats *stats);
 
-/* Device memory for traceback bits (4 bits per cell, in 32-bit words per lane and step), default 4 GiB.  A
+/* Device memory for traceback bits (4 bits per cell, in 32-bit words per lane and step); by default 16 GiB or a
+ * quarter of the device memory free when the context first aligns, whichever is less.  A
  * call whose alignments need more runs in several passes over the buffer; a single alignment larger than the
  * budget gets a pass of its own.  Values below 1 MiB are raised to 1 MiB. */
 int ghmm_sw_set_traceback_budget(ghmm_ctx *ctx, int64_t bytes);
