@@ -719,6 +719,7 @@ def run_sw(args):
         "config": {"workload": f"config1: {n_regions} regions, every read against its best haplotype",
                    "reads": int(wl.n_reads), "alignments_with_recurrence": int(st["n_alignments"] - st["n_shortcut"]),
                    "substring_shortcut": int(st["n_shortcut"]), "cells": int(cells), "chunks": int(st["chunks"]),
+                   "int16_paired_alignments": int(st["n_int16"]),
                    "parameters": "ALIGNMENT_TO_BEST_HAPLOTYPE_SW_PARAMETERS (10, -15, -30, -5), SOFTCLIP"},
         "realign_call_ms": dt_call * 1e3,
         "realign_host_ms": statistics.mean(x["ms_host"] for x in sts),

@@ -169,6 +169,12 @@ struct SwArgs {
 int launch_sw_forward(const SwArgs &a, int k, const int32_t *tasks, int n_tasks, int *cursor, int grid,
                       cudaStream_t s);
 int sw_forward_occupancy(int k, int *blocks_per_sm);
+// Two single-strip alignments per warp in 16-bit halves (tasks: A, B or -1); only for pairs whose scores the host
+// has bounded inside +-24000.  Writes each alignment's traceback words and edges in the int32 kernel's layout.
+int launch_sw_pair16(const SwArgs &a, int k, const int2 *tasks, int n_tasks, int *cursor, int grid, cudaStream_t s);
+int sw_pair16_occupancy(int k, int *blocks_per_sm);
+// The exact-substring shortcut of every alignment (state 1 + offset), or state 0 for all when a.shortcut is 0.
+int launch_sw_prepass(const SwArgs &a, int n_pairs, int sm_count, cudaStream_t s);
 int launch_sw_traceback(const SwArgs &a, int n_pairs, cudaStream_t s);
 // exclusive scan of the chunk's n_ops into starts (offset by *running, which then advances), gather into ops
 int launch_sw_compact(const SwArgs &a, int n_pairs, int64_t *starts, int64_t *running, uint32_t *ops, int64_t ops_cap,

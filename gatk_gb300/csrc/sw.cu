@@ -215,22 +215,207 @@ __global__ void __launch_bounds__(128) sw_forward_kernel(SwArgs A, const int32_t
         if (lane == 0) task = atomicAdd(cursor, 1);
         task = __shfl_sync(0xffffffffu, task, 0);
         if (task >= n_tasks) break;
-        const int p = tasks[task];
-        const SwPair P = A.pairs[p];
-        if (A.shortcut) {
-            const int idx = warp_last_index_of(A.ref_plane + P.ref_off, P.ref_len, A.alt_plane + P.alt_off,
-                                               P.alt_len);
-            if (idx >= 0) {
-                if (lane == 0) {
-                    A.state[p] = 1;
-                    A.offset[p] = idx;
-                }
-                continue;
-            }
-        }
-        if (lane == 0) A.state[p] = 0;
+        const SwPair P = A.pairs[tasks[task]];
         const int nstrips = (P.alt_len + 32 * K - 1) / (32 * K);
         for (int s = 0; s < nstrips; ++s) sw_strip<K, CLAMP>(A, P, s, nstrips);
+    }
+}
+
+// ---- two alignments per lane, in the 16-bit halves of 32-bit registers ----
+// Every score is kept as x + 32768 in its half (so unsigned 16-bit maxima order them as signed values), and with
+// every half inside [0, 65535] a plain 32-bit add of c * 0x10001 adds c to both halves without a carry or a borrow
+// crossing between them.  The host sends a pair here only when a bound on every score of both alignments keeps the
+// halves inside that range; the values are then exactly the int32 ones.
+constexpr int kSw16Low = -28672;  // the very low initial gap value (Java: Integer.MIN_VALUE / 2) as a 16-bit score
+
+__device__ __forceinline__ uint32_t vmax2(uint32_t a, uint32_t b) {
+    uint32_t d;
+    asm("max.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+__device__ __forceinline__ uint32_t vmin2(uint32_t a, uint32_t b) {
+    uint32_t d;
+    asm("min.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+__device__ __forceinline__ uint32_t both16(int x) { return (uint32_t)(x + 32768) * 0x10001u; }
+__device__ __forceinline__ uint32_t addc16(int c) { return (uint32_t)c * 0x10001u; }
+__device__ __forceinline__ int lo16(uint32_t w) { return (int)(w & 0xffffu) - 32768; }
+__device__ __forceinline__ int hi16(uint32_t w) { return (int)(w >> 16) - 32768; }
+
+template <int K>
+__device__ __forceinline__ void store_row16(int *dst, const uint32_t (&w)[K], bool high) {
+#pragma unroll
+    for (int q = 0; q < K; q += 4) {
+        int v[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) v[r] = q + r < K ? (high ? hi16(w[q + r < K ? q + r : 0]) : lo16(w[q + r < K ? q + r : 0])) : 0;
+        reinterpret_cast<int4 *>(dst)[q / 4] = make_int4(v[0], v[1], v[2], v[3]);
+    }
+}
+
+struct Pair16Ctx {
+    const uint8_t *ref_a, *ref_b;
+    uint32_t *tb_a, *tb_b;     // this lane's traceback word of step 0 in each alignment's own layout
+    int *last_a, *last_b;      // rows of the lane holding each alignment's last column (H + open, int32)
+    int *bottom_a, *bottom_b;  // each alignment's bottom row (H + open), this lane's first column
+    int n_a, n_b, n, m_a, m_b, jbase;
+    uint32_t ext2, open2, mo2, inject_const;
+    int dm, open, ext;
+    bool has_b, owns_a, owns_b, indel_edges;
+};
+
+template <int K>
+struct Lane16 {
+    uint32_t b[K];    // alt bases of alignment A (low half) and B (high half)
+    uint32_t hup[K];  // H[i-1][j] + open before a step, H[i][j] + open after it
+    uint32_t bv[K];
+    uint32_t hdiag, send_h, send_b, a_next;
+};
+
+template <int K, bool CHECK>
+__device__ __forceinline__ void pair16_step(const Pair16Ctx &C, Lane16<K> &L, int t, int lane) {
+    const int i = t - lane + 1;
+    const bool active = !CHECK || (i >= 1 && i <= C.n);
+    const uint32_t a2 = L.a_next;
+    L.a_next = (uint32_t)C.ref_a[min(max(i, 0), C.n_a - 1)] | ((uint32_t)C.ref_b[min(max(i, 0), C.n_b - 1)] << 16);
+    uint32_t h_left = __shfl_up_sync(0xffffffffu, L.send_h, 1);
+    uint32_t bh = __shfl_up_sync(0xffffffffu, L.send_b, 1);
+    if (lane == 0) {
+        h_left = C.indel_edges && i > 0 ? both16(C.open + (i - 1) * C.ext + C.open) : C.inject_const;
+        bh = both16(kSw16Low);
+    }
+    if (!active) return;
+    uint32_t bits0 = 0, bits1 = 0;
+    uint32_t hd = L.hdiag, hl = h_left;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const uint32_t ne = vmin2(a2 ^ L.b[k], 0x00010001u);       // 1 in a half whose bases differ
+        const uint32_t diag = ne * (uint32_t)C.dm + hd + C.mo2;      // + match (or mismatch) - open, per half
+        const uint32_t bvk = L.bv[k] + C.ext2, pv = L.hup[k];
+        const uint32_t v = vmax2(bvk, pv);
+        const uint32_t bhk = bh + C.ext2, ph = hl;
+        const uint32_t h = vmax2(bhk, ph);
+        const uint32_t g = vmax2(h, v);
+        const uint32_t hn = vmax2(diag, g);
+        // flags as 0/1 per half (each difference is >= 0 in both halves), placed at bit 4(k%4)+f of each half
+        const uint32_t f0 = vmin2(hn - diag, 0x00010001u);  // not diagonal
+        const uint32_t f1 = vmin2(g - h, 0x00010001u);      // right < down (flipped below)
+        const uint32_t f2 = vmin2(v - bvk, 0x00010001u);    // vertical gap opened here
+        const uint32_t f3 = vmin2(h - bhk, 0x00010001u);    // horizontal gap opened here
+        uint32_t &w = k < 4 ? bits0 : bits1;
+        const int sh = 4 * (k & 3);
+        w += f0 << sh;
+        w += f1 << (sh + 1);
+        w += f2 << (sh + 2);
+        w += f3 << (sh + 3);
+        const uint32_t hno = hn + C.open2;
+        L.bv[k] = v;
+        bh = h;
+        hd = L.hup[k];
+        L.hup[k] = hno;
+        hl = hno;
+    }
+    // each alignment's word in the int32 kernel's layout (bit 1 there: right >= down)
+    const uint32_t wa = __byte_perm(bits0, bits1, 0x5410) ^ 0x22222222u;
+    const uint32_t wb = __byte_perm(bits0, bits1, 0x7632) ^ 0x22222222u;
+    if (t < C.n_a + 31) C.tb_a[(int64_t)t * 32] = wa;
+    if (C.has_b && t < C.n_b + 31) C.tb_b[(int64_t)t * 32] = wb;
+    if (C.owns_a && i <= C.n_a) store_row16<K>(C.last_a + (int64_t)(i - 1) * kSwRowStride(K), L.hup, false);
+    if (C.owns_b && i <= C.n_b) store_row16<K>(C.last_b + (int64_t)(i - 1) * kSwRowStride(K), L.hup, true);
+    if (i == C.n_a) {
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (C.jbase + k < C.m_a) C.bottom_a[k] = lo16(L.hup[k]);
+    }
+    if (C.has_b && i == C.n_b) {
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (C.jbase + k < C.m_b) C.bottom_b[k] = hi16(L.hup[k]);
+    }
+    L.send_h = hl;
+    L.send_b = bh;
+    L.hdiag = h_left;
+}
+
+// tasks: (alignment A, alignment B or -1) of single-strip alignments with the same K, B's ref no longer than A's
+template <int K>
+__global__ void __launch_bounds__(128) sw_pair16_kernel(SwArgs A, const int2 *tasks, int n_tasks, int *cursor) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int task = 0;
+        if (lane == 0) task = atomicAdd(cursor, 1);
+        task = __shfl_sync(0xffffffffu, task, 0);
+        if (task >= n_tasks) break;
+        const int2 tk = tasks[task];
+        const SwPair PA = A.pairs[tk.x];
+        const bool has_b = tk.y >= 0;
+        const SwPair PB = has_b ? A.pairs[tk.y] : PA;
+        Pair16Ctx C;
+        C.ref_a = A.ref_plane + PA.ref_off;
+        C.ref_b = A.ref_plane + PB.ref_off;
+        C.n_a = PA.ref_len;
+        C.n_b = PB.ref_len;
+        C.n = max(C.n_a, C.n_b);
+        C.m_a = PA.alt_len;
+        C.m_b = PB.alt_len;
+        C.jbase = lane * K;
+        C.has_b = has_b;
+        C.open = A.open;
+        C.ext = A.extend;
+        C.ext2 = addc16(A.extend);
+        C.open2 = addc16(A.open);
+        C.mo2 = addc16(A.match - A.open);
+        C.dm = A.mismatch - A.match;
+        C.indel_edges = A.indel_edges != 0;
+        C.inject_const = both16(A.open);
+        C.tb_a = A.tb + PA.tb_off + lane;
+        C.tb_b = A.tb + PB.tb_off + lane;
+        const int km_a = (C.m_a - 1) - C.jbase, km_b = (C.m_b - 1) - C.jbase;
+        C.owns_a = km_a >= 0 && km_a < K;
+        C.owns_b = has_b && km_b >= 0 && km_b < K;
+        C.last_a = A.edges + PA.edge_off;
+        C.last_b = A.edges + PB.edge_off;
+        C.bottom_a = A.edges + PA.edge_off + (int64_t)C.n_a * kSwRowStride(K) + C.jbase;
+        C.bottom_b = A.edges + PB.edge_off + (int64_t)C.n_b * kSwRowStride(K) + C.jbase;
+        const uint8_t *alt_a = A.alt_plane + PA.alt_off, *alt_b = A.alt_plane + PB.alt_off;
+        Lane16<K> L;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int j = C.jbase + k + 1;
+            const uint32_t ba = j <= C.m_a ? alt_a[j - 1] : 0u, bb = j <= C.m_b ? alt_b[j - 1] : 0u;
+            L.b[k] = ba | (bb << 16);
+            L.hup[k] = both16(edge_init(A, j) + A.open);
+            L.bv[k] = both16(kSw16Low);
+        }
+        L.hdiag = both16(edge_init(A, C.jbase) + A.open);
+        L.send_h = 0;
+        L.send_b = both16(kSw16Low);
+        L.a_next = (uint32_t)C.ref_a[0] | ((uint32_t)C.ref_b[0] << 16);
+        if (lane > 0) L.a_next = 0;  // lanes start later; their first base is loaded by their own steps
+        int t = 0;
+        for (; t < 31; ++t) pair16_step<K, true>(C, L, t, lane);
+#pragma unroll 4
+        for (; t < C.n; ++t) pair16_step<K, false>(C, L, t, lane);
+        for (; t < C.n + 31; ++t) pair16_step<K, true>(C, L, t, lane);
+        __syncwarp();
+    }
+}
+
+// The exact-substring shortcut (Utils.lastIndexOf) of every alignment, one warp each, before the recurrence:
+// state 1 and the offset for an alt found in its ref, state 0 otherwise (and for every alignment when off).
+__global__ void __launch_bounds__(128) sw_prepass_kernel(SwArgs A, int n_pairs) {
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x / 32);
+    for (int p = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); p < n_pairs; p += warps) {
+        const SwPair P = A.pairs[p];
+        int idx = -1;
+        if (A.shortcut && P.ref_len > 0)
+            idx = warp_last_index_of(A.ref_plane + P.ref_off, P.ref_len, A.alt_plane + P.alt_off, P.alt_len);
+        if (lane == 0) {
+            A.state[p] = idx >= 0 ? 1 : 0;
+            if (idx >= 0) A.offset[p] = idx;
+        }
     }
 }
 
@@ -535,6 +720,52 @@ int launch_sw_forward(const SwArgs &a, int k, const int32_t *tasks, int n_tasks,
 #undef GHMM_SW_CASE
         default: return (int)cudaErrorInvalidValue;
     }
+    return (int)cudaGetLastError();
+}
+
+int launch_sw_pair16(const SwArgs &a, int k, const int2 *tasks, int n_tasks, int *cursor, int grid, cudaStream_t s) {
+    if (n_tasks <= 0) return 0;
+    switch (k) {
+#define GHMM_SW16_CASE(KK) \
+    case KK: sw_pair16_kernel<KK><<<grid, 128, 0, s>>>(a, tasks, n_tasks, cursor); break;
+        GHMM_SW16_CASE(1)
+        GHMM_SW16_CASE(2)
+        GHMM_SW16_CASE(3)
+        GHMM_SW16_CASE(4)
+        GHMM_SW16_CASE(5)
+        GHMM_SW16_CASE(6)
+        GHMM_SW16_CASE(7)
+        GHMM_SW16_CASE(8)
+#undef GHMM_SW16_CASE
+        default: return (int)cudaErrorInvalidValue;
+    }
+    return (int)cudaGetLastError();
+}
+
+int sw_pair16_occupancy(int k, int *blocks_per_sm) {
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (k) {
+#define GHMM_SW16_OCC(KK) \
+    case KK: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, sw_pair16_kernel<KK>, 128, 0); break;
+        GHMM_SW16_OCC(1)
+        GHMM_SW16_OCC(2)
+        GHMM_SW16_OCC(3)
+        GHMM_SW16_OCC(4)
+        GHMM_SW16_OCC(5)
+        GHMM_SW16_OCC(6)
+        GHMM_SW16_OCC(7)
+        GHMM_SW16_OCC(8)
+#undef GHMM_SW16_OCC
+        default: break;
+    }
+    return (int)e;
+}
+
+int launch_sw_prepass(const SwArgs &a, int n_pairs, int sm_count, cudaStream_t s) {
+    if (n_pairs <= 0) return 0;
+    const int64_t want = ((int64_t)n_pairs + 3) / 4;
+    const int grid = (int)(want < (int64_t)sm_count * 16 ? want : (int64_t)sm_count * 16);
+    sw_prepass_kernel<<<grid, 128, 0, s>>>(a, n_pairs);
     return (int)cudaGetLastError();
 }
 

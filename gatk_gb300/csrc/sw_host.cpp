@@ -32,6 +32,8 @@ struct SwEngine {
     DevBuf<SwPair> d_pairs;
     HostBuf<int32_t> h_tasks;
     DevBuf<int32_t> d_tasks;
+    HostBuf<int2> h_pair_tasks;
+    DevBuf<int2> d_pair_tasks;
     HostBuf<uint8_t> h_planes;
     DevBuf<uint8_t> d_planes;
     DevBuf<int32_t> d_res;      // state | offset | n_ops | best, n each
@@ -50,7 +52,7 @@ struct SwEngine {
     HostBuf<uint32_t> h_ops;
     std::vector<cudaEvent_t> events;
     ghmm_sw_stats stats{};
-    int stats_clamp = 0;
+    bool allow16 = true;  // pair eligible alignments in the 16-bit kernel
     int64_t tb_budget_words = 0;  // traceback words per chunk; 0: chosen on first use
 
     cudaEvent_t event(size_t i) {
@@ -63,6 +65,7 @@ struct SwEngine {
     }
     void release() {
         h_pairs.release(); d_pairs.release(); h_tasks.release(); d_tasks.release(); h_planes.release();
+        h_pair_tasks.release(); d_pair_tasks.release();
         d_planes.release(); d_res.release(); d_starts.release(); d_ops.release(); d_counters.release();
         d_tb.release(); d_edges.release(); d_scratch.release(); d_slot.release(); d_prio.release(); d_inf.release();
         h_res.release(); h_starts.release(); h_counters.release(); h_ops.release();
@@ -99,28 +102,52 @@ int sw_k(int alt_len) { return alt_len > 32 * kSwMaxK ? kSwMaxK : (alt_len + 31)
 struct Chunk {
     int64_t p0 = 0, p1 = 0;
     int64_t tb_words = 0, edges = 0, slots = 0, scratch = 0;
-    int64_t task_begin[kSwMaxK + 1]{}, task_count[kSwMaxK + 1]{};
+    int64_t task_begin[kSwMaxK + 1]{}, task_count[kSwMaxK + 1]{};      // int32 kernel: one alignment per task
+    int64_t pair_begin[kSwMaxK + 1]{}, pair_count[kSwMaxK + 1]{};      // 16-bit kernel: two alignments per task
 };
 
-// Buffer offsets (chunk-relative) and alt columns per lane of every pair, chunk boundaries, and per chunk the
-// pairs of each K sorted by decreasing work.  ref_bound[i] sizes pair i's buffers (its ref length, or an upper
-// bound of it when the ref is chosen on the device).
-void plan(SwPair *pairs, const int32_t *ref_bound, int64_t n, int64_t budget_words, std::vector<Chunk> &chunks,
-          int32_t *tasks) {
+// Whether every score of an alignment with a ref of n bases and K alt columns per lane (the lanes' padding columns
+// included) stays far inside the 16-bit halves of the paired kernel: scores lie between the best all-diagonal path
+// from the matrix edge and max(0, match) per diagonal step (gap penalties only lower a path), gap values between a
+// score plus the open penalty and the best score plus it, and the very low initial gap value must still lose to a
+// first opening.  Positive gap penalties or large parameters go to the int32 kernel.
+bool fits16(const ghmm_sw_params &p, int strategy, int64_t n, int k) {
+    const int64_t w = 32 * (int64_t)k;
+    const int64_t m = p.match_value, mm = p.mismatch_penalty, o = p.gap_open_penalty, e = p.gap_extend_penalty;
+    if (o > 0 || e > 0) return false;
+    const int64_t am = std::llabs(m), amm = std::llabs(mm), ao = -o, ae = -e;
+    if (am > 2048 || amm > 2048 || ao > 2048 || ae > 2048) return false;
+    const int64_t edge_min = (strategy == kSwIndel || strategy == kSwLeadingIndel) ? o + e * (std::max(n, w) - 1) : 0;
+    const int64_t diag = std::min(n, w);
+    const int64_t hmin = edge_min + std::min<int64_t>({0, m, mm}) * diag;
+    const int64_t hmax = std::max<int64_t>(0, m) * diag;
+    const int64_t slack = am + amm + ao + ae;
+    return hmin - slack >= -28000 && hmax + slack <= 28000;
+}
+
+// Buffer offsets (chunk-relative) of every alignment that runs the recurrence (state 0, ref_len > 0), chunk
+// boundaries over contiguous alignment ranges, and per chunk and K: the int32 kernel's tasks (longest ref first)
+// and the 16-bit kernel's pairs (neighbours in ref-length order, so the two halves of a warp finish together).
+void plan(SwPair *pairs, const int32_t *state, int64_t n, int64_t budget_words, const ghmm_sw_params &prm,
+          int strategy, bool allow16, std::vector<Chunk> &chunks, int32_t *tasks, int2 *pair_tasks,
+          int64_t *n_paired) {
     chunks.clear();
     Chunk c;
+    std::vector<uint8_t> use16((size_t)n, 0);
     for (int64_t i = 0; i < n; ++i) {
         SwPair &P = pairs[i];
-        if (ref_bound[i] <= 0) {  // nothing to align against: no task, no buffers
+        const bool runs = state[i] == 0 && P.ref_len > 0;
+        if (!runs) {  // shortcut or nothing to align against: a cigar slot only
             P.k = 1;
-            P.tb_off = P.edge_off = P.slot_off = c.slots;
+            P.tb_off = P.edge_off = 0;
+            P.slot_off = c.slots;
             P.scratch_off = -1;
             c.slots += 2 * (int64_t)P.alt_len + 4;
             continue;
         }
         const int k = sw_k(P.alt_len);
         const int64_t strips = (P.alt_len + 32 * k - 1) / (32 * k);
-        const int64_t rb = ref_bound[i];
+        const int64_t rb = P.ref_len;
         const int64_t words = strips * (rb + 31) * 32;
         if (i > c.p0 && c.tb_words + words > budget_words) {
             c.p1 = i;
@@ -137,35 +164,49 @@ void plan(SwPair *pairs, const int32_t *ref_bound, int64_t n, int64_t budget_wor
         c.edges += (rb * kSwRowStride(k) + P.alt_len + 3) / 4 * 4;  // int4-aligned rows
         c.slots += 2 * (int64_t)P.alt_len + 4;
         if (strips > 1) c.scratch += rb + 1;
+        use16[(size_t)i] = allow16 && strips == 1 && fits16(prm, strategy, rb, k);
     }
     c.p1 = n;
     if (n > 0) chunks.push_back(c);
-    // tasks: chunk-local pair indices, grouped by K, longest ref first (a stable counting sort on the ref length:
-    // the alt lengths within one K differ by less than 32 columns per lane)
-    int64_t pos = 0;
-    std::vector<int32_t> count, by_k[kSwMaxK + 1];
+    // a stable counting sort on the ref length, longest first, per chunk and K and kernel
+    int64_t pos = 0, ppos = 0, paired = 0;
+    std::vector<int32_t> count, by_k[2][kSwMaxK + 1], sorted;
     for (auto &ch : chunks) {
-        for (auto &v : by_k) v.clear();
+        for (auto &kk : by_k)
+            for (auto &v : kk) v.clear();
         for (int64_t i = ch.p0; i < ch.p1; ++i)
-            if (ref_bound[i] > 0) by_k[pairs[i].k].push_back((int32_t)(i - ch.p0));
-        for (int k = kSwMaxK; k >= 1; --k) {
-            const std::vector<int32_t> &v = by_k[k];
-            ch.task_begin[k] = pos;
-            ch.task_count[k] = (int64_t)v.size();
-            int32_t kmax = 0;
-            for (int32_t q : v) kmax = std::max(kmax, ref_bound[ch.p0 + q]);
-            count.assign((size_t)kmax + 2, 0);
-            for (int32_t q : v) ++count[(size_t)(kmax - ref_bound[ch.p0 + q])];  // descending: longest first
-            int32_t run = 0;
-            for (auto &c : count) {
-                const int32_t x = c;
-                c = run;
-                run += x;
+            if (state[i] == 0 && pairs[i].ref_len > 0) by_k[use16[(size_t)i]][pairs[i].k].push_back((int32_t)(i - ch.p0));
+        for (int kind = 0; kind < 2; ++kind) {
+            for (int k = kSwMaxK; k >= 1; --k) {
+                const std::vector<int32_t> &v = by_k[kind][k];
+                int32_t kmax = 0;
+                for (int32_t q : v) kmax = std::max(kmax, pairs[ch.p0 + q].ref_len);
+                count.assign((size_t)kmax + 2, 0);
+                for (int32_t q : v) ++count[(size_t)(kmax - pairs[ch.p0 + q].ref_len)];
+                int32_t run = 0;
+                for (auto &cc : count) {
+                    const int32_t x = cc;
+                    cc = run;
+                    run += x;
+                }
+                sorted.resize(v.size());
+                for (int32_t q : v) sorted[(size_t)count[(size_t)(kmax - pairs[ch.p0 + q].ref_len)]++] = q;
+                if (kind == 0) {
+                    ch.task_begin[k] = pos;
+                    ch.task_count[k] = (int64_t)sorted.size();
+                    std::copy(sorted.begin(), sorted.end(), tasks + pos);
+                    pos += (int64_t)sorted.size();
+                } else {
+                    ch.pair_begin[k] = ppos;
+                    ch.pair_count[k] = ((int64_t)sorted.size() + 1) / 2;
+                    for (size_t q = 0; q < sorted.size(); q += 2)
+                        pair_tasks[ppos++] = make_int2(sorted[q], q + 1 < sorted.size() ? sorted[q + 1] : -1);
+                    paired += (int64_t)sorted.size();
+                }
             }
-            for (int32_t q : v) tasks[pos + count[(size_t)(kmax - ref_bound[ch.p0 + q])]++] = q;
-            pos += (int64_t)v.size();
         }
     }
+    *n_paired = paired;
 }
 
 // Whether any score of these alignments can reach MATRIX_MIN_CUTOFF (or wrap): along the diagonal every score is
@@ -191,60 +232,52 @@ struct RunIn {
     const ghmm_sw_params *params;
     int strategy, shortcut;
     int64_t n;
-    const int32_t *ref_bound;
     int64_t ops_cap;
-    // realign: device setup before the chunks
+    // realign: the haplotype of each read is chosen on the device before the chunks are planned
     const BatchInfo *batch = nullptr;
     const double *priority = nullptr;  // host, per batch haplotype
     std::chrono::steady_clock::time_point t0;  // start of the call
 };
 
-// Everything after the host pairs are filled: plan, upload, kernels, results into the engine's host buffers.
-// On return h_res holds state | offset | n_ops | best (n each), h_starts the op starts, h_counters[0] the op
-// total, and h_ops the ops.
+// Everything after the host pairs hold their sequences: (1) upload, the realign setup and the substring shortcut on
+// the device, then the shortcut states (and chosen haplotypes) back to the host; (2) chunk and task planning with
+// the exact lengths; (3) per chunk the score kernels, the traceback and the cigar compaction.  On return h_res holds
+// state | offset | n_ops | best (n each), h_starts the op starts, h_counters[0] the op total, and h_ops the ops.
 int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t plane_bytes,
         std::vector<uint8_t> *informative) {
     const int64_t n = in.n;
     cudaStream_t s = ci.stream;
-    std::vector<Chunk> chunks;
-    SW_CUDA(E.h_tasks.reserve((size_t)std::max<int64_t>(n, 1)), "pinned tasks");
-    plan(E.h_pairs.p, in.ref_bound, n, E.tb_budget_words, chunks, E.h_tasks.p);
-    int64_t max_tb = 0, max_edges = 0, max_slots = 0, max_scratch = 0;
-    for (auto &c : chunks) {
-        max_tb = std::max(max_tb, c.tb_words);
-        max_edges = std::max(max_edges, c.edges);
-        max_slots = std::max(max_slots, c.slots);
-        max_scratch = std::max(max_scratch, c.scratch);
-    }
-    const int64_t n_cursors = 2 + (int64_t)chunks.size() * kCursorsPerChunk;
     SW_CUDA(E.d_pairs.reserve((size_t)n), "device pairs");
-    SW_CUDA(E.d_tasks.reserve((size_t)n), "device tasks");
     SW_CUDA(E.d_res.reserve((size_t)n * 4), "device results");
     SW_CUDA(E.d_starts.reserve((size_t)n), "device cigar starts");
     SW_CUDA(E.d_ops.reserve((size_t)std::max<int64_t>(in.ops_cap, 1)), "device cigar ops");
-    SW_CUDA(E.d_counters.reserve((size_t)n_cursors), "device counters");
-    SW_CUDA(E.d_tb.reserve((size_t)max_tb), "traceback buffer");
-    SW_CUDA(E.d_edges.reserve((size_t)max_edges), "edge scores");
-    SW_CUDA(E.d_scratch.reserve((size_t)std::max<int64_t>(max_scratch, 1)), "strip scratch");
-    SW_CUDA(E.d_slot.reserve((size_t)max_slots), "cigar slots");
     SW_CUDA(E.h_res.reserve((size_t)n * 4), "pinned results");
     SW_CUDA(E.h_starts.reserve((size_t)n), "pinned starts");
     SW_CUDA(E.h_counters.reserve(2), "pinned counters");
+    int32_t *d_state = E.d_res.p, *d_offset = E.d_res.p + n, *d_nops = E.d_res.p + 2 * n, *d_best = E.d_res.p + 3 * n;
     if (plane_bytes > 0)
         SW_CUDA(cudaMemcpyAsync(E.d_planes.p, E.h_planes.p, (size_t)plane_bytes, cudaMemcpyHostToDevice, s),
                 "H2D sequences");
     SW_CUDA(cudaMemcpyAsync(E.d_pairs.p, E.h_pairs.p, (size_t)n * sizeof(SwPair), cudaMemcpyHostToDevice, s),
             "H2D pairs");
-    SW_CUDA(cudaMemcpyAsync(E.d_tasks.p, E.h_tasks.p, (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice, s),
-            "H2D tasks");
-    SW_CUDA(cudaMemsetAsync(E.d_counters.p, 0, (size_t)n_cursors * sizeof(int64_t), s), "zero counters");
-    E.stats.h2d_bytes = plane_bytes + n * (int64_t)(sizeof(SwPair) + sizeof(int32_t));
+    E.stats.h2d_bytes = plane_bytes + 2 * n * (int64_t)sizeof(SwPair);
+    SwArgs A{};
+    A.ref_plane = in.ref_plane;
+    A.alt_plane = in.alt_plane;
+    A.match = in.params->match_value;
+    A.mismatch = in.params->mismatch_penalty;
+    A.open = in.params->gap_open_penalty;
+    A.extend = in.params->gap_extend_penalty;
+    A.strategy = in.strategy;
+    A.indel_edges = (in.strategy == kSwIndel || in.strategy == kSwLeadingIndel) ? 1 : 0;
+    A.shortcut = in.shortcut && (in.strategy == kSwSoftclip || in.strategy == kSwIgnore) ? 1 : 0;
+    A.pairs = E.d_pairs.p;
+    A.state = d_state;
+    A.offset = d_offset;
     int launches = 0;
-    int32_t *d_state = E.d_res.p, *d_offset = E.d_res.p + n, *d_nops = E.d_res.p + 2 * n, *d_best = E.d_res.p + 3 * n;
-    int *d_err = reinterpret_cast<int *>(E.d_counters.p + 1);
-    int *d_cursors = reinterpret_cast<int *>(E.d_counters.p + 2);
     E.stats.ms_host = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - in.t0).count();
     SW_CUDA(cudaEventRecord(E.event(0), s), "event");
+    // (1) haplotype choice, substring shortcut
     if (in.batch) {
         SwRealignArgs R{};
         if (in.priority) {
@@ -264,38 +297,101 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         if (e) return cuda_error(ctx, (cudaError_t)e, "realign setup launch");
         ++launches;
     }
-    SwArgs A{};
-    A.ref_plane = in.ref_plane;
-    A.alt_plane = in.alt_plane;
+    if (A.shortcut) {
+        const int e = launch_sw_prepass(A, (int)n, ci.sm_count, s);
+        if (e) return cuda_error(ctx, (cudaError_t)e, "substring shortcut launch");
+        ++launches;
+    } else {
+        SW_CUDA(cudaMemsetAsync(d_state, 0, (size_t)n * sizeof(int32_t), s), "zero states");
+    }
+    SW_CUDA(cudaEventRecord(E.event(1), s), "event");
+    SW_CUDA(cudaMemcpyAsync(E.h_res.p, d_state, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
+            "D2H shortcut states");
+    if (in.batch)
+        SW_CUDA(cudaMemcpyAsync(E.h_res.p + 3 * n, d_best, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
+                "D2H chosen haplotypes");
+    SW_CUDA(cudaStreamSynchronize(s), "substring shortcut");
+    const auto t_plan = std::chrono::steady_clock::now();
+    // (2) planning with exact lengths
+    if (in.batch) {  // each read's ref is the haplotype chosen on the device
+        const int64_t NR = in.batch->n_reads, NH = in.batch->n_haps;
+        const int64_t *hap_off = in.batch->h_off + NR + 1, *rro = hap_off + NH + 1, *rho = rro + in.batch->n_regions + 1;
+        const int32_t *best = E.h_res.p + 3 * n;
+        for (int64_t r = 0, g = 0; r < n; ++r) {
+            while (rro[g + 1] <= r) ++g;
+            SwPair &P = E.h_pairs.p[r];
+            if (best[r] < 0) {
+                P.ref_off = 0;
+                P.ref_len = 0;
+            } else {
+                const int64_t h = rho[g] + best[r];
+                P.ref_off = hap_off[h];
+                P.ref_len = (int32_t)(hap_off[h + 1] - hap_off[h]);
+            }
+        }
+    }
+    std::vector<Chunk> chunks;
+    SW_CUDA(E.h_tasks.reserve((size_t)std::max<int64_t>(n, 1)), "pinned tasks");
+    SW_CUDA(E.h_pair_tasks.reserve((size_t)std::max<int64_t>(n, 1)), "pinned pair tasks");
+    int64_t n_paired = 0;
+    plan(E.h_pairs.p, E.h_res.p, n, E.tb_budget_words, *in.params, in.strategy, E.allow16, chunks, E.h_tasks.p,
+         E.h_pair_tasks.p, &n_paired);
+    int64_t max_tb = 0, max_edges = 0, max_slots = 0, max_scratch = 0, n_tasks = 0, n_pair_tasks = 0;
+    int64_t max_ref = 0, max_alt = 0;
+    for (auto &c : chunks) {
+        max_tb = std::max(max_tb, c.tb_words);
+        max_edges = std::max(max_edges, c.edges);
+        max_slots = std::max(max_slots, c.slots);
+        max_scratch = std::max(max_scratch, c.scratch);
+        for (int k = 1; k <= kSwMaxK; ++k) {
+            n_tasks += c.task_count[k];
+            n_pair_tasks += c.pair_count[k];
+        }
+    }
+    for (int64_t i = 0; i < n; ++i)
+        if (E.h_res.p[i] == 0) {
+            max_ref = std::max<int64_t>(max_ref, E.h_pairs.p[i].ref_len);
+            max_alt = std::max<int64_t>(max_alt, E.h_pairs.p[i].alt_len);
+        }
+    A.clamp = needs_clamp(*in.params, in.strategy, max_ref, max_alt) ? 1 : 0;
+    const int64_t n_cursors = 2 + (int64_t)chunks.size() * 2 * kCursorsPerChunk;
+    SW_CUDA(E.d_tasks.reserve((size_t)std::max<int64_t>(n_tasks, 1)), "device tasks");
+    SW_CUDA(E.d_pair_tasks.reserve((size_t)std::max<int64_t>(n_pair_tasks, 1)), "device pair tasks");
+    SW_CUDA(E.d_counters.reserve((size_t)n_cursors), "device counters");
+    SW_CUDA(E.d_tb.reserve((size_t)std::max<int64_t>(max_tb, 1)), "traceback buffer");
+    SW_CUDA(E.d_edges.reserve((size_t)std::max<int64_t>(max_edges, 4)), "edge scores");
+    SW_CUDA(E.d_scratch.reserve((size_t)std::max<int64_t>(max_scratch, 1)), "strip scratch");
+    SW_CUDA(E.d_slot.reserve((size_t)std::max<int64_t>(max_slots, 1)), "cigar slots");
+    SW_CUDA(cudaMemcpyAsync(E.d_pairs.p, E.h_pairs.p, (size_t)n * sizeof(SwPair), cudaMemcpyHostToDevice, s),
+            "H2D planned pairs");
+    if (n_tasks)
+        SW_CUDA(cudaMemcpyAsync(E.d_tasks.p, E.h_tasks.p, (size_t)n_tasks * sizeof(int32_t), cudaMemcpyHostToDevice, s),
+                "H2D tasks");
+    if (n_pair_tasks)
+        SW_CUDA(cudaMemcpyAsync(E.d_pair_tasks.p, E.h_pair_tasks.p, (size_t)n_pair_tasks * sizeof(int2),
+                                cudaMemcpyHostToDevice, s), "H2D pair tasks");
+    SW_CUDA(cudaMemsetAsync(E.d_counters.p, 0, (size_t)n_cursors * sizeof(int64_t), s), "zero counters");
+    E.stats.h2d_bytes += n_tasks * 4 + n_pair_tasks * 8;
+    E.stats.ms_host += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_plan).count();
+    int *d_err = reinterpret_cast<int *>(E.d_counters.p + 1);
+    int *d_cursors = reinterpret_cast<int *>(E.d_counters.p + 2);
     A.tb = E.d_tb.p;
     A.edges = E.d_edges.p;
     A.strip_scratch = E.d_scratch.p;
     A.slot = E.d_slot.p;
     A.error = d_err;
-    A.match = in.params->match_value;
-    A.mismatch = in.params->mismatch_penalty;
-    A.open = in.params->gap_open_penalty;
-    A.extend = in.params->gap_extend_penalty;
-    A.strategy = in.strategy;
-    A.indel_edges = (in.strategy == kSwIndel || in.strategy == kSwLeadingIndel) ? 1 : 0;
-    A.shortcut = in.shortcut && (in.strategy == kSwSoftclip || in.strategy == kSwIgnore) ? 1 : 0;
-    {
-        int64_t max_ref = 0, max_alt = 0;
-        for (int64_t i = 0; i < n; ++i) {
-            max_ref = std::max<int64_t>(max_ref, in.ref_bound[i]);
-            max_alt = std::max<int64_t>(max_alt, E.h_pairs.p[i].alt_len);
-        }
-        A.clamp = needs_clamp(*in.params, in.strategy, max_ref, max_alt) ? 1 : 0;
-        E.stats_clamp = A.clamp;
-    }
-    int occ[kSwMaxK + 1]{};
+    int occ[kSwMaxK + 1]{}, occ16[kSwMaxK + 1]{};
     for (int k = 1; k <= kSwMaxK; ++k) {
-        int b = 0;
-        const int e = sw_forward_occupancy(k, &b);
+        int b = 0, b16 = 0;
+        int e = sw_forward_occupancy(k, &b);
+        if (!e) e = sw_pair16_occupancy(k, &b16);
         if (e) return cuda_error(ctx, (cudaError_t)e, "occupancy");
         occ[k] = std::max(b, 1);
+        occ16[k] = std::max(b16, 1);
     }
-    size_t ev = 1;
+    // (3) per chunk
+    SW_CUDA(cudaEventRecord(E.event(2), s), "event");
+    size_t ev = 3;
     std::vector<std::pair<size_t, size_t>> fwd_events;
     for (size_t c = 0; c < chunks.size(); ++c) {
         const Chunk &ch = chunks[c];
@@ -307,13 +403,21 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         a.n_ops = d_nops + ch.p0;
         const size_t e0 = ev++, e1 = ev++;
         SW_CUDA(cudaEventRecord(E.event(e0), s), "event");
+        int *cur = d_cursors + c * 2 * kCursorsPerChunk;
+        for (int k = kSwMaxK; k >= 1; --k) {
+            const int64_t cnt = ch.pair_count[k];
+            if (!cnt) continue;
+            const int grid = (int)std::min<int64_t>((cnt + 3) / 4, (int64_t)occ16[k] * ci.sm_count);
+            const int e = launch_sw_pair16(a, k, E.d_pair_tasks.p + ch.pair_begin[k], (int)cnt, cur + kCursorsPerChunk + k,
+                                           grid, s);
+            if (e) return cuda_error(ctx, (cudaError_t)e, "Smith-Waterman paired forward launch");
+            ++launches;
+        }
         for (int k = kSwMaxK; k >= 1; --k) {
             const int64_t cnt = ch.task_count[k];
             if (!cnt) continue;
-            const int64_t want = (cnt + 3) / 4;
-            const int grid = (int)std::min<int64_t>(want, (int64_t)occ[k] * ci.sm_count);
-            const int e = launch_sw_forward(a, k, E.d_tasks.p + ch.task_begin[k], (int)cnt,
-                                            d_cursors + c * kCursorsPerChunk + k, grid, s);
+            const int grid = (int)std::min<int64_t>((cnt + 3) / 4, (int64_t)occ[k] * ci.sm_count);
+            const int e = launch_sw_forward(a, k, E.d_tasks.p + ch.task_begin[k], (int)cnt, cur + k, grid, s);
             if (e) return cuda_error(ctx, (cudaError_t)e, "Smith-Waterman forward launch");
             ++launches;
         }
@@ -327,7 +431,7 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
     }
     const size_t ev_end = ev++;
     SW_CUDA(cudaEventRecord(E.event(ev_end), s), "event");
-    SW_CUDA(cudaMemcpyAsync(E.h_res.p, E.d_res.p, (size_t)n * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
+    SW_CUDA(cudaMemcpyAsync(E.h_res.p + n, d_offset, (size_t)n * 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
             "D2H results");
     SW_CUDA(cudaMemcpyAsync(E.h_starts.p, E.d_starts.p, (size_t)n * sizeof(int64_t), cudaMemcpyDeviceToHost, s),
             "D2H cigar starts");
@@ -352,9 +456,10 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         SW_CUDA(cudaStreamSynchronize(s), "D2H cigar ops");
     }
     E.stats.d2h_bytes += total * (int64_t)sizeof(uint32_t);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, E.event(0), E.event(ev_end));
-    E.stats.ms_device = ms;
+    float ms_pre = 0, ms_main = 0;  // device time, without the host planning between the two phases
+    cudaEventElapsedTime(&ms_pre, E.event(0), E.event(1));
+    cudaEventElapsedTime(&ms_main, E.event(2), E.event(ev_end));
+    E.stats.ms_device = ms_pre + ms_main;
     double fwd = 0;
     for (auto &fe : fwd_events) {
         float m = 0;
@@ -365,6 +470,7 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
     E.stats.chunks = (int32_t)chunks.size();
     E.stats.launches = launches;
     E.stats.n_alignments = n;
+    E.stats.n_int16 = n_paired;
     return GHMM_OK;
 }
 
@@ -472,7 +578,6 @@ int sw_batch(ghmm_ctx *ctx, const CtxInfo &ci, const ghmm_sw_pair *pairs, int64_
     in.strategy = strategy;
     in.shortcut = (flags & GHMM_SW_SUBSTRING_SHORTCUT) ? 1 : 0;
     in.n = n;
-    in.ref_bound = ref_len.data();
     in.ops_cap = res->cigar_cap;
     in.t0 = t0;
     int rc = run(ctx, ci, E, in, plane_bytes, nullptr);
@@ -564,23 +669,14 @@ int ghmm_batch_realign(ghmm_ctx *ctx, ghmm_batch *batch, const double *hap_prior
     SwEngine &E = *engine(ci);
     E.stats = ghmm_sw_stats{};
     SW_CUDA(cudaSetDevice(ci.device), "cudaSetDevice");
-    const int64_t NR = n, NH = bi.n_haps, G = bi.n_regions;
-    const int64_t *read_off = bi.h_off, *hap_off = read_off + NR + 1, *rro = hap_off + NH + 1, *rho = rro + G + 1;
+    const int64_t *read_off = bi.h_off;
     SW_CUDA(E.h_pairs.reserve((size_t)n), "pinned pairs");
-    // buffers of each read sized by the longest haplotype of its region; reads of regions without haplotypes
-    // get no alignment (the setup kernel marks them, the forward skips them through an empty task list)
-    std::vector<int32_t> bound((size_t)n);
-    for (int64_t g = 0; g < G; ++g) {
-        int32_t hmax = 0;
-        for (int64_t h = rho[g]; h < rho[g + 1]; ++h) hmax = std::max<int32_t>(hmax, (int32_t)(hap_off[h + 1] - hap_off[h]));
-        for (int64_t r = rro[g]; r < rro[g + 1]; ++r) {
-            SwPair &P = E.h_pairs.p[r];
-            P = SwPair{};
-            P.alt_off = read_off[r];
-            P.alt_len = (int32_t)(read_off[r + 1] - read_off[r]);
-            P.ref_len = 0;
-            bound[(size_t)r] = hmax;
-        }
+    // the reads; their haplotypes are chosen on the device (reads of a region without haplotypes are not aligned)
+    for (int64_t r = 0; r < n; ++r) {
+        SwPair &P = E.h_pairs.p[r];
+        P = SwPair{};
+        P.alt_off = read_off[r];
+        P.alt_len = (int32_t)(read_off[r + 1] - read_off[r]);
     }
     for (int64_t r = 0; r < n; ++r)
         if (E.h_pairs.p[r].alt_len <= 0)
@@ -593,7 +689,6 @@ int ghmm_batch_realign(ghmm_ctx *ctx, ghmm_batch *batch, const double *hap_prior
     in.strategy = kSwSoftclip;
     in.shortcut = 1;
     in.n = n;
-    in.ref_bound = bound.data();
     in.ops_cap = result->cigar_cap;
     in.batch = &bi;
     in.priority = hap_priority;
@@ -603,18 +698,22 @@ int ghmm_batch_realign(ghmm_ctx *ctx, ghmm_batch *batch, const double *hap_prior
     if (rc) return rc;
     const int32_t *best = E.h_res.p + 3 * n;
     std::vector<int32_t> ref_len((size_t)n);
-    // the chosen haplotype's length per read, for the cell count
-    for (int64_t r = 0, g = 0; r < n; ++r) {
+    for (int64_t r = 0; r < n; ++r) {
         best_hap[r] = best[r];
         informative[r] = inf[(size_t)r];
-        while (rro[g + 1] <= r) ++g;
-        const int64_t h = rho[g] + best[r];
-        ref_len[(size_t)r] = best[r] < 0 ? 0 : (int32_t)(hap_off[h + 1] - hap_off[h]);
+        ref_len[(size_t)r] = E.h_pairs.p[r].ref_len;  // the chosen haplotype's length (0: not aligned)
     }
     rc = deliver(ctx, E, n, ref_len.data(), result);
     E.stats.d2h_bytes += n * (int64_t)sizeof(int32_t);
     E.stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return rc;
+}
+
+int ghmm_sw_set_options(ghmm_ctx *ctx, int32_t flags) {
+    CtxInfo ci;
+    if (ctx_info(ctx, &ci)) return GHMM_ERR_STATE;
+    engine(ci)->allow16 = !(flags & GHMM_SW_OPT_INT32_ONLY);
+    return GHMM_OK;
 }
 
 int ghmm_sw_set_traceback_budget(ghmm_ctx *ctx, int64_t bytes) {

@@ -151,6 +151,7 @@ SW_SOFTCLIP, SW_INDEL, SW_LEADING_INDEL, SW_IGNORE = 0, 1, 2, 3
 SW_SUBSTRING_SHORTCUT = 1
 CIGAR_M, CIGAR_I, CIGAR_D, CIGAR_S = 0, 1, 2, 4
 SW_MAX_LEN = 1 << 20
+SW_OPT_INT32_ONLY = 1
 
 
 class SwParams(ctypes.Structure):
@@ -173,7 +174,7 @@ class SwStats(ctypes.Structure):
     _fields_ = [("n_alignments", ctypes.c_int64), ("n_shortcut", ctypes.c_int64), ("cells", ctypes.c_int64),
                 ("chunks", ctypes.c_int32), ("launches", ctypes.c_int32), ("ms_device", ctypes.c_double),
                 ("ms_forward", ctypes.c_double), ("ms_total", ctypes.c_double), ("h2d_bytes", ctypes.c_int64),
-                ("d2h_bytes", ctypes.c_int64), ("ms_host", ctypes.c_double)]
+                ("d2h_bytes", ctypes.c_int64), ("ms_host", ctypes.c_double), ("n_int16", ctypes.c_int64)]
 
 
 # Every exported symbol and its signature (restype, argtypes).  The tests check that the library
@@ -241,6 +242,7 @@ _SIGS = {
     "ghmm_sw_last_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SwStats)]),
     "ghmm_sw_set_traceback_budget": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
     "ghmm_sw_measure_peak": (ctypes.c_int, [ctypes.c_void_p, _f64p]),
+    "ghmm_sw_set_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
 }
 
 _lib = None

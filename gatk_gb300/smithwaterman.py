@@ -175,6 +175,10 @@ class SmithWatermanCudaAligner:
         native.check(self._ctx.L.ghmm_sw_measure_peak(self._ctx.h, ctypes.byref(v)), self._ctx.h)
         return v.value
 
+    def set_int32_only(self, on: bool = True) -> None:
+        """Run every alignment in the int32 kernel (by default bounded ones run two per warp in 16 bits)."""
+        native.check(self._ctx.L.ghmm_sw_set_options(self._ctx.h, native.SW_OPT_INT32_ONLY if on else 0), self._ctx.h)
+
     def set_traceback_budget(self, nbytes: int) -> None:
         native.check(self._ctx.L.ghmm_sw_set_traceback_budget(self._ctx.h, int(nbytes)), self._ctx.h)
 

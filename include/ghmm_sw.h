@@ -97,11 +97,12 @@ typedef struct ghmm_sw_stats {
     int64_t cells;         /* ref_len x alt_len summed over the alignments that ran the score recurrence */
     int32_t chunks;        /* passes over the traceback buffer */
     int32_t launches;      /* kernels launched */
-    double ms_device;      /* first to last kernel, CUDA events */
+    double ms_device;      /* device time of the kernels (CUDA events), without the host planning between phases */
     double ms_forward;     /* summed time of the score-recurrence kernels */
     double ms_total;       /* wall time of the call */
     int64_t h2d_bytes, d2h_bytes;
-    double ms_host;        /* host time before the first launch: checks, marshalling, chunk and task planning */
+    double ms_host;        /* host time: checks, marshalling, chunk and task planning */
+    int64_t n_int16;       /* alignments run two per warp in 16-bit halves (the rest in int32) */
 } ghmm_sw_stats;
 
 /* SWAlignerNativeBinding.align: the cigar as text into cigar[cigar_cap] (NUL-terminated; GHMM_ERR_ARG when
@@ -133,6 +134,12 @@ int ghmm_sw_last_stats(ghmm_ctx *ctx, ghmm_sw_stats *stats);
  * call whose alignments need more runs in several passes over the buffer; a single alignment larger than the
  * budget gets a pass of its own.  Values below 1 MiB are raised to 1 MiB. */
 int ghmm_sw_set_traceback_budget(ghmm_ctx *ctx, int64_t bytes);
+
+/* Kernel choice.  By default alignments whose scores provably fit in 16 bits (bounded by the sequence lengths and
+ * parameters) run two per warp in the 16-bit halves of each register, the rest in int32; results are identical.
+ * GHMM_SW_OPT_INT32_ONLY runs everything in int32. */
+#define GHMM_SW_OPT_INT32_ONLY 1
+int ghmm_sw_set_options(ghmm_ctx *ctx, int32_t flags);
 
 /* Measured int32 max/compare throughput of the device in Tops/s: a register-resident loop of independent max.s32
  * chains over all SMs, timed with CUDA events.  The roofline denominator of the score recurrence, whose cells are

@@ -254,3 +254,31 @@ def test_realign_after_postprocess_uses_the_normalised_likelihoods(engine):
     np.testing.assert_array_equal(best, exp_best)
     np.testing.assert_array_equal(inf, exp_inf)
     _assert_same(got, refs, alts, S.ALIGNMENT_TO_BEST_HAPLOTYPE_SW_PARAMETERS, S.SOFTCLIP, True)
+
+
+def test_int16_pairs_and_int32_give_the_oracle_alignments():
+    # bounded alignments run two per warp in 16-bit halves by default; the int32-only option runs the same ones
+    # one per warp; both must equal the oracle (an odd number per width leaves a half empty)
+    rng = random.Random(31)
+    refs, alts = _pairs(rng, 501, (40, 620), (1, 256))
+    params = S.ALIGNMENT_TO_BEST_HAPLOTYPE_SW_PARAMETERS
+    with SWG.SmithWatermanCudaAligner() as a:
+        for st in (S.SOFTCLIP, S.INDEL):
+            a.set_int32_only(False)
+            got16 = a.align_many(refs, alts, SWG.SWParameters(*params), SWG.SWOverhangStrategy(st))
+            s16 = a.last_stats()
+            a.set_int32_only(True)
+            got32 = a.align_many(refs, alts, SWG.SWParameters(*params), SWG.SWOverhangStrategy(st))
+            s32 = a.last_stats()
+            assert s16["n_int16"] > 300 and s32["n_int16"] == 0
+            _assert_same(got16, refs, alts, params, st, True)
+            _assert_same(got32, refs, alts, params, st, True)
+
+
+def test_unbounded_scores_stay_in_int32(aligner):
+    # NEW_SW_PARAMETERS' match value of 200 over a 256-column alt could leave the 16-bit range: int32 kernel
+    rng = random.Random(32)
+    refs, alts = _pairs(rng, 60, (300, 500), (200, 256))
+    got = aligner.align_many(refs, alts, SWG.NEW_SW_PARAMETERS, SWG.SWOverhangStrategy.SOFTCLIP, False)
+    assert aligner.last_stats()["n_int16"] == 0
+    _assert_same(got, refs, alts, S.NEW_SW_PARAMETERS, S.SOFTCLIP, False)

@@ -54,6 +54,7 @@ def test_header_constants_match_the_bindings():
     for op in "MIDS":
         assert int(swd[f"GHMM_CIGAR_{op}"]) == getattr(native, f"CIGAR_{op}")
     assert "#define GHMM_SW_MAX_LEN (1 << 20)" in sw and native.SW_MAX_LEN == 1 << 20
+    assert int(swd["GHMM_SW_OPT_INT32_ONLY"]) == native.SW_OPT_INT32_ONLY
 
 
 def test_struct_layouts_match_the_header(tmp_path):
