@@ -143,8 +143,8 @@ constexpr int kSwMaxK = 8;  // alt columns per lane; longer alts run in strips o
 struct SwPair {
     int64_t ref_off, alt_off;
     int64_t tb_off;       // first traceback word: strips x (ref_len + 31) steps x 32 lanes
-    int64_t edge_off;     // ref_len rows of the last-column lane's kSwRowStride(k) scores, then alt_len bottom-row
-                          // scores (a multiple of 4 ints, so the rows are int4-aligned)
+    int64_t edge_off;     // ref_len rows of the last-column lane's kSwRowStride(k) scores, then the bottom row as
+                          // one row of kSwRowStride(k) per lane and strip (a multiple of 4 ints: int4-aligned rows)
     int64_t slot_off;     // 2 * alt_len + 4 cigar ops, written in reverse by the traceback
     int64_t scratch_off;  // strip boundary (score, horizontal gap) per ref row 0..ref_len, multi-strip alts only
     int32_t ref_len, alt_len;
@@ -158,7 +158,8 @@ struct SwArgs {
     int *edges;
     int2 *strip_scratch;
     uint32_t *slot;
-    int32_t *state;       // 1: solved by the exact-substring shortcut
+    int32_t *state;       // 1: solved by the exact-substring shortcut; 0: int32 recurrence; 2 / 3: 16-bit pair, low /
+                          // high half (the 16-bit kernel sets them)
     int32_t *offset;      // alignment offset
     int32_t *n_ops;
     int *error;           // set when a traceback overruns its slot (cannot happen for valid input)

@@ -57,6 +57,16 @@ __device__ int warp_last_index_of(const uint8_t *ref, int n, const uint8_t *alt,
     return -1;
 }
 
+// K words to a 16-byte-aligned row (K rounded up to whole int4s)
+template <int K, typename T>
+__device__ __forceinline__ void store_row(int *dst, const T (&w)[K]) {
+#pragma unroll
+    for (int q = 0; q < K; q += 4)
+        reinterpret_cast<int4 *>(dst)[q / 4] =
+            make_int4((int)w[q], q + 1 < K ? (int)w[q + 1 < K ? q + 1 : 0] : 0, q + 2 < K ? (int)w[q + 2 < K ? q + 2 : 0] : 0,
+                      q + 3 < K ? (int)w[q + 3 < K ? q + 3 : 0] : 0);
+}
+
 // bits |= mask when a > b (a >= b): one compare and one predicated OR
 __device__ __forceinline__ void or_if_gt(uint32_t &bits, int a, int b, uint32_t mask) {
     asm("{\n\t.reg .pred p;\n\tsetp.gt.s32 p, %1, %2;\n\t@p or.b32 %0, %0, %3;\n\t}"
@@ -142,14 +152,7 @@ __device__ __forceinline__ void sw_step(const StripCtx &C, LaneState<K> &L, int 
         hl = hno;
     }
     C.tb[(int64_t)t * 32] = bits;
-    if (C.owns_last) {
-        int4 *row = reinterpret_cast<int4 *>(C.lastrow + (int64_t)(i - 1) * kSwRowStride(K));
-#pragma unroll
-        for (int q = 0; q < K; q += 4)
-            row[q / 4] = make_int4(L.hup[q], q + 1 < K ? L.hup[q + 1 < K ? q + 1 : 0] : 0,
-                                   q + 2 < K ? L.hup[q + 2 < K ? q + 2 : 0] : 0,
-                                   q + 3 < K ? L.hup[q + 3 < K ? q + 3 : 0] : 0);
-    }
+    if (C.owns_last) store_row<K>(C.lastrow + (int64_t)(i - 1) * kSwRowStride(K), L.hup);
     if (C.strip_out && lane == 31) C.strip_out[i] = make_int2(hl, bh);
     L.send_h = hl;
     L.send_b = bh;
@@ -197,13 +200,8 @@ __device__ __forceinline__ void sw_strip(const SwArgs &A, const SwPair &P, int s
 #pragma unroll 4
     for (; t < n; ++t) sw_step<K, CLAMP, false>(C, L, t, lane);  // every lane inside the matrix
     for (; t < n + 31; ++t) sw_step<K, CLAMP, true>(C, L, t, lane);
-    // the lanes finish on row n: their scores are the bottom row
-    int *bottom = A.edges + P.edge_off + (int64_t)n * kSwRowStride(K);  // H[n][j] + open at bottom[j-1]
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const int j = jbase + k + 1;
-        if (j <= m) bottom[j - 1] = L.hup[k];
-    }
+    // the lanes finish on row n: their scores (+ open) are the bottom row, one row of kSwRowStride(K) per lane
+    store_row<K>(A.edges + P.edge_off + ((int64_t)n + s * 32 + lane) * kSwRowStride(K), L.hup);
     __syncwarp();
 }
 
@@ -243,22 +241,11 @@ __device__ __forceinline__ uint32_t addc16(int c) { return (uint32_t)c * 0x10001
 __device__ __forceinline__ int lo16(uint32_t w) { return (int)(w & 0xffffu) - 32768; }
 __device__ __forceinline__ int hi16(uint32_t w) { return (int)(w >> 16) - 32768; }
 
-template <int K>
-__device__ __forceinline__ void store_row16(int *dst, const uint32_t (&w)[K], bool high) {
-#pragma unroll
-    for (int q = 0; q < K; q += 4) {
-        int v[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) v[r] = q + r < K ? (high ? hi16(w[q + r < K ? q + r : 0]) : lo16(w[q + r < K ? q + r : 0])) : 0;
-        reinterpret_cast<int4 *>(dst)[q / 4] = make_int4(v[0], v[1], v[2], v[3]);
-    }
-}
-
 struct Pair16Ctx {
     const uint8_t *ref_a, *ref_b;
     uint32_t *tb_a, *tb_b;     // this lane's traceback word of step 0 in each alignment's own layout
-    int *last_a, *last_b;      // rows of the lane holding each alignment's last column (H + open, int32)
-    int *bottom_a, *bottom_b;  // each alignment's bottom row (H + open), this lane's first column
+    int *last_a, *last_b;      // rows of the lane holding each alignment's last column (the lane's raw words)
+    int *bottom_a, *bottom_b;  // each alignment's bottom row, this lane's raw words
     int n_a, n_b, n, m_a, m_b, jbase;
     uint32_t ext2, open2, mo2, inject_const;
     int dm, open, ext;
@@ -321,18 +308,11 @@ __device__ __forceinline__ void pair16_step(const Pair16Ctx &C, Lane16<K> &L, in
     const uint32_t wb = __byte_perm(bits0, bits1, 0x7632) ^ 0x22222222u;
     if (t < C.n_a + 31) C.tb_a[(int64_t)t * 32] = wa;
     if (C.has_b && t < C.n_b + 31) C.tb_b[(int64_t)t * 32] = wb;
-    if (C.owns_a && i <= C.n_a) store_row16<K>(C.last_a + (int64_t)(i - 1) * kSwRowStride(K), L.hup, false);
-    if (C.owns_b && i <= C.n_b) store_row16<K>(C.last_b + (int64_t)(i - 1) * kSwRowStride(K), L.hup, true);
-    if (i == C.n_a) {
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (C.jbase + k < C.m_a) C.bottom_a[k] = lo16(L.hup[k]);
-    }
-    if (C.has_b && i == C.n_b) {
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (C.jbase + k < C.m_b) C.bottom_b[k] = hi16(L.hup[k]);
-    }
+    // raw 16-bit pairs; the traceback takes its alignment's half (state 2: low, 3: high)
+    if (C.owns_a && i <= C.n_a) store_row<K>(C.last_a + (int64_t)(i - 1) * kSwRowStride(K), L.hup);
+    if (C.owns_b && i <= C.n_b) store_row<K>(C.last_b + (int64_t)(i - 1) * kSwRowStride(K), L.hup);
+    if (i == C.n_a) store_row<K>(C.bottom_a, L.hup);
+    if (C.has_b && i == C.n_b) store_row<K>(C.bottom_b, L.hup);
     L.send_h = hl;
     L.send_b = bh;
     L.hdiag = h_left;
@@ -340,7 +320,7 @@ __device__ __forceinline__ void pair16_step(const Pair16Ctx &C, Lane16<K> &L, in
 
 // tasks: (alignment A, alignment B or -1) of single-strip alignments with the same K, B's ref no longer than A's
 template <int K>
-__global__ void __launch_bounds__(128) sw_pair16_kernel(SwArgs A, const int2 *tasks, int n_tasks, int *cursor) {
+__global__ void __launch_bounds__(128, 6) sw_pair16_kernel(SwArgs A, const int2 *tasks, int n_tasks, int *cursor) {
     const int lane = threadIdx.x & 31;
     for (;;) {
         int task = 0;
@@ -376,8 +356,12 @@ __global__ void __launch_bounds__(128) sw_pair16_kernel(SwArgs A, const int2 *ta
         C.owns_b = has_b && km_b >= 0 && km_b < K;
         C.last_a = A.edges + PA.edge_off;
         C.last_b = A.edges + PB.edge_off;
-        C.bottom_a = A.edges + PA.edge_off + (int64_t)C.n_a * kSwRowStride(K) + C.jbase;
-        C.bottom_b = A.edges + PB.edge_off + (int64_t)C.n_b * kSwRowStride(K) + C.jbase;
+        C.bottom_a = A.edges + PA.edge_off + ((int64_t)C.n_a + lane) * kSwRowStride(K);
+        C.bottom_b = A.edges + PB.edge_off + ((int64_t)C.n_b + lane) * kSwRowStride(K);
+        if (lane == 0) {
+            A.state[tk.x] = 2;
+            if (has_b) A.state[tk.y] = 3;
+        }
         const uint8_t *alt_a = A.alt_plane + PA.alt_off, *alt_b = A.alt_plane + PB.alt_off;
         Lane16<K> L;
 #pragma unroll
@@ -449,7 +433,14 @@ __global__ void sw_traceback_kernel(SwArgs A, int n_pairs) {
     const int K = P.k;
     const int stride = kSwRowStride(K);
     const int km = (m - 1) % (32 * K) % K;  // the last column's place among its lane's columns
+    const int st = A.state[p];              // 0: int32 scores; 2 / 3: 16-bit pairs, low / high half
     const int *lastcol = A.edges + P.edge_off + km, *bottom = A.edges + P.edge_off + (int64_t)n * stride;
+    // a stored score (H + open, or its biased 16-bit half) back to H
+    auto score = [&](int w) -> int {
+        if (st == 2) w = lo16((uint32_t)w);
+        else if (st == 3) w = hi16((uint32_t)w);
+        return wsub(w, A.open);
+    };
     int p1 = 0, p2 = 0;
     int maxscore = INT32_MIN;
     int segment = 0;
@@ -459,7 +450,7 @@ __global__ void sw_traceback_kernel(SwArgs A, int n_pairs) {
     } else {
         p2 = m;
         for (int i = 1; i <= n; ++i) {
-            const int sc = wsub(lastcol[(int64_t)(i - 1) * stride], A.open);  // stored as H + open
+            const int sc = score(lastcol[(int64_t)(i - 1) * stride]);
             if (sc >= maxscore) {
                 p1 = i;
                 maxscore = sc;
@@ -467,7 +458,7 @@ __global__ void sw_traceback_kernel(SwArgs A, int n_pairs) {
         }
         if (A.strategy != kSwLeadingIndel) {
             for (int j = 1; j <= m; ++j) {
-                const int sc = wsub(bottom[j - 1], A.open);
+                const int sc = score(bottom[(int64_t)((j - 1) / K) * stride + (j - 1) % K]);
                 const int dn = n - j < 0 ? j - n : n - j, dc = p1 - p2 < 0 ? p2 - p1 : p1 - p2;
                 if (sc > maxscore || (sc == maxscore && dn < dc)) {
                     p1 = n;

@@ -125,15 +125,16 @@ bool fits16(const ghmm_sw_params &p, int strategy, int64_t n, int k) {
     return hmin - slack >= -28000 && hmax + slack <= 28000;
 }
 
-// Buffer offsets (chunk-relative) of every alignment that runs the recurrence (state 0, ref_len > 0), chunk
-// boundaries over contiguous alignment ranges, and per chunk and K: the int32 kernel's tasks (longest ref first)
-// and the 16-bit kernel's pairs (neighbours in ref-length order, so the two halves of a warp finish together).
-void plan(SwPair *pairs, const int32_t *state, int64_t n, int64_t budget_words, const ghmm_sw_params &prm,
-          int strategy, bool allow16, std::vector<Chunk> &chunks, int32_t *tasks, int2 *pair_tasks,
-          int64_t *n_paired) {
+// Buffer offsets (chunk-relative) of every alignment that runs the recurrence (state 0, ref_len > 0), which of
+// them take the 16-bit kernel, and chunk boundaries over contiguous alignment ranges.
+// keys[i]: the alignment's task bucket (kernel * 9 + K) << 21 | ref length, or kNoTask.
+constexpr uint32_t kNoTask = 0xffffffffu;
+
+void plan_offsets(SwPair *pairs, const int32_t *state, int64_t n, int64_t budget_words, const ghmm_sw_params &prm,
+                  int strategy, bool allow16, std::vector<Chunk> &chunks, std::vector<uint32_t> &keys) {
     chunks.clear();
+    keys.assign((size_t)n, kNoTask);
     Chunk c;
-    std::vector<uint8_t> use16((size_t)n, 0);
     for (int64_t i = 0; i < n; ++i) {
         SwPair &P = pairs[i];
         const bool runs = state[i] == 0 && P.ref_len > 0;
@@ -161,52 +162,61 @@ void plan(SwPair *pairs, const int32_t *state, int64_t n, int64_t budget_words, 
         P.slot_off = c.slots;
         P.scratch_off = strips > 1 ? c.scratch : -1;
         c.tb_words += words;
-        c.edges += (rb * kSwRowStride(k) + P.alt_len + 3) / 4 * 4;  // int4-aligned rows
+        c.edges += (rb + strips * 32) * kSwRowStride(k);  // last-column rows, then one bottom row per lane
         c.slots += 2 * (int64_t)P.alt_len + 4;
         if (strips > 1) c.scratch += rb + 1;
-        use16[(size_t)i] = allow16 && strips == 1 && fits16(prm, strategy, rb, k);
+        const uint32_t kind = allow16 && strips == 1 && fits16(prm, strategy, rb, k) ? 1u : 0u;
+        keys[(size_t)i] = ((kind * (kSwMaxK + 1) + (uint32_t)k) << 21) | (uint32_t)rb;
     }
     c.p1 = n;
     if (n > 0) chunks.push_back(c);
-    // a stable counting sort on the ref length, longest first, per chunk and K and kernel
-    int64_t pos = 0, ppos = 0, paired = 0;
-    std::vector<int32_t> count, by_k[2][kSwMaxK + 1], sorted;
-    for (auto &ch : chunks) {
-        for (auto &kk : by_k)
-            for (auto &v : kk) v.clear();
-        for (int64_t i = ch.p0; i < ch.p1; ++i)
-            if (state[i] == 0 && pairs[i].ref_len > 0) by_k[use16[(size_t)i]][pairs[i].k].push_back((int32_t)(i - ch.p0));
-        for (int kind = 0; kind < 2; ++kind) {
-            for (int k = kSwMaxK; k >= 1; --k) {
-                const std::vector<int32_t> &v = by_k[kind][k];
-                int32_t kmax = 0;
-                for (int32_t q : v) kmax = std::max(kmax, pairs[ch.p0 + q].ref_len);
-                count.assign((size_t)kmax + 2, 0);
-                for (int32_t q : v) ++count[(size_t)(kmax - pairs[ch.p0 + q].ref_len)];
-                int32_t run = 0;
-                for (auto &cc : count) {
-                    const int32_t x = cc;
-                    cc = run;
-                    run += x;
-                }
-                sorted.resize(v.size());
-                for (int32_t q : v) sorted[(size_t)count[(size_t)(kmax - pairs[ch.p0 + q].ref_len)]++] = q;
-                if (kind == 0) {
-                    ch.task_begin[k] = pos;
-                    ch.task_count[k] = (int64_t)sorted.size();
-                    std::copy(sorted.begin(), sorted.end(), tasks + pos);
-                    pos += (int64_t)sorted.size();
-                } else {
-                    ch.pair_begin[k] = ppos;
-                    ch.pair_count[k] = ((int64_t)sorted.size() + 1) / 2;
-                    for (size_t q = 0; q < sorted.size(); q += 2)
-                        pair_tasks[ppos++] = make_int2(sorted[q], q + 1 < sorted.size() ? sorted[q + 1] : -1);
-                    paired += (int64_t)sorted.size();
-                }
-            }
+}
+
+// One chunk's tasks, at positions p0.. of the task arrays: per K the int32 kernel's alignments (longest ref first)
+// and the 16-bit kernel's pairs (neighbours in ref-length order, so the two halves of a warp finish together).  One
+// stable counting sort on (kernel, K, descending ref length).  Returns the number of alignments paired.
+int64_t plan_tasks(const std::vector<uint32_t> &keys, Chunk &ch, int32_t *tasks, int2 *pair_tasks) {
+    constexpr int kBuckets = 2 * (kSwMaxK + 1);
+    const uint32_t *kk = keys.data();
+    uint32_t lmax = 0;
+    for (int64_t i = ch.p0; i < ch.p1; ++i)
+        if (kk[i] != kNoTask) lmax = std::max(lmax, kk[i] & 0x1fffffu);
+    const int64_t L = (int64_t)lmax + 1;
+    std::vector<int32_t> count((size_t)(kBuckets * L + 1), 0);
+    auto key = [&](uint32_t x) { return (int64_t)(x >> 21) * L + (int64_t)(lmax - (x & 0x1fffffu)); };
+    int64_t runs = 0;
+    for (int64_t i = ch.p0; i < ch.p1; ++i)
+        if (kk[i] != kNoTask) {
+            ++count[(size_t)key(kk[i])];
+            ++runs;
         }
+    int32_t acc = 0;
+    for (auto &c : count) {
+        const int32_t x = c;
+        c = acc;
+        acc += x;
     }
-    *n_paired = paired;
+    std::vector<int32_t> bucket_start(kBuckets + 1);
+    for (int b = 0; b <= kBuckets; ++b) bucket_start[(size_t)b] = b < kBuckets ? count[(size_t)(b * L)] : (int32_t)runs;
+    std::vector<int32_t> order((size_t)std::max<int64_t>(runs, 1));
+    for (int64_t i = ch.p0; i < ch.p1; ++i)
+        if (kk[i] != kNoTask) order[(size_t)count[(size_t)key(kk[i])]++] = (int32_t)(i - ch.p0);
+    int64_t pos = ch.p0, ppos = ch.p0, paired = 0;
+    for (int k = kSwMaxK; k >= 1; --k) {  // int32 kernel
+        const int32_t b0 = bucket_start[(size_t)k], b1 = bucket_start[(size_t)k + 1];
+        ch.task_begin[k] = pos;
+        ch.task_count[k] = b1 - b0;
+        std::copy(order.begin() + b0, order.begin() + b1, tasks + pos);
+        pos += b1 - b0;
+    }
+    for (int k = kSwMaxK; k >= 1; --k) {  // 16-bit kernel
+        const int32_t b0 = bucket_start[(size_t)(kSwMaxK + 1 + k)], b1 = bucket_start[(size_t)(kSwMaxK + 2 + k)];
+        ch.pair_begin[k] = ppos;
+        ch.pair_count[k] = (b1 - b0 + 1) / 2;
+        for (int32_t q = b0; q < b1; q += 2) pair_tasks[ppos++] = make_int2(order[(size_t)q], q + 1 < b1 ? order[(size_t)q + 1] : -1);
+        paired += b1 - b0;
+    }
+    return paired;
 }
 
 // Whether any score of these alignments can reach MATRIX_MIN_CUTOFF (or wrap): along the diagonal every score is
@@ -331,22 +341,16 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         }
     }
     std::vector<Chunk> chunks;
+    std::vector<uint32_t> keys;
     SW_CUDA(E.h_tasks.reserve((size_t)std::max<int64_t>(n, 1)), "pinned tasks");
     SW_CUDA(E.h_pair_tasks.reserve((size_t)std::max<int64_t>(n, 1)), "pinned pair tasks");
-    int64_t n_paired = 0;
-    plan(E.h_pairs.p, E.h_res.p, n, E.tb_budget_words, *in.params, in.strategy, E.allow16, chunks, E.h_tasks.p,
-         E.h_pair_tasks.p, &n_paired);
-    int64_t max_tb = 0, max_edges = 0, max_slots = 0, max_scratch = 0, n_tasks = 0, n_pair_tasks = 0;
-    int64_t max_ref = 0, max_alt = 0;
+    plan_offsets(E.h_pairs.p, E.h_res.p, n, E.tb_budget_words, *in.params, in.strategy, E.allow16, chunks, keys);
+    int64_t max_tb = 0, max_edges = 0, max_slots = 0, max_scratch = 0, max_ref = 0, max_alt = 0;
     for (auto &c : chunks) {
         max_tb = std::max(max_tb, c.tb_words);
         max_edges = std::max(max_edges, c.edges);
         max_slots = std::max(max_slots, c.slots);
         max_scratch = std::max(max_scratch, c.scratch);
-        for (int k = 1; k <= kSwMaxK; ++k) {
-            n_tasks += c.task_count[k];
-            n_pair_tasks += c.pair_count[k];
-        }
     }
     for (int64_t i = 0; i < n; ++i)
         if (E.h_res.p[i] == 0) {
@@ -355,8 +359,8 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         }
     A.clamp = needs_clamp(*in.params, in.strategy, max_ref, max_alt) ? 1 : 0;
     const int64_t n_cursors = 2 + (int64_t)chunks.size() * 2 * kCursorsPerChunk;
-    SW_CUDA(E.d_tasks.reserve((size_t)std::max<int64_t>(n_tasks, 1)), "device tasks");
-    SW_CUDA(E.d_pair_tasks.reserve((size_t)std::max<int64_t>(n_pair_tasks, 1)), "device pair tasks");
+    SW_CUDA(E.d_tasks.reserve((size_t)std::max<int64_t>(n, 1)), "device tasks");
+    SW_CUDA(E.d_pair_tasks.reserve((size_t)std::max<int64_t>(n, 1)), "device pair tasks");
     SW_CUDA(E.d_counters.reserve((size_t)n_cursors), "device counters");
     SW_CUDA(E.d_tb.reserve((size_t)std::max<int64_t>(max_tb, 1)), "traceback buffer");
     SW_CUDA(E.d_edges.reserve((size_t)std::max<int64_t>(max_edges, 4)), "edge scores");
@@ -364,14 +368,7 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
     SW_CUDA(E.d_slot.reserve((size_t)std::max<int64_t>(max_slots, 1)), "cigar slots");
     SW_CUDA(cudaMemcpyAsync(E.d_pairs.p, E.h_pairs.p, (size_t)n * sizeof(SwPair), cudaMemcpyHostToDevice, s),
             "H2D planned pairs");
-    if (n_tasks)
-        SW_CUDA(cudaMemcpyAsync(E.d_tasks.p, E.h_tasks.p, (size_t)n_tasks * sizeof(int32_t), cudaMemcpyHostToDevice, s),
-                "H2D tasks");
-    if (n_pair_tasks)
-        SW_CUDA(cudaMemcpyAsync(E.d_pair_tasks.p, E.h_pair_tasks.p, (size_t)n_pair_tasks * sizeof(int2),
-                                cudaMemcpyHostToDevice, s), "H2D pair tasks");
     SW_CUDA(cudaMemsetAsync(E.d_counters.p, 0, (size_t)n_cursors * sizeof(int64_t), s), "zero counters");
-    E.stats.h2d_bytes += n_tasks * 4 + n_pair_tasks * 8;
     E.stats.ms_host += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_plan).count();
     int *d_err = reinterpret_cast<int *>(E.d_counters.p + 1);
     int *d_cursors = reinterpret_cast<int *>(E.d_counters.p + 2);
@@ -388,6 +385,32 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         if (e) return cuda_error(ctx, (cudaError_t)e, "occupancy");
         occ[k] = std::max(b, 1);
         occ16[k] = std::max(b16, 1);
+    }
+    int64_t n_paired = 0;
+    double ms_tasks = 0;
+    // a chunk's tasks are planned (and uploaded) while the previous chunk's kernels run
+    auto plan_chunk = [&](size_t c) -> int {
+        const auto t_tasks = std::chrono::steady_clock::now();
+        Chunk &ch = chunks[c];
+        n_paired += plan_tasks(keys, ch, E.h_tasks.p, E.h_pair_tasks.p);
+        int64_t nt = 0, np = 0;
+        for (int k = 1; k <= kSwMaxK; ++k) {
+            nt += ch.task_count[k];
+            np += ch.pair_count[k];
+        }
+        if (nt)
+            SW_CUDA(cudaMemcpyAsync(E.d_tasks.p + ch.p0, E.h_tasks.p + ch.p0, (size_t)nt * sizeof(int32_t),
+                                    cudaMemcpyHostToDevice, s), "H2D tasks");
+        if (np)
+            SW_CUDA(cudaMemcpyAsync(E.d_pair_tasks.p + ch.p0, E.h_pair_tasks.p + ch.p0, (size_t)np * sizeof(int2),
+                                    cudaMemcpyHostToDevice, s), "H2D pair tasks");
+        E.stats.h2d_bytes += nt * 4 + np * 8;
+        ms_tasks += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_tasks).count();
+        return GHMM_OK;
+    };
+    if (!chunks.empty()) {
+        const int rc = plan_chunk(0);
+        if (rc) return rc;
     }
     // (3) per chunk
     SW_CUDA(cudaEventRecord(E.event(2), s), "event");
@@ -428,6 +451,10 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         e = launch_sw_compact(a, (int)cn, E.d_starts.p + ch.p0, E.d_counters.p, E.d_ops.p, in.ops_cap, s);
         if (e) return cuda_error(ctx, (cudaError_t)e, "Smith-Waterman cigar compaction launch");
         launches += 3;
+        if (c + 1 < chunks.size()) {
+            const int rc = plan_chunk(c + 1);
+            if (rc) return rc;
+        }
     }
     const size_t ev_end = ev++;
     SW_CUDA(cudaEventRecord(E.event(ev_end), s), "event");
@@ -471,6 +498,7 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
     E.stats.launches = launches;
     E.stats.n_alignments = n;
     E.stats.n_int16 = n_paired;
+    E.stats.ms_host += ms_tasks;
     return GHMM_OK;
 }
 
