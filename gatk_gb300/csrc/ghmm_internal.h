@@ -138,11 +138,15 @@ constexpr uint32_t kSwOpM = 0, kSwOpI = 1, kSwOpD = 2, kSwOpS = 4;
 constexpr int kSwMaxK = 8;  // alt columns per lane; longer alts run in strips of 32 * 8 columns
 // Row stride of the last-column lane's scores in the edge array: K rounded up to whole int4s.
 #define kSwRowStride(k) ((((k) + 3) / 4) * 4)
+// Steps of one strip of a ref of n rows (n + 31), rounded up to whole groups of 4: traceback words are stored in
+// groups of 4 consecutive steps per lane (16 contiguous bytes).
+#define sw_steps4(n) ((((int64_t)(n) + 34) / 4) * 4)
 
 // One alignment: alt against ref.  Offsets index the ref / alt planes and the chunk's buffers.
 struct SwPair {
     int64_t ref_off, alt_off;
-    int64_t tb_off;       // first traceback word: strips x (ref_len + 31) steps x 32 lanes
+    int64_t tb_off;       // first traceback word: strips x sw_steps4(ref_len) steps x 32 lanes; within a strip the word
+                          // of step t and lane l is at ((t / 4) * 32 + l) * 4 + t % 4
     int64_t edge_off;     // ref_len rows of the last-column lane's kSwRowStride(k) scores, then the bottom row as
                           // one row of kSwRowStride(k) per lane and strip (a multiple of 4 ints: int4-aligned rows)
     int64_t slot_off;     // 2 * alt_len + 4 cigar ops, written in reverse by the traceback

@@ -108,7 +108,7 @@ struct LaneState {
 // one add per cell then serves as the next row's vertical gap opening and the next column's horizontal one, and
 // the diagonal adds the score minus open.  Every sum is the Java one modulo 2^32.
 template <int K, bool CLAMP, bool CHECK>
-__device__ __forceinline__ void sw_step(const StripCtx &C, LaneState<K> &L, int t, int lane) {
+__device__ __forceinline__ uint32_t sw_step(const StripCtx &C, LaneState<K> &L, int t, int lane) {
     const int i = t - lane + 1;
     const bool active = !CHECK || (i >= 1 && i <= C.n);
     const uint8_t a = L.a_next;
@@ -126,7 +126,7 @@ __device__ __forceinline__ void sw_step(const StripCtx &C, LaneState<K> &L, int 
             bh = v.y;
         }
     }
-    if (!active) return;
+    if (!active) return 0;
     uint32_t bits = 0;
     int hd = L.hdiag;
     int hl = h_left;
@@ -151,12 +151,12 @@ __device__ __forceinline__ void sw_step(const StripCtx &C, LaneState<K> &L, int 
         L.hup[k] = hno;
         hl = hno;
     }
-    C.tb[(int64_t)t * 32] = bits;
     if (C.owns_last) store_row<K>(C.lastrow + (int64_t)(i - 1) * kSwRowStride(K), L.hup);
     if (C.strip_out && lane == 31) C.strip_out[i] = make_int2(hl, bh);
     L.send_h = hl;
     L.send_b = bh;
     L.hdiag = h_left;
+    return bits;
 }
 
 template <int K, bool CLAMP>
@@ -178,8 +178,7 @@ __device__ __forceinline__ void sw_strip(const SwArgs &A, const SwPair &P, int s
     C.indel_edges = A.indel_edges != 0;
     const int km = (m - 1) - jbase;            // the alt's last column, on its lane in the last strip
     C.owns_last = last_strip && km >= 0 && km < K;
-    const int64_t steps = (int64_t)n + 31;
-    C.tb = A.tb + P.tb_off + (int64_t)s * steps * 32 + lane;
+    C.tb = A.tb + P.tb_off + (int64_t)s * sw_steps4(n) * 32 + lane * 4;
     C.lastrow = A.edges + P.edge_off;
     C.strip_in = s > 0 ? A.strip_scratch + P.scratch_off : nullptr;
     C.strip_out = !last_strip ? A.strip_scratch + P.scratch_off : nullptr;
@@ -195,11 +194,17 @@ __device__ __forceinline__ void sw_strip(const SwArgs &A, const SwPair &P, int s
     L.send_h = 0;
     L.send_b = kSwLowInit;
     L.a_next = C.ref[min(max(0 - lane, 0), n - 1)];
+    // traceback words: groups of 4 steps per lane, 16 contiguous bytes (steps t and t - 1 of a lane share a sector)
     int t = 0;
-    for (; t < 31; ++t) sw_step<K, CLAMP, true>(C, L, t, lane);
-#pragma unroll 4
-    for (; t < n; ++t) sw_step<K, CLAMP, false>(C, L, t, lane);  // every lane inside the matrix
-    for (; t < n + 31; ++t) sw_step<K, CLAMP, true>(C, L, t, lane);
+    for (; t < 32; ++t) C.tb[(int64_t)(t >> 2) * 128 + (t & 3)] = sw_step<K, CLAMP, true>(C, L, t, lane);
+    for (; t + 3 < n; t += 4) {  // every lane inside the matrix
+        const uint32_t w0 = sw_step<K, CLAMP, false>(C, L, t, lane);
+        const uint32_t w1 = sw_step<K, CLAMP, false>(C, L, t + 1, lane);
+        const uint32_t w2 = sw_step<K, CLAMP, false>(C, L, t + 2, lane);
+        const uint32_t w3 = sw_step<K, CLAMP, false>(C, L, t + 3, lane);
+        *reinterpret_cast<uint4 *>(C.tb + (int64_t)(t >> 2) * 128) = make_uint4(w0, w1, w2, w3);
+    }
+    for (; t < n + 31; ++t) C.tb[(int64_t)(t >> 2) * 128 + (t & 3)] = sw_step<K, CLAMP, true>(C, L, t, lane);
     // the lanes finish on row n: their scores (+ open) are the bottom row, one row of kSwRowStride(K) per lane
     store_row<K>(A.edges + P.edge_off + ((int64_t)n + s * 32 + lane) * kSwRowStride(K), L.hup);
     __syncwarp();
@@ -261,7 +266,7 @@ struct Lane16 {
 };
 
 template <int K, bool CHECK>
-__device__ __forceinline__ void pair16_step(const Pair16Ctx &C, Lane16<K> &L, int t, int lane) {
+__device__ __forceinline__ uint2 pair16_step(const Pair16Ctx &C, Lane16<K> &L, int t, int lane) {
     const int i = t - lane + 1;
     const bool active = !CHECK || (i >= 1 && i <= C.n);
     const uint32_t a2 = L.a_next;
@@ -272,7 +277,7 @@ __device__ __forceinline__ void pair16_step(const Pair16Ctx &C, Lane16<K> &L, in
         h_left = C.indel_edges && i > 0 ? both16(C.open + (i - 1) * C.ext + C.open) : C.inject_const;
         bh = both16(kSw16Low);
     }
-    if (!active) return;
+    if (!active) return make_uint2(0, 0);
     uint32_t bits0 = 0, bits1 = 0;
     uint32_t hd = L.hdiag, hl = h_left;
 #pragma unroll
@@ -306,8 +311,6 @@ __device__ __forceinline__ void pair16_step(const Pair16Ctx &C, Lane16<K> &L, in
     // each alignment's word in the int32 kernel's layout (bit 1 there: right >= down)
     const uint32_t wa = __byte_perm(bits0, bits1, 0x5410) ^ 0x22222222u;
     const uint32_t wb = __byte_perm(bits0, bits1, 0x7632) ^ 0x22222222u;
-    if (t < C.n_a + 31) C.tb_a[(int64_t)t * 32] = wa;
-    if (C.has_b && t < C.n_b + 31) C.tb_b[(int64_t)t * 32] = wb;
     // raw 16-bit pairs; the traceback takes its alignment's half (state 2: low, 3: high)
     if (C.owns_a && i <= C.n_a) store_row<K>(C.last_a + (int64_t)(i - 1) * kSwRowStride(K), L.hup);
     if (C.owns_b && i <= C.n_b) store_row<K>(C.last_b + (int64_t)(i - 1) * kSwRowStride(K), L.hup);
@@ -316,6 +319,7 @@ __device__ __forceinline__ void pair16_step(const Pair16Ctx &C, Lane16<K> &L, in
     L.send_h = hl;
     L.send_b = bh;
     L.hdiag = h_left;
+    return make_uint2(wa, wb);
 }
 
 // tasks: (alignment A, alignment B or -1) of single-strip alignments with the same K, B's ref no longer than A's
@@ -349,8 +353,8 @@ __global__ void __launch_bounds__(128, 6) sw_pair16_kernel(SwArgs A, const int2 
         C.dm = A.mismatch - A.match;
         C.indel_edges = A.indel_edges != 0;
         C.inject_const = both16(A.open);
-        C.tb_a = A.tb + PA.tb_off + lane;
-        C.tb_b = A.tb + PB.tb_off + lane;
+        C.tb_a = A.tb + PA.tb_off + lane * 4;
+        C.tb_b = A.tb + PB.tb_off + lane * 4;
         const int km_a = (C.m_a - 1) - C.jbase, km_b = (C.m_b - 1) - C.jbase;
         C.owns_a = km_a >= 0 && km_a < K;
         C.owns_b = has_b && km_b >= 0 && km_b < K;
@@ -377,11 +381,36 @@ __global__ void __launch_bounds__(128, 6) sw_pair16_kernel(SwArgs A, const int2 
         L.send_b = both16(kSw16Low);
         L.a_next = (uint32_t)C.ref_a[0] | ((uint32_t)C.ref_b[0] << 16);
         if (lane > 0) L.a_next = 0;  // lanes start later; their first base is loaded by their own steps
+        // each alignment's words for its own n + 31 steps, in groups of 4 steps per lane
+        auto put1 = [&](int t, uint2 w) {
+            const int64_t o = (int64_t)(t >> 2) * 128 + (t & 3);
+            if (t < C.n_a + 31) C.tb_a[o] = w.x;
+            if (C.has_b && t < C.n_b + 31) C.tb_b[o] = w.y;
+        };
         int t = 0;
-        for (; t < 31; ++t) pair16_step<K, true>(C, L, t, lane);
-#pragma unroll 4
-        for (; t < C.n; ++t) pair16_step<K, false>(C, L, t, lane);
-        for (; t < C.n + 31; ++t) pair16_step<K, true>(C, L, t, lane);
+        for (; t < 32; ++t) put1(t, pair16_step<K, true>(C, L, t, lane));
+        for (; t + 3 < C.n; t += 4) {  // every lane inside the matrix
+            const uint2 w0 = pair16_step<K, false>(C, L, t, lane);
+            const uint2 w1 = pair16_step<K, false>(C, L, t + 1, lane);
+            const uint2 w2 = pair16_step<K, false>(C, L, t + 2, lane);
+            const uint2 w3 = pair16_step<K, false>(C, L, t + 3, lane);
+            const int64_t o = (int64_t)(t >> 2) * 128;
+            if (t + 3 < C.n_a + 31) {
+                *reinterpret_cast<uint4 *>(C.tb_a + o) = make_uint4(w0.x, w1.x, w2.x, w3.x);
+            } else {
+                put1(t, make_uint2(w0.x, 0));
+            }
+            if (C.has_b) {
+                if (t + 3 < C.n_b + 31) {
+                    *reinterpret_cast<uint4 *>(C.tb_b + o) = make_uint4(w0.y, w1.y, w2.y, w3.y);
+                } else {
+                    if (t < C.n_b + 31) C.tb_b[o] = w0.y;
+                    if (t + 1 < C.n_b + 31) C.tb_b[o + 1] = w1.y;
+                    if (t + 2 < C.n_b + 31) C.tb_b[o + 2] = w2.y;
+                }
+            }
+        }
+        for (; t < C.n + 31; ++t) put1(t, pair16_step<K, true>(C, L, t, lane));
         __syncwarp();
     }
 }
@@ -408,9 +437,9 @@ __device__ __forceinline__ uint32_t tb_code(const SwArgs &A, const SwPair &P, in
     const int w = 32 * K;
     const int s = (j - 1) / w, within = (j - 1) - s * w;
     const int lane = within / K, k = within - lane * K;
-    const int64_t steps = (int64_t)P.ref_len + 31;
     const int64_t t = (int64_t)(i - 1) + lane;
-    return (A.tb[P.tb_off + ((int64_t)s * steps + t) * 32 + lane] >> (4 * k)) & 15u;
+    return (A.tb[P.tb_off + (int64_t)s * sw_steps4(P.ref_len) * 32 + ((t >> 2) * 32 + lane) * 4 + (t & 3)] >> (4 * k)) &
+           15u;
 }
 
 __global__ void sw_traceback_kernel(SwArgs A, int n_pairs) {

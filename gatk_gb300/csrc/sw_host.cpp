@@ -149,7 +149,7 @@ void plan_offsets(SwPair *pairs, const int32_t *state, int64_t n, int64_t budget
         const int k = sw_k(P.alt_len);
         const int64_t strips = (P.alt_len + 32 * k - 1) / (32 * k);
         const int64_t rb = P.ref_len;
-        const int64_t words = strips * (rb + 31) * 32;
+        const int64_t words = strips * sw_steps4(rb) * 32;
         if (i > c.p0 && c.tb_words + words > budget_words) {
             c.p1 = i;
             chunks.push_back(c);
