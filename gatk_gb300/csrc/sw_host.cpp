@@ -15,7 +15,6 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 #include "../../include/ghmm.h"
@@ -125,51 +124,65 @@ bool fits16(const ghmm_sw_params &p, int strategy, int64_t n, int k) {
     return hmin - slack >= -28000 && hmax + slack <= 28000;
 }
 
-// Buffer offsets (chunk-relative) of every alignment that runs the recurrence (state 0, ref_len > 0), which of
-// them take the 16-bit kernel, and chunk boundaries over contiguous alignment ranges.
 // keys[i]: the alignment's task bucket (kernel * 9 + K) << 21 | ref length, or kNoTask.
 constexpr uint32_t kNoTask = 0xffffffffu;
 
-void plan_offsets(SwPair *pairs, const int32_t *state, int64_t n, int64_t budget_words, const ghmm_sw_params &prm,
-                  int strategy, bool allow16, std::vector<Chunk> &chunks, std::vector<uint32_t> &keys) {
-    chunks.clear();
-    keys.assign((size_t)n, kNoTask);
+// Buffer sizes of one alignment: traceback words, edge ints, cigar slots, strip scratch rows.
+struct SwSizes {
+    int64_t words = 0, edges = 0, slots = 0, scratch = 0;
+};
+inline SwSizes sw_sizes(const SwPair &P, bool runs) {
+    SwSizes z;
+    z.slots = 2 * (int64_t)P.alt_len + 4;
+    if (!runs) return z;
+    const int k = sw_k(P.alt_len);
+    const int64_t strips = (P.alt_len + 32 * k - 1) / (32 * k);
+    z.words = strips * sw_steps4(P.ref_len) * 32;
+    z.edges = ((int64_t)P.ref_len + strips * 32) * kSwRowStride(k);  // last-column rows, one bottom row per lane
+    z.scratch = strips > 1 ? (int64_t)P.ref_len + 1 : 0;
+    return z;
+}
+
+struct SwCaps {
+    int64_t words, edges, scratch;
+};
+
+// The next chunk from alignment i0: buffer offsets (chunk-relative) of every alignment that runs the recurrence
+// (state 0, ref_len > 0) and its task key, until one more alignment would pass a buffer's capacity.
+Chunk plan_next_chunk(SwPair *pairs, const int32_t *state, int64_t n, int64_t i0, const SwCaps &cap,
+                      const ghmm_sw_params &prm, int strategy, bool allow16, std::vector<uint32_t> &keys) {
     Chunk c;
-    for (int64_t i = 0; i < n; ++i) {
+    c.p0 = i0;
+    int64_t i = i0;
+    for (; i < n; ++i) {
         SwPair &P = pairs[i];
         const bool runs = state[i] == 0 && P.ref_len > 0;
+        const SwSizes z = sw_sizes(P, runs);
+        if (i > i0 && (c.tb_words + z.words > cap.words || c.edges + z.edges > cap.edges ||
+                       c.scratch + z.scratch > cap.scratch))
+            break;
+        keys[(size_t)i] = kNoTask;
+        P.slot_off = c.slots;
+        c.slots += z.slots;
         if (!runs) {  // shortcut or nothing to align against: a cigar slot only
             P.k = 1;
             P.tb_off = P.edge_off = 0;
-            P.slot_off = c.slots;
             P.scratch_off = -1;
-            c.slots += 2 * (int64_t)P.alt_len + 4;
             continue;
         }
         const int k = sw_k(P.alt_len);
-        const int64_t strips = (P.alt_len + 32 * k - 1) / (32 * k);
-        const int64_t rb = P.ref_len;
-        const int64_t words = strips * sw_steps4(rb) * 32;
-        if (i > c.p0 && c.tb_words + words > budget_words) {
-            c.p1 = i;
-            chunks.push_back(c);
-            c = Chunk{};
-            c.p0 = i;
-        }
         P.k = k;
         P.tb_off = c.tb_words;
         P.edge_off = c.edges;
-        P.slot_off = c.slots;
-        P.scratch_off = strips > 1 ? c.scratch : -1;
-        c.tb_words += words;
-        c.edges += (rb + strips * 32) * kSwRowStride(k);  // last-column rows, then one bottom row per lane
-        c.slots += 2 * (int64_t)P.alt_len + 4;
-        if (strips > 1) c.scratch += rb + 1;
-        const uint32_t kind = allow16 && strips == 1 && fits16(prm, strategy, rb, k) ? 1u : 0u;
-        keys[(size_t)i] = ((kind * (kSwMaxK + 1) + (uint32_t)k) << 21) | (uint32_t)rb;
+        P.scratch_off = z.scratch ? c.scratch : -1;
+        c.tb_words += z.words;
+        c.edges += z.edges;
+        c.scratch += z.scratch;
+        const uint32_t kind = allow16 && z.scratch == 0 && fits16(prm, strategy, P.ref_len, k) ? 1u : 0u;
+        keys[(size_t)i] = ((kind * (kSwMaxK + 1) + (uint32_t)k) << 21) | (uint32_t)P.ref_len;
     }
-    c.p1 = n;
-    if (n > 0) chunks.push_back(c);
+    c.p1 = i;
+    return c;
 }
 
 // One chunk's tasks, at positions p0.. of the task arrays: per K the int32 kernel's alignments (longest ref first)
@@ -327,51 +340,74 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         const int64_t NR = in.batch->n_reads, NH = in.batch->n_haps;
         const int64_t *hap_off = in.batch->h_off + NR + 1, *rro = hap_off + NH + 1, *rho = rro + in.batch->n_regions + 1;
         const int32_t *best = E.h_res.p + 3 * n;
-        for (int64_t r = 0, g = 0; r < n; ++r) {
-            while (rro[g + 1] <= r) ++g;
-            SwPair &P = E.h_pairs.p[r];
-            if (best[r] < 0) {
-                P.ref_off = 0;
-                P.ref_len = 0;
-            } else {
-                const int64_t h = rho[g] + best[r];
-                P.ref_off = hap_off[h];
-                P.ref_len = (int32_t)(hap_off[h + 1] - hap_off[h]);
+        const int64_t G = in.batch->n_regions;
+        parallel_for(G, ci.threads, [&](int64_t g) {
+            for (int64_t r = rro[g]; r < rro[g + 1]; ++r) {
+                SwPair &P = E.h_pairs.p[r];
+                if (best[r] < 0) {
+                    P.ref_off = 0;
+                    P.ref_len = 0;
+                } else {
+                    const int64_t h = rho[g] + best[r];
+                    P.ref_off = hap_off[h];
+                    P.ref_len = (int32_t)(hap_off[h + 1] - hap_off[h]);
+                }
+            }
+        }, 256);
+    }
+    // totals and maxima for the buffers and the clamp decision
+    struct Part {
+        int64_t words = 0, max_words = 0, max_edges = 0, max_scratch = 0, slots = 0, max_ref = 0, max_alt = 0;
+    };
+    const int nparts = std::max(1, ci.threads);
+    std::vector<Part> parts((size_t)nparts);
+    const int64_t per = (n + nparts - 1) / nparts;
+    parallel_for(nparts, nparts, [&](int64_t t) {
+        Part &q = parts[(size_t)t];
+        for (int64_t i = t * per; i < std::min(n, (t + 1) * per); ++i) {
+            const SwPair &P = E.h_pairs.p[i];
+            const bool runs = E.h_res.p[i] == 0 && P.ref_len > 0;
+            const SwSizes z = sw_sizes(P, runs);
+            q.words += z.words;
+            q.slots += z.slots;
+            q.max_words = std::max(q.max_words, z.words);
+            q.max_edges = std::max(q.max_edges, z.edges);
+            q.max_scratch = std::max(q.max_scratch, z.scratch);
+            if (runs) {
+                q.max_ref = std::max<int64_t>(q.max_ref, P.ref_len);
+                q.max_alt = std::max<int64_t>(q.max_alt, P.alt_len);
             }
         }
+    }, 1);
+    Part tot;
+    for (auto &q : parts) {
+        tot.words += q.words;
+        tot.slots += q.slots;
+        tot.max_words = std::max(tot.max_words, q.max_words);
+        tot.max_edges = std::max(tot.max_edges, q.max_edges);
+        tot.max_scratch = std::max(tot.max_scratch, q.max_scratch);
+        tot.max_ref = std::max(tot.max_ref, q.max_ref);
+        tot.max_alt = std::max(tot.max_alt, q.max_alt);
     }
-    std::vector<Chunk> chunks;
-    std::vector<uint32_t> keys;
+    A.clamp = needs_clamp(*in.params, in.strategy, tot.max_ref, tot.max_alt) ? 1 : 0;
+    // a chunk is bounded by the traceback budget; its edges and scratch by fixed fractions of it (an alignment's
+    // edges are at most a quarter of its traceback words and its scratch a 32nd), or by the largest single alignment
+    SwCaps cap;
+    cap.words = std::max(std::min(E.tb_budget_words, tot.words), tot.max_words);
+    cap.edges = std::max(cap.words / 3, tot.max_edges);
+    cap.scratch = std::max(cap.words / 16, tot.max_scratch);
     SW_CUDA(E.h_tasks.reserve((size_t)std::max<int64_t>(n, 1)), "pinned tasks");
     SW_CUDA(E.h_pair_tasks.reserve((size_t)std::max<int64_t>(n, 1)), "pinned pair tasks");
-    plan_offsets(E.h_pairs.p, E.h_res.p, n, E.tb_budget_words, *in.params, in.strategy, E.allow16, chunks, keys);
-    int64_t max_tb = 0, max_edges = 0, max_slots = 0, max_scratch = 0, max_ref = 0, max_alt = 0;
-    for (auto &c : chunks) {
-        max_tb = std::max(max_tb, c.tb_words);
-        max_edges = std::max(max_edges, c.edges);
-        max_slots = std::max(max_slots, c.slots);
-        max_scratch = std::max(max_scratch, c.scratch);
-    }
-    for (int64_t i = 0; i < n; ++i)
-        if (E.h_res.p[i] == 0) {
-            max_ref = std::max<int64_t>(max_ref, E.h_pairs.p[i].ref_len);
-            max_alt = std::max<int64_t>(max_alt, E.h_pairs.p[i].alt_len);
-        }
-    A.clamp = needs_clamp(*in.params, in.strategy, max_ref, max_alt) ? 1 : 0;
-    const int64_t n_cursors = 2 + (int64_t)chunks.size() * 2 * kCursorsPerChunk;
     SW_CUDA(E.d_tasks.reserve((size_t)std::max<int64_t>(n, 1)), "device tasks");
     SW_CUDA(E.d_pair_tasks.reserve((size_t)std::max<int64_t>(n, 1)), "device pair tasks");
-    SW_CUDA(E.d_counters.reserve((size_t)n_cursors), "device counters");
-    SW_CUDA(E.d_tb.reserve((size_t)std::max<int64_t>(max_tb, 1)), "traceback buffer");
-    SW_CUDA(E.d_edges.reserve((size_t)std::max<int64_t>(max_edges, 4)), "edge scores");
-    SW_CUDA(E.d_scratch.reserve((size_t)std::max<int64_t>(max_scratch, 1)), "strip scratch");
-    SW_CUDA(E.d_slot.reserve((size_t)std::max<int64_t>(max_slots, 1)), "cigar slots");
-    SW_CUDA(cudaMemcpyAsync(E.d_pairs.p, E.h_pairs.p, (size_t)n * sizeof(SwPair), cudaMemcpyHostToDevice, s),
-            "H2D planned pairs");
-    SW_CUDA(cudaMemsetAsync(E.d_counters.p, 0, (size_t)n_cursors * sizeof(int64_t), s), "zero counters");
-    E.stats.ms_host += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_plan).count();
+    SW_CUDA(E.d_counters.reserve((size_t)(2 + kCursorsPerChunk)), "device counters");
+    SW_CUDA(E.d_tb.reserve((size_t)std::max<int64_t>(cap.words, 1)), "traceback buffer");
+    SW_CUDA(E.d_edges.reserve((size_t)std::max<int64_t>(cap.edges, 4)), "edge scores");
+    SW_CUDA(E.d_scratch.reserve((size_t)std::max<int64_t>(cap.scratch, 1)), "strip scratch");
+    SW_CUDA(E.d_slot.reserve((size_t)std::max<int64_t>(tot.slots, 1)), "cigar slots");
+    SW_CUDA(cudaMemsetAsync(E.d_counters.p, 0, 2 * sizeof(int64_t), s), "zero counters");
     int *d_err = reinterpret_cast<int *>(E.d_counters.p + 1);
-    int *d_cursors = reinterpret_cast<int *>(E.d_counters.p + 2);
+    int *d_cursors = reinterpret_cast<int *>(E.d_counters.p + 2);  // 2 x 9 task cursors, reset per chunk
     A.tb = E.d_tb.p;
     A.edges = E.d_edges.p;
     A.strip_scratch = E.d_scratch.p;
@@ -386,38 +422,45 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         occ[k] = std::max(b, 1);
         occ16[k] = std::max(b16, 1);
     }
-    int64_t n_paired = 0;
+    std::vector<uint32_t> keys((size_t)n);
+    int64_t n_paired = 0, n_chunks = 0;
     double ms_tasks = 0;
-    // a chunk's tasks are planned (and uploaded) while the previous chunk's kernels run
-    auto plan_chunk = [&](size_t c) -> int {
+    // the next chunk is planned (offsets and tasks) and uploaded while the previous chunk's kernels run
+    auto plan_chunk = [&](int64_t i0, Chunk &ch) -> int {
         const auto t_tasks = std::chrono::steady_clock::now();
-        Chunk &ch = chunks[c];
+        ch = plan_next_chunk(E.h_pairs.p, E.h_res.p, n, i0, cap, *in.params, in.strategy, E.allow16, keys);
         n_paired += plan_tasks(keys, ch, E.h_tasks.p, E.h_pair_tasks.p);
         int64_t nt = 0, np = 0;
         for (int k = 1; k <= kSwMaxK; ++k) {
             nt += ch.task_count[k];
             np += ch.pair_count[k];
         }
+        SW_CUDA(cudaMemcpyAsync(E.d_pairs.p + ch.p0, E.h_pairs.p + ch.p0, (size_t)(ch.p1 - ch.p0) * sizeof(SwPair),
+                                cudaMemcpyHostToDevice, s), "H2D planned pairs");
         if (nt)
             SW_CUDA(cudaMemcpyAsync(E.d_tasks.p + ch.p0, E.h_tasks.p + ch.p0, (size_t)nt * sizeof(int32_t),
                                     cudaMemcpyHostToDevice, s), "H2D tasks");
         if (np)
             SW_CUDA(cudaMemcpyAsync(E.d_pair_tasks.p + ch.p0, E.h_pair_tasks.p + ch.p0, (size_t)np * sizeof(int2),
                                     cudaMemcpyHostToDevice, s), "H2D pair tasks");
-        E.stats.h2d_bytes += nt * 4 + np * 8;
+        SW_CUDA(cudaMemsetAsync(d_cursors, 0, 2 * kCursorsPerChunk * sizeof(int), s), "zero task cursors");
+        E.stats.h2d_bytes += (ch.p1 - ch.p0) * (int64_t)sizeof(SwPair) + nt * 4 + np * 8;
         ms_tasks += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_tasks).count();
         return GHMM_OK;
     };
-    if (!chunks.empty()) {
-        const int rc = plan_chunk(0);
+    Chunk next;
+    if (n > 0) {
+        const int rc = plan_chunk(0, next);
         if (rc) return rc;
     }
+    E.stats.ms_host += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_plan).count();
     // (3) per chunk
     SW_CUDA(cudaEventRecord(E.event(2), s), "event");
     size_t ev = 3;
     std::vector<std::pair<size_t, size_t>> fwd_events;
-    for (size_t c = 0; c < chunks.size(); ++c) {
-        const Chunk &ch = chunks[c];
+    while (n_chunks == 0 || next.p0 < n) {
+        const Chunk ch = next;
+        ++n_chunks;
         const int64_t cn = ch.p1 - ch.p0;
         SwArgs a = A;
         a.pairs = E.d_pairs.p + ch.p0;
@@ -426,13 +469,12 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         a.n_ops = d_nops + ch.p0;
         const size_t e0 = ev++, e1 = ev++;
         SW_CUDA(cudaEventRecord(E.event(e0), s), "event");
-        int *cur = d_cursors + c * 2 * kCursorsPerChunk;
         for (int k = kSwMaxK; k >= 1; --k) {
             const int64_t cnt = ch.pair_count[k];
             if (!cnt) continue;
             const int grid = (int)std::min<int64_t>((cnt + 3) / 4, (int64_t)occ16[k] * ci.sm_count);
-            const int e = launch_sw_pair16(a, k, E.d_pair_tasks.p + ch.pair_begin[k], (int)cnt, cur + kCursorsPerChunk + k,
-                                           grid, s);
+            const int e = launch_sw_pair16(a, k, E.d_pair_tasks.p + ch.pair_begin[k], (int)cnt,
+                                           d_cursors + kCursorsPerChunk + k, grid, s);
             if (e) return cuda_error(ctx, (cudaError_t)e, "Smith-Waterman paired forward launch");
             ++launches;
         }
@@ -440,7 +482,7 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
             const int64_t cnt = ch.task_count[k];
             if (!cnt) continue;
             const int grid = (int)std::min<int64_t>((cnt + 3) / 4, (int64_t)occ[k] * ci.sm_count);
-            const int e = launch_sw_forward(a, k, E.d_tasks.p + ch.task_begin[k], (int)cnt, cur + k, grid, s);
+            const int e = launch_sw_forward(a, k, E.d_tasks.p + ch.task_begin[k], (int)cnt, d_cursors + k, grid, s);
             if (e) return cuda_error(ctx, (cudaError_t)e, "Smith-Waterman forward launch");
             ++launches;
         }
@@ -451,10 +493,9 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         e = launch_sw_compact(a, (int)cn, E.d_starts.p + ch.p0, E.d_counters.p, E.d_ops.p, in.ops_cap, s);
         if (e) return cuda_error(ctx, (cudaError_t)e, "Smith-Waterman cigar compaction launch");
         launches += 3;
-        if (c + 1 < chunks.size()) {
-            const int rc = plan_chunk(c + 1);
-            if (rc) return rc;
-        }
+        if (ch.p1 >= n) break;
+        const int rc = plan_chunk(ch.p1, next);
+        if (rc) return rc;
     }
     const size_t ev_end = ev++;
     SW_CUDA(cudaEventRecord(E.event(ev_end), s), "event");
@@ -494,7 +535,7 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         fwd += m;
     }
     E.stats.ms_forward = fwd;
-    E.stats.chunks = (int32_t)chunks.size();
+    E.stats.chunks = (int32_t)n_chunks;
     E.stats.launches = launches;
     E.stats.n_alignments = n;
     E.stats.n_int16 = n_paired;
@@ -558,22 +599,32 @@ int sw_batch(ghmm_ctx *ctx, const CtxInfo &ci, const ghmm_sw_pair *pairs, int64_
         if (p.ref_len > GHMM_SW_MAX_LEN || p.alt_len > GHMM_SW_MAX_LEN)
             return ctx_fail(ctx, GHMM_ERR_ARG, "sequence longer than GHMM_SW_MAX_LEN");
     }
-    // refs deduplicated by (address, length): a haplotype shared by many reads is copied once
-    std::unordered_map<const uint8_t *, std::pair<int64_t, int32_t>> seen;
-    seen.reserve((size_t)std::min<int64_t>(n, 1 << 20));
+    // refs deduplicated by (address, length): a haplotype shared by many reads is copied once (an open-addressing
+    // table keyed by the address, twice the pairs in size)
+    size_t tcap = 16;
+    while (tcap < (size_t)n * 2) tcap <<= 1;
+    struct Slot {
+        const uint8_t *ref;
+        int32_t len;
+        int64_t off;
+    };
+    std::vector<Slot> table(tcap, Slot{nullptr, 0, 0});
     std::vector<int64_t> ref_off((size_t)n);
     std::vector<int64_t> uniq;  // pair index of each distinct ref
     int64_t ref_bytes = 0;
     for (int64_t i = 0; i < n; ++i) {
-        auto it = seen.find(pairs[i].ref);
-        if (it != seen.end() && it->second.second == pairs[i].ref_len) {
-            ref_off[(size_t)i] = it->second.first;
+        const uint8_t *r = pairs[i].ref;
+        const int32_t len = pairs[i].ref_len;
+        size_t h = (size_t)(((uint64_t)(uintptr_t)r * 0x9E3779B97F4A7C15ull) >> 17) & (tcap - 1);
+        while (table[h].ref && !(table[h].ref == r && table[h].len == len)) h = (h + 1) & (tcap - 1);
+        if (table[h].ref) {
+            ref_off[(size_t)i] = table[h].off;
             continue;
         }
-        seen[pairs[i].ref] = {ref_bytes, pairs[i].ref_len};
+        table[h] = Slot{r, len, ref_bytes};
         ref_off[(size_t)i] = ref_bytes;
         uniq.push_back(i);
-        ref_bytes += pairs[i].ref_len;
+        ref_bytes += len;
     }
     std::vector<int64_t> alt_off((size_t)n + 1);
     alt_off[0] = 0;
