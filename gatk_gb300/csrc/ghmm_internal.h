@@ -181,9 +181,10 @@ int sw_pair16_occupancy(int k, int *blocks_per_sm);
 // The exact-substring shortcut of every alignment (state 1 + offset), or state 0 for all when a.shortcut is 0.
 int launch_sw_prepass(const SwArgs &a, int n_pairs, int sm_count, cudaStream_t s);
 int launch_sw_traceback(const SwArgs &a, int n_pairs, cudaStream_t s);
-// exclusive scan of the chunk's n_ops into starts (offset by *running, which then advances), gather into ops
+// exclusive scan of the chunk's n_ops into starts (offset by *running, which then advances), gather into ops;
+// block_sums: ceil(n_pairs / 1024) int64 of scratch
 int launch_sw_compact(const SwArgs &a, int n_pairs, int64_t *starts, int64_t *running, uint32_t *ops, int64_t ops_cap,
-                      cudaStream_t s);
+                      int64_t *block_sums, cudaStream_t s);
 
 // Read-to-best-haplotype realignment setup (sw.cu): per read, the best haplotype of its region by
 // AlleleLikelihoods.searchBestAllele with tie-breaking priorities, written into the read's SwPair (ref fields).

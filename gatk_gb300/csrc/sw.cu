@@ -4,20 +4,22 @@
 // of `alt` against `ref`, for the four overhang strategies, bit-identical to the Java code.
 //
 // Pipeline of one batch (all on one stream):
-//   sw_forward_kernel<K>  one warp per alignment.  The exact-substring shortcut (Utils.lastIndexOf, Utils.java:
-//                         1124-1138) is tested first when enabled.  Otherwise an anti-diagonal wavefront fills the
-//                         score recurrence of calculateMatrix (:109-228): lane l owns K consecutive alt columns,
-//                         the warp streams over the ref rows, each lane passing its last column's score and the
-//                         row's best horizontal gap to the next lane every step.  Alts longer than 32*K run in
-//                         strips of 32*K columns whose boundary column goes through a per-pair scratch.  Per cell
-//                         it keeps 4 traceback bits (not diagonal; horizontal >= vertical; vertical gap opened here;
-//                         horizontal gap opened here), from which the traceback rebuilds the backtrack entry
-//                         0 / -ki / +kd exactly: a gap's length is the distance to the cell that opened it.  The last
-//                         column's and the bottom row's scores go to an edge array for the end-cell choice.
+//   sw_prepass_kernel     the exact-substring shortcut (Utils.lastIndexOf, Utils.java:1124-1138), one warp per
+//                         alignment, when enabled; the host then plans chunks and tasks with the exact lengths.
+//   sw_pair16_kernel<K>   two alignments per warp in the 16-bit halves of each register, for alignments whose scores
+//                         provably fit; sw_forward_kernel<K, CLAMP> one alignment per warp in int32 for the rest.
+//                         Both run calculateMatrix's recurrence (:109-228) as an anti-diagonal wavefront: lane l owns
+//                         K consecutive alt columns, the warp streams over the ref rows, each lane passing its last
+//                         column's score and the row's best horizontal gap to the next lane every step.  Alts longer
+//                         than 32*K run in strips of 32*K columns (int32 kernel) whose boundary column goes through a
+//                         per-pair scratch.  Per cell 4 traceback bits (not diagonal; horizontal >= vertical;
+//                         vertical gap opened here; horizontal gap opened here), from which the traceback rebuilds
+//                         the backtrack entry 0 / -ki / +kd exactly: a gap's length is the distance to the cell that
+//                         opened it.  The last column's and the bottom row's scores go to an edge array.
 //   sw_traceback_kernel   one thread per alignment: end cell per strategy, traceback, cigar elements in reverse
 //                         into a per-pair slot (calculateCigar, :261-379).
-//   sw_scan_kernel        exclusive prefix sums (one block) of per-pair counts.
-//   sw_gather_kernel      slot -> compact, forward-ordered BAM-encoded cigar ops.
+//   sw_scan_*_kernel      exclusive prefix sums of per-pair element counts and the copy into one compact array of
+//                         forward-ordered BAM-encoded cigar ops.
 // Scores are int32 with Java's wrapping adds; every comparison is the Java one, so ties resolve identically.
 #include <cuda_runtime.h>
 
@@ -433,14 +435,29 @@ __global__ void __launch_bounds__(128) sw_prepass_kernel(SwArgs A, int n_pairs) 
 }
 
 // traceback bits of cell (i, j), 1-based
-__device__ __forceinline__ uint32_t tb_code(const SwArgs &A, const SwPair &P, int K, int i, int j) {
-    const int w = 32 * K;
-    const int s = (j - 1) / w, within = (j - 1) - s * w;
-    const int lane = within / K, k = within - lane * K;
-    const int64_t t = (int64_t)(i - 1) + lane;
-    return (A.tb[P.tb_off + (int64_t)s * sw_steps4(P.ref_len) * 32 + ((t >> 2) * 32 + lane) * 4 + (t & 3)] >> (4 * k)) &
-           15u;
-}
+// Traceback bits of cell (i, j), 1-based.  Keeps the last 16-byte group (4 steps of one lane) it loaded: walks move
+// one step back per cell along a lane, so most cells come from the group already held.
+struct TbReader {
+    const uint32_t *base;  // the alignment's words
+    int64_t strip_words;
+    int K;
+    int64_t held = -1;     // word index of the group held
+    uint4 g;
+    __device__ __forceinline__ uint32_t code(int i, int j) {
+        const int w = 32 * K;
+        const int s = (j - 1) / w, within = (j - 1) - s * w;
+        const int lane = within / K, k = within - lane * K;
+        const int64_t t = (int64_t)(i - 1) + lane;
+        const int64_t grp = (int64_t)s * strip_words + ((t >> 2) * 32 + lane) * 4;
+        if (grp != held) {
+            g = *reinterpret_cast<const uint4 *>(base + grp);
+            held = grp;
+        }
+        const int q = (int)(t & 3);
+        const uint32_t word = q == 0 ? g.x : q == 1 ? g.y : q == 2 ? g.z : g.w;
+        return (word >> (4 * k)) & 15u;
+    }
+};
 
 __global__ void sw_traceback_kernel(SwArgs A, int n_pairs) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -511,22 +528,26 @@ __global__ void sw_traceback_kernel(SwArgs A, int n_pairs) {
         push(kSwOpS, segment);
         segment = 0;
     }
+    TbReader rd;
+    rd.base = A.tb + P.tb_off;
+    rd.strip_words = sw_steps4(n) * 32;
+    rd.K = K;
     int state = kSwOpM;
     int guard = n + m + 2;
     do {
-        const uint32_t c = tb_code(A, P, K, p1, p2);
+        const uint32_t c = rd.code(p1, p2);
         int ns, step = 1;
         if (!(c & 1u)) {
             ns = kSwOpM;
         } else if (c & 2u) {  // horizontal: the gap's length is the distance back to the cell that opened it
             ns = kSwOpI;
             int q = p2;
-            while (q > 1 && !(tb_code(A, P, K, p1, q) & 8u)) --q;
+            while (q > 1 && !(rd.code(p1, q) & 8u)) --q;
             step = p2 - q + 1;
         } else {              // vertical
             ns = kSwOpD;
             int r = p1;
-            while (r > 1 && !(tb_code(A, P, K, r, p2) & 4u)) --r;
+            while (r > 1 && !(rd.code(r, p2) & 4u)) --r;
             step = p1 - r + 1;
         }
         if (ns == kSwOpM) {
@@ -569,45 +590,80 @@ __global__ void sw_traceback_kernel(SwArgs A, int n_pairs) {
     A.offset[p] = off;
 }
 
-// exclusive prefix sums of `n` int32 counts into int64, starting at *running, which then advances by their sum
-// (one block of 1024 threads, each over a contiguous chunk)
-__global__ void __launch_bounds__(1024) sw_scan_kernel(const int32_t *counts, int64_t *starts, int64_t n,
-                                                       int64_t *running) {
-    __shared__ int64_t part[1024];
-    const int t = threadIdx.x;
-    const int64_t chunk = (n + 1023) / 1024;
-    const int64_t b = min(n, (int64_t)t * chunk), e = min(n, b + chunk);
-    int64_t sum = 0;
-    for (int64_t i = b; i < e; ++i) sum += counts[i];
-    part[t] = sum;
-    __syncthreads();
-    for (int d = 1; d < 1024; d <<= 1) {
-        const int64_t v = t >= d ? part[t - d] : 0;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
+// Cigar compaction: exclusive prefix sums of the chunk's op counts, starting at *running (which then advances by
+// their sum), and the reversed per-pair slots copied out in forward order.  Three kernels: per-block sums of 1024
+// counts, one block scanning those sums, and a per-block scan plus the copy.
+constexpr int kScanBlock = 1024;
+
+__device__ __forceinline__ int64_t block_exclusive_scan(int64_t v, int64_t *sh, int64_t *total) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    int64_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
     }
-    const int64_t base = *running;
-    int64_t run = base + part[t] - sum;
-    for (int64_t i = b; i < e; ++i) {
-        starts[i] = run;
-        run += counts[i];
+    if (lane == 31) sh[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int64_t w = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, w, d);
+            if (lane >= d) w += y;
+        }
+        sh[lane] = w;
     }
     __syncthreads();
-    if (t == 1023) *running = base + part[1023];
+    const int64_t before = (warp > 0 ? sh[warp - 1] : 0) + x - v;
+    if (total) *total = sh[(blockDim.x >> 5) - 1];
+    return before;
 }
 
-// reversed per-pair slots -> compact forward-ordered ops (an output that would pass ops_cap sets the error flag)
-__global__ void sw_gather_kernel(SwArgs A, const int64_t *starts, uint32_t *ops, int64_t ops_cap, int n_pairs) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n_pairs) return;
-    const int c = A.n_ops[p];
-    if (starts[p] + c > ops_cap) {
+__global__ void __launch_bounds__(kScanBlock) sw_scan_partials_kernel(const int32_t *counts, int64_t n,
+                                                                      int64_t *block_sums) {
+    __shared__ int64_t sh[32];
+    const int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+    const int64_t v = i < n ? counts[i] : 0;
+    int64_t tot = 0;
+    block_exclusive_scan(v, sh, &tot);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
+}
+
+// one block: exclusive scan of the block sums in chunks of 1024, offset by *running, which advances
+__global__ void __launch_bounds__(kScanBlock) sw_scan_blocks_kernel(int64_t *block_sums, int64_t nb, int64_t *running) {
+    __shared__ int64_t sh[32];
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = *running;
+    __syncthreads();
+    for (int64_t b0 = 0; b0 < nb; b0 += kScanBlock) {
+        const int64_t b = b0 + threadIdx.x;
+        const int64_t v = b < nb ? block_sums[b] : 0;
+        int64_t tot = 0;
+        const int64_t before = block_exclusive_scan(v, sh, &tot);
+        if (b < nb) block_sums[b] = carry + before;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *running = carry;
+}
+
+__global__ void __launch_bounds__(kScanBlock) sw_scan_gather_kernel(SwArgs A, const int64_t *block_sums,
+                                                                    int64_t *starts, uint32_t *ops, int64_t ops_cap,
+                                                                    int64_t n) {
+    __shared__ int64_t sh[32];
+    const int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+    const int c = i < n ? A.n_ops[i] : 0;
+    const int64_t st = block_sums[blockIdx.x] + block_exclusive_scan(c, sh, nullptr);
+    if (i >= n) return;
+    starts[i] = st;
+    if (st + c > ops_cap) {
         atomicExch(A.error, 2);
         return;
     }
-    const uint32_t *slot = A.slot + A.pairs[p].slot_off;
-    uint32_t *o = ops + starts[p];
+    const uint32_t *slot = A.slot + A.pairs[i].slot_off;
+    uint32_t *o = ops + st;
     for (int q = 0; q < c; ++q) o[q] = slot[c - 1 - q];
 }
 
@@ -816,10 +872,12 @@ int launch_sw_traceback(const SwArgs &a, int n_pairs, cudaStream_t s) {
 }
 
 int launch_sw_compact(const SwArgs &a, int n_pairs, int64_t *starts, int64_t *running, uint32_t *ops, int64_t ops_cap,
-                      cudaStream_t s) {
+                      int64_t *block_sums, cudaStream_t s) {
     if (n_pairs <= 0) return 0;
-    sw_scan_kernel<<<1, 1024, 0, s>>>(a.n_ops, starts, n_pairs, running);
-    sw_gather_kernel<<<(n_pairs + 127) / 128, 128, 0, s>>>(a, starts, ops, ops_cap, n_pairs);
+    const int64_t nb = ((int64_t)n_pairs + kScanBlock - 1) / kScanBlock;
+    sw_scan_partials_kernel<<<(unsigned)nb, kScanBlock, 0, s>>>(a.n_ops, n_pairs, block_sums);
+    sw_scan_blocks_kernel<<<1, kScanBlock, 0, s>>>(block_sums, nb, running);
+    sw_scan_gather_kernel<<<(unsigned)nb, kScanBlock, 0, s>>>(a, block_sums, starts, ops, ops_cap, n_pairs);
     return (int)cudaGetLastError();
 }
 

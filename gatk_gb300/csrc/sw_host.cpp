@@ -37,6 +37,7 @@ struct SwEngine {
     DevBuf<uint8_t> d_planes;
     DevBuf<int32_t> d_res;      // state | offset | n_ops | best, n each
     DevBuf<int64_t> d_starts;
+    DevBuf<int64_t> d_block_sums;
     DevBuf<uint32_t> d_ops;
     DevBuf<int64_t> d_counters; // [0] running op total, [1] error flag (as int), then int cursors
     DevBuf<uint32_t> d_tb;
@@ -66,6 +67,7 @@ struct SwEngine {
         h_pairs.release(); d_pairs.release(); h_tasks.release(); d_tasks.release(); h_planes.release();
         h_pair_tasks.release(); d_pair_tasks.release();
         d_planes.release(); d_res.release(); d_starts.release(); d_ops.release(); d_counters.release();
+        d_block_sums.release();
         d_tb.release(); d_edges.release(); d_scratch.release(); d_slot.release(); d_prio.release(); d_inf.release();
         h_res.release(); h_starts.release(); h_counters.release(); h_ops.release();
         for (auto e : events) cudaEventDestroy(e);
@@ -405,6 +407,7 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
     SW_CUDA(E.d_edges.reserve((size_t)std::max<int64_t>(cap.edges, 4)), "edge scores");
     SW_CUDA(E.d_scratch.reserve((size_t)std::max<int64_t>(cap.scratch, 1)), "strip scratch");
     SW_CUDA(E.d_slot.reserve((size_t)std::max<int64_t>(tot.slots, 1)), "cigar slots");
+    SW_CUDA(E.d_block_sums.reserve((size_t)(n / 1024 + 2)), "scan block sums");
     SW_CUDA(cudaMemsetAsync(E.d_counters.p, 0, 2 * sizeof(int64_t), s), "zero counters");
     int *d_err = reinterpret_cast<int *>(E.d_counters.p + 1);
     int *d_cursors = reinterpret_cast<int *>(E.d_counters.p + 2);  // 2 x 9 task cursors, reset per chunk
@@ -490,9 +493,9 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         fwd_events.emplace_back(e0, e1);
         int e = launch_sw_traceback(a, (int)cn, s);
         if (e) return cuda_error(ctx, (cudaError_t)e, "Smith-Waterman traceback launch");
-        e = launch_sw_compact(a, (int)cn, E.d_starts.p + ch.p0, E.d_counters.p, E.d_ops.p, in.ops_cap, s);
+        e = launch_sw_compact(a, (int)cn, E.d_starts.p + ch.p0, E.d_counters.p, E.d_ops.p, in.ops_cap, E.d_block_sums.p, s);
         if (e) return cuda_error(ctx, (cudaError_t)e, "Smith-Waterman cigar compaction launch");
-        launches += 3;
+        launches += 4;
         if (ch.p1 >= n) break;
         const int rc = plan_chunk(ch.p1, next);
         if (rc) return rc;
