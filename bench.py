@@ -5,7 +5,7 @@
     python bench.py --stream [--regions N] [--batch-cells C]     (workload 4 through the streaming queue)
     python bench.py --calib                                      (workload 3: calibration forward + backward)
     python bench.py --pd [--regions N]                           (PD-HMM, DRAGEN-GATK mode)
-    python bench.py --sw [--regions N]                           (Smith-Waterman realignment to the best haplotype)
+    python bench.py --sw [--regions N] [--workload 2]            (Smith-Waterman realignment to the best haplotype)
 
 A step is one forward over the whole workload (default: workload 1, 10,000 synthetic active regions,
 seed 1, ~1.06e12 cells): every read x haplotype pair of every region, FP32 wavefront plus the FP64 rerun
@@ -652,7 +652,7 @@ def run_sw(args):
     from oracle import oracle as O
 
     eng = Engine()
-    wl = W.generate(1, regions=args.regions or None)
+    wl = W.generate(args.workload, regions=args.regions or (100 if args.workload == 2 else None))
     n_regions = wl.n_regions
     batch = Batch(eng, wl)
     batch.forward()
@@ -715,8 +715,8 @@ def run_sw(args):
         "metric": "Smith-Waterman realignment GCUPS (reads to their best haplotype) on 1 GB300",
         "value": cells / (ms_dev * 1e-3) / 1e9, "unit": "GCUPS", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_dev, "higher_is_better": True, "dtype": "int32",
-        "data": "synthetic (workload 1; best haplotypes from the PairHMM forward)",
-        "config": {"workload": f"config1: {n_regions} regions, every read against its best haplotype",
+        "data": f"synthetic (workload {args.workload}; best haplotypes from the PairHMM forward)",
+        "config": {"workload": f"config{args.workload}: {n_regions} regions, every read against its best haplotype",
                    "reads": int(wl.n_reads), "alignments_with_recurrence": int(st["n_alignments"] - st["n_shortcut"]),
                    "substring_shortcut": int(st["n_shortcut"]), "cells": int(cells), "chunks": int(st["chunks"]),
                    "int16_paired_alignments": int(st["n_int16"]),
