@@ -51,6 +51,14 @@ struct SwEngine {
     HostBuf<int64_t> h_counters;
     HostBuf<uint32_t> h_ops;
     std::vector<cudaEvent_t> events;
+    struct RefSlot {  // reference deduplication of ghmm_sw_align_batch
+        const uint8_t *ref;
+        int32_t len;
+        uint32_t gen;
+        int64_t off;
+    };
+    std::vector<RefSlot> ref_table;
+    uint32_t ref_gen = 0;
     ghmm_sw_stats stats{};
     bool allow16 = true;  // pair eligible alignments in the 16-bit kernel
     int64_t tb_budget_words = 0;  // traceback words per chunk; 0: chosen on first use
@@ -603,15 +611,21 @@ int sw_batch(ghmm_ctx *ctx, const CtxInfo &ci, const ghmm_sw_pair *pairs, int64_
             return ctx_fail(ctx, GHMM_ERR_ARG, "sequence longer than GHMM_SW_MAX_LEN");
     }
     // refs deduplicated by (address, length): a haplotype shared by many reads is copied once (an open-addressing
-    // table keyed by the address, twice the pairs in size)
+    // table keyed by the address, at least twice the pairs in size, kept by the engine; a slot is in use when it
+    // carries this call's generation, so nothing is cleared between calls)
     size_t tcap = 16;
     while (tcap < (size_t)n * 2) tcap <<= 1;
-    struct Slot {
-        const uint8_t *ref;
-        int32_t len;
-        int64_t off;
-    };
-    std::vector<Slot> table(tcap, Slot{nullptr, 0, 0});
+    if (E.ref_table.size() < tcap) {
+        E.ref_table.assign(tcap, SwEngine::RefSlot{nullptr, 0, 0, 0});
+        E.ref_gen = 0;
+    }
+    tcap = E.ref_table.size();
+    if (++E.ref_gen == 0) {  // the generation counter wrapped: start the table over
+        std::fill(E.ref_table.begin(), E.ref_table.end(), SwEngine::RefSlot{nullptr, 0, 0, 0});
+        E.ref_gen = 1;
+    }
+    const uint32_t gen = E.ref_gen;
+    SwEngine::RefSlot *table = E.ref_table.data();
     std::vector<int64_t> ref_off((size_t)n);
     std::vector<int64_t> uniq;  // pair index of each distinct ref
     int64_t ref_bytes = 0;
@@ -619,12 +633,12 @@ int sw_batch(ghmm_ctx *ctx, const CtxInfo &ci, const ghmm_sw_pair *pairs, int64_
         const uint8_t *r = pairs[i].ref;
         const int32_t len = pairs[i].ref_len;
         size_t h = (size_t)(((uint64_t)(uintptr_t)r * 0x9E3779B97F4A7C15ull) >> 17) & (tcap - 1);
-        while (table[h].ref && !(table[h].ref == r && table[h].len == len)) h = (h + 1) & (tcap - 1);
-        if (table[h].ref) {
+        while (table[h].gen == gen && !(table[h].ref == r && table[h].len == len)) h = (h + 1) & (tcap - 1);
+        if (table[h].gen == gen) {
             ref_off[(size_t)i] = table[h].off;
             continue;
         }
-        table[h] = Slot{r, len, ref_bytes};
+        table[h] = SwEngine::RefSlot{r, len, gen, ref_bytes};
         ref_off[(size_t)i] = ref_bytes;
         uniq.push_back(i);
         ref_bytes += len;
