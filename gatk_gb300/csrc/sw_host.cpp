@@ -14,6 +14,7 @@
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -460,8 +461,11 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
         return GHMM_OK;
     };
     Chunk next;
-    if (n > 0) {
+    if (n > 0) {  // a first chunk of a quarter of the budget starts the GPU sooner; later ones use all of it
+        const SwCaps full = cap;
+        cap.words = std::max(cap.words / 4, tot.max_words);
         const int rc = plan_chunk(0, next);
+        cap = full;
         if (rc) return rc;
     }
     E.stats.ms_host += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_plan).count();
@@ -575,24 +579,31 @@ SwEngine *engine(const CtxInfo &ci) {
 }
 
 // results of pairs [0, n) from the engine's host buffers into the caller's arrays
-int deliver(ghmm_ctx *ctx, SwEngine &E, int64_t n, const int32_t *ref_len_of, ghmm_sw_result *res) {
+int deliver(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, int64_t n, const int32_t *ref_len_of,
+            ghmm_sw_result *res) {
     const int32_t *state = E.h_res.p, *offset = E.h_res.p + n, *nops = E.h_res.p + 2 * n;
     const int64_t total = E.h_counters.p[0];
-    int64_t n_short = 0, cells = 0;
-    for (int64_t i = 0; i < n; ++i) {
-        res->alignment_offset[i] = offset[i];
-        res->cigar_start[i] = E.h_starts.p[i];
-        res->cigar_len[i] = nops[i];
-        if (ref_len_of && ref_len_of[i] <= 0) continue;  // not aligned
-        if (state[i] == 1)
-            ++n_short;
-        else if (ref_len_of)
-            cells += (int64_t)ref_len_of[i] * E.h_pairs.p[i].alt_len;
-    }
-    if (total > 0) std::memcpy(res->cigar_ops, E.h_ops.p, (size_t)total * sizeof(uint32_t));
+    const int parts = std::max(1, ci.threads);
+    std::vector<int64_t> n_short((size_t)parts, 0), cells((size_t)parts, 0);
+    const int64_t per = (n + parts - 1) / parts;
+    parallel_for(parts, parts, [&](int64_t t) {
+        for (int64_t i = t * per; i < std::min(n, (t + 1) * per); ++i) {
+            res->alignment_offset[i] = offset[i];
+            res->cigar_start[i] = E.h_starts.p[i];
+            res->cigar_len[i] = nops[i];
+            if (ref_len_of && ref_len_of[i] <= 0) continue;  // not aligned
+            if (state[i] == 1)
+                ++n_short[(size_t)t];
+            else if (ref_len_of)
+                cells[(size_t)t] += (int64_t)ref_len_of[i] * E.h_pairs.p[i].alt_len;
+        }
+        // this part's share of the cigar ops
+        const int64_t o0 = total * t / parts, o1 = total * (t + 1) / parts;
+        if (o1 > o0) std::memcpy(res->cigar_ops + o0, E.h_ops.p + o0, (size_t)(o1 - o0) * sizeof(uint32_t));
+    }, 1);
     res->cigar_total = total;
-    E.stats.n_shortcut = n_short;
-    E.stats.cells = cells;
+    E.stats.n_shortcut = std::accumulate(n_short.begin(), n_short.end(), int64_t(0));
+    E.stats.cells = std::accumulate(cells.begin(), cells.end(), int64_t(0));
     (void)ctx;
     return GHMM_OK;
 }
@@ -678,7 +689,7 @@ int sw_batch(ghmm_ctx *ctx, const CtxInfo &ci, const ghmm_sw_pair *pairs, int64_
     in.t0 = t0;
     int rc = run(ctx, ci, E, in, plane_bytes, nullptr);
     if (rc) return rc;
-    rc = deliver(ctx, E, n, ref_len.data(), res);
+    rc = deliver(ctx, ci, E, n, ref_len.data(), res);
     E.stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return rc;
 }
@@ -768,12 +779,12 @@ int ghmm_batch_realign(ghmm_ctx *ctx, ghmm_batch *batch, const double *hap_prior
     const int64_t *read_off = bi.h_off;
     SW_CUDA(E.h_pairs.reserve((size_t)n), "pinned pairs");
     // the reads; their haplotypes are chosen on the device (reads of a region without haplotypes are not aligned)
-    for (int64_t r = 0; r < n; ++r) {
+    parallel_for(n, ci.threads, [&](int64_t r) {
         SwPair &P = E.h_pairs.p[r];
         P = SwPair{};
         P.alt_off = read_off[r];
         P.alt_len = (int32_t)(read_off[r + 1] - read_off[r]);
-    }
+    }, 4096);
     for (int64_t r = 0; r < n; ++r)
         if (E.h_pairs.p[r].alt_len <= 0)
             return ctx_fail(ctx, GHMM_ERR_ARG,
@@ -799,7 +810,7 @@ int ghmm_batch_realign(ghmm_ctx *ctx, ghmm_batch *batch, const double *hap_prior
         informative[r] = inf[(size_t)r];
         ref_len[(size_t)r] = E.h_pairs.p[r].ref_len;  // the chosen haplotype's length (0: not aligned)
     }
-    rc = deliver(ctx, E, n, ref_len.data(), result);
+    rc = deliver(ctx, ci, E, n, ref_len.data(), result);
     E.stats.d2h_bytes += n * (int64_t)sizeof(int32_t);
     E.stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return rc;
