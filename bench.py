@@ -629,6 +629,132 @@ def run_pd(args):
     return 0
 
 
+def _prep_tables():
+    """The DRAGstr model the reference's HaplotypeCaller integration tests run with (its example parameter file,
+    extracted to tests/golden/dragstr_cases.json): GOP and GCP tables of 8 periods x 20 repeat lengths."""
+    import numpy as np
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "dragstr_cases.json")) as f:
+        t = json.load(f)["example_params"]
+    return np.array(t["gop"]), np.array(t["gcp"])
+
+
+def measured_hbm_peak() -> float:
+    """HBM copy bandwidth in GB/s from MEASURED_PEAKS.json (6800 GB/s, an earlier GB300 measurement, without it)."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
+
+
+PREP_BYTES_PER_BASE = {"pcr": 7, "dragstr": 6}  # pcr: read bases, quals, BI, BD; write quals, BI, BD.
+#                                                 dragstr: read bases, quals; write quals, GOP (ins = del), GCP
+
+
+def run_prep(args):
+    """--prep: the read preparation before the PairHMM on the device (ghmm_batch_create_raw), over every read of
+    workload 1 with seeded raw base qualities, BI / BD tags and mapping qualities.  Two imputations:
+    `pcr` (PairHMMLikelihoodCalculationEngine.modifyReadQualities with the CONSERVATIVE PCR indel model and the
+    standard imputation) and `dragstr` (DragstrPairHMMInputScoreImputator with the reference's example DRAGstr
+    model).  `value` is reads prepared per second by the device kernels (CUDA events around them, planes resident);
+    e2e is the likelihood call ghmm_compute_regions_raw from raw reads in host memory against the same call on
+    planes prepared beforehand (ghmm_compute_regions): the difference is what preparation costs inside a call."""
+    import numpy as np
+
+    from gatk_gb300 import native, workload as W
+    from gatk_gb300.pairhmm import Engine
+    from oracle import readprep as RP
+
+    mode = args.prep
+    eng = Engine()
+    n_regions = args.regions or 0
+    wl = W.generate(1, regions=n_regions) if n_regions else W.generate(1)
+    rng = np.random.default_rng(23)
+    wl.quals[:] = rng.integers(2, 45, size=len(wl.quals)).astype(np.uint8)
+    wl.ins[:] = rng.integers(20, 50, size=len(wl.ins)).astype(np.uint8)
+    wl.dels[:] = rng.integers(20, 50, size=len(wl.dels)).astype(np.uint8)
+    mapq = rng.integers(10, 70, size=wl.n_reads)
+    kw = {"pcr_rate_factor": 3.0}
+    if mode == "dragstr":
+        kw["dragstr"] = _prep_tables()
+    bases = int(len(wl.bases))
+    cells = int(wl.cells_per_region().sum())
+    for _ in range(args.warmup):
+        with eng.raw_batch(wl, mapq, **kw) as b:
+            b.stats()
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms = []
+    for _ in range(args.steps):
+        with eng.raw_batch(wl, mapq, **kw) as b:
+            ms.append(b.stats()["ms_prep"])
+    clk = clocks.stop()
+    with eng.raw_batch(wl, mapq, **kw) as b:
+        planes = b.read_planes()
+        b.forward()
+        fst = b.stats()
+    ms_prep = statistics.mean(ms)
+    # e2e: raw reads in host memory -> likelihoods in host memory, against the call on prepared planes
+    prepared = W.Workload(region_read_off=wl.region_read_off, region_hap_off=wl.region_hap_off, read_off=wl.read_off,
+                          bases=wl.bases, quals=planes[1], ins=planes[2], dels=planes[3], gcp=planes[4],
+                          hap_off=wl.hap_off, hap_bases=wl.hap_bases, out_off=wl.out_off)
+    raw_out = eng.compute_raw(wl, mapq, **kw)
+    prep_out = eng.compute(prepared)
+    t_raw, t_prep = [], []
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        eng.compute_raw(wl, mapq, **kw)
+        t_raw.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        eng.compute(prepared)
+        t_prep.append(time.perf_counter() - t0)
+    dt_raw, dt_prep = min(t_raw), min(t_prep)
+    # parity and the CPU baseline: the oracle's prepare_read on the leading reads (bounded sample)
+    n_cpu = 0
+    mism = 0
+    t1 = time.perf_counter()
+    while n_cpu < wl.n_reads and time.perf_counter() - t1 < args.cpu_seconds:
+        a, e = int(wl.read_off[n_cpu]), int(wl.read_off[n_cpu + 1])
+        _, q, i, d, g = RP.prepare_read(wl.bases[a:e], wl.quals[a:e], wl.ins[a:e], wl.dels[a:e], int(mapq[n_cpu]),
+                                        rate_factor=3.0, dragstr=kw.get("dragstr"))
+        got = [bytes(planes[k][a:e]) for k in (1, 2, 3, 4)]
+        mism += int(got != [q, i, d, g])
+        n_cpu += 1
+    cpu_dt = time.perf_counter() - t1
+    algo_bytes = PREP_BYTES_PER_BASE[mode] * bases
+    achieved = algo_bytes / (ms_prep * 1e-3) / 1e9
+    peak = measured_hbm_peak()
+    line = {
+        "metric": f"reads prepared per second ({mode} imputation) on 1 GB300", "value": wl.n_reads / (ms_prep * 1e-3),
+        "unit": "reads/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_prep,
+        "higher_is_better": True, "dtype": "u8", "data": "synthetic (workload 1 reads with seeded raw qualities)",
+        "config": {"workload": f"every read of config1 ({wl.n_regions} regions, {wl.n_reads} reads, {bases} bases), "
+                               f"{mode} imputation" + (" with the reference's example DRAGstr model (8 x 20)"
+                                                       if mode == "dragstr" else ", CONSERVATIVE PCR model"),
+                   "reads": wl.n_reads, "bases": bases},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "bytes_per_base": PREP_BYTES_PER_BASE[mode],
+                     "kernel": "prep_kernel + dragstr_kernel" if mode == "dragstr" else "prep_kernel"},
+        "e2e": {"value": cells / dt_raw / 1e9, "unit": "GCUPS", "ms_per_step": dt_raw * 1e3,
+                "api": "ghmm_compute_regions_raw", "prepared_planes_ms": dt_prep * 1e3,
+                "prepared_planes_gcups": cells / dt_prep / 1e9,
+                "h2d_bytes_per_step": int(5 * bases + len(wl.hap_bases) + 4 * wl.n_reads),
+                "d2h_bytes_per_step": int(8 * wl.n_pairs),
+                "max_abs_dlog10_vs_prepared_planes": float(absdiff(raw_out, prep_out).max()),
+                "fp64_direct_pairs": int(fst["n_fp64_direct"]), "fp64_rerun_pairs": int(fst["n_rerun"])},
+        "gpu_launches": args.steps * (2 if mode == "dragstr" else 1),
+        "clocks": clk,
+        "cpu_baseline": {"value": n_cpu / cpu_dt, "unit": "reads/s", "cores": 1, "kind": "port",
+                         "sample": f"first {n_cpu} reads through oracle/readprep.py prepare_read (Python)",
+                         "host": f"{platform.machine()} x{os.cpu_count()}"},
+        "parity": {"reads": n_cpu, "mismatched_reads": mism},
+    }
+    print(json.dumps(line), flush=True)
+    eng.close()
+    return 0
+
+
 SW_OPS_PER_CELL = 12  # calculateMatrix's inner loop: 5 adds, 6 compares / maxima, the base compare
 
 
@@ -810,6 +936,9 @@ def main():
     ap.add_argument("--pd", action="store_true", help="PD-HMM over workload 1 regions with synthetic PD flags")
     ap.add_argument("--calib", action="store_true",
                     help="time the calibration forward + backward on workload 3 and check its gradient")
+    ap.add_argument("--prep", choices=["pcr", "dragstr"], default=None,
+                    help="read preparation on the device over every workload 1 read (PCR model or DRAGstr)")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="time bound of the --prep CPU sample")
     ap.add_argument("--sw", action="store_true",
                     help="Smith-Waterman realignment of every workload 1 read to its best haplotype")
     args = ap.parse_args()
@@ -827,6 +956,8 @@ def main():
         return run_pd(args)
     if args.sw:
         return run_sw(args)
+    if args.prep:
+        return run_prep(args)
     return run_ours(args)
 
 

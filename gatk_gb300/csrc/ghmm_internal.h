@@ -111,8 +111,14 @@ struct PrepArgs {
     const int32_t *mapq;     // per read
     uint8_t pcr_cache[24];   // PCR indel model quality per repeat length 0..20
     int pcr, cap_to_mapq, threshold;
+    // DRAGstr imputation (dragstr != 0): DragstrParams' GOP and GCP tables [max period][max repeats]
+    const double *str_gop, *str_gcp;
+    int dragstr, str_max_period, str_max_repeats, max_read_len;
 };
 int launch_prep(const DevBatch &b, int64_t n_reads, const PrepArgs &p, int sm_count, cudaStream_t s);
+int launch_dragstr(const DevBatch &b, int64_t n_reads, const PrepArgs &p, int sm_count, cudaStream_t s);
+constexpr int kDragstrMaxRead = 28000;  // reads the DRAGstr kernel's shared memory holds (8 bytes per base)
+constexpr int kDragstrMaxPeriod = 32;
 
 // Post-likelihood normalisation and filtering (post.cu).
 struct PostArgs {

@@ -7,7 +7,9 @@
 //   - base qualities capped by the mapping quality (unless disabled), then base qualities below the threshold and
 //     insertion / deletion qualities below 6 set to 6 (compared as Java's signed bytes).
 // The batch's planes hold the raw values (missing insertion / deletion qualities as 45, the constant gap continuation
-// penalty filled in); this kernel rewrites quals, ins and dels in place, one thread per read.
+// penalty filled in); prep_kernel rewrites quals, ins and dels in place, one warp per read with its lanes over the
+// positions.  With the DRAGstr imputation (DragstrPairHMMInputScoreImputator.java:54-88, DragstrReadSTRAnalyzer)
+// dragstr_kernel caps the base qualities and writes ins, dels and gcp instead, also one warp per read.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -22,7 +24,7 @@ constexpr int kMaxRepeat = 20;
 
 // findNumberOfRepetitions over sub-ranges of the read: copies of unit b[u, u+L) at the start (leading) or the end
 // (trailing) of b[t, t+n)
-__device__ int repetitions(const uint8_t *b, int u, int L, int t, int n, bool leading) {
+__device__ __forceinline__ int repetitions(const uint8_t *b, int u, int L, int t, int n, bool leading) {
     if (n == 0) return 0;
     int count = 0;
     if (leading) {
@@ -41,7 +43,7 @@ __device__ int repetitions(const uint8_t *b, int u, int L, int t, int n, bool le
     return count;
 }
 
-__device__ bool same_unit(const uint8_t *b, int u1, int l1, int u2, int l2) {
+__device__ __forceinline__ bool same_unit(const uint8_t *b, int u1, int l1, int u2, int l2) {
     if (l1 != l2) return false;
     for (int k = 0; k < l1; ++k)
         if (b[u1 + k] != b[u2 + k]) return false;
@@ -49,7 +51,7 @@ __device__ bool same_unit(const uint8_t *b, int u1, int l1, int u2, int l2) {
 }
 
 // findTandemRepeatUnits(...).getRight() at `offset` of a read of n bases
-__device__ int tandem_repeat_length(const uint8_t *b, int n, int offset) {
+__device__ __forceinline__ int tandem_repeat_length(const uint8_t *b, int n, int offset) {
     int max_bw = 0, bw_u = offset, bw_l = 1;
     for (int L = 1; L <= kMaxUnit; ++L) {
         if (offset + 1 - L < 0) break;
@@ -81,40 +83,179 @@ __device__ int tandem_repeat_length(const uint8_t *b, int n, int offset) {
 
 __device__ __forceinline__ int as_java_byte(int v) { return v > 127 ? v - 256 : v; }
 
+// bases a warp stages in shared memory for the tandem-repeat search; longer reads are searched in place
+constexpr int kPrepWarps = 8;
+constexpr int kPrepStage = 1024;
+
+__device__ __forceinline__ uint8_t cap_base_quality(int q, int mapq, const PrepArgs &P) {
+    if (P.cap_to_mapq) q = (q < mapq ? q : mapq) & 0xFF;
+    if (as_java_byte(q) < P.threshold) q = 6;
+    return (uint8_t)q;
+}
+
 __global__ void prep_kernel(DevBatch B, uint8_t *quals, uint8_t *ins, uint8_t *dels, int64_t n_reads, PrepArgs P) {
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_reads; r += (int64_t)gridDim.x * blockDim.x) {
+    __shared__ uint8_t stage[kPrepWarps][kPrepStage];
+    __shared__ uint8_t cache[24];  // indexed by repeat length: shared rather than a local copy of the parameter
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 24; ++k) cache[k] = P.pcr_cache[k];
+    }
+    __syncthreads();
+    for (int64_t r = (int64_t)blockIdx.x * kPrepWarps + w; r < n_reads; r += (int64_t)gridDim.x * kPrepWarps) {
         const int64_t o = B.read_off[r];
         const int n = (int)(B.read_off[r + 1] - o);
         const uint8_t *b = B.bases + o;
-        if (P.pcr) {
-            for (int i = 1; i < n; ++i) {
-                const int cap = P.pcr_cache[tandem_repeat_length(b, n, i - 1)];
-                if (ins[o + i - 1] > cap) ins[o + i - 1] = (uint8_t)cap;
-                if (dels[o + i - 1] > cap) dels[o + i - 1] = (uint8_t)cap;
-            }
+        if (P.pcr && n <= kPrepStage) {
+            for (int x = lane; x < n; x += 32) stage[w][x] = b[x];
+            __syncwarp();
+            b = stage[w];
         }
         const int mapq = P.mapq[r];
-        for (int i = 0; i < n; ++i) {
-            int q = quals[o + i];
-            if (P.cap_to_mapq) q = (q < mapq ? q : mapq) & 0xFF;
-            if (as_java_byte(q) < P.threshold) q = 6;
-            quals[o + i] = (uint8_t)q;
-            if (as_java_byte(ins[o + i]) < 6) ins[o + i] = 6;
-            if (as_java_byte(dels[o + i]) < 6) dels[o + i] = 6;
+        for (int x = lane; x < n; x += 32) {
+            quals[o + x] = cap_base_quality(quals[o + x], mapq, P);
+            int iq = ins[o + x], dq = dels[o + x];
+            if (P.pcr && x < n - 1) {  // applyPCRErrorModel: min as unsigned bytes
+                const int cap = cache[tandem_repeat_length(b, n, x)];
+                iq = iq < cap ? iq : cap;
+                dq = dq < cap ? dq : cap;
+            }
+            ins[o + x] = (uint8_t)(as_java_byte(iq) < 6 ? 6 : iq);
+            dels[o + x] = (uint8_t)(as_java_byte(dq) < 6 ? 6 : dq);
         }
+        __syncwarp();
+    }
+}
+
+// Java's Math.round(double) (half up), cast to a byte
+__device__ __forceinline__ uint8_t java_round_byte(double x) {
+    double r = floor(x);
+    if (x - r >= 0.5) r += 1.0;
+    return (uint8_t)((long long)r & 0xFF);
+}
+
+// DRAGstr imputation, one warp per read, in shared memory.  DragstrReadSTRAnalyzer's repeat count of period p at
+// position i is the longest tandem run, in units of p, of a p-mer starting at x in [i - p + 1, i + 1] (a unit
+// starting at 0 counts one repeat fewer, not below 1, for positions before p - 1); the most repeated period wins,
+// ties to the shorter one.  The run through the unit at x is 1 + F + Bk copies, where F copies follow it and Bk
+// precede it.  With D[j] = (base j == base j + p), the units at x and x + p are equal exactly when D is 1 over
+// [x, x + p), so F = floor(LF(x) / p) for LF(x) the run of ones of D starting at x, and Bk = floor(LB(x) / p) for
+// LB(x) the run of ones ending at x - 1.  Both runs come from ballots of D's zeros, 32 positions at a time with the
+// nearest zero carried between chunks (backward for LF, forward for LB); then every position takes the maximum
+// over its window of p + 1 unit starts.
+__device__ __forceinline__ int div_small(int v, int p, uint32_t magic) {  // v / p for 0 <= v < 2^17, p <= 32
+    return p == 1 ? v : (int)__umulhi((uint32_t)v, magic);
+}
+
+__global__ void dragstr_kernel(DevBatch B, uint8_t *quals, uint8_t *ins, uint8_t *dels, uint8_t *gcp, int64_t n_reads,
+                               PrepArgs P, int lpad, int wstride) {
+    extern __shared__ unsigned char smem[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    uint8_t *S = smem + (size_t)w * wstride;  // bases, then LF, the run counts, best repeats and best periods
+    int16_t *LF = reinterpret_cast<int16_t *>(S + lpad);
+    int16_t *C = LF + lpad;
+    int16_t *BR = C + lpad;
+    uint8_t *BP = reinterpret_cast<uint8_t *>(BR + lpad);
+    const int maxp = P.str_max_period, maxr = P.str_max_repeats;
+    for (int64_t r = (int64_t)blockIdx.x * wpb + w; r < n_reads; r += (int64_t)gridDim.x * wpb) {
+        const int64_t o = B.read_off[r];
+        const int n = (int)(B.read_off[r + 1] - o);
+        const int mapq = P.mapq[r];
+        const int nch = (n + 31) >> 5;
+        for (int x = lane; x < n; x += 32) {
+            S[x] = B.bases[o + x];
+            quals[o + x] = cap_base_quality(quals[o + x], mapq, P);
+        }
+        __syncwarp();
+        for (int p = 1; p <= maxp && p <= n; ++p) {
+            const uint32_t magic = (uint32_t)((0x100000000ull + (uint64_t)p - 1) / (uint64_t)p);
+            const int nu = n - p + 1;  // unit starts 0 .. n - p
+            int carry = n;             // nearest zero of D at or after the chunk's end (D is 0 from n - p on)
+            for (int c = nch - 1; c >= 0; --c) {
+                const int x = (c << 5) + lane;
+                const bool d = x + p < n && S[x] == S[x + p];
+                const uint32_t zeros = __ballot_sync(0xffffffffu, !d);
+                const uint32_t ahead = zeros >> lane;
+                const int nz = ahead ? x + __ffs(ahead) - 1 : carry;
+                if (x < nu) LF[x] = (int16_t)(nz - x);
+                if (zeros) carry = (c << 5) + __ffs(zeros) - 1;
+            }
+            __syncwarp();
+            int before = -1;  // nearest zero of D before the chunk
+            for (int c = 0; c < nch; ++c) {
+                const int x = (c << 5) + lane;
+                const bool d = x + p < n && S[x] == S[x + p];
+                const uint32_t zeros = __ballot_sync(0xffffffffu, !d);
+                const uint32_t behind = zeros & ((1u << lane) - 1u);
+                const int pz = behind ? (c << 5) + 31 - __clz(behind) : before;
+                if (x < nu) C[x] = (int16_t)(1 + div_small(LF[x], p, magic) + div_small(x - 1 - pz, p, magic));
+                if (zeros) before = (c << 5) + 31 - __clz(zeros);
+            }
+            __syncwarp();
+            for (int i = lane; i < n; i += 32) {
+                const int lo = i - p + 1 > 0 ? i - p + 1 : 0, hi = i + 1 < nu - 1 ? i + 1 : nu - 1;
+                int best = 0;
+                for (int x = lo; x <= hi; ++x) {
+                    int c = C[x];
+                    if (x == 0 && i < p - 1) c = c - 1 > 1 ? c - 1 : 1;
+                    best = c > best ? c : best;
+                }
+                if (p == 1 || best > BR[i]) {
+                    BR[i] = (int16_t)best;
+                    BP[i] = (uint8_t)p;
+                }
+            }
+            __syncwarp();
+        }
+        // DragstrPairHMMInputScoreImputator.impute with DragstrParams.lookup's clamping of period and repeats
+        for (int i = lane; i < n - 1; i += 32) {
+            const int per = BP[i], rep = BR[i];
+            const int pi = per < maxp ? per - 1 : maxp - 1, ri = rep < maxr ? rep - 1 : maxr - 1;
+            const double g = P.str_gop[pi * maxr + ri], c = P.str_gcp[pi * maxr + ri];
+            const uint8_t gb = java_round_byte(g < 40.0 ? g : 40.0);
+            ins[o + i] = gb;
+            dels[o + i] = gb;
+            gcp[o + i] = java_round_byte(c);
+        }
+        if (lane == 0 && n > 0) {
+            ins[o + n - 1] = 45;
+            dels[o + n - 1] = 45;
+            gcp[o + n - 1] = 10;
+        }
+        __syncwarp();
     }
 }
 
 }  // namespace
 
+int launch_dragstr(const DevBatch &b, int64_t n_reads, const PrepArgs &p, int sm_count, cudaStream_t s) {
+    if (n_reads <= 0) return 0;
+    const int lpad = p.max_read_len > 32 ? (p.max_read_len + 31) / 32 * 32 : 32;
+    const size_t per_warp = (size_t)lpad * 8;  // bases, LF, C, best repeats (16-bit), best periods
+    int wpb = (int)(32768 / per_warp);
+    wpb = wpb < 1 ? 1 : wpb > 8 ? 8 : wpb;
+    const size_t smem = per_warp * wpb;
+    if (smem > 49152) {
+        cudaError_t e = cudaFuncSetAttribute(dragstr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e) return (int)e;
+    }
+    const int64_t want = (n_reads + wpb - 1) / wpb;
+    const int64_t cap = (int64_t)sm_count * (64 / wpb);
+    const int grid = (int)(want < cap ? want : cap);
+    dragstr_kernel<<<grid, 32 * wpb, smem, s>>>(b, const_cast<uint8_t *>(b.quals), const_cast<uint8_t *>(b.ins),
+                                              const_cast<uint8_t *>(b.dels), const_cast<uint8_t *>(b.gcp), n_reads, p,
+                                              lpad, (int)per_warp);
+    return (int)cudaGetLastError();
+}
+
 int launch_prep(const DevBatch &b, int64_t n_reads, const PrepArgs &p, int sm_count, cudaStream_t s) {
     if (n_reads <= 0) return 0;
-    const int block = 128;
-    const int64_t want = (n_reads + block - 1) / block;
-    const int grid = (int)(want < (int64_t)sm_count * 8 ? want : (int64_t)sm_count * 8);
+    const int64_t want = (n_reads + kPrepWarps - 1) / kPrepWarps;
+    const int64_t cap = (int64_t)sm_count * 8;
+    const int grid = (int)(want < cap ? want : cap);
     // the planes are the batch's own device buffers (DevBatch holds them as const for the forward kernels)
-    prep_kernel<<<grid, block, 0, s>>>(b, const_cast<uint8_t *>(b.quals), const_cast<uint8_t *>(b.ins),
-                                       const_cast<uint8_t *>(b.dels), n_reads, p);
+    prep_kernel<<<grid, kPrepWarps * 32, 0, s>>>(b, const_cast<uint8_t *>(b.quals), const_cast<uint8_t *>(b.ins),
+                                                 const_cast<uint8_t *>(b.dels), n_reads, p);
     return (int)cudaGetLastError();
 }
 

@@ -95,6 +95,8 @@ struct ghmm_batch {
     DevBuf<uint8_t> d_post;  // postprocess: reference haplotype per region, keep flags per read
     HostBuf<int32_t> h_mapq;  // raw-read batches: mapping quality per read
     DevBuf<int32_t> d_mapq;
+    HostBuf<double> h_dragstr;  // raw-read batches with the DRAGstr imputation: GOP then GCP table
+    DevBuf<double> d_dragstr;
     // PD-HMM batches: PD flags then state codes per haplotype column (pd.cu)
     HostBuf<uint8_t> h_pd;
     DevBuf<uint8_t> d_pd;
@@ -127,6 +129,8 @@ struct ghmm_batch {
     // asynchronous forward: events of the last enqueue, and the captured launch sequence
     cudaEvent_t ev[5]{};
     bool events_ready = false;
+    cudaEvent_t ev_prep[2]{};  // around the read preparation kernels of a raw batch's upload
+    bool prep_events = false, prep_timed = false;
     int64_t pending_n_pre = 0;
     int pending_mode = -1;
     cudaGraphExec_t graph[2]{};  // captured FP32 phase and FP64 phase
@@ -141,6 +145,9 @@ struct ghmm_batch {
         if (events_ready)
             for (auto &e : ev) cudaEventDestroy(e);
         events_ready = false;
+        if (prep_events)
+            for (auto &e : ev_prep) cudaEventDestroy(e);
+        prep_events = prep_timed = false;
         h_nout.release();
         d_nout.release();
         h_planes.release(); h_hap.release(); h_off.release(); h_read_region.release(); h_init_f.release();
@@ -148,7 +155,7 @@ struct ghmm_batch {
         d_planes.release(); d_hap.release(); d_off.release(); d_read_region.release(); d_init_f.release();
         d_init_d.release(); d_tasks.release(); d_rerun.release(); d_out.release(); d_counters.release();
         d_scratch32.release(); d_scratch64.release(); d_post.release(); h_pd.release(); d_pd.release();
-        h_mapq.release(); d_mapq.release();
+        h_mapq.release(); d_mapq.release(); h_dragstr.release(); d_dragstr.release();
         has_pd = false;
     }
 };
@@ -203,12 +210,21 @@ int cuda_fail(ghmm_ctx *ctx, cudaError_t e, const char *what) {
     } while (0)
 
 // Input view shared by the region-array and flat entry points.
+// Routing of reads whose gap penalties are only known after the device imputation (DRAGstr).  The checks that
+// guard against wrong finite results (a continuation penalty of 0, a matchToMatch probability of about 0) are
+// decided for the whole batch from every value the imputation tables can produce.  The growth checks only save
+// work: a pair whose rescaled FP32 or FP64 state overflows sums to a non-finite value and moves on to the next tier.
+struct RouteBound {
+    uint8_t force = 0;  // flags every read gets (bit0 FP64, bit2 exact FP64 tier)
+};
+
 struct Source {
     // either regions (per-read pointers) ...
     const ghmm_region *regions = nullptr;
     int64_t n_regions = 0;
     // ... or flat planes
     const ghmm_flat *flat = nullptr;
+    const RouteBound *bound = nullptr;  // set when the device rewrites the gap penalties after the upload
 };
 
 // Sizes + offsets (pass 1).  Returns error code.
@@ -354,6 +370,7 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                     break;
                 }
                 if (sg[i] == 0 || base_code(sb[i]) == 0) fl |= 1;
+                if (src.bound) continue;  // the gap planes are rewritten on the device
                 const double mm = HT.m2m[si[i] * 128 + sd[i]];
                 if (mm < 1e-6) fl |= 1 | 4;  // exact FP64 tier only (the rescaled forms divide by MM)
                 if (i > 0) {
@@ -364,6 +381,7 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                     if (growth > kMaxGrowth64) fl |= 1 | 4;  // the rescaled FP64 tier's headroom is 2^60
                 }
             }
+            if (src.bound) fl |= src.bound->force;
             read_flag[(size_t)r] = fl;
             b.h_read_region.p[r] = (int32_t)g;
         }
@@ -1447,7 +1465,40 @@ struct RawView {
     std::vector<std::vector<ghmm_read>> reads;
     std::vector<uint8_t> q45, qgcp;  // shared constant planes
     std::vector<int32_t> mapq;
+    int32_t max_len = 0;
+    bool has_bound = false;
+    RouteBound bound;
 };
+
+// Math.round(double) (half up), for table values already checked to lie in [-0.5, 127.5)
+int java_round(double x) {
+    double r = std::floor(x);
+    if (x - r >= 0.5) r += 1.0;
+    return (int)r;
+}
+
+// The penalties DRAGstr tables can impute (Math.round(min(40, gop)) and Math.round(gcp) over every cell, plus 45 / 10
+// at the last base) give the routing flags of the batch.
+int dragstr_bound(ghmm_ctx *ctx, const ghmm_dragstr &d, RouteBound &rb) {
+    const size_t cells = (size_t)d.max_period * (size_t)d.max_repeats;
+    int gmin = 45, gmax = 45, cmin = 10;
+    for (size_t k = 0; k < cells; k++) {
+        const double g = d.gop[k], c = d.gcp[k];
+        if (!(g >= -0.5) || !(c >= -0.5 && c < 127.5))
+            return fail(ctx, GHMM_ERR_ARG, "DRAGstr tables: gop >= 0 and gcp 0..127 expected");
+        const int gq = java_round(std::min(40.0, g)), cq = java_round(c);
+        gmin = std::min(gmin, gq);
+        gmax = std::max(gmax, gq);
+        cmin = std::min(cmin, cq);
+    }
+    const HostTables &HT = *ctx->host_tables;
+    double mm_min = 1.0;
+    for (int g = gmin; g <= gmax; g++) mm_min = std::min(mm_min, HT.m2m[g * 128 + g]);
+    rb.force = 0;
+    if (cmin == 0) rb.force |= 1;
+    if (mm_min < 1e-6) rb.force |= 1 | 4;
+    return GHMM_OK;
+}
 
 int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_read_prep *prep, RawView &v) {
     if (!prep) return fail(ctx, GHMM_ERR_ARG, "NULL read preparation arguments");
@@ -1455,6 +1506,15 @@ int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_re
     if (prep->base_quality_threshold < 6 || prep->base_quality_threshold > 127)
         return fail(ctx, GHMM_ERR_ARG, "base quality threshold must be 6..127 (QualityUtils.MIN_USABLE_Q_SCORE)");
     if (!(prep->pcr_rate_factor >= 0.0)) return fail(ctx, GHMM_ERR_ARG, "PCR rate factor must be >= 0");
+    if (prep->dragstr) {
+        const ghmm_dragstr &d = *prep->dragstr;
+        if (d.max_period < 1 || d.max_period > kDragstrMaxPeriod || d.max_repeats < 1 || d.max_repeats > (1 << 16) ||
+            !d.gop || !d.gcp)
+            return fail(ctx, GHMM_ERR_ARG, "DRAGstr tables: max_period 1..32, max_repeats >= 1, non-NULL gop and gcp");
+        const int rc = dragstr_bound(ctx, d, v.bound);
+        if (rc) return rc;
+        v.has_bound = true;
+    }
     int32_t max_len = 0;
     for (int64_t g = 0; g < G; g++) {
         const ghmm_raw_region &rg = raw[g];
@@ -1468,6 +1528,9 @@ int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_re
             max_len = std::max(max_len, rd.length);
         }
     }
+    if (prep->dragstr && max_len > kDragstrMaxRead)
+        return fail(ctx, GHMM_ERR_ARG, "the DRAGstr imputation takes reads of up to 28000 bases");
+    v.max_len = max_len;
     v.q45.assign((size_t)std::max(max_len, 1), 45);
     v.qgcp.assign((size_t)std::max(max_len, 1), (uint8_t)prep->gcp);
     v.regions.resize((size_t)G);
@@ -1511,8 +1574,32 @@ static int raw_prepare_device(ghmm_ctx *ctx, ghmm_batch &b, const RawView &v, co
         const int rounded = d > 0.0 ? (int)(d + 0.5) : (int)(d - 0.5);
         p.pcr_cache[rl] = (uint8_t)std::max(10, rounded);
     }
-    int e = launch_prep(b.dev, NR, p, ctx->sm_count, s);
-    if (e) return cuda_fail(ctx, (cudaError_t)e, "read preparation launch");
+    if (prep->dragstr) {
+        const ghmm_dragstr &d = *prep->dragstr;
+        const size_t cells = (size_t)d.max_period * (size_t)d.max_repeats;
+        GHMM_CUDA(b.h_dragstr.reserve(2 * cells), "pinned DRAGstr tables");
+        GHMM_CUDA(b.d_dragstr.reserve(2 * cells), "device DRAGstr tables");
+        memcpy(b.h_dragstr.p, d.gop, cells * sizeof(double));
+        memcpy(b.h_dragstr.p + cells, d.gcp, cells * sizeof(double));
+        GHMM_CUDA(cudaMemcpyAsync(b.d_dragstr.p, b.h_dragstr.p, 2 * cells * sizeof(double), cudaMemcpyHostToDevice, s),
+                  "H2D DRAGstr tables");
+        p.dragstr = 1;
+        p.str_gop = b.d_dragstr.p;
+        p.str_gcp = b.d_dragstr.p + cells;
+        p.str_max_period = d.max_period;
+        p.str_max_repeats = d.max_repeats;
+        p.max_read_len = v.max_len;
+        b.upload_bytes += (int64_t)(2 * cells * sizeof(double));
+    }
+    if (!b.prep_events) {
+        for (auto &ev : b.ev_prep) GHMM_CUDA(cudaEventCreate(&ev), "cudaEventCreate");
+        b.prep_events = true;
+    }
+    GHMM_CUDA(cudaEventRecord(b.ev_prep[0], s), "event");
+    const int e = p.dragstr ? launch_dragstr(b.dev, NR, p, ctx->sm_count, s) : launch_prep(b.dev, NR, p, ctx->sm_count, s);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, p.dragstr ? "DRAGstr imputation launch" : "read preparation launch");
+    GHMM_CUDA(cudaEventRecord(b.ev_prep[1], s), "event");
+    b.prep_timed = true;
     b.upload_bytes += NR * 4;
     return GHMM_OK;
 }
@@ -1788,6 +1875,13 @@ int ghmm_batch_stats(ghmm_ctx *ctx, const ghmm_batch *b, ghmm_stats *st) {
     st->d2h_bytes = b->forward_d2h + b->results_d2h;
     st->ms_host_marshal = b->ms_host_copy;
     st->ms_host_tasks = b->ms_host_tasks;
+    st->ms_prep = 0.0;
+    if (b->prep_timed) {
+        float ms = 0.0f;
+        GHMM_CUDA(cudaEventSynchronize(b->ev_prep[1]), "event");
+        GHMM_CUDA(cudaEventElapsedTime(&ms, b->ev_prep[0], b->ev_prep[1]), "event");
+        st->ms_prep = ms;
+    }
     return GHMM_OK;
 }
 
@@ -1935,6 +2029,7 @@ int ghmm_batch_create_raw(ghmm_ctx *ctx, const ghmm_raw_region *regions, int32_t
     Source src;
     src.regions = v.regions.data();
     src.n_regions = n_regions;
+    src.bound = v.has_bound ? &v.bound : nullptr;
     rc = batch_marshal(ctx, src, *b);
     if (!rc) rc = batch_upload(ctx, *b, ctx->stream);
     if (!rc) rc = raw_prepare_device(ctx, *b, v, prep, ctx->stream);
@@ -1975,6 +2070,7 @@ int ghmm_compute_regions_raw(ghmm_ctx *ctx, const ghmm_raw_region *regions, int3
     Source src;
     src.regions = v.regions.data();
     src.n_regions = n_regions;
+    src.bound = v.has_bound ? &v.bound : nullptr;
     ghmm_batch &b = ctx->scratch_batch;
     rc = batch_marshal(ctx, src, b);
     if (!rc) rc = batch_upload(ctx, b, ctx->stream);

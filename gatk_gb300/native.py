@@ -77,7 +77,7 @@ class Stats(ctypes.Structure):
                 ("reserved", ctypes.c_int32), ("ms_fp32", ctypes.c_double), ("ms_fp64", ctypes.c_double),
                 ("ms_plain", ctypes.c_double), ("ms_total", ctypes.c_double), ("h2d_bytes", ctypes.c_int64),
                 ("d2h_bytes", ctypes.c_int64), ("ms_host_marshal", ctypes.c_double),
-                ("ms_host_tasks", ctypes.c_double), ("n_fp64_exact", ctypes.c_int64)]
+                ("ms_host_tasks", ctypes.c_double), ("n_fp64_exact", ctypes.c_int64), ("ms_prep", ctypes.c_double)]
 
 
 class RawRead(ctypes.Structure):
@@ -90,9 +90,15 @@ class RawRegion(ctypes.Structure):
                 ("n_haps", ctypes.c_int32)]
 
 
+class Dragstr(ctypes.Structure):
+    _fields_ = [("max_period", ctypes.c_int32), ("max_repeats", ctypes.c_int32), ("gop", ctypes.c_void_p),
+                ("gcp", ctypes.c_void_p)]
+
+
 class ReadPrep(ctypes.Structure):
     _fields_ = [("base_quality_threshold", ctypes.c_int32), ("cap_to_mapq", ctypes.c_int32),
-                ("pcr_rate_factor", ctypes.c_double), ("gcp", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("pcr_rate_factor", ctypes.c_double), ("gcp", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("dragstr", ctypes.c_void_p)]
 
 
 class PdHap(ctypes.Structure):

@@ -50,6 +50,21 @@ def _u8(x) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(x, dtype=np.uint8))
 
 
+def _read_prep(threshold, cap_to_mapq, pcr_rate_factor, gcp, dragstr, keep_with) -> native.ReadPrep:
+    """ghmm_read_prep; dragstr = (gop, gcp) tables [max_period][max_repeats] (DragstrParams) or None.  The tables are
+    kept alive on keep_with (a Workload) for as long as the library may read them."""
+    d = None
+    if dragstr is not None:
+        gop_t = np.ascontiguousarray(dragstr[0], dtype=np.float64)
+        gcp_t = np.ascontiguousarray(dragstr[1], dtype=np.float64)
+        if gop_t.ndim != 2 or gop_t.shape != gcp_t.shape:
+            raise ValueError("DRAGstr gop and gcp tables must both be [max_period][max_repeats]")
+        d = native.Dragstr(gop_t.shape[0], gop_t.shape[1], gop_t.ctypes.data, gcp_t.ctypes.data)
+        keep_with._keep.append((gop_t, gcp_t, d))
+    return native.ReadPrep(int(threshold), int(cap_to_mapq), float(pcr_rate_factor), int(gcp), 0,
+                           ctypes.addressof(d) if d is not None else None)
+
+
 class _Context:
     def __init__(self, args: PairHMMNativeArguments):
         L = native.lib()
@@ -181,14 +196,16 @@ class Engine:
         return Batch(self, wl, via_regions)
 
     def compute_raw(self, wl: Workload, mapq, with_indel_quals: bool = True, base_quality_threshold: int = 18,
-                    cap_to_mapq: bool = True, pcr_rate_factor: float = 3.0, gcp: int = 10) -> np.ndarray:
+                    cap_to_mapq: bool = True, pcr_rate_factor: float = 3.0, gcp: int = 10,
+                    dragstr=None) -> np.ndarray:
         """Likelihoods from raw reads, prepared on the device (PairHMMLikelihoodCalculationEngine.modifyReadQualities
-        and the standard imputation); wl.quals are the raw base qualities, wl.ins / wl.dels the BI / BD tags."""
+        and the standard imputation, or with dragstr = (gop, gcp) tables of shape [max_period][max_repeats] the
+        DRAGstr imputation); wl.quals are the raw base qualities, wl.ins / wl.dels the BI / BD tags."""
         from .workload import as_raw_regions
 
         out = np.empty(max(wl.n_pairs, 1), dtype=np.float64)
         regs = as_raw_regions(wl, mapq, with_indel_quals)
-        p = native.ReadPrep(int(base_quality_threshold), int(cap_to_mapq), float(pcr_rate_factor), int(gcp), 0)
+        p = _read_prep(base_quality_threshold, cap_to_mapq, pcr_rate_factor, gcp, dragstr, wl)
         native.check(self.L.ghmm_compute_regions_raw(self._ctx.h, regs, wl.n_regions, ctypes.byref(p),
                                                      out.ctypes.data_as(native._f64p)), self._ctx.h)
         return out[:wl.n_pairs]
@@ -204,8 +221,8 @@ class Engine:
         return out[:wl.n_pairs]
 
     def raw_batch(self, wl: Workload, mapq, with_indel_quals: bool = True, base_quality_threshold: int = 18,
-                  cap_to_mapq: bool = True, pcr_rate_factor: float = 3.0, gcp: int = 10) -> "Batch":
-        p = native.ReadPrep(int(base_quality_threshold), int(cap_to_mapq), float(pcr_rate_factor), int(gcp), 0)
+                  cap_to_mapq: bool = True, pcr_rate_factor: float = 3.0, gcp: int = 10, dragstr=None) -> "Batch":
+        p = _read_prep(base_quality_threshold, cap_to_mapq, pcr_rate_factor, gcp, dragstr, wl)
         return Batch(self, wl, raw=(mapq, with_indel_quals, p))
 
     def pd_batch(self, wl: Workload, hap_pd: np.ndarray) -> "Batch":

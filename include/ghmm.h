@@ -132,6 +132,8 @@ typedef struct ghmm_stats {
     double ms_host_tasks;     /* host time of building and ordering the FP32 warp tasks */
     int64_t n_fp64_exact;     /* pairs of the last forward computed by the exact (unscaled, 2^1020) FP64 tier:
                                  results of the rescaled FP64 tier below log10 L = -500, and host-marked reads */
+    double ms_prep;           /* raw batches: device time of the read preparation kernels of the upload (quality
+                                 caps, PCR model or DRAGstr imputation); 0 for prepared batches */
 } ghmm_stats;
 
 /* Launch-shape choices of the FP32 pass (the autotuner's knobs; the reference has none besides its thread
@@ -236,12 +238,29 @@ typedef struct ghmm_raw_region {
     int32_t n_haps;
 } ghmm_raw_region;
 
+/* DRAGEN-GATK's STR-aware imputation (DragstrPairHMMInputScoreImputator.impute, HC/DragstrPairHMMInputScoreImputator
+ * .java:54-88): at every read position but the last, the most repeated short tandem repeat period around it and its
+ * repeat count (DragstrReadSTRAnalyzer, PH/DragstrReadSTRAnalyzer.java, periods 1..max_period, ties to the shorter
+ * period) index the model's tables (DragstrParams.gop / gcp, utils/dragstr/DragstrParams.java:194-220: periods and
+ * repeats beyond the table use its last row / column); the insertion and deletion open penalties are
+ * Math.round(min(40, gop)) and the continuation penalty Math.round(gcp), as Java bytes; the last position gets 45 and
+ * 10. */
+typedef struct ghmm_dragstr {
+    int32_t max_period;  /* DragstrParams.maximumPeriod(), 1..32 */
+    int32_t max_repeats; /* DragstrParams.maximumRepeats(), >= 1 */
+    const double *gop;   /* [max_period][max_repeats]: gop(period, repeats) at [period - 1][repeats - 1] */
+    const double *gcp;   /* same layout */
+} ghmm_dragstr;
+
 typedef struct ghmm_read_prep {
     int32_t base_quality_threshold; /* --base-quality-score-threshold (PairHMM.BASE_QUALITY_SCORE_THRESHOLD = 18) */
     int32_t cap_to_mapq;            /* !disableCapReadQualitiesToMapQ */
     double pcr_rate_factor;         /* PCRErrorModel: 0 NONE, 1 HOSTILE, 2 AGGRESSIVE, 3 CONSERVATIVE (GATK default) */
     int32_t gcp;                    /* constant gap continuation penalty (--gcp-hmm, default 10), 1..127 */
     int32_t reserved;
+    const ghmm_dragstr *dragstr;    /* NULL: the standard imputation above; else the DRAGstr imputation, which
+                                     * replaces the insertion / deletion / continuation penalties (the PCR model and
+                                     * the floor of 6 then do not apply to them) */
 } ghmm_read_prep;
 
 /* As ghmm_compute_regions, from raw reads; the preparation runs on the device before the forward. */

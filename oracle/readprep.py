@@ -12,6 +12,13 @@ ghmm_compute_regions_raw).  Pure Python loops, for small cases.  Follows (paths 
   MathUtils.fastRound                               utils/MathUtils.java:428-430
   ReadUtils.getBaseInsertionQualities / getBaseDeletionQualities (default 45)   utils/read/ReadUtils.java:44,838-862
   StandardPairHMMInputScoreImputator (constant gap continuation penalty)
+  DragstrPairHMMInputScoreImputator.impute (MAX_GOP_IN_READ 40, 45 / 10 at the last base)
+      tools/walkers/haplotypecaller/DragstrPairHMMInputScoreImputator.java:22-31,54-88
+  DragstrReadSTRAnalyzer (repeat count per period and position, most repeated period with ties to the shorter one)
+      utils/pairhmm/DragstrReadSTRAnalyzer.java:110-139; the position-by-position definition its test checks against,
+      DragstrReadSTRAnalyzerTest.calculateExpectedRepeatLength (src/test/.../DragstrReadSTRAnalyzerTest.java:131-168)
+  DragstrParams.lookup (periods / repeats past the table use its last row / column)
+      utils/dragstr/DragstrParams.java:194-220
 """
 from __future__ import annotations
 
@@ -79,12 +86,88 @@ def tandem_repeat_length(b: bytes, offset: int) -> int:
     return min(max_rl, MAX_REPEAT_LENGTH)
 
 
+def str_repeats(seq: bytes, pos: int, period: int) -> int:
+    """Repeat count of `period` at `pos`: the longest tandem run (in units) of a period-mer that contains pos or
+    starts right after it; a unit starting at 0 counts one fewer (not below 1) for positions before period - 1."""
+    n = len(seq)
+    if period > n:
+        return 0
+    best = 0
+    start = max(0, pos - period + 1)
+    while start <= pos + 1 and start + period <= n:
+        unit = seq[start:start + period]
+        count = 1
+        off = start + period
+        while off + period <= n and seq[off:off + period] == unit:
+            count += 1
+            off += period
+        off = start - period
+        while off >= 0 and seq[off:off + period] == unit:
+            count += 1
+            off -= period
+        if pos < period - 1 and start == 0:
+            count = max(1, count - 1)
+        best = max(best, count)
+        start += 1
+    return best
+
+
+def str_analyze(seq: bytes, max_period: int):
+    """(most repeated period, its repeat count) per position; ties go to the shorter period."""
+    periods, repeats = [], []
+    for pos in range(len(seq)):
+        bp, br = 1, str_repeats(seq, pos, 1)
+        for p in range(2, max_period + 1):
+            r = str_repeats(seq, pos, p)
+            if r > br:
+                bp, br = p, r
+        periods.append(bp)
+        repeats.append(br)
+    return periods, repeats
+
+
+def java_round(x: float) -> int:
+    """Math.round(double): half up."""
+    r = math.floor(x)
+    return int(r + 1 if x - r >= 0.5 else r)
+
+
+def dragstr_impute(bases, gop_table, gcp_table):
+    """DragstrPairHMMInputScoreImputator.impute: (GOP plane, GCP plane) of one read, tables [max_period][max_repeats]
+    (DragstrParams.gop / gcp at [period - 1][repeats - 1])."""
+    b = bytes(bases)
+    n = len(b)
+    max_period, max_repeats = len(gop_table), len(gop_table[0])
+    gop, gcp = bytearray(n), bytearray(n)
+    if n == 0:
+        return bytes(gop), bytes(gcp)
+    periods, repeats = str_analyze(b, max_period)
+    for i in range(n - 1):
+        p, r = periods[i], repeats[i]
+        pi = p - 1 if p < max_period else max_period - 1
+        ri = r - 1 if r < max_repeats else max_repeats - 1
+        gop[i] = java_round(min(40.0, float(gop_table[pi][ri]))) & 0xFF
+        gcp[i] = java_round(float(gcp_table[pi][ri])) & 0xFF
+    gop[n - 1], gcp[n - 1] = 45, 10
+    return bytes(gop), bytes(gcp)
+
+
 def prepare_read(bases, quals, ins, dels, mapq: int, threshold: int = 18, cap_to_mapq: bool = True,
-                 rate_factor: float = 0.0, gcp: int = 10):
-    """The five PairHMM inputs of one read: (bases, quals, insertion GOP, deletion GOP, GCP)."""
+                 rate_factor: float = 0.0, gcp: int = 10, dragstr=None):
+    """The five PairHMM inputs of one read: (bases, quals, insertion GOP, deletion GOP, GCP).  With dragstr = (gop,
+    gcp) tables the DRAGstr imputation gives the three gap planes (PairHMM.computeLog10Likelihoods takes them from
+    the imputator, not from the read's capped BI / BD values)."""
     b = bytes(bases)
     n = len(b)
     q = [int(x) for x in quals]
+    if dragstr is not None:
+        signed = lambda v: v - 256 if v > 127 else v
+        for i in range(n):
+            if cap_to_mapq:
+                q[i] = min(q[i], mapq) & 0xFF
+            q[i] = MIN_USABLE_Q_SCORE if signed(q[i]) < threshold else q[i]
+        g, c = dragstr_impute(b, dragstr[0], dragstr[1])
+        return b, bytes(q), g, g, c
     i_q = [DEFAULT_INDEL_QUAL] * n if ins is None else [int(x) for x in ins]
     d_q = [DEFAULT_INDEL_QUAL] * n if dels is None else [int(x) for x in dels]
     if rate_factor != 0.0:  # applyPCRErrorModel
