@@ -117,7 +117,7 @@ struct PrepArgs {
 };
 int launch_prep(const DevBatch &b, int64_t n_reads, const PrepArgs &p, int sm_count, cudaStream_t s);
 int launch_dragstr(const DevBatch &b, int64_t n_reads, const PrepArgs &p, int sm_count, cudaStream_t s);
-constexpr int kDragstrMaxRead = 28000;  // reads the DRAGstr kernel's shared memory holds (8 bytes per base)
+constexpr int kDragstrMaxRead = 28000;  // reads the DRAGstr kernel's shared memory holds (6.4 bytes per base)
 constexpr int kDragstrMaxPeriod = 32;
 
 // Post-likelihood normalisation and filtering (post.cu).

@@ -139,77 +139,123 @@ __device__ __forceinline__ uint8_t java_round_byte(double x) {
 // starting at 0 counts one repeat fewer, not below 1, for positions before p - 1); the most repeated period wins,
 // ties to the shorter one.  The run through the unit at x is 1 + F + Bk copies, where F copies follow it and Bk
 // precede it.  With D[j] = (base j == base j + p), the units at x and x + p are equal exactly when D is 1 over
-// [x, x + p), so F = floor(LF(x) / p) for LF(x) the run of ones of D starting at x, and Bk = floor(LB(x) / p) for
-// LB(x) the run of ones ending at x - 1.  Both runs come from ballots of D's zeros, 32 positions at a time with the
-// nearest zero carried between chunks (backward for LF, forward for LB); then every position takes the maximum
-// over its window of p + 1 unit starts.
-__device__ __forceinline__ int div_small(int v, int p, uint32_t magic) {  // v / p for 0 <= v < 2^17, p <= 32
+// [x, x + p), so F = floor(LF / p) for LF the run of ones of D starting at x, and Bk = floor(LB / p) for LB the run
+// of ones ending at x - 1: both follow from the nearest zeros of D on either side of x.  Per period: the zero masks
+// of D, 32 positions per ballot; the nearest zero before and after every 32-position chunk, 32 chunks per ballot;
+// the counts of every unit start; the maximum over every position's window of p + 1 unit starts.
+struct StrWarp {  // one warp's shared memory for a read of up to lpad - 1 bases
+    uint8_t *S;              // bases
+    uint32_t *ZM, *PZ, *NZ;  // per chunk: zero mask of D, nearest zero before it, nearest zero at or after its end
+    int16_t *C;              // run count of the unit starting at x (0 past the last unit start, as window padding)
+    int16_t *BR;             // most repeats so far
+    uint8_t *BP;             // their period
+};
+
+// v / p for 0 <= v < 2^17 and 2 <= p <= 32, with magic = ceil(2^32 / p); p = 1 passes v through
+__device__ __forceinline__ int div_period(int v, int p, uint32_t magic) {
     return p == 1 ? v : (int)__umulhi((uint32_t)v, magic);
+}
+
+// one period of the analysis, called from one place with the period at run time: a single copy of the code keeps
+// the kernel small enough for the instruction cache
+__device__ __forceinline__ void str_period(const StrWarp &W, int p, int n, int lane) {
+    const uint32_t magic = (uint32_t)((0x100000000ull + (uint64_t)p - 1) / (uint64_t)p);
+    const int nu = n - p + 1;  // unit starts 0 .. n - p
+    const int nch = (n + 31) >> 5;
+    for (int c = 0; c < nch; ++c) {
+        const int x = (c << 5) + lane;
+        const bool d = x + p < n && W.S[x] == W.S[x + p];
+        const uint32_t z = __ballot_sync(0xffffffffu, !d);
+        if (lane == 0) W.ZM[c] = z;
+    }
+    __syncwarp();
+    // nearest zeros outside each chunk, lane j of a group handling chunk 32 g + j
+    int carry = -1;
+    for (int g = 0; g < nch; g += 32) {
+        const int c = g + lane;
+        const uint32_t zm = c < nch ? W.ZM[c] : 0u;
+        const uint32_t has = __ballot_sync(0xffffffffu, zm != 0u);
+        const uint32_t below = has & ((1u << lane) - 1u);
+        const int kb = below ? 31 - __clz(below) : 0;
+        const uint32_t zb = __shfl_sync(0xffffffffu, zm, kb);
+        if (c < nch) W.PZ[c] = below ? ((g + kb) << 5) + 31 - __clz(zb) : carry;
+        if (has) {
+            const int kl = 31 - __clz(has);
+            carry = ((g + kl) << 5) + 31 - __clz(__shfl_sync(0xffffffffu, zm, kl));
+        }
+    }
+    carry = n;
+    for (int g = (nch - 1) & ~31; g >= 0; g -= 32) {
+        const int c = g + lane;
+        const uint32_t zm = c < nch ? W.ZM[c] : 0u;
+        const uint32_t has = __ballot_sync(0xffffffffu, zm != 0u);
+        const uint32_t above = lane < 31 ? has >> (lane + 1) : 0u;
+        const int ka = above ? lane + __ffs(above) : 0;
+        const uint32_t za = __shfl_sync(0xffffffffu, zm, ka);
+        if (c < nch) W.NZ[c] = above ? ((g + ka) << 5) + __ffs(za) - 1 : carry;
+        if (has) {
+            const int kf = __ffs(has) - 1;
+            carry = ((g + kf) << 5) + __ffs(__shfl_sync(0xffffffffu, zm, kf)) - 1;
+        }
+    }
+    __syncwarp();
+    for (int c = 0; c < nch; ++c) {
+        const int x = (c << 5) + lane;
+        const uint32_t z = W.ZM[c];
+        const uint32_t ahead = z >> lane, behind = z & ((1u << lane) - 1u);
+        const int nz = ahead ? x + __ffs(ahead) - 1 : (int)W.NZ[c];
+        const int pz = behind ? (c << 5) + 31 - __clz(behind) : (int)W.PZ[c];
+        if (x < nu) W.C[x] = (int16_t)(1 + div_period(nz - x, p, magic) + div_period(x - 1 - pz, p, magic));
+        else if (x <= n) W.C[x] = 0;
+    }
+    if (lane == 0 && (n & 31) == 0) W.C[n] = 0;
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) {
+        int best = 0;
+        if (i >= p - 1) {
+            const int16_t *w = W.C + (i - p + 1);
+            for (int k = 0; k <= p; ++k) best = max(best, (int)w[k]);
+        } else {  // the window starts at the read's first base, whose unit counts one repeat fewer here
+            best = max(W.C[0] - 1, 1);
+            for (int x = 1; x <= i + 1; ++x) best = max(best, (int)W.C[x]);
+        }
+        if (p == 1 || best > W.BR[i]) {
+            W.BR[i] = (int16_t)best;
+            W.BP[i] = (uint8_t)p;
+        }
+    }
+    __syncwarp();
 }
 
 __global__ void dragstr_kernel(DevBatch B, uint8_t *quals, uint8_t *ins, uint8_t *dels, uint8_t *gcp, int64_t n_reads,
                                PrepArgs P, int lpad, int wstride) {
-    extern __shared__ unsigned char smem[];
+    extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-    uint8_t *S = smem + (size_t)w * wstride;  // bases, then LF, the run counts, best repeats and best periods
-    int16_t *LF = reinterpret_cast<int16_t *>(S + lpad);
-    int16_t *C = LF + lpad;
-    int16_t *BR = C + lpad;
-    uint8_t *BP = reinterpret_cast<uint8_t *>(BR + lpad);
+    unsigned char *base = smem + (size_t)w * wstride;
+    const int nchunk = lpad >> 5;
+    StrWarp W;
+    W.S = base;
+    W.ZM = reinterpret_cast<uint32_t *>(base + lpad);
+    W.PZ = W.ZM + nchunk;
+    W.NZ = W.PZ + nchunk;
+    W.C = reinterpret_cast<int16_t *>(W.NZ + nchunk);
+    W.BR = W.C + lpad;
+    W.BP = reinterpret_cast<uint8_t *>(W.BR + lpad);
     const int maxp = P.str_max_period, maxr = P.str_max_repeats;
     for (int64_t r = (int64_t)blockIdx.x * wpb + w; r < n_reads; r += (int64_t)gridDim.x * wpb) {
         const int64_t o = B.read_off[r];
         const int n = (int)(B.read_off[r + 1] - o);
         const int mapq = P.mapq[r];
-        const int nch = (n + 31) >> 5;
         for (int x = lane; x < n; x += 32) {
-            S[x] = B.bases[o + x];
+            W.S[x] = B.bases[o + x];
             quals[o + x] = cap_base_quality(quals[o + x], mapq, P);
         }
         __syncwarp();
-        for (int p = 1; p <= maxp && p <= n; ++p) {
-            const uint32_t magic = (uint32_t)((0x100000000ull + (uint64_t)p - 1) / (uint64_t)p);
-            const int nu = n - p + 1;  // unit starts 0 .. n - p
-            int carry = n;             // nearest zero of D at or after the chunk's end (D is 0 from n - p on)
-            for (int c = nch - 1; c >= 0; --c) {
-                const int x = (c << 5) + lane;
-                const bool d = x + p < n && S[x] == S[x + p];
-                const uint32_t zeros = __ballot_sync(0xffffffffu, !d);
-                const uint32_t ahead = zeros >> lane;
-                const int nz = ahead ? x + __ffs(ahead) - 1 : carry;
-                if (x < nu) LF[x] = (int16_t)(nz - x);
-                if (zeros) carry = (c << 5) + __ffs(zeros) - 1;
-            }
-            __syncwarp();
-            int before = -1;  // nearest zero of D before the chunk
-            for (int c = 0; c < nch; ++c) {
-                const int x = (c << 5) + lane;
-                const bool d = x + p < n && S[x] == S[x + p];
-                const uint32_t zeros = __ballot_sync(0xffffffffu, !d);
-                const uint32_t behind = zeros & ((1u << lane) - 1u);
-                const int pz = behind ? (c << 5) + 31 - __clz(behind) : before;
-                if (x < nu) C[x] = (int16_t)(1 + div_small(LF[x], p, magic) + div_small(x - 1 - pz, p, magic));
-                if (zeros) before = (c << 5) + 31 - __clz(zeros);
-            }
-            __syncwarp();
-            for (int i = lane; i < n; i += 32) {
-                const int lo = i - p + 1 > 0 ? i - p + 1 : 0, hi = i + 1 < nu - 1 ? i + 1 : nu - 1;
-                int best = 0;
-                for (int x = lo; x <= hi; ++x) {
-                    int c = C[x];
-                    if (x == 0 && i < p - 1) c = c - 1 > 1 ? c - 1 : 1;
-                    best = c > best ? c : best;
-                }
-                if (p == 1 || best > BR[i]) {
-                    BR[i] = (int16_t)best;
-                    BP[i] = (uint8_t)p;
-                }
-            }
-            __syncwarp();
-        }
+        const int top = maxp < n ? maxp : n;
+        for (int p = 1; p <= top; ++p) str_period(W, p, n, lane);
         // DragstrPairHMMInputScoreImputator.impute with DragstrParams.lookup's clamping of period and repeats
         for (int i = lane; i < n - 1; i += 32) {
-            const int per = BP[i], rep = BR[i];
+            const int per = W.BP[i], rep = W.BR[i];
             const int pi = per < maxp ? per - 1 : maxp - 1, ri = rep < maxr ? rep - 1 : maxr - 1;
             const double g = P.str_gop[pi * maxr + ri], c = P.str_gcp[pi * maxr + ri];
             const uint8_t gb = java_round_byte(g < 40.0 ? g : 40.0);
@@ -230,8 +276,9 @@ __global__ void dragstr_kernel(DevBatch B, uint8_t *quals, uint8_t *ins, uint8_t
 
 int launch_dragstr(const DevBatch &b, int64_t n_reads, const PrepArgs &p, int sm_count, cudaStream_t s) {
     if (n_reads <= 0) return 0;
-    const int lpad = p.max_read_len > 32 ? (p.max_read_len + 31) / 32 * 32 : 32;
-    const size_t per_warp = (size_t)lpad * 8;  // bases, LF, C, best repeats (16-bit), best periods
+    const int lpad = (p.max_read_len + 1 + 31) / 32 * 32;  // one spare base: the count array is read up to n
+    // bases, C and best repeats (16-bit), best periods, and three 32-bit words per 32 bases
+    const size_t per_warp = ((size_t)lpad * 6 + (size_t)(lpad / 32) * 12 + 15) / 16 * 16;
     int wpb = (int)(32768 / per_warp);
     wpb = wpb < 1 ? 1 : wpb > 8 ? 8 : wpb;
     const size_t smem = per_warp * wpb;

@@ -1462,7 +1462,7 @@ namespace {
 
 struct RawView {
     std::vector<ghmm_region> regions;
-    std::vector<std::vector<ghmm_read>> reads;
+    std::vector<ghmm_read> reads;  // every region's reads, region after region
     std::vector<uint8_t> q45, qgcp;  // shared constant planes
     std::vector<int32_t> mapq;
     int32_t max_len = 0;
@@ -1515,18 +1515,34 @@ int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_re
         if (rc) return rc;
         v.has_bound = true;
     }
-    int32_t max_len = 0;
-    for (int64_t g = 0; g < G; g++) {
+    // checks and per-region read counts in parallel; the first bad region (in order) names the error
+    const int threads = hw_threads(ctx->max_threads);
+    std::vector<int8_t> bad((size_t)G, 0);
+    std::vector<int32_t> region_max((size_t)G, 0);
+    parallel_for(G, threads, [&](int64_t g) {
         const ghmm_raw_region &rg = raw[g];
-        if (rg.n_reads < 0 || rg.n_haps < 0 || (rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps))
-            return fail(ctx, GHMM_ERR_ARG, "bad raw region");
+        if (rg.n_reads < 0 || rg.n_haps < 0 || (rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps)) {
+            bad[(size_t)g] = 1;
+            return;
+        }
+        int32_t mx = 0;
         for (int32_t r = 0; r < rg.n_reads; r++) {
             const ghmm_raw_read &rd = rg.reads[r];
-            if (rd.length < 0 || rd.length > kMaxReadLen) return fail(ctx, GHMM_ERR_ARG, "read length out of range");
-            if (rd.length > 0 && (!rd.bases || !rd.quals)) return fail(ctx, GHMM_ERR_ARG, "NULL read array");
-            if (rd.mapping_quality < 0 || rd.mapping_quality > 255) return fail(ctx, GHMM_ERR_ARG, "mapping quality 0..255");
-            max_len = std::max(max_len, rd.length);
+            if (rd.length < 0 || rd.length > kMaxReadLen) { bad[(size_t)g] = 2; return; }
+            if (rd.length > 0 && (!rd.bases || !rd.quals)) { bad[(size_t)g] = 3; return; }
+            if (rd.mapping_quality < 0 || rd.mapping_quality > 255) { bad[(size_t)g] = 4; return; }
+            mx = std::max(mx, rd.length);
         }
+        region_max[(size_t)g] = mx;
+    }, 16);
+    static const char *const kRawErrors[] = {"", "bad raw region", "read length out of range", "NULL read array",
+                                             "mapping quality 0..255"};
+    int32_t max_len = 0;
+    std::vector<int64_t> first((size_t)G + 1, 0);
+    for (int64_t g = 0; g < G; g++) {
+        if (bad[(size_t)g]) return fail(ctx, GHMM_ERR_ARG, kRawErrors[bad[(size_t)g]]);
+        max_len = std::max(max_len, region_max[(size_t)g]);
+        first[(size_t)g + 1] = first[(size_t)g] + raw[g].n_reads;
     }
     if (prep->dragstr && max_len > kDragstrMaxRead)
         return fail(ctx, GHMM_ERR_ARG, "the DRAGstr imputation takes reads of up to 28000 bases");
@@ -1534,19 +1550,20 @@ int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_re
     v.q45.assign((size_t)std::max(max_len, 1), 45);
     v.qgcp.assign((size_t)std::max(max_len, 1), (uint8_t)prep->gcp);
     v.regions.resize((size_t)G);
-    v.reads.resize((size_t)G);
-    for (int64_t g = 0; g < G; g++) {
+    v.reads.resize((size_t)first[(size_t)G]);
+    v.mapq.resize((size_t)first[(size_t)G]);
+    parallel_for(G, threads, [&](int64_t g) {
         const ghmm_raw_region &rg = raw[g];
-        auto &rr = v.reads[(size_t)g];
-        rr.resize((size_t)rg.n_reads);
+        ghmm_read *rr = v.reads.data() + first[(size_t)g];
+        int32_t *mq = v.mapq.data() + first[(size_t)g];
         for (int32_t r = 0; r < rg.n_reads; r++) {
             const ghmm_raw_read &rd = rg.reads[r];
-            rr[(size_t)r] = ghmm_read{rd.bases, rd.quals, rd.ins_quals ? rd.ins_quals : v.q45.data(),
-                                      rd.del_quals ? rd.del_quals : v.q45.data(), v.qgcp.data(), rd.length};
-            v.mapq.push_back(rd.mapping_quality);
+            rr[r] = ghmm_read{rd.bases, rd.quals, rd.ins_quals ? rd.ins_quals : v.q45.data(),
+                              rd.del_quals ? rd.del_quals : v.q45.data(), v.qgcp.data(), rd.length};
+            mq[r] = rd.mapping_quality;
         }
-        v.regions[(size_t)g] = ghmm_region{rr.data(), rg.n_reads, rg.haps, rg.n_haps};
-    }
+        v.regions[(size_t)g] = ghmm_region{rr, rg.n_reads, rg.haps, rg.n_haps};
+    }, 16);
     return GHMM_OK;
 }
 

@@ -115,51 +115,46 @@ class Workload:
 
     def as_regions(self):
         """ghmm_region array with per-read pointers into the planes (the JNI-shaped input)."""
-        NR, NH, G = self.n_reads, self.n_haps, self.n_regions
+        NR = self.n_reads
         assert ctypes.sizeof(native.Read) == 48 and ctypes.sizeof(native.Hap) == 16
         assert ctypes.sizeof(native.Region) == 32
-        rd = np.zeros(max(NR, 1), dtype=[("p", "<u8", (5,)), ("len", "<i4"), ("pad", "<i4")])
+        rd = np.zeros((max(NR, 1), 6), dtype=np.uint64)  # five plane pointers, then length and padding
         o = self.read_off[:-1].astype(np.uint64)
         for k, plane in enumerate((self.bases, self.quals, self.ins, self.dels, self.gcp)):
-            rd["p"][:NR, k] = np.uint64(plane.ctypes.data) + o
-        rd["len"][:NR] = np.diff(self.read_off)
-        hp = np.zeros(max(NH, 1), dtype=[("p", "<u8"), ("len", "<i4"), ("pad", "<i4")])
-        hp["p"][:NH] = np.uint64(self.hap_bases.ctypes.data) + self.hap_off[:-1].astype(np.uint64)
-        hp["len"][:NH] = np.diff(self.hap_off)
-        rg = np.zeros(max(G, 1), dtype=[("reads", "<u8"), ("n_reads", "<i4"), ("pad0", "<i4"), ("haps", "<u8"),
-                                        ("n_haps", "<i4"), ("pad1", "<i4")])
-        rg["reads"][:G] = np.uint64(rd.ctypes.data) + self.region_read_off[:-1].astype(np.uint64) * np.uint64(48)
-        rg["n_reads"][:G] = np.diff(self.region_read_off)
-        rg["haps"][:G] = np.uint64(hp.ctypes.data) + self.region_hap_off[:-1].astype(np.uint64) * np.uint64(16)
-        rg["n_haps"][:G] = np.diff(self.region_hap_off)
-        self._keep.append((rd, hp, rg))
-        return rg.ctypes.data_as(ctypes.POINTER(native.Region))
+            np.add(o, np.uint64(plane.ctypes.data), out=rd[:NR, k])
+        rd.view(np.int32)[:NR, 10] = np.diff(self.read_off)
+        return _region_table(self, rd, 48)
+
+
+def _region_table(wl: Workload, rd: np.ndarray, read_size: int):
+    """ghmm_region-shaped array (reads pointer, count, haplotypes pointer, count) over the per-read table rd."""
+    NH, G = wl.n_haps, wl.n_regions
+    hp = np.zeros((max(NH, 1), 2), dtype=np.uint64)
+    np.add(wl.hap_off[:-1].astype(np.uint64), np.uint64(wl.hap_bases.ctypes.data), out=hp[:NH, 0])
+    hp.view(np.int32)[:NH, 2] = np.diff(wl.hap_off)
+    rg = np.zeros((max(G, 1), 4), dtype=np.uint64)
+    rg[:G, 0] = np.uint64(rd.ctypes.data) + wl.region_read_off[:-1].astype(np.uint64) * np.uint64(read_size)
+    rg.view(np.int32)[:G, 2] = np.diff(wl.region_read_off)
+    rg[:G, 2] = np.uint64(hp.ctypes.data) + wl.region_hap_off[:-1].astype(np.uint64) * np.uint64(16)
+    rg.view(np.int32)[:G, 6] = np.diff(wl.region_hap_off)
+    wl._keep.append((rd, hp, rg))
+    return rg.ctypes.data_as(ctypes.POINTER(native.Region))
 
 
 def as_raw_regions(wl: Workload, mapq: np.ndarray, with_indel_quals: bool = True):
     """ghmm_raw_region array: the workload's bases and base qualities as raw reads with a mapping quality each;
     the insertion / deletion planes as BI / BD tags, or none (the library's 45) when with_indel_quals is False."""
-    NR, NH, G = wl.n_reads, wl.n_haps, wl.n_regions
+    NR = wl.n_reads
+    assert ctypes.sizeof(native.RawRead) == 40 and ctypes.sizeof(native.RawRegion) == 32
+    rd = np.zeros((max(NR, 1), 5), dtype=np.uint64)  # four pointers, then length and mapping quality
     o = wl.read_off[:-1].astype(np.uint64)
-    rd = np.zeros(max(NR, 1), dtype=[("p", "<u8", (4,)), ("len", "<i4"), ("mapq", "<i4")])
-    rd["p"][:NR, 0] = np.uint64(wl.bases.ctypes.data) + o
-    rd["p"][:NR, 1] = np.uint64(wl.quals.ctypes.data) + o
-    if with_indel_quals:
-        rd["p"][:NR, 2] = np.uint64(wl.ins.ctypes.data) + o
-        rd["p"][:NR, 3] = np.uint64(wl.dels.ctypes.data) + o
-    rd["len"][:NR] = np.diff(wl.read_off)
-    rd["mapq"][:NR] = np.asarray(mapq, dtype=np.int32)
-    hp = np.zeros(max(NH, 1), dtype=[("p", "<u8"), ("len", "<i4"), ("pad", "<i4")])
-    hp["p"][:NH] = np.uint64(wl.hap_bases.ctypes.data) + wl.hap_off[:-1].astype(np.uint64)
-    hp["len"][:NH] = np.diff(wl.hap_off)
-    rg = np.zeros(max(G, 1), dtype=[("reads", "<u8"), ("n_reads", "<i4"), ("pad0", "<i4"), ("haps", "<u8"),
-                                    ("n_haps", "<i4"), ("pad1", "<i4")])
-    rg["reads"][:G] = np.uint64(rd.ctypes.data) + wl.region_read_off[:-1].astype(np.uint64) * np.uint64(40)
-    rg["n_reads"][:G] = np.diff(wl.region_read_off)
-    rg["haps"][:G] = np.uint64(hp.ctypes.data) + wl.region_hap_off[:-1].astype(np.uint64) * np.uint64(16)
-    rg["n_haps"][:G] = np.diff(wl.region_hap_off)
-    wl._keep.append((rd, hp, rg))
-    return rg.ctypes.data
+    planes = (wl.bases, wl.quals, wl.ins, wl.dels) if with_indel_quals else (wl.bases, wl.quals)
+    for k, plane in enumerate(planes):
+        np.add(o, np.uint64(plane.ctypes.data), out=rd[:NR, k])
+    i32 = rd.view(np.int32)
+    i32[:NR, 8] = np.diff(wl.read_off)
+    i32[:NR, 9] = np.asarray(mapq, dtype=np.int32)
+    return ctypes.cast(_region_table(wl, rd, 40), ctypes.c_void_p).value
 
 
 def as_pd_regions(wl: Workload, hap_pd: np.ndarray):
@@ -168,16 +163,16 @@ def as_pd_regions(wl: Workload, hap_pd: np.ndarray):
     wl.as_regions()  # builds the per-read structs (kept alive in wl._keep)
     rd = wl._keep[-1][0]
     pd = np.ascontiguousarray(hap_pd, dtype=np.uint8)
-    hp = np.zeros(max(NH, 1), dtype=[("p", "<u8"), ("f", "<u8"), ("len", "<i4"), ("pad", "<i4")])
-    hp["p"][:NH] = np.uint64(wl.hap_bases.ctypes.data) + wl.hap_off[:-1].astype(np.uint64)
-    hp["f"][:NH] = np.uint64(pd.ctypes.data) + wl.hap_off[:-1].astype(np.uint64)
-    hp["len"][:NH] = np.diff(wl.hap_off)
-    rg = np.zeros(max(G, 1), dtype=[("reads", "<u8"), ("n_reads", "<i4"), ("pad0", "<i4"), ("haps", "<u8"),
-                                    ("n_haps", "<i4"), ("pad1", "<i4")])
-    rg["reads"][:G] = np.uint64(rd.ctypes.data) + wl.region_read_off[:-1].astype(np.uint64) * np.uint64(48)
-    rg["n_reads"][:G] = np.diff(wl.region_read_off)
-    rg["haps"][:G] = np.uint64(hp.ctypes.data) + wl.region_hap_off[:-1].astype(np.uint64) * np.uint64(24)
-    rg["n_haps"][:G] = np.diff(wl.region_hap_off)
+    hp = np.zeros((max(NH, 1), 3), dtype=np.uint64)  # bases pointer, PD flags pointer, length and padding
+    ho = wl.hap_off[:-1].astype(np.uint64)
+    np.add(ho, np.uint64(wl.hap_bases.ctypes.data), out=hp[:NH, 0])
+    np.add(ho, np.uint64(pd.ctypes.data), out=hp[:NH, 1])
+    hp.view(np.int32)[:NH, 4] = np.diff(wl.hap_off)
+    rg = np.zeros((max(G, 1), 4), dtype=np.uint64)
+    rg[:G, 0] = np.uint64(rd.ctypes.data) + wl.region_read_off[:-1].astype(np.uint64) * np.uint64(48)
+    rg.view(np.int32)[:G, 2] = np.diff(wl.region_read_off)
+    rg[:G, 2] = np.uint64(hp.ctypes.data) + wl.region_hap_off[:-1].astype(np.uint64) * np.uint64(24)
+    rg.view(np.int32)[:G, 6] = np.diff(wl.region_hap_off)
     wl._keep.append((pd, hp, rg))
     return rg.ctypes.data
 

@@ -244,8 +244,8 @@ def test_device_dragstr_gives_the_restatements_planes(engine, tables):
 def test_device_dragstr_long_reads(engine):
     # reads of 1..2000 bases: several warps' worth of positions per read, one block per read's shared memory
     rng = np.random.default_rng(11)
-    lens = [1, 2, 31, 32, 33, 700, 2000]
-    reads = [_str_read(rng, n) for n in lens]
+    lens = [1, 2, 31, 32, 33, 64, 700, 1024, 1025, 2000]
+    reads = [_str_read(rng, n) for n in lens] + [b"A" * 300, b"AC" * 200, b"ACGTTGCA" * 40 + b"T"]
     hap = _str_read(rng, 2100)
     wl = _one_region(reads, [hap], rng)
     mapq = np.full(wl.n_reads, 60)
@@ -286,6 +286,15 @@ def test_dragstr_fp32_path_within_tolerance(engine):
         e64.close()
     assert np.all(np.isfinite(got))
     assert np.abs(got - ref).max() <= 1e-3  # CUDA_LOGLESS FP32 bar (absolute, log10 space)
+
+
+@pytest.mark.gpu
+def test_dragstr_read_length_limit(engine):
+    # the imputation holds a read in shared memory: 28000 bases at most, longer reads are refused
+    rng = np.random.default_rng(2)
+    wl = _one_region([_str_read(rng, 28001)], [_str_read(rng, 300)], rng)
+    with pytest.raises(Exception, match="28000"):
+        engine.compute_raw(wl, np.full(1, 60), dragstr=EXAMPLE)
 
 
 @pytest.mark.gpu
