@@ -227,8 +227,10 @@ __device__ __forceinline__ void str_period(const StrWarp &W, int p, int n, int l
     __syncwarp();
 }
 
-__global__ void dragstr_kernel(DevBatch B, uint8_t *quals, uint8_t *ins, uint8_t *dels, uint8_t *gcp, int64_t n_reads,
-                               PrepArgs P, int lpad, int wstride) {
+// 6 blocks of 8 warps per SM: 40 registers a thread
+__global__ void __launch_bounds__(256, 6) dragstr_kernel(DevBatch B, uint8_t *quals, uint8_t *ins, uint8_t *dels,
+                                                         uint8_t *gcp, int64_t n_reads, PrepArgs P, int lpad,
+                                                         int wstride) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
     unsigned char *base = smem + (size_t)w * wstride;
@@ -287,7 +289,7 @@ int launch_dragstr(const DevBatch &b, int64_t n_reads, const PrepArgs &p, int sm
         if (e) return (int)e;
     }
     const int64_t want = (n_reads + wpb - 1) / wpb;
-    const int64_t cap = (int64_t)sm_count * (64 / wpb);
+    const int64_t cap = (int64_t)sm_count * (48 / wpb);  // the blocks that are resident at once
     const int grid = (int)(want < cap ? want : cap);
     dragstr_kernel<<<grid, 32 * wpb, smem, s>>>(b, const_cast<uint8_t *>(b.quals), const_cast<uint8_t *>(b.ins),
                                               const_cast<uint8_t *>(b.dels), const_cast<uint8_t *>(b.gcp), n_reads, p,
