@@ -93,8 +93,127 @@ __device__ __forceinline__ uint8_t cap_base_quality(int q, int mapq, const PrepA
     return (uint8_t)q;
 }
 
+// v / p for 0 <= v < 2^17 and 2 <= p <= 32, with magic = ceil(2^32 / p); p = 1 passes v through
+__device__ __forceinline__ int div_period(int v, int p, uint32_t magic) {
+    return p == 1 ? v : (int)__umulhi((uint32_t)v, magic);
+}
+
+__device__ __forceinline__ uint32_t period_magic(int p) {
+    return (uint32_t)((0x100000000ull + (uint64_t)p - 1) / (uint64_t)p);
+}
+
+// Where D[j] = (base j == base j + p) is 0, for the n bases of S (D is 0 from n - p on): ZM[c] is the zero mask of
+// positions 32 c .. 32 c + 31 (one ballot each), PZ[c] the nearest zero before the chunk (-1 if none) and NZ[c] the
+// nearest zero after it (n if none), found 32 chunks per ballot.  Together they answer "nearest zero at or after y"
+// and "nearest zero before y" for any y in [0, n) in a few instructions.  Warp-collective; ends with __syncwarp.
+__device__ __forceinline__ void zero_index(const uint8_t *S, int n, int p, uint32_t *ZM, uint32_t *PZ, uint32_t *NZ,
+                                           int lane) {
+    const int nch = (n + 31) >> 5;
+    for (int c = 0; c < nch; ++c) {
+        const int x = (c << 5) + lane;
+        const bool d = x + p < n && S[x] == S[x + p];
+        const uint32_t z = __ballot_sync(0xffffffffu, !d);
+        if (lane == 0) ZM[c] = z;
+    }
+    __syncwarp();
+    int carry = -1;  // lane j of a group handles chunk 32 g + j
+    for (int g = 0; g < nch; g += 32) {
+        const int c = g + lane;
+        const uint32_t zm = c < nch ? ZM[c] : 0u;
+        const uint32_t has = __ballot_sync(0xffffffffu, zm != 0u);
+        const uint32_t below = has & ((1u << lane) - 1u);
+        const int kb = below ? 31 - __clz(below) : 0;
+        const uint32_t zb = __shfl_sync(0xffffffffu, zm, kb);
+        if (c < nch) PZ[c] = (uint32_t)(below ? ((g + kb) << 5) + 31 - __clz(zb) : carry);
+        if (has) {
+            const int kl = 31 - __clz(has);
+            carry = ((g + kl) << 5) + 31 - __clz(__shfl_sync(0xffffffffu, zm, kl));
+        }
+    }
+    carry = n;
+    for (int g = (nch - 1) & ~31; g >= 0; g -= 32) {
+        const int c = g + lane;
+        const uint32_t zm = c < nch ? ZM[c] : 0u;
+        const uint32_t has = __ballot_sync(0xffffffffu, zm != 0u);
+        const uint32_t above = lane < 31 ? has >> (lane + 1) : 0u;
+        const int ka = above ? lane + __ffs(above) : 0;
+        const uint32_t za = __shfl_sync(0xffffffffu, zm, ka);
+        if (c < nch) NZ[c] = (uint32_t)(above ? ((g + ka) << 5) + __ffs(za) - 1 : carry);
+        if (has) {
+            const int kf = __ffs(has) - 1;
+            carry = ((g + kf) << 5) + __ffs(__shfl_sync(0xffffffffu, zm, kf)) - 1;
+        }
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ int zero_at_or_after(const uint32_t *ZM, const uint32_t *NZ, int y) {
+    const uint32_t a = ZM[y >> 5] >> (y & 31);
+    return a ? y + __ffs(a) - 1 : (int)NZ[y >> 5];
+}
+
+__device__ __forceinline__ int zero_before(const uint32_t *ZM, const uint32_t *PZ, int y) {
+    const uint32_t b = ZM[y >> 5] & ((1u << (y & 31)) - 1u);
+    return b ? ((y >> 5) << 5) + 31 - __clz(b) : (int)PZ[y >> 5];
+}
+
+// findTandemRepeatUnits(bases, offset).getRight() for every offset of a staged read, from the runs of D for unit
+// lengths L = 1..8.  A unit of L bases ending at offset repeats 1 + floor(run of ones of D ending at offset - L / L)
+// times backward; the unit after offset repeats 1 + floor(run of ones starting at offset + 1 / L) times forward;
+// the first L with more than one copy is the unit, as in the Java loops.  The units are equal when both loops stop
+// at the same L and D is 1 over [offset - L + 1, offset]; otherwise the forward unit's copies ending at offset are
+// floor(run of ones ending at offset / L).  Per offset the state of the two loops packs into one word:
+// bits 0-3 backward L (0: not found), 4-8 its copies, 9-12 forward L, 13-17 its copies, 18-22 copies of the forward
+// unit ending at offset, 23 D1[offset], 24-28 the run of D1 ones ending at offset, 29 units equal.  Copies are
+// capped at 21, which keeps min(sum, 20) exact.
+__device__ __forceinline__ int cap21(int v) { return v < 21 ? v : 21; }
+
+__device__ __forceinline__ void tandem_pass(const uint32_t *ZM, const uint32_t *PZ, const uint32_t *NZ, uint32_t *st,
+                                            int n, int L, uint32_t magic, int lane) {
+    for (int off = lane; off < n - 1; off += 32) {
+        uint32_t w = st[off];
+        if (L == 1) w = 0;
+        int bwL = w & 15, fwL = (w >> 9) & 15;
+        if (bwL == 0 && off + 1 - L >= 0) {
+            const int s = off + 1 - L;
+            const int c = 1 + div_period(s - 1 - zero_before(ZM, PZ, s), L, magic);
+            if (c > 1) {
+                bwL = L;
+                w |= (uint32_t)L | ((uint32_t)cap21(c) << 4);
+            }
+        }
+        if (fwL == 0 && off + L + 1 <= n) {
+            const int x = off + 1;
+            const int c = 1 + div_period(zero_at_or_after(ZM, NZ, x) - x, L, magic);
+            if (c > 1) {
+                fwL = L;
+                const int rep = div_period(x - 1 - zero_before(ZM, PZ, x), L, magic);
+                w |= ((uint32_t)L << 9) | ((uint32_t)cap21(c) << 13) | ((uint32_t)cap21(rep) << 18);
+            }
+        }
+        if (L == 1) {
+            const uint32_t d1 = zero_at_or_after(ZM, NZ, off) > off ? 1u : 0u;
+            w |= (d1 << 23) | ((uint32_t)cap21(off - zero_before(ZM, PZ, off + 1)) << 24);
+        }
+        if (bwL == L && fwL == L && zero_at_or_after(ZM, NZ, off - L + 1) >= off + 1) w |= 1u << 29;
+        st[off] = w;
+    }
+}
+
+__device__ __forceinline__ int tandem_from_state(uint32_t w) {
+    const int bwL = w & 15, fwL = (w >> 9) & 15;
+    const int bw = bwL ? (int)((w >> 4) & 31) : 1, fw = fwL ? (int)((w >> 13) & 31) : 1;
+    const int lb = bwL ? bwL : 1, lf = fwL ? fwL : 1;
+    const bool same = lb == lf && (lb == 1 ? ((w >> 23) & 1u) : ((w >> 29) & 1u));
+    const int rep = fwL ? (int)((w >> 18) & 31) : (int)((w >> 24) & 31);
+    const int rl = same ? bw + fw : fw + rep;
+    return rl < kMaxRepeat ? rl : kMaxRepeat;
+}
+
 __global__ void prep_kernel(DevBatch B, uint8_t *quals, uint8_t *ins, uint8_t *dels, int64_t n_reads, PrepArgs P) {
     __shared__ uint8_t stage[kPrepWarps][kPrepStage];
+    __shared__ uint32_t state[kPrepWarps][kPrepStage];
+    __shared__ uint32_t zidx[kPrepWarps][3 * (kPrepStage / 32)];
     __shared__ uint8_t cache[24];  // indexed by repeat length: shared rather than a local copy of the parameter
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
@@ -102,21 +221,28 @@ __global__ void prep_kernel(DevBatch B, uint8_t *quals, uint8_t *ins, uint8_t *d
         for (int k = 0; k < 24; ++k) cache[k] = P.pcr_cache[k];
     }
     __syncthreads();
+    uint32_t *ZM = zidx[w], *PZ = ZM + kPrepStage / 32, *NZ = PZ + kPrepStage / 32;
     for (int64_t r = (int64_t)blockIdx.x * kPrepWarps + w; r < n_reads; r += (int64_t)gridDim.x * kPrepWarps) {
         const int64_t o = B.read_off[r];
         const int n = (int)(B.read_off[r + 1] - o);
-        const uint8_t *b = B.bases + o;
-        if (P.pcr && n <= kPrepStage) {
-            for (int x = lane; x < n; x += 32) stage[w][x] = b[x];
+        const bool staged = P.pcr && n > 1 && n <= kPrepStage;
+        if (staged) {
+            for (int x = lane; x < n; x += 32) stage[w][x] = B.bases[o + x];
             __syncwarp();
-            b = stage[w];
+            const int top = n - 1 < kMaxUnit ? n - 1 : kMaxUnit;
+            for (int L = 1; L <= top; ++L) {
+                zero_index(stage[w], n, L, ZM, PZ, NZ, lane);
+                tandem_pass(ZM, PZ, NZ, state[w], n, L, period_magic(L), lane);
+                __syncwarp();
+            }
         }
         const int mapq = P.mapq[r];
         for (int x = lane; x < n; x += 32) {
             quals[o + x] = cap_base_quality(quals[o + x], mapq, P);
             int iq = ins[o + x], dq = dels[o + x];
             if (P.pcr && x < n - 1) {  // applyPCRErrorModel: min as unsigned bytes
-                const int cap = cache[tandem_repeat_length(b, n, x)];
+                const int rl = staged ? tandem_from_state(state[w][x]) : tandem_repeat_length(B.bases + o, n, x);
+                const int cap = cache[rl];
                 iq = iq < cap ? iq : cap;
                 dq = dq < cap ? dq : cap;
             }
@@ -151,54 +277,13 @@ struct StrWarp {  // one warp's shared memory for a read of up to lpad - 1 bases
     uint8_t *BP;             // their period
 };
 
-// v / p for 0 <= v < 2^17 and 2 <= p <= 32, with magic = ceil(2^32 / p); p = 1 passes v through
-__device__ __forceinline__ int div_period(int v, int p, uint32_t magic) {
-    return p == 1 ? v : (int)__umulhi((uint32_t)v, magic);
-}
-
 // one period of the analysis, called from one place with the period at run time: a single copy of the code keeps
 // the kernel small enough for the instruction cache
 __device__ __forceinline__ void str_period(const StrWarp &W, int p, int n, int lane) {
-    const uint32_t magic = (uint32_t)((0x100000000ull + (uint64_t)p - 1) / (uint64_t)p);
+    const uint32_t magic = period_magic(p);
     const int nu = n - p + 1;  // unit starts 0 .. n - p
     const int nch = (n + 31) >> 5;
-    for (int c = 0; c < nch; ++c) {
-        const int x = (c << 5) + lane;
-        const bool d = x + p < n && W.S[x] == W.S[x + p];
-        const uint32_t z = __ballot_sync(0xffffffffu, !d);
-        if (lane == 0) W.ZM[c] = z;
-    }
-    __syncwarp();
-    // nearest zeros outside each chunk, lane j of a group handling chunk 32 g + j
-    int carry = -1;
-    for (int g = 0; g < nch; g += 32) {
-        const int c = g + lane;
-        const uint32_t zm = c < nch ? W.ZM[c] : 0u;
-        const uint32_t has = __ballot_sync(0xffffffffu, zm != 0u);
-        const uint32_t below = has & ((1u << lane) - 1u);
-        const int kb = below ? 31 - __clz(below) : 0;
-        const uint32_t zb = __shfl_sync(0xffffffffu, zm, kb);
-        if (c < nch) W.PZ[c] = below ? ((g + kb) << 5) + 31 - __clz(zb) : carry;
-        if (has) {
-            const int kl = 31 - __clz(has);
-            carry = ((g + kl) << 5) + 31 - __clz(__shfl_sync(0xffffffffu, zm, kl));
-        }
-    }
-    carry = n;
-    for (int g = (nch - 1) & ~31; g >= 0; g -= 32) {
-        const int c = g + lane;
-        const uint32_t zm = c < nch ? W.ZM[c] : 0u;
-        const uint32_t has = __ballot_sync(0xffffffffu, zm != 0u);
-        const uint32_t above = lane < 31 ? has >> (lane + 1) : 0u;
-        const int ka = above ? lane + __ffs(above) : 0;
-        const uint32_t za = __shfl_sync(0xffffffffu, zm, ka);
-        if (c < nch) W.NZ[c] = above ? ((g + ka) << 5) + __ffs(za) - 1 : carry;
-        if (has) {
-            const int kf = __ffs(has) - 1;
-            carry = ((g + kf) << 5) + __ffs(__shfl_sync(0xffffffffu, zm, kf)) - 1;
-        }
-    }
-    __syncwarp();
+    zero_index(W.S, n, p, W.ZM, W.PZ, W.NZ, lane);
     for (int c = 0; c < nch; ++c) {
         const int x = (c << 5) + lane;
         const uint32_t z = W.ZM[c];

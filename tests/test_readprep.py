@@ -258,6 +258,23 @@ def test_device_dragstr_long_reads(engine):
 
 
 @pytest.mark.gpu
+def test_device_pcr_model_long_and_repetitive_reads(engine):
+    # reads up to 1,024 bases are searched in shared memory through runs of base-equality masks, longer ones base by
+    # base in place; both against findTandemRepeatUnits as restated
+    rng = np.random.default_rng(12)
+    lens = [1, 2, 3, 9, 31, 32, 33, 64, 700, 1023, 1024, 1025, 2000]
+    reads = [_str_read(rng, n) for n in lens] + [b"A" * 300, b"AC" * 200, b"ACGTTGCA" * 40 + b"T", b"AAC" * 90,
+                                                 b"A" * 1100]
+    wl = _one_region(reads, [_str_read(rng, 2100)], rng)
+    mapq = np.full(wl.n_reads, 60)
+    want = _prepared_workload(wl, mapq, True, 3.0)
+    with engine.raw_batch(wl, mapq, pcr_rate_factor=3.0) as b:
+        _, q, i, d, g = b.read_planes()
+    assert np.array_equal(i, want.ins) and np.array_equal(d, want.dels)
+    assert np.array_equal(q, want.quals) and np.array_equal(g, want.gcp)
+
+
+@pytest.mark.gpu
 def test_dragstr_likelihoods_match_the_prepared_planes():
     # FP64: the raw DRAGstr path against the regular forward on the restatement's planes
     from gatk_gb300.pairhmm import Engine
