@@ -367,28 +367,40 @@ def run_stream(args):
     peaks = eng.measure_peaks()
     n_regions = args.regions or int(native.lib().ghmm_synth_default_regions(args.workload))
     g0, g1 = sharding.block_range(n_regions, rank)
-    blocks = []  # (workload, region struct addresses, output array, output addresses)
+    blocks = []  # (workload, region struct addresses, output array, output addresses, mapping qualities)
     t_gen = time.perf_counter()
     block = 5000
     for a in range(g0, g1, block):
         wl = W.generate(args.workload, regions=min(block, g1 - a), region_begin=a)
-        regs = wl.as_regions()
-        base = ctypes_addr(regs)
+        mapq = None
+        if args.raw:  # the generator's qualities and 45s as raw base qualities and BI / BD tags, seeded MAPQs
+            mapq = np.random.default_rng(1000 + a).integers(20, 70, size=wl.n_reads)
+            base = W.as_raw_regions(wl, mapq, True)
+            regs = wl
+        else:
+            regs = wl.as_regions()
+            base = ctypes_addr(regs)
         out = np.empty(max(wl.n_pairs, 1), dtype=np.float64)
         ra = base + np.arange(wl.n_regions, dtype=np.int64) * 32
         oa = np.where(np.diff(wl.out_off) > 0, out.ctypes.data + wl.out_off[:-1] * 8, 0)
-        blocks.append((wl, regs, out, ra.tolist(), oa.tolist()))
+        blocks.append((wl, regs, out, ra.tolist(), oa.tolist(), mapq))
     t_gen = time.perf_counter() - t_gen
     cells = sum(int(b[0].cells_per_region().sum()) for b in blocks)
     pairs = sum(b[0].n_pairs for b in blocks)
     L = eng.L
-    q = eng.queue(int(args.batch_cells))
+    raw_kw = {}
+    if args.raw == "pcr":
+        raw_kw = {"pcr_rate_factor": 3.0}
+    elif args.raw == "dragstr":
+        raw_kw = {"dragstr": _prep_tables()}
+    q = eng.raw_queue(blocks[0][0], int(args.batch_cells), **raw_kw) if args.raw else eng.queue(int(args.batch_cells))
+    push = L.ghmm_queue_push_raw if args.raw else L.ghmm_queue_push
 
     def push_block(b, limit=None):
         ra, oa = b[3], b[4]
         n = len(ra) if limit is None else min(limit, len(ra))
         for g in range(n):
-            rc = L.ghmm_queue_push(q.h, ra[g], 1, oa[g] or None)
+            rc = push(q.h, ra[g], 1, oa[g] or None)
             if rc:
                 native.check(rc, eng.handle)
 
@@ -421,8 +433,10 @@ def run_stream(args):
     from oracle import oracle as O
 
     wl0, _, out0 = blocks[0][0], blocks[0][1], blocks[0][2]
-    n_cpu, cpu_cells = cpu_sample(wl0, args.cpu_cells)
+    n_cpu, cpu_cells = cpu_sample(wl0, args.cpu_cells / 20 if args.raw else args.cpu_cells)
     sub = wl0.subset(0, n_cpu)
+    if args.raw:  # the oracle's own preparation of the raw reads (untimed), then its forward
+        sub = _oracle_prepared(sub, blocks[0][5][:sub.n_reads], raw_kw)
     t1 = time.perf_counter()
     ref = O.compute_workload(sub, threads=0)
     cpu_dt = time.perf_counter() - t1
@@ -434,9 +448,11 @@ def run_stream(args):
         "metric": METRIC, "value": gcups, "unit": "GCUPS", "n_gpus": world, "steps": 1, "warmup": args.warmup,
         "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (deterministic generator; seeded stand-in for a HaplotypeCaller region stream)",
-        "config": {"workload": ("config4: 100,000 regions of config1's distributions with a 5% tail of "
-                                "2,000 reads x 64 haplotypes, seed 4, streamed one region per push")
-                   if args.workload == 4 else f"workload {args.workload}, streamed one region per push",
+        "config": {"workload": (("config4: 100,000 regions of config1's distributions with a 5% tail of "
+                                 "2,000 reads x 64 haplotypes, seed 4, streamed one region per push")
+                                if args.workload == 4 else f"workload {args.workload}, streamed one region per push")
+                   + (f"; raw reads prepared on the device ({args.raw} imputation, seeded MAPQ 20-69)"
+                      if args.raw else ""),
                    "regions": g1 - g0, "pairs": pairs, "cells": cells, "batch_cells": int(args.batch_cells),
                    "l2": "inputs larger than L2 (streamed from host memory)"},
         "roofline": {"bound": "fp32_fma_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -445,7 +461,8 @@ def run_stream(args):
                      "flop_per_cell": FLOP_PER_CELL},
         "e2e": {"value": gcups, "unit": "GCUPS", "ms_per_step": dt * 1e3, "h2d_bytes_per_step": int(info["h2d_bytes"]),
                 "d2h_bytes_per_step": int(info["d2h_bytes"]),
-                "api": "ghmm_queue_push per region + ghmm_queue_flush (host arrays in, host results out)"},
+                "api": ("ghmm_queue_push_raw" if args.raw else "ghmm_queue_push")
+                + " per region + ghmm_queue_flush (host arrays in, host results out)"},
         "gpu_launches": int(info["n_launches"]),
         "clocks": clk,
         "queue": {"batches": int(info["n_batches"]), "device_ms_fp32_summed": info["ms_fp32"],
@@ -647,6 +664,25 @@ def measured_hbm_peak() -> float:
             return float(json.load(f)["hbm_gbs"])
     except (OSError, KeyError, ValueError):
         return 6800.0
+
+
+def _oracle_prepared(wl, mapq, raw_kw):
+    """wl with its quality planes replaced by oracle/readprep.py's preparation of its raw reads."""
+    import numpy as np
+
+    from gatk_gb300 import workload as W
+    from oracle import readprep as RP
+
+    planes = [np.empty_like(wl.bases) for _ in range(4)]
+    for r in range(wl.n_reads):
+        a, e = int(wl.read_off[r]), int(wl.read_off[r + 1])
+        _, q, i, d, g = RP.prepare_read(wl.bases[a:e], wl.quals[a:e], wl.ins[a:e], wl.dels[a:e], int(mapq[r]),
+                                        rate_factor=raw_kw.get("pcr_rate_factor", 3.0), dragstr=raw_kw.get("dragstr"))
+        for k, v in enumerate((q, i, d, g)):
+            planes[k][a:e] = np.frombuffer(v, dtype=np.uint8)
+    return W.Workload(region_read_off=wl.region_read_off, region_hap_off=wl.region_hap_off, read_off=wl.read_off,
+                      bases=wl.bases, quals=planes[0], ins=planes[1], dels=planes[2], gcp=planes[3],
+                      hap_off=wl.hap_off, hap_bases=wl.hap_bases, out_off=wl.out_off)
 
 
 PREP_BYTES_PER_BASE = {"pcr": 7, "dragstr": 6}  # pcr: read bases, quals, BI, BD; write quals, BI, BD.
@@ -958,6 +994,8 @@ def main():
     ap.add_argument("--prep", choices=["pcr", "dragstr"], default=None,
                     help="read preparation on the device over every workload 1 read (PCR model or DRAGstr)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="time bound of the --prep CPU sample")
+    ap.add_argument("--raw", choices=["pcr", "dragstr"], default=None,
+                    help="with --stream: push raw reads (ghmm_queue_push_raw), prepared on the device")
     ap.add_argument("--sw", action="store_true",
                     help="Smith-Waterman realignment of every workload 1 read to its best haplotype")
     args = ap.parse_args()

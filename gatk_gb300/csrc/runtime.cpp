@@ -905,6 +905,8 @@ struct QueueUnit {
     ghmm_flat flat{};
     std::vector<std::pair<double *, int64_t>> dests;  // output runs in region order
     int64_t cells = 0, n_out = 0, n_regions = 0;
+    std::vector<int32_t> mapq;  // raw queues: mapping quality per read
+    int32_t max_len = 0;        // raw queues: longest read
 
     void seal_flat() {  // point the flat view at the owned vectors
         flat = ghmm_flat{};
@@ -931,6 +933,7 @@ struct QueueUnit {
         std::vector<int64_t>().swap(hap_off);
         std::vector<int64_t>().swap(region_read_off);
         std::vector<int64_t>().swap(region_hap_off);
+        std::vector<int32_t>().swap(mapq);
     }
 };
 
@@ -948,6 +951,13 @@ struct ghmm_queue {
     std::string error_msg;
     ghmm_queue_info info{};
     std::thread worker;
+    // raw queues: the read preparation of every batch (DRAGstr tables copied)
+    bool raw = false;
+    ghmm_read_prep prep{};
+    ghmm_dragstr dragstr{};
+    std::vector<double> str_tables;
+    bool has_bound = false;
+    RouteBound bound;
     // worker-owned
     ghmm_batch slot[2];
     cudaStream_t stream[2]{};
@@ -993,15 +1003,27 @@ int queue_deliver(ghmm_ctx *ctx, ghmm_batch &b, const QueueUnit &u, int threads)
     return GHMM_OK;
 }
 
-// Worker: marshal + upload + launch one unit into slot i (which is free).
+}  // namespace
+
+static int raw_prepare_device(ghmm_ctx *ctx, ghmm_batch &b, const int32_t *mapq, int32_t max_len,
+                              const ghmm_read_prep *prep, cudaStream_t s);
+
+namespace {
+
+// Worker: marshal + upload (+ read preparation for a raw queue) + launch one unit into slot i (which is free).
 int queue_launch(ghmm_queue *q, int i, QueueUnit &u) {
     ghmm_ctx *ctx = q->ctx;
     ghmm_batch &b = q->slot[i];
+    if (q->raw) u.src.bound = q->has_bound ? &q->bound : nullptr;
     int rc = batch_marshal(ctx, u.src, b);
     if (rc) return rc;
     if (b.n_out != u.n_out) return fail(ctx, GHMM_ERR_STATE, "queued batch size mismatch");
     rc = batch_upload(ctx, b, q->stream[i]);
     if (rc) return rc;
+    if (q->raw) {
+        rc = raw_prepare_device(ctx, b, u.mapq.data(), u.max_len, &q->prep, q->stream[i]);
+        if (rc) return rc;
+    }
     rc = batch_enqueue(ctx, b, q->mode, q->stream[i]);
     if (rc) return rc;
     if (b.n_out > 0) {
@@ -1126,11 +1148,30 @@ int queue_wait_all(ghmm_queue *q) {
     return q->error;
 }
 
-int queue_open(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **out) {
+// raw_prep: NULL for a queue of prepared reads; else the (already checked) read preparation of a raw queue
+int queue_open(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **out, const ghmm_read_prep *raw_prep = nullptr,
+               const RouteBound *bound = nullptr) {
     auto *q = new ghmm_queue();
     q->ctx = ctx;
     q->batch_cells = batch_cells > 0 ? batch_cells : (int64_t)2e11;
     q->mode = ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN;
+    if (raw_prep) {
+        q->raw = true;
+        q->prep = *raw_prep;
+        q->prep.dragstr = nullptr;
+        if (raw_prep->dragstr) {
+            const ghmm_dragstr &d = *raw_prep->dragstr;
+            const size_t cells = (size_t)d.max_period * (size_t)d.max_repeats;
+            q->str_tables.assign(d.gop, d.gop + cells);
+            q->str_tables.insert(q->str_tables.end(), d.gcp, d.gcp + cells);
+            q->dragstr = ghmm_dragstr{d.max_period, d.max_repeats, q->str_tables.data(), q->str_tables.data() + cells};
+            q->prep.dragstr = &q->dragstr;
+        }
+        if (bound) {
+            q->has_bound = true;
+            q->bound = *bound;
+        }
+    }
     for (auto &st : q->stream) {
         cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
         if (e != cudaSuccess) {
@@ -1569,13 +1610,13 @@ int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_re
 
 }  // namespace
 
-static int raw_prepare_device(ghmm_ctx *ctx, ghmm_batch &b, const RawView &v, const ghmm_read_prep *prep,
-                              cudaStream_t s) {
+static int raw_prepare_device(ghmm_ctx *ctx, ghmm_batch &b, const int32_t *mapq, int32_t max_len,
+                              const ghmm_read_prep *prep, cudaStream_t s) {
     const int64_t NR = b.n_reads;
     if (NR == 0) return GHMM_OK;
     GHMM_CUDA(b.h_mapq.reserve((size_t)NR), "pinned mapping qualities");
     GHMM_CUDA(b.d_mapq.reserve((size_t)NR), "device mapping qualities");
-    memcpy(b.h_mapq.p, v.mapq.data(), (size_t)NR * sizeof(int32_t));
+    memcpy(b.h_mapq.p, mapq, (size_t)NR * sizeof(int32_t));
     GHMM_CUDA(cudaMemcpyAsync(b.d_mapq.p, b.h_mapq.p, (size_t)NR * sizeof(int32_t), cudaMemcpyHostToDevice, s),
               "H2D mapping qualities");
     PrepArgs p{};
@@ -1605,7 +1646,7 @@ static int raw_prepare_device(ghmm_ctx *ctx, ghmm_batch &b, const RawView &v, co
         p.str_gcp = b.d_dragstr.p + cells;
         p.str_max_period = d.max_period;
         p.str_max_repeats = d.max_repeats;
-        p.max_read_len = v.max_len;
+        p.max_read_len = max_len;
         b.upload_bytes += (int64_t)(2 * cells * sizeof(double));
     }
     if (!b.prep_events) {
@@ -2049,7 +2090,7 @@ int ghmm_batch_create_raw(ghmm_ctx *ctx, const ghmm_raw_region *regions, int32_t
     src.bound = v.has_bound ? &v.bound : nullptr;
     rc = batch_marshal(ctx, src, *b);
     if (!rc) rc = batch_upload(ctx, *b, ctx->stream);
-    if (!rc) rc = raw_prepare_device(ctx, *b, v, prep, ctx->stream);
+    if (!rc) rc = raw_prepare_device(ctx, *b, v.mapq.data(), v.max_len, prep, ctx->stream);
     if (!rc) rc = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? GHMM_OK : fail(ctx, GHMM_ERR_CUDA, "upload");
     if (rc) {
         b->release();
@@ -2091,7 +2132,7 @@ int ghmm_compute_regions_raw(ghmm_ctx *ctx, const ghmm_raw_region *regions, int3
     ghmm_batch &b = ctx->scratch_batch;
     rc = batch_marshal(ctx, src, b);
     if (!rc) rc = batch_upload(ctx, b, ctx->stream);
-    if (!rc) rc = raw_prepare_device(ctx, b, v, prep, ctx->stream);
+    if (!rc) rc = raw_prepare_device(ctx, b, v.mapq.data(), v.max_len, prep, ctx->stream);
     if (!rc) rc = batch_forward(ctx, b, ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN);
     if (!rc) rc = batch_results(ctx, b, out);
     return rc;
@@ -2143,10 +2184,106 @@ int ghmm_queue_create(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **queue) {
     return queue_open(ctx, batch_cells, queue);
 }
 
+int ghmm_queue_create_raw(ghmm_ctx *ctx, int64_t batch_cells, const ghmm_read_prep *prep, ghmm_queue **queue) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!queue || batch_cells < 0) return fail(ctx, GHMM_ERR_ARG, "bad arguments");
+    *queue = nullptr;
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    RawView v;  // checks the preparation arguments (no regions)
+    const int rc = raw_view(ctx, nullptr, 0, prep, v);
+    if (rc) return rc;
+    return queue_open(ctx, batch_cells, queue, prep, v.has_bound ? &v.bound : nullptr);
+}
+
+int ghmm_queue_push_raw(ghmm_queue *q, const ghmm_raw_region *regions, int32_t n_regions, double *out) {
+    if (!q) return GHMM_ERR_STATE;
+    ghmm_ctx *ctx = q->ctx;
+    if (int rc = queue_status(q)) return rc;
+    if (!q->raw) return fail(ctx, GHMM_ERR_STATE, "raw reads go to a queue made by ghmm_queue_create_raw");
+    if (n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad region array");
+    // check everything first, so that a rejected push leaves the queue as it was
+    int64_t n_out = 0;
+    for (int32_t g = 0; g < n_regions; g++) {
+        const ghmm_raw_region &rg = regions[g];
+        if (rg.n_reads < 0 || rg.n_haps < 0 || (rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps))
+            return fail(ctx, GHMM_ERR_ARG, "bad raw region");
+        for (int32_t r = 0; r < rg.n_reads; r++) {
+            const ghmm_raw_read &rd = rg.reads[r];
+            if (rd.length < 0 || rd.length > kMaxReadLen) return fail(ctx, GHMM_ERR_ARG, "read length out of range");
+            if (rd.length > 0 && (!rd.bases || !rd.quals)) return fail(ctx, GHMM_ERR_ARG, "NULL read array");
+            if (rd.mapping_quality < 0 || rd.mapping_quality > 255)
+                return fail(ctx, GHMM_ERR_ARG, "mapping quality 0..255");
+            if (q->prep.dragstr && rd.length > kDragstrMaxRead)
+                return fail(ctx, GHMM_ERR_ARG, "the DRAGstr imputation takes reads of up to 28000 bases");
+            for (int32_t i = 0; i < rd.length; i++)
+                if (rd.quals[i] > kMaxQual || (rd.ins_quals && rd.ins_quals[i] > 127) ||
+                    (rd.del_quals && rd.del_quals[i] > 127))
+                    return fail(ctx, GHMM_ERR_ARG,
+                                "quality out of range (base quality must be <= 254; insertion and deletion qualities "
+                                "0..127)");
+        }
+        for (int32_t h = 0; h < rg.n_haps; h++) {
+            const ghmm_hap &hp = rg.haps[h];
+            if (hp.length < 0 || hp.length > kMaxHapLen) return fail(ctx, GHMM_ERR_ARG, "haplotype length out of range");
+            if (hp.length > 0 && !hp.bases) return fail(ctx, GHMM_ERR_ARG, "NULL haplotype bases");
+        }
+        n_out += (int64_t)rg.n_reads * rg.n_haps;
+    }
+    if (n_out > 0 && !out) return fail(ctx, GHMM_ERR_ARG, "NULL output");
+    if (!q->open) q->open = std::make_unique<QueueUnit>();
+    QueueUnit &u = *q->open;
+    for (int32_t g = 0; g < n_regions; g++) {
+        const ghmm_raw_region &rg = regions[g];
+        int64_t sr = 0, sh = 0;
+        for (int32_t r = 0; r < rg.n_reads; r++) {
+            const ghmm_raw_read &rd = rg.reads[r];
+            const size_t L = (size_t)rd.length;
+            u.planes[0].insert(u.planes[0].end(), rd.bases, rd.bases + L);
+            u.planes[1].insert(u.planes[1].end(), rd.quals, rd.quals + L);
+            if (rd.ins_quals) u.planes[2].insert(u.planes[2].end(), rd.ins_quals, rd.ins_quals + L);
+            else u.planes[2].resize(u.planes[2].size() + L, 45);  // ReadUtils.DEFAULT_INSERTION_DELETION_QUAL
+            if (rd.del_quals) u.planes[3].insert(u.planes[3].end(), rd.del_quals, rd.del_quals + L);
+            else u.planes[3].resize(u.planes[3].size() + L, 45);
+            u.planes[4].resize(u.planes[4].size() + L, (uint8_t)q->prep.gcp);
+            u.read_off.push_back(u.read_off.back() + rd.length);
+            u.mapq.push_back(rd.mapping_quality);
+            u.max_len = std::max(u.max_len, rd.length);
+            sr += rd.length;
+        }
+        for (int32_t h = 0; h < rg.n_haps; h++) {
+            const ghmm_hap &hp = rg.haps[h];
+            u.hap_bases.insert(u.hap_bases.end(), hp.bases, hp.bases + hp.length);
+            u.hap_off.push_back(u.hap_off.back() + hp.length);
+            sh += hp.length;
+        }
+        u.region_read_off.push_back(u.region_read_off.back() + rg.n_reads);
+        u.region_hap_off.push_back(u.region_hap_off.back() + rg.n_haps);
+        u.n_regions++;
+        u.cells += sr * sh;
+        std::lock_guard<std::mutex> lk(q->mu);
+        q->info.n_cells += sr * sh;
+    }
+    if (n_out > 0) {
+        if (!u.dests.empty() && u.dests.back().first + u.dests.back().second == out)
+            u.dests.back().second += n_out;  // contiguous with the previous push
+        else
+            u.dests.emplace_back(out, n_out);
+    }
+    u.n_out += n_out;
+    {
+        std::lock_guard<std::mutex> lk(q->mu);
+        q->info.n_regions += n_regions;
+        q->info.n_pairs += n_out;
+    }
+    if (u.cells >= q->batch_cells) queue_submit(q, std::move(q->open));
+    return queue_status(q);
+}
+
 int ghmm_queue_push(ghmm_queue *q, const ghmm_region *regions, int32_t n_regions, double *out) {
     if (!q) return GHMM_ERR_STATE;
     ghmm_ctx *ctx = q->ctx;
     if (int rc = queue_status(q)) return rc;
+    if (q->raw) return fail(ctx, GHMM_ERR_STATE, "a raw queue takes ghmm_queue_push_raw");
     if (n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad region array");
     // check everything first, so that a rejected push leaves the queue as it was
     int64_t n_out = 0;

@@ -221,6 +221,9 @@ _SIGS = {
     "ghmm_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
     "ghmm_queue_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
     "ghmm_queue_push": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "ghmm_queue_create_raw": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                             ctypes.POINTER(ctypes.c_void_p)]),
+    "ghmm_queue_push_raw": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
     "ghmm_queue_flush": (ctypes.c_int, [ctypes.c_void_p]),
     "ghmm_queue_get_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(QueueInfo)]),
     "ghmm_queue_destroy": (ctypes.c_int, [ctypes.c_void_p]),

@@ -231,6 +231,13 @@ class Engine:
     def queue(self, batch_cells: int = 0) -> "Queue":
         return Queue(self, batch_cells)
 
+    def raw_queue(self, wl_keep: Workload, batch_cells: int = 0, base_quality_threshold: int = 18,
+                  cap_to_mapq: bool = True, pcr_rate_factor: float = 3.0, gcp: int = 10, dragstr=None) -> "Queue":
+        """A queue of raw reads prepared on the device (ghmm_queue_create_raw); the preparation arguments are kept
+        alive on wl_keep until the queue is created (the library copies them, tables included)."""
+        p = _read_prep(base_quality_threshold, cap_to_mapq, pcr_rate_factor, gcp, dragstr, wl_keep)
+        return Queue(self, batch_cells, raw_prep=p)
+
     def measure_peaks(self):
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         native.check(self.L.ghmm_measure_peaks(self._ctx.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
@@ -333,12 +340,34 @@ class Queue:
     here) until ``flush`` returns.
     """
 
-    def __init__(self, engine: Engine, batch_cells: int = 0):
+    def __init__(self, engine: Engine, batch_cells: int = 0, raw_prep: native.ReadPrep | None = None):
         self.engine = engine
         h = ctypes.c_void_p()
-        native.check(engine.L.ghmm_queue_create(engine.handle, int(batch_cells), ctypes.byref(h)), engine.handle)
+        if raw_prep is None:
+            rc = engine.L.ghmm_queue_create(engine.handle, int(batch_cells), ctypes.byref(h))
+        else:
+            rc = engine.L.ghmm_queue_create_raw(engine.handle, int(batch_cells), ctypes.byref(raw_prep), ctypes.byref(h))
+        native.check(rc, engine.handle)
         self.h = h
+        self.raw = raw_prep is not None
         self._keep: list = []
+
+    def push_raw(self, wl: Workload, mapq, with_indel_quals: bool = True, out: np.ndarray | None = None) -> np.ndarray:
+        """Push every region of a workload as raw reads (one push per region) into a raw queue; wl.quals are the raw
+        base qualities, wl.ins / wl.dels the BI / BD tags (or none with with_indel_quals False)."""
+        from .workload import as_raw_regions
+
+        regs = as_raw_regions(wl, mapq, with_indel_quals)
+        if out is None:
+            out = np.empty(wl.n_pairs, dtype=np.float64)
+        size = ctypes.sizeof(native.RawRegion)
+        oo = wl.out_off
+        for g in range(wl.n_regions):
+            rc = self.engine.L.ghmm_queue_push_raw(self.h, regs + g * size, 1,
+                                                   out.ctypes.data + int(oo[g]) * 8 if oo[g + 1] > oo[g] else None)
+            native.check(rc, self.engine.handle)
+        self._keep.append((out, wl))
+        return out
 
     def push_regions(self, regions, n_regions: int, out: np.ndarray, keep=None) -> None:
         """Push n_regions ghmm_region structs starting at ``regions`` (a ctypes pointer); out is float64."""

@@ -339,6 +339,15 @@ int ghmm_queue_flush(ghmm_queue *queue);
 int ghmm_queue_get_info(ghmm_queue *queue, ghmm_queue_info *info);
 int ghmm_queue_destroy(ghmm_queue *queue);
 
+/* A queue of raw reads, prepared on the device batch by batch (as ghmm_compute_regions_raw prepares them):
+ *   ghmm_queue_create_raw: prep (checked as ghmm_compute_regions_raw checks it, DRAGstr tables copied) applies to
+ *                          every batch of the queue;
+ *   ghmm_queue_push_raw:   as ghmm_queue_push, for raw regions.
+ * A raw queue takes only ghmm_queue_push_raw, a queue from ghmm_queue_create only ghmm_queue_push
+ * (GHMM_ERR_STATE otherwise).  Flush, info and destroy are shared. */
+int ghmm_queue_create_raw(ghmm_ctx *ctx, int64_t batch_cells, const ghmm_read_prep *prep, ghmm_queue **queue);
+int ghmm_queue_push_raw(ghmm_queue *queue, const ghmm_raw_region *regions, int32_t n_regions, double *out);
+
 /* Measured FP32 FMA-pipe peak of the device in TFLOP/s (FMA = 2 FLOP): best of a scalar FFMA and a
  * packed FFMA2 register-resident loop over all SMs, timed with CUDA events.  Also reports the FP64
  * DFMA peak.  Either output may be NULL. */

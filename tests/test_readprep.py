@@ -329,3 +329,65 @@ def test_dragstr_rejects_bad_tables(engine, bad):
     wl, mapq = _dragstr_workload()
     with pytest.raises(Exception, match="DRAGstr"):
         engine.compute_raw(wl, mapq, dragstr=(gop, gcp))
+
+
+# ---- raw reads through the streaming queue (ghmm_queue_create_raw / ghmm_queue_push_raw) ----
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["pcr", "dragstr"])
+def test_raw_queue_matches_the_raw_call(engine, kind):
+    # small batches, so that the regions spread over several batches and both buffer slots
+    if kind == "pcr":
+        wl, mapq = _raw_workload(21)
+        kw = {"pcr_rate_factor": 3.0}
+    else:
+        wl, mapq = _dragstr_workload(22)
+        kw = {"dragstr": EXAMPLE}
+    want = engine.compute_raw(wl, mapq, **kw)
+    q = engine.raw_queue(wl, batch_cells=int(wl.cells() // 3) + 1, **kw)
+    try:
+        got = q.push_raw(wl, mapq)
+        q.flush()
+        info = q.info()
+    finally:
+        q.close()
+    assert info["n_batches"] >= 3 and info["n_regions"] == wl.n_regions
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.gpu
+def test_raw_and_plain_queues_take_their_own_pushes(engine):
+    from gatk_gb300 import native
+
+    wl, mapq = _raw_workload(23)
+    rq = engine.raw_queue(wl)
+    try:
+        with pytest.raises(native.GhmmError, match="ghmm_queue_push_raw"):
+            rq.push(wl)
+        rq.push_raw(wl, mapq)  # the rejected push left the queue usable
+        rq.flush()
+    finally:
+        rq.close()
+    pq = engine.queue()
+    try:
+        with pytest.raises(native.GhmmError, match="ghmm_queue_create_raw"):
+            pq.push_raw(wl, mapq)
+    finally:
+        pq.close()
+
+
+@pytest.mark.gpu
+def test_raw_queue_rejects_bad_reads_at_push(engine):
+    from gatk_gb300 import native
+
+    wl, mapq = _raw_workload(24)
+    bad = mapq.copy()
+    bad[0] = 300  # the first read of the first region: the first push fails, nothing is queued
+    q = engine.raw_queue(wl)
+    try:
+        with pytest.raises(native.GhmmError, match="mapping quality"):
+            q.push_raw(wl, bad)
+        got = q.push_raw(wl, mapq)
+        q.flush()
+    finally:
+        q.close()
+    assert np.array_equal(got, engine.compute_raw(wl, mapq))
