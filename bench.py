@@ -129,7 +129,7 @@ def run_reference(args):
     from gatk_gb300 import workload as W
     from oracle import oracle as O
 
-    wl_full = W.generate(args.workload, regions=args.regions)
+    wl_full = W.generate(args.workload, regions=args.regions or None)
     n, cells = cpu_sample(wl_full, args.cpu_cells)
     sub = wl_full.subset(0, n)
     threads = O.num_threads()
