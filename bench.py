@@ -578,8 +578,9 @@ def run_calib(args):
 def run_pd(args):
     """--pd: the PD-HMM (LoglessPDPairHMM, DRAGEN-GATK mode) over workload 1's regions with synthetic
     partially-determined haplotypes (1-3 undetermined SNPs and 0-2 undetermined deletions per haplotype,
-    seeded).  Device-resident GCUPS of the FP64 PD kernel, e2e through ghmm_pd_compute_regions, accuracy and the
-    CPU baseline against the FP64 PD oracle on the leading regions."""
+    seeded).  Device-resident GCUPS of the default path (GHMM_MODE_PD_FP32: the FP32 PD kernel, pairs whose sums
+    underflow recomputed by the FP64 one) and of the all-FP64 path (GHMM_MODE_PD), e2e through
+    ghmm_pd_compute_regions, accuracy and the CPU baseline against the FP64 PD oracle on the leading regions."""
     import numpy as np
 
     from gatk_gb300 import native, workload as W
@@ -593,20 +594,27 @@ def run_pd(args):
     pd = W.pd_flags(wl, 5)
     cells = int(wl.cells_per_region().sum())
     batch = eng.pd_batch(wl, pd)
-    for _ in range(args.warmup):
-        batch.forward(native.MODE_PD)
+
+    def timed(mode):
+        for _ in range(args.warmup):
+            batch.forward(mode)
+        sts = []
+        for _ in range(args.steps):
+            batch.forward(mode)
+            sts.append(batch.stats())
+        return sts, batch.results()
+
     clocks = ClockSampler(0)
     clocks.start()
-    sts = []
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        batch.forward(native.MODE_PD)
-        sts.append(batch.stats())
-    dt_host = (time.perf_counter() - t0) / args.steps
+    sts, res = timed(native.MODE_PD_FP32)
     clk = clocks.stop()
+    sts64, res64 = timed(native.MODE_PD)
     ms = statistics.mean(s["ms_total"] for s in sts)
-    ms_kernel = statistics.mean(s["ms_fp64"] for s in sts)
-    res = batch.results()
+    ms_fp32 = statistics.mean(s["ms_fp32"] for s in sts)
+    ms_rerun = statistics.mean(s["ms_fp64"] for s in sts)
+    ms64 = statistics.mean(s["ms_total"] for s in sts64)
+    ms64_kernel = statistics.mean(s["ms_fp64"] for s in sts64)
+    n_rerun = int(sts[-1]["n_rerun"])
     io = batch.stats()
     batch.close()
     out = eng.pd_compute(wl, pd)  # warm
@@ -620,21 +628,33 @@ def run_pd(args):
     ref = O.pd_compute_workload(sub, sub_pd)
     cpu_dt = time.perf_counter() - t1
     d = absdiff(res[: sub.n_pairs], ref)
-    dp_flop_per_cell = 11  # M: add, mul, fma, mul; I: mul, fma; D: mul, fma (FMA = 2): 8 FP64-pipe operations
-    achieved = dp_flop_per_cell * cells / (ms_kernel * 1e-3) / 1e12
+    d64 = absdiff(res64[: sub.n_pairs], ref)
+    flop_per_cell = 11  # M: mul + 2 fma, D: mul + fma, I: mul + fma (FMA = 2), as the regular recurrence
+    achieved = flop_per_cell * cells / (ms_fp32 * 1e-3) / 1e12
+    peak32 = max(peaks["fp32_tflops"], peaks["fp32x2_tflops"])
+    dp_achieved = 11 * cells / (ms64_kernel * 1e-3) / 1e12
     line = {
-        "metric": "PD-HMM GCUPS (FP64, partially determined haplotypes) on 1 GB300", "value": cells / (ms * 1e-3) / 1e9,
+        "metric": "PD-HMM GCUPS (partially determined haplotypes) on 1 GB300", "value": cells / (ms * 1e-3) / 1e9,
         "unit": "GCUPS", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-        "higher_is_better": True, "dtype": "f64", "data": "synthetic (workload 1 regions with seeded PD flags)",
+        "higher_is_better": True, "dtype": "f32",
+        "data": "synthetic (workload 1 regions with seeded PD flags)",
         "config": {"workload": f"first {n_regions} regions of config1 with 1-3 undetermined SNPs and 0-2 undetermined "
-                               "deletions per haplotype", "regions": n_regions, "pairs": wl.n_pairs, "cells": cells},
-        "roofline": {"bound": "fp64_pipe", "achieved": achieved, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
-                     "frac": achieved / peaks["fp64_tflops"], "flop_per_cell": dp_flop_per_cell,
-                     "kernel": "pd_fp64_kernel<4>"},
+                               "deletions per haplotype", "regions": n_regions, "pairs": wl.n_pairs, "cells": cells,
+                   "mode": "GHMM_MODE_PD_FP32 (FP32 PD kernel, FP64 reruns of underflows)"},
+        "roofline": {"bound": "fp32_fma_pipe", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
+                     "frac": achieved / peak32, "flop_per_cell": flop_per_cell,
+                     "kernel": "pd_kernel<float, K> (the FP32 pass)", "ms_fp32_pass": ms_fp32,
+                     "ms_fp64_reruns": ms_rerun},
+        "fp64_rerun": {"pairs": n_rerun, "fraction": n_rerun / max(1, wl.n_pairs)},
+        "fp64_mode": {"value": cells / (ms64 * 1e-3) / 1e9, "unit": "GCUPS", "ms_per_step": ms64,
+                      "mode": "GHMM_MODE_PD (every pair in FP64 at the reference's 2^1020 scale)",
+                      "roofline": {"bound": "fp64_pipe", "achieved": dp_achieved, "peak": peaks["fp64_tflops"],
+                                   "unit": "TFLOP/s", "frac": dp_achieved / peaks["fp64_tflops"]},
+                      "max_abs_dlog10_vs_oracle": float(d64.max())},
         "e2e": {"value": cells / dt_e2e / 1e9, "unit": "GCUPS", "ms_per_step": dt_e2e * 1e3,
                 "h2d_bytes_per_step": int(io["h2d_bytes"]), "d2h_bytes_per_step": int(io["d2h_bytes"]),
                 "api": "ghmm_pd_compute_regions", "matches_batch": bool(np.array_equal(out, res))},
-        "gpu_launches": args.steps,
+        "gpu_launches": int(sts[-1]["n_launches"]) * args.steps,
         "clocks": clk,
         "cpu_baseline": {"value": cpu_cells / cpu_dt / 1e9, "unit": "GCUPS", "cores": O.num_threads(), "kind": "port",
                          "sample": f"first {n_cpu} regions ({cpu_cells:.3e} cells, {sub.n_pairs} pairs)",

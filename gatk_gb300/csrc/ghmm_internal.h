@@ -101,10 +101,15 @@ struct PdPlanes {
     const uint8_t *states;
 };
 int pd_kernel_occupancy(int *blocks_per_sm);
-int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int k, int begin, int count, int grid,
-              cudaStream_t s);
+// PD pairs [begin, begin + count) of the pair list (count_dev: the count in device memory), K rows per lane, in
+// FP32 (underflows queued for FP64 at rerun[rerun_capacity..)) or FP64; cursor is the counter the warps draw from.
+int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int k, bool fp32, int begin, int count,
+              int cursor, const int32_t *count_dev, int grid, cudaStream_t s);
 constexpr int kPdMaxK = 4;          // PD kernel: rows per lane 1..4
-constexpr int kCounterPdBase = 40;  // counters[40 + K]: PD task cursors (inside the 64 counters, above the buckets)
+constexpr int kCounterPdBase = 40;  // counters[40 + K]: PD FP64 task cursors (inside the 64 counters, above the buckets)
+constexpr int kCounterPdF32Base = 45;  // counters[45 + K]: PD FP32 task cursors
+constexpr int kCounterPdRerun = 50;    // PD pairs the FP32 pass queued for FP64
+constexpr int kCounterPdRerunCursor = 51;
 
 // Read preparation on the device (prep.cu).
 struct PrepArgs {

@@ -15,10 +15,16 @@
 //
 // Kernel: one (read, haplotype) pair per warp, K rows per lane (K = 1..4, per read the strip height that wastes the
 // fewest padding rows), the anti-diagonal wavefront of the FP64 kernels in kernels.cu with six values per row,
-// strips of 32*K rows through per-warp scratch (six doubles per column), FP64 at the reference's scale 2^1020.  Steps where no lane of the warp is at an AFTER_DEL or DEL_END column (nearly all)
-// take a path without max(); the rest take the general one.
+// strips of 32*K rows through per-warp scratch (six values per column).  Steps where no lane of the warp is at an
+// AFTER_DEL or DEL_END column (nearly all) take a path without max(); the rest take the general one.  Two precisions
+// of the same code:
+//   double: the reference's scale 2^1020 and FP64 arithmetic (GHMM_MODE_PD, and the reruns below);
+//   float:  scale 2^120, FP32 arithmetic (64 times the FP64 rate on this part); a sum below
+//           GHMM_FP32_RERUN_THRESHOLD at that scale, or not finite, queues the pair for the FP64 kernel, as the
+//           regular FP32 pass does (GHMM_MODE_PD_FP32).
 #include <cuda_runtime.h>
 
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 
@@ -28,8 +34,29 @@ namespace ghmm {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr double kLog10Scale = 307.0505955772608;  // log10(2^1020)
+constexpr double kLog10Scale = 307.0505955772608;    // log10(2^1020)
+constexpr double kLog10Scale32 = 36.12359947967774;  // log10(2^120)
+constexpr float kLog2Threshold = -93.01398f;         // log2(GHMM_FP32_RERUN_THRESHOLD)
 constexpr int kPdBlock = 128;
+
+__device__ __forceinline__ double vfma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float vfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double vmax(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ float vmax(float a, float b) { return fmaxf(a, b); }
+
+// The transition and prior tables in the kernel's precision
+template <typename V>
+struct PdTab;
+template <>
+struct PdTab<double> {
+    const double *prob, *err3, *m2m, *err;
+    __device__ explicit PdTab(const DevTables &T) : prob(T.prob_d), err3(T.err3_d), m2m(T.m2m_d), err(T.err_d) {}
+};
+template <>
+struct PdTab<float> {
+    const float *prob, *err3, *m2m, *err;
+    __device__ explicit PdTab(const DevTables &T) : prob(T.prob_f), err3(T.err3_f), m2m(T.m2m_f), err(T.err_f) {}
+};
 
 __device__ __forceinline__ uint32_t pd_base_bit(uint32_t x) {
     switch (x) {
@@ -41,15 +68,19 @@ __device__ __forceinline__ uint32_t pd_base_bit(uint32_t x) {
     }
 }
 
-// Pairs [begin, begin + count) of the batch's pair list, all of whose reads take K rows per lane: the host picks,
-// per read, the strip height 32 K (K = 1..4) that wastes the fewest padding rows.
-template <int K>
-__global__ void __launch_bounds__(kPdBlock, 3) pd_fp64_kernel(DevTables T, DevBatch B, PdPlanes P, int begin, int count,
-                                                              int cursor) {
+// Pairs [begin, begin + count) of the batch's pair list (count_dev: the count in device memory instead), all of
+// whose reads take K rows per lane: the host picks, per read, the strip height 32 K (K = 1..4) that wastes the fewest
+// padding rows; FP64 reruns all take K = 4.
+template <typename V, int K>
+__global__ void __launch_bounds__(kPdBlock, sizeof(V) == 4 ? 4 : 3) pd_kernel(DevTables TT, DevBatch B, PdPlanes P, int begin, int count,
+                                                         int cursor, const int32_t *count_dev) {
+    constexpr bool F32 = sizeof(V) == 4;
     constexpr int S = 32 * K;
+    const PdTab<V> T(TT);
     const int lane = threadIdx.x & 31;
     const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    double *scratch = B.scratch64 + warp_global * B.scratch64_cols * 6;
+    V *scratch = reinterpret_cast<V *>(B.scratch64) + warp_global * B.scratch64_cols * 6;
+    if (count_dev) count = min(*count_dev, (int)B.rerun_capacity);
     for (;;) {
         int t = 0;
         if (lane == 0) t = atomicAdd(&B.counters[cursor], 1);
@@ -73,20 +104,20 @@ __global__ void __launch_bounds__(kPdBlock, 3) pd_fp64_kernel(DevTables T, DevBa
             if (lane == 0) atomicExch(&B.counters[3], 2);
             continue;
         }
-        const double init = B.hap_init_d[hap];
+        const V init = F32 ? (V)B.hap_init_f[hap] : (V)B.hap_init_d[hap];
         const int nstrips = (R + S - 1) / S;
         const int pad = nstrips * S - R;
         const uint8_t *hb = B.hap_bases + hoff;
         const uint8_t *hf = P.flags + hoff;
         const uint8_t *hs = P.states + hoff;
-        double acc = 0.0;
+        V acc = 0;
         for (int strip = 0; strip < nstrips; ++strip) {
             // tii doubles as DD (equal for read rows); a dummy row has tii = 1 so its D holds the row-0 value and its
             // I stays at the (zero) value above it
             // the prior is folded into M's coefficients: (prior x MM, prior x IM) for a match and a mismatch, so a
             // cell's M costs one multiply and two fused multiply-adds (this part's FP64 pipe takes a DMUL or DADD
             // for two DFMAs)
-            double mMM[K], mIM[K], eMM[K], eIM[K], tmi[K], tii[K], tmd[K];
+            V mMM[K], mIM[K], eMM[K], eIM[K], tmi[K], tii[K], tmd[K];
             uint32_t rbase[K], rbit[K];
             bool first[K], dummy[K];
 #pragma unroll
@@ -95,42 +126,42 @@ __global__ void __launch_bounds__(kPdBlock, 3) pd_fp64_kernel(DevTables T, DevBa
                 dummy[k] = p < 0;
                 first[k] = p == 0;
                 if (p < 0) {
-                    mMM[k] = mIM[k] = eMM[k] = eIM[k] = 0.0;
-                    tmi[k] = tmd[k] = 0.0;
-                    tii[k] = 1.0;
+                    mMM[k] = mIM[k] = eMM[k] = eIM[k] = 0;
+                    tmi[k] = tmd[k] = 0;
+                    tii[k] = 1;
                     rbase[k] = 0x100u;
                     rbit[k] = 0u;
                 } else {
                     const uint8_t base = B.bases[roff + p], q = B.quals[roff + p];
                     const uint8_t ins = B.ins[roff + p], del = B.dels[roff + p], gcp = B.gcp[roff + p];
-                    const double pm = __ldg(T.prob_d + q), pe = __ldg(T.err3_d + q);
-                    const double mm = __ldg(T.m2m_d + ins * 128 + del), im = __ldg(T.prob_d + gcp);
+                    const V pm = __ldg(T.prob + q), pe = __ldg(T.err3 + q);
+                    const V mm = __ldg(T.m2m + ins * 128 + del), im = __ldg(T.prob + gcp);
                     mMM[k] = pm * mm;
                     mIM[k] = pm * im;
                     eMM[k] = pe * mm;
                     eIM[k] = pe * im;
-                    tmi[k] = __ldg(T.err_d + ins);
-                    tii[k] = __ldg(T.err_d + gcp);
-                    tmd[k] = __ldg(T.err_d + del);
+                    tmi[k] = __ldg(T.err + ins);
+                    tii[k] = __ldg(T.err + gcp);
+                    tmd[k] = __ldg(T.err + del);
                     rbase[k] = base;
                     rbit[k] = pd_base_bit(base);
                 }
             }
-            double Mp[K], Ip[K], Dp[K], bM[K], bI[K], bD[K];
+            V Mp[K], Ip[K], Dp[K], bM[K], bI[K], bD[K];
             auto reset = [&]() {
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
-                    Mp[k] = Ip[k] = 0.0;
-                    Dp[k] = dummy[k] ? init : 0.0;
-                    bM[k] = bI[k] = bD[k] = 0.0;
+                    Mp[k] = Ip[k] = 0;
+                    Dp[k] = dummy[k] ? init : (V)0;
+                    bM[k] = bI[k] = bD[k] = 0;
                 }
             };
             reset();
-            double gM = 0.0, gI = 0.0, gbM = 0.0, gbI = 0.0, gbD = 0.0;
+            V gM = 0, gI = 0, gbM = 0, gbI = 0, gbD = 0;
             const bool above_dummy = (strip == 0) && (lane * K - 1 < pad);
-            double gD = above_dummy ? init : 0.0;
+            V gD = above_dummy ? init : (V)0;
             const bool last_strip = strip == nstrips - 1;
-            double nx[6] = {0, 0, 0, 0, 0, 0};
+            V nx[6] = {0, 0, 0, 0, 0, 0};
             if (strip > 0 && lane == 0)
 #pragma unroll
                 for (int v = 0; v < 6; ++v) nx[v] = scratch[v];
@@ -144,12 +175,12 @@ __global__ void __launch_bounds__(kPdBlock, 3) pd_fp64_kernel(DevTables T, DevBa
                     f = __ldg(hf + c);
                     st = __ldg(hs + c);
                 }
-                if (c == 0) {  // column-0 boundary: M = I = D = 0 (row 0: D = 2^1020 / H), branches 0
+                if (c == 0) {  // column-0 boundary: M = I = D = 0 (row 0: D = scale / H), branches 0
                     reset();
-                    gM = gI = gbM = gbI = gbD = 0.0;
-                    gD = above_dummy ? init : 0.0;
+                    gM = gI = gbM = gbI = gbD = 0;
+                    gD = above_dummy ? init : (V)0;
                 }
-                double u[6];
+                V u[6];
                 u[0] = __shfl_up_sync(kFull, Mp[K - 1], 1);
                 u[1] = __shfl_up_sync(kFull, Ip[K - 1], 1);
                 u[2] = __shfl_up_sync(kFull, Dp[K - 1], 1);
@@ -158,7 +189,7 @@ __global__ void __launch_bounds__(kPdBlock, 3) pd_fp64_kernel(DevTables T, DevBa
                 u[5] = __shfl_up_sync(kFull, bD[K - 1], 1);
                 if (lane == 0) {
                     if (strip == 0) {
-                        u[0] = u[1] = u[3] = u[4] = u[5] = 0.0;
+                        u[0] = u[1] = u[3] = u[4] = u[5] = 0;
                         u[2] = init;
                     } else {
 #pragma unroll
@@ -176,26 +207,26 @@ __global__ void __launch_bounds__(kPdBlock, 3) pd_fp64_kernel(DevTables T, DevBa
                 // pass 1 (bottom-up, the row above still holds the previous column): branches, M, D
 #pragma unroll
                 for (int k = K - 1; k >= 0; --k) {
-                    const double dM = k ? Mp[k - 1] : gM, dI = k ? Ip[k - 1] : gI, dD = k ? Dp[k - 1] : gD;
+                    const V dM = k ? Mp[k - 1] : gM, dI = k ? Ip[k - 1] : gI, dD = k ? Dp[k - 1] : gD;
                     const uint32_t sk = first[k] ? st1 : st2;
                     const bool match = rbase[k] == y || rbase[k] == 'N' || yn || ((f & 1u) && (f & rbit[k]));
-                    const double cMM = match ? mMM[k] : eMM[k], cIM = match ? mIM[k] : eIM[k];
-                    double Mn, Dn, nbM, nbI, nbD;
+                    const V cMM = match ? mMM[k] : eMM[k], cIM = match ? mIM[k] : eIM[k];
+                    V Mn, Dn, nbM, nbI, nbD;
                     if (!special) {
                         const bool inside = sk == 1u;
                         nbM = inside ? bM[k] : Mp[k];
                         nbI = inside ? bI[k] : Ip[k];
                         nbD = inside ? bD[k] : Dp[k];
-                        Mn = fma(dM, cMM, fma(dI, cIM, dD * cIM));
-                        Dn = fma(Dp[k], tii[k], Mp[k] * tmd[k]);
+                        Mn = vfma(dM, cMM, vfma(dI, cIM, dD * cIM));
+                        Dn = vfma(Dp[k], tii[k], Mp[k] * tmd[k]);
                     } else {
-                        const double dbM = k ? bM[k - 1] : gbM, dbI = k ? bI[k - 1] : gbI, dbD = k ? bD[k - 1] : gbD;
+                        const V dbM = k ? bM[k - 1] : gbM, dbI = k ? bI[k - 1] : gbI, dbD = k ? bD[k - 1] : gbD;
                         if (sk == 2u) {
-                            nbM = fmax(bM[k], Mp[k]);
-                            nbI = fmax(bI[k], Ip[k]);
-                            nbD = fmax(bD[k], Dp[k]);
-                            Mn = fma(fmax(dbM, dM), cMM, fma(fmax(dbI, dI), cIM, fmax(dbD, dD) * cIM));
-                            Dn = fma(fmax(bD[k], Dp[k]), tii[k], fmax(bM[k], Mp[k]) * tmd[k]);
+                            nbM = vmax(bM[k], Mp[k]);
+                            nbI = vmax(bI[k], Ip[k]);
+                            nbD = vmax(bD[k], Dp[k]);
+                            Mn = vfma(vmax(dbM, dM), cMM, vfma(vmax(dbI, dI), cIM, vmax(dbD, dD) * cIM));
+                            Dn = vfma(vmax(bD[k], Dp[k]), tii[k], vmax(bM[k], Mp[k]) * tmd[k]);
                         } else {
                             const bool inside = sk == 1u;
                             nbM = inside ? bM[k] : Mp[k];
@@ -205,7 +236,7 @@ __global__ void __launch_bounds__(kPdBlock, 3) pd_fp64_kernel(DevTables T, DevBa
                             Dn = fma(Dp[k], tii[k], Mp[k] * tmd[k]);
                         }
                     }
-                    if (!valid) Mn = Dn = 0.0, nbM = nbI = nbD = 0.0;
+                    if (!valid) Mn = Dn = 0, nbM = nbI = nbD = 0;
                     Mp[k] = Mn;
                     Dp[k] = Dn;
                     bM[k] = nbM;
@@ -213,15 +244,15 @@ __global__ void __launch_bounds__(kPdBlock, 3) pd_fp64_kernel(DevTables T, DevBa
                     bD[k] = nbD;
                 }
                 // pass 2 (top-down): I from the row above at this column
-                double aM = u[0], aI = u[1], abM = u[3], abI = u[4];
+                V aM = u[0], aI = u[1], abM = u[3], abI = u[4];
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
-                    double In;
+                    V In;
                     if (special && del_end)
-                        In = fma(fmax(abI, aI), tii[k], fmax(abM, aM) * tmi[k]);
+                        In = vfma(vmax(abI, aI), tii[k], vmax(abM, aM) * tmi[k]);
                     else
-                        In = fma(aI, tii[k], aM * tmi[k]);
-                    if (!valid) In = 0.0;
+                        In = vfma(aI, tii[k], aM * tmi[k]);
+                    if (!valid) In = 0;
                     Ip[k] = In;
                     aM = Mp[k];
                     aI = In;
@@ -238,7 +269,7 @@ __global__ void __launch_bounds__(kPdBlock, 3) pd_fp64_kernel(DevTables T, DevBa
                     if (last_strip) {
                         acc += Mp[K - 1] + Ip[K - 1];
                     } else {
-                        double *d = scratch + 6 * c;
+                        V *d = scratch + 6 * c;
                         d[0] = Mp[K - 1];
                         d[1] = Ip[K - 1];
                         d[2] = Dp[K - 1];
@@ -250,24 +281,32 @@ __global__ void __launch_bounds__(kPdBlock, 3) pd_fp64_kernel(DevTables T, DevBa
             }
             __syncwarp();
         }
-        if (lane == 31) B.out[out_index] = log10(acc) - kLog10Scale;
+        if (lane == 31) {
+            if (!F32) {
+                B.out[out_index] = log10((double)acc) - kLog10Scale;
+            } else if (acc > 0.f && acc <= FLT_MAX && log2f((float)acc) >= kLog2Threshold) {
+                B.out[out_index] = log10((double)acc) - kLog10Scale32;
+            } else {  // underflow at 2^120 (or not finite): the FP64 kernel recomputes the pair
+                const int idx = atomicAdd(&B.counters[kCounterPdRerun], 1);
+                if ((int64_t)idx < B.rerun_capacity)
+                    B.rerun[B.rerun_capacity + idx] = pr;
+                else
+                    atomicExch(&B.counters[3], 1);
+            }
+        }
     }
 }
 
 }  // namespace
 
 int pd_kernel_occupancy(int *blocks_per_sm) {
-    // every K variant runs on the same grid and scratch: the smallest occupancy of the four
+    // the FP64 variants run on one grid and scratch: the smallest occupancy of them (FP32 variants: launch_pd)
     int best = 1 << 30;
-    for (int k = 1; k <= kPdMaxK; ++k) {
+    const void *fns[] = {(const void *)pd_kernel<double, 1>, (const void *)pd_kernel<double, 2>,
+                         (const void *)pd_kernel<double, 3>, (const void *)pd_kernel<double, 4>};
+    for (const void *fn : fns) {
         int n = 0;
-        cudaError_t e;
-        switch (k) {
-            case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pd_fp64_kernel<1>, kPdBlock, 0); break;
-            case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pd_fp64_kernel<2>, kPdBlock, 0); break;
-            case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pd_fp64_kernel<3>, kPdBlock, 0); break;
-            default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pd_fp64_kernel<4>, kPdBlock, 0); break;
-        }
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kPdBlock, 0);
         if (e != cudaSuccess) return (int)e;
         best = n < best ? n : best;
     }
@@ -275,16 +314,34 @@ int pd_kernel_occupancy(int *blocks_per_sm) {
     return 0;
 }
 
-int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int k, int begin, int count, int grid,
-              cudaStream_t s) {
-    const int cursor = kCounterPdBase + k;
+int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int k, bool fp32, int begin, int count,
+              int cursor, const int32_t *count_dev, int grid, cudaStream_t s) {
+    // grid is the FP64 kernels' (the strip scratch is sized for it, six doubles per column and warp); an FP32
+    // variant fits as many more resident blocks as its registers allow, up to twice that grid in the same scratch
+    auto f32_grid = [&](const void *fn) {
+        int n = 0, dev = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kPdBlock, 0) != cudaSuccess || n <= 0) return grid;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int want = n * sms;
+        return want < 2 * grid ? (want > grid ? want : grid) : 2 * grid;
+    };
+#define GHMM_PD_CASE(KK)                                                                                      \
+    case KK:                                                                                                  \
+        if (fp32)                                                                                             \
+            pd_kernel<float, KK><<<f32_grid((const void *)pd_kernel<float, KK>), kPdBlock, 0, s>>>(          \
+                t, b, p, begin, count, cursor, count_dev);                                                    \
+        else                                                                                                  \
+            pd_kernel<double, KK><<<grid, kPdBlock, 0, s>>>(t, b, p, begin, count, cursor, count_dev);        \
+        break;
     switch (k) {
-        case 1: pd_fp64_kernel<1><<<grid, kPdBlock, 0, s>>>(t, b, p, begin, count, cursor); break;
-        case 2: pd_fp64_kernel<2><<<grid, kPdBlock, 0, s>>>(t, b, p, begin, count, cursor); break;
-        case 3: pd_fp64_kernel<3><<<grid, kPdBlock, 0, s>>>(t, b, p, begin, count, cursor); break;
-        case 4: pd_fp64_kernel<4><<<grid, kPdBlock, 0, s>>>(t, b, p, begin, count, cursor); break;
+        GHMM_PD_CASE(1)
+        GHMM_PD_CASE(2)
+        GHMM_PD_CASE(3)
+        GHMM_PD_CASE(4)
         default: return (int)cudaErrorInvalidValue;
     }
+#undef GHMM_PD_CASE
     return (int)cudaGetLastError();
 }
 

@@ -689,14 +689,15 @@ static int fill_fp64_all(ghmm_ctx *ctx, ghmm_batch &b) {
 static int batch_enqueue(ghmm_ctx *ctx, ghmm_batch &b, int mode, cudaStream_t s);
 static int batch_finish(ghmm_ctx *ctx, ghmm_batch &b);
 
-static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b);
+static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32);
 
 static int batch_forward(ghmm_ctx *ctx, ghmm_batch &b, int mode) {
     if (!b.uploaded) return fail(ctx, GHMM_ERR_STATE, "batch not uploaded");
-    if (b.has_pd != (mode == GHMM_MODE_PD))
-        return fail(ctx, GHMM_ERR_ARG, b.has_pd ? "a PD-HMM batch runs in GHMM_MODE_PD only"
-                                                : "GHMM_MODE_PD needs a batch from ghmm_pd_batch_create");
-    if (mode == GHMM_MODE_PD) return batch_forward_pd(ctx, b);
+    const bool pd_mode = mode == GHMM_MODE_PD || mode == GHMM_MODE_PD_FP32;
+    if (b.has_pd != pd_mode)
+        return fail(ctx, GHMM_ERR_ARG, b.has_pd ? "a PD-HMM batch runs in GHMM_MODE_PD or GHMM_MODE_PD_FP32 only"
+                                                : "the PD-HMM modes need a batch from ghmm_pd_batch_create");
+    if (pd_mode) return batch_forward_pd(ctx, b, mode == GHMM_MODE_PD_FP32);
     if (ctx->double_precision && mode == GHMM_MODE_FP32_RERUN) mode = GHMM_MODE_FP64;
     cudaStream_t s = ctx->stream;
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -1414,7 +1415,9 @@ static int pd_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
     return GHMM_OK;
 }
 
-static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b) {
+// fp32: every pair in the FP32 PD kernel, then the pairs whose sums underflow in the FP64 one (K = 4 for all);
+// otherwise every pair in FP64
+static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32) {
     cudaStream_t s = ctx->stream;
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     // every pair, grouped by the rows per lane K of its read (the strip height 32 K, K = 1..4, that needs the
@@ -1468,8 +1471,16 @@ static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b) {
     int launches = 0;
     for (int kk = kPdMaxK; kk >= 1; --kk) {  // longest strips first
         if (kcount[kk] == 0) continue;
-        int e = launch_pd(ctx->tables, b.dev, b.pd, kk, (int)kbegin[kk], (int)kcount[kk], grid, s);
+        const int cursor = (fp32 ? kCounterPdF32Base : kCounterPdBase) + kk;
+        int e = launch_pd(ctx->tables, b.dev, b.pd, kk, fp32, (int)kbegin[kk], (int)kcount[kk], cursor, nullptr, grid, s);
         if (e) return cuda_fail(ctx, (cudaError_t)e, "PD-HMM launch");
+        launches++;
+    }
+    GHMM_CUDA(cudaEventRecord(b.ev[4], s), "event");
+    if (fp32 && k > 0) {  // the FP32 pass's underflows, queued at rerun[capacity..), in FP64
+        int e = launch_pd(ctx->tables, b.dev, b.pd, kPdMaxK, false, (int)b.dev.rerun_capacity, 0,
+                          kCounterPdRerunCursor, b.d_counters.p + kCounterPdRerun, grid, s);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "PD-HMM FP64 rerun launch");
         launches++;
     }
     GHMM_CUDA(cudaEventRecord(b.ev[2], s), "event");
@@ -1477,17 +1488,21 @@ static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b) {
               "D2H counters");
     GHMM_CUDA(cudaEventRecord(b.ev[3], s), "event");
     GHMM_CUDA(cudaEventSynchronize(b.ev[3]), "PD-HMM kernel");
-    float ms = 0;
-    cudaEventElapsedTime(&ms, b.ev[1], b.ev[2]);
-    b.ms_fp64 = ms;
-    b.ms_fp32 = b.ms_plain = 0;
+    float ms = 0, ms_a = 0, ms_b = 0;
+    cudaEventElapsedTime(&ms_a, b.ev[1], b.ev[4]);
+    cudaEventElapsedTime(&ms_b, b.ev[4], b.ev[2]);
+    b.ms_fp32 = fp32 ? ms_a : 0;
+    b.ms_fp64 = fp32 ? ms_b : ms_a + ms_b;
+    b.ms_plain = 0;
     cudaEventElapsedTime(&ms, b.ev[0], b.ev[3]);
     b.ms_total = ms;
-    b.last_mode = GHMM_MODE_PD;
+    b.last_mode = fp32 ? GHMM_MODE_PD_FP32 : GHMM_MODE_PD;
     b.last_launches = launches;
-    b.last_rerun = b.last_exact = 0;
+    b.last_rerun = fp32 ? hc[kCounterPdRerun] : 0;
+    b.last_exact = 0;
     b.forward_h2d = k * (int64_t)sizeof(PairRef) + (kNumCounters + 2 * kNumBucketKeys) * 4;
     b.forward_d2h = kNumCounters * 4;
+    if (hc[3] == 1) return fail(ctx, GHMM_ERR_CUDA, "PD-HMM FP64 rerun queue overflow");
     if (hc[3] != 0) return fail(ctx, GHMM_ERR_CUDA, "device-side scratch bound exceeded");
     return GHMM_OK;
 }
@@ -1904,7 +1919,7 @@ int ghmm_batch_create_flat(ghmm_ctx *ctx, const ghmm_flat *flat, ghmm_batch **ou
 int ghmm_batch_forward(ghmm_ctx *ctx, ghmm_batch *b, int32_t mode) {
     if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
     if (!b) return fail(ctx, GHMM_ERR_ARG, "NULL batch");
-    if (mode < 0 || mode > 3) return fail(ctx, GHMM_ERR_ARG, "unknown mode");
+    if (mode < 0 || mode > GHMM_MODE_PD_FP32) return fail(ctx, GHMM_ERR_ARG, "unknown mode");
     return batch_forward(ctx, *b, mode);
 }
 
@@ -1919,8 +1934,10 @@ int ghmm_batch_stats(ghmm_ctx *ctx, const ghmm_batch *b, ghmm_stats *st) {
     if (!b || !st) return fail(ctx, GHMM_ERR_ARG, "NULL argument");
     st->n_pairs = b->n_out;
     st->n_cells = b->n_cells;
-    st->n_rerun = b->last_mode == GHMM_MODE_FP32_RERUN ? b->last_rerun : 0;
-    st->n_fp64_direct = b->last_mode == GHMM_MODE_FP64 ? b->n_out : b->n_direct + b->n_direct_exact;
+    st->n_rerun = (b->last_mode == GHMM_MODE_FP32_RERUN || b->last_mode == GHMM_MODE_PD_FP32) ? b->last_rerun : 0;
+    st->n_fp64_direct = (b->last_mode == GHMM_MODE_FP64 || b->last_mode == GHMM_MODE_PD) ? b->n_out
+                        : b->last_mode == GHMM_MODE_PD_FP32                            ? 0
+                                                                                       : b->n_direct + b->n_direct_exact;
     st->n_fp64_exact = b->last_mode == GHMM_MODE_PLAIN_FP64 ? 0 : b->last_exact;
     st->n_tasks_fp32 = b->n_tasks;
     st->n_launches = b->last_launches;
@@ -2163,7 +2180,7 @@ int ghmm_pd_compute_regions(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_
     ghmm_batch &b = ctx->pd_batch;
     int rc = pd_marshal(ctx, regions, n_regions, b);
     if (!rc) rc = pd_upload(ctx, b, ctx->stream);
-    if (!rc) rc = batch_forward(ctx, b, GHMM_MODE_PD);
+    if (!rc) rc = batch_forward(ctx, b, ctx->double_precision ? GHMM_MODE_PD : GHMM_MODE_PD_FP32);
     if (!rc) rc = batch_results(ctx, b, out);
     return rc;
 }

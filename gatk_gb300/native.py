@@ -23,6 +23,7 @@ GHMM_ERR_TIMEOUT = 7
 MODE_FP32_RERUN = 0
 MODE_FP64 = 1
 MODE_PD = 3
+MODE_PD_FP32 = 4
 FP64_RESCALED_FLOOR = -500.0  # GHMM_FP64_RESCALED_FLOOR
 MODE_PLAIN_FP64 = 2
 

@@ -60,6 +60,8 @@ extern "C" {
 
 /* Forward modes for ghmm_batch_forward. */
 #define GHMM_MODE_PD 3         /* PD-HMM batch (ghmm_pd_batch_create): every pair in the FP64 PD-HMM kernel */
+#define GHMM_MODE_PD_FP32 4    /* PD-HMM batch: FP32 PD-HMM kernel (scale 2^120) + FP64 rerun of underflowing pairs;
+                                  ghmm_pd_compute_* use it unless the context is double precision */
 #define GHMM_MODE_FP32_RERUN 0 /* batched FP32 wavefront + FP64 rerun of underflowing pairs (default) */
 #define GHMM_MODE_FP64 1       /* every pair in the FP64 wavefront kernel (useDoublePrecision) */
 #define GHMM_MODE_PLAIN_FP64 2 /* plain FP64 kernel, one pair per thread block, one launch per region; reads <= 2048 */
@@ -277,8 +279,10 @@ int ghmm_batch_read_planes(ghmm_ctx *ctx, const ghmm_batch *batch, uint8_t *base
  * (PH/LoglessPDPairHMM.java:35-150), whose native binding IntelPDHMM.computeLikelihoods(ReadDataHolder[],
  * HaplotypeDataHolder[], double[]) is called at PH/VectorLoglessPairPDHMM.java:98.  A PD haplotype carries, beside its
  * bases, one flag byte per base (PartiallyDeterminedHaplotype.java:59-66: SNP 1, DEL_START 2, DEL_END 4, and the
- * alternative-base bits A 8, C 16, G 32, T 64, N 128), HaplotypeDataHolder.haplotypePDBases.  Results are FP64 at
- * the reference's 2^1020 scale, read-major as ghmm_compute_likelihoods.  A read base other than A, C, G, T (either
+ * alternative-base bits A 8, C 16, G 32, T 64, N 128), HaplotypeDataHolder.haplotypePDBases.  Results are read-major
+ * as ghmm_compute_likelihoods.  ghmm_pd_compute_* run GHMM_MODE_PD_FP32 (FP32 at scale 2^120, pairs whose sums
+ * underflow recomputed in FP64), or GHMM_MODE_PD (FP64 at the reference's 2^1020 scale for every pair) when the
+ * context is double precision, as the regular path does.  A read base other than A, C, G, T (either
  * case) or N that meets an undetermined SNP column is an argument error, where the reference throws
  * ("Found unexpected base in alt alleles", LoglessPDPairHMM.java:196-210). */
 typedef struct ghmm_pd_hap {
@@ -298,7 +302,7 @@ typedef struct ghmm_pd_region {
 int ghmm_pd_compute_likelihoods(ghmm_ctx *ctx, const ghmm_read *reads, int32_t n_reads, const ghmm_pd_hap *haps,
                                 int32_t n_haps, double *out);
 int ghmm_pd_compute_regions(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_t n_regions, double *out);
-/* A device-resident PD batch; run it with ghmm_batch_forward(..., GHMM_MODE_PD). */
+/* A device-resident PD batch; run it with ghmm_batch_forward(..., GHMM_MODE_PD or GHMM_MODE_PD_FP32). */
 int ghmm_pd_batch_create(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_t n_regions, ghmm_batch **batch);
 
 /* Streaming queue: regions enqueued one at a time as they arrive, as HaplotypeCaller produces them.

@@ -43,6 +43,7 @@ def test_header_constants_match_the_bindings():
     assert int(defs["GHMM_MODE_FP64"]) == native.MODE_FP64
     assert int(defs["GHMM_MODE_PLAIN_FP64"]) == native.MODE_PLAIN_FP64
     assert int(defs["GHMM_MODE_PD"]) == native.MODE_PD
+    assert int(defs["GHMM_MODE_PD_FP32"]) == native.MODE_PD_FP32
     assert float(defs["GHMM_FP64_RESCALED_FLOOR"]) == native.FP64_RESCALED_FLOOR
     sw = open(os.path.join(ROOT, "include", "ghmm_sw.h")).read()
     swd = dict(re.findall(r"#define (GHMM_\w+) \(?([-0-9]+)", sw))

@@ -151,20 +151,63 @@ def _pd_workload(regions=6, seed=5):
     return wl, W.pd_flags(wl, seed)
 
 
+@pytest.fixture(scope="module")
+def engine64():
+    """A double-precision engine: ghmm_pd_compute_* run every pair in FP64 (GHMM_MODE_PD)."""
+    from gatk_gb300.pairhmm import Engine
+
+    e = Engine(use_double_precision=True)
+    yield e
+    e.close()
+
+
 @pytest.mark.gpu
-def test_gpu_pdhmm_matches_oracle(engine):
+def test_gpu_pdhmm_matches_oracle(engine, engine64):
     wl, pd = _pd_workload(8)
     ref = O.pd_compute_workload(wl, pd)
-    got = engine.pd_compute(wl, pd)
-    assert np.abs(got - ref).max() <= 1e-9
+    assert np.abs(engine64.pd_compute(wl, pd) - ref).max() <= 1e-9  # FP64 PD kernel
+    assert np.abs(engine.pd_compute(wl, pd) - ref).max() <= 1e-3    # FP32 PD kernel + FP64 reruns (the FP32 bar)
 
 
 @pytest.mark.gpu
-def test_gpu_pdhmm_without_flags_equals_plain(engine):
+def test_gpu_pdhmm_without_flags_equals_plain(engine, engine64):
     wl = W.generate(1, regions=4)
-    got = engine.pd_compute(wl, np.zeros(len(wl.hap_bases), dtype=np.uint8))
+    flags = np.zeros(len(wl.hap_bases), dtype=np.uint8)
     ref = O.compute_workload(wl)
-    assert np.abs(got - ref).max() <= 1e-9
+    assert np.abs(engine64.pd_compute(wl, flags) - ref).max() <= 1e-9
+    assert np.abs(engine.pd_compute(wl, flags) - ref).max() <= 1e-3
+
+
+@pytest.mark.gpu
+def test_gpu_pdhmm_fp32_reruns_underflows_in_fp64(engine):
+    # long reads against long haplotypes with many mismatches: log10 L far below the FP32 range at 2^120, so the FP32
+    # pass queues them and the FP64 kernel recomputes them; every result within the FP64 bar of the oracle for
+    # those pairs and the FP32 bar for the rest
+    from gatk_gb300 import native
+
+    rng = np.random.default_rng(33)
+    regions, pds = [], []
+    for k in range(6):
+        H = int(rng.integers(500, 900))
+        R = int(rng.integers(200, 400)) if k % 2 == 0 else int(rng.integers(40, 80))
+        hap, pd, read, q, ins, dls, g = _case(rng, H=H, R=R, n_snp=4, n_del=2, end_flag=False)
+        read = bytearray(read)
+        if k % 2 == 0:  # one base in four replaced: far beyond the FP32 range
+            for i in range(0, len(read), 4):
+                read[i] = ord("ACGT"[(("ACGT".index(chr(read[i])) if chr(read[i]) in "ACGT" else 0) + 1) % 4])
+        regions.append(([bytes(hap)], [(bytes(read), q, ins, dls, g)]))
+        pds.append(pd)
+    wl = W.from_pairs(regions)
+    pd = np.concatenate(pds)
+    ref = O.pd_compute_workload(wl, pd)
+    with engine.pd_batch(wl, pd) as b:
+        b.forward(native.MODE_PD_FP32)
+        got = b.results()
+        st = b.stats()
+    low = ref < -120.0
+    assert low.any() and st["n_rerun"] >= int(low.sum())
+    assert np.abs(got[low] - ref[low]).max() <= 1e-9
+    assert np.abs(got - ref).max() <= 1e-3
 
 
 @pytest.mark.gpu
@@ -185,8 +228,13 @@ def test_gpu_pdhmm_hand_cases_and_long_reads(engine):
     wl = W.from_pairs(regions)
     pd = np.concatenate(pds)
     ref = O.pd_compute_workload(wl, pd)
-    got = engine.pd_compute(wl, pd)
-    assert np.abs(got - ref).max() <= 1e-9
+    from gatk_gb300 import native
+
+    with engine.pd_batch(wl, pd) as b:
+        b.forward(native.MODE_PD)
+        assert np.abs(b.results() - ref).max() <= 1e-9
+        b.forward(native.MODE_PD_FP32)
+        assert np.abs(b.results() - ref).max() <= 1e-3
 
 
 @pytest.mark.gpu
@@ -195,10 +243,11 @@ def test_gpu_pdhmm_batch_and_errors(engine):
 
     wl, pd = _pd_workload(3)
     with engine.pd_batch(wl, pd) as b:
-        b.forward(native.MODE_PD)
-        a = b.results()
-        b.forward(native.MODE_PD)
-        assert np.array_equal(a, b.results())
+        for mode in (native.MODE_PD, native.MODE_PD_FP32):
+            b.forward(mode)
+            a = b.results()
+            b.forward(mode)
+            assert np.array_equal(a, b.results())
         with pytest.raises(native.GhmmError):
             b.forward(native.MODE_FP32_RERUN)
     # a read base outside ACGTacgtN meeting an undetermined SNP: the reference throws
