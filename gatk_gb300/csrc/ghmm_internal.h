@@ -105,11 +105,12 @@ int pd_kernel_occupancy(int *blocks_per_sm);
 // FP32 (underflows queued for FP64 at rerun[rerun_capacity..)) or FP64; cursor is the counter the warps draw from.
 int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int k, bool fp32, int begin, int count,
               int cursor, const int32_t *count_dev, int grid, cudaStream_t s);
-constexpr int kPdMaxK = 4;          // PD kernel: rows per lane 1..4
+constexpr int kPdMaxK = 4;          // PD kernel: rows per lane 1..4 in FP64
+constexpr int kPdMaxK32 = 8;        // and 1..8 in FP32
 constexpr int kCounterPdBase = 40;  // counters[40 + K]: PD FP64 task cursors (inside the 64 counters, above the buckets)
-constexpr int kCounterPdF32Base = 45;  // counters[45 + K]: PD FP32 task cursors
-constexpr int kCounterPdRerun = 50;    // PD pairs the FP32 pass queued for FP64
-constexpr int kCounterPdRerunCursor = 51;
+constexpr int kCounterPdRerun = 45;        // PD pairs the FP32 pass queued for FP64
+constexpr int kCounterPdRerunCursor = 46;
+constexpr int kCounterPdF32Base = 50;      // counters[50 + K]: PD FP32 task cursors (51..58)
 
 // Read preparation on the device (prep.cu).
 struct PrepArgs {

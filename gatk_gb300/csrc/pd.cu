@@ -70,9 +70,9 @@ __device__ __forceinline__ uint32_t pd_base_bit(uint32_t x) {
 
 // Pairs [begin, begin + count) of the batch's pair list (count_dev: the count in device memory instead), all of
 // whose reads take K rows per lane: the host picks, per read, the strip height 32 K (K = 1..4) that wastes the fewest
-// padding rows; FP64 reruns all take K = 4.
+// padding rows (K = 1..4 in FP64, 1..8 in FP32); FP64 reruns all take K = 4.
 template <typename V, int K>
-__global__ void __launch_bounds__(kPdBlock, sizeof(V) == 4 ? 4 : 3) pd_kernel(DevTables TT, DevBatch B, PdPlanes P, int begin, int count,
+__global__ void __launch_bounds__(kPdBlock, (sizeof(V) == 4 && K <= 4) ? 4 : 3) pd_kernel(DevTables TT, DevBatch B, PdPlanes P, int begin, int count,
                                                          int cursor, const int32_t *count_dev) {
     constexpr bool F32 = sizeof(V) == 4;
     constexpr int S = 32 * K;
@@ -334,14 +334,25 @@ int launch_pd(const DevTables &t, const DevBatch &b, const PdPlanes &p, int k, b
         else                                                                                                  \
             pd_kernel<double, KK><<<grid, kPdBlock, 0, s>>>(t, b, p, begin, count, cursor, count_dev);        \
         break;
+#define GHMM_PD_CASE32(KK)                                                                                    \
+    case KK:                                                                                                  \
+        if (!fp32) return (int)cudaErrorInvalidValue;                                                         \
+        pd_kernel<float, KK><<<f32_grid((const void *)pd_kernel<float, KK>), kPdBlock, 0, s>>>(              \
+            t, b, p, begin, count, cursor, count_dev);                                                        \
+        break;
     switch (k) {
         GHMM_PD_CASE(1)
         GHMM_PD_CASE(2)
         GHMM_PD_CASE(3)
         GHMM_PD_CASE(4)
+        GHMM_PD_CASE32(5)
+        GHMM_PD_CASE32(6)
+        GHMM_PD_CASE32(7)
+        GHMM_PD_CASE32(8)
         default: return (int)cudaErrorInvalidValue;
     }
 #undef GHMM_PD_CASE
+#undef GHMM_PD_CASE32
     return (int)cudaGetLastError();
 }
 

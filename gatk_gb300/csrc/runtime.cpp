@@ -1425,28 +1425,29 @@ static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32) {
     GHMM_CUDA(b.h_fp64all.reserve((size_t)std::max<int64_t>(b.n_out, 1)), "pinned PD pairs");
     const int64_t *o = b.h_off.p;
     const int64_t *rro = o + b.n_reads + 1 + b.n_haps + 1, *rho = rro + b.n_regions + 1;
-    auto pick_k = [](int64_t R) {
-        int best_k = kPdMaxK;
+    const int maxk = fp32 ? kPdMaxK32 : kPdMaxK;
+    auto pick_k = [maxk](int64_t R) {
+        int best_k = maxk;
         int64_t best_rows = INT64_MAX;
-        for (int k = kPdMaxK; k >= 1; --k) {
+        for (int k = maxk; k >= 1; --k) {
             const int64_t rows = ((R + 32 * k - 1) / (32 * k)) * 32 * k;
             if (rows < best_rows) best_rows = rows, best_k = k;
         }
         return best_k;
     };
-    int64_t kcount[kPdMaxK + 1] = {0};
+    int64_t kcount[kPdMaxK32 + 1] = {0};
     for (int64_t g = 0; g < b.n_regions; g++)
         for (int64_t r = rro[g]; r < rro[g + 1]; r++) kcount[pick_k(o[r + 1] - o[r])] += rho[g + 1] - rho[g];
-    int64_t kbegin[kPdMaxK + 2] = {0};
-    for (int kk = 1; kk <= kPdMaxK; kk++) kbegin[kk + 1] = kbegin[kk] + kcount[kk];
-    int64_t kpos[kPdMaxK + 1];
-    for (int kk = 1; kk <= kPdMaxK; kk++) kpos[kk] = kbegin[kk];
+    int64_t kbegin[kPdMaxK32 + 2] = {0};
+    for (int kk = 1; kk <= maxk; kk++) kbegin[kk + 1] = kbegin[kk] + kcount[kk];
+    int64_t kpos[kPdMaxK32 + 1];
+    for (int kk = 1; kk <= maxk; kk++) kpos[kk] = kbegin[kk];
     for (int64_t g = 0; g < b.n_regions; g++)
         for (int64_t r = rro[g]; r < rro[g + 1]; r++) {
             const int kk = pick_k(o[r + 1] - o[r]);
             for (int64_t h = rho[g]; h < rho[g + 1]; h++) b.h_fp64all.p[kpos[kk]++] = PairRef{(int32_t)r, (int32_t)h};
         }
-    const int64_t k = kbegin[kPdMaxK + 1];
+    const int64_t k = kbegin[maxk + 1];
     int bpsm = 0;
     if (pd_kernel_occupancy(&bpsm) != 0 || bpsm <= 0) bpsm = 1;
     const int grid = ctx->sm_count * bpsm;
@@ -1469,7 +1470,7 @@ static int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32) {
                               cudaMemcpyHostToDevice, s), "H2D counters");
     GHMM_CUDA(cudaEventRecord(b.ev[1], s), "event");
     int launches = 0;
-    for (int kk = kPdMaxK; kk >= 1; --kk) {  // longest strips first
+    for (int kk = maxk; kk >= 1; --kk) {  // longest strips first
         if (kcount[kk] == 0) continue;
         const int cursor = (fp32 ? kCounterPdF32Base : kCounterPdBase) + kk;
         int e = launch_pd(ctx->tables, b.dev, b.pd, kk, fp32, (int)kbegin[kk], (int)kcount[kk], cursor, nullptr, grid, s);
