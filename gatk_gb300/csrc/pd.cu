@@ -27,6 +27,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
 
 #include "ghmm_internal.h"
 
@@ -166,16 +167,19 @@ __global__ void __launch_bounds__(kPdBlock, (sizeof(V) == 4 && K <= 4) ? 4 : 3) 
 #pragma unroll
                 for (int v = 0; v < 6; ++v) nx[v] = scratch[v];
             const int nsteps = H + 31;
-            for (int s = 0; s < nsteps; ++s) {
+            // one wavefront step; CHK steps handle lanes outside the haplotype's columns and the column-0 reset, which
+            // fall in the first 32 and the last 31 steps only
+            auto step = [&](const int s, auto chk_tag) {
+                constexpr bool CHK = decltype(chk_tag)::value;
                 const int c = s - lane;
-                const bool valid = c >= 0 && c < H;
+                const bool valid = !CHK || (c >= 0 && c < H);
                 uint32_t y = 0x200u, f = 0u, st = 0u;
                 if (valid) {
                     y = __ldg(hb + c);
                     f = __ldg(hf + c);
                     st = __ldg(hs + c);
                 }
-                if (c == 0) {  // column-0 boundary: M = I = D = 0 (row 0: D = scale / H), branches 0
+                if (CHK && c == 0) {  // column-0 boundary: M = I = D = 0 (row 0: D = scale / H), branches 0
                     reset();
                     gM = gI = gbM = gbI = gbD = 0;
                     gD = above_dummy ? init : (V)0;
@@ -236,7 +240,7 @@ __global__ void __launch_bounds__(kPdBlock, (sizeof(V) == 4 && K <= 4) ? 4 : 3) 
                             Dn = fma(Dp[k], tii[k], Mp[k] * tmd[k]);
                         }
                     }
-                    if (!valid) Mn = Dn = 0, nbM = nbI = nbD = 0;
+                    if (CHK && !valid) Mn = Dn = 0, nbM = nbI = nbD = 0;
                     Mp[k] = Mn;
                     Dp[k] = Dn;
                     bM[k] = nbM;
@@ -252,7 +256,7 @@ __global__ void __launch_bounds__(kPdBlock, (sizeof(V) == 4 && K <= 4) ? 4 : 3) 
                         In = vfma(vmax(abI, aI), tii[k], vmax(abM, aM) * tmi[k]);
                     else
                         In = vfma(aI, tii[k], aM * tmi[k]);
-                    if (!valid) In = 0;
+                    if (CHK && !valid) In = 0;
                     Ip[k] = In;
                     aM = Mp[k];
                     aI = In;
@@ -278,7 +282,11 @@ __global__ void __launch_bounds__(kPdBlock, (sizeof(V) == 4 && K <= 4) ? 4 : 3) 
                         d[5] = bD[K - 1];
                     }
                 }
-            }
+            };
+            int s = 0;
+            for (; s < nsteps && s < 32; ++s) step(s, std::true_type{});
+            for (; s < H; ++s) step(s, std::false_type{});  // every lane at a column in 1 .. H - 1
+            for (; s < nsteps; ++s) step(s, std::true_type{});
             __syncwarp();
         }
         if (lane == 31) {
