@@ -1557,6 +1557,23 @@ int dragstr_bound(ghmm_ctx *ctx, const ghmm_dragstr &d, RouteBound &rb) {
     return GHMM_OK;
 }
 
+// Checks of one raw region and its reads shared by the raw entry points: 0, or an index into kRawErrors
+const char *const kRawErrors[] = {"", "bad raw region", "read length out of range", "NULL read array",
+                                  "mapping quality 0..255"};
+int raw_region_problem(const ghmm_raw_region &rg, int32_t *max_len) {
+    if (rg.n_reads < 0 || rg.n_haps < 0 || (rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps)) return 1;
+    int32_t mx = 0;
+    for (int32_t r = 0; r < rg.n_reads; r++) {
+        const ghmm_raw_read &rd = rg.reads[r];
+        if (rd.length < 0 || rd.length > kMaxReadLen) return 2;
+        if (rd.length > 0 && (!rd.bases || !rd.quals)) return 3;
+        if (rd.mapping_quality < 0 || rd.mapping_quality > 255) return 4;
+        mx = std::max(mx, rd.length);
+    }
+    *max_len = mx;
+    return 0;
+}
+
 int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_read_prep *prep, RawView &v) {
     if (!prep) return fail(ctx, GHMM_ERR_ARG, "NULL read preparation arguments");
     if (prep->gcp < 1 || prep->gcp > 127) return fail(ctx, GHMM_ERR_ARG, "gap continuation penalty must be 1..127");
@@ -1577,23 +1594,8 @@ int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_re
     std::vector<int8_t> bad((size_t)G, 0);
     std::vector<int32_t> region_max((size_t)G, 0);
     parallel_for(G, threads, [&](int64_t g) {
-        const ghmm_raw_region &rg = raw[g];
-        if (rg.n_reads < 0 || rg.n_haps < 0 || (rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps)) {
-            bad[(size_t)g] = 1;
-            return;
-        }
-        int32_t mx = 0;
-        for (int32_t r = 0; r < rg.n_reads; r++) {
-            const ghmm_raw_read &rd = rg.reads[r];
-            if (rd.length < 0 || rd.length > kMaxReadLen) { bad[(size_t)g] = 2; return; }
-            if (rd.length > 0 && (!rd.bases || !rd.quals)) { bad[(size_t)g] = 3; return; }
-            if (rd.mapping_quality < 0 || rd.mapping_quality > 255) { bad[(size_t)g] = 4; return; }
-            mx = std::max(mx, rd.length);
-        }
-        region_max[(size_t)g] = mx;
+        bad[(size_t)g] = (int8_t)raw_region_problem(raw[g], &region_max[(size_t)g]);
     }, 16);
-    static const char *const kRawErrors[] = {"", "bad raw region", "read length out of range", "NULL read array",
-                                             "mapping quality 0..255"};
     int32_t max_len = 0;
     std::vector<int64_t> first((size_t)G + 1, 0);
     for (int64_t g = 0; g < G; g++) {
@@ -2223,16 +2225,12 @@ int ghmm_queue_push_raw(ghmm_queue *q, const ghmm_raw_region *regions, int32_t n
     int64_t n_out = 0;
     for (int32_t g = 0; g < n_regions; g++) {
         const ghmm_raw_region &rg = regions[g];
-        if (rg.n_reads < 0 || rg.n_haps < 0 || (rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps))
-            return fail(ctx, GHMM_ERR_ARG, "bad raw region");
+        int32_t max_len = 0;
+        if (const int e = raw_region_problem(rg, &max_len)) return fail(ctx, GHMM_ERR_ARG, kRawErrors[e]);
+        if (q->prep.dragstr && max_len > kDragstrMaxRead)
+            return fail(ctx, GHMM_ERR_ARG, "the DRAGstr imputation takes reads of up to 28000 bases");
         for (int32_t r = 0; r < rg.n_reads; r++) {
             const ghmm_raw_read &rd = rg.reads[r];
-            if (rd.length < 0 || rd.length > kMaxReadLen) return fail(ctx, GHMM_ERR_ARG, "read length out of range");
-            if (rd.length > 0 && (!rd.bases || !rd.quals)) return fail(ctx, GHMM_ERR_ARG, "NULL read array");
-            if (rd.mapping_quality < 0 || rd.mapping_quality > 255)
-                return fail(ctx, GHMM_ERR_ARG, "mapping quality 0..255");
-            if (q->prep.dragstr && rd.length > kDragstrMaxRead)
-                return fail(ctx, GHMM_ERR_ARG, "the DRAGstr imputation takes reads of up to 28000 bases");
             for (int32_t i = 0; i < rd.length; i++)
                 if (rd.quals[i] > kMaxQual || (rd.ins_quals && rd.ins_quals[i] > 127) ||
                     (rd.del_quals && rd.del_quals[i] > 127))
