@@ -621,6 +621,13 @@ def run_pd(args):
     t0 = time.perf_counter()
     out = eng.pd_compute(wl, pd)
     dt_e2e = time.perf_counter() - t0
+    # the DRAGEN-GATK chain from raw reads: DRAGstr imputation on the device, then the PD-HMM, in one call
+    mapq = np.random.default_rng(31).integers(20, 70, size=wl.n_reads)
+    tables = _prep_tables()
+    eng.pd_compute_raw(wl, pd, mapq, dragstr=tables)  # warm
+    t0 = time.perf_counter()
+    eng.pd_compute_raw(wl, pd, mapq, dragstr=tables)
+    dt_raw = time.perf_counter() - t0
     n_cpu, cpu_cells = cpu_sample(wl, args.cpu_cells / 4)
     sub = wl.subset(0, n_cpu)
     sub_pd = pd[: int(wl.hap_off[int(wl.region_hap_off[n_cpu])])]
@@ -654,6 +661,9 @@ def run_pd(args):
         "e2e": {"value": cells / dt_e2e / 1e9, "unit": "GCUPS", "ms_per_step": dt_e2e * 1e3,
                 "h2d_bytes_per_step": int(io["h2d_bytes"]), "d2h_bytes_per_step": int(io["d2h_bytes"]),
                 "api": "ghmm_pd_compute_regions", "matches_batch": bool(np.array_equal(out, res))},
+        "e2e_raw_dragstr": {"value": cells / dt_raw / 1e9, "unit": "GCUPS", "ms_per_step": dt_raw * 1e3,
+                            "api": "ghmm_pd_compute_regions_raw with the reference's example DRAGstr model "
+                                   "(imputation on the device, then the PD-HMM; seeded MAPQ 20-69)"},
         "gpu_launches": int(sts[-1]["n_launches"]) * args.steps,
         "clocks": clk,
         "cpu_baseline": {"value": cpu_cells / cpu_dt / 1e9, "unit": "GCUPS", "cores": O.num_threads(), "kind": "port",

@@ -2188,6 +2188,58 @@ int ghmm_pd_compute_regions(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_
     return rc;
 }
 
+// PD regions of raw reads: the raw reads' view (checks, 45s and the constant GCP) as the regular raw path builds it,
+// then the PD marshal over it, the upload, and the read preparation on the device.
+static int pd_raw_build(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions, int32_t n_regions, const ghmm_read_prep *prep,
+                        ghmm_batch &b) {
+    std::vector<ghmm_raw_region> rr((size_t)n_regions);
+    for (int32_t g = 0; g < n_regions; g++) {
+        const ghmm_pd_raw_region &rg = regions[g];
+        if (rg.n_haps < 0 || (rg.n_haps > 0 && !rg.haps)) return fail(ctx, GHMM_ERR_ARG, "bad PD region");
+        rr[(size_t)g] = ghmm_raw_region{rg.reads, rg.n_reads, nullptr, 0};
+    }
+    RawView v;
+    int rc = raw_view(ctx, rr.data(), n_regions, prep, v);
+    if (rc) return rc;
+    std::vector<ghmm_pd_region> pr((size_t)n_regions);
+    for (int32_t g = 0; g < n_regions; g++)
+        pr[(size_t)g] = ghmm_pd_region{v.regions[(size_t)g].reads, regions[g].n_reads, regions[g].haps, regions[g].n_haps};
+    rc = pd_marshal(ctx, pr.data(), n_regions, b);
+    if (!rc) rc = pd_upload(ctx, b, ctx->stream);
+    if (!rc) rc = raw_prepare_device(ctx, b, v.mapq.data(), v.max_len, prep, ctx->stream);
+    return rc;
+}
+
+int ghmm_pd_batch_create_raw(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions, int32_t n_regions,
+                             const ghmm_read_prep *prep, ghmm_batch **out) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!out || n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad arguments");
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    auto *b = new ghmm_batch();
+    int rc = pd_raw_build(ctx, regions, n_regions, prep, *b);
+    if (!rc) rc = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? GHMM_OK : fail(ctx, GHMM_ERR_CUDA, "upload");
+    if (rc) {
+        b->release();
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return GHMM_OK;
+}
+
+int ghmm_pd_compute_regions_raw(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions, int32_t n_regions,
+                                const ghmm_read_prep *prep, double *out) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad region array");
+    if (n_regions == 0) return GHMM_OK;
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    ghmm_batch &b = ctx->pd_batch;
+    int rc = pd_raw_build(ctx, regions, n_regions, prep, b);
+    if (!rc) rc = batch_forward(ctx, b, ctx->double_precision ? GHMM_MODE_PD : GHMM_MODE_PD_FP32);
+    if (!rc) rc = batch_results(ctx, b, out);
+    return rc;
+}
+
 int ghmm_pd_compute_likelihoods(ghmm_ctx *ctx, const ghmm_read *reads, int32_t n_reads, const ghmm_pd_hap *haps,
                                 int32_t n_haps, double *out) {
     if (!ctx || !ctx->alive) return GHMM_ERR_STATE;

@@ -86,6 +86,11 @@ class RawRead(ctypes.Structure):
                 ("del_quals", ctypes.c_void_p), ("length", ctypes.c_int32), ("mapping_quality", ctypes.c_int32)]
 
 
+class PdRawRegion(ctypes.Structure):
+    _fields_ = [("reads", ctypes.c_void_p), ("n_reads", ctypes.c_int32), ("haps", ctypes.c_void_p),
+                ("n_haps", ctypes.c_int32)]
+
+
 class RawRegion(ctypes.Structure):
     _fields_ = [("reads", ctypes.c_void_p), ("n_reads", ctypes.c_int32), ("haps", ctypes.c_void_p),
                 ("n_haps", ctypes.c_int32)]
@@ -216,6 +221,10 @@ _SIGS = {
     "ghmm_pd_compute_regions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, _f64p]),
     "ghmm_pd_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                             ctypes.POINTER(ctypes.c_void_p)]),
+    "ghmm_pd_compute_regions_raw": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                                   ctypes.POINTER(ReadPrep), _f64p]),
+    "ghmm_pd_batch_create_raw": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                                ctypes.POINTER(ReadPrep), ctypes.POINTER(ctypes.c_void_p)]),
     "ghmm_batch_postprocess": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Postprocess),
                                               ctypes.c_void_p]),
     "ghmm_compute_flat": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Flat), _f64p]),

@@ -228,6 +228,26 @@ class Engine:
     def pd_batch(self, wl: Workload, hap_pd: np.ndarray) -> "Batch":
         return Batch(self, wl, pd=hap_pd)
 
+    def pd_compute_raw(self, wl: Workload, hap_pd: np.ndarray, mapq, with_indel_quals: bool = True,
+                       base_quality_threshold: int = 18, cap_to_mapq: bool = True, pcr_rate_factor: float = 3.0,
+                       gcp: int = 10, dragstr=None) -> np.ndarray:
+        """PD-HMM likelihoods from raw reads prepared on the device (ghmm_pd_compute_regions_raw); with dragstr =
+        (gop, gcp) tables the DRAGEN-GATK chain of DRAGstr imputation and PD-HMM."""
+        from .workload import as_pd_raw_regions
+
+        out = np.empty(max(wl.n_pairs, 1), dtype=np.float64)
+        regs = as_pd_raw_regions(wl, hap_pd, mapq, with_indel_quals)
+        p = _read_prep(base_quality_threshold, cap_to_mapq, pcr_rate_factor, gcp, dragstr, wl)
+        native.check(self.L.ghmm_pd_compute_regions_raw(self._ctx.h, regs, wl.n_regions, ctypes.byref(p),
+                                                        out.ctypes.data_as(native._f64p)), self._ctx.h)
+        return out[:wl.n_pairs]
+
+    def pd_raw_batch(self, wl: Workload, hap_pd: np.ndarray, mapq, with_indel_quals: bool = True,
+                     base_quality_threshold: int = 18, cap_to_mapq: bool = True, pcr_rate_factor: float = 3.0,
+                     gcp: int = 10, dragstr=None) -> "Batch":
+        p = _read_prep(base_quality_threshold, cap_to_mapq, pcr_rate_factor, gcp, dragstr, wl)
+        return Batch(self, wl, pd_raw=(hap_pd, mapq, with_indel_quals, p))
+
     def queue(self, batch_cells: int = 0) -> "Queue":
         return Queue(self, batch_cells)
 
@@ -260,11 +280,18 @@ class Engine:
 class Batch:
     """A device-resident batch: inputs uploaded once; forward() reruns the kernels on them."""
 
-    def __init__(self, engine: Engine, wl: Workload, via_regions: bool = False, pd=None, raw=None):
+    def __init__(self, engine: Engine, wl: Workload, via_regions: bool = False, pd=None, raw=None, pd_raw=None):
         self.engine = engine
         self.wl = wl
         h = ctypes.c_void_p()
-        if raw is not None:
+        if pd_raw is not None:
+            from .workload import as_pd_raw_regions
+
+            hap_pd, mapq, with_indel, prep = pd_raw
+            regs = as_pd_raw_regions(wl, hap_pd, mapq, with_indel)
+            rc = engine.L.ghmm_pd_batch_create_raw(engine.handle, regs, wl.n_regions, ctypes.byref(prep),
+                                                   ctypes.byref(h))
+        elif raw is not None:
             from .workload import as_raw_regions
 
             mapq, with_indel, prep = raw

@@ -157,6 +157,23 @@ def as_raw_regions(wl: Workload, mapq: np.ndarray, with_indel_quals: bool = True
     return ctypes.cast(_region_table(wl, rd, 40), ctypes.c_void_p).value
 
 
+def as_pd_raw_regions(wl: Workload, hap_pd: np.ndarray, mapq: np.ndarray, with_indel_quals: bool = True):
+    """ghmm_pd_raw_region array: the workload's reads as raw reads (as as_raw_regions) against its haplotypes with PD
+    flags (as as_pd_regions)."""
+    as_raw_regions(wl, mapq, with_indel_quals)
+    rd = wl._keep[-1][0]
+    as_pd_regions(wl, hap_pd)
+    _, hp, _ = wl._keep[-1]
+    G = wl.n_regions
+    rg = np.zeros((max(G, 1), 4), dtype=np.uint64)
+    rg[:G, 0] = np.uint64(rd.ctypes.data) + wl.region_read_off[:-1].astype(np.uint64) * np.uint64(40)
+    rg.view(np.int32)[:G, 2] = np.diff(wl.region_read_off)
+    rg[:G, 2] = np.uint64(hp.ctypes.data) + wl.region_hap_off[:-1].astype(np.uint64) * np.uint64(24)
+    rg.view(np.int32)[:G, 6] = np.diff(wl.region_hap_off)
+    wl._keep.append((rd, hp, rg))
+    return rg.ctypes.data
+
+
 def as_pd_regions(wl: Workload, hap_pd: np.ndarray):
     """ghmm_pd_region array for a workload whose haplotypes carry PD flags (hap_pd, parallel to hap_bases)."""
     NR, NH, G = wl.n_reads, wl.n_haps, wl.n_regions

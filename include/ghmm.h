@@ -305,6 +305,20 @@ int ghmm_pd_compute_regions(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_
 /* A device-resident PD batch; run it with ghmm_batch_forward(..., GHMM_MODE_PD or GHMM_MODE_PD_FP32). */
 int ghmm_pd_batch_create(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_t n_regions, ghmm_batch **batch);
 
+/* The PD-HMM from raw reads, prepared on the device as ghmm_compute_regions_raw prepares them: the DRAGEN-GATK
+ * mode's chain of DRAGstr imputation (ghmm_read_prep.dragstr) and PD-HMM likelihoods in one call. */
+typedef struct ghmm_pd_raw_region {
+    const ghmm_raw_read *reads;
+    int32_t n_reads;
+    const ghmm_pd_hap *haps;
+    int32_t n_haps;
+} ghmm_pd_raw_region;
+
+int ghmm_pd_compute_regions_raw(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions, int32_t n_regions,
+                                const ghmm_read_prep *prep, double *out);
+int ghmm_pd_batch_create_raw(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions, int32_t n_regions,
+                             const ghmm_read_prep *prep, ghmm_batch **batch);
+
 /* Streaming queue: regions enqueued one at a time as they arrive, as HaplotypeCaller produces them.
  * No counterpart in the reference's binding, whose computeLikelihoods is synchronous per active region
  * (PH/VectorLoglessPairHMM.java:138, called once per region from HC/HaplotypeCallerEngine.java:734-918

@@ -72,6 +72,7 @@ def test_struct_layouts_match_the_header(tmp_path):
                "ghmm_dev_pairs": native.DevPairs, "ghmm_calib_batch": native.CalibBatch,
                "ghmm_postprocess": native.Postprocess, "ghmm_pd_hap": native.PdHap, "ghmm_pd_region": native.PdRegion,
                "ghmm_raw_read": native.RawRead, "ghmm_raw_region": native.RawRegion, "ghmm_read_prep": native.ReadPrep,
+               "ghmm_pd_raw_region": native.PdRawRegion,
                "ghmm_dragstr": native.Dragstr,
                "ghmm_sw_params": native.SwParams, "ghmm_sw_pair": native.SwPair, "ghmm_sw_result": native.SwResult,
                "ghmm_sw_stats": native.SwStats}

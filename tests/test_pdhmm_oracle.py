@@ -258,3 +258,47 @@ def test_gpu_pdhmm_batch_and_errors(engine):
     with pytest.raises(native.GhmmError) as e:
         engine.pd_compute(bad, f)
     assert e.value.code == native.GHMM_ERR_ARG
+
+
+def _oracle_prepared(wl, mapq, dragstr):
+    from oracle import readprep as RP
+
+    planes = [np.empty_like(wl.bases) for _ in range(4)]
+    for r in range(wl.n_reads):
+        a, b = int(wl.read_off[r]), int(wl.read_off[r + 1])
+        _, q, i, d, g = RP.prepare_read(wl.bases[a:b], wl.quals[a:b], wl.ins[a:b], wl.dels[a:b], int(mapq[r]),
+                                        rate_factor=3.0, dragstr=dragstr)
+        for k, v in enumerate((q, i, d, g)):
+            planes[k][a:b] = np.frombuffer(v, dtype=np.uint8)
+    return W.Workload(region_read_off=wl.region_read_off, region_hap_off=wl.region_hap_off, read_off=wl.read_off,
+                      bases=wl.bases, quals=planes[0], ins=planes[1], dels=planes[2], gcp=planes[3],
+                      hap_off=wl.hap_off, hap_bases=wl.hap_bases, out_off=wl.out_off)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["pcr", "dragstr"])
+def test_gpu_pdhmm_from_raw_reads(engine, engine64, kind):
+    # ghmm_pd_compute_regions_raw / ghmm_pd_batch_create_raw: the reads prepared on the device (the DRAGEN-GATK
+    # chain with DRAGstr), then the PD-HMM; against the PD oracle on the restatement's own preparation
+    import json
+    import os
+
+    wl, pd = _pd_workload(4, seed=8)
+    rng = np.random.default_rng(19)
+    wl.quals[:] = rng.integers(2, 45, size=len(wl.quals)).astype(np.uint8)
+    wl.ins[:] = rng.integers(10, 50, size=len(wl.ins)).astype(np.uint8)
+    wl.dels[:] = rng.integers(10, 50, size=len(wl.dels)).astype(np.uint8)
+    mapq = rng.integers(10, 70, size=wl.n_reads)
+    dragstr = None
+    if kind == "dragstr":
+        with open(os.path.join(os.path.dirname(__file__), "golden", "dragstr_cases.json")) as f:
+            t = json.load(f)["example_params"]
+        dragstr = (np.array(t["gop"]), np.array(t["gcp"]))
+    prepared = _oracle_prepared(wl, mapq, dragstr)
+    ref = O.pd_compute_workload(prepared, pd)
+    assert np.abs(engine64.pd_compute_raw(wl, pd, mapq, dragstr=dragstr) - ref).max() <= 1e-9
+    assert np.abs(engine.pd_compute_raw(wl, pd, mapq, dragstr=dragstr) - ref).max() <= 1e-3
+    with engine.pd_raw_batch(wl, pd, mapq, dragstr=dragstr) as b:
+        _, q, i, d, g = b.read_planes()
+    assert np.array_equal(q, prepared.quals) and np.array_equal(i, prepared.ins)
+    assert np.array_equal(d, prepared.dels) and np.array_equal(g, prepared.gcp)
