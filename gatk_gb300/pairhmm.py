@@ -52,7 +52,7 @@ def _u8(x) -> np.ndarray:
 
 def _read_prep(threshold, cap_to_mapq, pcr_rate_factor, gcp, dragstr, keep_with) -> native.ReadPrep:
     """ghmm_read_prep; dragstr = (gop, gcp) tables [max_period][max_repeats] (DragstrParams) or None.  The tables are
-    kept alive on keep_with (a Workload) for as long as the library may read them."""
+    kept alive on keep_with (a Workload, or a list) for as long as the library may read them."""
     d = None
     if dragstr is not None:
         gop_t = np.ascontiguousarray(dragstr[0], dtype=np.float64)
@@ -60,7 +60,7 @@ def _read_prep(threshold, cap_to_mapq, pcr_rate_factor, gcp, dragstr, keep_with)
         if gop_t.ndim != 2 or gop_t.shape != gcp_t.shape:
             raise ValueError("DRAGstr gop and gcp tables must both be [max_period][max_repeats]")
         d = native.Dragstr(gop_t.shape[0], gop_t.shape[1], gop_t.ctypes.data, gcp_t.ctypes.data)
-        keep_with._keep.append((gop_t, gcp_t, d))
+        (keep_with if isinstance(keep_with, list) else keep_with._keep).append((gop_t, gcp_t, d))
     return native.ReadPrep(int(threshold), int(cap_to_mapq), float(pcr_rate_factor), int(gcp), 0,
                            ctypes.addressof(d) if d is not None else None)
 
@@ -89,6 +89,21 @@ class _Context:
             self.close()
         except Exception:
             pass
+
+
+@dataclass(frozen=True)
+class StandardPairHMMInputScoreImputator:
+    """StandardPairHMMInputScoreImputator.newInstance(gcp): insertion / deletion GOP from the read's BI / BD tags (45
+    without them), a constant gap continuation penalty (HC/StandardPairHMMInputScoreImputator.java:55-74)."""
+    gcp: int = 10
+
+
+@dataclass(frozen=True)
+class DragstrPairHMMInputScoreImputator:
+    """DragstrPairHMMInputScoreImputator.of(DragstrParams): GOP and GCP tables [period - 1][repeats - 1]
+    (HC/DragstrPairHMMInputScoreImputator.java:45-88)."""
+    gop: np.ndarray
+    gcp: np.ndarray
 
 
 class CudaLoglessPairHMM:
@@ -134,6 +149,47 @@ class CudaLoglessPairHMM:
         native.check(rc, self._ctx.h)
         self._last = out
         return out
+
+    def compute_log10_likelihoods_raw(self, reads: Iterable[Sequence], imputator=None, base_quality_threshold: int = 18,
+                                      cap_to_mapq: bool = True, pcr_rate_factor: float = 3.0) -> np.ndarray | None:
+        """The same step from unprocessed reads, as PairHMMLikelihoodCalculationEngine.computeReadLikelihoods runs it:
+        each read is (bases, base qualities, BI tag or None, BD tag or None, mapping quality); modifyReadQualities
+        (MAPQ cap, threshold, PCR indel model) and the imputator's penalties are applied on the device
+        (ghmm_compute_regions_raw).  imputator: StandardPairHMMInputScoreImputator (default, GCP 10) or
+        DragstrPairHMMInputScoreImputator."""
+        reads = list(reads)
+        if not reads:
+            return None
+        imputator = imputator or StandardPairHMMInputScoreImputator()
+        keep = []
+        rr = (native.RawRead * len(reads))()
+        for i, (b, q, ins, dl, mq) in enumerate(reads):
+            b, q = _u8(b), _u8(q)
+            ins = None if ins is None else _u8(ins)
+            dl = None if dl is None else _u8(dl)
+            if len(q) != len(b) or (ins is not None and len(ins) != len(b)) or (dl is not None and len(dl) != len(b)):
+                raise ValueError("each read's quality arrays must match its bases in length")
+            keep.append((b, q, ins, dl))
+            rr[i] = native.RawRead(b.ctypes.data, q.ctypes.data, ins.ctypes.data if ins is not None else None,
+                                   dl.ctypes.data if dl is not None else None, len(b), int(mq))
+        nh = len(self._haps)
+        hs = (native.Hap * max(nh, 1))()
+        for i, h in enumerate(self._haps):
+            hs[i] = native.Hap(h.ctypes.data_as(native._u8p), len(h))
+        region = native.RawRegion(ctypes.addressof(rr), len(reads), ctypes.addressof(hs), nh)
+        if isinstance(imputator, DragstrPairHMMInputScoreImputator):
+            prep = _read_prep(base_quality_threshold, cap_to_mapq, pcr_rate_factor, 10, (imputator.gop, imputator.gcp),
+                              keep)
+        else:
+            prep = _read_prep(base_quality_threshold, cap_to_mapq, pcr_rate_factor, imputator.gcp, None, keep)
+        out = np.empty(max(len(reads) * nh, 1), dtype=np.float64)
+        rc = self._ctx.L.ghmm_compute_regions_raw(self._ctx.h, ctypes.byref(region), 1, ctypes.byref(prep),
+                                                  out.ctypes.data_as(native._f64p))
+        if rc == native.GHMM_ERR_ARG:
+            raise ValueError(native.last_error(self._ctx.h))
+        native.check(rc, self._ctx.h)
+        self._last = out[:len(reads) * nh]
+        return self._last
 
     def get_log_likelihood_array(self) -> np.ndarray | None:
         return self._last

@@ -391,3 +391,29 @@ def test_raw_queue_rejects_bad_reads_at_push(engine):
     finally:
         q.close()
     assert np.array_equal(got, engine.compute_raw(wl, mapq))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["standard", "dragstr"])
+def test_mirror_computes_from_raw_reads_with_an_imputator(kind):
+    # CudaLoglessPairHMM.compute_log10_likelihoods_raw (computeLog10Likelihoods with an input score imputator) on one
+    # region's raw reads, against the prepared-planes call on the restatement's planes
+    from gatk_gb300.pairhmm import (CudaLoglessPairHMM, DragstrPairHMMInputScoreImputator, PairHMMNativeArguments,
+                                    StandardPairHMMInputScoreImputator)
+
+    wl, mapq = _dragstr_workload(31, regions=1)
+    imp = DragstrPairHMMInputScoreImputator(*EXAMPLE) if kind == "dragstr" else StandardPairHMMInputScoreImputator(10)
+    dragstr = EXAMPLE if kind == "dragstr" else None
+    prepared = _prepared_workload(wl, mapq, True, 3.0, dragstr=dragstr)
+    reads_raw, reads_prep = [], []
+    for r in range(wl.n_reads):
+        a, b = int(wl.read_off[r]), int(wl.read_off[r + 1])
+        reads_raw.append((wl.bases[a:b], wl.quals[a:b], wl.ins[a:b], wl.dels[a:b], int(mapq[r])))
+        reads_prep.append((wl.bases[a:b], prepared.quals[a:b], prepared.ins[a:b], prepared.dels[a:b],
+                           prepared.gcp[a:b]))
+    haps = [wl.hap_bases[int(wl.hap_off[h]):int(wl.hap_off[h + 1])] for h in range(wl.n_haps)]
+    with CudaLoglessPairHMM(PairHMMNativeArguments(0, True)) as hmm:
+        hmm.initialize(haps)
+        got = hmm.compute_log10_likelihoods_raw(reads_raw, imp).copy()
+        want = hmm.compute_log10_likelihoods(reads_prep)
+    assert np.abs(got - want).max() <= 1e-9
