@@ -160,10 +160,10 @@ def run_reference(args):
 
 
 def workload_config(args, wl):
-    names = {0: "config0: 1 region, 8 haps x 64 reads, seed 0",
-             1: "config1: 10,000 active regions, seed 1 (haps U[2,32] of U[200,600] bp, "
+    names = {0: "workload 0: 1 region, 8 haps x 64 reads, seed 0",
+             1: "workload 1: 10,000 active regions, seed 1 (haps U[2,32] of U[200,600] bp, "
                 "reads lognormal(4,1) of U[100,250] bp)",
-             2: "config2: 2,000 long-pair regions, seed 2", 4: "config4 body: config1 distributions, seed 4"}
+             2: "workload 2: 2,000 long-pair regions, seed 2", 4: "workload 4 body: workload 1 distributions, seed 4"}
     return {"workload": names.get(args.workload, f"workload {args.workload}"), "regions": wl.n_regions,
             "pairs": wl.n_pairs, "cells": int(wl.cells_per_region().sum()),
             "l2": f"inputs larger than L2 ({(wl.bases.nbytes * 5 + wl.hap_bases.nbytes) / 1e6:.0f} MB of read and "
@@ -448,7 +448,7 @@ def run_stream(args):
         "metric": METRIC, "value": gcups, "unit": "GCUPS", "n_gpus": world, "steps": 1, "warmup": args.warmup,
         "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (deterministic generator; seeded stand-in for a HaplotypeCaller region stream)",
-        "config": {"workload": (("config4: 100,000 regions of config1's distributions with a 5% tail of "
+        "config": {"workload": (("workload 4: 100,000 regions of workload 1's distributions with a 5% tail of "
                                  "2,000 reads x 64 haplotypes, seed 4, streamed one region per push")
                                 if args.workload == 4 else f"workload {args.workload}, streamed one region per push")
                    + (f"; raw reads prepared on the device ({args.raw} imputation, seeded MAPQ 20-69)"
@@ -563,7 +563,7 @@ def run_calib(args):
         "metric": "PairHMM calibration: FP32 forward + hand-written backward, GCUPS", "value": cells / dt_fb / 1e9,
         "unit": "GCUPS", "n_gpus": 1, "steps": reps, "warmup": args.warmup, "ms_per_step": dt_fb * 1e3,
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (workload 3: STR regions, seed 3)",
-        "config": {"workload": "config3: 4,096 read x haplotype pairs, 150 bp reads, 300 bp STR haplotypes",
+        "config": {"workload": "workload 3: 4,096 read x haplotype pairs, 150 bp reads, 300 bp STR haplotypes",
                    "pairs": cs.n_pairs, "cells": cells, "parameters": "8 x 20 x 2 (period, repeat) log10 table"},
         "forward_gcups": cells / dt_f / 1e9, "forward_ms": dt_f * 1e3,
         "gradient_vs_fp64_central_differences": {"max_rel": float(fd_rel), "params": int(len(order) * 2), "step": h,
@@ -645,7 +645,7 @@ def run_pd(args):
         "unit": "GCUPS", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "dtype": "f32",
         "data": "synthetic (workload 1 regions with seeded PD flags)",
-        "config": {"workload": f"first {n_regions} regions of config1 with 1-3 undetermined SNPs and 0-2 undetermined "
+        "config": {"workload": f"first {n_regions} regions of workload 1 with 1-3 undetermined SNPs and 0-2 undetermined "
                                "deletions per haplotype", "regions": n_regions, "pairs": wl.n_pairs, "cells": cells,
                    "mode": "GHMM_MODE_PD_FP32 (FP32 PD kernel, FP64 reruns of underflows)"},
         "roofline": {"bound": "fp32_fma_pipe", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
@@ -813,7 +813,7 @@ def run_prep(args):
         "metric": f"reads prepared per second ({mode} imputation) on 1 GB300", "value": wl.n_reads / (ms_prep * 1e-3),
         "unit": "reads/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_prep,
         "higher_is_better": True, "dtype": "u8", "data": "synthetic (workload 1 reads with seeded raw qualities)",
-        "config": {"workload": f"every read of config1 ({wl.n_regions} regions, {wl.n_reads} reads, {bases} bases), "
+        "config": {"workload": f"every read of workload 1 ({wl.n_regions} regions, {wl.n_reads} reads, {bases} bases), "
                                f"{mode} imputation" + (" with the reference's example DRAGstr model (8 x 20)"
                                                        if mode == "dragstr" else ", CONSERVATIVE PCR model"),
                    "reads": wl.n_reads, "bases": bases},
