@@ -208,44 +208,57 @@ __global__ void __launch_bounds__(kPdBlock, (sizeof(V) == 4 && K <= 4) ? 4 : 3) 
                 const bool yn = (y == 'N');
                 // the general path only when a lane of this warp sits at an AFTER_DEL or DEL_END column
                 const bool special = __any_sync(kFull, valid && (st1 == 2u || st2 == 2u || del_end));
-                // pass 1 (bottom-up, the row above still holds the previous column): branches, M, D
+                // pass 1 (bottom-up, the row above still holds the previous column): branches, M, D.  PLAIN: every
+                // lane's column is NORMAL for all its rows (no deletion state, the common case), so the branch
+                // states just take the previous column's values
+                auto pass1 = [&](auto plain_tag) {
+                    constexpr bool PLAIN = decltype(plain_tag)::value;
 #pragma unroll
-                for (int k = K - 1; k >= 0; --k) {
-                    const V dM = k ? Mp[k - 1] : gM, dI = k ? Ip[k - 1] : gI, dD = k ? Dp[k - 1] : gD;
-                    const uint32_t sk = first[k] ? st1 : st2;
-                    const bool match = rbase[k] == y || rbase[k] == 'N' || yn || ((f & 1u) && (f & rbit[k]));
-                    const V cMM = match ? mMM[k] : eMM[k], cIM = match ? mIM[k] : eIM[k];
-                    V Mn, Dn, nbM, nbI, nbD;
-                    if (!special) {
-                        const bool inside = sk == 1u;
-                        nbM = inside ? bM[k] : Mp[k];
-                        nbI = inside ? bI[k] : Ip[k];
-                        nbD = inside ? bD[k] : Dp[k];
-                        Mn = vfma(dM, cMM, vfma(dI, cIM, dD * cIM));
-                        Dn = vfma(Dp[k], tii[k], Mp[k] * tmd[k]);
-                    } else {
-                        const V dbM = k ? bM[k - 1] : gbM, dbI = k ? bI[k - 1] : gbI, dbD = k ? bD[k - 1] : gbD;
-                        if (sk == 2u) {
-                            nbM = vmax(bM[k], Mp[k]);
-                            nbI = vmax(bI[k], Ip[k]);
-                            nbD = vmax(bD[k], Dp[k]);
-                            Mn = vfma(vmax(dbM, dM), cMM, vfma(vmax(dbI, dI), cIM, vmax(dbD, dD) * cIM));
-                            Dn = vfma(vmax(bD[k], Dp[k]), tii[k], vmax(bM[k], Mp[k]) * tmd[k]);
+                    for (int k = K - 1; k >= 0; --k) {
+                        const V dM = k ? Mp[k - 1] : gM, dI = k ? Ip[k - 1] : gI, dD = k ? Dp[k - 1] : gD;
+                        const bool match = rbase[k] == y || rbase[k] == 'N' || yn || ((f & 1u) && (f & rbit[k]));
+                        const V cMM = match ? mMM[k] : eMM[k], cIM = match ? mIM[k] : eIM[k];
+                        V Mn, Dn, nbM, nbI, nbD;
+                        if (PLAIN) {
+                            nbM = Mp[k];
+                            nbI = Ip[k];
+                            nbD = Dp[k];
+                            Mn = vfma(dM, cMM, vfma(dI, cIM, dD * cIM));
+                            Dn = vfma(Dp[k], tii[k], Mp[k] * tmd[k]);
                         } else {
-                            const bool inside = sk == 1u;
-                            nbM = inside ? bM[k] : Mp[k];
-                            nbI = inside ? bI[k] : Ip[k];
-                            nbD = inside ? bD[k] : Dp[k];
-                            Mn = fma(dM, cMM, fma(dI, cIM, dD * cIM));
-                            Dn = fma(Dp[k], tii[k], Mp[k] * tmd[k]);
+                            const uint32_t sk = first[k] ? st1 : st2;
+                            if (special && sk == 2u) {
+                                const V dbM = k ? bM[k - 1] : gbM, dbI = k ? bI[k - 1] : gbI;
+                                const V dbD = k ? bD[k - 1] : gbD;
+                                nbM = vmax(bM[k], Mp[k]);
+                                nbI = vmax(bI[k], Ip[k]);
+                                nbD = vmax(bD[k], Dp[k]);
+                                Mn = vfma(vmax(dbM, dM), cMM, vfma(vmax(dbI, dI), cIM, vmax(dbD, dD) * cIM));
+                                Dn = vfma(vmax(bD[k], Dp[k]), tii[k], vmax(bM[k], Mp[k]) * tmd[k]);
+                            } else {
+                                const bool inside = sk == 1u;
+                                nbM = inside ? bM[k] : Mp[k];
+                                nbI = inside ? bI[k] : Ip[k];
+                                nbD = inside ? bD[k] : Dp[k];
+                                Mn = vfma(dM, cMM, vfma(dI, cIM, dD * cIM));
+                                Dn = vfma(Dp[k], tii[k], Mp[k] * tmd[k]);
+                            }
                         }
+                        if (CHK && !valid) Mn = Dn = 0, nbM = nbI = nbD = 0;
+                        Mp[k] = Mn;
+                        Dp[k] = Dn;
+                        bM[k] = nbM;
+                        bI[k] = nbI;
+                        bD[k] = nbD;
                     }
-                    if (CHK && !valid) Mn = Dn = 0, nbM = nbI = nbD = 0;
-                    Mp[k] = Mn;
-                    Dp[k] = Dn;
-                    bM[k] = nbM;
-                    bI[k] = nbI;
-                    bD[k] = nbD;
+                };
+                if constexpr (!CHK && F32) {  // (the FP64 kernels keep one form: registers, not issue, bind them)
+                    if (!__any_sync(kFull, st != 0u))
+                        pass1(std::true_type{});
+                    else
+                        pass1(std::false_type{});
+                } else {
+                    pass1(std::false_type{});
                 }
                 // pass 2 (top-down): I from the row above at this column
                 V aM = u[0], aI = u[1], abM = u[3], abI = u[4];
