@@ -69,6 +69,7 @@ struct DevBatch {
     const int32_t *bucket_info; // [key] first task of bucket key, [kNumBucketKeys + key] its task count
     const int64_t *n_out_dev;   // number of outputs (for the FP64 epilogue)
     int64_t rerun_capacity;
+    int64_t force_rerun_every;  // test hook (ghmm_debug_inject): every n-th output of the FP32 pass goes to FP64; 0 off
     // strip-boundary scratch of multi-strip FP32 tasks: per resident warp, max_cols float2 x 3
     float2 *scratch32;
     int64_t scratch32_cols;

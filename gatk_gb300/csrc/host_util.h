@@ -19,12 +19,17 @@ struct ghmm_batch;
 
 namespace ghmm {
 
+// Test hook (ghmm_debug_inject): the number of device allocations still to be refused as out of memory
+extern std::atomic<int64_t> g_refuse_allocations;
+
 template <typename T>
 struct DevBuf {
     T *p = nullptr;
     size_t cap = 0;
     cudaError_t reserve(size_t n) {
         if (n <= cap && p) return cudaSuccess;
+        if (g_refuse_allocations.load(std::memory_order_relaxed) > 0 && g_refuse_allocations.fetch_sub(1) > 0)
+            return cudaErrorMemoryAllocation;
         // a buffer that has to grow again grows by a quarter more than asked, so that batches of slowly
         // rising size do not free (and so synchronise the device) every time
         const size_t want = std::max<size_t>(cap ? std::max(n, cap + cap / 4) : n, 1);

@@ -145,7 +145,8 @@ constexpr float kLog2Threshold = -93.01398f;
 // as the float pair (t, la) in the output slot; finalize_fp32_kernel turns them into log10 in FP64 with every lane
 // busy, rather than one lane per warp running the FP64 log10 here on the 1/64-rate FP64 pipe.
 __device__ __forceinline__ void emit_fp32(const DevBatch &B, float t, float la, int read, int hap, int64_t out_index) {
-    if (t > 0.f && t <= FLT_MAX && log2f(t) - la >= kLog2Threshold) {
+    const bool forced = B.force_rerun_every > 0 && out_index % B.force_rerun_every == 0;  // test hook
+    if (t > 0.f && t <= FLT_MAX && log2f(t) - la >= kLog2Threshold && !forced) {
         reinterpret_cast<float2 *>(B.out)[out_index] = make_float2(t, la);
     } else {
         const int idx = atomicAdd(&B.counters[1], 1);

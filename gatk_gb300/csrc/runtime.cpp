@@ -29,6 +29,10 @@
 
 using namespace ghmm;
 
+namespace ghmm {
+std::atomic<int64_t> g_refuse_allocations{0};
+}
+
 namespace {
 
 std::mutex g_init_error_mu;
@@ -161,6 +165,7 @@ struct ghmm_batch {
 };
 
 struct ghmm_ctx {
+    int64_t debug_force_rerun = 0;  // test hook: every n-th FP32 output rerun in FP64 (batches uploaded afterwards)
     int device = 0;
     int sm_count = 0;
     int max_threads = 0;
@@ -656,6 +661,7 @@ static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
     d.bucket_info = b.d_counters.p + kNumCounters;
     d.n_out_dev = b.d_nout.p;
     d.rerun_capacity = capacity;
+    d.force_rerun_every = ctx->debug_force_rerun;
     d.scratch32 = b.d_scratch32.p;
     d.scratch32_cols = b.scratch32_cols;
     d.scratch64 = b.d_scratch64.p;
@@ -1690,6 +1696,9 @@ void ghmm::set_global_error(const char *msg) {
 extern "C" {
 
 int ghmm_load(void) {
+    // test hook: report the hardware as unsupported, as a caller's fallback chain sees it on a machine without one
+    const char *unsupported = getenv("GHMM_REPORT_UNSUPPORTED");
+    if (unsupported && unsupported[0] && strcmp(unsupported, "0") != 0) return 0;
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return 0;
     for (int d = 0; d < n; d++) {
@@ -1697,6 +1706,16 @@ int ghmm_load(void) {
         if (cudaGetDeviceProperties(&p, d) == cudaSuccess && p.major == 10 && p.minor == 3) return 1;
     }
     return 0;
+}
+
+int ghmm_debug_inject(ghmm_ctx *ctx, int32_t kind, int64_t arg) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (arg < 0) return fail(ctx, GHMM_ERR_ARG, "negative injection argument");
+    switch (kind) {
+        case GHMM_INJECT_REFUSE_ALLOCATIONS: ghmm::g_refuse_allocations.store(arg); return GHMM_OK;
+        case GHMM_INJECT_FP64_RERUN_EVERY: ctx->debug_force_rerun = arg; return GHMM_OK;
+        default: return fail(ctx, GHMM_ERR_ARG, "unknown injection");
+    }
 }
 
 int ghmm_initialize(const ghmm_args *args, ghmm_ctx **out) {

@@ -24,6 +24,8 @@ MODE_FP32_RERUN = 0
 MODE_FP64 = 1
 MODE_PD = 3
 MODE_PD_FP32 = 4
+INJECT_REFUSE_ALLOCATIONS = 1
+INJECT_FP64_RERUN_EVERY = 2
 FP64_RESCALED_FLOOR = -500.0  # GHMM_FP64_RESCALED_FLOOR
 MODE_PLAIN_FP64 = 2
 
@@ -231,6 +233,7 @@ _SIGS = {
     "ghmm_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
     "ghmm_queue_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
     "ghmm_queue_push": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),
+    "ghmm_debug_inject": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64]),
     "ghmm_queue_create_raw": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                              ctypes.POINTER(ctypes.c_void_p)]),
     "ghmm_queue_push_raw": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]),

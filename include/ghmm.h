@@ -366,6 +366,17 @@ int ghmm_queue_destroy(ghmm_queue *queue);
 int ghmm_queue_create_raw(ghmm_ctx *ctx, int64_t batch_cells, const ghmm_read_prep *prep, ghmm_queue **queue);
 int ghmm_queue_push_raw(ghmm_queue *queue, const ghmm_raw_region *regions, int32_t n_regions, double *out);
 
+/* Failure injection for tests, all on the host side (nothing faults, traps or stalls a GPU):
+ *   GHMM_INJECT_REFUSE_ALLOCATIONS: the next arg device allocations of the process fail as out of memory, so the
+ *                                   calls that need them return GHMM_ERR_NOMEM and the context stays usable;
+ *   GHMM_INJECT_FP64_RERUN_EVERY:   every arg-th output of the FP32 pass is treated as an underflow and recomputed
+ *                                   in FP64 (batches uploaded after the call; 0 turns it off).
+ * Setting the environment variable GHMM_REPORT_UNSUPPORTED (not "0") makes ghmm_load report no usable GPU, as a
+ * caller's fallback chain sees it (VectorLoglessPairHMM.java:60-79 -> HardwareFeatureException). */
+#define GHMM_INJECT_REFUSE_ALLOCATIONS 1
+#define GHMM_INJECT_FP64_RERUN_EVERY 2
+int ghmm_debug_inject(ghmm_ctx *ctx, int32_t kind, int64_t arg);
+
 /* Measured FP32 FMA-pipe peak of the device in TFLOP/s (FMA = 2 FLOP): best of a scalar FFMA and a
  * packed FFMA2 register-resident loop over all SMs, timed with CUDA events.  Also reports the FP64
  * DFMA peak.  Either output may be NULL. */
