@@ -87,7 +87,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
     if ptxas_verbose:
         print("\n".join(logs))
     tmp = LIB + ".tmp"
-    _run([nv, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *[o for _, o in jobs], "-lpthread"], verbose)
+    _run([nv, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *[o for _, o in jobs], "-lpthread", "-ldl"], verbose)
     os.replace(tmp, LIB)
     return LIB
 

@@ -12,12 +12,23 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "ghmm_internal.h"
 
 struct ghmm_ctx;
 struct ghmm_batch;
 
 namespace ghmm {
+
+// An NVTX range over a host phase (marshalling, upload, launches, planning), visible to Nsight tools; without a
+// tool attached the calls return at once
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Test hook (ghmm_debug_inject): the number of device allocations still to be refused as out of memory
 extern std::atomic<int64_t> g_refuse_allocations;

@@ -302,6 +302,7 @@ int plan_sizes(ghmm_ctx *ctx, const Source &src, ghmm_batch &b, std::vector<int6
 // -------------------------------------------------------------------------------------------------
 // Marshal inputs into the batch's pinned staging and build tasks.
 static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
+    NvtxRange range("ghmm marshal");
     const auto t_start = std::chrono::steady_clock::now();
     std::vector<int64_t> read_off, hap_off, rro, rho, oo;
     int rc = plan_sizes(ctx, src, b, read_off, hap_off, rro, rho, oo);
@@ -600,6 +601,7 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
 
 // Allocate device buffers and upload the staged batch.
 static int batch_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
+    NvtxRange range("ghmm upload");
     const int64_t NR = b.n_reads, NH = b.n_haps, G = b.n_regions;
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     GHMM_CUDA(b.d_planes.reserve((size_t)b.read_bytes * 5), "device read planes");
@@ -784,6 +786,7 @@ static int kernel_launch_count(const ghmm_batch &b, int mode) {
 // Enqueue a forward on stream s without waiting: control words, FP64 pre-queue, the kernel graph, and the
 // D2H of the counters.  batch_finish waits and reads the outcome.
 static int batch_enqueue(ghmm_ctx *ctx, ghmm_batch &b, int mode, cudaStream_t s) {
+    NvtxRange range("ghmm forward launch");
     if (!b.events_ready) {
         for (auto &e : b.ev) GHMM_CUDA(cudaEventCreate(&e), "cudaEventCreate");
         b.events_ready = true;
@@ -862,6 +865,7 @@ static int batch_enqueue(ghmm_ctx *ctx, ghmm_batch &b, int mode, cudaStream_t s)
 }
 
 static int batch_finish(ghmm_ctx *ctx, ghmm_batch &b) {
+    NvtxRange range("ghmm forward wait");
     GHMM_CUDA(cudaEventSynchronize(b.ev[4]), "forward kernels");
     float ms = 0;
     cudaEventElapsedTime(&ms, b.ev[1], b.ev[2]);
@@ -1636,6 +1640,7 @@ int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_re
 
 static int raw_prepare_device(ghmm_ctx *ctx, ghmm_batch &b, const int32_t *mapq, int32_t max_len,
                               const ghmm_read_prep *prep, cudaStream_t s) {
+    NvtxRange range("ghmm read preparation");
     const int64_t NR = b.n_reads;
     if (NR == 0) return GHMM_OK;
     GHMM_CUDA(b.h_mapq.reserve((size_t)NR), "pinned mapping qualities");

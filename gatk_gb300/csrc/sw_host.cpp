@@ -279,6 +279,7 @@ struct RunIn {
 // state | offset | n_ops | best (n each), h_starts the op starts, h_counters[0] the op total, and h_ops the ops.
 int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t plane_bytes,
         std::vector<uint8_t> *informative) {
+    NvtxRange range("ghmm Smith-Waterman");
     const int64_t n = in.n;
     cudaStream_t s = ci.stream;
     SW_CUDA(E.d_pairs.reserve((size_t)n), "device pairs");
