@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(kPdBlock, (sizeof(V) == 4 && K <= 4) ? 4 : 3) 
             // for two DFMAs)
             V mMM[K], mIM[K], eMM[K], eIM[K], tmi[K], tii[K], tmd[K];
             uint32_t rbase[K], rbit[K];
-            bool first[K], dummy[K];
+            bool first[K], dummy[K], rN[K];
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 const int p = strip * S + lane * K + k - pad;
@@ -131,6 +131,7 @@ __global__ void __launch_bounds__(kPdBlock, (sizeof(V) == 4 && K <= 4) ? 4 : 3) 
                     tmi[k] = tmd[k] = 0;
                     tii[k] = 1;
                     rbase[k] = 0x100u;
+                    rN[k] = false;
                     rbit[k] = 0u;
                 } else {
                     const uint8_t base = B.bases[roff + p], q = B.quals[roff + p];
@@ -145,6 +146,7 @@ __global__ void __launch_bounds__(kPdBlock, (sizeof(V) == 4 && K <= 4) ? 4 : 3) 
                     tii[k] = __ldg(T.err + gcp);
                     tmd[k] = __ldg(T.err + del);
                     rbase[k] = base;
+                    rN[k] = base == 'N';
                     rbit[k] = pd_base_bit(base);
                 }
             }
@@ -209,14 +211,16 @@ __global__ void __launch_bounds__(kPdBlock, (sizeof(V) == 4 && K <= 4) ? 4 : 3) 
                 // the general path only when a lane of this warp sits at an AFTER_DEL or DEL_END column
                 const bool special = __any_sync(kFull, valid && (st1 == 2u || st2 == 2u || del_end));
                 // pass 1 (bottom-up, the row above still holds the previous column): branches, M, D.  PLAIN: every
-                // lane's column is NORMAL for all its rows (no deletion state, the common case), so the branch
-                // states just take the previous column's values
+                // lane's column is NORMAL for all its rows (no deletion state) and is neither an undetermined SNP nor
+                // an N (the common case), so the branch states just take the previous column's values and a read
+                // base matches the column exactly when it equals it or is N
                 auto pass1 = [&](auto plain_tag) {
                     constexpr bool PLAIN = decltype(plain_tag)::value;
 #pragma unroll
                     for (int k = K - 1; k >= 0; --k) {
                         const V dM = k ? Mp[k - 1] : gM, dI = k ? Ip[k - 1] : gI, dD = k ? Dp[k - 1] : gD;
-                        const bool match = rbase[k] == y || rbase[k] == 'N' || yn || ((f & 1u) && (f & rbit[k]));
+                        const bool match = PLAIN ? (rbase[k] == y || rN[k])
+                                                 : (rbase[k] == y || rN[k] || yn || ((f & 1u) && (f & rbit[k])));
                         const V cMM = match ? mMM[k] : eMM[k], cIM = match ? mIM[k] : eIM[k];
                         V Mn, Dn, nbM, nbI, nbD;
                         if (PLAIN) {
@@ -253,7 +257,7 @@ __global__ void __launch_bounds__(kPdBlock, (sizeof(V) == 4 && K <= 4) ? 4 : 3) 
                     }
                 };
                 if constexpr (!CHK && F32) {  // (the FP64 kernels keep one form: registers, not issue, bind them)
-                    if (!__any_sync(kFull, st != 0u))
+                    if (!__any_sync(kFull, st != 0u || (f & 1u) || yn))
                         pass1(std::true_type{});
                     else
                         pass1(std::false_type{});
