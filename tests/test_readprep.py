@@ -306,6 +306,19 @@ def test_dragstr_fp32_path_within_tolerance(engine):
 
 
 @pytest.mark.gpu
+def test_device_dragstr_very_long_read(engine):
+    # a read whose shared-memory arrays exceed the default 48 KB a block (one warp per block, opt-in size)
+    rng = np.random.default_rng(41)
+    reads = [_str_read(rng, 12000, max_reps=8), _str_read(rng, 300)]
+    wl = _one_region(reads, [_str_read(rng, 400)], rng)
+    mapq = np.full(wl.n_reads, 60)
+    want = _prepared_workload(wl, mapq, True, 3.0, dragstr=EXAMPLE)
+    with engine.raw_batch(wl, mapq, dragstr=EXAMPLE) as b:
+        _, q, i, d, g = b.read_planes()
+    assert np.array_equal(i, want.ins) and np.array_equal(g, want.gcp) and np.array_equal(q, want.quals)
+
+
+@pytest.mark.gpu
 def test_dragstr_read_length_limit(engine):
     # the imputation holds a read in shared memory: 28000 bases at most, longer reads are refused
     rng = np.random.default_rng(2)
