@@ -1,11 +1,13 @@
-"""ctypes binding of the CPU oracle (oracle/pairhmm_oracle.c, oracle_grad.c, pdhmm_oracle.c, sw_oracle.c).
+"""ctypes binding of the CPU oracle (oracle/pairhmm_oracle.c, oracle_grad.c, pdhmm_oracle.c, sw_oracle.c,
+readprep_oracle.c).
 
 TEST INFRASTRUCTURE ONLY.  Imported by tests/, by ``__graft_entry__.smoke()`` as the
 checker, and by the cpu_baseline / ``--impl reference`` leg of bench.py.  The product
 package (gatk_gb300) never imports this module.
 
 The C sources restate GATK's LoglessPairHMM / Log10PairHMM / PairHMMModel /
-QualityUtils / MathUtils.JacobianLogTable, LoglessPDPairHMM and SmithWatermanJavaAligner;
+QualityUtils / MathUtils.JacobianLogTable, LoglessPDPairHMM, SmithWatermanJavaAligner and the read preparation
+(modifyReadQualities, the PCR indel model, the DRAGstr imputation);
 the file:line citations are in their headers.
 """
 from __future__ import annotations
@@ -28,7 +30,7 @@ _f64p = ctypes.POINTER(ctypes.c_double)
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, OpenMP, -ffp-contract=off)."""
     srcs = [os.path.join(_HERE, f) for f in ("pairhmm_oracle.c", "oracle_grad.c", "pdhmm_oracle.c", "sw_oracle.c",
-                                            "Makefile")]
+                                            "readprep_oracle.c", "Makefile")]
     if not force and os.path.exists(_LIB_PATH):
         if os.path.getmtime(_LIB_PATH) >= max(os.path.getmtime(s) for s in srcs):
             return _LIB_PATH
@@ -91,6 +93,10 @@ def lib():
         L.sw_oracle_align_batch.restype = ctypes.c_int
         L.sw_oracle_align_batch.argtypes = [ctypes.c_int64, _u8p, _i64p, _i32p, _u8p, _i64p, _i32p, _i32p, ctypes.c_int,
                                             ctypes.c_int, _u32p, _i64p, _i32p, _i32p, ctypes.c_int]
+        L.rp_prepare_reads.restype = ctypes.c_int
+        L.rp_prepare_reads.argtypes = [ctypes.c_int64, _i64p, _u8p, _u8p, _u8p, _u8p, _i32p, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_double, ctypes.c_int, _f64p, _f64p, ctypes.c_int, ctypes.c_int, _u8p,
+                                       _u8p, _u8p, _u8p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -244,3 +250,33 @@ def sw_align_pairs(ref_plane, ref_off, ref_len, alt_plane, alt_off, alt_len, par
     if st != 0:
         raise ValueError(f"sw_oracle_align_batch status {st}")
     return ops, start, n_ops, off
+
+
+def prepare_reads(read_off, bases, quals, ins, dels, mapq, threshold: int = 18, cap_to_mapq: bool = True,
+                  rate_factor: float = 0.0, gcp: int = 10, dragstr=None, threads: int = 0):
+    """readprep_oracle.c over reads laid back to back at read_off: the (quals, ins, dels, gcp) planes, as
+    oracle/readprep.py's prepare_read gives them read by read.  ins / dels None: 45 everywhere; dragstr = (gop, gcp)
+    tables [max_period][max_repeats] or None."""
+    read_off = np.ascontiguousarray(read_off, dtype=np.int64)
+    n_reads = len(read_off) - 1
+    bases, quals = _u8(bases), _u8(quals)
+    ins_a = None if ins is None else _u8(ins)
+    dels_a = None if dels is None else _u8(dels)
+    mq = np.ascontiguousarray(mapq, dtype=np.int32)
+    outs = [np.zeros(max(len(bases), 1), dtype=np.uint8) for _ in range(4)]
+    gop_t = gcp_t = None
+    maxp = maxr = 0
+    if dragstr is not None:
+        gop_t = np.ascontiguousarray(dragstr[0], dtype=np.float64)
+        gcp_t = np.ascontiguousarray(dragstr[1], dtype=np.float64)
+        maxp, maxr = gop_t.shape
+    st = lib().rp_prepare_reads(n_reads, _p(read_off, _i64p), _p(bases, _u8p), _p(quals, _u8p),
+                                _p(ins_a, _u8p) if ins_a is not None else None,
+                                _p(dels_a, _u8p) if dels_a is not None else None, _p(mq, _i32p), int(threshold),
+                                int(cap_to_mapq), float(rate_factor), int(gcp),
+                                _p(gop_t, _f64p) if gop_t is not None else None,
+                                _p(gcp_t, _f64p) if gcp_t is not None else None, int(maxp), int(maxr),
+                                *[_p(o, _u8p) for o in outs], int(threads))
+    if st != 0:
+        raise ValueError(f"rp_prepare_reads status {st}")
+    return tuple(o[:len(bases)] for o in outs)

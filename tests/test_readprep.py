@@ -430,3 +430,22 @@ def test_mirror_computes_from_raw_reads_with_an_imputator(kind):
         got = hmm.compute_log10_likelihoods_raw(reads_raw, imp).copy()
         want = hmm.compute_log10_likelihoods(reads_prep)
     assert np.abs(got - want).max() <= 1e-9
+
+
+@pytest.mark.parametrize("mode", ["pcr", "pcr_no_tags", "no_pcr", "dragstr"])
+def test_c_restatement_matches_the_python_one(mode):
+    # oracle/readprep_oracle.c (the large-sample CPU baseline) against oracle/readprep.py, read by read
+    from oracle import oracle as O
+
+    wl, mapq = _dragstr_workload(51, regions=2)
+    rng = np.random.default_rng(52)
+    wl.ins[:] = rng.integers(0, 60, size=len(wl.ins)).astype(np.uint8)
+    wl.dels[:] = rng.integers(0, 60, size=len(wl.dels)).astype(np.uint8)
+    tags = mode != "pcr_no_tags"
+    rate = 0.0 if mode == "no_pcr" else 3.0
+    dragstr = EXAMPLE if mode == "dragstr" else None
+    q, i, d, g = O.prepare_reads(wl.read_off, wl.bases, wl.quals, wl.ins if tags else None, wl.dels if tags else None,
+                                 mapq, rate_factor=rate, dragstr=dragstr)
+    want = _prepared_workload(wl, mapq, tags, rate, dragstr=dragstr)
+    assert np.array_equal(q, want.quals) and np.array_equal(i, want.ins)
+    assert np.array_equal(d, want.dels) and np.array_equal(g, want.gcp)
