@@ -521,7 +521,21 @@ def run_calib(args):
 
     reps = max(args.steps, 10)
     dt_f = timed(fwd, reps)
+    clocks = ClockSampler(0)
+    clocks.start()
     dt_fb = timed(fwd_bwd, reps)
+    clk = clocks.stop()
+
+    # e2e: the parameter table from pinned host memory to the device, forward + backward, its gradient back
+    theta_host = theta.detach().cpu().pin_memory()
+    grad_host = torch.empty_like(theta_host).pin_memory()
+
+    def fwd_bwd_host():
+        t = theta_host.to(cs.device, non_blocking=True).requires_grad_(True)
+        C.log10_likelihoods(t, cs, eng, precision=0).sum().backward()
+        grad_host.copy_(t.grad, non_blocking=True)
+
+    dt_e2e = timed(fwd_bwd_host, reps)
     # gradient checks
     t = theta.detach().requires_grad_(True)
     C.log10_likelihoods(t, cs, eng, precision=0).sum().backward()
@@ -552,13 +566,19 @@ def run_calib(args):
     gn, cn = g.detach().cpu().numpy(), c.detach().cpu().numpy()
     pr, ph = wl.pair_index()
     oracle_rel = 0.0
+    oracle_cells = 0
+    t_or = time.perf_counter()
     for p in range(0, cs.n_pairs, 128):
         r, hh = int(pr[p]), int(ph[p])
         a, b = int(wl.read_off[r]), int(wl.read_off[r + 1])
         _, dg, dc = O.cont_grad(wl.hap(hh), wl.bases[a:b], wl.quals[a:b], gn[a:b].astype(np.float64),
                                 cn[a:b].astype(np.float64))
+        oracle_cells += (b - a) * len(wl.hap(hh))
         sc = max(np.abs(dg).max(), np.abs(dc).max())
         oracle_rel = max(oracle_rel, np.abs(gg[a:b] - dg).max() / sc, np.abs(gc[a:b] - dc).max() / sc)
+    cpu_dt = time.perf_counter() - t_or
+    peaks = eng.measure_peaks()
+    peak32 = max(peaks["fp32_tflops"], peaks["fp32x2_tflops"])
     line = {
         "metric": "PairHMM calibration: FP32 forward + hand-written backward, GCUPS", "value": cells / dt_fb / 1e9,
         "unit": "GCUPS", "n_gpus": 1, "steps": reps, "warmup": args.warmup, "ms_per_step": dt_fb * 1e3,
@@ -569,6 +589,19 @@ def run_calib(args):
         "gradient_vs_fp64_central_differences": {"max_rel": float(fd_rel), "params": int(len(order) * 2), "step": h,
                                                  "budget": 1e-3},
         "gradient_vs_fp64_oracle_adjoint": {"max_rel": float(oracle_rel), "sample_pairs": len(range(0, cs.n_pairs, 128))},
+        "roofline": {"bound": "fp32_fma_pipe", "achieved": CALIB_FLOP_PER_CELL * cells / dt_fb / 1e12,
+                     "peak": peak32, "unit": "TFLOP/s", "frac": CALIB_FLOP_PER_CELL * cells / dt_fb / 1e12 / peak32,
+                     "flop_per_cell": CALIB_FLOP_PER_CELL,
+                     "kernel": "calib_kernel<float, K, true> over the whole autograd step (latency-bound at 4,096 pairs)"},
+        "e2e": {"value": cells / dt_e2e / 1e9, "unit": "GCUPS", "ms_per_step": dt_e2e * 1e3,
+                "h2d_bytes_per_step": int(theta_host.numel() * 4), "d2h_bytes_per_step": int(grad_host.numel() * 4),
+                "api": "calibration.log10_likelihoods(...).sum().backward() with the table from and the gradient to "
+                       "pinned host memory"},
+        "gpu_launches": reps,
+        "clocks": clk,
+        "cpu_baseline": {"value": oracle_cells / cpu_dt / 1e9, "unit": "GCUPS", "cores": 1, "kind": "port",
+                         "sample": f"every 128th pair ({len(range(0, cs.n_pairs, 128))} pairs, {oracle_cells:.3e} cells): "
+                                   "FP64 forward + adjoint of oracle/oracle_grad.c, one pair at a time"},
     }
     print(json.dumps(line), flush=True)
     eng.close()
@@ -851,6 +884,9 @@ def run_prep(args):
     eng.close()
     return 0
 
+
+# calibration step: forward (11), checkpointed recompute (11) and the adjoint wavefront (about twice a forward, 22)
+CALIB_FLOP_PER_CELL = 44
 
 SW_OPS_PER_CELL = 12  # calculateMatrix's inner loop: 5 adds, 6 compares / maxima, the base compare
 
