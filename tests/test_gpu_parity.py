@@ -389,3 +389,27 @@ def test_steep_insertion_penalties_route_to_the_exact_tier(engine):
     assert st["n_fp64_exact"] == 1
     assert _absdiff(got[:1], ref[:1]).max() <= TOL64
     assert _absdiff(got[1:], ref[1:]).max() <= TOL32
+
+
+@pytest.mark.gpu
+def test_exhaustive_small_shapes(engine):
+    # every read length on a grid around the 32-row lane and strip granularities against every haplotype length on
+    # a grid around the 32-column wavefront width, one region per haplotype length, in FP32 and in FP64
+    rng = np.random.default_rng(77)
+    read_lens = (1, 2, 3, 5, 8, 13, 21, 29, 30, 31, 32, 33, 34, 62, 63, 64, 65, 66, 94, 126, 254, 255, 256)
+    hap_lens = (1, 2, 3, 5, 8, 31, 32, 33, 63, 64, 65, 100)
+    regions = []
+    for H in hap_lens:
+        haps = [_rand_seq(rng, H), _rand_seq(rng, H + 1)]
+        reads = [(_rand_seq(rng, R), rng.integers(10, 41, size=R), rng.integers(20, 46, size=R),
+                  rng.integers(20, 46, size=R), np.full(R, 10)) for R in read_lens]
+        regions.append((haps, reads))
+    wl = W.from_pairs(regions)
+    ref = _oracle_all(wl)
+    got, _ = _run(engine, wl, native.MODE_FP32_RERUN)
+    under = ref < RERUN_LOG10 - 0.01
+    assert _absdiff(got[~under], ref[~under]).max() <= TOL32
+    if under.any():
+        assert _absdiff(got[under], ref[under]).max() <= TOL64
+    got64, _ = _run(engine, wl, native.MODE_FP64)
+    assert _absdiff(got64, ref).max() <= TOL64
