@@ -1159,6 +1159,29 @@ int queue_wait_all(ghmm_queue *q) {
     return q->error;
 }
 
+// Make q a queue of raw reads with the (already checked) read preparation prep (DRAGstr tables copied), or, with
+// prep NULL, a queue of prepared reads again.  Only while no batch is queued or in flight.
+void queue_set_raw(ghmm_queue *q, const ghmm_read_prep *prep, const RouteBound *bound) {
+    q->raw = prep != nullptr;
+    q->has_bound = false;
+    q->str_tables.clear();
+    if (!prep) return;
+    q->prep = *prep;
+    q->prep.dragstr = nullptr;
+    if (prep->dragstr) {
+        const ghmm_dragstr &d = *prep->dragstr;
+        const size_t cells = (size_t)d.max_period * (size_t)d.max_repeats;
+        q->str_tables.assign(d.gop, d.gop + cells);
+        q->str_tables.insert(q->str_tables.end(), d.gcp, d.gcp + cells);
+        q->dragstr = ghmm_dragstr{d.max_period, d.max_repeats, q->str_tables.data(), q->str_tables.data() + cells};
+        q->prep.dragstr = &q->dragstr;
+    }
+    if (bound) {
+        q->has_bound = true;
+        q->bound = *bound;
+    }
+}
+
 // raw_prep: NULL for a queue of prepared reads; else the (already checked) read preparation of a raw queue
 int queue_open(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **out, const ghmm_read_prep *raw_prep = nullptr,
                const RouteBound *bound = nullptr) {
@@ -1166,23 +1189,7 @@ int queue_open(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **out, const ghmm_
     q->ctx = ctx;
     q->batch_cells = batch_cells > 0 ? batch_cells : (int64_t)2e11;
     q->mode = ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN;
-    if (raw_prep) {
-        q->raw = true;
-        q->prep = *raw_prep;
-        q->prep.dragstr = nullptr;
-        if (raw_prep->dragstr) {
-            const ghmm_dragstr &d = *raw_prep->dragstr;
-            const size_t cells = (size_t)d.max_period * (size_t)d.max_repeats;
-            q->str_tables.assign(d.gop, d.gop + cells);
-            q->str_tables.insert(q->str_tables.end(), d.gcp, d.gcp + cells);
-            q->dragstr = ghmm_dragstr{d.max_period, d.max_repeats, q->str_tables.data(), q->str_tables.data() + cells};
-            q->prep.dragstr = &q->dragstr;
-        }
-        if (bound) {
-            q->has_bound = true;
-            q->bound = *bound;
-        }
-    }
+    if (raw_prep) queue_set_raw(q, raw_prep, bound);
     for (auto &st : q->stream) {
         cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
         if (e != cudaSuccess) {
@@ -1248,8 +1255,11 @@ std::unique_ptr<QueueUnit> borrowed_unit(const Source &src, int64_t g0, int64_t 
 // is small so that the GPU starts early, later ones grow to a third of the input.
 constexpr int64_t kPipelineMinCells = (int64_t)6e10;
 
+// Raw reads (mapq non-NULL, src.regions over the raw view's reads): every batch gets the read preparation prep on
+// the device after its upload.
 int pipelined_compute(ghmm_ctx *ctx, const Source &src, const std::vector<int64_t> &reg_cells,
-                      const std::vector<int64_t> &reg_out, double *out) {
+                      const std::vector<int64_t> &reg_out, double *out, const int32_t *mapq = nullptr,
+                      int32_t max_len = 0, const ghmm_read_prep *prep = nullptr, const RouteBound *bound = nullptr) {
     if (!ctx->pipe) {
         int rc = queue_open(ctx, 0, &ctx->pipe);
         if (rc) return rc;
@@ -1260,8 +1270,14 @@ int pipelined_compute(ghmm_ctx *ctx, const Source &src, const std::vector<int64_
         q->error = GHMM_OK;
         q->error_msg.clear();
         q->mode = ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN;
+        queue_set_raw(q, mapq ? prep : nullptr, bound);
     }
     const int64_t G = src.n_regions;
+    std::vector<int64_t> first_read;  // raw reads: the batch's reads' mapping qualities go with the batch
+    if (mapq) {
+        first_read.assign((size_t)G + 1, 0);
+        for (int64_t g = 0; g < G; g++) first_read[(size_t)g + 1] = first_read[(size_t)g] + src.regions[g].n_reads;
+    }
     int64_t total = 0;
     for (int64_t g = 0; g < G; g++) total += reg_cells[(size_t)g];
     int64_t target = std::max<int64_t>(total / 16, 1), g0 = 0;
@@ -1271,11 +1287,20 @@ int pipelined_compute(ghmm_ctx *ctx, const Source &src, const std::vector<int64_
         if (G - g1 < 8) {  // do not leave a sliver
             for (; g1 < G; g1++) c += reg_cells[(size_t)g1];
         }
-        queue_submit(q, borrowed_unit(src, g0, g1, out + reg_out[(size_t)g0], reg_out[(size_t)g1] - reg_out[(size_t)g0], c));
+        auto u = borrowed_unit(src, g0, g1, out + reg_out[(size_t)g0], reg_out[(size_t)g1] - reg_out[(size_t)g0], c);
+        if (mapq) {
+            u->mapq.assign(mapq + first_read[(size_t)g0], mapq + first_read[(size_t)g1]);
+            u->max_len = max_len;
+        }
+        queue_submit(q, std::move(u));
         target = std::min(target * 5 / 2, std::max<int64_t>(total / 3, 1));
         g0 = g1;
     }
     int rc = queue_wait_all(q);
+    {
+        std::lock_guard<std::mutex> lk(q->mu);
+        queue_set_raw(q, nullptr, nullptr);
+    }
     if (rc) return queue_status(q);
     return GHMM_OK;
 }
@@ -2173,6 +2198,16 @@ int ghmm_compute_regions_raw(ghmm_ctx *ctx, const ghmm_raw_region *regions, int3
     src.regions = v.regions.data();
     src.n_regions = n_regions;
     src.bound = v.has_bound ? &v.bound : nullptr;
+    {  // large inputs: the pipeline of batches, each prepared on the device after its upload
+        std::vector<int64_t> cells, outo;
+        if (!region_sizes(src, cells, outo)) return fail(ctx, GHMM_ERR_ARG, "negative count or NULL array in a region");
+        int64_t total = 0;
+        for (auto c : cells) total += c;
+        if (outo.back() > 0 && !out) return fail(ctx, GHMM_ERR_ARG, "NULL output");
+        if (total >= kPipelineMinCells && n_regions >= 4)
+            return pipelined_compute(ctx, src, cells, outo, out, v.mapq.data(), v.max_len, prep,
+                                     v.has_bound ? &v.bound : nullptr);
+    }
     ghmm_batch &b = ctx->scratch_batch;
     rc = batch_marshal(ctx, src, b);
     if (!rc) rc = batch_upload(ctx, b, ctx->stream);

@@ -449,3 +449,25 @@ def test_c_restatement_matches_the_python_one(mode):
     want = _prepared_workload(wl, mapq, tags, rate, dragstr=dragstr)
     assert np.array_equal(q, want.quals) and np.array_equal(i, want.ins)
     assert np.array_equal(d, want.dels) and np.array_equal(g, want.gcp)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["pcr", "dragstr"])
+def test_large_raw_call_is_pipelined_with_identical_results(engine, kind):
+    # ghmm_compute_regions_raw on more than 6e10 cells runs as a pipeline of batches through the context's queue, each
+    # prepared on the device after its upload; a region's results do not depend on the batching
+    wl = W.generate(1, regions=700)
+    rng = np.random.default_rng(61)
+    wl.quals[:] = rng.integers(2, 45, size=len(wl.quals)).astype(np.uint8)
+    mapq = rng.integers(10, 70, size=wl.n_reads)
+    assert wl.cells() >= 6e10
+    kw = {"dragstr": EXAMPLE} if kind == "dragstr" else {"pcr_rate_factor": 3.0}
+    got = engine.compute_raw(wl, mapq, **kw)
+    with engine.raw_batch(wl, mapq, **kw) as b:
+        b.forward()
+        want = b.results()
+    assert np.array_equal(got, want)
+    again = engine.compute(wl)  # a prepared-planes call afterwards runs the same queue without the preparation
+    with engine.batch(wl) as b:
+        b.forward()
+        assert np.array_equal(again, b.results())
