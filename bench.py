@@ -203,7 +203,7 @@ def run_ours(args):
     eng = Engine(device=device)
     peaks = eng.measure_peaks()
     # weak scaling: every rank owns its own block of regions of the same distribution
-    n_regions = args.regions or int(native.lib().ghmm_synth_default_regions(args.workload))
+    n_regions = args.regions or int(native.synth_lib().ghmm_synth_default_regions(args.workload))
     g0, g1 = sharding.block_range(n_regions, rank)
     wl = W.generate(args.workload, regions=g1 - g0, region_begin=g0)
     cells = int(wl.cells_per_region().sum())
@@ -253,7 +253,7 @@ def run_ours(args):
         barrier()
         torch.cuda.synchronize(device)
         t0 = time.perf_counter()
-        e2e_steps = max(1, min(args.steps, 3))
+        e2e_steps = args.steps  # as many calls as the device-resident value times
         for _ in range(e2e_steps):
             native.check(L.ghmm_compute_regions(eng.handle, regs, wl.n_regions, out.ctypes.data_as(native._f64p)),
                          eng.handle)
@@ -262,10 +262,24 @@ def run_ours(args):
         barrier()
         dt = max_over_ranks(dt)
         same = bool(np.array_equal(out, results))
-        e2e = {"value": total_cells / dt / 1e9, "unit": "GCUPS", "ms_per_step": dt * 1e3,
+        e2e = {"value": total_cells / dt / 1e9, "unit": "GCUPS", "ms_per_step": dt * 1e3, "steps": e2e_steps,
                "h2d_bytes_per_step": int(io["h2d_bytes"]), "d2h_bytes_per_step": int(io["d2h_bytes"]),
                "api": "ghmm_compute_regions (per-read pointer arrays, as the JNI binding passes them)",
                "matches_device_resident_results": same}
+
+    # ---- the whole workload against the GPU's FP64 mode (every pair in FP64, pinned to the oracle at 1e-9) ----
+    full_fp64 = None
+    if not args.no_full_check:
+        batch.forward(native.MODE_FP64)
+        st64 = batch.stats()
+        res64 = batch.results()
+        dd = absdiff(results, res64)
+        full_fp64 = {"pairs": int(len(dd)), "max_abs_dlog10": float(dd.max()), "median_abs_dlog10": float(np.median(dd)),
+                     "pairs_above_1e-3": int((dd > 1e-3).sum()), "pairs_above_1e-5": int((dd > 1e-5).sum()),
+                     "fp64_mode_ms": st64["ms_total"], "fp64_mode_gcups": cells / (st64["ms_total"] * 1e-3) / 1e9,
+                     "budget": 1e-3,
+                     "what": "every FP32 + FP64-rerun result of the timed forward against the same batch in "
+                             "GHMM_MODE_FP64 (all pairs in the FP64 kernel)"}
 
     if rank != 0:
         batch.close()
@@ -277,20 +291,51 @@ def run_ours(args):
     # ---- accuracy and CPU baseline on the deterministic sample ----
     from oracle import oracle as O
 
-    n_cpu, cpu_cells = cpu_sample(wl, args.cpu_cells)
-    sub = wl.subset(0, n_cpu)
-    t0 = time.perf_counter()
-    ref = O.compute_workload(sub, threads=0)
-    cpu_dt = time.perf_counter() - t0
-    got = results[:sub.n_pairs]
+    # the sample: leading and trailing regions of the timed workload, half the CPU cells each
+    head_n, head_cells = cpu_sample(wl, args.cpu_cells / 2)
+    cpr = wl.cells_per_region()
+    tail_n = int(np.searchsorted(np.cumsum(cpr[::-1]), args.cpu_cells / 2)) + 1
+    tail_n = max(0, min(tail_n, wl.n_regions - head_n))
+    spans = [(0, head_n)] + ([(wl.n_regions - tail_n, wl.n_regions)] if tail_n else [])
+    # plus the regions holding the lowest results of the timed forward: the exact FP64 tier's pairs (log10 L < -500,
+    # and -Infinity where the reference's 2^1020 scale underflows too), when the workload has any
+    region_of_out = np.repeat(np.arange(wl.n_regions), np.diff(wl.out_off))
+    extra = []
+    for mask in (np.isneginf(results), results < native.FP64_RESCALED_FLOOR):
+        idx = np.nonzero(mask)[0]
+        if len(idx):
+            g = int(region_of_out[idx[np.argmin(results[idx]) if not np.isneginf(results[idx]).all() else 0]])
+            if not any(a <= g < b for a, b in spans) and g not in extra:
+                extra.append(g)
+    spans += [(g, g + 1) for g in extra]
+    refs, gots, cpu_dt, cpu_cells, sample_pairs = [], [], 0.0, 0, 0
+    for g0, g1 in spans:
+        sub = wl.subset(g0, g1)
+        t0 = time.perf_counter()
+        refs.append(O.compute_workload(sub, threads=0))
+        cpu_dt += time.perf_counter() - t0
+        gots.append(results[int(wl.out_off[g0]):int(wl.out_off[g1])])
+        cpu_cells += int(cpr[g0:g1].sum())
+        sample_pairs += sub.n_pairs
+    ref, got = np.concatenate(refs), np.concatenate(gots)
     d = absdiff(got, ref)
     under = ref < -64.2
-    accuracy = {"sample_pairs": int(sub.n_pairs), "max_abs_dlog10": float(d.max()),
+    accuracy = {"sample_pairs": int(sample_pairs), "max_abs_dlog10": float(d.max()),
                 "median_abs_dlog10": float(np.median(d)),
+                "regions": f"{head_n} leading and {tail_n} trailing regions of {wl.n_regions}"
+                           + (f", and regions {extra} (the timed forward's lowest results)" if extra else ""),
                 "fp64_rerun_pairs_in_sample": int(under.sum()),
-                "max_abs_dlog10_fp64_reruns": float(d[under].max()) if under.any() else None}
+                "max_abs_dlog10_fp64_reruns": float(d[under].max()) if under.any() else None,
+                "exact_tier_pairs_in_sample": int((ref < native.FP64_RESCALED_FLOOR).sum()),
+                "max_abs_dlog10_exact_tier": (float(d[ref < native.FP64_RESCALED_FLOOR].max())
+                                              if (ref < native.FP64_RESCALED_FLOOR).any() else None),
+                "neg_inf_pairs_in_sample": int(np.isneginf(ref).sum())}
+    if full_fp64 is not None:
+        d64 = absdiff(np.concatenate([res64[int(wl.out_off[g0]):int(wl.out_off[g1])] for g0, g1 in spans]), ref)
+        full_fp64["fp64_mode_vs_oracle_on_sample_max_abs_dlog10"] = float(d64.max())
     cpu_baseline = {"value": cpu_cells / cpu_dt / 1e9, "unit": "GCUPS", "cores": O.num_threads(), "kind": "port",
-                    "sample": f"first {n_cpu} regions of the timed workload ({cpu_cells:.3e} cells, {sub.n_pairs} pairs)",
+                    "sample": f"first {head_n} and last {tail_n} regions of the timed workload ({cpu_cells:.3e} cells, "
+                              f"{sample_pairs} pairs)",
                     "host": f"{platform.machine()} x{os.cpu_count()}"}
 
     # ---- plain FP64 kernel, one pair per block, one launch per region ----
@@ -304,10 +349,13 @@ def run_ours(args):
     plain_vs_ours = float(absdiff(plain_res, results[:len(plain_res)]).max())
 
     # ---- roofline of the dominant kernel: the FP32 bucket launches of one forward ----
-    direct_cells = 0  # pairs sent straight to FP64 (none in the synthetic workloads)
+    direct_cells = int(st["n_cells_fp64_direct"])  # pairs routed straight to FP64 (none on workload 1)
     fp32_cells = cells - direct_cells
     achieved = FLOP_PER_CELL * fp32_cells / (ms_fp32 * 1e-3) / 1e12
     peak = max(peaks["fp32_tflops"], peaks["fp32x2_tflops"])
+    # the same peak from the clock: SMs x 128 FP32 lanes x 2 FLOP per FMA x the median SM clock of the timed region
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    clock_peak = sms * 128 * 2 * clk["sm_mhz"] * 1e6 / 1e12 if clk.get("sm_mhz") else None
     traffic = read_profile_traffic()
     line = {
         "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
@@ -317,22 +365,31 @@ def run_ours(args):
         "config": workload_config(args, wl),
         "roofline": {"bound": "fp32_fma_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
+                     "traffic_source": "profiles (scaled): ncu dram bytes of a 2,000-region capture of the same "
+                                       "kernels, scaled by cells to the full launch set",
                      "kernel": "fp32_bucket_kernel (all rows-per-lane buckets of one forward)",
                      "flop_per_cell": FLOP_PER_CELL, "cells_per_launch_set": fp32_cells,
                      "ms_per_launch_set": ms_fp32,
                      "peak_source": ("measured in this run: FFMA and FFMA2 register loops over all SMs "
                                      f"({peaks['fp32_tflops']:.1f} / {peaks['fp32x2_tflops']:.1f} TFLOP/s); "
-                                     "MEASURED_PEAKS.json carries no FP32 figure")},
+                                     "MEASURED_PEAKS.json carries no FP32 figure"),
+                     "peak_from_clock": clock_peak,
+                     "frac_vs_peak_from_clock": achieved / clock_peak if clock_peak else None,
+                     "peak_from_clock_source": f"{sms} SMs x 128 FP32 lanes x 2 FLOP x median SM clock of the timed "
+                                               "region"},
         "cpu_baseline": cpu_baseline,
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk,
-        "fp64_rerun": {"pairs": int(st["n_rerun"]), "fraction": rerun_frac, "ms": ms_fp64},
+        "fp64_rerun": {"pairs": int(st["n_rerun"]), "fraction": rerun_frac, "ms": ms_fp64,
+                       "direct_pairs": int(st["n_fp64_direct"]), "direct_cells": direct_cells,
+                       "exact_tier_pairs": int(st["n_fp64_exact"])},
         "tuning": tuning,
         "plain_fp64": {"value": plain_gcups, "unit": "GCUPS", "regions": n_pl, "cells": pl_cells,
                        "launches": int(pst["n_launches"]), "speedup_batched_vs_plain": value / world / plain_gcups,
                        "max_abs_diff_vs_batched": plain_vs_ours},
         "accuracy_vs_fp64_oracle": accuracy,
+        "accuracy_vs_gpu_fp64_full_workload": full_fp64,
         "peaks_measured": peaks,
     }
     print(json.dumps(line), flush=True)
@@ -365,7 +422,7 @@ def run_stream(args):
         dist = None
     eng = Engine(device=local)
     peaks = eng.measure_peaks()
-    n_regions = args.regions or int(native.lib().ghmm_synth_default_regions(args.workload))
+    n_regions = args.regions or int(native.synth_lib().ghmm_synth_default_regions(args.workload))
     g0, g1 = sharding.block_range(n_regions, rank)
     blocks = []  # (workload, region struct addresses, output array, output addresses, mapping qualities)
     t_gen = time.perf_counter()
@@ -441,6 +498,21 @@ def run_stream(args):
     ref = O.compute_workload(sub, threads=0)
     cpu_dt = time.perf_counter() - t1
     d = absdiff(out0[:sub.n_pairs], ref)
+    # the high-depth tail (2,000 reads x 64 haplotypes): the first two such regions of the stream, checked apart
+    tail = None
+    if args.workload == 4 and not args.raw:
+        nr, nh = np.diff(wl0.region_read_off), np.diff(wl0.region_hap_off)
+        tail_regions = [int(g) for g in np.nonzero((nr == 2000) & (nh == 64))[0][:2]]
+        if tail_regions:
+            dts = []
+            for g in tail_regions:
+                tsub = wl0.subset(g, g + 1)
+                tref = O.compute_workload(tsub, threads=0)
+                dts.append(absdiff(out0[int(wl0.out_off[g]):int(wl0.out_off[g + 1])], tref))
+            dt_all = np.concatenate(dts)
+            tail = {"regions": tail_regions, "pairs": int(len(dt_all)),
+                    "cells": int(wl0.cells_per_region()[tail_regions].sum()),
+                    "max_abs_dlog10": float(dt_all.max()), "median_abs_dlog10": float(np.median(dt_all))}
     fp32_cells = cells - info["n_cells_fp64_direct"]
     achieved = FLOP_PER_CELL * fp32_cells / dt / 1e12
     peak = max(peaks["fp32_tflops"], peaks["fp32x2_tflops"])
@@ -474,7 +546,9 @@ def run_stream(args):
                          "sample": f"first {n_cpu} regions of the stream ({cpu_cells:.3e} cells, {sub.n_pairs} pairs)",
                          "host": f"{platform.machine()} x{os.cpu_count()}"},
         "accuracy_vs_fp64_oracle": {"sample_pairs": int(sub.n_pairs), "max_abs_dlog10": float(d.max()),
-                                    "median_abs_dlog10": float(np.median(d))},
+                                    "median_abs_dlog10": float(np.median(d)),
+                                    "sample": f"first {n_cpu} regions of the stream"},
+        "accuracy_vs_fp64_oracle_high_depth_tail": tail,
         "peaks_measured": peaks,
     }
     print(json.dumps(line), flush=True)
@@ -541,10 +615,12 @@ def run_calib(args):
     C.log10_likelihoods(t, cs, eng, precision=0).sum().backward()
     grad = t.grad.detach().cpu().numpy().reshape(-1, 2)
     used = np.bincount(cs.param_index_np[cs.param_index_np >= 0], minlength=160)
-    order = np.argsort(-used)[:8]
+    order = np.nonzero(used)[0]  # every entry some read position uses
+    unused_nonzero = int((grad[used == 0] != 0).sum())  # must be 0: unused entries get no gradient
     h = 1e-4
     scale = np.abs(grad).max()
     fd_rel = 0.0
+    t_fd = time.perf_counter()
     with torch.no_grad():
         for k in order:
             for comp in (0, 1):
@@ -556,7 +632,8 @@ def run_calib(args):
                 step = float(tp.view(-1, 2)[k, comp].double() - tm.view(-1, 2)[k, comp].double())
                 fd = (sp - sm) / step
                 fd_rel = max(fd_rel, abs(grad[k, comp] - fd) / max(abs(fd), 1e-2 * scale))
-    # per-position gradients against the FP64 oracle's adjoint on a sample of pairs
+    fd_s = time.perf_counter() - t_fd
+    # per-position gradients against the FP64 oracle's adjoint on every pair
     g, c = cs.position_params(theta)
     g = g.detach().requires_grad_(True)
     c = c.detach().requires_grad_(True)
@@ -568,7 +645,7 @@ def run_calib(args):
     oracle_rel = 0.0
     oracle_cells = 0
     t_or = time.perf_counter()
-    for p in range(0, cs.n_pairs, 128):
+    for p in range(cs.n_pairs):
         r, hh = int(pr[p]), int(ph[p])
         a, b = int(wl.read_off[r]), int(wl.read_off[r + 1])
         _, dg, dc = O.cont_grad(wl.hap(hh), wl.bases[a:b], wl.quals[a:b], gn[a:b].astype(np.float64),
@@ -587,8 +664,12 @@ def run_calib(args):
                    "pairs": cs.n_pairs, "cells": cells, "parameters": "8 x 20 x 2 (period, repeat) log10 table"},
         "forward_gcups": cells / dt_f / 1e9, "forward_ms": dt_f * 1e3,
         "gradient_vs_fp64_central_differences": {"max_rel": float(fd_rel), "params": int(len(order) * 2), "step": h,
-                                                 "budget": 1e-3},
-        "gradient_vs_fp64_oracle_adjoint": {"max_rel": float(oracle_rel), "sample_pairs": len(range(0, cs.n_pairs, 128))},
+                                                 "budget": 1e-3, "used_entries": int(len(order)),
+                                                 "unused_entries": int((used == 0).sum()),
+                                                 "unused_entries_with_nonzero_gradient": unused_nonzero,
+                                                 "seconds": fd_s,
+                                                 "relative_to": "max(|fd|, 1e-2 x the largest gradient component)"},
+        "gradient_vs_fp64_oracle_adjoint": {"max_rel": float(oracle_rel), "sample_pairs": int(cs.n_pairs)},
         "roofline": {"bound": "fp32_fma_pipe", "achieved": CALIB_FLOP_PER_CELL * cells / dt_fb / 1e12,
                      "peak": peak32, "unit": "TFLOP/s", "frac": CALIB_FLOP_PER_CELL * cells / dt_fb / 1e12 / peak32,
                      "flop_per_cell": CALIB_FLOP_PER_CELL,
@@ -600,7 +681,7 @@ def run_calib(args):
         "gpu_launches": reps,
         "clocks": clk,
         "cpu_baseline": {"value": oracle_cells / cpu_dt / 1e9, "unit": "GCUPS", "cores": 1, "kind": "port",
-                         "sample": f"every 128th pair ({len(range(0, cs.n_pairs, 128))} pairs, {oracle_cells:.3e} cells): "
+                         "sample": f"every pair ({cs.n_pairs} pairs, {oracle_cells:.3e} cells): "
                                    "FP64 forward + adjoint of oracle/oracle_grad.c, one pair at a time"},
     }
     print(json.dumps(line), flush=True)
@@ -1059,6 +1140,8 @@ def main():
     ap.add_argument("--cpu-cells", type=float, default=CPU_SAMPLE_CELLS)
     ap.add_argument("--plain-cells", type=float, default=PLAIN_SAMPLE_CELLS)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-full-check", action="store_true",
+                    help="skip the comparison of every timed result with the GPU's FP64 mode")
     ap.add_argument("--stream", action="store_true",
                     help="push the workload one region at a time through the queue (default workload 4)")
     ap.add_argument("--batch-cells", type=float, default=2e11, help="queue batch size in cells (--stream)")

@@ -3,7 +3,9 @@
     python -m gatk_gb300.build [--force] [--verbose]
 
 The library lands in gatk_gb300/_lib/libghmm.so (git-ignored) and links the CUDA runtime
-statically, so it loads with only the driver present.
+statically, so it loads with only the driver present.  The synthetic workload generator
+(include/ghmm_synth.h) is input generation for tests and benchmarks, not part of the product: it is
+built beside it as gatk_gb300/_lib/libghmm_synth.so, host code only.
 """
 from __future__ import annotations
 
@@ -24,7 +26,9 @@ LIB = os.path.join(OUT_DIR, "libghmm.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kernels.cu", "noalloc.cu", "calib.cu", "post.cu", "pd.cu", "prep.cu", "sw.cu"]
-CPP_SOURCES = ["runtime.cpp", "tables.cpp", "synth.cpp", "str_analyzer.cpp", "sw_host.cpp"]
+CPP_SOURCES = ["runtime.cpp", "tables.cpp", "str_analyzer.cpp", "sw_host.cpp"]
+SYNTH_SOURCES = ["synth.cpp"]
+SYNTH_LIB = os.path.join(OUT_DIR, "libghmm_synth.so")
 HEADERS = ["ghmm_internal.h", "tables.h", "str_analyzer.h", "host_util.h"]
 
 
@@ -40,7 +44,7 @@ def cuda_include() -> str:
 
 
 def _sources():
-    return [os.path.join(CSRC, s) for s in CU_SOURCES + CPP_SOURCES]
+    return [os.path.join(CSRC, s) for s in CU_SOURCES + CPP_SOURCES + SYNTH_SOURCES]
 
 
 def _deps():
@@ -49,9 +53,9 @@ def _deps():
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not (os.path.exists(LIB) and os.path.exists(SYNTH_LIB)):
         return False
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(SYNTH_LIB))
     return all(os.path.getmtime(d) <= t for d in _deps() if os.path.exists(d))
 
 
@@ -82,8 +86,13 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
         cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off",
                "-fno-fast-math", "-Wall", "-I", INCLUDE, "-I", cuda_include(), "-c", os.path.join(CSRC, s), "-o", obj]
         jobs.append((cmd, obj))
-    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
-        logs = list(ex.map(lambda j: _run(j[0], verbose), jobs))
+    synth_tmp = SYNTH_LIB + ".tmp"
+    synth_job = ([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off",
+                  "-fno-fast-math", "-Wall", "-shared", "-I", INCLUDE, *[os.path.join(CSRC, x) for x in SYNTH_SOURCES],
+                  "-o", synth_tmp], synth_tmp)
+    with ThreadPoolExecutor(max_workers=len(jobs) + 1) as ex:
+        logs = list(ex.map(lambda j: _run(j[0], verbose), jobs + [synth_job]))
+    os.replace(synth_tmp, SYNTH_LIB)
     if ptxas_verbose:
         print("\n".join(logs))
     tmp = LIB + ".tmp"

@@ -11,8 +11,15 @@
 // holds until the process exits (12 MiB of scratch plus 134 KiB of tables).
 //
 // Set-up: the first call on a device, with that device current, resolves the scratch array's device
-// address with cudaGetSymbolAddress and copies the tables into their arrays.  That first call should
-// therefore come before any stream capture.  Later calls only launch the kernel on the caller's stream.
+// address with cudaGetSymbolAddress, copies the tables into their arrays and waits for the copies to land
+// (cudaDeviceSynchronize), so that a kernel launched afterwards on any stream, blocking or not, reads them.
+// That first call should therefore come before any stream capture.  Later calls only launch the kernel on
+// the caller's stream.  The caller's current device is restored before every return.
+//
+// Input bytes are checked on the device, as the other entry points check them on the host: a pair whose
+// read has a base quality above 254, or an insertion, deletion or gap-continuation penalty above 127, gets
+// NaN as its result (the caller reads its outputs back and treats NaN as an input error), and so does a pair
+// whose haplotype is longer than GHMM_NOALLOC_MAX_HAP_LEN although max_hap_len promised otherwise.
 //
 // Every call shares the one scratch array, and the array keeps the last call's contents.  Nothing in it
 // needs to start at zero (each warp writes a strip boundary before it reads it), but calls that overlap
@@ -73,6 +80,15 @@ __global__ void __launch_bounds__(kBlock) noalloc_pairs_kernel(ghmm_dev_pairs in
             if (lane == 0) out[p] = -INFINITY;
             continue;
         }
+        // the read's bytes against the ranges the other entry points enforce (runtime.cpp): flagged as NaN
+        bool bad = false;
+        for (int i = lane; i < R; i += 32)
+            bad |= in.quals[roff + i] > ghmm::kMaxQual || in.ins_gop[roff + i] > 127 || in.del_gop[roff + i] > 127 ||
+                   in.gcp[roff + i] > 127;
+        if (__any_sync(kFull, bad)) {
+            if (lane == 0) out[p] = __longlong_as_double(0x7ff8000000000000LL);
+            continue;
+        }
         const double init = ldexp(1.0, 1020) / (double)H;
         const int nstrips = (R + kS - 1) / kS;
         const int pad = nstrips * kS - R;
@@ -94,11 +110,11 @@ __global__ void __launch_bounds__(kBlock) noalloc_pairs_kernel(ghmm_dev_pairs in
                     const uint8_t gcp = in.gcp[roff + pos];
                     pm[k] = g_noalloc_prob[q];
                     pe[k] = base == 'N' ? pm[k] : g_noalloc_err3[q];
-                    tmm[k] = g_noalloc_m2m[(ins & 127) * 128 + (del & 127)];
-                    tim[k] = g_noalloc_prob[gcp & 127];
-                    tmi[k] = g_noalloc_err[ins & 127];
-                    tii[k] = g_noalloc_err[gcp & 127];
-                    tmd[k] = g_noalloc_err[del & 127];
+                    tmm[k] = g_noalloc_m2m[ins * 128 + del];  // all <= 127: checked above
+                    tim[k] = g_noalloc_prob[gcp];
+                    tmi[k] = g_noalloc_err[ins];
+                    tii[k] = g_noalloc_err[gcp];
+                    tmd[k] = g_noalloc_err[del];
                     tdd[k] = tii[k];
                     rbase[k] = base;
                 }
@@ -208,6 +224,13 @@ int setup_device(int device) {
         set_error("copying the Phred tables into the no-allocation arrays failed");
         return GHMM_ERR_CUDA;
     }
+    // the copies above come from pageable memory and may return before their DMA lands; wait for them once, so
+    // that the first kernel reads the tables whatever stream it is launched on
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        set_error("waiting for the no-allocation tables to land failed");
+        return GHMM_ERR_CUDA;
+    }
     g_scratch_addr[device] = (double *)addr;
     g_ready[device] = true;
     return GHMM_OK;
@@ -240,21 +263,26 @@ extern "C" int ghmm_forward_pairs_noalloc(int32_t device, const ghmm_dev_pairs *
         return GHMM_ERR_ARG;
     }
     int cur = -1;
-    if (cudaGetDevice(&cur) != cudaSuccess || cur != device) {
-        if (cudaSetDevice(device) != cudaSuccess) {
-            set_error("ghmm_forward_pairs_noalloc: cudaSetDevice failed");
-            return GHMM_ERR_CUDA;
-        }
-    }
-    int rc = setup_device(device);
-    if (rc != GHMM_OK) return rc;
-    const int64_t want_blocks = (in->n_pairs + (kBlock / 32) - 1) / (kBlock / 32);
-    const int grid = (int)(want_blocks < kWarps / (kBlock / 32) ? want_blocks : kWarps / (kBlock / 32));
-    noalloc_pairs_kernel<<<grid, kBlock, 0, (cudaStream_t)stream>>>(*in, d_out, g_scratch_addr[device]);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) {
-        set_error(cudaGetErrorString(e));
+    if (cudaGetDevice(&cur) != cudaSuccess) {
+        set_error("ghmm_forward_pairs_noalloc: cudaGetDevice failed");
         return GHMM_ERR_CUDA;
     }
-    return GHMM_OK;
+    if (cur != device && cudaSetDevice(device) != cudaSuccess) {
+        set_error("ghmm_forward_pairs_noalloc: cudaSetDevice failed");
+        cudaSetDevice(cur);
+        return GHMM_ERR_CUDA;
+    }
+    int rc = setup_device(device);
+    if (rc == GHMM_OK) {
+        const int64_t want_blocks = (in->n_pairs + (kBlock / 32) - 1) / (kBlock / 32);
+        const int grid = (int)(want_blocks < kWarps / (kBlock / 32) ? want_blocks : kWarps / (kBlock / 32));
+        noalloc_pairs_kernel<<<grid, kBlock, 0, (cudaStream_t)stream>>>(*in, d_out, g_scratch_addr[device]);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error(cudaGetErrorString(e));
+            rc = GHMM_ERR_CUDA;
+        }
+    }
+    if (cur != device) cudaSetDevice(cur);  // the caller's current device, as it was
+    return rc;
 }

@@ -40,6 +40,9 @@ std::string g_init_error;
 
 constexpr int kBlock = 128;
 constexpr int kWarpsPerBlock = kBlock / 32;
+// Default of ghmm_tuning.route_fp64_below: the FP32 pass can represent log10 L down to about -64 (the rerun
+// threshold); a read expected 36 decades below that goes to FP64 without trying.
+constexpr int kRouteFp64Log10 = -100;
 
 uint8_t base_code(uint8_t b) {
     switch (b) {
@@ -179,6 +182,11 @@ struct ghmm_ctx {
     ghmm_batch scratch_batch;  // reused by the one-shot entry points
     ghmm_batch pd_batch;       // reused by the one-shot PD-HMM entry points
     int max_k = kMaxK32, max_k_multi = kMaxK32, chunk_cols = 16384;
+    // Reads whose expected log10 prior product (sum over positions of the per-quality expectation below) is under
+    // route_fp64_log10 go to the FP64 kernel directly: their FP32 results would fall below the rerun threshold and
+    // be recomputed there anyway, so the FP32 pass over them would be wasted.  A wrong guess costs only time.
+    int route_fp64_log10 = kRouteFp64Log10;
+    double expect_log10_prior[256] = {};  // (1 - e) log10(1 - e) + e log10(e / 3), e = 10^(-q/10)
     // calibration scratch (checkpointed fronts per resident warp), FP64-redo flags, unit weights
     DevBuf<uint8_t> calib_scratch;
     DevBuf<int> calib_flags;
@@ -369,8 +377,9 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                 memcpy(pg + ofs, sg, (size_t)R);
             }
             uint8_t fl = (R == 0) ? 1 : 0;
-            double growth = 1.0;
+            double growth = 1.0, expect = 0.0;
             for (int i = 0; i < R; i++) {
+                expect += ctx->expect_log10_prior[sq[i]];
                 if (sq[i] > kMaxQual || si[i] > 127 || sd[i] > 127 || sg[i] > 127) {
                     fl |= 2;
                     break;
@@ -388,6 +397,7 @@ static int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                 }
             }
             if (src.bound) fl |= src.bound->force;
+            if (expect < (double)ctx->route_fp64_log10) fl |= 1;  // predicted to underflow the FP32 pass
             read_flag[(size_t)r] = fl;
             b.h_read_region.p[r] = (int32_t)g;
         }
@@ -1799,6 +1809,10 @@ int ghmm_initialize(const ghmm_args *args, ghmm_ctx **out) {
     e = cudaMemcpy(ctx->table_mem, ht, bytes, cudaMemcpyHostToDevice);
     ctx->host_tables = ht;
     if (e != cudaSuccess) return bail(e, "upload tables");
+    for (int q = 0; q < 256; q++) {
+        const double err = ht->err[q], ok = 1.0 - err;
+        ctx->expect_log10_prior[q] = (ok > 0.0 ? ok * std::log10(ok) : 0.0) + err * std::log10(err / 3.0);
+    }
     const HostTables *dt = (const HostTables *)ctx->table_mem;
     ctx->tables.err_f = dt->err_f;
     ctx->tables.prob_f = dt->prob_f;
@@ -1866,11 +1880,13 @@ int ghmm_set_tuning(ghmm_ctx *ctx, const ghmm_tuning *t) {
     const int mk = t->max_rows_per_lane ? t->max_rows_per_lane : kMaxK32;
     const int mm = t->max_rows_per_lane_multi ? t->max_rows_per_lane_multi : kMaxK32;
     const int cc = t->chunk_cols ? t->chunk_cols : 16384;
-    if (mk < 1 || mk > kMaxK32 || mm < 1 || mm > kMaxK32 || cc < 1)
-        return fail(ctx, GHMM_ERR_ARG, "tuning out of range (rows per lane 1..8, chunk_cols >= 1)");
+    const int rf = t->route_fp64_below ? t->route_fp64_below : kRouteFp64Log10;
+    if (mk < 1 || mk > kMaxK32 || mm < 1 || mm > kMaxK32 || cc < 1 || rf > 0)
+        return fail(ctx, GHMM_ERR_ARG, "tuning out of range (rows per lane 1..8, chunk_cols >= 1, route_fp64_below <= 0)");
     ctx->max_k = mk;
     ctx->max_k_multi = mm;
     ctx->chunk_cols = cc;
+    ctx->route_fp64_log10 = rf;
     return GHMM_OK;
 }
 
@@ -2002,6 +2018,9 @@ int ghmm_batch_stats(ghmm_ctx *ctx, const ghmm_batch *b, ghmm_stats *st) {
     st->d2h_bytes = b->forward_d2h + b->results_d2h;
     st->ms_host_marshal = b->ms_host_copy;
     st->ms_host_tasks = b->ms_host_tasks;
+    st->n_cells_fp64_direct = (b->last_mode == GHMM_MODE_FP64 || b->last_mode == GHMM_MODE_PD) ? b->n_cells
+                              : (b->last_mode == GHMM_MODE_PD_FP32 || b->last_mode == GHMM_MODE_PLAIN_FP64) ? 0
+                                                                                                         : b->cells_direct;
     st->ms_prep = 0.0;
     if (b->prep_timed) {
         float ms = 0.0f;
@@ -2120,7 +2139,7 @@ int ghmm_autotune(ghmm_ctx *ctx, const ghmm_flat *sample, const ghmm_tuning *can
             best_i = (int)i;
             best_ms = med;
         }
-        cand[i] = ghmm_tuning{mk, mm, cc, 0};
+        cand[i] = ghmm_tuning{mk, mm, cc, ctx->route_fp64_log10};
     }
     cudaStreamSynchronize(ctx->stream);
     tb.release();
@@ -2140,7 +2159,7 @@ int ghmm_autotune(ghmm_ctx *ctx, const ghmm_flat *sample, const ghmm_tuning *can
 int ghmm_get_tuning(ghmm_ctx *ctx, ghmm_tuning *t) {
     if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
     if (!t) return fail(ctx, GHMM_ERR_ARG, "NULL tuning");
-    *t = ghmm_tuning{ctx->max_k, ctx->max_k_multi, ctx->chunk_cols, 0};
+    *t = ghmm_tuning{ctx->max_k, ctx->max_k_multi, ctx->chunk_cols, ctx->route_fp64_log10};
     return GHMM_OK;
 }
 

@@ -1,8 +1,10 @@
-"""ctypes binding of libghmm.so (include/ghmm.h, ghmm_sw.h, ghmm_synth.h, ghmm_calib.h).
+"""ctypes binding of libghmm.so (include/ghmm.h, ghmm_sw.h, ghmm_calib.h) and of the synthetic workload
+generator libghmm_synth.so (include/ghmm_synth.h).
 
 The library is the product: there is no Python or CPU fallback.  ``lib()`` builds it in-tree if it
 is missing and raises if that fails; compute calls raise ``GhmmError`` with the library's message
-when the device is absent or a call fails.
+when the device is absent or a call fails.  The generator is test and benchmark input, kept in a library
+of its own (``synth_lib()``) so that loading it does not load the product.
 """
 from __future__ import annotations
 
@@ -51,7 +53,7 @@ class Args(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("max_rows_per_lane", ctypes.c_int32), ("max_rows_per_lane_multi", ctypes.c_int32),
-                ("chunk_cols", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("chunk_cols", ctypes.c_int32), ("route_fp64_below", ctypes.c_int32)]
 
 
 class Read(ctypes.Structure):
@@ -80,7 +82,8 @@ class Stats(ctypes.Structure):
                 ("reserved", ctypes.c_int32), ("ms_fp32", ctypes.c_double), ("ms_fp64", ctypes.c_double),
                 ("ms_plain", ctypes.c_double), ("ms_total", ctypes.c_double), ("h2d_bytes", ctypes.c_int64),
                 ("d2h_bytes", ctypes.c_int64), ("ms_host_marshal", ctypes.c_double),
-                ("ms_host_tasks", ctypes.c_double), ("n_fp64_exact", ctypes.c_int64), ("ms_prep", ctypes.c_double)]
+                ("ms_host_tasks", ctypes.c_double), ("n_fp64_exact", ctypes.c_int64), ("ms_prep", ctypes.c_double),
+                ("n_cells_fp64_direct", ctypes.c_int64)]
 
 
 class RawRead(ctypes.Structure):
@@ -242,11 +245,6 @@ _SIGS = {
     "ghmm_queue_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "ghmm_measure_peaks": (ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p]),
     "ghmm_debug_tables": (ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p]),
-    "ghmm_synth_default_regions": (ctypes.c_int64, [ctypes.c_int32]),
-    "ghmm_synth_generate": (ctypes.c_int, [ctypes.c_int32, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
-                                           ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
-    "ghmm_synth_view": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SynthArrays)]),
-    "ghmm_synth_free": (None, [ctypes.c_void_p]),
     "ghmm_str_analyze": (ctypes.c_int, [_u8p, ctypes.c_int32, ctypes.c_int32, _i32p, _i32p, _i32p]),
     "ghmm_calib_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CalibBatch), ctypes.c_int32, ctypes.c_void_p]),
     "ghmm_calib_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CalibBatch), ctypes.c_int32, ctypes.c_void_p,
@@ -267,7 +265,17 @@ _SIGS = {
     "ghmm_sw_set_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
 }
 
+# The synthetic generator's symbols (include/ghmm_synth.h), exported by libghmm_synth.so.
+_SYNTH_SIGS = {
+    "ghmm_synth_default_regions": (ctypes.c_int64, [ctypes.c_int32]),
+    "ghmm_synth_generate": (ctypes.c_int, [ctypes.c_int32, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
+                                           ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+    "ghmm_synth_view": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SynthArrays)]),
+    "ghmm_synth_free": (None, [ctypes.c_void_p]),
+}
+
 _lib = None
+_synth = None
 _lock = threading.Lock()
 
 
@@ -292,8 +300,29 @@ def lib():
     return _lib
 
 
+def synth_lib():
+    """Load libghmm_synth.so, the synthetic workload generator (building it in-tree first if needed)."""
+    global _synth
+    with _lock:
+        if _synth is None:
+            _build.build()
+            L = ctypes.CDLL(_build.SYNTH_LIB)
+            for name, (res, args) in _SYNTH_SIGS.items():
+                f = getattr(L, name, None)
+                if f is None:
+                    raise ImportError(f"{_build.SYNTH_LIB} does not export {name}")
+                f.restype = res
+                f.argtypes = args
+            _synth = L
+    return _synth
+
+
 def exported_symbols():
     return sorted(_SIGS)
+
+
+def synth_symbols():
+    return sorted(_SYNTH_SIGS)
 
 
 def last_error(ctx) -> str:

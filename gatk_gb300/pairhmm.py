@@ -232,9 +232,15 @@ class Engine:
         native.check(rc, self._ctx.h)
         return out
 
-    def set_tuning(self, max_rows_per_lane: int = 0, max_rows_per_lane_multi: int = 0, chunk_cols: int = 0):
-        """FP32 launch shape for batches created afterwards (0 keeps a field's default)."""
-        t = native.Tuning(max_rows_per_lane, max_rows_per_lane_multi, chunk_cols, 0)
+    def set_tuning(self, max_rows_per_lane: int = 0, max_rows_per_lane_multi: int = 0, chunk_cols: int = 0,
+                   route_fp64_below: int | None = None):
+        """FP32 launch shape for batches created afterwards (0 keeps a field's default).  route_fp64_below (log10,
+        < 0) sends reads expected to underflow the FP32 pass straight to FP64; None keeps the current setting."""
+        if route_fp64_below is None:
+            cur = native.Tuning()
+            native.check(self.L.ghmm_get_tuning(self._ctx.h, ctypes.byref(cur)), self._ctx.h)
+            route_fp64_below = cur.route_fp64_below
+        t = native.Tuning(max_rows_per_lane, max_rows_per_lane_multi, chunk_cols, route_fp64_below)
         native.check(self.L.ghmm_set_tuning(self._ctx.h, ctypes.byref(t)), self._ctx.h)
 
     def get_tuning(self) -> tuple[int, int, int]:

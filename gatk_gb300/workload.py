@@ -197,7 +197,7 @@ def as_pd_regions(wl: Workload, hap_pd: np.ndarray):
 def generate(workload: int, regions: int | None = None, seed: int | None = None, region_begin: int = 0,
              threads: int = 0) -> Workload:
     """Synthetic workload `workload` (0-4), regions [region_begin, region_begin + regions)."""
-    L = native.lib()
+    L = native.synth_lib()
     if seed is None:
         seed = DEFAULT_SEEDS[workload]
     if regions is None:

@@ -136,17 +136,23 @@ typedef struct ghmm_stats {
                                  results of the rescaled FP64 tier below log10 L = -500, and host-marked reads */
     double ms_prep;           /* raw batches: device time of the read preparation kernels of the upload (quality
                                  caps, PCR model or DRAGstr imputation); 0 for prepared batches */
+    int64_t n_cells_fp64_direct; /* cells of the pairs the last forward sent to FP64 without an FP32 pass */
 } ghmm_stats;
 
 /* Launch-shape choices of the FP32 pass (the autotuner's knobs; the reference has none besides its thread
  * count).  A read of R bases runs single-strip with ceil(R/32) rows per lane when that is at most
  * max_rows_per_lane, otherwise as the fewest strips of at most max_rows_per_lane_multi rows per lane.
- * Zero fields keep their defaults (8, 8, 16384). */
+ * route_fp64_below sends a read's pairs to the FP64 kernel without an FP32 pass when the read's expected
+ * log10 prior product -- the sum over its positions of (1 - e) log10(1 - e) + e log10(e / 3), e the base
+ * error probability -- is below it: such pairs would fall under GHMM_FP32_RERUN_THRESHOLD (log10 L < -64)
+ * and be recomputed in FP64 anyway.  Results are the same either way (the FP64 result of a pair does not
+ * depend on how it reached the FP64 kernel); only time changes.  The autotuner keeps it as set.
+ * Zero fields keep their defaults (8, 8, 16384, -100). */
 typedef struct ghmm_tuning {
     int32_t max_rows_per_lane;       /* 1..8 */
     int32_t max_rows_per_lane_multi; /* 1..8 */
     int32_t chunk_cols;              /* haplotype columns per FP32 task, >= 1 */
-    int32_t reserved;
+    int32_t route_fp64_below;        /* log10 units, < 0; -1000000 in effect turns the routing off */
 } ghmm_tuning;
 
 /* PairHMMNativeBinding.load: 1 if a usable GPU (compute capability 10.3) is present, else 0. */
@@ -394,12 +400,16 @@ int ghmm_debug_tables(ghmm_ctx *ctx, double *err, double *prob, double *m2m);
  * memory, written to d_out[n_pairs] (device), with the FP64 wavefront kernel.  The call allocates
  * nothing: its scratch (strip-boundary rows for reads longer than 128 bases, 12 MiB) and its Phred
  * tables are static device arrays that every GPU which loads the library holds until the process exits.
- * The first call on a device (made with that device current) resolves the scratch address and fills
- * the tables, so it should come before any stream capture.  Calls share the scratch array and must not
- * overlap on the GPU.  Haplotypes longer than GHMM_NOALLOC_MAX_HAP_LEN are rejected with GHMM_ERR_ARG
- * (max_hap_len is the caller's bound; a longer haplotype found on the device yields NaN for its pair).
- * Launches on `stream` (a cudaStream_t; NULL is the legacy default stream) and returns without waiting;
- * error messages come from ghmm_last_error(NULL, ...). */
+ * The first call on a device (made with that device current) resolves the scratch address, fills the
+ * tables and waits for them to land (a device synchronisation, once), so it should come before any stream
+ * capture.  Calls share the scratch array, which keeps the last call's contents, and must not overlap on
+ * the GPU: overlapping calls race on it.  Haplotypes longer than GHMM_NOALLOC_MAX_HAP_LEN are rejected
+ * with GHMM_ERR_ARG (max_hap_len is the caller's bound; a longer haplotype found on the device yields NaN
+ * for its pair).  The input bytes live on the device, so they are checked there: a pair whose read has a
+ * base quality above 254 or an insertion, deletion or gap-continuation penalty above 127 (a negative Java
+ * byte) yields NaN, where the other entry points return GHMM_ERR_ARG.  Launches on `stream` (a
+ * cudaStream_t; NULL is the legacy default stream) and returns without waiting; the caller's current
+ * device is left as it was.  Error messages come from ghmm_last_error(NULL, ...). */
 #define GHMM_NOALLOC_MAX_HAP_LEN 2048
 #define GHMM_NOALLOC_WARPS 256
 

@@ -70,4 +70,6 @@ def main(root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_dragstr_golden.py GATK_CHECKOUT  (the root of a broadinstitute/gatk source tree)")
+    main(sys.argv[1])

@@ -106,13 +106,35 @@ def test_workload1_subsample(engine):
 def test_workload2_rerun_path(engine):
     wl = W.generate(2, regions=2)
     ref = _oracle_all(wl)
-    got, st = _run(engine, wl, native.MODE_FP32_RERUN)
-    assert st["n_rerun"] > 0
+    # with the predicted-underflow routing off, every underflowing pair goes through the FP32 pass and its rerun
+    engine.set_tuning(route_fp64_below=-1000000)
+    try:
+        got, st = _run(engine, wl, native.MODE_FP32_RERUN)
+    finally:
+        engine.set_tuning(route_fp64_below=0)  # back to the default
+    assert st["n_rerun"] > 0 and st["n_fp64_direct"] == 0
     d = _absdiff(got, ref)
     # reruns are the underflowing pairs (log10 L below about -64)
     under = ref < RERUN_LOG10 - 0.01
     assert _absdiff(got[under], ref[under]).max() <= TOL64
     assert d.max() <= TOL32
+    # with the routing on (the default), reads expected far below the FP32 range skip the FP32 pass.  A pair's FP64
+    # result does not depend on the way it reached the FP64 kernel, so every rerun pair keeps its bits; the pairs
+    # that change are FP32 results now computed in FP64
+    got2, st2 = _run(engine, wl, native.MODE_FP32_RERUN)
+    assert st2["n_fp64_direct"] > 0 and st2["n_cells_fp64_direct"] > 0
+    assert st2["n_rerun"] + st2["n_fp64_direct"] >= st["n_rerun"]
+    assert np.array_equal(got2[under], got[under])
+    changed = got2 != got
+    assert _absdiff(got2[changed], ref[changed]).max(initial=0.0) <= TOL64
+    assert _absdiff(got2, ref).max() <= TOL32
+
+
+def test_predicted_underflow_routing_leaves_workload1_alone(engine):
+    wl = W.generate(1, regions=60)
+    got, st = _run(engine, wl, native.MODE_FP32_RERUN)
+    assert st["n_fp64_direct"] == 0  # reads of 100-250 bases at Q10-40 are far above the routing bound
+    assert _absdiff(got, _oracle_all(wl)).max() <= TOL32
 
 
 def _single(hap, read, q=30, ins=45, dl=45, gcp=10):

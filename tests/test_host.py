@@ -13,10 +13,11 @@ from gatk_gb300 import native, workload as W
 from oracle import oracle as O
 
 
-def _declared_functions():
+def _declared_functions(synth: bool):
+    """ghmm_* functions declared by the product headers (synth False) or by the generator's header (True)."""
     names = set()
     for h in os.listdir(os.path.join(ROOT, "include")):
-        if not h.endswith(".h"):
+        if not h.endswith(".h") or (h == "ghmm_synth.h") != synth:
             continue
         src = open(os.path.join(ROOT, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
@@ -26,11 +27,21 @@ def _declared_functions():
 
 def test_library_exports_every_declared_symbol():
     L = native.lib()
-    declared = _declared_functions()
+    declared = _declared_functions(False)
     assert declared, "no declarations found"
     for name in declared:
         assert hasattr(L, name), name
     assert declared == set(native.exported_symbols())
+
+
+def test_generator_lives_outside_the_product_library():
+    # the synthetic generator is test and benchmark input: its own library exports it, the product does not
+    S = native.synth_lib()
+    declared = _declared_functions(True)
+    assert declared == set(native.synth_symbols())
+    for name in declared:
+        assert hasattr(S, name), name
+        assert not hasattr(native.lib(), name), name
 
 
 def test_header_constants_match_the_bindings():
