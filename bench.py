@@ -23,7 +23,8 @@ same run, and the FP64 oracle's GCUPS on the host cores.
 LoglessPairHMM (oracle/, OpenMP over pairs on every host core) on a bounded sample of the same workload;
 GATK's Java and GKL's AVX code cannot run on this machine (no JVM; GKL is x86-only).
 Under torchrun with N > 1 each rank runs its own 10,000 regions on its own GPU (weak scaling; the regions
-are independent so no collective touches the data path); rank 0 prints.
+are independent so no collective touches the data path), or with --scaling strong its share of one workload as the
+library's multi-device split (ghmm_multi_plan) cuts it; rank 0 prints.
 """
 from __future__ import annotations
 
@@ -202,10 +203,17 @@ def run_ours(args):
 
     eng = Engine(device=device)
     peaks = eng.measure_peaks()
-    # weak scaling: every rank owns its own block of regions of the same distribution
     n_regions = args.regions or int(native.synth_lib().ghmm_synth_default_regions(args.workload))
-    g0, g1 = sharding.block_range(n_regions, rank)
-    wl = W.generate(args.workload, regions=g1 - g0, region_begin=g0)
+    if args.scaling == "strong":
+        # strong scaling: one workload, cut by the library's split (ghmm_multi_plan) into one read range per rank
+        wl_all = W.generate(args.workload, regions=n_regions)
+        mine = sharding.read_slices(wl_all, world)[rank]
+        wl = wl_all.read_slice(mine["read_begin"], mine["read_end"])
+        del wl_all
+    else:
+        # weak scaling: every rank owns its own block of regions of the same distribution
+        g0, g1 = sharding.block_range(n_regions, rank)
+        wl = W.generate(args.workload, regions=g1 - g0, region_begin=g0)
     cells = int(wl.cells_per_region().sum())
     tuning = apply_tuning(args, eng, wl)
 
@@ -359,7 +367,7 @@ def run_ours(args):
     traffic = read_profile_traffic()
     line = {
         "metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": args.scaling,
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (deterministic generator; seeded stand-in for HaplotypeCaller active regions)",
         "config": workload_config(args, wl),
@@ -1136,7 +1144,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", type=int, default=1)
-    ap.add_argument("--regions", type=int, default=0, help="regions per rank (0: the workload's full size)")
+    ap.add_argument("--regions", type=int, default=0, help="regions per rank, or in all with --scaling strong "
+                    "(0: the workload's full size)")
+    ap.add_argument("--scaling", choices=["weak", "strong"], default="weak",
+                    help="weak: every rank runs its own full-size block of regions; strong: the ranks split one "
+                         "workload with the library's split (ghmm_multi_plan)")
     ap.add_argument("--cpu-cells", type=float, default=CPU_SAMPLE_CELLS)
     ap.add_argument("--plain-cells", type=float, default=PLAIN_SAMPLE_CELLS)
     ap.add_argument("--no-e2e", action="store_true")

@@ -148,6 +148,11 @@ class DevPairs(ctypes.Structure):
 NOALLOC_MAX_HAP_LEN = 2048
 
 
+class MultiSlice(ctypes.Structure):
+    _fields_ = [("read_begin", ctypes.c_int64), ("read_end", ctypes.c_int64), ("out_begin", ctypes.c_int64),
+                ("out_end", ctypes.c_int64), ("cells", ctypes.c_int64)]
+
+
 class CalibBatch(ctypes.Structure):
     _fields_ = [("bases", ctypes.c_void_p), ("quals", ctypes.c_void_p), ("read_off", ctypes.c_void_p),
                 ("hap_bases", ctypes.c_void_p), ("hap_off", ctypes.c_void_p), ("pair_read", ctypes.c_void_p),
@@ -249,6 +254,12 @@ _SIGS = {
     "ghmm_calib_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CalibBatch), ctypes.c_int32, ctypes.c_void_p]),
     "ghmm_calib_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CalibBatch), ctypes.c_int32, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "ghmm_multi_create": (ctypes.c_int, [_i32p, ctypes.c_int32, ctypes.POINTER(Args), ctypes.POINTER(ctypes.c_void_p)]),
+    "ghmm_multi_compute_regions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, _f64p]),
+    "ghmm_multi_plan": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(MultiSlice)]),
+    "ghmm_multi_context": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+    "ghmm_multi_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
+    "ghmm_multi_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "ghmm_forward_pairs_noalloc": (ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(DevPairs), ctypes.c_void_p,
                                                   ctypes.c_void_p]),
     "ghmm_sw_align": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,

@@ -204,6 +204,56 @@ class CudaLoglessPairHMM:
         self.close()
 
 
+class MultiEngine:
+    """One caller driving several GPUs (ghmm_multi_*): a context per listed device; each call's reads are cut into
+    contiguous ranges of about equal cells, one per device, whose results land straight in their slice of the
+    read-major output.  Devices may repeat (independent contexts on one GPU)."""
+
+    def __init__(self, devices, max_threads: int = 0, use_double_precision: bool = False):
+        self.L = native.lib()
+        self.devices = [int(d) for d in devices]
+        devs = (ctypes.c_int32 * len(self.devices))(*self.devices)
+        a = native.Args(0, int(max_threads), int(use_double_precision), 0)
+        h = ctypes.c_void_p()
+        rc = self.L.ghmm_multi_create(devs, len(self.devices), ctypes.byref(a), ctypes.byref(h))
+        if rc == native.GHMM_ERR_UNSUPPORTED:
+            raise HardwareFeatureException(native.last_error(None))
+        native.check(rc, None)
+        self.h = h
+
+    def _check(self, rc: int):
+        if rc != native.GHMM_OK:
+            buf = ctypes.create_string_buffer(1024)
+            self.L.ghmm_multi_last_error(self.h, buf, len(buf))
+            raise native.GhmmError(rc, buf.value.decode(errors="replace"))
+
+    def compute(self, wl: Workload, out: np.ndarray | None = None) -> np.ndarray:
+        """All pairs of wl (host buffers in, host results out), split over the devices."""
+        if out is None:
+            out = np.empty(wl.n_pairs, dtype=np.float64)
+        regs = wl.as_regions()
+        self._check(self.L.ghmm_multi_compute_regions(self.h, ctypes.cast(regs, ctypes.c_void_p), wl.n_regions,
+                                                      out.ctypes.data_as(native._f64p)))
+        return out
+
+    def close(self):
+        if self.h:
+            self.L.ghmm_multi_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Engine:
     """Batched, device-resident use of the kernels (the batcher): one context, many regions."""
 

@@ -1,24 +1,24 @@
-"""Sharding of active regions across GPUs: regions are independent, so ranks split them with no
-collective on the data path; only timings are reduced (max over ranks) for reporting."""
+"""Sharding of active regions across GPUs: pairs are independent, so ranks split them with no
+collective on the data path; only timings are reduced (max over ranks) for reporting.
+
+Strong scaling uses the library's own split (ghmm_multi_plan, the split ghmm_multi_compute_regions applies
+within one process): reads numbered in region order are cut into one contiguous range per device of about
+equal cells, and each range owns a contiguous slice of the read-major output."""
 from __future__ import annotations
 
-import heapq
+import ctypes
 
 import numpy as np
 
+from . import native
 
-def partition_by_cells(cells_per_region, world: int) -> list[np.ndarray]:
-    """Greedy longest-first assignment of regions to `world` ranks by cell count (strong scaling).
-    Returns, per rank, the sorted region indices it owns; every region appears exactly once."""
-    cells = np.asarray(cells_per_region, dtype=np.int64)
-    order = np.argsort(-cells, kind="stable")
-    heap = [(0, r) for r in range(world)]
-    owned = [[] for _ in range(world)]
-    for g in order:
-        load, r = heapq.heappop(heap)
-        owned[r].append(int(g))
-        heapq.heappush(heap, (load + int(cells[g]), r))
-    return [np.array(sorted(o), dtype=np.int64) for o in owned]
+
+def read_slices(wl, world: int) -> list[dict]:
+    """Per rank: {read_begin, read_end, out_begin, out_end, cells} of the workload's strong-scaling split."""
+    regs = wl.as_regions()
+    sl = (native.MultiSlice * world)()
+    native.check(native.lib().ghmm_multi_plan(ctypes.cast(regs, ctypes.c_void_p), wl.n_regions, world, sl))
+    return [{k: int(getattr(s, k)) for k, _ in native.MultiSlice._fields_} for s in sl]
 
 
 def block_range(n_regions_per_rank: int, rank: int) -> tuple[int, int]:

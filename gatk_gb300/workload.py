@@ -105,6 +105,35 @@ class Workload:
             hap_off=self.hap_off[h0:h1 + 1] - c0, hap_bases=self.hap_bases[c0:c1].copy(),
             out_off=self.out_off[g0:g1 + 1] - self.out_off[g0])
 
+    def read_slice(self, read_begin: int, read_end: int) -> "Workload":
+        """Reads [read_begin, read_end) (numbered across regions in order) as a self-contained workload: every
+        region that overlaps the range, restricted to its reads in the range, with all its haplotypes.  Its
+        read-major outputs are the slice of this workload's outputs that those reads own."""
+        rro = self.region_read_off
+        g0 = int(np.searchsorted(rro, read_begin, side="right")) - 1
+        g1 = int(np.searchsorted(rro, read_end, side="left"))
+        g0 = max(g0, 0)
+        g1 = max(g1, g0)
+        sub = self.subset(g0, g1) if g1 > g0 else self.subset(g0, g0)
+        if g1 == g0:
+            return sub
+        # trim the first region's leading reads and the last region's trailing reads
+        lead = read_begin - int(rro[g0])
+        trail = int(rro[g1]) - read_end
+        n_reads = read_end - read_begin
+        nr = np.diff(sub.region_read_off).copy()
+        nr[0] -= lead
+        nr[-1] -= trail
+        b0 = int(sub.read_off[lead])
+        b1 = int(sub.read_off[lead + n_reads])
+        nh = np.diff(sub.region_hap_off)
+        return Workload(
+            region_read_off=np.concatenate([[0], np.cumsum(nr)]).astype(np.int64),
+            region_hap_off=sub.region_hap_off, read_off=sub.read_off[lead:lead + n_reads + 1] - b0,
+            bases=sub.bases[b0:b1].copy(), quals=sub.quals[b0:b1].copy(), ins=sub.ins[b0:b1].copy(),
+            dels=sub.dels[b0:b1].copy(), gcp=sub.gcp[b0:b1].copy(), hap_off=sub.hap_off, hap_bases=sub.hap_bases,
+            out_off=np.concatenate([[0], np.cumsum(nr * nh)]).astype(np.int64))
+
     def as_flat(self) -> native.Flat:
         p = lambda a, t: a.ctypes.data_as(t)
         f = native.Flat(self.n_regions, p(self.region_read_off, native._i64p), p(self.region_hap_off, native._i64p),

@@ -393,6 +393,38 @@ int ghmm_measure_peaks(ghmm_ctx *ctx, double *fp32_tflops, double *fp32x2_tflops
  * With ctx == NULL the host-built tables are returned (no device needed). */
 int ghmm_debug_tables(ghmm_ctx *ctx, double *err, double *prob, double *m2m);
 
+/* ---- Several devices from one caller ----
+ * One handle drives several GPUs (HaplotypeCaller's one JVM; the reference parallelises the host side with GKL's
+ * thread count, HC/PairHMMNativeArgumentCollection.java:11-12, or one engine per Spark partition,
+ * tools/HaplotypeCallerSpark.java:175-179).  The handle owns one context per device.  A call's reads, numbered
+ * in region order, are cut into one contiguous range per device carrying about equal cells (read length x the
+ * summed lengths of its region's haplotypes); a contiguous read range owns a contiguous slice of the read-major
+ * `out`, so each device writes its results straight into its slice.  No device-to-device traffic, no collective.
+ *   ghmm_multi_create:           a context per listed device (devices may repeat: independent contexts on one
+ *                                GPU); args as ghmm_initialize, device ignored, max_threads <= 0 shares the host
+ *                                cores between the devices.  Setting the environment variable
+ *                                GHMM_MULTI_STUB_DEVICES (not "0") creates host-only stand-ins that subtract
+ *                                (index + 1) over their slice of `out` instead of computing, so the split can be
+ *                                tested without a GPU.
+ *   ghmm_multi_compute_regions:  as ghmm_compute_regions over all devices, one host thread per device.
+ *   ghmm_multi_plan:             the split alone (host only): slices[d] for n_devices devices.
+ *   ghmm_multi_context:          the context of device index `index` (for tuning, statistics, batches).
+ *   ghmm_multi_last_error / ghmm_multi_destroy. */
+typedef struct ghmm_multi ghmm_multi;
+
+typedef struct ghmm_multi_slice {
+    int64_t read_begin, read_end; /* reads of the call, numbered across regions in order: [read_begin, read_end) */
+    int64_t out_begin, out_end;   /* the slice of out those reads' likelihoods fill */
+    int64_t cells;                /* cells of the slice */
+} ghmm_multi_slice;
+
+int ghmm_multi_create(const int32_t *devices, int32_t n_devices, const ghmm_args *args, ghmm_multi **multi);
+int ghmm_multi_compute_regions(ghmm_multi *multi, const ghmm_region *regions, int32_t n_regions, double *out);
+int ghmm_multi_plan(const ghmm_region *regions, int32_t n_regions, int32_t n_devices, ghmm_multi_slice *slices);
+int ghmm_multi_context(ghmm_multi *multi, int32_t index, ghmm_ctx **ctx);
+int ghmm_multi_last_error(const ghmm_multi *multi, char *buf, size_t buf_len);
+int ghmm_multi_destroy(ghmm_multi *multi);
+
 /* ---- No-allocation entry point.  It has no counterpart in the reference. ----
  * For callers that cannot allocate GPU memory (code running inside another framework's memory pool or
  * a fixed device-memory budget, or that must not take the synchronisation an allocation implies):
