@@ -12,10 +12,12 @@
 //  * fp32_bucket_kernel<K, MULTI>: the batched FP32 forward.  One warp runs a read-pair task: two reads of
 //    one region, packed into the .x/.y halves of float2 so every cell update is a packed FFMA2/FMUL2/FADD2,
 //    against all (or a chunk of) the region's haplotypes streamed back to back.  Lane l owns K consecutive
-//    rows; at step s it computes column c = s - l, receiving the row above from lane l-1 by __shfl_up_sync
-//    (an anti-diagonal wavefront); lane l-1 hands lane l two packed values per step, its row 0's I~ at this
-//    column and the inner sum b I~ + c D~ + M~ of its row 0's next M~, computed with lane l's row-0 coefficients,
-//    instead of three raw states (K >= 2).  Each read is followed by two accumulator rows that sum the last row over
+//    rows; at step s it computes column c = s - 2l, receiving the row above from lane l-1 by __shfl_up_sync
+//    (an anti-diagonal wavefront with a skew of two columns per lane, so that a value shuffled at the start of
+//    a step is consumed one step later and the shuffle's latency stays off the per-step chain); lane l-1 hands
+//    lane l two packed values per step, its row 0's I~ at a column and the inner sum b I~ + c D~ + M~ of its
+//    row 0's M~ at the next column, computed with lane l's row-0 coefficients, instead of three raw states
+//    (K >= 2).  Each read is followed by two accumulator rows that sum the last row over
 //    the haplotype (row_coef), and padded at the top with "dummy" rows that reproduce the row-0 boundary, so
 //    the accumulator rows always sit in lane 31's last two slots.  Reads longer than 32*K rows run
 //    as several strips whose boundary row goes through per-warp global scratch.  Each row's states are
@@ -260,27 +262,32 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
             float2 Mp[K], Ip[K], Dp[K];
 #pragma unroll
             for (int k = 0; k < K; ++k) Mp[k] = Ip[k] = Dp[k] = zero2();
-            float2 gW = zero2();   // row 0's M~ inner sum for this step (from the lane above, one step late)
+            float2 gW = zero2();   // row 0's M~ inner sum consumed this step (the diagonal input of row 0)
             float2 w0 = zero2();   // lane 0, strip 0: the row-0 boundary's inner sum c_0 X
+            // Lane l runs column s - 2l at step s (a skew of two columns per lane), so what lane l-1 hands over
+            // at the end of a step is shuffled at the start of the next one and consumed a step later: the
+            // shuffle's latency is off the per-step chain (the I~ recurrence down the lane's rows).
+            float2 pendV = zero2();                     // I~ of row 0 for next step's column
+            float2 pendW1 = zero2(), pendW2 = zero2();  // row 0's M~ inner sums for the next two steps
             int hap = task.hap_begin - 1;
             const bool last_strip = (strip == nstrips - 1);
-            float2 nxV = zero2(), nxW = zero2();  // prefetched strip boundary (MULTI, lane 0)
+            float2 nxV = zero2(), nxW = zero2(), l0W = zero2();  // strip boundary (MULTI, lane 0): prefetched
             if (MULTI && strip > 0 && lane == 0 && ncols > 0) {
                 nxV = scratch[0];
                 nxW = scratch[1];
             }
             float2 sV = zero2(), sW = zero2();  // what this lane hands the lane below at the end of a step
-            const int nsteps = ncols + 31;
+            const int nsteps = ncols + 62;
             // column code of the next step, loaded one step ahead (the code plane has kCodePad bytes on
             // both sides, so columns just outside the stream are readable; CHK steps mask them)
-            uint32_t code_next = (uint32_t)__ldg(stream - lane);
+            uint32_t code_next = (uint32_t)__ldg(stream - 2 * lane);
             // One wavefront step.  CHK steps handle columns outside the stream (lanes that have not started
             // or have finished), haplotype starts (state reset) and ends (lane 31 emits); they are needed
-            // only in the 32 steps after each haplotype start, where those events fall.  Every other step
+            // only in the 63 steps after each haplotype start, where those events fall.  Every other step
             // runs the check-free form.
             auto step = [&](const int s, auto chk_tag) {
                 constexpr bool CHK = decltype(chk_tag)::value;
-                const int c = s - lane;
+                const int c = s - 2 * lane;
                 bool valid = true;
                 uint32_t code = code_next;
                 code_next = (uint32_t)__ldg(stream + c + 1);
@@ -288,11 +295,31 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                     valid = (c >= 0) && (c < ncols);
                     code = valid ? code : 0u;
                 }
-                // row above at this column: lane l-1's last row as computed last step.  Shuffled before
-                // this lane resets its own state at a haplotype start, since lane l+1 still needs the
-                // previous haplotype's last column from it.
-                float2 uV = shfl_up2(sV);  // I~ of this lane's row 0 at this column
-                float2 uW = shfl_up2(sW);  // row 0's M~ inner sum for the next column
+                // Lane l-1's hand-over from its last step (its column c + 1): shuffled now, consumed next step
+                // (I~) and the step after (the inner sum for column c + 2).  Shuffled before this lane resets its
+                // own state at a haplotype start, since lane l+1 still needs this lane's previous column.
+                const float2 shV = shfl_up2(sV);
+                const float2 shW = shfl_up2(sW);
+                float2 uV = pendV;  // I~ of this lane's row 0 at this column
+                gW = pendW2;        // row 0's M~ inner sum for this column
+                pendV = shV;
+                pendW2 = pendW1;
+                pendW1 = shW;
+                // lane 0 takes the row-0 boundary (strip 0) or the previous strip's last row instead
+                // (selects on the ALU pipe, not multiplies on the FMA pipe)
+                if (MULTI && strip > 0) {
+                    if (lane == 0) {
+                        uV = nxV;
+                        gW = l0W;
+                        l0W = nxW;
+                        if (c + 1 < ncols) {
+                            nxV = scratch[2 * (c + 1) + 0];
+                            nxW = scratch[2 * (c + 1) + 1];
+                        }
+                    }
+                } else if (lane == 0) {
+                    uV = zero2();
+                }
                 if constexpr (CHK) {
                     if (code & kColFirst) {
                         ++hap;
@@ -312,21 +339,7 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                         if (lane == 0 && strip == 0) w0 = mul2(cc[0], X);
                     }
                 }
-                // lane 0 takes the row-0 boundary (strip 0) or the previous strip's last row instead
-                // (selects on the ALU pipe, not multiplies on the FMA pipe)
-                if (MULTI && strip > 0) {
-                    if (lane == 0) {
-                        uV = nxV;
-                        uW = nxW;
-                        if (c + 1 < ncols) {
-                            nxV = scratch[2 * (c + 1) + 0];
-                            nxW = scratch[2 * (c + 1) + 1];
-                        }
-                    }
-                } else if (lane == 0) {
-                    uV = zero2();
-                    uW = w0;
-                }
+                if (!(MULTI && strip > 0) && lane == 0) gW = w0;
                 const float4 *pri4 = prior_tbl4 + (code & 7u) * 32;
                 float2 prs[2 * KP];
 #pragma unroll
@@ -354,7 +367,6 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
 #pragma unroll
                 for (int k = 1; k < K; ++k) Ip[k] = fma2(Ip[k - 1], ce[k], Mp[k - 1]);
                 const float2 i_acc = Ip[K >= 2 ? K - 2 : 0];  // I~(R+1) at this column (K >= 2)
-                gW = uW;
                 // hand the lane below its row 0's I~ at this column and M~ inner sum for the next
                 sV = fma2(Ip[K - 1], e0n, Mp[K - 1]);
                 sW = fma2(Ip[K - 1], b0n, fma2(Dp[K - 1], c0n, Mp[K - 1]));
@@ -377,7 +389,7 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
             int s = 0, j = 0;
             while (s < nsteps) {
                 while (j <= nh_task && (int)(hoff[j] - col0) <= s) ++j;
-                const int window_end = min((int)(hoff[j - 1] - col0) + 32, nsteps);
+                const int window_end = min((int)(hoff[j - 1] - col0) + 63, nsteps);
                 // unrolled (4 checked, 16 check-free steps; measured best of 2-32): the scheduler interleaves
                 // one step's I~ chain and shuffles with the following steps' M~ and D~
                 if (s < window_end) {

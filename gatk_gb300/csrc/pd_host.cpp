@@ -1,0 +1,314 @@
+// pd_host.cpp -- PD-HMM batches on the host side (ghmm_pd_*): the regular marshal over the haplotypes' bases plus
+// the PD flag and HMM state planes, and the forward through pd.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "runtime_internal.h"
+
+namespace ghmm {
+namespace rt {
+
+// -------------------------------------------------------------------------------------------------
+// PD-HMM batches: the regular marshal over the haplotypes' bases, plus per haplotype column the PD flags and the
+// HMM state codes (PdPlanes), and a forward that runs every pair through pd.cu.
+
+
+// State sequence along one row (LoglessPDPairHMM.java:62-142): the state a column is processed in, then AFTER_DEL
+// ends, DEL_START enters INSIDE_DEL, DEL_END enters AFTER_DEL.  Returns the state after the last column.
+int pd_states(const uint8_t *f, int H, int start, uint8_t *code, int shift) {
+    int st = start;
+    for (int j = 0; j < H; j++) {
+        code[j] |= (uint8_t)(st << shift);
+        if (st == 2) st = 0;
+        if (f[j] & 2) st = 1;
+        if (f[j] & 4) st = 2;
+    }
+    return st;
+}
+
+bool pd_read_base_ok(uint8_t x) {
+    switch (x) {
+        case 'A': case 'C': case 'G': case 'T': case 'a': case 'c': case 'g': case 't': case 'N': return true;
+        default: return false;
+    }
+}
+
+
+int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch &b) {
+    std::vector<ghmm_region> rr((size_t)G);
+    std::vector<std::vector<ghmm_hap>> hh((size_t)G);
+    std::vector<const uint8_t *> pdp;
+    for (int64_t g = 0; g < G; g++) {
+        const ghmm_pd_region &rg = regs[g];
+        if (rg.n_reads < 0 || rg.n_haps < 0 || (rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps))
+            return fail(ctx, GHMM_ERR_ARG, "bad PD region");
+        hh[(size_t)g].resize((size_t)rg.n_haps);
+        for (int32_t h = 0; h < rg.n_haps; h++) {
+            const ghmm_pd_hap &hp = rg.haps[h];
+            if (hp.length > 0 && (!hp.bases || !hp.pd_bases)) return fail(ctx, GHMM_ERR_ARG, "NULL PD haplotype array");
+            hh[(size_t)g][(size_t)h] = ghmm_hap{hp.bases, hp.length};
+            pdp.push_back(hp.pd_bases);
+        }
+        rr[(size_t)g] = ghmm_region{rg.reads, rg.n_reads, hh[(size_t)g].data(), rg.n_haps};
+    }
+    Source src;
+    src.regions = rr.data();
+    src.n_regions = G;
+    int rc = batch_marshal(ctx, src, b);
+    if (rc) return rc;
+    const int64_t NH = b.n_haps, HB = b.hap_bytes;
+    GHMM_CUDA(b.h_pd.reserve((size_t)std::max<int64_t>(2 * HB, 1)), "pinned PD planes");
+    const int64_t *o = b.h_off.p;
+    const int64_t *hap_off = o + b.n_reads + 1;
+    uint8_t *flags = b.h_pd.p, *states = b.h_pd.p + HB;
+    parallel_for(NH, hw_threads(ctx->max_threads), [&](int64_t h) {
+        const int64_t a = hap_off[h];
+        const int H = (int)(hap_off[h + 1] - a);
+        if (H <= 0) return;
+        memcpy(flags + a, pdp[(size_t)h], (size_t)H);
+        uint8_t *code = states + a;
+        memset(code, 0, (size_t)H);
+        const int end1 = pd_states(flags + a, H, 0, code, 0);
+        pd_states(flags + a, H, end1, code, 2);
+        for (int j = 0; j < H; j++)
+            if (flags[a + j] & 4) code[j] |= 16;
+    });
+    // a read base outside ACGTacgtN that meets an undetermined SNP column throws in the reference
+    const int64_t *rro = o + b.n_reads + 1 + NH + 1, *rho = rro + G + 1;
+    const uint8_t *bases = b.h_planes.p;
+    const uint8_t *hraw = b.h_hap.p;
+    for (int64_t g = 0; g < G; g++)
+        for (int64_t r = rro[g]; r < rro[g + 1]; r++)
+            for (int64_t i = o[r]; i < o[r + 1]; i++) {
+                const uint8_t x = bases[i];
+                if (pd_read_base_ok(x)) continue;
+                for (int64_t h = rho[g]; h < rho[g + 1]; h++)
+                    for (int64_t j = hap_off[h]; j < hap_off[h + 1]; j++)
+                        if ((flags[j] & 1) && hraw[j] != x && hraw[j] != 'N')
+                            return fail(ctx, GHMM_ERR_ARG, "Found unexpected base in alt alleles");
+            }
+    b.has_pd = true;
+    return GHMM_OK;
+}
+
+int pd_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
+    int rc = batch_upload(ctx, b, s);
+    if (rc) return rc;
+    const int64_t HB = b.hap_bytes;
+    GHMM_CUDA(b.d_pd.reserve((size_t)std::max<int64_t>(2 * HB, 1)), "device PD planes");
+    if (HB > 0)
+        GHMM_CUDA(cudaMemcpyAsync(b.d_pd.p, b.h_pd.p, (size_t)(2 * HB), cudaMemcpyHostToDevice, s), "H2D PD planes");
+    b.pd.flags = b.d_pd.p;
+    b.pd.states = b.d_pd.p + HB;
+    b.upload_bytes += 2 * HB;
+    return GHMM_OK;
+}
+
+// fp32: every pair in the FP32 PD kernel, then the pairs whose sums underflow in the FP64 one (K = 4 for all);
+// otherwise every pair in FP64
+int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32) {
+    cudaStream_t s = ctx->stream;
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    // every pair, grouped by the rows per lane K of its read (the strip height 32 K, K = 1..4, that needs the
+    // fewest rows; ties to the larger K, i.e. fewer strips), read-major per region within a group
+    GHMM_CUDA(b.h_fp64all.reserve((size_t)std::max<int64_t>(b.n_out, 1)), "pinned PD pairs");
+    const int64_t *o = b.h_off.p;
+    const int64_t *rro = o + b.n_reads + 1 + b.n_haps + 1, *rho = rro + b.n_regions + 1;
+    const int maxk = fp32 ? kPdMaxK32 : kPdMaxK;
+    auto pick_k = [maxk](int64_t R) {
+        int best_k = maxk;
+        int64_t best_rows = INT64_MAX;
+        for (int k = maxk; k >= 1; --k) {
+            const int64_t rows = ((R + 32 * k - 1) / (32 * k)) * 32 * k;
+            if (rows < best_rows) best_rows = rows, best_k = k;
+        }
+        return best_k;
+    };
+    int64_t kcount[kPdMaxK32 + 1] = {0};
+    for (int64_t g = 0; g < b.n_regions; g++)
+        for (int64_t r = rro[g]; r < rro[g + 1]; r++) kcount[pick_k(o[r + 1] - o[r])] += rho[g + 1] - rho[g];
+    int64_t kbegin[kPdMaxK32 + 2] = {0};
+    for (int kk = 1; kk <= maxk; kk++) kbegin[kk + 1] = kbegin[kk] + kcount[kk];
+    int64_t kpos[kPdMaxK32 + 1];
+    for (int kk = 1; kk <= maxk; kk++) kpos[kk] = kbegin[kk];
+    for (int64_t g = 0; g < b.n_regions; g++)
+        for (int64_t r = rro[g]; r < rro[g + 1]; r++) {
+            const int kk = pick_k(o[r + 1] - o[r]);
+            for (int64_t h = rho[g]; h < rho[g + 1]; h++) b.h_fp64all.p[kpos[kk]++] = PairRef{(int32_t)r, (int32_t)h};
+        }
+    const int64_t k = kbegin[maxk + 1];
+    int bpsm = 0;
+    if (pd_kernel_occupancy(&bpsm) != 0 || bpsm <= 0) bpsm = 1;
+    const int grid = ctx->sm_count * bpsm;
+    const size_t scr = (size_t)grid * (kBlock / 32) * (size_t)std::max(b.max_hap_len, 1) * 6;
+    GHMM_CUDA(b.d_scratch64.reserve(scr), "device PD strip scratch");
+    b.dev.scratch64 = b.d_scratch64.p;
+    b.dev.scratch64_cols = std::max(b.max_hap_len, 1);
+    if (!b.events_ready) {
+        for (auto &e : b.ev) GHMM_CUDA(cudaEventCreate(&e), "cudaEventCreate");
+        b.events_ready = true;
+    }
+    GHMM_CUDA(cudaEventRecord(b.ev[0], s), "event");
+    if (k > 0)
+        GHMM_CUDA(cudaMemcpyAsync(b.d_rerun.p, b.h_fp64all.p, (size_t)k * sizeof(PairRef), cudaMemcpyHostToDevice, s),
+                  "H2D PD pairs");
+    int32_t *hc = b.h_counters.p;
+    for (int i = 0; i < kNumCounters + 2 * kNumBucketKeys; i++) hc[i] = 0;
+    hc[1] = (int32_t)k;
+    GHMM_CUDA(cudaMemcpyAsync(b.d_counters.p, hc, (kNumCounters + 2 * kNumBucketKeys) * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, s), "H2D counters");
+    GHMM_CUDA(cudaEventRecord(b.ev[1], s), "event");
+    int launches = 0;
+    for (int kk = maxk; kk >= 1; --kk) {  // longest strips first
+        if (kcount[kk] == 0) continue;
+        const int cursor = (fp32 ? kCounterPdF32Base : kCounterPdBase) + kk;
+        int e = launch_pd(ctx->tables, b.dev, b.pd, kk, fp32, (int)kbegin[kk], (int)kcount[kk], cursor, nullptr, grid, s);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "PD-HMM launch");
+        launches++;
+    }
+    GHMM_CUDA(cudaEventRecord(b.ev[4], s), "event");
+    if (fp32 && k > 0) {  // the FP32 pass's underflows, queued at rerun[capacity..), in FP64
+        int e = launch_pd(ctx->tables, b.dev, b.pd, kPdMaxK, false, (int)b.dev.rerun_capacity, 0,
+                          kCounterPdRerunCursor, b.d_counters.p + kCounterPdRerun, grid, s);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "PD-HMM FP64 rerun launch");
+        launches++;
+    }
+    GHMM_CUDA(cudaEventRecord(b.ev[2], s), "event");
+    GHMM_CUDA(cudaMemcpyAsync(hc, b.d_counters.p, kNumCounters * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
+              "D2H counters");
+    GHMM_CUDA(cudaEventRecord(b.ev[3], s), "event");
+    GHMM_CUDA(cudaEventSynchronize(b.ev[3]), "PD-HMM kernel");
+    float ms = 0, ms_a = 0, ms_b = 0;
+    cudaEventElapsedTime(&ms_a, b.ev[1], b.ev[4]);
+    cudaEventElapsedTime(&ms_b, b.ev[4], b.ev[2]);
+    b.ms_fp32 = fp32 ? ms_a : 0;
+    b.ms_fp64 = fp32 ? ms_b : ms_a + ms_b;
+    b.ms_plain = 0;
+    cudaEventElapsedTime(&ms, b.ev[0], b.ev[3]);
+    b.ms_total = ms;
+    b.last_mode = fp32 ? GHMM_MODE_PD_FP32 : GHMM_MODE_PD;
+    b.last_launches = launches;
+    b.last_rerun = fp32 ? hc[kCounterPdRerun] : 0;
+    b.last_exact = 0;
+    b.forward_h2d = k * (int64_t)sizeof(PairRef) + (kNumCounters + 2 * kNumBucketKeys) * 4;
+    b.forward_d2h = kNumCounters * 4;
+    if (hc[3] == 1) return fail(ctx, GHMM_ERR_CUDA, "PD-HMM FP64 rerun queue overflow");
+    if (hc[3] != 0) return fail(ctx, GHMM_ERR_CUDA, "device-side scratch bound exceeded");
+    return GHMM_OK;
+}
+
+
+// PD regions of raw reads: the raw reads' view (checks, 45s and the constant GCP) as the regular raw path builds it,
+// then the PD marshal over it, the upload, and the read preparation on the device.
+int pd_raw_build(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions, int32_t n_regions, const ghmm_read_prep *prep,
+                        ghmm_batch &b) {
+    std::vector<ghmm_raw_region> rr((size_t)n_regions);
+    for (int32_t g = 0; g < n_regions; g++) {
+        const ghmm_pd_raw_region &rg = regions[g];
+        if (rg.n_haps < 0 || (rg.n_haps > 0 && !rg.haps)) return fail(ctx, GHMM_ERR_ARG, "bad PD region");
+        rr[(size_t)g] = ghmm_raw_region{rg.reads, rg.n_reads, nullptr, 0};
+    }
+    RawView v;
+    int rc = raw_view(ctx, rr.data(), n_regions, prep, v);
+    if (rc) return rc;
+    std::vector<ghmm_pd_region> pr((size_t)n_regions);
+    for (int32_t g = 0; g < n_regions; g++)
+        pr[(size_t)g] = ghmm_pd_region{v.regions[(size_t)g].reads, regions[g].n_reads, regions[g].haps, regions[g].n_haps};
+    rc = pd_marshal(ctx, pr.data(), n_regions, b);
+    if (!rc) rc = pd_upload(ctx, b, ctx->stream);
+    if (!rc) rc = raw_prepare_device(ctx, b, v.mapq.data(), v.max_len, prep, ctx->stream);
+    return rc;
+}
+
+
+
+}  // namespace rt
+}  // namespace ghmm
+
+extern "C" {
+
+int ghmm_pd_batch_create(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_t n_regions, ghmm_batch **out) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!out || n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad arguments");
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    auto *b = new ghmm_batch();
+    int rc = pd_marshal(ctx, regions, n_regions, *b);
+    if (!rc) rc = pd_upload(ctx, *b, ctx->stream);
+    if (!rc) rc = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? GHMM_OK : fail(ctx, GHMM_ERR_CUDA, "upload");
+    if (rc) {
+        b->release();
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return GHMM_OK;
+}
+
+int ghmm_pd_compute_regions(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_t n_regions, double *out) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad region array");
+    if (n_regions == 0) return GHMM_OK;
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    ghmm_batch &b = ctx->pd_batch;
+    int rc = pd_marshal(ctx, regions, n_regions, b);
+    if (!rc) rc = pd_upload(ctx, b, ctx->stream);
+    if (!rc) rc = batch_forward(ctx, b, ctx->double_precision ? GHMM_MODE_PD : GHMM_MODE_PD_FP32);
+    if (!rc) rc = batch_results(ctx, b, out);
+    return rc;
+}
+
+int ghmm_pd_batch_create_raw(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions, int32_t n_regions,
+                             const ghmm_read_prep *prep, ghmm_batch **out) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (!out || n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad arguments");
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    auto *b = new ghmm_batch();
+    int rc = pd_raw_build(ctx, regions, n_regions, prep, *b);
+    if (!rc) rc = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? GHMM_OK : fail(ctx, GHMM_ERR_CUDA, "upload");
+    if (rc) {
+        b->release();
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return GHMM_OK;
+}
+
+int ghmm_pd_compute_regions_raw(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions, int32_t n_regions,
+                                const ghmm_read_prep *prep, double *out) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad region array");
+    if (n_regions == 0) return GHMM_OK;
+    GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    ghmm_batch &b = ctx->pd_batch;
+    int rc = pd_raw_build(ctx, regions, n_regions, prep, b);
+    if (!rc) rc = batch_forward(ctx, b, ctx->double_precision ? GHMM_MODE_PD : GHMM_MODE_PD_FP32);
+    if (!rc) rc = batch_results(ctx, b, out);
+    return rc;
+}
+
+int ghmm_pd_compute_likelihoods(ghmm_ctx *ctx, const ghmm_read *reads, int32_t n_reads, const ghmm_pd_hap *haps,
+                                int32_t n_haps, double *out) {
+    if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
+    if (n_reads == 0 || n_haps == 0) return GHMM_OK;
+    ghmm_pd_region r{reads, n_reads, haps, n_haps};
+    return ghmm_pd_compute_regions(ctx, &r, 1, out);
+}
+
+
+}  // extern "C"
