@@ -273,6 +273,12 @@ int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
     parallel_for(n_parts, threads, [&](int64_t part) {
         PartOut &po = parts[(size_t)part];
         std::vector<std::pair<int64_t, int64_t>> groups;  // ((key, strips, length), read)
+        struct ReadPair {
+            int key;
+            int64_t a, b;  // b < 0: a single read
+        };
+        std::vector<ReadPair> pairs;
+        std::vector<std::pair<int, int64_t>> leftovers;  // (key, read) of the single-strip classes' odd reads
         std::vector<std::pair<int64_t, int64_t>> chunks;  // haplotype ranges of one task
         for (int64_t g = G * part / n_parts; g < G * (part + 1) / n_parts; g++) {
             const int64_t h0 = rho[(size_t)g], h1 = rho[(size_t)g + 1];
@@ -314,6 +320,11 @@ int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                 chunks.emplace_back(a, e);
                 a = e;
             }
+            // neighbours of one class share a task; the single-strip classes' leftovers (one read of each class with
+            // an odd count) then pair up with each other from the largest K down, each pair at the larger K (the
+            // shorter read gets more dummy rows above it), so a region keeps at most one half-empty task
+            pairs.clear();
+            leftovers.clear();
             for (size_t i = 0; i < groups.size();) {
                 const int64_t cls = groups[i].first / 100000;
                 const int key = (int)(cls / 4096);
@@ -321,6 +332,23 @@ int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
                 int64_t rb = -1;
                 if (i + 1 < groups.size() && groups[i + 1].first / 100000 == cls) rb = groups[i + 1].second;
                 i += (rb >= 0) ? 2 : 1;
+                if (rb < 0 && !(key & 16))
+                    leftovers.emplace_back(key, ra);
+                else
+                    pairs.push_back(ReadPair{key, ra, rb});
+            }
+            for (size_t i = leftovers.size(); i > 0;) {  // ascending keys: pair from the top
+                if (i >= 2) {
+                    pairs.push_back(ReadPair{leftovers[i - 1].first, leftovers[i - 1].second, leftovers[i - 2].second});
+                    i -= 2;
+                } else {
+                    pairs.push_back(ReadPair{leftovers[0].first, leftovers[0].second, -1});
+                    i -= 1;
+                }
+            }
+            for (const ReadPair &rp : pairs) {
+                const int key = rp.key;
+                const int64_t ra = rp.a, rb = rp.b;
                 const int K = key & 15;
                 const bool multi = (key & 16) != 0;
                 const int S = 32 * K;

@@ -10,8 +10,11 @@
 // LoglessPairHMM.initializePriors (:79-93).  This is the parameter space of the DRAGstr model, whose per-(period,
 // repeat) GOP/GCP tables (DragstrParams.java:49-117) set g and c of each read position.
 //
-// Kernel.  One warp per (read, haplotype) pair, K rows per lane (reads up to 256 bases, single strip), the
-// anti-diagonal wavefront of the forward kernels: lane l computes column s - l at step s.
+// Kernel.  One warp per (read, haplotype) pair, K rows per lane (reads up to 256 bases in one strip of 32 K rows;
+// longer reads in strips of 256 rows, K = 8), the anti-diagonal wavefront of the forward kernels: lane l computes
+// column s - l at step s.  A strip's last row (M, I, D per column) is kept in scratch as the next strip's row above;
+// the backward runs the strips last to first, and the adjoint values a strip's first row hands the row above are
+// kept in scratch per column for the strip above it.
 //  * Forward: the whole warp front (each lane's K rows of M, I, D plus the diagonal inputs) is saved to scratch
 //    every kSeg steps (the checkpoints); lane 31 sums the last row into L_s (scaled likelihood).
 //  * Backward: segments are processed last to first.  Each segment's forward is recomputed from its checkpoint,
@@ -110,9 +113,11 @@ struct Front {
 };
 
 // One forward step; returns the "up" values (row above at this lane's column) through uM/uI/uD.
+// pad: dummy rows above the strip's first row (the read's top padding in strip 0, <= 0 in later strips); bnd: the
+// previous strip's last row (M, I, D per column), or NULL in strip 0 (row 0: M = I = 0, D = scale / H).
 template <typename T, int K>
 __device__ __forceinline__ void fwd_step(const Rows<T, K> &w, Front<T, K> &f, const uint8_t *hb, int H, int s, int lane,
-                                         int pad, T init, T &uM, T &uI, T &uD) {
+                                         int pad, T init, const T *bnd, T &uM, T &uI, T &uD) {
     const int c = s - lane;
     const bool valid = c >= 0 && c < H;
     const uint32_t y = valid ? (uint32_t)hb[c] : 0x200u;
@@ -128,10 +133,16 @@ __device__ __forceinline__ void fwd_step(const Rows<T, K> &w, Front<T, K> &f, co
         f.gM = f.gI = (T)0;
         f.gD = (lane * K - 1 < pad) ? init : (T)0;
     }
-    if (lane == 0) {  // row 0: M = I = 0, D = scale / H
-        uM = (T)0;
-        uI = (T)0;
-        uD = init;
+    if (lane == 0) {
+        if (!bnd) {  // row 0: M = I = 0, D = scale / H
+            uM = (T)0;
+            uI = (T)0;
+            uD = init;
+        } else {  // the previous strip's last row at this column
+            uM = valid ? bnd[3 * c + 0] : (T)0;
+            uI = valid ? bnd[3 * c + 1] : (T)0;
+            uD = valid ? bnd[3 * c + 2] : (T)0;
+        }
     }
 #pragma unroll
     for (int k = K - 1; k >= 0; --k) {
@@ -155,7 +166,8 @@ __device__ __forceinline__ void fwd_step(const Rows<T, K> &w, Front<T, K> &f, co
     f.gD = uD;
 }
 
-// scratch layout per warp (all T): checkpoints [nck][3K+3][32], then segment fronts [kSeg][3K+3][32]
+// scratch layout per warp (all T): checkpoints [nck][3K+3][32], segment fronts [kSeg][3K+3][32], the strips' last
+// rows [nstrips - 1][H][3] (forward), and two buffers [H][4] of first-row adjoint values (backward, by strip parity)
 template <typename T, int K>
 __device__ __forceinline__ void save_front(T *dst, const Front<T, K> &f, int lane) {
 #pragma unroll
@@ -195,23 +207,44 @@ __device__ void calib_pair(const DevTables &TB, const ghmm_calib_batch &in, int6
         if (lane == 0) loglik[pair] = -INFINITY;
         return;
     }
-    const int pad = 32 * K - R;
+    constexpr int S = 32 * K;
+    const int nstrips = (R + S - 1) / S;
+    const int pad0 = nstrips * S - R;  // dummy rows above the read, in strip 0
     const uint8_t *hb = in.hap_bases + hoff;
     const T init = CalibScale<T>::init(H);
-    Rows<T, K> w;
-    load_rows<T, K>(TB, in, roff, R, pad, lane, w);
-    Front<T, K> f;
-#pragma unroll
-    for (int k = 0; k < K; ++k) f.M[k] = f.I[k] = f.D[k] = (T)0;
-    f.gM = f.gI = f.gD = (T)0;
     const int nsteps = H + 31;
+    const int nseg = (nsteps + kSeg - 1) / kSeg;
+    T *seg = scratch + (size_t)nseg * F * 32;
+    T *fwd_bnd = seg + (size_t)kSeg * F * 32;                 // [nstrips - 1][H][3]
+    T *adj_bnd = fwd_bnd + (size_t)(nstrips - 1) * H * 3;     // [2][H][4]
+    Rows<T, K> w;
+    Front<T, K> f;
+    // forward, strip by strip; checkpoints of the strip being run (the last strip's stay for its backward)
     T acc = (T)0;
-    for (int s = 0; s < nsteps; ++s) {
-        if (BACKWARD && s % kSeg == 0) save_front<T, K>(scratch + (size_t)(s / kSeg) * F * 32, f, lane);
-        T uM, uI, uD;
-        fwd_step<T, K>(w, f, hb, H, s, lane, pad, init, uM, uI, uD);
-        const int c = s - lane;
-        if (lane == 31 && c >= 0 && c < H) acc += f.M[K - 1] + f.I[K - 1];
+    for (int st = 0; st < nstrips; ++st) {
+        const int pad = pad0 - st * S;
+        const T *bnd = st ? fwd_bnd + (size_t)(st - 1) * H * 3 : nullptr;
+        T *bnd_out = fwd_bnd + (size_t)st * H * 3;
+        load_rows<T, K>(TB, in, roff, R, pad, lane, w);
+#pragma unroll
+        for (int k = 0; k < K; ++k) f.M[k] = f.I[k] = f.D[k] = (T)0;
+        f.gM = f.gI = f.gD = (T)0;
+        for (int s = 0; s < nsteps; ++s) {
+            if (BACKWARD && s % kSeg == 0) save_front<T, K>(scratch + (size_t)(s / kSeg) * F * 32, f, lane);
+            T uM, uI, uD;
+            fwd_step<T, K>(w, f, hb, H, s, lane, pad, init, bnd, uM, uI, uD);
+            const int c = s - lane;
+            if (lane == 31 && c >= 0 && c < H) {
+                if (st == nstrips - 1) {
+                    acc += f.M[K - 1] + f.I[K - 1];
+                } else {
+                    bnd_out[3 * c + 0] = f.M[K - 1];
+                    bnd_out[3 * c + 1] = f.I[K - 1];
+                    bnd_out[3 * c + 2] = f.D[K - 1];
+                }
+            }
+        }
+        __syncwarp();
     }
     const T Ls = __shfl_sync(kFullMask, acc, 31);
     const bool under = !(Ls >= (T)GHMM_FP32_RERUN_THRESHOLD) || !(Ls <= (T)FLT_MAX);
@@ -222,119 +255,153 @@ __device__ void calib_pair(const DevTables &TB, const ghmm_calib_batch &in, int6
     if (lane == 0) loglik[pair] = log10((double)Ls) - CalibScale<T>::log10_scale;
     if (!BACKWARD) return;
 
-    // ---------------- backward ----------------
+    // ---------------- backward, strips last to first ----------------
     const T seed = (T)weights[pair] / Ls;
-    T *seg = scratch + (size_t)((nsteps + kSeg - 1) / kSeg) * F * 32;
-    // adjoint state of this lane's rows at the previous reverse step (column c+1)
-    T gam[K], bI[K], bD[K];
-    T Ga[K], Gb[K], Ge[K], Gf[K], Gh[K], Gk[K];
+    for (int st = nstrips - 1; st >= 0; --st) {
+        const int pad = pad0 - st * S;
+        const T *bnd = st ? fwd_bnd + (size_t)(st - 1) * H * 3 : nullptr;
+        const bool last = st == nstrips - 1;
+        // the first-row adjoints of the strip below (read by lane 31) and of this strip (written by lane 0)
+        const T *adj_in = adj_bnd + (size_t)((st + 1) & 1) * H * 4;
+        T *adj_out = adj_bnd + (size_t)(st & 1) * H * 4;
+        if (!last) {  // this strip's checkpoints: its forward again, from the row above it
+            load_rows<T, K>(TB, in, roff, R, pad, lane, w);
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-        gam[k] = bI[k] = bD[k] = (T)0;
-        Ga[k] = Gb[k] = Ge[k] = Gf[k] = Gh[k] = Gk[k] = (T)0;
-    }
-    T dgA = (T)0, dgB = (T)0;  // from lane l+1: a*gamma, b*gamma of its row 0 at column c+1
-    T snA = (T)0, snB = (T)0, snE = (T)0, snF = (T)0;  // what this lane sent last reverse step
-    const int nseg = (nsteps + kSeg - 1) / kSeg;
-    for (int sg = nseg - 1; sg >= 0; --sg) {
-        const int s0 = sg * kSeg, s1 = min(s0 + kSeg, nsteps);
-        // recompute the segment's fronts (front after each step, plus the step's "up" values)
-        Front<T, K> r;
-        load_front<T, K>(scratch + (size_t)sg * F * 32, r, lane);
-        for (int s = s0; s < s1; ++s) {
-            T uM, uI, uD;
-            fwd_step<T, K>(w, r, hb, H, s, lane, pad, init, uM, uI, uD);
-            T *dst = seg + (size_t)(s - s0) * F * 32;
-            save_front<T, K>(dst, r, lane);  // gM/gI/gD slots now hold this step's up values
-        }
-        __syncwarp();
-        for (int s = s1 - 1; s >= s0; --s) {
-            const int c = s - lane;
-            const bool valid = c >= 0 && c < H;
-            // below (row under this lane's last row) at column c, and its a*gamma, b*gamma for column c
-            const T inE = __shfl_down_sync(kFullMask, snE, 1), inF = __shfl_down_sync(kFullMask, snF, 1);
-            const T inA = __shfl_down_sync(kFullMask, snA, 1), inB = __shfl_down_sync(kFullMask, snB, 1);
-            // forward values: column c (after step s) and c-1 (after step s-1)
-            Front<T, K> cur, prv;
-            load_front<T, K>(seg + (size_t)(s - s0) * F * 32, cur, lane);
-            if (s > s0) {
-                load_front<T, K>(seg + (size_t)(s - 1 - s0) * F * 32, prv, lane);
-            } else {
-                load_front<T, K>(scratch + (size_t)sg * F * 32, prv, lane);  // checkpoint = front before step s0
-                // the checkpoint's gM/gI/gD are the diagonal inputs of step s0 = up values of step s0-1
+            for (int k = 0; k < K; ++k) f.M[k] = f.I[k] = f.D[k] = (T)0;
+            f.gM = f.gI = f.gD = (T)0;
+            for (int s = 0; s < nsteps; ++s) {
+                if (s % kSeg == 0) save_front<T, K>(scratch + (size_t)(s / kSeg) * F * 32, f, lane);
+                T uM, uI, uD;
+                fwd_step<T, K>(w, f, hb, H, s, lane, pad, init, bnd, uM, uI, uD);
             }
-            if (c == 0) {  // the forward used the column-0 boundary as left and diagonal inputs here
+            __syncwarp();
+        }
+        // adjoint state of this lane's rows at the previous reverse step (column c+1)
+        T gam[K], bI[K], bD[K];
+        T Ga[K], Gb[K], Ge[K], Gf[K], Gh[K], Gk[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            gam[k] = bI[k] = bD[k] = (T)0;
+            Ga[k] = Gb[k] = Ge[k] = Gf[k] = Gh[k] = Gk[k] = (T)0;
+        }
+        T dgA = (T)0, dgB = (T)0;  // from the row below: a*gamma, b*gamma of its first row at column c+1
+        T snA = (T)0, snB = (T)0, snE = (T)0, snF = (T)0;  // what this lane sent last reverse step
+        const bool below = lane != 31 || !last;  // lane 31 of the last strip holds the read's last row
+        for (int sg = nseg - 1; sg >= 0; --sg) {
+            const int s0 = sg * kSeg, s1 = min(s0 + kSeg, nsteps);
+            // recompute the segment's fronts (front after each step, plus the step's "up" values)
+            Front<T, K> r;
+            load_front<T, K>(scratch + (size_t)sg * F * 32, r, lane);
+            for (int s = s0; s < s1; ++s) {
+                T uM, uI, uD;
+                fwd_step<T, K>(w, r, hb, H, s, lane, pad, init, bnd, uM, uI, uD);
+                T *dst = seg + (size_t)(s - s0) * F * 32;
+                save_front<T, K>(dst, r, lane);  // gM/gI/gD slots now hold this step's up values
+            }
+            __syncwarp();
+            for (int s = s1 - 1; s >= s0; --s) {
+                const int c = s - lane;
+                const bool valid = c >= 0 && c < H;
+                // below (row under this lane's last row) at column c, and its a*gamma, b*gamma for column c: from
+                // lane l+1, or for lane 31 from the first row of the strip below
+                T inE = __shfl_down_sync(kFullMask, snE, 1), inF = __shfl_down_sync(kFullMask, snF, 1);
+                T inA = __shfl_down_sync(kFullMask, snA, 1), inB = __shfl_down_sync(kFullMask, snB, 1);
+                if (lane == 31) {
+                    const bool have = !last && valid;
+                    inE = have ? adj_in[4 * c + 0] : (T)0;
+                    inF = have ? adj_in[4 * c + 1] : (T)0;
+                    inA = have ? adj_in[4 * c + 2] : (T)0;
+                    inB = have ? adj_in[4 * c + 3] : (T)0;
+                }
+                // forward values: column c (after step s) and c-1 (after step s-1)
+                Front<T, K> cur, prv;
+                load_front<T, K>(seg + (size_t)(s - s0) * F * 32, cur, lane);
+                if (s > s0) {
+                    load_front<T, K>(seg + (size_t)(s - 1 - s0) * F * 32, prv, lane);
+                } else {
+                    load_front<T, K>(scratch + (size_t)sg * F * 32, prv, lane);  // checkpoint = front before step s0
+                    // the checkpoint's gM/gI/gD are the diagonal inputs of step s0 = up values of step s0-1
+                }
+                if (c == 0) {  // the forward used the column-0 boundary as left and diagonal inputs here
+#pragma unroll
+                    for (int k = 0; k < K; ++k) {
+                        prv.M[k] = prv.I[k] = (T)0;
+                        prv.D[k] = (lane * K + k < pad) ? init : (T)0;
+                    }
+                    prv.gM = prv.gI = (T)0;
+                    prv.gD = (lane * K - 1 < pad) ? init : (T)0;
+                }
+                // up values of step s (row above at column c) and diagonal (column c-1)
+                const T upM = cur.gM, upI = cur.gI;
+                const T dgM = prv.gM, dgI = prv.gI, dgD = prv.gD;
+                const uint32_t y = valid ? (uint32_t)hb[c] : 0x200u;
+                const bool last_lane = lane == 31;
+                T newGam[K], newBI[K], newBD[K];
+                T belowE = below ? inE : (T)0, belowF = below ? inF : (T)0;  // e,f of row below times its betaI
+                T diagA = below ? dgA : (T)0, diagB = below ? dgB : (T)0;    // a,b of row below times gamma(c+1)
+#pragma unroll
+                for (int k = K - 1; k >= 0; --k) {
+                    T seedM = (T)0;
+                    if (last && last_lane && k == K - 1) seedM = seed;
+                    const T bD_new = diagB + w.k[k] * bD[k];
+                    const T bI_new = seedM + diagB + belowF;
+                    const T bM = seedM + diagA + belowE + w.h[k] * bD[k];
+                    const T pr = prior_of<T>(w.rb[k], y, w.pm[k], w.pe[k]);
+                    T g = pr * bM;
+                    T bi = bI_new, bd = bD_new;
+                    if (!valid) g = bi = bd = (T)0;
+                    newGam[k] = g;
+                    newBI[k] = bi;
+                    newBD[k] = bd;
+                    // forward neighbours of cell (row k, column c)
+                    const T mUp = k ? cur.M[k - 1] : upM, iUp = k ? cur.I[k - 1] : upI;
+                    const T mDg = k ? prv.M[k - 1] : dgM, iDg = k ? prv.I[k - 1] : dgI, dDg = k ? prv.D[k - 1] : dgD;
+                    Ga[k] += g * mDg;
+                    Gb[k] += g * (iDg + dDg);
+                    Ge[k] += bi * mUp;
+                    Gf[k] += bi * iUp;
+                    Gh[k] += bd * prv.M[k];
+                    Gk[k] += bd * prv.D[k];
+                    // for the row above (k-1) in this lane: this row's coefficients times its adjoints
+                    belowE = w.e[k] * bi;
+                    belowF = w.f[k] * bi;
+                    diagA = w.a[k] * gam[k];  // gamma of this row at column c+1 (previous reverse step)
+                    diagB = w.b[k] * gam[k];
+                }
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
-                    prv.M[k] = prv.I[k] = (T)0;
-                    prv.D[k] = (lane * K + k < pad) ? init : (T)0;
+                    gam[k] = newGam[k];
+                    bI[k] = newBI[k];
+                    bD[k] = newBD[k];
                 }
-                prv.gM = prv.gI = (T)0;
-                prv.gD = (lane * K - 1 < pad) ? init : (T)0;
+                // what the row above needs: row 0's e,f * betaI at column c (used now) and a,b * gamma at column c
+                snE = w.e[0] * bI[0];
+                snF = w.f[0] * bI[0];
+                snA = w.a[0] * gam[0];
+                snB = w.b[0] * gam[0];
+                if (lane == 0 && st > 0 && valid) {  // for lane 31 of the strip above
+                    adj_out[4 * c + 0] = snE;
+                    adj_out[4 * c + 1] = snF;
+                    adj_out[4 * c + 2] = snA;
+                    adj_out[4 * c + 3] = snB;
+                }
+                dgA = inA;  // the row below's a*gamma at column c becomes the diagonal input of column c-1
+                dgB = inB;
             }
-            // up values of step s (row above at column c) and diagonal (column c-1)
-            const T upM = cur.gM, upI = cur.gI;
-            const T dgM = prv.gM, dgI = prv.gI, dgD = prv.gD;
-            const uint32_t y = valid ? (uint32_t)hb[c] : 0x200u;
-            const bool last_lane = lane == 31;
-            T newGam[K], newBI[K], newBD[K];
-            T belowE = last_lane ? (T)0 : inE, belowF = last_lane ? (T)0 : inF;  // e,f of row below times its betaI
-            T diagA = last_lane ? (T)0 : dgA, diagB = last_lane ? (T)0 : dgB;    // a,b of row below times gamma(c+1)
+            __syncwarp();
+        }
+        // per-row parameter gradients of this strip: d(w log10 L)/dg and /dc
 #pragma unroll
-            for (int k = K - 1; k >= 0; --k) {
-                T seedM = (T)0;
-                if (last_lane && k == K - 1) seedM = seed;
-                const T bD_new = diagB + w.k[k] * bD[k];
-                const T bI_new = seedM + diagB + belowF;
-                const T bM = seedM + diagA + belowE + w.h[k] * bD[k];
-                const T pr = prior_of<T>(w.rb[k], y, w.pm[k], w.pe[k]);
-                T g = pr * bM;
-                T bi = bI_new, bd = bD_new;
-                if (!valid) g = bi = bd = (T)0;
-                newGam[k] = g;
-                newBI[k] = bi;
-                newBD[k] = bd;
-                // forward neighbours of cell (row k, column c)
-                const T mUp = k ? cur.M[k - 1] : upM, iUp = k ? cur.I[k - 1] : upI;
-                const T mDg = k ? prv.M[k - 1] : dgM, iDg = k ? prv.I[k - 1] : dgI, dDg = k ? prv.D[k - 1] : dgD;
-                Ga[k] += g * mDg;
-                Gb[k] += g * (iDg + dDg);
-                Ge[k] += bi * mUp;
-                Gf[k] += bi * iUp;
-                Gh[k] += bd * prv.M[k];
-                Gk[k] += bd * prv.D[k];
-                // for the row above (k-1) in this lane: this row's coefficients times its adjoints
-                belowE = w.e[k] * bi;
-                belowF = w.f[k] * bi;
-                diagA = w.a[k] * gam[k];  // gamma of this row at column c+1 (previous reverse step)
-                diagB = w.b[k] * gam[k];
+        for (int k = 0; k < K; ++k) {
+            const int p = lane * K + k - pad;
+            if (p >= 0) {
+                const T dg = w.eo[k] * (Ge[k] + Gh[k] - (T)2 * Ga[k]);
+                const T dc = w.ec[k] * (Gf[k] + Gk[k] - Gb[k]);
+                atomicAdd(grad_open + roff + p, (float)dg);
+                atomicAdd(grad_cont + roff + p, (float)dc);
             }
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                gam[k] = newGam[k];
-                bI[k] = newBI[k];
-                bD[k] = newBD[k];
-            }
-            // what the lane above needs: row 0's e,f * betaI at column c (used now) and a,b * gamma at column c
-            snE = w.e[0] * bI[0];
-            snF = w.f[0] * bI[0];
-            snA = w.a[0] * gam[0];
-            snB = w.b[0] * gam[0];
-            dgA = inA;  // lane l+1's a*gamma at column c becomes the diagonal input of column c-1
-            dgB = inB;
         }
         __syncwarp();
-    }
-    // per-row parameter gradients: d(w log10 L)/dg and /dc
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const int p = lane * K + k - pad;
-        if (p >= 0) {
-            const T dg = w.eo[k] * (Ge[k] + Gh[k] - (T)2 * Ga[k]);
-            const T dc = w.ec[k] * (Gf[k] + Gk[k] - Gb[k]);
-            atomicAdd(grad_open + roff + p, (float)dg);
-            atomicAdd(grad_cont + roff + p, (float)dc);
-        }
     }
 }
 
@@ -355,11 +422,13 @@ __global__ void __launch_bounds__(kCalibBlock) calib_kernel(DevTables TB, ghmm_c
 
 }  // namespace
 
-int64_t calib_scratch_per_warp(int k, int max_hap_len, bool fp64) {
+int64_t calib_scratch_per_warp(int k, int max_hap_len, int max_read_len, bool fp64) {
     const int64_t F = 3 * k + 3;
     const int64_t nsteps = max_hap_len + 31;
     const int64_t fronts = (nsteps + kSeg - 1) / kSeg + kSeg;
-    return fronts * F * 32 * (fp64 ? 8 : 4);
+    const int64_t nstrips = ((int64_t)max_read_len + 32 * k - 1) / (32 * k);
+    const int64_t boundaries = (nstrips - 1) * max_hap_len * 3 + 2 * (int64_t)max_hap_len * 4;
+    return (fronts * F * 32 + boundaries) * (fp64 ? 8 : 4);
 }
 
 int calib_grid(int sm_count) { return sm_count * 4; }

@@ -139,7 +139,8 @@ int launch_postprocess(const DevBatch &b, int64_t n_reads, const PostArgs &p, ui
                        cudaStream_t s);
 int measure_peaks_device(int sm_count, double *fp32, double *fp32x2, double *fp64, cudaStream_t s);
 // Calibration forward/backward (calib.cu).
-int64_t calib_scratch_per_warp(int k, int max_hap_len, bool fp64);
+int64_t calib_scratch_per_warp(int k, int max_hap_len, int max_read_len, bool fp64);
+constexpr int kCalibMaxRead = 65536;  // calibration reads: one strip up to 256 bases, strips of 256 rows beyond
 int calib_grid(int sm_count);
 int calib_block();
 int launch_calib(const DevTables &TB, const ghmm_calib_batch &in, int k, bool backward, bool fp64, void *scratch,

@@ -167,12 +167,13 @@ static int calib_run(ghmm_ctx *ctx, const ghmm_calib_batch *in, int precision, c
     if (precision < 0 || precision > 1) return fail(ctx, GHMM_ERR_ARG, "precision must be 0 (FP32 + FP64 redo) or 1 (FP64)");
     if (in->n_pairs < 0) return fail(ctx, GHMM_ERR_ARG, "negative pair count");
     if (in->n_pairs == 0) return GHMM_OK;
-    if (in->max_read_len < 1 || in->max_read_len > 256)
-        return fail(ctx, GHMM_ERR_ARG, "calibration supports reads of 1..256 bases (max_read_len)");
+    if (in->max_read_len < 1 || in->max_read_len > kCalibMaxRead)
+        return fail(ctx, GHMM_ERR_ARG, "calibration supports reads of 1..65536 bases (max_read_len)");
     if (in->max_hap_len < 1) return fail(ctx, GHMM_ERR_ARG, "max_hap_len must be >= 1");
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-    const int k = (in->max_read_len + 31) / 32;
-    const int64_t per_warp = calib_scratch_per_warp(k, in->max_hap_len, true);  // sized for the FP64 pass
+    // one strip of 32 k rows up to 256 bases, strips of 256 rows (k = 8) beyond
+    const int k = std::min((in->max_read_len + 31) / 32, 8);
+    const int64_t per_warp = calib_scratch_per_warp(k, in->max_hap_len, in->max_read_len, true);  // sized for FP64
     const int64_t warps = (int64_t)calib_grid(ctx->sm_count) * calib_block() / 32;
     if (backward) GHMM_CUDA(ctx->calib_scratch.reserve((size_t)(per_warp * warps)), "calibration scratch");
     GHMM_CUDA(ctx->calib_flags.reserve((size_t)in->n_pairs), "calibration flags");
@@ -192,7 +193,8 @@ static int calib_run(ghmm_ctx *ctx, const ghmm_calib_batch *in, int precision, c
         GHMM_CUDA(cudaStreamSynchronize(s), "H2D flags");
     } else {
         int e = launch_calib(ctx->tables, *in, k, backward, false, ctx->calib_scratch.p,
-                             calib_scratch_per_warp(k, in->max_hap_len, false), loglik, weights, gopen, gcont, flags,
+                             calib_scratch_per_warp(k, in->max_hap_len, in->max_read_len, false), loglik, weights,
+                             gopen, gcont, flags,
                              ctx->sm_count, s);
         if (e) return cuda_fail(ctx, (cudaError_t)e, "calibration FP32 launch");
     }

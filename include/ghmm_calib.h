@@ -39,7 +39,7 @@ typedef struct ghmm_calib_batch {
     const int32_t *pair_read, *pair_hap; /* [n_pairs] */
     const float *gap_open, *gap_cont;    /* per read position, indexed like the read planes */
     int64_t n_pairs;
-    int32_t max_read_len;                /* <= 256 */
+    int32_t max_read_len;                /* 1..65536: one strip up to 256 bases, strips of 256 rows beyond */
     int32_t max_hap_len;
 } ghmm_calib_batch;
 
@@ -50,7 +50,9 @@ int ghmm_calib_forward(ghmm_ctx *ctx, const ghmm_calib_batch *batch, int32_t pre
 /* Forward and hand-written backward.  d_loglik as above; d_grad_open / d_grad_cont (device, one float per
  * read position, accumulated into, so zero them first) receive sum_p w_p * d log10 L_p / d g (resp. c) with
  * w_p = d_weights[p] (device, NULL: all ones).  The forward is recomputed from checkpoints every 16 wavefront
- * steps during the backward sweep. */
+ * steps during the backward sweep; reads longer than 256 bases run in strips of 256 rows, whose boundary rows
+ * (forward) and first-row adjoints (backward) pass through per-warp scratch, the backward taking the strips last
+ * to first. */
 int ghmm_calib_backward(ghmm_ctx *ctx, const ghmm_calib_batch *batch, int32_t precision, const double *d_weights,
                         double *d_loglik, float *d_grad_open, float *d_grad_cont);
 

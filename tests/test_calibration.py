@@ -120,6 +120,57 @@ def test_theta_gradient_matches_fp64_central_differences(calib):
                 assert abs(grad[k, comp] - fd) <= 1e-3 * max(abs(fd), 1e-2 * scale), (k, comp, grad[k, comp], fd)
 
 
+def _long_read_workload():
+    """Reads of one to four 256-row strips (and one short read in the same batch), some longer than their
+    haplotype, sampled with 2-4 % substitutions so that the FP32 pass underflows for some and redoes them in FP64."""
+    rng = np.random.default_rng(17)
+    regions = []
+    # (the reads stay within a few hundred decades of likelihood: far below that the oracle's unscaled FP64 adjoints
+    # underflow, while the kernel's, seeded with w / L, do not)
+    for R, H, sub in ((300, 420, 0.02), (513, 600, 0.03), (330, 300, 0.02), (1000, 1200, 0.04), (257, 257, 0.02),
+                      (256, 500, 0.02), (150, 900, 0.02), (2, 40, 0.0)):
+        base = rng.choice(list(b"ACGT"), size=H).astype(np.uint8)
+        start = int(rng.integers(0, max(1, H - R + 1)))
+        rd = np.concatenate([base[start:start + R], rng.choice(list(b"ACGT"), size=max(0, R - H)).astype(np.uint8)])[:R]
+        flip = rng.random(R) < sub
+        rd[flip] = rng.choice(list(b"ACGT"), size=int(flip.sum())).astype(np.uint8)
+        regions.append(([base.tobytes()], [(rd, rng.integers(10, 41, size=R), np.full(R, 45), np.full(R, 45),
+                                             np.full(R, 10))]))
+    return W.from_pairs(regions)
+
+
+@pytest.mark.gpu
+def test_reads_longer_than_one_strip_match_the_oracle(calib):
+    # the strips of a long read pass their last row down (forward) and their first row's adjoints up (backward)
+    torch, e, _, _ = calib
+    wl = _long_read_workload()
+    cs = C.CalibrationSet(wl)
+    assert cs.max_read_len == 1000
+    theta = C.default_theta()
+    g, c = cs.position_params(theta)
+    g = g.detach().requires_grad_(True)
+    c = c.detach().requires_grad_(True)
+    fn = C._function() if C._FN is None else C._FN
+    gn, cn = g.detach().cpu().numpy(), c.detach().cpu().numpy()
+    pr, _ = wl.pair_index()
+    refs = [_oracle_pair(wl, cs, gn, cn, p, grad=True) for p in range(cs.n_pairs)]
+    for precision, tol_l, tol_g in ((0, 1e-3, 1e-3), (1, 1e-9, 1e-6)):
+        g.grad = None
+        c.grad = None
+        ll = fn.apply(g, c, cs, e, precision)
+        ll.sum().backward()
+        lln = ll.detach().cpu().numpy()
+        gg, gc = g.grad.cpu().numpy(), c.grad.cpu().numpy()
+        for p in range(cs.n_pairs):
+            lref, dg, dc = refs[p]
+            assert abs(lln[p] - lref) <= tol_l, (p, precision, lln[p], lref)
+            r = int(pr[p])
+            a, b = int(wl.read_off[r]), int(wl.read_off[r + 1])
+            scale = max(np.abs(dg).max(), np.abs(dc).max())
+            assert np.abs(gg[a:b] - dg).max() <= tol_g * scale + 1e-9, (p, precision)
+            assert np.abs(gc[a:b] - dc).max() <= tol_g * scale + 1e-9, (p, precision)
+
+
 @pytest.mark.gpu
 def test_fit_increases_likelihood(calib):
     torch, e, wl, cs = calib
