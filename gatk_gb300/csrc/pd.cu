@@ -116,8 +116,8 @@ __global__ void __launch_bounds__(kPdBlock, (sizeof(V) == 4 && K <= 4) ? 4 : 3) 
             // tii doubles as DD (equal for read rows); a dummy row has tii = 1 so its D holds the row-0 value and its
             // I stays at the (zero) value above it
             // the prior is folded into M's coefficients: (prior x MM, prior x IM) for a match and a mismatch, so a
-            // cell's M costs one multiply and two fused multiply-adds (this part's FP64 pipe takes a DMUL or DADD
-            // for two DFMAs)
+            // cell's M costs one multiply and two fused multiply-adds (on this part a DMUL or DADD issues at about
+            // 0.85 of the DFMA rate)
             V mMM[K], mIM[K], eMM[K], eIM[K], tmi[K], tii[K], tmd[K];
             uint32_t rbase[K], rbit[K];
             bool first[K], dummy[K], rN[K];
