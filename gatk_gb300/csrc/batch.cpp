@@ -469,6 +469,7 @@ int batch_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
     GHMM_CUDA(b.d_scratch32.reserve(std::max<size_t>(s32, 1)), "device FP32 strip scratch");
     const size_t s64 = (size_t)b.fp64_grid * kWarpsPerBlock * (size_t)std::max(b.max_hap_len, 1) * 3;
     GHMM_CUDA(b.d_scratch64.reserve(s64), "device FP64 strip scratch");
+    GHMM_CUDA(b.d_read_scale.reserve((size_t)std::max<int64_t>(NR, 1)), "device read scales");
 
     GHMM_CUDA(cudaMemcpyAsync(b.d_planes.p, b.h_planes.p, (size_t)b.read_bytes * 5, cudaMemcpyHostToDevice, s), "H2D planes");
     GHMM_CUDA(cudaMemcpyAsync(b.d_hap.p, b.h_hap.p, (size_t)b.hap_bytes * 2 + 2 * kCodePad, cudaMemcpyHostToDevice, s),
@@ -513,6 +514,10 @@ int batch_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
     d.scratch32_cols = b.scratch32_cols;
     d.scratch64 = b.d_scratch64.p;
     d.scratch64_cols = std::max(b.max_hap_len, 1);
+    d.read_scale = b.d_read_scale.p;
+    // the FP32 pass's per-read scale from the uploaded planes (raw batches redo it after their preparation)
+    const int e = launch_read_scale(ctx->tables, d, NR, b.d_read_scale.p, ctx->sm_count, s);
+    if (e) return cuda_fail(ctx, (cudaError_t)e, "read scale launch");
     b.uploaded = true;
     return GHMM_OK;
 }

@@ -75,12 +75,16 @@ struct DevBatch {
     int64_t scratch32_cols;
     double *scratch64;          // FP64 multi-strip boundary: per resident warp, max_hap_len x 3 doubles
     int64_t scratch64_cols;
+    const float2 *read_scale;   // per read: (2^-(la - n), n) with la = log2 a_R of the FP32 pass, n = round(la)
 };
 
 // Kernel launchers (kernels.cu).  All return cudaError_t as int.
 int launch_fp32_bucket(const DevTables &t, const DevBatch &b, int key, int grid, int block, cudaStream_t s);
 int launch_fp64_queue(const DevTables &t, const DevBatch &b, int grid, int block, cudaStream_t s);
 int launch_finalize_fp32(double *out, const int64_t *n_out, int sm_count, cudaStream_t s);
+// Per-read log2 a_R of the FP32 pass (kernels.cu), into scale[n_reads]; after the read planes are final.
+int launch_read_scale(const DevTables &t, const DevBatch &b, int64_t n_reads, float2 *scale, int sm_count,
+                      cudaStream_t s);
 int launch_plain_region(const DevTables &t, const DevBatch &b, int region, int n_reads, int n_haps, int max_read_len,
                         cudaStream_t s);
 constexpr int kPlainMaxRead = 2048;

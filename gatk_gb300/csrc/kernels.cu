@@ -29,8 +29,9 @@
 //       D~ = fma(D~_left, DD_i, M~_left)
 //    with b_i = IM_i MI_{i-1} / (MM_i MM_{i-1}), c_i = IM_i MD_{i-1} / MM_i, e_i = II_i MI_{i-1} / (MI_i MM_{i-1})
 //    (MM_0 = MI_0 = MD_0 = 1) and  M_R + I_R = (M~_R + I~_R MI_R / MM_R) / a_R.  Only ratios of adjacent rows'
-//    coefficients appear; log2 a_R is summed per read.  Reads whose I~ could outgrow FP32 (steeply rising
-//    insertion penalties) or whose MM is 0 are sent to FP64 by the host.
+//    coefficients appear; log2 a_R is summed per read once per upload (read_scale_kernel, in FP64 and in an order
+//    fixed by the read, so a read's result is the same whatever task or batch it runs in).  Reads whose I~ could
+//    outgrow FP32 (steeply rising insertion penalties) or whose MM is 0 are sent to FP64 by the host.
 //    Scale 2^120; a sum below GHMM_FP32_RERUN_THRESHOLD (or not finite) queues the pair for FP64.
 //  * fp64_queue_kernel<K, RESCALED>: the FP64 wavefront, one pair per warp, used for reruns and
 //    double-precision mode: a rescaled tier (5 DP operations per cell) and an exact unscaled tier (scale
@@ -84,7 +85,7 @@ __device__ __constant__ uint32_t kBaseMask[kBases] = {1u, 2u, 4u, 8u, 15u};
 
 // Per-row coefficients of one read half (see header comment); dummy rows reproduce the row-0 boundary.
 struct RowCoef {
-    float pm, pe, b, c, e, dd, lmm;
+    float pm, pe, b, c, e, dd;
     uint32_t code;
 };
 
@@ -95,7 +96,6 @@ struct RowCoef {
 // columns H-2, H-1 and H), and no per-step accumulation is left in the wavefront.
 __device__ __forceinline__ RowCoef row_coef(const DevTables &T, const DevBatch &B, int64_t off, int R, int p) {
     RowCoef c;
-    c.lmm = 0.f;
     c.code = 0u;
     if (p < 0 || p > R + 1 || R == 0) {  // dummy row: holds the row-0 boundary
         c.pm = c.pe = 0.f;
@@ -135,7 +135,6 @@ __device__ __forceinline__ RowCoef row_coef(const DevTables &T, const DevBatch &
     c.c = im * md_p / mm;
     c.e = (p > 0) ? ii * mi_p / (mi * mm_p) : 0.f;
     c.dd = ii;
-    c.lmm = -log2f(mm);
     c.code = base_code(base);
     return c;
 }
@@ -143,10 +142,14 @@ __device__ __forceinline__ RowCoef row_coef(const DevTables &T, const DevBatch &
 // log2(GHMM_FP32_RERUN_THRESHOLD) = log2(1e-28)
 constexpr float kLog2Threshold = -93.01398f;
 
-// t = a_R (M_R + I_R) summed over the haplotype (scaled by 2^120), la = log2 a_R.  Accepted sums are stored raw
-// as the float pair (t, la) in the output slot; finalize_fp32_kernel turns them into log10 in FP64 with every lane
+// t = a_R (M_R + I_R) summed over the haplotype (scaled by 2^120); the read's scale (s, n) from read_scale_kernel
+// splits log2 a_R = n - log2 s into an integer n and a factor s in [2^-1/2, 2^1/2].  Accepted sums are stored raw
+// as the float pair (t s, n) in the output slot; finalize_fp32_kernel turns them into log10 in FP64 with every lane
 // busy, rather than one lane per warp running the FP64 log10 here on the 1/64-rate FP64 pipe.
-__device__ __forceinline__ void emit_fp32(const DevBatch &B, float t, float la, int read, int hap, int64_t out_index) {
+__device__ __forceinline__ void emit_fp32(const DevBatch &B, float t, float2 scale, int read, int hap,
+                                          int64_t out_index) {
+    t *= scale.x;
+    const float la = scale.y;
     const bool forced = B.force_rerun_every > 0 && out_index % B.force_rerun_every == 0;  // test hook
     if (t > 0.f && t <= FLT_MAX && log2f(t) - la >= kLog2Threshold && !forced) {
         reinterpret_cast<float2 *>(B.out)[out_index] = make_float2(t, la);
@@ -214,11 +217,9 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
         const int ncols = (int)(B.hap_off[task.hap_end] - col0);
         const uint8_t *stream = B.hap_code + col0;
         const int nstrips = MULTI ? task.nstrips : 1;
-        float2 la = zero2();  // log2 a_R of both reads, summed over strips
 
         for (int strip = 0; strip < nstrips; ++strip) {
             float2 cb[K], cc[K], ce[K], cdd[K];
-            float2 lsum = zero2();
             __syncwarp();  // the previous strip's steps have finished reading this warp's table
 #pragma unroll
             for (int k = 0; k < K; ++k) {
@@ -229,8 +230,6 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                 cc[k] = make_float2(a.c, b.c);
                 ce[k] = make_float2(a.e, b.e);
                 cdd[k] = make_float2(a.dd, b.dd);
-                lsum.x += a.lmm;
-                lsum.y += b.lmm;
 #pragma unroll
                 for (int h = 0; h < kBases; ++h) {
                     const uint32_t hm = kBaseMask[h];
@@ -238,12 +237,6 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                         make_float2((a.code & hm) ? a.pm : a.pe, (b.code & hm) ? b.pm : b.pe);
                 }
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                lsum.x += __shfl_xor_sync(kFull, lsum.x, o);
-                lsum.y += __shfl_xor_sync(kFull, lsum.y, o);
-            }
-            la = add2(la, lsum);
             // row-0 coefficients of the lane below (lane 31: of the next strip's first row), with which this lane
             // hands it its row 0's I~ and M~ inner sum instead of three raw states
             float2 b0n = shfl_down2(cb[0]), c0n = shfl_down2(cc[0]), e0n = shfl_down2(ce[0]);
@@ -374,8 +367,8 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                     if constexpr (CHK) {
                         if (lane == 31 && (code & kColLast)) {
                             const float2 t = add2(add2(Dp[K - 1], Mp[K - 1]), i_acc);
-                            emit_fp32(B, t.x, la.x, ra, hap, out_a + hap);
-                            if (rb >= 0) emit_fp32(B, t.y, la.y, rb, hap, out_b + hap);
+                            emit_fp32(B, t.x, __ldg(B.read_scale + ra), ra, hap, out_a + hap);
+                            if (rb >= 0) emit_fp32(B, t.y, __ldg(B.read_scale + rb), rb, hap, out_b + hap);
                         }
                     }
                 } else if (MULTI && lane == 31 && valid) {
@@ -402,6 +395,27 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
                 for (; s < next_boundary; ++s) step(s, std::false_type{});
             }
             if (MULTI) __syncwarp();
+        }
+    }
+}
+
+// Per read: log2 a_R = sum over its positions of -log2 MM (the FP32 pass's row rescaling, with the float
+// matchToMatch values its coefficients use), summed in FP64 in an order fixed by the read alone, so that a read's
+// result does not depend on the task, rows per lane or batch it runs in.  Stored as (2^-(la - n), n), n = round(la).
+// One warp per read; computed once per upload (after the read preparation for raw batches).
+__global__ void read_scale_kernel(DevTables T, DevBatch B, int64_t n_reads, float2 *scale) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_reads;
+         r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const int64_t off = B.read_off[r], len = B.read_off[r + 1] - off;
+        double la = 0.0;
+        for (int64_t p = lane; p < len; p += 32)
+            la -= log2((double)__ldg(T.m2m_f + B.ins[off + p] * 128 + B.dels[off + p]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) la += __shfl_xor_sync(kFull, la, o);
+        if (lane == 0) {
+            const double n = rint(la);
+            scale[r] = make_float2((float)exp2(n - la), (float)n);
         }
     }
 }
@@ -848,6 +862,15 @@ int launch_fp64_queue(const DevTables &t, const DevBatch &b, int grid, int block
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return (int)e;
     fp64_queue_kernel<kMaxK64, false><<<grid, block, 0, s>>>(t, b);
+    return (int)cudaGetLastError();
+}
+
+int launch_read_scale(const DevTables &t, const DevBatch &b, int64_t n_reads, float2 *scale, int sm_count,
+                      cudaStream_t s) {
+    if (n_reads <= 0) return 0;
+    const int64_t want = (n_reads + 7) / 8;  // 8 warps per 256-thread block
+    read_scale_kernel<<<(int)(want < (int64_t)sm_count * 8 ? want : (int64_t)sm_count * 8), 256, 0, s>>>(t, b, n_reads,
+                                                                                                          scale);
     return (int)cudaGetLastError();
 }
 

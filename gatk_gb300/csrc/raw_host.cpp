@@ -179,6 +179,9 @@ int raw_prepare_device(ghmm_ctx *ctx, ghmm_batch &b, const int32_t *mapq, int32_
     const int e = p.dragstr ? launch_dragstr(b.dev, NR, p, ctx->sm_count, s) : launch_prep(b.dev, NR, p, ctx->sm_count, s);
     if (e) return cuda_fail(ctx, (cudaError_t)e, p.dragstr ? "DRAGstr imputation launch" : "read preparation launch");
     GHMM_CUDA(cudaEventRecord(b.ev_prep[1], s), "event");
+    // the gap penalties changed: the FP32 pass's per-read scale again
+    const int e2 = launch_read_scale(ctx->tables, b.dev, NR, b.d_read_scale.p, ctx->sm_count, s);
+    if (e2) return cuda_fail(ctx, (cudaError_t)e2, "read scale launch");
     b.prep_timed = true;
     b.upload_bytes += NR * 4;
     return GHMM_OK;

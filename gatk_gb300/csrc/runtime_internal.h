@@ -98,6 +98,7 @@ struct ghmm_batch {
     PdPlanes pd{};
     DevBuf<float2> d_scratch32;
     DevBuf<double> d_scratch64;
+    DevBuf<float2> d_read_scale;  // per read: the FP32 pass's log2 a_R as (2^-(la - n), n), from launch_read_scale
     // sizes
     int64_t n_regions = 0, n_reads = 0, n_haps = 0, read_bytes = 0, hap_bytes = 0, n_out = 0;
     int64_t n_cells = 0;
@@ -148,7 +149,8 @@ struct ghmm_batch {
         h_init_d.release(); h_tasks.release(); h_direct.release(); h_fp64all.release(); h_out.release(); h_counters.release();
         d_planes.release(); d_hap.release(); d_off.release(); d_read_region.release(); d_init_f.release();
         d_init_d.release(); d_tasks.release(); d_rerun.release(); d_out.release(); d_counters.release();
-        d_scratch32.release(); d_scratch64.release(); d_post.release(); h_pd.release(); d_pd.release();
+        d_scratch32.release(); d_scratch64.release(); d_read_scale.release(); d_post.release(); h_pd.release();
+        d_pd.release();
         h_mapq.release(); d_mapq.release(); h_dragstr.release(); d_dragstr.release();
         has_pd = false;
     }

@@ -198,6 +198,23 @@ def test_tunings_agree_with_oracle(tuning):
         assert _absdiff(got[under], ref[under]).max() <= TOL64
 
 
+def test_results_do_not_depend_on_launch_shape():
+    # a read's FP32 result is the same bits whatever rows per lane, strips, haplotype chunks or task partner it gets
+    # (its row rescaling log2 a_R is summed by the read alone, dummy rows above it reproduce the row-0 boundary)
+    wl = W.generate(1, regions=30)
+    outs = []
+    for tuning in ((8, 8, 16384), (4, 2, 1000), (6, 3, 300), (2, 1, 64)):
+        e = Engine()
+        try:
+            e.set_tuning(*tuning)
+            outs.append(_run(e, wl, native.MODE_FP32_RERUN)[0])
+        finally:
+            e.close()
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+    assert _absdiff(outs[0], _oracle_all(wl)).max() <= TOL32
+
+
 def test_reads_longer_than_haplotypes_across_haplotype_boundaries(engine):
     # Every haplotype but the last hands the wavefront to the next one mid-warp; reads longer than the
     # haplotypes make the insertion chain at each haplotype's last column dominate the likelihood.
