@@ -30,6 +30,7 @@ struct DevTables {
     const double *prob_d;
     const double *err3_d;
     const double *m2m_d;
+    const double *lm2m_d;   // [128*128] -log2(m2m_f), the FP32 pass's row rescaling exponent
 };
 
 // Read-pair task of the FP32 pass: two reads of one region (b < 0: single read) against the

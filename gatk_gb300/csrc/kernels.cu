@@ -400,7 +400,8 @@ __global__ void __launch_bounds__(128, Fp32MinBlocks<K>::value) fp32_bucket_kern
 }
 
 // Per read: log2 a_R = sum over its positions of -log2 MM (the FP32 pass's row rescaling, with the float
-// matchToMatch values its coefficients use), summed in FP64 in an order fixed by the read alone, so that a read's
+// matchToMatch values its coefficients use, from a host-built FP64 table), summed in FP64 in an order fixed by the
+// read alone, so that a read's
 // result does not depend on the task, rows per lane or batch it runs in.  Stored as (2^-(la - n), n), n = round(la).
 // One warp per read; computed once per upload (after the read preparation for raw batches).
 __global__ void read_scale_kernel(DevTables T, DevBatch B, int64_t n_reads, float2 *scale) {
@@ -410,7 +411,7 @@ __global__ void read_scale_kernel(DevTables T, DevBatch B, int64_t n_reads, floa
         const int64_t off = B.read_off[r], len = B.read_off[r + 1] - off;
         double la = 0.0;
         for (int64_t p = lane; p < len; p += 32)
-            la -= log2((double)__ldg(T.m2m_f + B.ins[off + p] * 128 + B.dels[off + p]));
+            la += __ldg(T.lm2m_d + B.ins[off + p] * 128 + B.dels[off + p]);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) la += __shfl_xor_sync(kFull, la, o);
         if (lane == 0) {

@@ -153,6 +153,7 @@ int ghmm_initialize(const ghmm_args *args, ghmm_ctx **out) {
     ctx->tables.prob_d = dt->prob;
     ctx->tables.err3_d = dt->err3;
     ctx->tables.m2m_d = dt->m2m;
+    ctx->tables.lm2m_d = dt->lm2m;
     ctx->alive = true;
     *out = ctx;
     return GHMM_OK;

@@ -71,7 +71,10 @@ void build_host_tables(HostTables &t) {
         t.prob_f[q] = (float)t.prob[q];
         t.err3_f[q] = (float)t.err3[q];
     }
-    for (int k = 0; k < 128 * 128; k++) t.m2m_f[k] = (float)t.m2m[k];
+    for (int k = 0; k < 128 * 128; k++) {
+        t.m2m_f[k] = (float)t.m2m[k];
+        t.lm2m[k] = t.m2m_f[k] > 0.0f ? -std::log2((double)t.m2m_f[k]) : 0.0;  // MM = 0 reads never run in FP32
+    }
 }
 
 }  // namespace ghmm

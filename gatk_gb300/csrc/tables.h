@@ -10,6 +10,7 @@ struct HostTables {
     double m2m[128 * 128];
     float err_f[256], prob_f[256], err3_f[256];
     float m2m_f[128 * 128];
+    double lm2m[128 * 128];  // -log2(m2m_f): the FP32 pass's per-row rescaling exponent (kernels.cu read_scale_kernel)
 };
 
 void build_host_tables(HostTables &t);
