@@ -104,6 +104,24 @@ def test_stub_devices_write_every_output_once():
     assert "stub ok" in r.stdout
 
 
+def test_multi_device_argument_errors():
+    L = native.lib()
+    h = ctypes.c_void_p()
+    devs = (ctypes.c_int32 * 2)(0, 0)
+    a = native.Args(0, 0, 0, 0)
+    assert L.ghmm_multi_create(devs, 0, ctypes.byref(a), ctypes.byref(h)) == native.GHMM_ERR_ARG
+    assert L.ghmm_multi_create(None, 2, ctypes.byref(a), ctypes.byref(h)) == native.GHMM_ERR_ARG
+    sl = (native.MultiSlice * 2)()
+    assert L.ghmm_multi_plan(None, 3, 2, sl) == native.GHMM_ERR_ARG  # regions missing
+    assert L.ghmm_multi_plan(None, 0, 0, sl) == native.GHMM_ERR_ARG  # no device
+    assert L.ghmm_multi_plan(None, 0, 2, sl) == native.GHMM_OK       # nothing to split
+    assert [(s.read_begin, s.read_end, s.out_begin, s.out_end) for s in sl] == [(0, 0, 0, 0)] * 2
+    assert L.ghmm_multi_compute_regions(None, None, 0, None) == native.GHMM_ERR_STATE
+    assert L.ghmm_multi_destroy(None) == native.GHMM_OK
+    if not L.ghmm_load():  # without a usable GPU the real devices cannot be opened
+        assert L.ghmm_multi_create(devs, 2, ctypes.byref(a), ctypes.byref(h)) == native.GHMM_ERR_UNSUPPORTED
+
+
 def test_block_range_is_disjoint():
     assert sharding.block_range(10000, 0) == (0, 10000)
     assert sharding.block_range(10000, 3) == (30000, 40000)
