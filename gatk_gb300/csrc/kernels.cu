@@ -166,10 +166,12 @@ __device__ __forceinline__ void emit_fp32(const DevBatch &B, float t, float2 sca
 
 }  // namespace
 
-// Blocks of 128 threads the FP32 kernel asks ptxas to fit per SM (register budget 65536 / (128 * n)).
+// Blocks of 128 threads the FP32 kernel asks ptxas to fit per SM (register budget 65536 / (128 * n)).  K <= 5 fits
+// four without spilling (126 registers at K = 5: 0.4 % faster than three); K = 6 and 7 at four spill a little and
+// ran 1-2 % slower, K = 8 spills 600 bytes.
 template <int K>
 struct Fp32MinBlocks {
-    static constexpr int value = K >= 5 ? 3 : 4;
+    static constexpr int value = K >= 6 ? 3 : 4;
 };
 
 // The bucket's task range and cursor live in device memory (B.bucket_info, B.counters), so the launch
