@@ -305,7 +305,7 @@ def run_ours(args):
     tail_n = int(np.searchsorted(np.cumsum(cpr[::-1]), args.cpu_cells / 2)) + 1
     tail_n = max(0, min(tail_n, wl.n_regions - head_n))
     spans = [(0, head_n)] + ([(wl.n_regions - tail_n, wl.n_regions)] if tail_n else [])
-    # plus the regions holding the lowest results of the timed forward: the exact FP64 tier's pairs (log10 L < -500,
+    # plus the regions holding the lowest results of the timed forward: the exact FP64 tier's pairs (log10 L < -560,
     # and -Infinity where the reference's 2^1020 scale underflows too), when the workload has any
     region_of_out = np.repeat(np.arange(wl.n_regions), np.diff(wl.out_off))
     extra = []

@@ -94,8 +94,10 @@ constexpr int kAccRows = 2;
 // Zero bytes on both sides of the column-code plane, so the FP32 kernel may load a code one step ahead
 // (and lanes that have not started may load before the first column) without leaving the allocation.
 constexpr int kCodePad = 64;
-// Largest insertion-state growth bound G (I~ <= G max M~) the rescaled FP64 tier takes (headroom 2^60).
-constexpr double kMaxGrowth64 = 1e10;
+// Largest insertion-state growth bound G (I~ <= G max M~) the rescaled FP64 tier takes (headroom 2^60; the bound is a
+// worst case, and a pair whose rescaled states do overflow sums to a non-finite value and moves to the exact tier, so
+// this only keeps pairs that would almost surely overflow from running twice).
+constexpr double kMaxGrowth64 = 1e15;
 int fp32_kernel_occupancy(int k, int block, int *blocks_per_sm);
 int fp64_kernel_occupancy(int block, int *blocks_per_sm);
 

@@ -28,7 +28,7 @@ MODE_PD = 3
 MODE_PD_FP32 = 4
 INJECT_REFUSE_ALLOCATIONS = 1
 INJECT_FP64_RERUN_EVERY = 2
-FP64_RESCALED_FLOOR = -500.0  # GHMM_FP64_RESCALED_FLOOR
+FP64_RESCALED_FLOOR = -560.0  # GHMM_FP64_RESCALED_FLOOR
 MODE_PLAIN_FP64 = 2
 
 FP32_RERUN_THRESHOLD = 1e-28

@@ -56,7 +56,7 @@ extern "C" {
  * and LoglessPairHMM's unscaled recurrence (scale 2^1020) for pairs whose rescaled result falls below
  * log10 L = GHMM_FP64_RESCALED_FLOOR or is not finite, so results near the bottom of the FP64 range, and
  * -Infinity, come out as the reference computes them. */
-#define GHMM_FP64_RESCALED_FLOOR (-500.0)
+#define GHMM_FP64_RESCALED_FLOOR (-560.0)
 
 /* Forward modes for ghmm_batch_forward. */
 #define GHMM_MODE_PD 3         /* PD-HMM batch (ghmm_pd_batch_create): every pair in the FP64 PD-HMM kernel */
@@ -133,7 +133,7 @@ typedef struct ghmm_stats {
     double ms_host_marshal;   /* host time of the last marshal: copies into pinned planes, checks, routing */
     double ms_host_tasks;     /* host time of building and ordering the FP32 warp tasks */
     int64_t n_fp64_exact;     /* pairs of the last forward computed by the exact (unscaled, 2^1020) FP64 tier:
-                                 results of the rescaled FP64 tier below log10 L = -500, and host-marked reads */
+                                 results of the rescaled FP64 tier below log10 L = -560, and host-marked reads */
     double ms_prep;           /* raw batches: device time of the read preparation kernels of the upload (quality
                                  caps, PCR model or DRAGstr imputation); 0 for prepared batches */
     int64_t n_cells_fp64_direct; /* cells of the pairs the last forward sent to FP64 without an FP32 pass */

@@ -394,7 +394,7 @@ def test_peaks_are_sane(engine):
 
 def test_fp64_tiers_near_the_bottom_of_the_range(engine):
     # random reads against unrelated haplotypes at low base quality: log10 L from about -150 to below the
-    # FP64 range (-Infinity in LoglessPairHMM too); results below the rescaled tier's floor (-500) come
+    # FP64 range (-Infinity in LoglessPairHMM too); results below the rescaled tier's floor (-560) come
     # from the exact tier, and everything matches the oracle to the FP64 bar
     rng = np.random.default_rng(11)
     regions = []
