@@ -415,19 +415,21 @@ def test_fp64_tiers_near_the_bottom_of_the_range(engine):
         assert st["n_fp64_exact"] >= int((ref < native.FP64_RESCALED_FLOOR).sum()), mode
 
 
-def test_steep_insertion_penalties_route_to_the_exact_tier(engine):
-    # insertion penalty jumping 10 -> 127 between neighbours: the rescaled forms' I~ could outgrow their
-    # headroom, so the host sends the read to the exact FP64 tier
+def test_insertion_growth_routes_to_the_exact_tier(engine):
+    # the rescaled forms carry 1 / MI, so a read's insertion state can grow by err(gcp) err(ins_prev) / (err(ins) MM_prev)
+    # per row.  A read whose bound on that growth passes 1e15 (low, flat gap penalties: about 7e30 here) goes to the
+    # exact FP64 tier; one whose bound stays under it (an insertion penalty jumping 10 -> 127 at every other base: about
+    # 6e10) runs in the rescaled FP64 tier, inside its 2^60 headroom.  Both match the oracle to the FP64 bar.
     rng = np.random.default_rng(5)
     hap = _rand_seq(rng, 120)
     read = hap[20:90]
     ins = np.where(np.arange(70) % 2 == 0, 10, 127)
-    wl = W.from_pairs([_single(hap, read, ins=ins), _single(hap, read)])
+    wl = W.from_pairs([_single(hap, read, ins=ins), _single(hap, read, ins=4, dl=5, gcp=1), _single(hap, read)])
     ref = _oracle_all(wl)
     got, st = _run(engine, wl, native.MODE_FP32_RERUN)
-    assert st["n_fp64_exact"] == 1
-    assert _absdiff(got[:1], ref[:1]).max() <= TOL64
-    assert _absdiff(got[1:], ref[1:]).max() <= TOL32
+    assert st["n_fp64_exact"] == 1 and st["n_fp64_direct"] == 2
+    assert _absdiff(got[:2], ref[:2]).max() <= TOL64
+    assert _absdiff(got[2:], ref[2:]).max() <= TOL32
 
 
 @pytest.mark.gpu
