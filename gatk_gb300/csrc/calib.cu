@@ -193,7 +193,9 @@ __device__ __forceinline__ void load_front(const T *src, Front<T, K> &f, int lan
     f.gD = src[(3 * K + 2) * 32 + lane];
 }
 
-template <typename T, int K, bool BACKWARD>
+// MULTI: reads may need more than one strip (K = 8 batches with reads longer than 256 bases); otherwise every read fits
+// one strip and the strip logic folds away.
+template <typename T, int K, bool BACKWARD, bool MULTI>
 __device__ void calib_pair(const DevTables &TB, const ghmm_calib_batch &in, int64_t pair, T *scratch, double *loglik,
                            const double *weights, float *grad_open, float *grad_cont, int *need_fp64, bool fp64_pass) {
     constexpr int F = 3 * K + 3;  // values per lane in a front
@@ -208,7 +210,7 @@ __device__ void calib_pair(const DevTables &TB, const ghmm_calib_batch &in, int6
         return;
     }
     constexpr int S = 32 * K;
-    const int nstrips = (R + S - 1) / S;
+    const int nstrips = MULTI ? (R + S - 1) / S : 1;
     const int pad0 = nstrips * S - R;  // dummy rows above the read, in strip 0
     const uint8_t *hb = in.hap_bases + hoff;
     const T init = CalibScale<T>::init(H);
@@ -405,7 +407,7 @@ __device__ void calib_pair(const DevTables &TB, const ghmm_calib_batch &in, int6
     }
 }
 
-template <typename T, int K, bool BACKWARD>
+template <typename T, int K, bool BACKWARD, bool MULTI>
 __global__ void __launch_bounds__(kCalibBlock) calib_kernel(DevTables TB, ghmm_calib_batch in, T *scratch,
                                                             int64_t scratch_per_warp, double *loglik,
                                                             const double *weights, float *grad_open, float *grad_cont,
@@ -415,7 +417,8 @@ __global__ void __launch_bounds__(kCalibBlock) calib_kernel(DevTables TB, ghmm_c
     T *my = scratch + warp * scratch_per_warp;
     for (int64_t p = warp; p < in.n_pairs; p += nwarps) {
         if (fp64_pass && !need_fp64[p]) continue;
-        calib_pair<T, K, BACKWARD>(TB, in, p, my, loglik, weights, grad_open, grad_cont, need_fp64, fp64_pass != 0);
+        calib_pair<T, K, BACKWARD, MULTI>(TB, in, p, my, loglik, weights, grad_open, grad_cont, need_fp64,
+                                          fp64_pass != 0);
         __syncwarp();
     }
 }
@@ -438,41 +441,42 @@ int launch_calib(const DevTables &TB, const ghmm_calib_batch &in, int k, bool ba
                  int64_t scratch_bytes_per_warp, double *loglik, const double *weights, float *grad_open,
                  float *grad_cont, int *need_fp64, int sm_count, cudaStream_t s) {
     const int grid = calib_grid(sm_count);
-#define GHMM_CALIB(KK)                                                                                              \
-    case KK:                                                                                                        \
-        if (fp64) {                                                                                                 \
-            if (backward)                                                                                           \
-                calib_kernel<double, KK, true><<<grid, kCalibBlock, 0, s>>>(                                        \
-                    TB, in, (double *)scratch, scratch_bytes_per_warp / 8, loglik, weights, grad_open, grad_cont,   \
-                    need_fp64, 1);                                                                                  \
-            else                                                                                                    \
-                calib_kernel<double, KK, false><<<grid, kCalibBlock, 0, s>>>(                                       \
-                    TB, in, (double *)scratch, scratch_bytes_per_warp / 8, loglik, weights, grad_open, grad_cont,   \
-                    need_fp64, 1);                                                                                  \
-        } else {                                                                                                    \
-            if (backward)                                                                                           \
-                calib_kernel<float, KK, true><<<grid, kCalibBlock, 0, s>>>(                                         \
-                    TB, in, (float *)scratch, scratch_bytes_per_warp / 4, loglik, weights, grad_open, grad_cont,    \
-                    need_fp64, 0);                                                                                  \
-            else                                                                                                    \
-                calib_kernel<float, KK, false><<<grid, kCalibBlock, 0, s>>>(                                        \
-                    TB, in, (float *)scratch, scratch_bytes_per_warp / 4, loglik, weights, grad_open, grad_cont,    \
-                    need_fp64, 0);                                                                                  \
-        }                                                                                                           \
-        break;
+#define GHMM_CALIB_ONE(T, KK, BWD, MUL)                                                                             \
+    calib_kernel<T, KK, BWD, MUL><<<grid, kCalibBlock, 0, s>>>(TB, in, (T *)scratch,                                \
+                                                                scratch_bytes_per_warp / (int64_t)sizeof(T), loglik, \
+                                                                weights, grad_open, grad_cont, need_fp64, fp64 ? 1 : 0)
+#define GHMM_CALIB(KK, MUL)                                                                                         \
+    if (fp64) {                                                                                                     \
+        if (backward)                                                                                               \
+            GHMM_CALIB_ONE(double, KK, true, MUL);                                                                  \
+        else                                                                                                        \
+            GHMM_CALIB_ONE(double, KK, false, MUL);                                                                 \
+    } else {                                                                                                        \
+        if (backward)                                                                                               \
+            GHMM_CALIB_ONE(float, KK, true, MUL);                                                                   \
+        else                                                                                                        \
+            GHMM_CALIB_ONE(float, KK, false, MUL);                                                                  \
+    }
     switch (k) {
-        GHMM_CALIB(1)
-        GHMM_CALIB(2)
-        GHMM_CALIB(3)
-        GHMM_CALIB(4)
-        GHMM_CALIB(5)
-        GHMM_CALIB(6)
-        GHMM_CALIB(7)
-        GHMM_CALIB(8)
+        case 1: GHMM_CALIB(1, false) break;
+        case 2: GHMM_CALIB(2, false) break;
+        case 3: GHMM_CALIB(3, false) break;
+        case 4: GHMM_CALIB(4, false) break;
+        case 5: GHMM_CALIB(5, false) break;
+        case 6: GHMM_CALIB(6, false) break;
+        case 7: GHMM_CALIB(7, false) break;
+        case 8:
+            if (in.max_read_len > 32 * 8) {
+                GHMM_CALIB(8, true)
+            } else {
+                GHMM_CALIB(8, false)
+            }
+            break;
         default:
             return (int)cudaErrorInvalidValue;
     }
 #undef GHMM_CALIB
+#undef GHMM_CALIB_ONE
     return (int)cudaGetLastError();
 }
 
