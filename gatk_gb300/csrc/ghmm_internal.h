@@ -148,11 +148,11 @@ int measure_peaks_device(int sm_count, double *fp32, double *fp32x2, double *fp6
 // Calibration forward/backward (calib.cu).
 int64_t calib_scratch_per_warp(int k, int max_hap_len, int max_read_len, bool fp64);
 constexpr int kCalibMaxRead = 65536;  // calibration reads: one strip up to 256 bases, strips of 256 rows beyond
-int calib_grid(int sm_count);
+int calib_grid(int sm_count);  // blocks of a full grid; a call may launch fewer (scratch budget)
 int calib_block();
 int launch_calib(const DevTables &TB, const ghmm_calib_batch &in, int k, bool backward, bool fp64, void *scratch,
                  int64_t scratch_bytes_per_warp, double *loglik, const double *weights, float *grad_open,
-                 float *grad_cont, int *need_fp64, int sm_count, cudaStream_t s);
+                 float *grad_cont, int *need_fp64, int grid, int sm_count, cudaStream_t s);
 // Smith-Waterman (sw.cu).  Overhang strategies (SWOverhangStrategy) and BAM cigar op codes.
 constexpr int kSwSoftclip = 0, kSwIndel = 1, kSwLeadingIndel = 2, kSwIgnore = 3;
 constexpr uint32_t kSwOpM = 0, kSwOpI = 1, kSwOpD = 2, kSwOpS = 4;

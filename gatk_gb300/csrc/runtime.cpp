@@ -9,6 +9,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <condition_variable>
 #include <deque>
@@ -159,6 +160,17 @@ int ghmm_initialize(const ghmm_args *args, ghmm_ctx **out) {
     return GHMM_OK;
 }
 
+// Bytes of per-warp calibration scratch one call may hold: GHMM_CALIB_SCRATCH_BYTES, else 4 GiB.
+static int64_t calib_scratch_budget() {
+    const char *v = std::getenv("GHMM_CALIB_SCRATCH_BYTES");
+    if (v && *v) {
+        char *end = nullptr;
+        const long long b = std::strtoll(v, &end, 10);
+        if (end && *end == 0 && b > 0) return (int64_t)b;
+    }
+    return (int64_t)4 << 30;
+}
+
 // Calibration forward (+ backward): FP32 pass over every pair, then an FP64 pass over the pairs it flagged
 // (precision 0), or an FP64 pass over every pair (precision 1).
 static int calib_run(ghmm_ctx *ctx, const ghmm_calib_batch *in, int precision, const double *weights, double *loglik,
@@ -174,9 +186,18 @@ static int calib_run(ghmm_ctx *ctx, const ghmm_calib_batch *in, int precision, c
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     // one strip of 32 k rows up to 256 bases, strips of 256 rows (k = 8) beyond
     const int k = std::min((in->max_read_len + 31) / 32, 8);
+    // the backward keeps checkpoints in per-warp scratch, and a read of several strips passes each strip's last
+    // row through it in the forward too
+    const bool strips = in->max_read_len > 32 * 8;
     const int64_t per_warp = calib_scratch_per_warp(k, in->max_hap_len, in->max_read_len, true);  // sized for FP64
-    const int64_t warps = (int64_t)calib_grid(ctx->sm_count) * calib_block() / 32;
-    if (backward) GHMM_CUDA(ctx->calib_scratch.reserve((size_t)(per_warp * warps)), "calibration scratch");
+    const int64_t warps_per_block = calib_block() / 32;
+    int64_t blocks = calib_grid(ctx->sm_count);
+    if (backward || strips) {
+        // fewer warps (each taking more pairs) where long pairs would make a full grid's scratch exceed the budget
+        const int64_t budget = calib_scratch_budget();
+        blocks = std::max<int64_t>(1, std::min(blocks, budget / (per_warp * warps_per_block)));
+        GHMM_CUDA(ctx->calib_scratch.reserve((size_t)(per_warp * warps_per_block * blocks)), "calibration scratch");
+    }
     GHMM_CUDA(ctx->calib_flags.reserve((size_t)in->n_pairs), "calibration flags");
     cudaStream_t s = ctx->stream;
     if (backward && !weights) {
@@ -195,12 +216,11 @@ static int calib_run(ghmm_ctx *ctx, const ghmm_calib_batch *in, int precision, c
     } else {
         int e = launch_calib(ctx->tables, *in, k, backward, false, ctx->calib_scratch.p,
                              calib_scratch_per_warp(k, in->max_hap_len, in->max_read_len, false), loglik, weights,
-                             gopen, gcont, flags,
-                             ctx->sm_count, s);
+                             gopen, gcont, flags, (int)blocks, ctx->sm_count, s);
         if (e) return cuda_fail(ctx, (cudaError_t)e, "calibration FP32 launch");
     }
     int e = launch_calib(ctx->tables, *in, k, backward, true, ctx->calib_scratch.p, per_warp, loglik, weights, gopen,
-                         gcont, flags, ctx->sm_count, s);
+                         gcont, flags, (int)blocks, ctx->sm_count, s);
     if (e) return cuda_fail(ctx, (cudaError_t)e, "calibration FP64 launch");
     GHMM_CUDA(cudaStreamSynchronize(s), "calibration kernels");
     return GHMM_OK;

@@ -52,7 +52,9 @@ int ghmm_calib_forward(ghmm_ctx *ctx, const ghmm_calib_batch *batch, int32_t pre
  * w_p = d_weights[p] (device, NULL: all ones).  The forward is recomputed from checkpoints every 16 wavefront
  * steps during the backward sweep; reads longer than 256 bases run in strips of 256 rows, whose boundary rows
  * (forward) and first-row adjoints (backward) pass through per-warp scratch, the backward taking the strips last
- * to first. */
+ * to first.  The context holds that scratch (for the forward too when reads exceed 256 bases): at most
+ * GHMM_CALIB_SCRATCH_BYTES bytes (environment, read at each call; default 4 GiB), launching fewer warps, each
+ * taking more pairs, where long pairs would need more for a full grid. */
 int ghmm_calib_backward(ghmm_ctx *ctx, const ghmm_calib_batch *batch, int32_t precision, const double *d_weights,
                         double *d_loglik, float *d_grad_open, float *d_grad_cont);
 

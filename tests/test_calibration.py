@@ -172,6 +172,49 @@ def test_reads_longer_than_one_strip_match_the_oracle(calib):
 
 
 @pytest.mark.gpu
+def test_long_reads_forward_only_first_and_under_a_one_block_scratch_budget(monkeypatch):
+    # A fresh context's first calibration call is a forward without backward over reads of several strips: their
+    # boundary rows pass through scratch that this call itself has to reserve.  Then a scratch budget below one
+    # warp's need leaves a single block of two warps, which takes all eight pairs in turn, reusing its scratch.
+    torch = pytest.importorskip("torch")
+    from gatk_gb300.pairhmm import Engine
+
+    wl = _long_read_workload()
+    cs = C.CalibrationSet(wl)
+    theta = C.default_theta()
+    g, c = cs.position_params(theta)
+    gn, cn = g.detach().cpu().numpy(), c.detach().cpu().numpy()
+    refs = [_oracle_pair(wl, cs, gn, cn, p, grad=True) for p in range(cs.n_pairs)]
+    pr, _ = wl.pair_index()
+    e = Engine()
+    try:
+        with torch.no_grad():
+            for precision, tol in ((0, 1e-3), (1, 1e-9)):
+                ll = C.log10_likelihoods(theta, cs, e, precision=precision).cpu().numpy()
+                for p in range(cs.n_pairs):
+                    assert abs(ll[p] - refs[p][0]) <= tol, (p, precision, ll[p], refs[p][0])
+        monkeypatch.setenv("GHMM_CALIB_SCRATCH_BYTES", "1")
+        fn = C._function() if C._FN is None else C._FN
+        for precision, tol_l, tol_g in ((0, 1e-3, 1e-3), (1, 1e-9, 1e-6)):
+            gg = g.detach().clone().requires_grad_(True)
+            cc = c.detach().clone().requires_grad_(True)
+            ll = fn.apply(gg, cc, cs, e, precision)
+            ll.sum().backward()
+            lln = ll.detach().cpu().numpy()
+            dgn, dcn = gg.grad.cpu().numpy(), cc.grad.cpu().numpy()
+            for p in range(cs.n_pairs):
+                lref, dg, dc = refs[p]
+                assert abs(lln[p] - lref) <= tol_l, (p, precision)
+                r = int(pr[p])
+                a, b = int(wl.read_off[r]), int(wl.read_off[r + 1])
+                scale = max(np.abs(dg).max(), np.abs(dc).max())
+                assert np.abs(dgn[a:b] - dg).max() <= tol_g * scale + 1e-9, (p, precision)
+                assert np.abs(dcn[a:b] - dc).max() <= tol_g * scale + 1e-9, (p, precision)
+    finally:
+        e.close()
+
+
+@pytest.mark.gpu
 def test_fit_increases_likelihood(calib):
     torch, e, wl, cs = calib
     theta, hist = C.fit(cs, e, steps=8, lr=0.05)
