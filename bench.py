@@ -700,8 +700,9 @@ def run_calib(args):
 def run_pd(args):
     """--pd: the PD-HMM (LoglessPDPairHMM, DRAGEN-GATK mode) over workload 1's regions with synthetic
     partially-determined haplotypes (1-3 undetermined SNPs and 0-2 undetermined deletions per haplotype,
-    seeded).  Device-resident GCUPS of the default path (GHMM_MODE_PD_FP32: the FP32 PD kernel, pairs whose sums
-    underflow recomputed by the FP64 one) and of the all-FP64 path (GHMM_MODE_PD), e2e through
+    seeded).  Device-resident GCUPS of the default path (GHMM_MODE_PD_FP32: read-pair tasks in the packed FP32 PD
+    kernel, pairs without a task in the general FP32 one, pairs whose sums underflow recomputed by the FP64 one) and
+    of the all-FP64 path (GHMM_MODE_PD), e2e through
     ghmm_pd_compute_regions, accuracy and the CPU baseline against the FP64 PD oracle on the leading regions."""
     import numpy as np
 
@@ -769,10 +770,11 @@ def run_pd(args):
         "data": "synthetic (workload 1 regions with seeded PD flags)",
         "config": {"workload": f"first {n_regions} regions of workload 1 with 1-3 undetermined SNPs and 0-2 undetermined "
                                "deletions per haplotype", "regions": n_regions, "pairs": wl.n_pairs, "cells": cells,
-                   "mode": "GHMM_MODE_PD_FP32 (FP32 PD kernel, FP64 reruns of underflows)"},
+                   "mode": "GHMM_MODE_PD_FP32 (FP32 PD kernels, FP64 reruns of underflows)"},
         "roofline": {"bound": "fp32_fma_pipe", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                      "frac": achieved / peak32, "flop_per_cell": flop_per_cell,
-                     "kernel": "pd_kernel<float, K> (the FP32 pass)", "ms_fp32_pass": ms_fp32,
+                     "kernel": "pd_bucket_kernel<K> (read-pair tasks) and pd_kernel<float, K> (pairs without a task): the FP32 pass",
+                     "ms_fp32_pass": ms_fp32,
                      "ms_fp64_reruns": ms_rerun},
         "fp64_rerun": {"pairs": n_rerun, "fraction": n_rerun / max(1, wl.n_pairs)},
         "fp64_mode": {"value": cells / (ms64 * 1e-3) / 1e9, "unit": "GCUPS", "ms_per_step": ms64,

@@ -25,12 +25,12 @@ OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libghmm.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kernels.cu", "noalloc.cu", "calib.cu", "post.cu", "pd.cu", "prep.cu", "sw.cu"]
+CU_SOURCES = ["kernels.cu", "noalloc.cu", "calib.cu", "post.cu", "pd.cu", "pd_packed.cu", "prep.cu", "sw.cu"]
 CPP_SOURCES = ["runtime.cpp", "batch.cpp", "queue.cpp", "pd_host.cpp", "raw_host.cpp", "tables.cpp", "str_analyzer.cpp",
                "sw_host.cpp", "multi.cpp"]
 SYNTH_SOURCES = ["synth.cpp"]
 SYNTH_LIB = os.path.join(OUT_DIR, "libghmm_synth.so")
-HEADERS = ["ghmm_internal.h", "runtime_internal.h", "tables.h", "str_analyzer.h", "host_util.h"]
+HEADERS = ["fp32_rows.cuh", "ghmm_internal.h", "runtime_internal.h", "tables.h", "str_analyzer.h", "host_util.h"]
 
 
 def nvcc() -> str:

@@ -284,13 +284,13 @@ int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
             const int64_t h0 = rho[(size_t)g], h1 = rho[(size_t)g + 1];
             const int64_t r0 = rro[(size_t)g], r1 = rro[(size_t)g + 1];
             if (h1 == h0 || r1 == r0) continue;
-            bool region_fp64 = false;
+            bool region_fp64 = src.region_direct && src.region_direct[g];
             for (int64_t h = h0; h < h1; h++) region_fp64 |= (hap_flag[(size_t)h] != 0);
             const int64_t region_cols = hap_off[(size_t)h1] - hap_off[(size_t)h0];
             groups.clear();
             for (int64_t r = r0; r < r1; r++) {
                 const int R = (int)(read_off[(size_t)r + 1] - read_off[(size_t)r]);
-                if (region_fp64 || (read_flag[(size_t)r] & 1)) {
+                if (region_fp64 || (read_flag[(size_t)r] & 1) || (src.single_strip && R + kAccRows > 32 * max_k)) {
                     auto &dst = (read_flag[(size_t)r] & 4) ? po.direct_exact : po.direct;
                     for (int64_t h = h0; h < h1; h++) dst.push_back(PairRef{(int32_t)r, (int32_t)h});
                     po.cells_direct += (int64_t)R * region_cols;

@@ -107,7 +107,19 @@ int fp64_kernel_occupancy(int block, int *blocks_per_sm);
 struct PdPlanes {
     const uint8_t *flags;
     const uint8_t *states;
+    const uint8_t *ops;  // per column the packed FP32 kernel's op byte, indexed like hap_code (kCodePad zeros around)
 };
+// Op bits of the packed FP32 PD kernel (pd_packed.cu), derived per haplotype column by the host (pd_host.cpp).
+constexpr uint32_t kPdOpCopy = 1;       // NORMAL column whose branch state a later column reads: bX = previous X
+constexpr uint32_t kPdOpAfter = 2;      // AFTER_DEL column
+constexpr uint32_t kPdOpDelEnd = 4;     // DEL_END column: I reads max(bX, X) of the row above
+constexpr uint32_t kPdOpNextAfter = 8;  // the next column is AFTER_DEL
+constexpr uint32_t kPdOpSnp = 16;       // undetermined SNP: its alternative in bits 5-6 (A, C, G, T = 0..3)
+constexpr int kPdOpAltShift = 5;
+constexpr uint32_t kPdOpSnpAllBut = 128;  // with kPdOpSnp: three bases match, bits 5-6 name the fourth
+// FP32 PD read-pair tasks of bucket k (2..8 rows per lane, single strip) from the batch's task list.
+int launch_pd_bucket(const DevTables &t, const DevBatch &b, const uint8_t *ops, int k, int grid, cudaStream_t s);
+int pd_bucket_occupancy(int k, int *blocks_per_sm);
 int pd_kernel_occupancy(int *blocks_per_sm);
 // PD pairs [begin, begin + count) of the pair list (count_dev: the count in device memory), K rows per lane, in
 // FP32 (underflows queued for FP64 at rerun[rerun_capacity..)) or FP64; cursor is the counter the warps draw from.

@@ -49,10 +49,63 @@ bool pd_read_base_ok(uint8_t x) {
 }
 
 
-int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch &b) {
+// Whether the packed FP32 kernel (pd_packed.cu) can take a haplotype: its row-end state is NORMAL, so every row, the
+// first included, sees one state sequence.
+static bool pd_packable(const uint8_t *f, int H) {
+    int st = 0;
+    for (int j = 0; j < H; j++) {
+        if (st == 2) st = 0;
+        if (f[j] & 2) st = 1;
+        if (f[j] & 4) st = 2;
+    }
+    return st == 0;
+}
+
+// The packed kernel's op byte of every column of one haplotype (pd_packed.cu), from its flags f, its bytes y and the
+// state codes of pd_states (bits 2-3: the state of rows >= 2, equal to the first row's for a packable haplotype).
+// A column's branch state is needed when the next column is AFTER_DEL (it reads it), when the next column is
+// INSIDE_DEL and needs its own (it keeps it), or when the column ends a deletion (the row below's I reads it).  An
+// SNP column whose alternatives and base cover all four bases gets the column code of N in code (the column-code
+// plane), which matches every read base as isBasePDMatching then does.
+static void pd_ops(const uint8_t *f, const uint8_t *y, const uint8_t *states, int H, uint8_t *op, uint8_t *code) {
+    bool need_next = false;
+    for (int j = H - 1; j >= 0; --j) {
+        const int st = (states[j] >> 2) & 3;
+        const int st_next = j + 1 < H ? (states[j + 1] >> 2) & 3 : 0;
+        const bool del_end = (f[j] & 4) != 0;
+        const bool need = st_next == 2 || (st_next == 1 && need_next) || del_end;
+        uint32_t o = 0;
+        if (st == 0 && need) o |= kPdOpCopy;
+        if (st == 2) o |= kPdOpAfter;
+        if (del_end) o |= kPdOpDelEnd;
+        if (st_next == 2) o |= kPdOpNextAfter;
+        const int ref = base_index(y[j]);
+        const int alts = (f[j] >> 3) & 15;
+        if ((f[j] & 1) && ref < 4 && (alts & ~(1 << ref))) {  // (an N column matches every read base already)
+            const int match = alts | (1 << ref);  // bases A, C, G, T = bits 0..3 that match the column
+            const int n = ((match >> 0) & 1) + ((match >> 1) & 1) + ((match >> 2) & 1) + ((match >> 3) & 1);
+            if (n == 4) {
+                code[j] = (uint8_t)((code[j] & ~7u) | 4u);
+            } else if (n == 3) {
+                int u = 0;
+                while ((match >> u) & 1) ++u;
+                o |= kPdOpSnp | kPdOpSnpAllBut | ((uint32_t)u << kPdOpAltShift);
+            } else {
+                int alt = 0;
+                while (!((alts >> alt) & 1) || alt == ref) ++alt;
+                o |= kPdOpSnp | ((uint32_t)alt << kPdOpAltShift);
+            }
+        }
+        op[j] = (uint8_t)o;
+        need_next = need;
+    }
+}
+
+int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch &b, const RouteBound *bound) {
     std::vector<ghmm_region> rr((size_t)G);
     std::vector<std::vector<ghmm_hap>> hh((size_t)G);
     std::vector<const uint8_t *> pdp;
+    std::vector<uint8_t> region_direct((size_t)G, 0);
     for (int64_t g = 0; g < G; g++) {
         const ghmm_pd_region &rg = regs[g];
         if (rg.n_reads < 0 || rg.n_haps < 0 || (rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps))
@@ -63,19 +116,29 @@ int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch 
             if (hp.length > 0 && (!hp.bases || !hp.pd_bases)) return fail(ctx, GHMM_ERR_ARG, "NULL PD haplotype array");
             hh[(size_t)g][(size_t)h] = ghmm_hap{hp.bases, hp.length};
             pdp.push_back(hp.pd_bases);
+            if (hp.length > 0 && !pd_packable(hp.pd_bases, hp.length)) region_direct[(size_t)g] = 1;
         }
         rr[(size_t)g] = ghmm_region{rg.reads, rg.n_reads, hh[(size_t)g].data(), rg.n_haps};
     }
     Source src;
     src.regions = rr.data();
     src.n_regions = G;
+    src.bound = bound;
+    src.region_direct = region_direct.data();
+    src.single_strip = true;
     int rc = batch_marshal(ctx, src, b);
     if (rc) return rc;
     const int64_t NH = b.n_haps, HB = b.hap_bytes;
-    GHMM_CUDA(b.h_pd.reserve((size_t)std::max<int64_t>(2 * HB, 1)), "pinned PD planes");
+    // flags | states | kCodePad zeros | ops | kCodePad zeros
+    const int64_t pd_bytes = 3 * HB + 2 * kCodePad;
+    GHMM_CUDA(b.h_pd.reserve((size_t)pd_bytes), "pinned PD planes");
     const int64_t *o = b.h_off.p;
     const int64_t *hap_off = o + b.n_reads + 1;
-    uint8_t *flags = b.h_pd.p, *states = b.h_pd.p + HB;
+    uint8_t *flags = b.h_pd.p, *states = b.h_pd.p + HB, *ops = b.h_pd.p + 2 * HB + kCodePad;
+    memset(ops - kCodePad, 0, (size_t)kCodePad);
+    memset(ops + HB, 0, (size_t)kCodePad);
+    const uint8_t *hraw = b.h_hap.p;
+    uint8_t *hcode = b.h_hap.p + HB + kCodePad;
     parallel_for(NH, hw_threads(ctx->max_threads), [&](int64_t h) {
         const int64_t a = hap_off[h];
         const int H = (int)(hap_off[h + 1] - a);
@@ -87,11 +150,11 @@ int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch 
         pd_states(flags + a, H, end1, code, 2);
         for (int j = 0; j < H; j++)
             if (flags[a + j] & 4) code[j] |= 16;
+        pd_ops(flags + a, hraw + a, code, H, ops + a, hcode + a);
     });
     // a read base outside ACGTacgtN that meets an undetermined SNP column throws in the reference
     const int64_t *rro = o + b.n_reads + 1 + NH + 1, *rho = rro + G + 1;
     const uint8_t *bases = b.h_planes.p;
-    const uint8_t *hraw = b.h_hap.p;
     for (int64_t g = 0; g < G; g++)
         for (int64_t r = rro[g]; r < rro[g + 1]; r++)
             for (int64_t i = o[r]; i < o[r + 1]; i++) {
@@ -109,23 +172,25 @@ int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch 
 int pd_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
     int rc = batch_upload(ctx, b, s);
     if (rc) return rc;
-    const int64_t HB = b.hap_bytes;
-    GHMM_CUDA(b.d_pd.reserve((size_t)std::max<int64_t>(2 * HB, 1)), "device PD planes");
-    if (HB > 0)
-        GHMM_CUDA(cudaMemcpyAsync(b.d_pd.p, b.h_pd.p, (size_t)(2 * HB), cudaMemcpyHostToDevice, s), "H2D PD planes");
+    const int64_t HB = b.hap_bytes, pd_bytes = 3 * HB + 2 * kCodePad;
+    GHMM_CUDA(b.d_pd.reserve((size_t)pd_bytes), "device PD planes");
+    GHMM_CUDA(cudaMemcpyAsync(b.d_pd.p, b.h_pd.p, (size_t)pd_bytes, cudaMemcpyHostToDevice, s), "H2D PD planes");
     b.pd.flags = b.d_pd.p;
     b.pd.states = b.d_pd.p + HB;
-    b.upload_bytes += 2 * HB;
+    b.pd.ops = b.d_pd.p + 2 * HB + kCodePad;
+    b.upload_bytes += pd_bytes;
     return GHMM_OK;
 }
 
-// fp32: every pair in the FP32 PD kernel, then the pairs whose sums underflow in the FP64 one (K = 4 for all);
+// fp32: the read-pair tasks of the regular marshal through the packed FP32 kernel (pd_packed.cu) and the pairs without
+// a task through the general FP32 one (pd.cu), then the pairs whose FP32 sums underflow in the FP64 one (K = 4);
 // otherwise every pair in FP64
 int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32) {
     cudaStream_t s = ctx->stream;
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-    // every pair, grouped by the rows per lane K of its read (the strip height 32 K, K = 1..4, that needs the
-    // fewest rows; ties to the larger K, i.e. fewer strips), read-major per region within a group
+    // the general kernel's pairs (FP64: every pair; FP32: those without a task), grouped by the rows per lane K of the
+    // read (the strip height 32 K, K = 1..4, that needs the fewest rows; ties to the larger K, i.e. fewer strips), in
+    // region order within a group
     GHMM_CUDA(b.h_fp64all.reserve((size_t)std::max<int64_t>(b.n_out, 1)), "pinned PD pairs");
     const int64_t *o = b.h_off.p;
     const int64_t *rro = o + b.n_reads + 1 + b.n_haps + 1, *rho = rro + b.n_regions + 1;
@@ -139,18 +204,23 @@ int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32) {
         }
         return best_k;
     };
+    auto for_each_pair = [&](auto fn) {
+        if (fp32) {
+            const int64_t n = b.n_direct + b.n_direct_exact;
+            for (int64_t i = 0; i < n; i++) fn(b.h_direct.p[i]);
+        } else {
+            for (int64_t g = 0; g < b.n_regions; g++)
+                for (int64_t r = rro[g]; r < rro[g + 1]; r++)
+                    for (int64_t h = rho[g]; h < rho[g + 1]; h++) fn(PairRef{(int32_t)r, (int32_t)h});
+        }
+    };
     int64_t kcount[kPdMaxK32 + 1] = {0};
-    for (int64_t g = 0; g < b.n_regions; g++)
-        for (int64_t r = rro[g]; r < rro[g + 1]; r++) kcount[pick_k(o[r + 1] - o[r])] += rho[g + 1] - rho[g];
+    for_each_pair([&](const PairRef &p) { kcount[pick_k(o[p.read + 1] - o[p.read])]++; });
     int64_t kbegin[kPdMaxK32 + 2] = {0};
     for (int kk = 1; kk <= maxk; kk++) kbegin[kk + 1] = kbegin[kk] + kcount[kk];
     int64_t kpos[kPdMaxK32 + 1];
     for (int kk = 1; kk <= maxk; kk++) kpos[kk] = kbegin[kk];
-    for (int64_t g = 0; g < b.n_regions; g++)
-        for (int64_t r = rro[g]; r < rro[g + 1]; r++) {
-            const int kk = pick_k(o[r + 1] - o[r]);
-            for (int64_t h = rho[g]; h < rho[g + 1]; h++) b.h_fp64all.p[kpos[kk]++] = PairRef{(int32_t)r, (int32_t)h};
-        }
+    for_each_pair([&](const PairRef &p) { b.h_fp64all.p[kpos[pick_k(o[p.read + 1] - o[p.read])]++] = p; });
     const int64_t k = kbegin[maxk + 1];
     int bpsm = 0;
     if (pd_kernel_occupancy(&bpsm) != 0 || bpsm <= 0) bpsm = 1;
@@ -170,10 +240,33 @@ int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32) {
     int32_t *hc = b.h_counters.p;
     for (int i = 0; i < kNumCounters + 2 * kNumBucketKeys; i++) hc[i] = 0;
     hc[1] = (int32_t)k;
+    const bool packed = fp32 && b.n_tasks > 0;
+    if (packed)
+        for (auto &bk : b.buckets) {
+            hc[kNumCounters + bk.key] = bk.begin;
+            hc[kNumCounters + kNumBucketKeys + bk.key] = bk.count;
+        }
     GHMM_CUDA(cudaMemcpyAsync(b.d_counters.p, hc, (kNumCounters + 2 * kNumBucketKeys) * sizeof(int32_t),
                               cudaMemcpyHostToDevice, s), "H2D counters");
+    b.h_nout.p[0] = b.n_out;
+    if (packed)
+        GHMM_CUDA(cudaMemcpyAsync(b.d_nout.p, b.h_nout.p, sizeof(int64_t), cudaMemcpyHostToDevice, s), "H2D output count");
     GHMM_CUDA(cudaEventRecord(b.ev[1], s), "event");
     int launches = 0;
+    if (packed) {  // read-pair tasks, then the log10 epilogue of their sums (before the kernels that write log10)
+        for (auto &bk : b.buckets) {
+            int bp = 0;
+            if (pd_bucket_occupancy(bk.key, &bp) != 0 || bp <= 0) bp = 1;
+            const int64_t want = (bk.count + kWarpsPerBlock - 1) / kWarpsPerBlock;
+            const int g = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->sm_count * bp));
+            int e = launch_pd_bucket(ctx->tables, b.dev, b.pd.ops, bk.key, g, s);
+            if (e) return cuda_fail(ctx, (cudaError_t)e, "PD-HMM packed launch");
+            launches++;
+        }
+        int e = launch_finalize_fp32(b.dev.out, b.dev.n_out_dev, ctx->sm_count, s);
+        if (e) return cuda_fail(ctx, (cudaError_t)e, "PD-HMM FP32 finalize launch");
+        launches++;
+    }
     for (int kk = maxk; kk >= 1; --kk) {  // longest strips first
         if (kcount[kk] == 0) continue;
         const int cursor = (fp32 ? kCounterPdF32Base : kCounterPdBase) + kk;
@@ -182,7 +275,7 @@ int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32) {
         launches++;
     }
     GHMM_CUDA(cudaEventRecord(b.ev[4], s), "event");
-    if (fp32 && k > 0) {  // the FP32 pass's underflows, queued at rerun[capacity..), in FP64
+    if (fp32) {  // the FP32 pass's underflows, queued at rerun[capacity..), in FP64
         int e = launch_pd(ctx->tables, b.dev, b.pd, kPdMaxK, false, (int)b.dev.rerun_capacity, 0,
                           kCounterPdRerunCursor, b.d_counters.p + kCounterPdRerun, grid, s);
         if (e) return cuda_fail(ctx, (cudaError_t)e, "PD-HMM FP64 rerun launch");
@@ -205,7 +298,7 @@ int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32) {
     b.last_launches = launches;
     b.last_rerun = fp32 ? hc[kCounterPdRerun] : 0;
     b.last_exact = 0;
-    b.forward_h2d = k * (int64_t)sizeof(PairRef) + (kNumCounters + 2 * kNumBucketKeys) * 4;
+    b.forward_h2d = k * (int64_t)sizeof(PairRef) + (kNumCounters + 2 * kNumBucketKeys) * 4 + (packed ? 8 : 0);
     b.forward_d2h = kNumCounters * 4;
     if (hc[3] == 1) return fail(ctx, GHMM_ERR_CUDA, "PD-HMM FP64 rerun queue overflow");
     if (hc[3] != 0) return fail(ctx, GHMM_ERR_CUDA, "device-side scratch bound exceeded");
@@ -229,7 +322,7 @@ int pd_raw_build(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions, int32_t n_reg
     std::vector<ghmm_pd_region> pr((size_t)n_regions);
     for (int32_t g = 0; g < n_regions; g++)
         pr[(size_t)g] = ghmm_pd_region{v.regions[(size_t)g].reads, regions[g].n_reads, regions[g].haps, regions[g].n_haps};
-    rc = pd_marshal(ctx, pr.data(), n_regions, b);
+    rc = pd_marshal(ctx, pr.data(), n_regions, b, v.has_bound ? &v.bound : nullptr);
     if (!rc) rc = pd_upload(ctx, b, ctx->stream);
     if (!rc) rc = raw_prepare_device(ctx, b, v.mapq.data(), v.max_len, prep, ctx->stream);
     return rc;
@@ -247,7 +340,7 @@ int ghmm_pd_batch_create(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_t n
     if (!out || n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad arguments");
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     auto *b = new ghmm_batch();
-    int rc = pd_marshal(ctx, regions, n_regions, *b);
+    int rc = pd_marshal(ctx, regions, n_regions, *b, nullptr);
     if (!rc) rc = pd_upload(ctx, *b, ctx->stream);
     if (!rc) rc = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? GHMM_OK : fail(ctx, GHMM_ERR_CUDA, "upload");
     if (rc) {
@@ -265,7 +358,7 @@ int ghmm_pd_compute_regions(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_
     if (n_regions == 0) return GHMM_OK;
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     ghmm_batch &b = ctx->pd_batch;
-    int rc = pd_marshal(ctx, regions, n_regions, b);
+    int rc = pd_marshal(ctx, regions, n_regions, b, nullptr);
     if (!rc) rc = pd_upload(ctx, b, ctx->stream);
     if (!rc) rc = batch_forward(ctx, b, ctx->double_precision ? GHMM_MODE_PD : GHMM_MODE_PD_FP32);
     if (!rc) rc = batch_results(ctx, b, out);

@@ -53,6 +53,10 @@ struct Source {
     // ... or flat planes
     const ghmm_flat *flat = nullptr;
     const RouteBound *bound = nullptr;  // set when the device rewrites the gap penalties after the upload
+    // PD-HMM batches: per region 1 = no read-pair tasks (every pair to the general PD kernel); reads that need more
+    // than one strip get no tasks either
+    const uint8_t *region_direct = nullptr;
+    bool single_strip = false;
 };
 
 }  // namespace rt
@@ -284,6 +288,7 @@ int cuda_fail(ghmm_ctx *ctx, cudaError_t e, const char *what);
 
 // batch.cpp
 int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b);
+uint8_t base_index(uint8_t b);  // column-code base index of a haplotype byte: A, C, G, T = 0..3, anything else 4
 int batch_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s);
 int fill_fp64_all(ghmm_ctx *ctx, ghmm_batch &b);
 int batch_forward(ghmm_ctx *ctx, ghmm_batch &b, int mode);
@@ -309,7 +314,7 @@ bool region_sizes(const Source &src, std::vector<int64_t> &cells, std::vector<in
 int compute_sync(ghmm_ctx *ctx, const Source &src, double *out);
 
 // pd_host.cpp
-int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch &b);
+int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch &b, const RouteBound *bound);
 int pd_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s);
 int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32);
 

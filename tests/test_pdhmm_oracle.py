@@ -302,3 +302,115 @@ def test_gpu_pdhmm_from_raw_reads(engine, engine64, kind):
         _, q, i, d, g = b.read_planes()
     assert np.array_equal(q, prepared.quals) and np.array_equal(i, prepared.ins)
     assert np.array_equal(d, prepared.dels) and np.array_equal(g, prepared.gcp)
+
+
+def _packed_case_workload(seed=41):
+    """Regions of several reads (lengths 20-254, so read-pair tasks of 2 to 8 rows per lane pair reads of different
+    lengths) against haplotypes whose flags reach every per-column op of the packed FP32 kernel (pd_packed.cu):
+    single-base deletions (DEL_START and DEL_END on one column), a deletion from column 1, a DEL_END on the
+    second-to-last column (AFTER_DEL at the last), an AFTER_DEL column that ends another deletion (AFTER_DEL twice in
+    a row), SNP columns inside a deletion, an SNP on an N column, SNP columns with two and with three alternatives
+    (three or four matching bases), reads with N; plus one region with a deletion ending on the last column (the
+    state carries into the next row), which the host sends to the general kernel."""
+    rng = np.random.default_rng(seed)
+    regions, pds = [], []
+    lengths = [20, 33, 40, 62, 63, 64, 90, 126, 150, 190, 222, 254]
+    for g in range(26):
+        nh = int(rng.integers(1, 4))
+        haps, hpd = [], []
+        for h in range(nh):
+            H = int(rng.integers(80, 420))
+            hap = rng.choice(list(b"ACGT"), size=H).astype(np.uint8)
+            pd = np.zeros(H, dtype=np.uint8)
+            kind = (g + h) % 6
+            if kind == 0:
+                for j in rng.choice(np.arange(2, H - 2), size=4, replace=False):
+                    pd[j] |= DS | DE
+            elif kind == 1:
+                n = int(rng.integers(1, 8))
+                pd[1] |= DS
+                pd[n] |= DE
+            elif kind == 2:
+                n = int(rng.integers(1, 8))
+                pd[H - 1 - n] |= DS
+                pd[H - 2] |= DE
+            elif kind == 3:
+                j = int(rng.integers(5, H - 12))
+                pd[j] |= DS
+                pd[j + 2] |= DE
+                pd[j + 3] |= DE
+                pd[j + 5] |= DS | DE
+            elif kind == 4:
+                j = int(rng.integers(5, H - 12))
+                pd[j] |= DS
+                pd[j + 6] |= DE
+                for k in (j + 2, j + 6, j + 7):
+                    alt = [c for c in b"ACGT" if c != hap[k]][int(rng.integers(0, 3))]
+                    pd[k] |= SNP | BIT[alt]
+                k = int(rng.integers(j + 10, H))
+                hap[k] = ord("N")
+                pd[k] |= SNP | BIT[ord("A")]
+            else:
+                for _ in range(4):
+                    k = int(rng.integers(0, H))
+                    alt = [c for c in b"ACGT" if c != hap[k]][int(rng.integers(0, 3))]
+                    pd[k] |= SNP | BIT[alt]
+                for _ in range(3):
+                    n = int(rng.integers(1, 10))
+                    j = int(rng.integers(1, H - n - 1))
+                    pd[j] |= DS
+                    pd[j + n - 1] |= DE
+            if g == 24 and h == 0:
+                pd[H - 1] |= DE  # the row-end state carries into the next row: general kernel
+            if g >= 20:  # SNP columns listing two and three alternatives
+                for k in rng.choice(np.arange(H), size=6, replace=False):
+                    others = [c for c in b"ACGT" if c != hap[k]]
+                    chosen = others if k % 2 else [others[int(rng.integers(0, 3))], others[int(rng.integers(0, 3))]]
+                    pd[k] |= SNP
+                    for c in chosen:
+                        pd[k] |= BIT[c]
+            haps.append(bytes(hap))
+            hpd.append(pd)
+        base = np.frombuffer(haps[0], dtype=np.uint8)
+        reads = []
+        for _ in range(int(rng.integers(2, 9))):
+            R = int(rng.choice(lengths))
+            start = int(rng.integers(0, max(1, len(base) - R + 1)))
+            rd = np.concatenate([base[start:start + R], rng.choice(list(b"ACGT"), size=max(0, R - len(base)))])
+            rd = rd[:R].astype(np.uint8).copy()
+            rd[rd == ord("N")] = ord("A")
+            flip = rng.random(R) < 0.03
+            rd[flip] = rng.choice(list(b"ACGT"), size=int(flip.sum()))
+            if rng.random() < 0.3:
+                rd[int(rng.integers(0, R))] = ord("N")
+            reads.append((bytes(rd), rng.integers(10, 41, size=R), rng.integers(20, 46, size=R),
+                          rng.integers(20, 46, size=R), np.full(R, 10)))
+        regions.append((haps, reads))
+        pds.extend(hpd)
+    return W.from_pairs(regions), np.concatenate(pds)
+
+
+@pytest.mark.gpu
+def test_gpu_pdhmm_packed_kernel_every_op(engine, engine64):
+    from gatk_gb300 import native
+
+    wl, pd = _packed_case_workload()
+    ref = O.pd_compute_workload(wl, pd)
+    assert np.isfinite(ref).all()
+    assert np.abs(engine64.pd_compute(wl, pd) - ref).max() <= 1e-9
+    with engine.pd_batch(wl, pd) as b:
+        b.forward(native.MODE_PD_FP32)
+        got = b.results()
+        st = b.stats()
+        b.forward(native.MODE_PD_FP32)
+        assert np.array_equal(got, b.results())
+    assert st["n_tasks_fp32"] > 0  # read-pair tasks ran in the packed kernel
+    assert np.abs(got - ref).max() <= 1e-3
+    # the same pairs with one read per region: tasks of a single read, the other half empty
+    single = [([wl.hap(h) for h in range(int(wl.region_hap_off[g]), int(wl.region_hap_off[g + 1]))], [wl.read(r)])
+              for g in range(wl.n_regions) for r in range(int(wl.region_read_off[g]), int(wl.region_read_off[g + 1]))]
+    wl1 = W.from_pairs(single)
+    pd1 = np.concatenate([pd[int(wl.hap_off[wl.region_hap_off[g]]):int(wl.hap_off[wl.region_hap_off[g + 1]])]
+                          for g in range(wl.n_regions) for _ in range(int(wl.region_read_off[g + 1] - wl.region_read_off[g]))])
+    ref1 = O.pd_compute_workload(wl1, pd1)
+    assert np.abs(engine.pd_compute(wl1, pd1) - ref1).max() <= 1e-3
