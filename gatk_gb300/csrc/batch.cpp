@@ -729,19 +729,37 @@ int batch_finish(ghmm_ctx *ctx, ghmm_batch &b) {
     return GHMM_OK;
 }
 
-int batch_results(ghmm_ctx *ctx, ghmm_batch &b, double *out) {
+int batch_results(ghmm_ctx *ctx, ghmm_batch &b, double *out) { return batch_results_on(ctx, b, out, ctx->stream); }
+
+// The results through pinned staging (a copy into the caller's pageable memory ran at about 1 GB/s), then copied out
+// and checked (PairHMM.java:305-306) in parallel blocks.
+int batch_results_on(ghmm_ctx *ctx, ghmm_batch &b, double *out, cudaStream_t s) {
     if (b.n_out == 0) return GHMM_OK;
     if (!out) return fail(ctx, GHMM_ERR_ARG, "NULL output");
-    GHMM_CUDA(cudaMemcpyAsync(out, b.d_out.p, (size_t)b.n_out * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "D2H results");
-    b.results_d2h = b.n_out * 8;
-    GHMM_CUDA(cudaStreamSynchronize(ctx->stream), "D2H results");
-    for (int64_t i = 0; i < b.n_out; i++)
-        if (!(out[i] <= 0.0)) {
-            char msg[160];
-            snprintf(msg, sizeof msg, "PairHMM log10 likelihood %g at output %lld is not a valid log10 probability", out[i],
-                     (long long)i);
-            return fail(ctx, GHMM_ERR_RESULT, msg);
+    const int64_t n = b.n_out;
+    GHMM_CUDA(b.h_out.reserve((size_t)n), "pinned results");
+    GHMM_CUDA(cudaMemcpyAsync(b.h_out.p, b.d_out.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H results");
+    b.results_d2h = n * 8;
+    GHMM_CUDA(cudaStreamSynchronize(s), "D2H results");
+    const double *src = b.h_out.p;
+    std::atomic<int64_t> bad{-1};
+    parallel_for((n + (1 << 20) - 1) >> 20, hw_threads(ctx->max_threads), [&](int64_t k) {
+        const int64_t a = k << 20, e = std::min<int64_t>(n, a + (1 << 20));
+        for (int64_t i = a; i < e; i++) {
+            const double v = src[i];
+            out[i] = v;
+            if (!(v <= 0.0)) {
+                int64_t expect = -1;
+                bad.compare_exchange_strong(expect, i);
+            }
         }
+    }, 1);
+    if (bad.load() >= 0) {
+        char msg[160];
+        snprintf(msg, sizeof msg, "PairHMM log10 likelihood %g at output %lld is not a valid log10 probability",
+                 src[bad.load()], (long long)bad.load());
+        return fail(ctx, GHMM_ERR_RESULT, msg);
+    }
     return GHMM_OK;
 }
 

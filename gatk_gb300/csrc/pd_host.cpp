@@ -11,6 +11,7 @@
 #include <cstring>
 #include <condition_variable>
 #include <deque>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <numeric>
@@ -155,16 +156,17 @@ int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch 
     // a read base outside ACGTacgtN that meets an undetermined SNP column throws in the reference
     const int64_t *rro = o + b.n_reads + 1 + NH + 1, *rho = rro + G + 1;
     const uint8_t *bases = b.h_planes.p;
-    for (int64_t g = 0; g < G; g++)
-        for (int64_t r = rro[g]; r < rro[g + 1]; r++)
-            for (int64_t i = o[r]; i < o[r + 1]; i++) {
-                const uint8_t x = bases[i];
-                if (pd_read_base_ok(x)) continue;
-                for (int64_t h = rho[g]; h < rho[g + 1]; h++)
-                    for (int64_t j = hap_off[h]; j < hap_off[h + 1]; j++)
-                        if ((flags[j] & 1) && hraw[j] != x && hraw[j] != 'N')
-                            return fail(ctx, GHMM_ERR_ARG, "Found unexpected base in alt alleles");
-            }
+    std::atomic<bool> unexpected{false};
+    parallel_for(G, hw_threads(ctx->max_threads), [&](int64_t g) {
+        for (int64_t i = o[rro[g]]; i < o[rro[g + 1]]; i++) {
+            const uint8_t x = bases[i];
+            if (pd_read_base_ok(x)) continue;
+            for (int64_t h = rho[g]; h < rho[g + 1]; h++)
+                for (int64_t j = hap_off[h]; j < hap_off[h + 1]; j++)
+                    if ((flags[j] & 1) && hraw[j] != x && hraw[j] != 'N') unexpected = true;
+        }
+    }, 16);
+    if (unexpected) return fail(ctx, GHMM_ERR_ARG, "Found unexpected base in alt alleles");
     b.has_pd = true;
     return GHMM_OK;
 }
@@ -186,7 +188,12 @@ int pd_upload(ghmm_ctx *ctx, ghmm_batch &b, cudaStream_t s) {
 // a task through the general FP32 one (pd.cu), then the pairs whose FP32 sums underflow in the FP64 one (K = 4);
 // otherwise every pair in FP64
 int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32) {
-    cudaStream_t s = ctx->stream;
+    const int rc = pd_forward_enqueue(ctx, b, fp32, ctx->stream);
+    return rc ? rc : pd_forward_finish(ctx, b);
+}
+
+// The kernels of one PD forward on stream s, and the D2H of its counters, without waiting (pd_forward_finish waits).
+int pd_forward_enqueue(ghmm_ctx *ctx, ghmm_batch &b, bool fp32, cudaStream_t s) {
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
     // the general kernel's pairs (FP64: every pair; FP32: those without a task), grouped by the rows per lane K of the
     // read (the strip height 32 K, K = 1..4, that needs the fewest rows; ties to the larger K, i.e. fewer strips), in
@@ -285,7 +292,16 @@ int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32) {
     GHMM_CUDA(cudaMemcpyAsync(hc, b.d_counters.p, kNumCounters * sizeof(int32_t), cudaMemcpyDeviceToHost, s),
               "D2H counters");
     GHMM_CUDA(cudaEventRecord(b.ev[3], s), "event");
+    b.last_mode = fp32 ? GHMM_MODE_PD_FP32 : GHMM_MODE_PD;
+    b.last_launches = launches;
+    b.forward_h2d = k * (int64_t)sizeof(PairRef) + (kNumCounters + 2 * kNumBucketKeys) * 4 + (packed ? 8 : 0);
+    b.forward_d2h = kNumCounters * 4;
+    return GHMM_OK;
+}
+
+int pd_forward_finish(ghmm_ctx *ctx, ghmm_batch &b) {
     GHMM_CUDA(cudaEventSynchronize(b.ev[3]), "PD-HMM kernel");
+    const bool fp32 = b.last_mode == GHMM_MODE_PD_FP32;
     float ms = 0, ms_a = 0, ms_b = 0;
     cudaEventElapsedTime(&ms_a, b.ev[1], b.ev[4]);
     cudaEventElapsedTime(&ms_b, b.ev[4], b.ev[2]);
@@ -294,17 +310,66 @@ int batch_forward_pd(ghmm_ctx *ctx, ghmm_batch &b, bool fp32) {
     b.ms_plain = 0;
     cudaEventElapsedTime(&ms, b.ev[0], b.ev[3]);
     b.ms_total = ms;
-    b.last_mode = fp32 ? GHMM_MODE_PD_FP32 : GHMM_MODE_PD;
-    b.last_launches = launches;
+    const int32_t *hc = b.h_counters.p;
     b.last_rerun = fp32 ? hc[kCounterPdRerun] : 0;
     b.last_exact = 0;
-    b.forward_h2d = k * (int64_t)sizeof(PairRef) + (kNumCounters + 2 * kNumBucketKeys) * 4 + (packed ? 8 : 0);
-    b.forward_d2h = kNumCounters * 4;
     if (hc[3] == 1) return fail(ctx, GHMM_ERR_CUDA, "PD-HMM FP64 rerun queue overflow");
     if (hc[3] != 0) return fail(ctx, GHMM_ERR_CUDA, "device-side scratch bound exceeded");
     return GHMM_OK;
 }
 
+
+// The one-shot PD-HMM calls in chunks of regions, pipelined on two streams: chunk i+1 is marshalled on the host and
+// enqueued (upload, preparation, forward) on the other slot's stream while chunk i runs, so its kernels start as
+// chunk i's last tasks leave SMs free; then chunk i's results are read.  Three chunks, of 1/8, 3/8 and 1/2 of the
+// cells: on 1,000 regions of workload 1 with PD flags, 85 ms a call against 112 ms for the regular pipelined calls'
+// finer cut (1/16 growing by 2.5) and 84 ms unchunked; on 3,000 regions, 198 ms against 209 ms and 232 ms.
+// host(g0, g1, slot) stages regions [g0, g1) in ctx->pd_batch[slot]; device(slot, stream) uploads it (and prepares
+// raw reads).
+int pd_pipelined(ghmm_ctx *ctx, const std::vector<int64_t> &cells, const std::vector<int64_t> &outo, double *out,
+                 const std::function<int(int64_t, int64_t, int)> &host,
+                 const std::function<int(int, cudaStream_t)> &device) {
+    const int64_t G = (int64_t)cells.size();
+    std::vector<int64_t> cut{0};
+    int64_t total = 0;
+    for (int64_t c : cells) total += c;
+    {  // cuts after 1/8 and 1/2 of the cells, none that leaves fewer than 8 regions behind
+        const int64_t marks[2] = {total / 8, total / 2};
+        int64_t c = 0;
+        int m = 0;
+        for (int64_t g = 0; g < G && m < 2; g++) {
+            c += cells[(size_t)g];
+            if (c >= marks[m] && G - g - 1 >= 8) {
+                cut.push_back(g + 1);
+                m++;
+            }
+        }
+        cut.push_back(G);
+    }
+    if (!ctx->pd_stream2) GHMM_CUDA(cudaStreamCreateWithFlags(&ctx->pd_stream2, cudaStreamNonBlocking), "cudaStreamCreate");
+    const cudaStream_t streams[2] = {ctx->stream, ctx->pd_stream2};
+    const bool fp32 = !ctx->double_precision;
+    auto start = [&](size_t i) {
+        const int slot = (int)(i & 1);
+        int rc = host(cut[i], cut[i + 1], slot);
+        if (!rc) rc = device(slot, streams[slot]);
+        if (!rc) rc = pd_forward_enqueue(ctx, ctx->pd_batch[slot], fp32, streams[slot]);
+        return rc;
+    };
+    int rc = start(0);
+    for (size_t i = 0; !rc && i + 1 < cut.size(); i++) {
+        const int slot = (int)(i & 1);
+        const int rc_next = i + 2 < cut.size() ? start(i + 1) : GHMM_OK;
+        ghmm_batch &b = ctx->pd_batch[slot];
+        rc = pd_forward_finish(ctx, b);
+        if (!rc) rc = batch_results_on(ctx, b, out + outo[(size_t)cut[i]], streams[slot]);
+        if (!rc) rc = rc_next;
+    }
+    // nothing of this call may still run on either stream when it returns
+    cudaStreamSynchronize(streams[0]);
+    cudaStreamSynchronize(streams[1]);
+    return rc;
+}
 
 // PD regions of raw reads: the raw reads' view (checks, 45s and the constant GCP) as the regular raw path builds it,
 // then the PD marshal over it, the upload, and the read preparation on the device.
@@ -357,12 +422,23 @@ int ghmm_pd_compute_regions(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_
     if (n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad region array");
     if (n_regions == 0) return GHMM_OK;
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-    ghmm_batch &b = ctx->pd_batch;
-    int rc = pd_marshal(ctx, regions, n_regions, b, nullptr);
-    if (!rc) rc = pd_upload(ctx, b, ctx->stream);
-    if (!rc) rc = batch_forward(ctx, b, ctx->double_precision ? GHMM_MODE_PD : GHMM_MODE_PD_FP32);
-    if (!rc) rc = batch_results(ctx, b, out);
-    return rc;
+    std::vector<int64_t> cells((size_t)n_regions, 0), outo((size_t)n_regions + 1, 0);
+    for (int32_t g = 0; g < n_regions; g++) {
+        const ghmm_pd_region &rg = regions[g];
+        if (rg.n_reads < 0 || rg.n_haps < 0 || (rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps))
+            return fail(ctx, GHMM_ERR_ARG, "bad PD region");
+        int64_t sr = 0, sh = 0;
+        for (int32_t r = 0; r < rg.n_reads; r++) sr += std::max(rg.reads[r].length, 0);
+        for (int32_t h = 0; h < rg.n_haps; h++) sh += std::max(rg.haps[h].length, 0);
+        cells[(size_t)g] = sr * sh;
+        outo[(size_t)g + 1] = outo[(size_t)g] + (int64_t)rg.n_reads * rg.n_haps;
+    }
+    return pd_pipelined(
+        ctx, cells, outo, out,
+        [&](int64_t g0, int64_t g1, int slot) {
+            return pd_marshal(ctx, regions + g0, g1 - g0, ctx->pd_batch[slot], nullptr);
+        },
+        [&](int slot, cudaStream_t st) { return pd_upload(ctx, ctx->pd_batch[slot], st); });
 }
 
 int ghmm_pd_batch_create_raw(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions, int32_t n_regions,
@@ -388,11 +464,40 @@ int ghmm_pd_compute_regions_raw(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions
     if (n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad region array");
     if (n_regions == 0) return GHMM_OK;
     GHMM_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-    ghmm_batch &b = ctx->pd_batch;
-    int rc = pd_raw_build(ctx, regions, n_regions, prep, b);
-    if (!rc) rc = batch_forward(ctx, b, ctx->double_precision ? GHMM_MODE_PD : GHMM_MODE_PD_FP32);
-    if (!rc) rc = batch_results(ctx, b, out);
-    return rc;
+    std::vector<int64_t> cells((size_t)n_regions, 0), outo((size_t)n_regions + 1, 0);
+    for (int32_t g = 0; g < n_regions; g++) {
+        const ghmm_pd_raw_region &rg = regions[g];
+        if (rg.n_reads < 0 || rg.n_haps < 0 || (rg.n_reads > 0 && !rg.reads) || (rg.n_haps > 0 && !rg.haps))
+            return fail(ctx, GHMM_ERR_ARG, "bad PD region");
+        int64_t sr = 0, sh = 0;
+        for (int32_t r = 0; r < rg.n_reads; r++) sr += std::max(rg.reads[r].length, 0);
+        for (int32_t h = 0; h < rg.n_haps; h++) sh += std::max(rg.haps[h].length, 0);
+        cells[(size_t)g] = sr * sh;
+        outo[(size_t)g + 1] = outo[(size_t)g] + (int64_t)rg.n_reads * rg.n_haps;
+    }
+    // the raw view of each slot's chunk (its mapping qualities) lives until that chunk's preparation has read them
+    RawView views[2];
+    return pd_pipelined(
+        ctx, cells, outo, out,
+        [&](int64_t g0, int64_t g1, int slot) {
+            RawView &v = views[slot];
+            v = RawView();
+            std::vector<ghmm_raw_region> rr((size_t)(g1 - g0));
+            for (int64_t g = g0; g < g1; g++) rr[(size_t)(g - g0)] = ghmm_raw_region{regions[g].reads, regions[g].n_reads, nullptr, 0};
+            int rc = raw_view(ctx, rr.data(), g1 - g0, prep, v);
+            if (rc) return rc;
+            std::vector<ghmm_pd_region> pr((size_t)(g1 - g0));
+            for (int64_t g = g0; g < g1; g++)
+                pr[(size_t)(g - g0)] = ghmm_pd_region{v.regions[(size_t)(g - g0)].reads, regions[g].n_reads,
+                                                      regions[g].haps, regions[g].n_haps};
+            return pd_marshal(ctx, pr.data(), g1 - g0, ctx->pd_batch[slot], v.has_bound ? &v.bound : nullptr);
+        },
+        [&](int slot, cudaStream_t st) {
+            ghmm_batch &b = ctx->pd_batch[slot];
+            int rc = pd_upload(ctx, b, st);
+            if (!rc) rc = raw_prepare_device(ctx, b, views[slot].mapq.data(), views[slot].max_len, prep, st);
+            return rc;
+        });
 }
 
 int ghmm_pd_compute_likelihoods(ghmm_ctx *ctx, const ghmm_read *reads, int32_t n_reads, const ghmm_pd_hap *haps,

@@ -90,7 +90,7 @@ __device__ __forceinline__ void emit_pd(const DevBatch &B, float t, float2 scale
 // regular kernel's.
 template <int K>
 struct PdMinBlocks {
-    static constexpr int value = K >= 6 ? 2 : 3;
+    static constexpr int value = 3;
 };
 
 template <int K>
@@ -104,6 +104,9 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
     extern __shared__ float4 pd_prior_smem4[];
     float4 *prior_tbl4 = pd_prior_smem4 + (size_t)(threadIdx.x >> 5) * (KP * kBases * 32) + lane;
     float2 *prior_tbl2 = reinterpret_cast<float2 *>(prior_tbl4);
+    // branch states bM, bI, bD of the lane's rows, lane-private: [row][M, I, D][lane] after the 4 warps' tables
+    float2 *bst = reinterpret_cast<float2 *>(pd_prior_smem4 + 4 * (KP * kBases * 32)) +
+                  (size_t)(threadIdx.x >> 5) * (K * 3 * 32) + lane;
     const bool acc_lane = lane == 31;  // its last two rows are the accumulator rows of both reads
 
     for (;;) {
@@ -153,9 +156,12 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
         float2 b0n = shfl_down2(cb[0]), c0n = shfl_down2(cc[0]), e0n = shfl_down2(ce[0]);
         if (lane == 31) b0n = c0n = e0n = zero2();
         __syncwarp();
-        float2 Mp[K], Ip[K], Dp[K], bM[K], bI[K], bD[K];
+        float2 Mp[K], Ip[K], Dp[K];
 #pragma unroll
-        for (int k = 0; k < K; ++k) Mp[k] = Ip[k] = Dp[k] = bM[k] = bI[k] = bD[k] = zero2();
+        for (int k = 0; k < K; ++k) {
+            Mp[k] = Ip[k] = Dp[k] = zero2();
+            bst[(3 * k + 0) * 32] = bst[(3 * k + 1) * 32] = bst[(3 * k + 2) * 32] = zero2();
+        }
         float2 gW = zero2(), w0 = zero2();
         float2 pendV = zero2(), pendW1 = zero2(), pendW2 = zero2();
         float2 sV = zero2(), sW = zero2();
@@ -194,7 +200,6 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
                     for (int k = 0; k < K; ++k) {
                         Mp[k] = Ip[k] = zero2();
                         Dp[k] = make_float2((slot0 + k < task.pad_a) ? X.x : 0.f, (slot0 + k < task.pad_b) ? X.y : 0.f);
-                        bM[k] = bI[k] = bD[k] = zero2();
                     }
                     const float2 gD = make_float2((slot0 - 1 < task.pad_a) ? X.x : 0.f,
                                                   (slot0 - 1 < task.pad_b) ? X.y : 0.f);
@@ -208,17 +213,17 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
                 if (op & kPdOpAfter) {
 #pragma unroll
                     for (int k = 0; k < K; ++k) {
-                        Mp[k] = max2(bM[k], Mp[k]);
-                        Ip[k] = max2(bI[k], Ip[k]);
-                        Dp[k] = max2(bD[k], Dp[k]);
+                        Mp[k] = max2(bst[(3 * k + 0) * 32], Mp[k]);
+                        Ip[k] = max2(bst[(3 * k + 1) * 32], Ip[k]);
+                        Dp[k] = max2(bst[(3 * k + 2) * 32], Dp[k]);
                     }
                 }
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
                     if (k >= K - 2 && acc_lane) continue;
-                    bM[k] = Mp[k];
-                    bI[k] = Ip[k];
-                    bD[k] = Dp[k];
+                    bst[(3 * k + 0) * 32] = Mp[k];
+                    bst[(3 * k + 1) * 32] = Ip[k];
+                    bst[(3 * k + 2) * 32] = Dp[k];
                 }
             }
             const uint32_t ref = code & 7u;
@@ -272,7 +277,7 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
             if (op & kPdOpDelEnd) {
 #pragma unroll
                 for (int k = 1; k < K; ++k) {
-                    float2 bi = bI[k - 1], bm = bM[k - 1];
+                    float2 bi = bst[(3 * (k - 1) + 1) * 32], bm = bst[(3 * (k - 1) + 0) * 32];
                     if (k == K - 2 && acc_lane) bi = bm = zero2();  // the first accumulator row sums row R as is
                     Ip[k] = fma2(max2(bi, Ip[k - 1]), ce[k], max2(bm, Mp[k - 1]));
                 }
@@ -284,15 +289,15 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
             // hand-over to the lane below: row 0's I~ at this column and its M~ inner sum for the next column
             float2 hI = Ip[K - 1], hM = Mp[K - 1];
             if ((op & kPdOpDelEnd) && !(K == 2 && lane == 30)) {  // (K = 2: lane 31's row 0 is an accumulator row)
-                hI = max2(bI[K - 1], hI);
-                hM = max2(bM[K - 1], hM);
+                hI = max2(bst[(3 * (K - 1) + 1) * 32], hI);
+                hM = max2(bst[(3 * (K - 1) + 0) * 32], hM);
             }
             sV = fma2(hI, e0n, hM);
             float2 wI = Ip[K - 1], wD = Dp[K - 1], wM = Mp[K - 1];
             if (op & kPdOpNextAfter) {
-                wI = max2(bI[K - 1], wI);
-                wD = max2(bD[K - 1], wD);
-                wM = max2(bM[K - 1], wM);
+                wI = max2(bst[(3 * (K - 1) + 1) * 32], wI);
+                wD = max2(bst[(3 * (K - 1) + 2) * 32], wD);
+                wM = max2(bst[(3 * (K - 1) + 0) * 32], wM);
             }
             sW = fma2(wI, b0n, fma2(wD, c0n, wM));
             if constexpr (CHK) {
@@ -324,7 +329,9 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
     }
 }
 
-size_t pd_bucket_smem_bytes(int k) { return (size_t)(128 / 32) * ((k + 1) / 2) * kBases * 32 * sizeof(float4); }
+size_t pd_bucket_smem_bytes(int k) {
+    return (size_t)(128 / 32) * (((k + 1) / 2) * kBases * 32 * sizeof(float4) + (size_t)k * 3 * 32 * sizeof(float2));
+}
 
 template <int K>
 int launch_pd_bucket_k(const DevTables &t, const DevBatch &b, const uint8_t *ops, int grid, cudaStream_t s) {
@@ -365,7 +372,12 @@ int pd_bucket_occupancy(int k, int *blocks_per_sm) {
         case 8: fn = (const void *)pd_bucket_kernel<8>; break;
         default: return (int)cudaErrorInvalidValue;
     }
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, 128, pd_bucket_smem_bytes(k));
+    const size_t smem = pd_bucket_smem_bytes(k);
+    if (smem > 48 * 1024) {  // (above 48 KB the kernel must opt in before the query counts it)
+        const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+    }
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, 128, smem);
 }
 
 }  // namespace ghmm

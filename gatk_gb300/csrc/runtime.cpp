@@ -253,7 +253,7 @@ int ghmm_done(ghmm_ctx *ctx) {
     ctx->pipe = nullptr;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     ctx->scratch_batch.release();
-    ctx->pd_batch.release();
+    for (auto &pb : ctx->pd_batch) pb.release();
     ctx->calib_scratch.release();
     ctx->calib_flags.release();
     ctx->calib_ones.release();
@@ -264,6 +264,7 @@ int ghmm_done(ghmm_ctx *ctx) {
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->pd_stream2) cudaStreamDestroy(ctx->pd_stream2);
     delete ctx;
     return GHMM_OK;
 }

@@ -173,7 +173,8 @@ struct ghmm_ctx {
     HostTables *host_tables = nullptr;  // host copy, for routing decisions
     std::string last_error;
     ghmm_batch scratch_batch;  // reused by the one-shot entry points
-    ghmm_batch pd_batch;       // reused by the one-shot PD-HMM entry points
+    ghmm_batch pd_batch[2];    // the one-shot PD-HMM entry points' two pipeline slots, reused across calls
+    cudaStream_t pd_stream2 = nullptr;  // the second slot's stream (created on first use)
     int max_k = kMaxK32, max_k_multi = kMaxK32, chunk_cols = 16384;
     // Reads whose expected log10 prior product (sum over positions of the per-quality expectation below) is under
     // route_fp64_log10 go to the FP64 kernel directly: their FP32 results would fall below the rerun threshold and
@@ -295,6 +296,9 @@ int batch_forward(ghmm_ctx *ctx, ghmm_batch &b, int mode);
 int batch_enqueue(ghmm_ctx *ctx, ghmm_batch &b, int mode, cudaStream_t s);
 int batch_finish(ghmm_ctx *ctx, ghmm_batch &b);
 int batch_results(ghmm_ctx *ctx, ghmm_batch &b, double *out);
+int batch_results_on(ghmm_ctx *ctx, ghmm_batch &b, double *out, cudaStream_t s);
+int pd_forward_enqueue(ghmm_ctx *ctx, ghmm_batch &b, bool fp32, cudaStream_t s);
+int pd_forward_finish(ghmm_ctx *ctx, ghmm_batch &b);
 
 // queue.cpp.  Large synchronous inputs run as a pipeline of batches through the context's own queue: the first
 // batch is small so that the GPU starts early, later ones grow to a third of the input.

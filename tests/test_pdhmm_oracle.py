@@ -283,7 +283,7 @@ def test_gpu_pdhmm_from_raw_reads(engine, engine64, kind):
     import json
     import os
 
-    wl, pd = _pd_workload(4, seed=8)
+    wl, pd = _pd_workload(12, seed=8)  # enough regions for the one-shot calls to run in two pipelined chunks
     rng = np.random.default_rng(19)
     wl.quals[:] = rng.integers(2, 45, size=len(wl.quals)).astype(np.uint8)
     wl.ins[:] = rng.integers(10, 50, size=len(wl.ins)).astype(np.uint8)
