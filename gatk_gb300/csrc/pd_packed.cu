@@ -29,9 +29,10 @@
 //    base or the alternative (or is N), picked from three rows of the prior table without a per-row base compare;
 //    with kPdOpSnpAllBut, three bases match (two alternatives) and bits 5-6 name the fourth.  A column whose
 //    alternatives cover all four bases carries the code of N (pd_host.cpp), which matches every read base.
-// These run only in lanes at such columns (lane-divergent branches); the accumulator rows below each read never
-// take a branch state (theirs stay 0, so max(bX, X) = X for them), and the first accumulator row's I never takes
-// the DEL_END max, since it sums the read's last row rather than stepping the recurrence.
+// These run only in lanes at such columns (lane-divergent branches), and only in steps where some lane of the warp
+// is at such a column (a warp vote; the other steps are the regular kernel's).  The accumulator rows below each read
+// never take a branch state (theirs stay 0, so max(bX, X) = X for them), and the first accumulator row's I never
+// takes the DEL_END max, since it sums the read's last row rather than stepping the recurrence.
 //
 // The host sends a region to the general PD kernel (pd.cu) instead when a haplotype's state carries from the end
 // of a row into the next row (the first row would then see other states than the rest); reads the regular routing
@@ -208,105 +209,118 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
                 }
             }
             if (lane == 0) gW = w0;
-            // branch states at this column, from the previous column's values (still in Mp, Ip, Dp)
-            if (op & (kPdOpCopy | kPdOpAfter)) {
-                if (op & kPdOpAfter) {
+            auto body = [&](auto ops_tag) {
+                constexpr bool OPS = decltype(ops_tag)::value;
+                // branch states at this column, from the previous column's values (still in Mp, Ip, Dp)
+                if (OPS && (op & (kPdOpCopy | kPdOpAfter))) {
+                    if (op & kPdOpAfter) {
+#pragma unroll
+                        for (int k = 0; k < K; ++k) {
+                            Mp[k] = max2(bst[(3 * k + 0) * 32], Mp[k]);
+                            Ip[k] = max2(bst[(3 * k + 1) * 32], Ip[k]);
+                            Dp[k] = max2(bst[(3 * k + 2) * 32], Dp[k]);
+                        }
+                    }
 #pragma unroll
                     for (int k = 0; k < K; ++k) {
-                        Mp[k] = max2(bst[(3 * k + 0) * 32], Mp[k]);
-                        Ip[k] = max2(bst[(3 * k + 1) * 32], Ip[k]);
-                        Dp[k] = max2(bst[(3 * k + 2) * 32], Dp[k]);
+                        if (k >= K - 2 && acc_lane) continue;
+                        bst[(3 * k + 0) * 32] = Mp[k];
+                        bst[(3 * k + 1) * 32] = Ip[k];
+                        bst[(3 * k + 2) * 32] = Dp[k];
                     }
                 }
+                const uint32_t ref = code & 7u;
+                const float4 *pri4 = prior_tbl4 + ref * 32;
+                float2 prs[2 * KP];
 #pragma unroll
-                for (int k = 0; k < K; ++k) {
-                    if (k >= K - 2 && acc_lane) continue;
-                    bst[(3 * k + 0) * 32] = Mp[k];
-                    bst[(3 * k + 1) * 32] = Ip[k];
-                    bst[(3 * k + 2) * 32] = Dp[k];
+                for (int kk = 0; kk < KP; ++kk) {
+                    const float4 v = pri4[kk * kBases * 32];
+                    prs[2 * kk] = make_float2(v.x, v.y);
+                    prs[2 * kk + 1] = make_float2(v.z, v.w);
                 }
-            }
-            const uint32_t ref = code & 7u;
-            const float4 *pri4 = prior_tbl4 + ref * 32;
-            float2 prs[2 * KP];
+                if (OPS && (op & kPdOpSnp)) {
+                    const uint32_t alt = (op >> kPdOpAltShift) & 3u;
+                    if (op & kPdOpSnpAllBut) {  // three bases match: all but `alt`
+                        const uint32_t w = alt ? 0u : 1u;
+                        const float4 *pu = prior_tbl4 + alt * 32, *pn = prior_tbl4 + 4 * 32;
+                        const float4 *pw = prior_tbl4 + w * 32;
 #pragma unroll
-            for (int kk = 0; kk < KP; ++kk) {
-                const float4 v = pri4[kk * kBases * 32];
-                prs[2 * kk] = make_float2(v.x, v.y);
-                prs[2 * kk + 1] = make_float2(v.z, v.w);
-            }
-            if (op & kPdOpSnp) {
-                const uint32_t alt = (op >> kPdOpAltShift) & 3u;
-                if (op & kPdOpSnpAllBut) {  // three bases match: all but `alt`
-                    const uint32_t w = alt ? 0u : 1u;
-                    const float4 *pu = prior_tbl4 + alt * 32, *pn = prior_tbl4 + 4 * 32, *pw = prior_tbl4 + w * 32;
+                        for (int kk = 0; kk < KP; ++kk) {
+                            const float4 tu = pu[kk * kBases * 32], tn = pn[kk * kBases * 32];
+                            const float4 tw = pw[kk * kBases * 32];
+                            prs[2 * kk] = make_float2(all_but_prior(tu.x, tn.x, tw.x), all_but_prior(tu.y, tn.y, tw.y));
+                            prs[2 * kk + 1] =
+                                make_float2(all_but_prior(tu.z, tn.z, tw.z), all_but_prior(tu.w, tn.w, tw.w));
+                        }
+                    } else {  // two bases match: the column's and `alt`
+                        const uint32_t third = (uint32_t)__ffs(~((1u << ref) | (1u << alt))) - 1u;
+                        const float4 *pa = prior_tbl4 + alt * 32, *pt = prior_tbl4 + third * 32;
 #pragma unroll
-                    for (int kk = 0; kk < KP; ++kk) {
-                        const float4 tu = pu[kk * kBases * 32], tn = pn[kk * kBases * 32], tw = pw[kk * kBases * 32];
-                        prs[2 * kk] = make_float2(all_but_prior(tu.x, tn.x, tw.x), all_but_prior(tu.y, tn.y, tw.y));
-                        prs[2 * kk + 1] = make_float2(all_but_prior(tu.z, tn.z, tw.z), all_but_prior(tu.w, tn.w, tw.w));
-                    }
-                } else {  // two bases match: the column's and `alt`
-                    const uint32_t third = (uint32_t)__ffs(~((1u << ref) | (1u << alt))) - 1u;
-                    const float4 *pa = prior_tbl4 + alt * 32, *pt = prior_tbl4 + third * 32;
-#pragma unroll
-                    for (int kk = 0; kk < KP; ++kk) {
-                        const float4 t2 = pa[kk * kBases * 32], t3 = pt[kk * kBases * 32];
-                        const float2 p0 = prs[2 * kk], p1 = prs[2 * kk + 1];
-                        prs[2 * kk] = make_float2(snp_prior(p0.x, t2.x, t3.x), snp_prior(p0.y, t2.y, t3.y));
-                        prs[2 * kk + 1] = make_float2(snp_prior(p1.x, t2.z, t3.z), snp_prior(p1.y, t2.w, t3.w));
+                        for (int kk = 0; kk < KP; ++kk) {
+                            const float4 t2 = pa[kk * kBases * 32], t3 = pt[kk * kBases * 32];
+                            const float2 p0 = prs[2 * kk], p1 = prs[2 * kk + 1];
+                            prs[2 * kk] = make_float2(snp_prior(p0.x, t2.x, t3.x), snp_prior(p0.y, t2.y, t3.y));
+                            prs[2 * kk + 1] = make_float2(snp_prior(p1.x, t2.z, t3.z), snp_prior(p1.y, t2.w, t3.w));
+                        }
                     }
                 }
-            }
-            // pass 1 (bottom-up): M~ and D~
+                // pass 1 (bottom-up): M~ and D~
 #pragma unroll
-            for (int k = K - 1; k >= 0; --k) {
-                const float2 pr = prs[k];
-                float2 Mn;
-                if (k) {
-                    Mn = mul2(pr, fma2(Ip[k - 1], cb[k], fma2(Dp[k - 1], cc[k], Mp[k - 1])));
+                for (int k = K - 1; k >= 0; --k) {
+                    const float2 pr = prs[k];
+                    float2 Mn;
+                    if (k) {
+                        Mn = mul2(pr, fma2(Ip[k - 1], cb[k], fma2(Dp[k - 1], cc[k], Mp[k - 1])));
+                    } else {
+                        Mn = mul2(pr, gW);
+                    }
+                    const float2 Dn = fma2(Dp[k], cdd[k], Mp[k]);
+                    Mp[k] = Mn;
+                    Dp[k] = Dn;
+                }
+                // pass 2 (top-down): I~ from the row above at this column
+                Ip[0] = uV;
+                if (OPS && (op & kPdOpDelEnd)) {
+#pragma unroll
+                    for (int k = 1; k < K; ++k) {
+                        float2 bi = bst[(3 * (k - 1) + 1) * 32], bm = bst[(3 * (k - 1) + 0) * 32];
+                        if (k == K - 2 && acc_lane) bi = bm = zero2();  // the first accumulator row sums row R as is
+                        Ip[k] = fma2(max2(bi, Ip[k - 1]), ce[k], max2(bm, Mp[k - 1]));
+                    }
                 } else {
-                    Mn = mul2(pr, gW);
-                }
-                const float2 Dn = fma2(Dp[k], cdd[k], Mp[k]);
-                Mp[k] = Mn;
-                Dp[k] = Dn;
-            }
-            // pass 2 (top-down): I~ from the row above at this column
-            Ip[0] = uV;
-            if (op & kPdOpDelEnd) {
 #pragma unroll
-                for (int k = 1; k < K; ++k) {
-                    float2 bi = bst[(3 * (k - 1) + 1) * 32], bm = bst[(3 * (k - 1) + 0) * 32];
-                    if (k == K - 2 && acc_lane) bi = bm = zero2();  // the first accumulator row sums row R as is
-                    Ip[k] = fma2(max2(bi, Ip[k - 1]), ce[k], max2(bm, Mp[k - 1]));
+                    for (int k = 1; k < K; ++k) Ip[k] = fma2(Ip[k - 1], ce[k], Mp[k - 1]);
                 }
-            } else {
-#pragma unroll
-                for (int k = 1; k < K; ++k) Ip[k] = fma2(Ip[k - 1], ce[k], Mp[k - 1]);
-            }
-            const float2 i_acc = Ip[K - 2];  // I~(R+1) at this column
-            // hand-over to the lane below: row 0's I~ at this column and its M~ inner sum for the next column
-            float2 hI = Ip[K - 1], hM = Mp[K - 1];
-            if ((op & kPdOpDelEnd) && !(K == 2 && lane == 30)) {  // (K = 2: lane 31's row 0 is an accumulator row)
-                hI = max2(bst[(3 * (K - 1) + 1) * 32], hI);
-                hM = max2(bst[(3 * (K - 1) + 0) * 32], hM);
-            }
-            sV = fma2(hI, e0n, hM);
-            float2 wI = Ip[K - 1], wD = Dp[K - 1], wM = Mp[K - 1];
-            if (op & kPdOpNextAfter) {
-                wI = max2(bst[(3 * (K - 1) + 1) * 32], wI);
-                wD = max2(bst[(3 * (K - 1) + 2) * 32], wD);
-                wM = max2(bst[(3 * (K - 1) + 0) * 32], wM);
-            }
-            sW = fma2(wI, b0n, fma2(wD, c0n, wM));
-            if constexpr (CHK) {
-                if (lane == 31 && (code & kColLast)) {
-                    const float2 t2 = add2(add2(Dp[K - 1], Mp[K - 1]), i_acc);
-                    emit_pd(B, t2.x, __ldg(B.read_scale + ra), ra, hap, out_a + hap);
-                    if (rb >= 0) emit_pd(B, t2.y, __ldg(B.read_scale + rb), rb, hap, out_b + hap);
+                const float2 i_acc = Ip[K - 2];  // I~(R+1) at this column
+                // hand-over to the lane below: row 0's I~ at this column and its M~ inner sum for the next column
+                float2 hI = Ip[K - 1], hM = Mp[K - 1];
+                // (K = 2: lane 31's row 0 is an accumulator row, whose I takes no max)
+                if (OPS && (op & kPdOpDelEnd) && !(K == 2 && lane == 30)) {
+                    hI = max2(bst[(3 * (K - 1) + 1) * 32], hI);
+                    hM = max2(bst[(3 * (K - 1) + 0) * 32], hM);
                 }
-            }
+                sV = fma2(hI, e0n, hM);
+                float2 wI = Ip[K - 1], wD = Dp[K - 1], wM = Mp[K - 1];
+                if (OPS && (op & kPdOpNextAfter)) {
+                    wI = max2(bst[(3 * (K - 1) + 1) * 32], wI);
+                    wD = max2(bst[(3 * (K - 1) + 2) * 32], wD);
+                    wM = max2(bst[(3 * (K - 1) + 0) * 32], wM);
+                }
+                sW = fma2(wI, b0n, fma2(wD, c0n, wM));
+                if constexpr (CHK) {
+                    if (lane == 31 && (code & kColLast)) {
+                        const float2 t2 = add2(add2(Dp[K - 1], Mp[K - 1]), i_acc);
+                        emit_pd(B, t2.x, __ldg(B.read_scale + ra), ra, hap, out_a + hap);
+                        if (rb >= 0) emit_pd(B, t2.y, __ldg(B.read_scale + rb), rb, hap, out_b + hap);
+                    }
+                }
+            };
+            // steps where no lane is at a column with PD work (about two in three) run the regular kernel's step,
+            // without the op tests: 8 % faster than testing the op bits in every step
+            if (__any_sync(kFull, op != 0u))
+                body(std::true_type{});
+            else
+                body(std::false_type{});
         };
         // Step loops unrolled 1 (checked) and 2 (check-free): the lane-divergent op branches split each step into
         // several blocks anyway, and deeper unrolling (4 and 8) overflowed the instruction cache (ncu: 6-8 cycles of
