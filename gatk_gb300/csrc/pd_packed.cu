@@ -322,9 +322,10 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
             else
                 body(std::false_type{});
         };
-        // Step loops unrolled 1 (checked) and 2 (check-free): the lane-divergent op branches split each step into
-        // several blocks anyway, and deeper unrolling (4 and 8) overflowed the instruction cache (ncu: 6-8 cycles of
-        // "no instruction" stall per issue, half the speed)
+        // Step loops not unrolled: the lane-divergent op branches and the two step bodies behind the warp vote split
+        // each step into several blocks anyway; unrolled 4 (checked) and 8 (check-free) the steps overflowed the
+        // instruction cache (ncu: 6-8 cycles of "no instruction" stall per issue, half the speed), and with the vote
+        // 2 (check-free) was still 4 % slower than 1
         const int64_t *hoff = B.hap_off + task.hap_begin;
         const int nh_task = task.hap_end - task.hap_begin;
         int s = 0, j = 0;
@@ -337,7 +338,7 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
                 continue;
             }
             const int next_boundary = (j <= nh_task) ? (int)(hoff[j] - col0) : nsteps;
-#pragma unroll 2
+#pragma unroll 1
             for (; s < next_boundary; ++s) step(s, std::false_type{});
         }
     }
