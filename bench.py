@@ -759,6 +759,7 @@ def run_pd(args):
     cpu_dt = time.perf_counter() - t1
     d = absdiff(res[: sub.n_pairs], ref)
     d64 = absdiff(res64[: sub.n_pairs], ref)
+    dall = absdiff(res[: wl.n_pairs], res64[: wl.n_pairs])
     flop_per_cell = 11  # M: mul + 2 fma, D: mul + fma, I: mul + fma (FMA = 2), as the regular recurrence
     achieved = flop_per_cell * cells / (ms_fp32 * 1e-3) / 1e12
     peak32 = max(peaks["fp32_tflops"], peaks["fp32x2_tflops"])
@@ -795,6 +796,11 @@ def run_pd(args):
                          "host": f"{platform.machine()} x{os.cpu_count()}"},
         "accuracy_vs_fp64_oracle": {"sample_pairs": int(sub.n_pairs), "max_abs_dlog10": float(d.max()),
                                     "median_abs_dlog10": float(np.median(d))},
+        # every pair of the timed workload: the default FP32 path against the GPU's all-FP64 mode (itself pinned to the
+        # oracle on the sample above, fp64_mode.max_abs_dlog10_vs_oracle)
+        "accuracy_vs_gpu_fp64_full_workload": {"pairs": int(len(dall)), "max_abs_dlog10": float(dall.max()),
+                                               "median_abs_dlog10": float(np.median(dall)),
+                                               "pairs_above_1e-3": int((dall > 1e-3).sum())},
     }
     print(json.dumps(line), flush=True)
     eng.close()
