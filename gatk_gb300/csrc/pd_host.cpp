@@ -400,6 +400,19 @@ int pd_raw_build(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions, int32_t n_reg
 
 extern "C" {
 
+int ghmm_debug_pd_ops(const uint8_t *bases, const uint8_t *pd_flags, int32_t H, uint8_t *ops, uint8_t *codes) {
+    if (H < 0 || (H > 0 && (!bases || !pd_flags || !ops || !codes))) return GHMM_ERR_ARG;
+    std::vector<uint8_t> st((size_t)H, 0);
+    const int end1 = pd_states(pd_flags, H, 0, st.data(), 0);
+    pd_states(pd_flags, H, end1, st.data(), 2);
+    for (int32_t j = 0; j < H; j++) {
+        if (pd_flags[j] & 4) st[(size_t)j] |= 16;
+        codes[j] = base_index(bases[j]);
+    }
+    pd_ops(pd_flags, bases, st.data(), H, ops, codes);
+    return pd_packable(pd_flags, H) ? 1 : 0;
+}
+
 int ghmm_pd_batch_create(ghmm_ctx *ctx, const ghmm_pd_region *regions, int32_t n_regions, ghmm_batch **out) {
     if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
     if (!out || n_regions < 0 || (n_regions > 0 && !regions)) return fail(ctx, GHMM_ERR_ARG, "bad arguments");

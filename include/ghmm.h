@@ -393,6 +393,15 @@ int ghmm_measure_peaks(ghmm_ctx *ctx, double *fp32_tflops, double *fp32x2_tflops
  * With ctx == NULL the host-built tables are returned (no device needed). */
 int ghmm_debug_tables(ghmm_ctx *ctx, double *err, double *prob, double *m2m);
 
+/* Debug/test (no device needed): the per-column op bytes of the packed FP32 PD-HMM kernel for one haplotype of H
+ * bases with PD flags (PartiallyDeterminedHaplotype bits) into ops[H] -- bit 0: copy the branch states; 1: an
+ * AFTER_DEL column; 2: a DEL_END column; 3: the next column is AFTER_DEL; 4: an undetermined SNP, its alternative in
+ * bits 5-6 (A, C, G, T = 0..3); 7 (with 4): three bases match, bits 5-6 name the fourth -- and the column base codes
+ * that kernel reads into codes[H] (A, C, G, T, N = 0..4; an SNP column whose alternatives cover all four bases reads
+ * as N).  Returns 1 when the packed kernel takes the haplotype (its row-end state is NORMAL), 0 when its pairs go to
+ * the general PD kernel, GHMM_ERR_ARG for bad arguments. */
+int ghmm_debug_pd_ops(const uint8_t *bases, const uint8_t *pd_flags, int32_t H, uint8_t *ops, uint8_t *codes);
+
 /* ---- Several devices from one caller ----
  * One handle drives several GPUs (HaplotypeCaller's one JVM; the reference parallelises the host side with GKL's
  * thread count, HC/PairHMMNativeArgumentCollection.java:11-12, or one engine per Spark partition,

@@ -144,6 +144,120 @@ def test_synthetic_flags_are_deterministic_and_well_formed():
 
 
 # ---------------------------------------------------------------------------------------------------------------
+# The packed FP32 kernel's scheme (pd_packed.cu) on the CPU, from the library's own op bytes (ghmm_debug_pd_ops):
+# branch states materialised only where an op byte asks for them, the AFTER_DEL replacement of the previous column
+# by max(bX, X), the DEL_END max, and the prior of SNP columns picked from rows of the read's prior table the way the
+# kernel picks it.  Unscaled FP64 in the oracle's operation order, so it must reproduce the oracle bit for bit.
+
+def _pd_ops(hap, pd):
+    from gatk_gb300 import native
+
+    H = len(hap)
+    ops, codes = np.zeros(H, dtype=np.uint8), np.zeros(H, dtype=np.uint8)
+    h, f = np.ascontiguousarray(hap, dtype=np.uint8), np.ascontiguousarray(pd, dtype=np.uint8)
+    rc = native.lib().ghmm_debug_pd_ops(h.ctypes.data_as(native._u8p), f.ctypes.data_as(native._u8p), H,
+                                        ops.ctypes.data_as(native._u8p), codes.ctypes.data_as(native._u8p))
+    assert rc in (0, 1)
+    return rc == 1, ops, codes
+
+
+def _lazy_branch_pdhmm(hap, read, q, ins, dl, gcp, ops, codes):
+    R, H = len(read), len(hap)
+    init = 2.0 ** 1020 / H
+    M, I, D = [0.0] * (H + 1), [0.0] * (H + 1), [init] * (H + 1)
+    B = [[0.0] * (H + 1) for _ in range(3)]  # the branch registers (stale where no op wrote them)
+    for i in range(R):
+        t = np.zeros(6)
+        O.lib().oracle_qual_to_trans_probs(t.ctypes.data_as(O._f64p), int(ins[i]), int(dl[i]), int(gcp[i]))
+        MM, IM, MI, II, MD, DD = t
+        pm = O.lib().oracle_qual_to_prob(int(q[i]))
+        pe = pm if read[i] == ord("N") else O.lib().oracle_qual_to_error_prob(int(q[i])) / 3.0
+        tbl = [pm if read[i] in (c, ord("N")) else pe for c in b"ACGT"] + [pm]  # prior table row: codes A,C,G,T,N
+        cM, cI, cD = [0.0] * (H + 1), [0.0] * (H + 1), [0.0] * (H + 1)
+        cB = [[0.0] * (H + 1) for _ in range(3)]
+        for j in range(1, H + 1):
+            o, code = int(ops[j - 1]), int(codes[j - 1])
+            prior = tbl[code]
+            if o & 16:
+                alt = (o >> 5) & 3
+                if o & 128:
+                    tu, tn, tw = tbl[alt], tbl[4], tbl[0 if alt else 1]
+                    prior = tw if tu == tn else tn
+                else:
+                    third = min(b for b in range(4) if b not in (code, alt))
+                    t1, t2, t3 = tbl[code], tbl[alt], tbl[third]
+                    prior = t1 if (t1 == t2 or t1 != t3) else t2
+            xprev = [cM[j - 1], cI[j - 1], cD[j - 1]]
+            for v in range(3):
+                if o & 2:
+                    xprev[v] = max(cB[v][j - 1], xprev[v])
+                cB[v][j] = xprev[v] if o & 3 else cB[v][j - 1]
+            above = [M[j - 1], I[j - 1], D[j - 1]]
+            if o & 2:
+                above = [max(B[v][j - 1], above[v]) for v in range(3)]
+            cM[j] = prior * (above[0] * MM + above[1] * IM + above[2] * IM)
+            cD[j] = xprev[0] * MD + xprev[2] * DD
+            if o & 4:
+                cI[j] = max(B[0][j], M[j]) * MI + max(B[1][j], I[j]) * II
+            else:
+                cI[j] = M[j] * MI + I[j] * II
+        M, I, D, B = cM, cI, cD, cB
+    s = 0.0
+    for j in range(1, H + 1):
+        s += M[j] + I[j]
+    return math.log10(s) - math.log10(2.0 ** 1020)
+
+
+def test_packed_kernel_ops_reproduce_the_oracle():
+    rng = np.random.default_rng(29)
+    n_packed = n_general = 0
+    for k in range(160):
+        H, R = int(rng.integers(20, 60)), int(rng.integers(4, 18))
+        hap, pd, read, q, ins, dls, g = _case(rng, H=H, R=R, n_snp=int(rng.integers(0, 5)),
+                                               n_del=int(rng.integers(0, 5)), dl=(1, 6), end_flag=(k % 9 == 8))
+        hap, read = hap.copy(), read.copy()
+        if k % 3 == 0:
+            pd[int(rng.integers(1, H - 1))] |= DS | DE  # single-base deletion
+        if k % 4 == 1:  # SNP columns with two and three alternatives, and one on an N column
+            for j in rng.choice(np.arange(H), size=3, replace=False):
+                pd[j] |= SNP
+                for c in rng.choice(list(b"ACGT"), size=int(rng.integers(2, 4)), replace=False):
+                    pd[j] |= BIT[int(c)]
+            j = int(rng.integers(0, H))
+            hap[j] = ord("N")
+            pd[j] |= SNP | BIT[ord("C")]
+        if k % 5 == 2:
+            read[int(rng.integers(0, R))] = ord("N")
+        packed, ops, codes = _pd_ops(hap, pd)
+        if not packed:  # a state left open at the row's end: the general kernel's pairs
+            n_general += 1
+            continue
+        n_packed += 1
+        ref = O.pd_logless(hap, pd, read, q, ins, dls, g)
+        assert _lazy_branch_pdhmm(hap, read, q, ins, dls, g, ops, codes) == ref, k
+    assert n_packed > 120 and n_general > 0
+
+
+def test_packed_kernel_ops_hand_cases():
+    # a deletion from column 2 to 4 (0-based): copy at its start column, DEL_END and next-AFTER at its end, AFTER after
+    hap = np.frombuffer(b"ACGTACGTAC", dtype=np.uint8)
+    pd = np.zeros(10, dtype=np.uint8)
+    pd[2] |= DS
+    pd[4] |= DE
+    pd[7] |= SNP | BIT[ord("G")]  # column base T, alternative G
+    pd[8] |= SNP | BIT[ord("A")] | BIT[ord("C")] | BIT[ord("G")] | BIT[ord("T")]
+    pd[9] |= SNP | BIT[ord("A")] | BIT[ord("G")]  # column base C: C, A and G match, T does not
+    packed, ops, codes = _pd_ops(hap, pd)
+    assert packed
+    assert list(ops[:6]) == [0, 0, 1, 0, 4 | 8, 2]
+    assert ops[7] == 16 | (2 << 5) and codes[7] == 3
+    assert ops[8] == 0 and codes[8] == 4  # every base matches: the column reads as N
+    assert ops[9] == 16 | 128 | (3 << 5) and codes[9] == 1
+    pd[9] = DE  # a deletion ending on the last column leaves AFTER_DEL open for the next row
+    assert not _pd_ops(hap, pd)[0]
+
+
+# ---------------------------------------------------------------------------------------------------------------
 # the GPU PD-HMM kernel (pd.cu) against the oracle
 
 def _pd_workload(regions=6, seed=5):
