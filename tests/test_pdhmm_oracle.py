@@ -524,7 +524,27 @@ def test_gpu_pdhmm_packed_kernel_every_op(engine, engine64):
     single = [([wl.hap(h) for h in range(int(wl.region_hap_off[g]), int(wl.region_hap_off[g + 1]))], [wl.read(r)])
               for g in range(wl.n_regions) for r in range(int(wl.region_read_off[g]), int(wl.region_read_off[g + 1]))]
     wl1 = W.from_pairs(single)
-    pd1 = np.concatenate([pd[int(wl.hap_off[wl.region_hap_off[g]]):int(wl.hap_off[wl.region_hap_off[g + 1]])]
-                          for g in range(wl.n_regions) for _ in range(int(wl.region_read_off[g + 1] - wl.region_read_off[g]))])
+    region_pd = [pd[int(wl.hap_off[wl.region_hap_off[g]]):int(wl.hap_off[wl.region_hap_off[g + 1]])]
+                 for g in range(wl.n_regions)]
+    pd1 = np.concatenate([region_pd[g] for g in range(wl.n_regions)
+                          for _ in range(int(wl.region_read_off[g + 1] - wl.region_read_off[g]))])
     ref1 = O.pd_compute_workload(wl1, pd1)
     assert np.abs(engine.pd_compute(wl1, pd1) - ref1).max() <= 1e-3
+    # regions without reads or without haplotypes among ordinary ones, over several pipelined chunks
+    rng = np.random.default_rng(43)
+    mixed = []
+    for g in range(40):
+        haps = [] if g % 7 == 3 else [bytes(rng.choice(list(b"ACGT"), size=int(rng.integers(30, 200))).astype(np.uint8))
+                                      for _ in range(3)]
+        reads = []
+        if g % 5 != 2:
+            for _ in range(int(rng.integers(1, 6))):
+                n = int(rng.integers(10, 120))
+                reads.append((bytes(rng.choice(list(b"ACGT"), size=n).astype(np.uint8)), rng.integers(10, 41, size=n),
+                              np.full(n, 40), np.full(n, 40), np.full(n, 10)))
+        mixed.append((haps, reads))
+    wl2 = W.from_pairs(mixed)
+    pd2 = W.pd_flags(wl2, 9)
+    ref2 = O.pd_compute_workload(wl2, pd2)
+    assert np.abs(engine.pd_compute(wl2, pd2) - ref2).max() <= 1e-3
+    assert np.abs(engine64.pd_compute(wl2, pd2) - ref2).max() <= 1e-9
