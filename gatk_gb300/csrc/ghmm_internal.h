@@ -110,7 +110,8 @@ struct PdPlanes {
     const uint8_t *ops;  // per column the packed FP32 kernel's op byte, indexed like hap_code (kCodePad zeros around)
 };
 // Op bits of the packed FP32 PD kernel (pd_packed.cu), derived per haplotype column by the host (pd_host.cpp).
-constexpr uint32_t kPdOpCopy = 1;       // NORMAL column whose branch state a later column reads: bX = previous X
+constexpr uint32_t kPdOpCopy = 1;       // a later column reads this column's branch state: store it (NORMAL: bX =
+                                        // previous X; AFTER_DEL: bX = max(bX, previous X))
 constexpr uint32_t kPdOpAfter = 2;      // AFTER_DEL column
 constexpr uint32_t kPdOpDelEnd = 4;     // DEL_END column: I reads max(bX, X) of the row above
 constexpr uint32_t kPdOpNextAfter = 8;  // the next column is AFTER_DEL

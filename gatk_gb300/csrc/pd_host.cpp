@@ -65,7 +65,8 @@ static bool pd_packable(const uint8_t *f, int H) {
 // The packed kernel's op byte of every column of one haplotype (pd_packed.cu), from its flags f, its bytes y and the
 // state codes of pd_states (bits 2-3: the state of rows >= 2, equal to the first row's for a packable haplotype).
 // A column's branch state is needed when the next column is AFTER_DEL (it reads it), when the next column is
-// INSIDE_DEL and needs its own (it keeps it), or when the column ends a deletion (the row below's I reads it).  An
+// INSIDE_DEL and needs its own (it keeps it), or when the column ends a deletion (the row below's I reads it); only
+// then does a NORMAL or AFTER_DEL column store it (kPdOpCopy).  An
 // SNP column whose alternatives and base cover all four bases gets the column code of N in code (the column-code
 // plane), which matches every read base as isBasePDMatching then does.
 static void pd_ops(const uint8_t *f, const uint8_t *y, const uint8_t *states, int H, uint8_t *op, uint8_t *code) {
@@ -76,7 +77,7 @@ static void pd_ops(const uint8_t *f, const uint8_t *y, const uint8_t *states, in
         const bool del_end = (f[j] & 4) != 0;
         const bool need = st_next == 2 || (st_next == 1 && need_next) || del_end;
         uint32_t o = 0;
-        if (st == 0 && need) o |= kPdOpCopy;
+        if (st != 1 && need) o |= kPdOpCopy;  // (INSIDE_DEL keeps the branch state it has)
         if (st == 2) o |= kPdOpAfter;
         if (del_end) o |= kPdOpDelEnd;
         if (st_next == 2) o |= kPdOpNextAfter;

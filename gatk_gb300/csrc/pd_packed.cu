@@ -16,11 +16,11 @@
 // positive factor commutes with max, so the branch states live in the same rescaled form as the states they copy.
 //
 // The PD work is per column, from an op byte the host derives from the flags (pd_host.cpp):
-//  * kPdOpCopy: bX(j) = X(j-1), only at NORMAL columns whose branch state a later column reads (the column before
-//    a deletion's INSIDE_DEL or AFTER_DEL columns, or a DEL_END column).  Elsewhere the branch registers go stale
-//    and nothing reads them, so most columns do no branch work at all.
+//  * kPdOpCopy: store the column's branch states, only where a later column reads them (the column before a
+//    deletion's INSIDE_DEL or AFTER_DEL columns, or a DEL_END column): bX(j) = X(j-1) at a NORMAL column.  Elsewhere
+//    the branch states go stale and nothing reads them, so most columns do no branch work at all.
 //  * kPdOpAfter: the previous column's M, I, D of every row are replaced by max(bX, X) before the step (every use
-//    of them in an AFTER_DEL column is that max) and the branch states take the same values.
+//    of them in an AFTER_DEL column is that max); with kPdOpCopy the branch states take the same values.
 //  * kPdOpDelEnd: I of rows 1..K-1 reads max(bX, X) of the row above; row 0's I~ comes from the lane above, which
 //    applies the max in its hand-over at this column.
 //  * kPdOpNextAfter: the next column is AFTER_DEL, so the lane's hand-over of row 0's M~ inner sum for it (the
@@ -221,12 +221,14 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
                             Dp[k] = max2(bst[(3 * k + 2) * 32], Dp[k]);
                         }
                     }
+                    if (op & kPdOpCopy) {  // (an AFTER_DEL column stores only when a later column reads it)
 #pragma unroll
-                    for (int k = 0; k < K; ++k) {
-                        if (k >= K - 2 && acc_lane) continue;
-                        bst[(3 * k + 0) * 32] = Mp[k];
-                        bst[(3 * k + 1) * 32] = Ip[k];
-                        bst[(3 * k + 2) * 32] = Dp[k];
+                        for (int k = 0; k < K; ++k) {
+                            if (k >= K - 2 && acc_lane) continue;
+                            bst[(3 * k + 0) * 32] = Mp[k];
+                            bst[(3 * k + 1) * 32] = Ip[k];
+                            bst[(3 * k + 2) * 32] = Dp[k];
+                        }
                     }
                 }
                 const uint32_t ref = code & 7u;

@@ -191,7 +191,7 @@ def _lazy_branch_pdhmm(hap, read, q, ins, dl, gcp, ops, codes):
             for v in range(3):
                 if o & 2:
                     xprev[v] = max(cB[v][j - 1], xprev[v])
-                cB[v][j] = xprev[v] if o & 3 else cB[v][j - 1]
+                cB[v][j] = xprev[v] if o & 1 else cB[v][j - 1]  # stored only where a later column reads it
             above = [M[j - 1], I[j - 1], D[j - 1]]
             if o & 2:
                 above = [max(B[v][j - 1], above[v]) for v in range(3)]
