@@ -118,10 +118,18 @@ int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch 
             if (hp.length > 0 && (!hp.bases || !hp.pd_bases)) return fail(ctx, GHMM_ERR_ARG, "NULL PD haplotype array");
             hh[(size_t)g][(size_t)h] = ghmm_hap{hp.bases, hp.length};
             pdp.push_back(hp.pd_bases);
-            if (hp.length > 0 && !pd_packable(hp.pd_bases, hp.length)) region_direct[(size_t)g] = 1;
         }
         rr[(size_t)g] = ghmm_region{rg.reads, rg.n_reads, hh[(size_t)g].data(), rg.n_haps};
     }
+    parallel_for(G, hw_threads(ctx->max_threads), [&](int64_t g) {
+        for (int32_t h = 0; h < regs[g].n_haps; h++) {
+            const ghmm_pd_hap &hp = regs[g].haps[h];
+            if (hp.length > 0 && !pd_packable(hp.pd_bases, hp.length)) {
+                region_direct[(size_t)g] = 1;
+                break;
+            }
+        }
+    }, 16);
     Source src;
     src.regions = rr.data();
     src.n_regions = G;
