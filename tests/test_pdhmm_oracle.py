@@ -352,6 +352,32 @@ def test_gpu_pdhmm_hand_cases_and_long_reads(engine):
 
 
 @pytest.mark.gpu
+def test_gpu_pdhmm_error_in_a_later_chunk(engine):
+    # a read base outside ACGTacgtN meets an undetermined SNP in the last of 30 regions: the one-shot call marshals
+    # that region's chunk while earlier chunks run, returns GHMM_ERR_ARG, and the engine computes correctly afterwards
+    from gatk_gb300 import native
+
+    wl, pd = _pd_workload(30, seed=6)
+    g = wl.n_regions - 1
+    r, h = int(wl.region_read_off[g]), int(wl.region_hap_off[g])
+    a, j = int(wl.read_off[r]), int(wl.hap_off[h])
+    bases = wl.bases.copy()
+    bases[a] = ord("R")
+    flags = pd.copy()
+    flags[j] |= SNP | BIT[ord("A")]
+    bad = W.Workload(region_read_off=wl.region_read_off, region_hap_off=wl.region_hap_off, read_off=wl.read_off,
+                     bases=bases, quals=wl.quals, ins=wl.ins, dels=wl.dels, gcp=wl.gcp, hap_off=wl.hap_off,
+                     hap_bases=wl.hap_bases, out_off=wl.out_off)
+    if wl.hap_bases[j] == ord("R"):
+        pytest.skip("the haplotype base equals the planted read base")
+    with pytest.raises(native.GhmmError) as e:
+        engine.pd_compute(bad, flags)
+    assert e.value.code == native.GHMM_ERR_ARG
+    ref = O.pd_compute_workload(wl, pd)
+    assert np.abs(engine.pd_compute(wl, pd) - ref).max() <= 1e-3
+
+
+@pytest.mark.gpu
 def test_gpu_pdhmm_batch_and_errors(engine):
     from gatk_gb300 import native
 
