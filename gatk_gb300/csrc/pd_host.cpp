@@ -330,31 +330,15 @@ int pd_forward_finish(ghmm_ctx *ctx, ghmm_batch &b) {
 
 // The one-shot PD-HMM calls in chunks of regions, pipelined on two streams: chunk i+1 is marshalled on the host and
 // enqueued (upload, preparation, forward) on the other slot's stream while chunk i runs, so its kernels start as
-// chunk i's last tasks leave SMs free; then chunk i's results are read.  Three chunks, of 1/8, 3/8 and 1/2 of the
-// cells: on 1,000 regions of workload 1 with PD flags, 85 ms a call against 112 ms for the regular pipelined calls'
-// finer cut (1/16 growing by 2.5) and 84 ms unchunked; on 3,000 regions, 198 ms against 209 ms and 232 ms.
-// host(g0, g1, slot) stages regions [g0, g1) in ctx->pd_batch[slot]; device(slot, stream) uploads it (and prepares
-// raw reads).
+// chunk i's last tasks leave SMs free; then chunk i's results are read.  Chunks as pipeline_cuts cuts them (below
+// 5e11 cells three, of 1/8, 3/8 and 1/2 of the cells: on 1,000 regions of workload 1 with PD flags, 85 ms a call
+// against 112 ms for the finer cut of large inputs and 84 ms unchunked; on 3,000 regions, 198 ms against 209 ms and
+// 232 ms).  host(g0, g1, slot) stages regions [g0, g1) in ctx->pd_batch[slot]; device(slot, stream) uploads it (and
+// prepares raw reads).
 int pd_pipelined(ghmm_ctx *ctx, const std::vector<int64_t> &cells, const std::vector<int64_t> &outo, double *out,
                  const std::function<int(int64_t, int64_t, int)> &host,
                  const std::function<int(int, cudaStream_t)> &device) {
-    const int64_t G = (int64_t)cells.size();
-    std::vector<int64_t> cut{0};
-    int64_t total = 0;
-    for (int64_t c : cells) total += c;
-    {  // cuts after 1/8 and 1/2 of the cells, none that leaves fewer than 8 regions behind
-        const int64_t marks[2] = {total / 8, total / 2};
-        int64_t c = 0;
-        int m = 0;
-        for (int64_t g = 0; g < G && m < 2; g++) {
-            c += cells[(size_t)g];
-            if (c >= marks[m] && G - g - 1 >= 8) {
-                cut.push_back(g + 1);
-                m++;
-            }
-        }
-        cut.push_back(G);
-    }
+    const std::vector<int64_t> cut = pipeline_cuts(cells);
     if (!ctx->pd_stream2) GHMM_CUDA(cudaStreamCreateWithFlags(&ctx->pd_stream2, cudaStreamNonBlocking), "cudaStreamCreate");
     const cudaStream_t streams[2] = {ctx->stream, ctx->pd_stream2};
     const bool fp32 = !ctx->double_precision;

@@ -316,6 +316,7 @@ int pipelined_compute(ghmm_ctx *ctx, const Source &src, const std::vector<int64_
                       int32_t max_len = 0, const ghmm_read_prep *prep = nullptr, const RouteBound *bound = nullptr);
 bool region_sizes(const Source &src, std::vector<int64_t> &cells, std::vector<int64_t> &outo);
 int compute_sync(ghmm_ctx *ctx, const Source &src, double *out);
+std::vector<int64_t> pipeline_cuts(const std::vector<int64_t> &cells);  // region cuts of a pipelined call
 
 // pd_host.cpp
 int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch &b, const RouteBound *bound);
