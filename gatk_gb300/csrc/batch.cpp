@@ -290,7 +290,7 @@ int batch_marshal(ghmm_ctx *ctx, const Source &src, ghmm_batch &b) {
             groups.clear();
             for (int64_t r = r0; r < r1; r++) {
                 const int R = (int)(read_off[(size_t)r + 1] - read_off[(size_t)r]);
-                if (region_fp64 || (read_flag[(size_t)r] & 1) || (src.single_strip && R + kAccRows > 32 * max_k)) {
+                if (region_fp64 || (read_flag[(size_t)r] & 1)) {
                     auto &dst = (read_flag[(size_t)r] & 4) ? po.direct_exact : po.direct;
                     for (int64_t h = h0; h < h1; h++) dst.push_back(PairRef{(int32_t)r, (int32_t)h});
                     po.cells_direct += (int64_t)R * region_cols;

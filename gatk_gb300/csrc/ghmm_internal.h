@@ -118,9 +118,9 @@ constexpr uint32_t kPdOpNextAfter = 8;  // the next column is AFTER_DEL
 constexpr uint32_t kPdOpSnp = 16;       // undetermined SNP: its alternative in bits 5-6 (A, C, G, T = 0..3)
 constexpr int kPdOpAltShift = 5;
 constexpr uint32_t kPdOpSnpAllBut = 128;  // with kPdOpSnp: three bases match, bits 5-6 name the fourth
-// FP32 PD read-pair tasks of bucket k (2..8 rows per lane, single strip) from the batch's task list.
-int launch_pd_bucket(const DevTables &t, const DevBatch &b, const uint8_t *ops, int k, int grid, cudaStream_t s);
-int pd_bucket_occupancy(int k, int *blocks_per_sm);
+// FP32 PD read-pair tasks of bucket key (2..8 rows per lane, | 16 for multi-strip tasks) from the batch's task list.
+int launch_pd_bucket(const DevTables &t, const DevBatch &b, const uint8_t *ops, int key, int grid, cudaStream_t s);
+int pd_bucket_occupancy(int key, int *blocks_per_sm);
 int pd_kernel_occupancy(int *blocks_per_sm);
 // PD pairs [begin, begin + count) of the pair list (count_dev: the count in device memory), K rows per lane, in
 // FP32 (underflows queued for FP64 at rerun[rerun_capacity..)) or FP64; cursor is the counter the warps draw from.

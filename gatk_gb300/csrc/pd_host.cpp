@@ -135,7 +135,6 @@ int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch 
     src.n_regions = G;
     src.bound = bound;
     src.region_direct = region_direct.data();
-    src.single_strip = true;
     int rc = batch_marshal(ctx, src, b);
     if (rc) return rc;
     const int64_t NH = b.n_haps, HB = b.hap_bytes;
@@ -274,7 +273,8 @@ int pd_forward_enqueue(ghmm_ctx *ctx, ghmm_batch &b, bool fp32, cudaStream_t s) 
             int bp = 0;
             if (pd_bucket_occupancy(bk.key, &bp) != 0 || bp <= 0) bp = 1;
             const int64_t want = (bk.count + kWarpsPerBlock - 1) / kWarpsPerBlock;
-            const int g = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->sm_count * bp));
+            int g = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->sm_count * bp));
+            if (bk.key & 16) g = std::min(g, bk.grid);  // the strip scratch is sized for the regular kernel's grid
             int e = launch_pd_bucket(ctx->tables, b.dev, b.pd.ops, bk.key, g, s);
             if (e) return cuda_fail(ctx, (cudaError_t)e, "PD-HMM packed launch");
             launches++;

@@ -34,10 +34,12 @@
 // never take a branch state (theirs stay 0, so max(bX, X) = X for them), and the first accumulator row's I never
 // takes the DEL_END max, since it sums the read's last row rather than stepping the recurrence.
 //
-// The host sends a region to the general PD kernel (pd.cu) instead when a haplotype's state carries from the end
-// of a row into the next row (the first row would then see other states than the rest); reads the regular routing
-// sends to FP64, and reads that need more than one strip, go there too.  A sum below GHMM_FP32_RERUN_THRESHOLD (or
-// not finite) queues the pair for the FP64 PD kernel.
+// Reads longer than 32 K - 2 rows run in strips as in the regular kernel: lane 31 of a strip stores per column its
+// hand-over to the row below (with the PD max where the column asks for it) for lane 0 of the next strip; the
+// accumulator rows and their exclusions belong to the last strip.  The host sends a region to the general PD kernel
+// (pd.cu) instead when a haplotype's state carries from the end of a row into the next row (the first row would then
+// see other states than the rest); reads the regular routing sends to FP64 go there too.  A sum below
+// GHMM_FP32_RERUN_THRESHOLD (or not finite) queues the pair for the FP64 PD kernel.
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -94,12 +96,14 @@ struct PdMinBlocks {
     static constexpr int value = 3;
 };
 
-template <int K>
+template <int K, bool MULTI>
 __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(DevTables T, DevBatch B,
                                                                              const uint8_t *ops_plane) {
     static_assert(K >= 2, "the accumulator rows need two rows of lane 31");
-    const int task_begin = B.bucket_info[K], task_count = B.bucket_info[kNumBucketKeys + K];
-    const int counter_slot = kCounterBucketBase + K;
+    constexpr int KEY = K | (MULTI ? 16 : 0);
+    constexpr int S = 32 * K;
+    const int task_begin = B.bucket_info[KEY], task_count = B.bucket_info[kNumBucketKeys + KEY];
+    const int counter_slot = kCounterBucketBase + KEY;
     const int lane = threadIdx.x & 31;
     constexpr int KP = (K + 1) / 2;  // row pairs of the prior table
     extern __shared__ float4 pd_prior_smem4[];
@@ -108,7 +112,10 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
     // branch states bM, bI, bD of the lane's rows, lane-private: [row][M, I, D][lane] after the 4 warps' tables
     float2 *bst = reinterpret_cast<float2 *>(pd_prior_smem4 + 4 * (KP * kBases * 32)) +
                   (size_t)(threadIdx.x >> 5) * (K * 3 * 32) + lane;
-    const bool acc_lane = lane == 31;  // its last two rows are the accumulator rows of both reads
+    // strip boundary of multi-strip tasks: per column lane 31's hand-over (I~ and the M~ inner sum) for lane 0 of
+    // the next strip, as the regular kernel passes it
+    float2 *scratch = nullptr;
+    if (MULTI) scratch = B.scratch32 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * B.scratch32_cols * 3;
 
     for (;;) {
         int t = 0;
@@ -135,213 +142,255 @@ __global__ void __launch_bounds__(128, PdMinBlocks<K>::value) pd_bucket_kernel(D
         const int ncols = (int)(B.hap_off[task.hap_end] - col0);
         const uint8_t *stream = B.hap_code + col0;
         const uint8_t *opstream = ops_plane + col0;
+        const int nstrips = MULTI ? task.nstrips : 1;
 
-        float2 cb[K], cc[K], ce[K], cdd[K];
-        __syncwarp();  // the previous task's steps have finished reading this warp's table
+        for (int strip = 0; strip < nstrips; ++strip) {
+            const bool last_strip = strip == nstrips - 1;
+            const bool acc_lane = lane == 31 && last_strip;  // its last two rows are the accumulator rows of both reads
+            float2 cb[K], cc[K], ce[K], cdd[K];
+            __syncwarp();  // the previous task's (or strip's) steps have finished reading this warp's table
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const int slot = lane * K + k;
-            const RowCoef a = row_coef(T, B, off_a, len_a, slot - task.pad_a);
-            const RowCoef b = row_coef(T, B, off_b, rb >= 0 ? len_b : 0, slot - task.pad_b);
-            cb[k] = make_float2(a.b, b.b);
-            cc[k] = make_float2(a.c, b.c);
-            ce[k] = make_float2(a.e, b.e);
-            cdd[k] = make_float2(a.dd, b.dd);
+            for (int k = 0; k < K; ++k) {
+                const int slot = strip * S + lane * K + k;
+                const RowCoef a = row_coef(T, B, off_a, len_a, slot - task.pad_a);
+                const RowCoef b = row_coef(T, B, off_b, rb >= 0 ? len_b : 0, slot - task.pad_b);
+                cb[k] = make_float2(a.b, b.b);
+                cc[k] = make_float2(a.c, b.c);
+                ce[k] = make_float2(a.e, b.e);
+                cdd[k] = make_float2(a.dd, b.dd);
 #pragma unroll
-            for (int h = 0; h < kBases; ++h) {
-                const uint32_t hm = kBaseMask[h];
-                prior_tbl2[((k / 2) * kBases + h) * 64 + (k & 1)] =
-                    make_float2((a.code & hm) ? a.pm : a.pe, (b.code & hm) ? b.pm : b.pe);
-            }
-        }
-        float2 b0n = shfl_down2(cb[0]), c0n = shfl_down2(cc[0]), e0n = shfl_down2(ce[0]);
-        if (lane == 31) b0n = c0n = e0n = zero2();
-        __syncwarp();
-        float2 Mp[K], Ip[K], Dp[K];
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            Mp[k] = Ip[k] = Dp[k] = zero2();
-            bst[(3 * k + 0) * 32] = bst[(3 * k + 1) * 32] = bst[(3 * k + 2) * 32] = zero2();
-        }
-        float2 gW = zero2(), w0 = zero2();
-        float2 pendV = zero2(), pendW1 = zero2(), pendW2 = zero2();
-        float2 sV = zero2(), sW = zero2();
-        int hap = task.hap_begin - 1;
-        const int nsteps = ncols + 62;
-        // code and op of the next step's column, loaded a step ahead (both planes have kCodePad zero bytes on
-        // either side, so columns just outside the stream read as code 0 and no op)
-        uint32_t code_next = (uint32_t)__ldg(stream - 2 * lane);
-        uint32_t op_next = (uint32_t)__ldg(opstream - 2 * lane);
-        auto step = [&](const int s, auto chk_tag) {
-            constexpr bool CHK = decltype(chk_tag)::value;
-            const int c = s - 2 * lane;
-            uint32_t code = code_next, op = op_next;
-            code_next = (uint32_t)__ldg(stream + c + 1);
-            op_next = (uint32_t)__ldg(opstream + c + 1);
-            if constexpr (CHK) {
-                const bool valid = (c >= 0) && (c < ncols);
-                code = valid ? code : 0u;
-                op = valid ? op : 0u;
-            }
-            const float2 shV = shfl_up2(sV);
-            const float2 shW = shfl_up2(sW);
-            float2 uV = pendV;
-            gW = pendW2;
-            pendV = shV;
-            pendW2 = pendW1;
-            pendW1 = shW;
-            if (lane == 0) uV = zero2();
-            if constexpr (CHK) {
-                if (code & kColFirst) {
-                    ++hap;
-                    const float init = __ldg(B.hap_init_f + hap);
-                    const float2 X = make_float2(init, rb >= 0 ? init : 0.f);
-                    const int slot0 = lane * K;
-#pragma unroll
-                    for (int k = 0; k < K; ++k) {
-                        Mp[k] = Ip[k] = zero2();
-                        Dp[k] = make_float2((slot0 + k < task.pad_a) ? X.x : 0.f, (slot0 + k < task.pad_b) ? X.y : 0.f);
-                    }
-                    const float2 gD = make_float2((slot0 - 1 < task.pad_a) ? X.x : 0.f,
-                                                  (slot0 - 1 < task.pad_b) ? X.y : 0.f);
-                    gW = mul2(cc[0], gD);
-                    if (lane == 0) w0 = mul2(cc[0], X);
+                for (int h = 0; h < kBases; ++h) {
+                    const uint32_t hm = kBaseMask[h];
+                    prior_tbl2[((k / 2) * kBases + h) * 64 + (k & 1)] =
+                        make_float2((a.code & hm) ? a.pm : a.pe, (b.code & hm) ? b.pm : b.pe);
                 }
             }
-            if (lane == 0) gW = w0;
-            auto body = [&](auto ops_tag) {
-                constexpr bool OPS = decltype(ops_tag)::value;
-                // branch states at this column, from the previous column's values (still in Mp, Ip, Dp)
-                if (OPS && (op & (kPdOpCopy | kPdOpAfter))) {
-                    if (op & kPdOpAfter) {
-#pragma unroll
-                        for (int k = 0; k < K; ++k) {
-                            Mp[k] = max2(bst[(3 * k + 0) * 32], Mp[k]);
-                            Ip[k] = max2(bst[(3 * k + 1) * 32], Ip[k]);
-                            Dp[k] = max2(bst[(3 * k + 2) * 32], Dp[k]);
-                        }
-                    }
-                    if (op & kPdOpCopy) {  // (an AFTER_DEL column stores only when a later column reads it)
-#pragma unroll
-                        for (int k = 0; k < K; ++k) {
-                            if (k >= K - 2 && acc_lane) continue;
-                            bst[(3 * k + 0) * 32] = Mp[k];
-                            bst[(3 * k + 1) * 32] = Ip[k];
-                            bst[(3 * k + 2) * 32] = Dp[k];
-                        }
-                    }
+            float2 b0n = shfl_down2(cb[0]), c0n = shfl_down2(cc[0]), e0n = shfl_down2(ce[0]);
+            if (lane == 31) {  // the row below lane 31: the next strip's first row, or none
+                b0n = c0n = e0n = zero2();
+                if (MULTI && !last_strip) {
+                    const int slot = (strip + 1) * S;
+                    const RowCoef a = row_coef(T, B, off_a, len_a, slot - task.pad_a);
+                    const RowCoef b = row_coef(T, B, off_b, rb >= 0 ? len_b : 0, slot - task.pad_b);
+                    b0n = make_float2(a.b, b.b);
+                    c0n = make_float2(a.c, b.c);
+                    e0n = make_float2(a.e, b.e);
                 }
-                const uint32_t ref = code & 7u;
-                const float4 *pri4 = prior_tbl4 + ref * 32;
-                float2 prs[2 * KP];
+            }
+            __syncwarp();
+            float2 Mp[K], Ip[K], Dp[K];
 #pragma unroll
-                for (int kk = 0; kk < KP; ++kk) {
-                    const float4 v = pri4[kk * kBases * 32];
-                    prs[2 * kk] = make_float2(v.x, v.y);
-                    prs[2 * kk + 1] = make_float2(v.z, v.w);
-                }
-                if (OPS && (op & kPdOpSnp)) {
-                    const uint32_t alt = (op >> kPdOpAltShift) & 3u;
-                    if (op & kPdOpSnpAllBut) {  // three bases match: all but `alt`
-                        const uint32_t w = alt ? 0u : 1u;
-                        const float4 *pu = prior_tbl4 + alt * 32, *pn = prior_tbl4 + 4 * 32;
-                        const float4 *pw = prior_tbl4 + w * 32;
-#pragma unroll
-                        for (int kk = 0; kk < KP; ++kk) {
-                            const float4 tu = pu[kk * kBases * 32], tn = pn[kk * kBases * 32];
-                            const float4 tw = pw[kk * kBases * 32];
-                            prs[2 * kk] = make_float2(all_but_prior(tu.x, tn.x, tw.x), all_but_prior(tu.y, tn.y, tw.y));
-                            prs[2 * kk + 1] =
-                                make_float2(all_but_prior(tu.z, tn.z, tw.z), all_but_prior(tu.w, tn.w, tw.w));
-                        }
-                    } else {  // two bases match: the column's and `alt`
-                        const uint32_t third = (uint32_t)__ffs(~((1u << ref) | (1u << alt))) - 1u;
-                        const float4 *pa = prior_tbl4 + alt * 32, *pt = prior_tbl4 + third * 32;
-#pragma unroll
-                        for (int kk = 0; kk < KP; ++kk) {
-                            const float4 t2 = pa[kk * kBases * 32], t3 = pt[kk * kBases * 32];
-                            const float2 p0 = prs[2 * kk], p1 = prs[2 * kk + 1];
-                            prs[2 * kk] = make_float2(snp_prior(p0.x, t2.x, t3.x), snp_prior(p0.y, t2.y, t3.y));
-                            prs[2 * kk + 1] = make_float2(snp_prior(p1.x, t2.z, t3.z), snp_prior(p1.y, t2.w, t3.w));
-                        }
-                    }
-                }
-                // pass 1 (bottom-up): M~ and D~
-#pragma unroll
-                for (int k = K - 1; k >= 0; --k) {
-                    const float2 pr = prs[k];
-                    float2 Mn;
-                    if (k) {
-                        Mn = mul2(pr, fma2(Ip[k - 1], cb[k], fma2(Dp[k - 1], cc[k], Mp[k - 1])));
-                    } else {
-                        Mn = mul2(pr, gW);
-                    }
-                    const float2 Dn = fma2(Dp[k], cdd[k], Mp[k]);
-                    Mp[k] = Mn;
-                    Dp[k] = Dn;
-                }
-                // pass 2 (top-down): I~ from the row above at this column
-                Ip[0] = uV;
-                if (OPS && (op & kPdOpDelEnd)) {
-#pragma unroll
-                    for (int k = 1; k < K; ++k) {
-                        float2 bi = bst[(3 * (k - 1) + 1) * 32], bm = bst[(3 * (k - 1) + 0) * 32];
-                        if (k == K - 2 && acc_lane) bi = bm = zero2();  // the first accumulator row sums row R as is
-                        Ip[k] = fma2(max2(bi, Ip[k - 1]), ce[k], max2(bm, Mp[k - 1]));
-                    }
-                } else {
-#pragma unroll
-                    for (int k = 1; k < K; ++k) Ip[k] = fma2(Ip[k - 1], ce[k], Mp[k - 1]);
-                }
-                const float2 i_acc = Ip[K - 2];  // I~(R+1) at this column
-                // hand-over to the lane below: row 0's I~ at this column and its M~ inner sum for the next column
-                float2 hI = Ip[K - 1], hM = Mp[K - 1];
-                // (K = 2: lane 31's row 0 is an accumulator row, whose I takes no max)
-                if (OPS && (op & kPdOpDelEnd) && !(K == 2 && lane == 30)) {
-                    hI = max2(bst[(3 * (K - 1) + 1) * 32], hI);
-                    hM = max2(bst[(3 * (K - 1) + 0) * 32], hM);
-                }
-                sV = fma2(hI, e0n, hM);
-                float2 wI = Ip[K - 1], wD = Dp[K - 1], wM = Mp[K - 1];
-                if (OPS && (op & kPdOpNextAfter)) {
-                    wI = max2(bst[(3 * (K - 1) + 1) * 32], wI);
-                    wD = max2(bst[(3 * (K - 1) + 2) * 32], wD);
-                    wM = max2(bst[(3 * (K - 1) + 0) * 32], wM);
-                }
-                sW = fma2(wI, b0n, fma2(wD, c0n, wM));
+            for (int k = 0; k < K; ++k) {
+                Mp[k] = Ip[k] = Dp[k] = zero2();
+                bst[(3 * k + 0) * 32] = bst[(3 * k + 1) * 32] = bst[(3 * k + 2) * 32] = zero2();
+            }
+            float2 gW = zero2(), w0 = zero2();
+            float2 pendV = zero2(), pendW1 = zero2(), pendW2 = zero2();
+            float2 sV = zero2(), sW = zero2();
+            float2 nxV = zero2(), nxW = zero2(), l0W = zero2();  // lane 0 of a later strip: the strip above's hand-over
+            if (MULTI && strip > 0 && lane == 0 && ncols > 0) {
+                nxV = scratch[0];
+                nxW = scratch[1];
+            }
+            int hap = task.hap_begin - 1;
+            const int nsteps = ncols + 62;
+            // code and op of the next step's column, loaded a step ahead (both planes have kCodePad zero bytes on
+            // either side, so columns just outside the stream read as code 0 and no op)
+            uint32_t code_next = (uint32_t)__ldg(stream - 2 * lane);
+            uint32_t op_next = (uint32_t)__ldg(opstream - 2 * lane);
+            auto step = [&](const int s, auto chk_tag) {
+                constexpr bool CHK = decltype(chk_tag)::value;
+                const int c = s - 2 * lane;
+                uint32_t code = code_next, op = op_next;
+                code_next = (uint32_t)__ldg(stream + c + 1);
+                op_next = (uint32_t)__ldg(opstream + c + 1);
+                bool valid = true;
                 if constexpr (CHK) {
-                    if (lane == 31 && (code & kColLast)) {
-                        const float2 t2 = add2(add2(Dp[K - 1], Mp[K - 1]), i_acc);
-                        emit_pd(B, t2.x, __ldg(B.read_scale + ra), ra, hap, out_a + hap);
-                        if (rb >= 0) emit_pd(B, t2.y, __ldg(B.read_scale + rb), rb, hap, out_b + hap);
+                    valid = (c >= 0) && (c < ncols);
+                    code = valid ? code : 0u;
+                    op = valid ? op : 0u;
+                }
+                const float2 shV = shfl_up2(sV);
+                const float2 shW = shfl_up2(sW);
+                float2 uV = pendV;
+                gW = pendW2;
+                pendV = shV;
+                pendW2 = pendW1;
+                pendW1 = shW;
+                if (MULTI && strip > 0) {  // lane 0 takes the strip above's last row (W one step later, as it comes)
+                    if (lane == 0) {
+                        uV = nxV;
+                        gW = l0W;
+                        l0W = nxW;
+                        if (c + 1 < ncols) {
+                            nxV = scratch[2 * (c + 1) + 0];
+                            nxW = scratch[2 * (c + 1) + 1];
+                        }
+                    }
+                } else if (lane == 0) {
+                    uV = zero2();
+                }
+                if constexpr (CHK) {
+                    if (code & kColFirst) {
+                        ++hap;
+                        const float init = __ldg(B.hap_init_f + hap);
+                        const float2 X = make_float2(init, rb >= 0 ? init : 0.f);
+                        const int slot0 = strip * S + lane * K;
+#pragma unroll
+                        for (int k = 0; k < K; ++k) {
+                            Mp[k] = Ip[k] = zero2();
+                            Dp[k] = make_float2((slot0 + k < task.pad_a) ? X.x : 0.f,
+                                                (slot0 + k < task.pad_b) ? X.y : 0.f);
+                        }
+                        const float2 gD = make_float2((slot0 - 1 < task.pad_a) ? X.x : 0.f,
+                                                      (slot0 - 1 < task.pad_b) ? X.y : 0.f);
+                        gW = mul2(cc[0], gD);
+                        if (lane == 0 && strip == 0) w0 = mul2(cc[0], X);
                     }
                 }
+                if (!(MULTI && strip > 0) && lane == 0) gW = w0;
+                auto body = [&](auto ops_tag) {
+                    constexpr bool OPS = decltype(ops_tag)::value;
+                    // branch states at this column, from the previous column's values (still in Mp, Ip, Dp)
+                    if (OPS && (op & (kPdOpCopy | kPdOpAfter))) {
+                        if (op & kPdOpAfter) {
+#pragma unroll
+                            for (int k = 0; k < K; ++k) {
+                                Mp[k] = max2(bst[(3 * k + 0) * 32], Mp[k]);
+                                Ip[k] = max2(bst[(3 * k + 1) * 32], Ip[k]);
+                                Dp[k] = max2(bst[(3 * k + 2) * 32], Dp[k]);
+                            }
+                        }
+                        if (op & kPdOpCopy) {  // (an AFTER_DEL column stores only when a later column reads it)
+#pragma unroll
+                            for (int k = 0; k < K; ++k) {
+                                if (k >= K - 2 && acc_lane) continue;
+                                bst[(3 * k + 0) * 32] = Mp[k];
+                                bst[(3 * k + 1) * 32] = Ip[k];
+                                bst[(3 * k + 2) * 32] = Dp[k];
+                            }
+                        }
+                    }
+                    const uint32_t ref = code & 7u;
+                    const float4 *pri4 = prior_tbl4 + ref * 32;
+                    float2 prs[2 * KP];
+#pragma unroll
+                    for (int kk = 0; kk < KP; ++kk) {
+                        const float4 v = pri4[kk * kBases * 32];
+                        prs[2 * kk] = make_float2(v.x, v.y);
+                        prs[2 * kk + 1] = make_float2(v.z, v.w);
+                    }
+                    if (OPS && (op & kPdOpSnp)) {
+                        const uint32_t alt = (op >> kPdOpAltShift) & 3u;
+                        if (op & kPdOpSnpAllBut) {  // three bases match: all but `alt`
+                            const uint32_t w = alt ? 0u : 1u;
+                            const float4 *pu = prior_tbl4 + alt * 32, *pn = prior_tbl4 + 4 * 32;
+                            const float4 *pw = prior_tbl4 + w * 32;
+#pragma unroll
+                            for (int kk = 0; kk < KP; ++kk) {
+                                const float4 tu = pu[kk * kBases * 32], tn = pn[kk * kBases * 32];
+                                const float4 tw = pw[kk * kBases * 32];
+                                prs[2 * kk] =
+                                    make_float2(all_but_prior(tu.x, tn.x, tw.x), all_but_prior(tu.y, tn.y, tw.y));
+                                prs[2 * kk + 1] =
+                                    make_float2(all_but_prior(tu.z, tn.z, tw.z), all_but_prior(tu.w, tn.w, tw.w));
+                            }
+                        } else {  // two bases match: the column's and `alt`
+                            const uint32_t third = (uint32_t)__ffs(~((1u << ref) | (1u << alt))) - 1u;
+                            const float4 *pa = prior_tbl4 + alt * 32, *pt = prior_tbl4 + third * 32;
+#pragma unroll
+                            for (int kk = 0; kk < KP; ++kk) {
+                                const float4 t2 = pa[kk * kBases * 32], t3 = pt[kk * kBases * 32];
+                                const float2 p0 = prs[2 * kk], p1 = prs[2 * kk + 1];
+                                prs[2 * kk] = make_float2(snp_prior(p0.x, t2.x, t3.x), snp_prior(p0.y, t2.y, t3.y));
+                                prs[2 * kk + 1] = make_float2(snp_prior(p1.x, t2.z, t3.z), snp_prior(p1.y, t2.w, t3.w));
+                            }
+                        }
+                    }
+                    // pass 1 (bottom-up): M~ and D~
+#pragma unroll
+                    for (int k = K - 1; k >= 0; --k) {
+                        const float2 pr = prs[k];
+                        float2 Mn;
+                        if (k) {
+                            Mn = mul2(pr, fma2(Ip[k - 1], cb[k], fma2(Dp[k - 1], cc[k], Mp[k - 1])));
+                        } else {
+                            Mn = mul2(pr, gW);
+                        }
+                        const float2 Dn = fma2(Dp[k], cdd[k], Mp[k]);
+                        Mp[k] = Mn;
+                        Dp[k] = Dn;
+                    }
+                    // pass 2 (top-down): I~ from the row above at this column
+                    Ip[0] = uV;
+                    if (OPS && (op & kPdOpDelEnd)) {
+#pragma unroll
+                        for (int k = 1; k < K; ++k) {
+                            float2 bi = bst[(3 * (k - 1) + 1) * 32], bm = bst[(3 * (k - 1) + 0) * 32];
+                            // the first accumulator row sums row R as is
+                            if (k == K - 2 && acc_lane) bi = bm = zero2();
+                            Ip[k] = fma2(max2(bi, Ip[k - 1]), ce[k], max2(bm, Mp[k - 1]));
+                        }
+                    } else {
+#pragma unroll
+                        for (int k = 1; k < K; ++k) Ip[k] = fma2(Ip[k - 1], ce[k], Mp[k - 1]);
+                    }
+                    // hand-over to the lane below: row 0's I~ at this column and its M~ inner sum for the next column
+                    float2 hI = Ip[K - 1], hM = Mp[K - 1];
+                    // (K = 2: lane 31's row 0 in the last strip is an accumulator row, whose I takes no max)
+                    if (OPS && (op & kPdOpDelEnd) && !(K == 2 && lane == 30 && last_strip)) {
+                        hI = max2(bst[(3 * (K - 1) + 1) * 32], hI);
+                        hM = max2(bst[(3 * (K - 1) + 0) * 32], hM);
+                    }
+                    sV = fma2(hI, e0n, hM);
+                    float2 wI = Ip[K - 1], wD = Dp[K - 1], wM = Mp[K - 1];
+                    if (OPS && (op & kPdOpNextAfter)) {
+                        wI = max2(bst[(3 * (K - 1) + 1) * 32], wI);
+                        wD = max2(bst[(3 * (K - 1) + 2) * 32], wD);
+                        wM = max2(bst[(3 * (K - 1) + 0) * 32], wM);
+                    }
+                    sW = fma2(wI, b0n, fma2(wD, c0n, wM));
+                    if (last_strip) {
+                        if constexpr (CHK) {
+                            if (lane == 31 && (code & kColLast)) {
+                                const float2 i_acc = Ip[K - 2];  // I~(R+1) at this column
+                                const float2 t2 = add2(add2(Dp[K - 1], Mp[K - 1]), i_acc);
+                                emit_pd(B, t2.x, __ldg(B.read_scale + ra), ra, hap, out_a + hap);
+                                if (rb >= 0) emit_pd(B, t2.y, __ldg(B.read_scale + rb), rb, hap, out_b + hap);
+                            }
+                        }
+                    } else if (MULTI && lane == 31 && valid) {
+                        scratch[2 * c + 0] = sV;
+                        scratch[2 * c + 1] = sW;
+                    }
+                };
+                // steps where no lane is at a column with PD work (about two in three) run the regular kernel's step,
+                // without the op tests: 8 % faster than testing the op bits in every step
+                if (__any_sync(kFull, op != 0u))
+                    body(std::true_type{});
+                else
+                    body(std::false_type{});
             };
-            // steps where no lane is at a column with PD work (about two in three) run the regular kernel's step,
-            // without the op tests: 8 % faster than testing the op bits in every step
-            if (__any_sync(kFull, op != 0u))
-                body(std::true_type{});
-            else
-                body(std::false_type{});
-        };
-        // Step loops not unrolled: the lane-divergent op branches and the two step bodies behind the warp vote split
-        // each step into several blocks anyway; unrolled 4 (checked) and 8 (check-free) the steps overflowed the
-        // instruction cache (ncu: 6-8 cycles of "no instruction" stall per issue, half the speed), and with the vote
-        // 2 (check-free) was still 4 % slower than 1
-        const int64_t *hoff = B.hap_off + task.hap_begin;
-        const int nh_task = task.hap_end - task.hap_begin;
-        int s = 0, j = 0;
-        while (s < nsteps) {
-            while (j <= nh_task && (int)(hoff[j] - col0) <= s) ++j;
-            const int window_end = min((int)(hoff[j - 1] - col0) + 63, nsteps);
-            if (s < window_end) {
+            // Step loops not unrolled: the lane-divergent op branches and the two step bodies behind the warp vote
+            // split each step into several blocks anyway; unrolled 4 (checked) and 8 (check-free) the steps overflowed
+            // the instruction cache (ncu: 6-8 cycles of "no instruction" stall per issue, half the speed), and with the
+            // vote 2 (check-free) was still 4 % slower than 1
+            const int64_t *hoff = B.hap_off + task.hap_begin;
+            const int nh_task = task.hap_end - task.hap_begin;
+            int s = 0, j = 0;
+            while (s < nsteps) {
+                while (j <= nh_task && (int)(hoff[j] - col0) <= s) ++j;
+                const int window_end = min((int)(hoff[j - 1] - col0) + 63, nsteps);
+                if (s < window_end) {
 #pragma unroll 1
-                for (; s < window_end; ++s) step(s, std::true_type{});
-                continue;
+                    for (; s < window_end; ++s) step(s, std::true_type{});
+                    continue;
+                }
+                const int next_boundary = (j <= nh_task) ? (int)(hoff[j] - col0) : nsteps;
+#pragma unroll 1
+                for (; s < next_boundary; ++s) step(s, std::false_type{});
             }
-            const int next_boundary = (j <= nh_task) ? (int)(hoff[j] - col0) : nsteps;
-#pragma unroll 1
-            for (; s < next_boundary; ++s) step(s, std::false_type{});
+            if (MULTI) __syncwarp();  // the next strip's lane 0 reads what this strip's lane 31 wrote
         }
     }
 }
@@ -350,51 +399,67 @@ size_t pd_bucket_smem_bytes(int k) {
     return (size_t)(128 / 32) * (((k + 1) / 2) * kBases * 32 * sizeof(float4) + (size_t)k * 3 * 32 * sizeof(float2));
 }
 
-template <int K>
+template <int K, bool MULTI>
 int launch_pd_bucket_k(const DevTables &t, const DevBatch &b, const uint8_t *ops, int grid, cudaStream_t s) {
     const size_t smem = pd_bucket_smem_bytes(K);
     if (smem > 48 * 1024) {
         const cudaError_t e =
-            cudaFuncSetAttribute(pd_bucket_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(pd_bucket_kernel<K, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return (int)e;
     }
-    pd_bucket_kernel<K><<<grid, 128, smem, s>>>(t, b, ops);
+    pd_bucket_kernel<K, MULTI><<<grid, 128, smem, s>>>(t, b, ops);
     return (int)cudaGetLastError();
 }
 
-}  // namespace
-
-int launch_pd_bucket(const DevTables &t, const DevBatch &b, const uint8_t *ops, int k, int grid, cudaStream_t s) {
-    switch (k) {
-        case 2: return launch_pd_bucket_k<2>(t, b, ops, grid, s);
-        case 3: return launch_pd_bucket_k<3>(t, b, ops, grid, s);
-        case 4: return launch_pd_bucket_k<4>(t, b, ops, grid, s);
-        case 5: return launch_pd_bucket_k<5>(t, b, ops, grid, s);
-        case 6: return launch_pd_bucket_k<6>(t, b, ops, grid, s);
-        case 7: return launch_pd_bucket_k<7>(t, b, ops, grid, s);
-        case 8: return launch_pd_bucket_k<8>(t, b, ops, grid, s);
-        default: return (int)cudaErrorInvalidValue;
-    }
-}
-
-int pd_bucket_occupancy(int k, int *blocks_per_sm) {
-    const void *fn = nullptr;
-    switch (k) {
-        case 2: fn = (const void *)pd_bucket_kernel<2>; break;
-        case 3: fn = (const void *)pd_bucket_kernel<3>; break;
-        case 4: fn = (const void *)pd_bucket_kernel<4>; break;
-        case 5: fn = (const void *)pd_bucket_kernel<5>; break;
-        case 6: fn = (const void *)pd_bucket_kernel<6>; break;
-        case 7: fn = (const void *)pd_bucket_kernel<7>; break;
-        case 8: fn = (const void *)pd_bucket_kernel<8>; break;
-        default: return (int)cudaErrorInvalidValue;
-    }
-    const size_t smem = pd_bucket_smem_bytes(k);
+template <int K, bool MULTI>
+int pd_bucket_occupancy_k(int *blocks_per_sm) {
+    const void *fn = (const void *)pd_bucket_kernel<K, MULTI>;
+    const size_t smem = pd_bucket_smem_bytes(K);
     if (smem > 48 * 1024) {  // (above 48 KB the kernel must opt in before the query counts it)
         const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return (int)e;
     }
     return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, 128, smem);
+}
+
+}  // namespace
+
+// key: rows per lane (2..8) in the low bits, 16 for multi-strip tasks, as the regular buckets
+int launch_pd_bucket(const DevTables &t, const DevBatch &b, const uint8_t *ops, int key, int grid, cudaStream_t s) {
+    const bool multi = (key & 16) != 0;
+    switch (key & 15) {
+#define GHMM_PD_BUCKET(KK)                                                  \
+    case KK:                                                                \
+        return multi ? launch_pd_bucket_k<KK, true>(t, b, ops, grid, s)     \
+                     : launch_pd_bucket_k<KK, false>(t, b, ops, grid, s);
+        GHMM_PD_BUCKET(2)
+        GHMM_PD_BUCKET(3)
+        GHMM_PD_BUCKET(4)
+        GHMM_PD_BUCKET(5)
+        GHMM_PD_BUCKET(6)
+        GHMM_PD_BUCKET(7)
+        GHMM_PD_BUCKET(8)
+#undef GHMM_PD_BUCKET
+        default: return (int)cudaErrorInvalidValue;
+    }
+}
+
+int pd_bucket_occupancy(int key, int *blocks_per_sm) {
+    const bool multi = (key & 16) != 0;
+    switch (key & 15) {
+#define GHMM_PD_OCC(KK) \
+    case KK:            \
+        return multi ? pd_bucket_occupancy_k<KK, true>(blocks_per_sm) : pd_bucket_occupancy_k<KK, false>(blocks_per_sm);
+        GHMM_PD_OCC(2)
+        GHMM_PD_OCC(3)
+        GHMM_PD_OCC(4)
+        GHMM_PD_OCC(5)
+        GHMM_PD_OCC(6)
+        GHMM_PD_OCC(7)
+        GHMM_PD_OCC(8)
+#undef GHMM_PD_OCC
+        default: return (int)cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace ghmm

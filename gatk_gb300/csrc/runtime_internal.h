@@ -53,10 +53,8 @@ struct Source {
     // ... or flat planes
     const ghmm_flat *flat = nullptr;
     const RouteBound *bound = nullptr;  // set when the device rewrites the gap penalties after the upload
-    // PD-HMM batches: per region 1 = no read-pair tasks (every pair to the general PD kernel); reads that need more
-    // than one strip get no tasks either
+    // PD-HMM batches: per region 1 = no read-pair tasks (every pair to the general PD kernel)
     const uint8_t *region_direct = nullptr;
-    bool single_strip = false;
 };
 
 }  // namespace rt

@@ -352,6 +352,60 @@ def test_gpu_pdhmm_hand_cases_and_long_reads(engine):
 
 
 @pytest.mark.gpu
+def test_gpu_pdhmm_packed_kernel_reads_of_several_strips(engine):
+    # reads of 260-690 bases (two to four strips of the packed kernel) against 700-1,200-base haplotypes with every
+    # kind of PD column: each strip's last row reaches the next strip through scratch, the PD max included
+    from gatk_gb300 import native
+
+    rng = np.random.default_rng(47)
+    regions, pds = [], []
+    for g in range(12):
+        haps, hpd = [], []
+        first = rng.choice(list(b"ACGT"), size=int(rng.integers(700, 1200))).astype(np.uint8)
+        for h in range(int(rng.integers(1, 3))):
+            hap = first.copy()  # the region's haplotypes: variants of one sequence
+            if h:
+                snv = rng.choice(np.arange(len(hap)), size=5, replace=False)
+                hap[snv] = [[c for c in b"ACGT" if c != hap[k]][0] for k in snv]
+                cut = int(rng.integers(100, len(hap) - 100))
+                hap = np.concatenate([hap[:cut], hap[cut + 3:]])
+            H = len(hap)
+            pd = np.zeros(H, dtype=np.uint8)
+            for _ in range(4):
+                k = int(rng.integers(0, H))
+                pd[k] |= SNP | BIT[[c for c in b"ACGT" if c != hap[k]][int(rng.integers(0, 3))]]
+            for _ in range(3):
+                n = int(rng.integers(1, 10))
+                j = int(rng.integers(1, H - n - 1))
+                pd[j] |= DS
+                pd[j + n - 1] |= DE
+            pd[int(rng.integers(2, H - 2))] |= DS | DE
+            haps.append(bytes(hap))
+            hpd.append(pd)
+        base = np.frombuffer(haps[0], dtype=np.uint8)
+        reads = []
+        for _ in range(int(rng.integers(2, 6))):
+            R = int(rng.integers(260, 690))
+            start = int(rng.integers(0, len(base) - R))
+            rd = base[start:start + R].copy()
+            flip = rng.random(R) < 0.01
+            rd[flip] = rng.choice(list(b"ACGT"), size=int(flip.sum())).astype(np.uint8)
+            reads.append((bytes(rd), rng.integers(25, 41, size=R), rng.integers(30, 46, size=R),
+                          rng.integers(30, 46, size=R), np.full(R, 10)))
+        regions.append((haps, reads))
+        pds.extend(hpd)
+    wl, pd = W.from_pairs(regions), np.concatenate(pds)
+    ref = O.pd_compute_workload(wl, pd)
+    with engine.pd_batch(wl, pd) as b:
+        b.forward(native.MODE_PD_FP32)
+        got = b.results()
+        st = b.stats()
+    assert np.isfinite(ref).all() and st["n_tasks_fp32"] > 0
+    assert st["n_rerun"] < wl.n_pairs // 4  # most pairs stay in the FP32 packed path
+    assert np.abs(got - ref).max() <= 1e-3
+
+
+@pytest.mark.gpu
 def test_gpu_pdhmm_error_in_a_later_chunk(engine):
     # a read base outside ACGTacgtN meets an undetermined SNP in the last of 30 regions: the one-shot call marshals
     # that region's chunk while earlier chunks run, returns GHMM_ERR_ARG, and the engine computes correctly afterwards
