@@ -50,8 +50,10 @@ bool pd_read_base_ok(uint8_t x) {
 }
 
 
-// Whether the packed FP32 kernel (pd_packed.cu) can take a haplotype: its row-end state is NORMAL, so every row, the
-// first included, sees one state sequence.
+// Whether the packed FP32 kernel (pd_packed.cu) can take a haplotype: its row-end state is not INSIDE_DEL.  Row 1
+// starts NORMAL and the later rows start in the previous row's end state; an AFTER_DEL there changes nothing (the
+// first column's inputs from column 0 are zero in every row below row 1, branch states included), so every row
+// sees one state sequence, while an open INSIDE_DEL keeps the later rows' branch states where row 1 renews them.
 static bool pd_packable(const uint8_t *f, int H) {
     int st = 0;
     for (int j = 0; j < H; j++) {
@@ -59,7 +61,7 @@ static bool pd_packable(const uint8_t *f, int H) {
         if (f[j] & 2) st = 1;
         if (f[j] & 4) st = 2;
     }
-    return st == 0;
+    return st != 1;
 }
 
 // The packed kernel's op byte of every column of one haplotype (pd_packed.cu), from its flags f, its bytes y and the
@@ -78,7 +80,7 @@ static void pd_ops(const uint8_t *f, const uint8_t *y, const uint8_t *states, in
         const bool need = st_next == 2 || (st_next == 1 && need_next) || del_end;
         uint32_t o = 0;
         if (st != 1 && need) o |= kPdOpCopy;  // (INSIDE_DEL keeps the branch state it has)
-        if (st == 2) o |= kPdOpAfter;
+        if (st == 2 && j > 0) o |= kPdOpAfter;  // (at the first column AFTER_DEL acts as NORMAL, pd_packable)
         if (del_end) o |= kPdOpDelEnd;
         if (st_next == 2) o |= kPdOpNextAfter;
         const int ref = base_index(y[j]);
@@ -265,7 +267,8 @@ int pd_forward_enqueue(ghmm_ctx *ctx, ghmm_batch &b, bool fp32, cudaStream_t s) 
                               cudaMemcpyHostToDevice, s), "H2D counters");
     b.h_nout.p[0] = b.n_out;
     if (packed)
-        GHMM_CUDA(cudaMemcpyAsync(b.d_nout.p, b.h_nout.p, sizeof(int64_t), cudaMemcpyHostToDevice, s), "H2D output count");
+        GHMM_CUDA(cudaMemcpyAsync(b.d_nout.p, b.h_nout.p, sizeof(int64_t), cudaMemcpyHostToDevice, s),
+                  "H2D output count");
     GHMM_CUDA(cudaEventRecord(b.ev[1], s), "event");
     int launches = 0;
     if (packed) {  // read-pair tasks, then the log10 epilogue of their sums (before the kernels that write log10)
@@ -339,7 +342,8 @@ int pd_pipelined(ghmm_ctx *ctx, const std::vector<int64_t> &cells, const std::ve
                  const std::function<int(int64_t, int64_t, int)> &host,
                  const std::function<int(int, cudaStream_t)> &device) {
     const std::vector<int64_t> cut = pipeline_cuts(cells);
-    if (!ctx->pd_stream2) GHMM_CUDA(cudaStreamCreateWithFlags(&ctx->pd_stream2, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!ctx->pd_stream2)
+        GHMM_CUDA(cudaStreamCreateWithFlags(&ctx->pd_stream2, cudaStreamNonBlocking), "cudaStreamCreate");
     const cudaStream_t streams[2] = {ctx->stream, ctx->pd_stream2};
     const bool fp32 = !ctx->double_precision;
     auto start = [&](size_t i) {
@@ -489,7 +493,8 @@ int ghmm_pd_compute_regions_raw(ghmm_ctx *ctx, const ghmm_pd_raw_region *regions
             RawView &v = views[slot];
             v = RawView();
             std::vector<ghmm_raw_region> rr((size_t)(g1 - g0));
-            for (int64_t g = g0; g < g1; g++) rr[(size_t)(g - g0)] = ghmm_raw_region{regions[g].reads, regions[g].n_reads, nullptr, 0};
+            for (int64_t g = g0; g < g1; g++)
+                rr[(size_t)(g - g0)] = ghmm_raw_region{regions[g].reads, regions[g].n_reads, nullptr, 0};
             int rc = raw_view(ctx, rr.data(), g1 - g0, prep, v);
             if (rc) return rc;
             std::vector<ghmm_pd_region> pr((size_t)(g1 - g0));

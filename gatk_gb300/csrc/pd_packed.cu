@@ -37,8 +37,8 @@
 // Reads longer than 32 K - 2 rows run in strips as in the regular kernel: lane 31 of a strip stores per column its
 // hand-over to the row below (with the PD max where the column asks for it) for lane 0 of the next strip; the
 // accumulator rows and their exclusions belong to the last strip.  The host sends a region to the general PD kernel
-// (pd.cu) instead when a haplotype's state carries from the end of a row into the next row (the first row would then
-// see other states than the rest); reads the regular routing sends to FP64 go there too.  A sum below
+// (pd.cu) instead when a haplotype leaves a deletion open at its last column (the later rows would start INSIDE_DEL,
+// the first row NORMAL); reads the regular routing sends to FP64 go there too.  A sum below
 // GHMM_FP32_RERUN_THRESHOLD (or not finite) queues the pair for the FP64 PD kernel.
 #include <cuda_runtime.h>
 

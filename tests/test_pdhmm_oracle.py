@@ -253,7 +253,10 @@ def test_packed_kernel_ops_hand_cases():
     assert ops[7] == 16 | (2 << 5) and codes[7] == 3
     assert ops[8] == 0 and codes[8] == 4  # every base matches: the column reads as N
     assert ops[9] == 16 | 128 | (3 << 5) and codes[9] == 1
-    pd[9] = DE  # a deletion ending on the last column leaves AFTER_DEL open for the next row
+    pd[9] = DE  # a deletion ending on the last column: the next row starts in AFTER_DEL, which acts as NORMAL there
+    packed, ops, _ = _pd_ops(hap, pd)
+    assert packed and not ops[0] & 2
+    pd[9] = DS  # a deletion left open: the next row starts INSIDE_DEL, for the general kernel
     assert not _pd_ops(hap, pd)[0]
 
 
@@ -504,8 +507,9 @@ def _packed_case_workload(seed=41):
     single-base deletions (DEL_START and DEL_END on one column), a deletion from column 1, a DEL_END on the
     second-to-last column (AFTER_DEL at the last), an AFTER_DEL column that ends another deletion (AFTER_DEL twice in
     a row), SNP columns inside a deletion, an SNP on an N column, SNP columns with two and with three alternatives
-    (three or four matching bases), reads with N; plus one region with a deletion ending on the last column (the
-    state carries into the next row), which the host sends to the general kernel."""
+    (three or four matching bases), reads with N, a deletion ending on the last column (the next row starts in
+    AFTER_DEL); plus one region with a deletion left open at the last column, which the host sends to the general
+    kernel."""
     rng = np.random.default_rng(seed)
     regions, pds = [], []
     lengths = [20, 33, 40, 62, 63, 64, 90, 126, 150, 190, 222, 254]
@@ -555,7 +559,9 @@ def _packed_case_workload(seed=41):
                     pd[j] |= DS
                     pd[j + n - 1] |= DE
             if g == 24 and h == 0:
-                pd[H - 1] |= DE  # the row-end state carries into the next row: general kernel
+                pd[H - 1] |= DS  # a deletion left open at the row's end carries into the next row: general kernel
+            if g == 23 and h == 0:
+                pd[H - 1] |= DE  # the next row starts in AFTER_DEL (the packed kernel takes it)
             if g >= 20:  # SNP columns listing two and three alternatives
                 for k in rng.choice(np.arange(H), size=6, replace=False):
                     others = [c for c in b"ACGT" if c != hap[k]]
