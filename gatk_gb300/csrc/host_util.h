@@ -84,25 +84,32 @@ inline int hw_threads(int requested) {
     return requested > 0 ? std::min(requested, hw) : hw;
 }
 
+// f(i) for i in [0, n) on up to `threads` threads, the calling thread one of them.  Threads take `grain`
+// consecutive indices at a time; grain 0 (the default) takes about a quarter of an even share, at most 64, so
+// that a loop over a few dozen regions or blocks still spreads over all threads.
 template <typename F>
-inline void parallel_for(int64_t n, int threads, F f, int64_t grain = 64) {
+inline void parallel_for(int64_t n, int threads, F f, int64_t grain = 0) {
     if (n <= 0) return;
-    threads = (int)std::min<int64_t>(threads, n);
+    threads = std::max(threads, 1);
+    if (grain <= 0) grain = std::min<int64_t>(64, std::max<int64_t>(1, n / ((int64_t)threads * 4)));
+    threads = (int)std::min<int64_t>(threads, (n + grain - 1) / grain);
     if (threads <= 1) {
         for (int64_t i = 0; i < n; i++) f(i);
         return;
     }
     std::atomic<int64_t> next{0};
+    auto work = [&] {
+        for (;;) {
+            const int64_t i0 = next.fetch_add(grain);
+            if (i0 >= n) break;
+            const int64_t i1 = std::min(n, i0 + grain);
+            for (int64_t i = i0; i < i1; i++) f(i);
+        }
+    };
     std::vector<std::thread> pool;
-    for (int t = 0; t < threads; t++)
-        pool.emplace_back([&] {
-            for (;;) {
-                const int64_t i0 = next.fetch_add(grain);
-                if (i0 >= n) break;
-                const int64_t i1 = std::min(n, i0 + grain);
-                for (int64_t i = i0; i < i1; i++) f(i);
-            }
-        });
+    pool.reserve((size_t)threads - 1);
+    for (int t = 1; t < threads; t++) pool.emplace_back(work);
+    work();
     for (auto &th : pool) th.join();
 }
 

@@ -75,6 +75,11 @@ int queue_launch(ghmm_queue *q, int i, QueueUnit &u) {
         rc = raw_prepare_device(ctx, b, u.mapq.data(), u.max_len, &q->prep, q->stream[i]);
         if (rc) return rc;
     }
+    if (q->serial_fp32) {  // the FP32 pass after the other slot's (its FP64 reruns and copies still overlap)
+        const int o = 1 - i;
+        if (q->inflight[o] && q->slot[o].events_ready)
+            GHMM_CUDA(cudaStreamWaitEvent(q->stream[i], q->slot[o].ev[2], 0), "wait for the previous FP32 pass");
+    }
     rc = batch_enqueue(ctx, b, q->mode, q->stream[i]);
     if (rc) return rc;
     if (b.n_out > 0) {
@@ -228,6 +233,9 @@ int queue_open(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **out, const ghmm_
     auto *q = new ghmm_queue();
     q->ctx = ctx;
     q->batch_cells = batch_cells > 0 ? batch_cells : (int64_t)2e11;
+    // a streaming queue's batches run their FP32 passes in turn (workload 4 through the queue, 30,000 regions in
+    // batches of 2e11 cells: 3,848 against 3,698 GCUPS side by side)
+    q->serial_fp32 = true;
     q->mode = ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN;
     if (raw_prep) queue_set_raw(q, raw_prep, bound);
     for (auto &st : q->stream) {
@@ -305,7 +313,7 @@ std::vector<int64_t> pipeline_cuts(const std::vector<int64_t> &cells) {
     int64_t total = 0;
     for (int64_t c : cells) total += c;
     std::vector<int64_t> cut{0};
-    if (total < (int64_t)5e11) {
+    if (total < kPipelineLargeCells) {
         const int64_t marks[2] = {total / 8, total / 2};
         int64_t c = 0;
         int m = 0;
@@ -345,6 +353,12 @@ int pipelined_compute(ghmm_ctx *ctx, const Source &src, const std::vector<int64_
         q->error_msg.clear();
         q->mode = ctx->double_precision ? GHMM_MODE_FP64 : GHMM_MODE_FP32_RERUN;
         queue_set_raw(q, mapq ? prep : nullptr, bound);
+        // the large schedule's chunks run their FP32 passes in turn: bucket kernels of two such chunks side by side
+        // ran slower than one after the other (workload 1 end to end at 10,000 regions: 290 against 282 ms), while the
+        // small schedule's chunks gain from filling each other's kernel tails (42.4 against 44.5 ms at 1,000 regions)
+        int64_t total = 0;
+        for (int64_t c : reg_cells) total += c;
+        q->serial_fp32 = total >= kPipelineLargeCells;
     }
     const int64_t G = src.n_regions;
     std::vector<int64_t> first_read;  // raw reads: the batch's reads' mapping qualities go with the batch

@@ -259,6 +259,8 @@ struct ghmm_queue {
     std::vector<double> str_tables;
     bool has_bound = false;
     RouteBound bound;
+    // each batch's kernels wait for the FP32 pass of the batch in the other slot (streaming queues, large pipelined calls)
+    bool serial_fp32 = false;
     // worker-owned
     ghmm_batch slot[2];
     cudaStream_t stream[2]{};
@@ -314,6 +316,8 @@ int pipelined_compute(ghmm_ctx *ctx, const Source &src, const std::vector<int64_
                       int32_t max_len = 0, const ghmm_read_prep *prep = nullptr, const RouteBound *bound = nullptr);
 bool region_sizes(const Source &src, std::vector<int64_t> &cells, std::vector<int64_t> &outo);
 int compute_sync(ghmm_ctx *ctx, const Source &src, double *out);
+// cells from which a pipelined call takes the large schedule (growing chunks, FP32 passes in turn)
+constexpr int64_t kPipelineLargeCells = (int64_t)5e11;
 std::vector<int64_t> pipeline_cuts(const std::vector<int64_t> &cells);  // region cuts of a pipelined call
 
 // pd_host.cpp
