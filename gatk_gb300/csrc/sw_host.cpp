@@ -367,7 +367,7 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
     std::vector<Part> parts((size_t)nparts);
     const int64_t per = (n + nparts - 1) / nparts;
     parallel_for(nparts, nparts, [&](int64_t t) {
-        Part &q = parts[(size_t)t];
+        Part q;  // (filled locally: neighbouring parts share cache lines)
         for (int64_t i = t * per; i < std::min(n, (t + 1) * per); ++i) {
             const SwPair &P = E.h_pairs.p[i];
             const bool runs = E.h_res.p[i] == 0 && P.ref_len > 0;
@@ -382,6 +382,7 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
                 q.max_alt = std::max<int64_t>(q.max_alt, P.alt_len);
             }
         }
+        parts[(size_t)t] = q;
     }, 1);
     Part tot;
     for (auto &q : parts) {
@@ -580,16 +581,19 @@ int deliver(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, int64_t n, const int3
     std::vector<int64_t> n_short((size_t)parts, 0), cells((size_t)parts, 0);
     const int64_t per = (n + parts - 1) / parts;
     parallel_for(parts, parts, [&](int64_t t) {
+        int64_t my_short = 0, my_cells = 0;  // (counted locally: neighbouring parts' totals share a cache line)
         for (int64_t i = t * per; i < std::min(n, (t + 1) * per); ++i) {
             res->alignment_offset[i] = offset[i];
             res->cigar_start[i] = E.h_starts.p[i];
             res->cigar_len[i] = nops[i];
             if (ref_len_of && ref_len_of[i] <= 0) continue;  // not aligned
             if (state[i] == 1)
-                ++n_short[(size_t)t];
+                ++my_short;
             else if (ref_len_of)
-                cells[(size_t)t] += (int64_t)ref_len_of[i] * E.h_pairs.p[i].alt_len;
+                my_cells += (int64_t)ref_len_of[i] * E.h_pairs.p[i].alt_len;
         }
+        n_short[(size_t)t] = my_short;
+        cells[(size_t)t] = my_cells;
         // this part's share of the cigar ops
         const int64_t o0 = total * t / parts, o1 = total * (t + 1) / parts;
         if (o1 > o0) std::memcpy(res->cigar_ops + o0, E.h_ops.p + o0, (size_t)(o1 - o0) * sizeof(uint32_t));
@@ -812,16 +816,16 @@ int ghmm_batch_realign(ghmm_ctx *ctx, ghmm_batch *batch, const double *hap_prior
     const int64_t *read_off = bi.h_off;
     SW_CUDA(E.h_pairs.reserve((size_t)n), "pinned pairs");
     // the reads; their haplotypes are chosen on the device (reads of a region without haplotypes are not aligned)
+    std::atomic<bool> empty_read{false};
     parallel_for(n, ci.threads, [&](int64_t r) {
         SwPair &P = E.h_pairs.p[r];
         P = SwPair{};
         P.alt_off = read_off[r];
         P.alt_len = (int32_t)(read_off[r + 1] - read_off[r]);
+        if (P.alt_len <= 0) empty_read.store(true, std::memory_order_relaxed);
     }, 4096);
-    for (int64_t r = 0; r < n; ++r)
-        if (E.h_pairs.p[r].alt_len <= 0)
-            return ctx_fail(ctx, GHMM_ERR_ARG,
-                            "Non-null, non-empty sequences are required for the Smith-Waterman calculation");
+    if (empty_read.load())
+        return ctx_fail(ctx, GHMM_ERR_ARG, "Non-null, non-empty sequences are required for the Smith-Waterman calculation");
     RunIn in{};
     in.ref_plane = bi.dev->hap_bases;
     in.alt_plane = bi.dev->bases;
@@ -838,11 +842,11 @@ int ghmm_batch_realign(ghmm_ctx *ctx, ghmm_batch *batch, const double *hap_prior
     if (rc) return rc;
     const int32_t *best = E.h_res.p + 3 * n;
     std::vector<int32_t> ref_len((size_t)n);
-    for (int64_t r = 0; r < n; ++r) {
+    parallel_for(n, ci.threads, [&](int64_t r) {
         best_hap[r] = best[r];
         informative[r] = inf[(size_t)r];
         ref_len[(size_t)r] = E.h_pairs.p[r].ref_len;  // the chosen haplotype's length (0: not aligned)
-    }
+    }, 4096);
     rc = deliver(ctx, ci, E, n, ref_len.data(), result);
     E.stats.d2h_bytes += n * (int64_t)sizeof(int32_t);
     E.stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -282,3 +282,71 @@ def test_unbounded_scores_stay_in_int32(aligner):
     got = aligner.align_many(refs, alts, SWG.NEW_SW_PARAMETERS, SWG.SWOverhangStrategy.SOFTCLIP, False)
     assert aligner.last_stats()["n_int16"] == 0
     _assert_same(got, refs, alts, S.NEW_SW_PARAMETERS, S.SOFTCLIP, False)
+
+
+def _native_pairs(ref_buf, ref_pos, ref_len, alts):
+    """SwPair array of refs at ref_buf[ref_pos[i]:ref_pos[i] + ref_len[i]] against alts (kept alive by the caller)."""
+    abuf = np.frombuffer(b"".join(alts), dtype=np.uint8)
+    aoff = np.cumsum([0] + [len(a) for a in alts])
+    pairs = (native.SwPair * len(alts))()
+    for i in range(len(alts)):
+        pairs[i] = native.SwPair(ref_buf.ctypes.data + int(ref_pos[i]), abuf.ctypes.data + int(aoff[i]),
+                                 int(ref_len[i]), len(alts[i]))
+    return pairs, abuf
+
+
+def test_batch_call_shares_refs_across_blocks_of_pairs(aligner):
+    # 20,000 pairs: the call checks and deduplicates its refs in several blocks of pairs at once.  Six haplotypes in
+    # one buffer, every block pointing at the same ones, three pairs in ten at a prefix of one (the same address with a
+    # shorter length, a different ref); the alignments must equal the oracle's on the same bytes
+    rng = random.Random(41)
+    haps = [bytes(rng.choice(b"ACGT") for _ in range(rng.randint(150, 300))) for _ in range(6)]
+    buf = np.frombuffer(b"".join(haps), dtype=np.uint8)
+    hoff = np.cumsum([0] + [len(h) for h in haps])
+    refs, alts, pos, lens = [], [], [], []
+    for _ in range(20000):
+        h = rng.randrange(len(haps))
+        n_ref = len(haps[h]) if rng.random() < 0.7 else rng.choice((60, 100, 140))
+        ref = haps[h][:n_ref]
+        m = rng.randint(20, min(120, n_ref))
+        a0 = rng.randint(0, n_ref - m)
+        alt = _mutate(rng, ref[a0:a0 + m], b"ACGT", 0.03, 0.01) or b"A"
+        refs.append(ref)
+        alts.append(alt)
+        pos.append(hoff[h])
+        lens.append(n_ref)
+    pairs, keep = _native_pairs(buf, pos, lens, alts)
+    n = len(alts)
+    L = aligner._ctx.L
+    res, off, start, length, ops = SWG._result(n, int(L.ghmm_sw_cigar_bound(pairs, n)))
+    p = S.ALIGNMENT_TO_BEST_HAPLOTYPE_SW_PARAMETERS
+    native.check(L.ghmm_sw_align_batch(aligner.handle, pairs, n, SWG.SWParameters(*p).as_native(), S.SOFTCLIP,
+                                       native.SW_SUBSTRING_SHORTCUT, res), aligner.handle)
+    got = SWG.AlignmentBatch(off[:n], start[:n], length[:n], ops[:res.cigar_total])
+    _assert_same(got, refs, alts, p, S.SOFTCLIP, True)
+    # each of the 24 distinct refs goes up once per block, not once per pair (besides the planes: 64-byte pairs up
+    # twice and once more per pass, at most 8 task bytes a pair)
+    assert aligner.last_stats()["h2d_bytes"] < sum(len(a) for a in alts) + sum(lens) // 4 + 200 * n
+
+
+def test_batch_call_reports_the_first_bad_pair(aligner):
+    # a ref longer than GHMM_SW_MAX_LEN at pair 9,000 and an empty alt at pair 15,000, in different blocks of the
+    # call's parallel checks: the first one is reported, and nothing is aligned
+    n, max_len = 20000, 1 << 20
+    buf = np.frombuffer(b"ACGT" * (max_len // 4 + 1), dtype=np.uint8)
+    lens = [40] * n
+    lens[9000] = max_len + 1
+    alts = [b"CGTACGTA"] * n
+    pairs, keep = _native_pairs(buf, [0] * n, lens, alts)
+    pairs[15000] = native.SwPair(buf.ctypes.data, None, 40, 0)
+    L = aligner._ctx.L
+    res, off, start, length, ops = SWG._result(n, int(4 * n * 16))
+    p = SWG.ORIGINAL_DEFAULT.as_native()
+    rc = L.ghmm_sw_align_batch(aligner.handle, pairs, n, p, S.SOFTCLIP, 0, res)
+    assert rc == native.GHMM_ERR_ARG and "GHMM_SW_MAX_LEN" in native.last_error(aligner.handle)
+    pairs[9000] = native.SwPair(buf.ctypes.data, keep.ctypes.data, 40, 8)
+    rc = L.ghmm_sw_align_batch(aligner.handle, pairs, n, p, S.SOFTCLIP, 0, res)
+    assert rc == native.GHMM_ERR_ARG and "non-empty sequences" in native.last_error(aligner.handle)
+    pairs[15000] = native.SwPair(buf.ctypes.data, keep.ctypes.data, 40, 8)
+    native.check(L.ghmm_sw_align_batch(aligner.handle, pairs, n, p, S.SOFTCLIP, 0, res), aligner.handle)
+    assert len(set(off[:n].tolist())) == 1 and len(set(length[:n].tolist())) == 1
