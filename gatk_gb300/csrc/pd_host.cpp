@@ -131,7 +131,7 @@ int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch 
                 break;
             }
         }
-    }, 16);
+    });
     Source src;
     src.regions = rr.data();
     src.n_regions = G;
@@ -175,7 +175,7 @@ int pd_marshal(ghmm_ctx *ctx, const ghmm_pd_region *regs, int64_t G, ghmm_batch 
                 for (int64_t j = hap_off[h]; j < hap_off[h + 1]; j++)
                     if ((flags[j] & 1) && hraw[j] != x && hraw[j] != 'N') unexpected = true;
         }
-    }, 16);
+    });
     if (unexpected) return fail(ctx, GHMM_ERR_ARG, "Found unexpected base in alt alleles");
     b.has_pd = true;
     return GHMM_OK;

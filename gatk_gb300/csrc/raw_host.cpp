@@ -99,7 +99,7 @@ int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_re
     std::vector<int32_t> region_max((size_t)G, 0);
     parallel_for(G, threads, [&](int64_t g) {
         bad[(size_t)g] = (int8_t)raw_region_problem(raw[g], &region_max[(size_t)g]);
-    }, 16);
+    });
     int32_t max_len = 0;
     std::vector<int64_t> first((size_t)G + 1, 0);
     for (int64_t g = 0; g < G; g++) {
@@ -126,7 +126,7 @@ int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_re
             mq[r] = rd.mapping_quality;
         }
         v.regions[(size_t)g] = ghmm_region{rr, rg.n_reads, rg.haps, rg.n_haps};
-    }, 16);
+    });
     return GHMM_OK;
 }
 

@@ -357,7 +357,7 @@ int run(ghmm_ctx *ctx, const CtxInfo &ci, SwEngine &E, const RunIn &in, int64_t 
                     P.ref_len = (int32_t)(hap_off[h + 1] - hap_off[h]);
                 }
             }
-        }, 256);
+        });
     }
     // totals and maxima for the buffers and the clamp decision
     struct Part {
