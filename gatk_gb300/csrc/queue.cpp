@@ -304,8 +304,9 @@ std::unique_ptr<QueueUnit> borrowed_unit(const Source &src, int64_t g0, int64_t 
 // the device after its upload.
 // Region cuts [0 = c_0 < c_1 < ... = G] of a pipelined call over regions of the given cells.  Below 5e11 cells: three
 // chunks, after 1/8 and 1/2 of the cells, because each chunk's launches, graph capture and kernel tails cost a fixed
-// time (workload 1 end to end through ghmm_compute_regions: 45.6 ms against 58.9 ms for the finer cut at 1,000
-// regions, 95.6 against 101.5 ms at 3,000).  Above: 1/16 of the cells first, each next chunk 2.5 times the last up to
+// time (workload 1 end to end through ghmm_compute_regions: 95.6 ms against 101.5 ms for the finer cut at 3,000
+// regions; the regular calls run below 1.5e11 cells as one batch, the one-shot PD-HMM calls in chunks down to 8
+// regions, which gain or lose nothing measurable against one chunk at 1,000 regions).  Above: 1/16 of the cells first, each next chunk 2.5 times the last up to
 // 1/3, so the first marshal the device waits for stays short (281.5 ms against 285.8 ms for three chunks at 10,000
 // regions).  No cut leaves fewer than 8 regions behind it.
 std::vector<int64_t> pipeline_cuts(const std::vector<int64_t> &cells) {

@@ -301,8 +301,10 @@ int pd_forward_enqueue(ghmm_ctx *ctx, ghmm_batch &b, bool fp32, cudaStream_t s);
 int pd_forward_finish(ghmm_ctx *ctx, ghmm_batch &b);
 
 // queue.cpp.  Large synchronous inputs run as a pipeline of batches through the context's own queue: the first
-// batch is small so that the GPU starts early, later ones grow to a third of the input.
-constexpr int64_t kPipelineMinCells = (int64_t)6e10;
+// batch is small so that the GPU starts early, later ones grow to a third of the input.  Below 1.5e11 cells one batch
+// is faster, the marshal being shorter than what the extra batches' launches and kernel tails cost (workload 1 end to
+// end at 1,000 regions, 1.09e11 cells: 38.7 ms in one batch against 42.4 ms in three).
+constexpr int64_t kPipelineMinCells = (int64_t)1.5e11;
 int queue_open(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **out, const ghmm_read_prep *raw_prep = nullptr,
                const RouteBound *bound = nullptr);
 void queue_close(ghmm_queue *q);

@@ -185,7 +185,7 @@ int ghmm_done(ghmm_ctx *ctx);
 int ghmm_last_error(const ghmm_ctx *ctx, char *buf, size_t buf_len);
 
 /* Batcher: many regions in one call (regions of HaplotypeCallerEngine.callRegion batched together).
- * out receives each region's read-major block back to back, in region order.  Inputs of 6e10 cells or
+ * out receives each region's read-major block back to back, in region order.  Inputs of 1.5e11 cells or
  * more run as a pipeline of batches (the first small, later ones up to a third of the input) on the
  * context's internal queue, so that marshalling overlaps the kernels; the results are the same. */
 int ghmm_compute_regions(ghmm_ctx *ctx, const ghmm_region *regions, int32_t n_regions, double *out);

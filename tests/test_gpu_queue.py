@@ -22,8 +22,8 @@ def _one_batch(engine, wl, mode=native.MODE_FP32_RERUN):
 
 
 def test_pipelined_compute_regions_matches_one_batch(engine):
-    wl = W.generate(1, regions=700)  # about 7e10 cells: above the pipelining threshold of 6e10
-    assert int(wl.cells_per_region().sum()) >= 6e10
+    wl = W.generate(1, regions=1500)  # about 1.6e11 cells: above the pipelining threshold of 1.5e11
+    assert int(wl.cells_per_region().sum()) >= 1.5e11
     ref = _one_batch(engine, wl)
     got = engine.compute(wl, via_regions=True)
     np.testing.assert_array_equal(got, ref)

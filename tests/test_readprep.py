@@ -454,13 +454,13 @@ def test_c_restatement_matches_the_python_one(mode):
 @pytest.mark.gpu
 @pytest.mark.parametrize("kind", ["pcr", "dragstr"])
 def test_large_raw_call_is_pipelined_with_identical_results(engine, kind):
-    # ghmm_compute_regions_raw on more than 6e10 cells runs as a pipeline of batches through the context's queue, each
-    # prepared on the device after its upload; a region's results do not depend on the batching
-    wl = W.generate(1, regions=700)
+    # ghmm_compute_regions_raw on more than 1.5e11 cells runs as a pipeline of batches through the context's queue,
+    # each prepared on the device after its upload; a region's results do not depend on the batching
+    wl = W.generate(1, regions=1500)
     rng = np.random.default_rng(61)
     wl.quals[:] = rng.integers(2, 45, size=len(wl.quals)).astype(np.uint8)
     mapq = rng.integers(10, 70, size=wl.n_reads)
-    assert wl.cells() >= 6e10
+    assert wl.cells() >= 1.5e11
     kw = {"dragstr": EXAMPLE} if kind == "dragstr" else {"pcr_rate_factor": 3.0}
     got = engine.compute_raw(wl, mapq, **kw)
     with engine.raw_batch(wl, mapq, **kw) as b:
