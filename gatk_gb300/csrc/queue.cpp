@@ -388,38 +388,49 @@ int pipelined_compute(ghmm_ctx *ctx, const Source &src, const std::vector<int64_
     return GHMM_OK;
 }
 
-// Per-region cells and output offsets of a region array or flat input; false if a count is negative.
-bool region_sizes(const Source &src, std::vector<int64_t> &cells, std::vector<int64_t> &outo) {
+// Per-region cells and output offsets of a region array or flat input; false if a count is negative or a region's
+// array is NULL.  The counts are checked in region order first (nothing past the first bad region is read); then a
+// region array's read and haplotype lengths are summed with the regions in parallel.
+bool region_sizes(const Source &src, std::vector<int64_t> &cells, std::vector<int64_t> &outo, int threads) {
     const int64_t G = src.n_regions;
     cells.assign((size_t)G, 0);
     outo.assign((size_t)G + 1, 0);
     for (int64_t g = 0; g < G; g++) {
-        int64_t sr = 0, sh = 0, nr, nh;
+        int64_t nr, nh;
         if (src.flat) {
             const ghmm_flat *f = src.flat;
             nr = f->region_read_off[g + 1] - f->region_read_off[g];
             nh = f->region_hap_off[g + 1] - f->region_hap_off[g];
             if (nr < 0 || nh < 0) return false;
-            sr = f->read_off[f->region_read_off[g + 1]] - f->read_off[f->region_read_off[g]];
-            sh = f->hap_off[f->region_hap_off[g + 1]] - f->hap_off[f->region_hap_off[g]];
         } else {
             const ghmm_region &rg = src.regions[g];
             nr = rg.n_reads;
             nh = rg.n_haps;
             if (nr < 0 || nh < 0 || (nr > 0 && !rg.reads) || (nh > 0 && !rg.haps)) return false;
+        }
+        outo[(size_t)g + 1] = outo[(size_t)g] + nr * nh;
+    }
+    parallel_for(G, src.flat ? 1 : threads, [&](int64_t g) {
+        int64_t sr = 0, sh = 0;
+        if (src.flat) {
+            const ghmm_flat *f = src.flat;
+            sr = f->read_off[f->region_read_off[g + 1]] - f->read_off[f->region_read_off[g]];
+            sh = f->hap_off[f->region_hap_off[g + 1]] - f->hap_off[f->region_hap_off[g]];
+        } else {
+            const ghmm_region &rg = src.regions[g];
             for (int32_t r = 0; r < rg.n_reads; r++) sr += std::max(rg.reads[r].length, 0);
             for (int32_t h = 0; h < rg.n_haps; h++) sh += std::max(rg.haps[h].length, 0);
         }
         cells[(size_t)g] = sr * sh;
-        outo[(size_t)g + 1] = outo[(size_t)g] + nr * nh;
-    }
+    });
     return true;
 }
 
 // Synchronous compute of regions or flat input: one batch for small inputs, the pipeline for large ones.
 int compute_sync(ghmm_ctx *ctx, const Source &src, double *out) {
     std::vector<int64_t> cells, outo;
-    if (!region_sizes(src, cells, outo)) return fail(ctx, GHMM_ERR_ARG, "negative count or NULL array in a region");
+    if (!region_sizes(src, cells, outo, hw_threads(ctx->max_threads)))
+        return fail(ctx, GHMM_ERR_ARG, "negative count or NULL array in a region");
     int64_t total = 0;
     for (auto c : cells) total += c;
     if (outo.back() > 0 && !out) return fail(ctx, GHMM_ERR_ARG, "NULL output");

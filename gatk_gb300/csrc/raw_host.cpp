@@ -113,11 +113,11 @@ int raw_view(ghmm_ctx *ctx, const ghmm_raw_region *raw, int64_t G, const ghmm_re
     v.q45.assign((size_t)std::max(max_len, 1), 45);
     v.qgcp.assign((size_t)std::max(max_len, 1), (uint8_t)prep->gcp);
     v.regions.resize((size_t)G);
-    v.reads.resize((size_t)first[(size_t)G]);
+    v.reads.reset(new ghmm_read[(size_t)std::max<int64_t>(first[(size_t)G], 1)]);
     v.mapq.resize((size_t)first[(size_t)G]);
     parallel_for(G, threads, [&](int64_t g) {
         const ghmm_raw_region &rg = raw[g];
-        ghmm_read *rr = v.reads.data() + first[(size_t)g];
+        ghmm_read *rr = v.reads.get() + first[(size_t)g];
         int32_t *mq = v.mapq.data() + first[(size_t)g];
         for (int32_t r = 0; r < rg.n_reads; r++) {
             const ghmm_raw_read &rd = rg.reads[r];
@@ -248,7 +248,8 @@ int ghmm_compute_regions_raw(ghmm_ctx *ctx, const ghmm_raw_region *regions, int3
     src.bound = v.has_bound ? &v.bound : nullptr;
     {  // large inputs: the pipeline of batches, each prepared on the device after its upload
         std::vector<int64_t> cells, outo;
-        if (!region_sizes(src, cells, outo)) return fail(ctx, GHMM_ERR_ARG, "negative count or NULL array in a region");
+        if (!region_sizes(src, cells, outo, hw_threads(ctx->max_threads)))
+            return fail(ctx, GHMM_ERR_ARG, "negative count or NULL array in a region");
         int64_t total = 0;
         for (auto c : cells) total += c;
         if (outo.back() > 0 && !out) return fail(ctx, GHMM_ERR_ARG, "NULL output");

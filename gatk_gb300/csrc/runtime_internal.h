@@ -274,7 +274,8 @@ namespace rt {
 
 struct RawView {
     std::vector<ghmm_region> regions;
-    std::vector<ghmm_read> reads;  // every region's reads, region after region
+    std::unique_ptr<ghmm_read[]> reads;  // every region's reads, region after region (each entry written once, in
+                                         // parallel: not zero-filled first)
     std::vector<uint8_t> q45, qgcp;  // shared constant planes
     std::vector<int32_t> mapq;
     int32_t max_len = 0;
@@ -316,7 +317,7 @@ int queue_wait_all(ghmm_queue *q);
 int pipelined_compute(ghmm_ctx *ctx, const Source &src, const std::vector<int64_t> &reg_cells,
                       const std::vector<int64_t> &reg_out, double *out, const int32_t *mapq = nullptr,
                       int32_t max_len = 0, const ghmm_read_prep *prep = nullptr, const RouteBound *bound = nullptr);
-bool region_sizes(const Source &src, std::vector<int64_t> &cells, std::vector<int64_t> &outo);
+bool region_sizes(const Source &src, std::vector<int64_t> &cells, std::vector<int64_t> &outo, int threads);
 int compute_sync(ghmm_ctx *ctx, const Source &src, double *out);
 // cells from which a pipelined call takes the large schedule (growing chunks, FP32 passes in turn)
 constexpr int64_t kPipelineLargeCells = (int64_t)5e11;
