@@ -449,6 +449,16 @@ int compute_sync(ghmm_ctx *ctx, const Source &src, double *out) {
 
 extern "C" {
 
+int ghmm_debug_pipeline_cuts(const int64_t *cells, int64_t n_regions, int64_t *cuts, int64_t cap, int64_t *n_cuts) {
+    if (n_regions < 0 || (n_regions > 0 && !cells) || cap < 0 || (cap > 0 && !cuts) || !n_cuts) return GHMM_ERR_ARG;
+    for (int64_t g = 0; g < n_regions; g++)
+        if (cells[g] < 0) return GHMM_ERR_ARG;
+    const std::vector<int64_t> cut = pipeline_cuts(std::vector<int64_t>(cells, cells + n_regions));
+    *n_cuts = (int64_t)cut.size();
+    for (int64_t i = 0; i < std::min<int64_t>(cap, (int64_t)cut.size()); i++) cuts[i] = cut[(size_t)i];
+    return GHMM_OK;
+}
+
 int ghmm_queue_create(ghmm_ctx *ctx, int64_t batch_cells, ghmm_queue **queue) {
     if (!ctx || !ctx->alive) return GHMM_ERR_STATE;
     if (!queue || batch_cells < 0) return fail(ctx, GHMM_ERR_ARG, "bad arguments");

@@ -251,6 +251,7 @@ _SIGS = {
     "ghmm_measure_peaks": (ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p]),
     "ghmm_debug_tables": (ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p]),
     "ghmm_debug_pd_ops": (ctypes.c_int, [_u8p, _u8p, ctypes.c_int32, _u8p, _u8p]),
+    "ghmm_debug_pipeline_cuts": (ctypes.c_int, [_i64p, ctypes.c_int64, _i64p, ctypes.c_int64, _i64p]),
     "ghmm_str_analyze": (ctypes.c_int, [_u8p, ctypes.c_int32, ctypes.c_int32, _i32p, _i32p, _i32p]),
     "ghmm_calib_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CalibBatch), ctypes.c_int32, ctypes.c_void_p]),
     "ghmm_calib_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CalibBatch), ctypes.c_int32, ctypes.c_void_p,

@@ -402,6 +402,14 @@ int ghmm_debug_tables(ghmm_ctx *ctx, double *err, double *prob, double *m2m);
  * the general PD kernel, GHMM_ERR_ARG for bad arguments. */
 int ghmm_debug_pd_ops(const uint8_t *bases, const uint8_t *pd_flags, int32_t H, uint8_t *ops, uint8_t *codes);
 
+/* Debug/test (no device needed): the chunks a pipelined call cuts regions of these cells into (ghmm_compute_regions,
+ * _flat and _raw on inputs of 1.5e11 cells or more; the one-shot PD-HMM calls on every input): cuts[0] = 0 <
+ * cuts[1] < ... = n_regions, chunk i being regions [cuts[i], cuts[i + 1]).  Below 5e11 cells the cuts fall where
+ * the running sum of cells first reaches 1/8 and 1/2 of the total; from 5e11, the first chunk takes 1/16 of the cells
+ * and each next one 2.5 times the last, up to 1/3.  No cut leaves fewer than 8 regions behind it.  Writes
+ * min(cap, *n_cuts) entries; GHMM_ERR_ARG for a negative count or cell number or a NULL array. */
+int ghmm_debug_pipeline_cuts(const int64_t *cells, int64_t n_regions, int64_t *cuts, int64_t cap, int64_t *n_cuts);
+
 /* ---- Several devices from one caller ----
  * One handle drives several GPUs (HaplotypeCaller's one JVM; the reference parallelises the host side with GKL's
  * thread count, HC/PairHMMNativeArgumentCollection.java:11-12, or one engine per Spark partition,

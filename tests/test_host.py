@@ -260,3 +260,75 @@ def test_str_matches_bruteforce(seq):
             if exp[p - 1] > best_r:
                 best_p, best_r = p, exp[p - 1]
         assert (bp[pos], br[pos]) == (best_p, best_r)
+
+
+def _pipeline_cuts(cells):
+    """The library's chunk rule restated: below 5e11 cells, cuts where the running sum first reaches 1/8 and 1/2 of
+    the total; from 5e11, chunks of 1/16 of the cells growing 2.5 times up to 1/3; no cut leaves fewer than 8 regions
+    behind it."""
+    G, total, cut = len(cells), int(sum(cells)), [0]
+    if total < 500_000_000_000:
+        marks, c, m = (total // 8, total // 2), 0, 0
+        for g in range(G):
+            if m >= 2:
+                break
+            c += int(cells[g])
+            if c >= marks[m] and G - g - 1 >= 8:
+                cut.append(g + 1)
+                m += 1
+        return cut + [G]
+    target, g0 = max(total // 16, 1), 0
+    while g0 < G:
+        g1, c = g0, 0
+        while g1 < G and (c < target or g1 == g0):
+            c += int(cells[g1])
+            g1 += 1
+        if G - g1 < 8:
+            g1 = G
+        cut.append(g1)
+        target = min(target * 5 // 2, max(total // 3, 1))
+        g0 = g1
+    return cut
+
+
+def _library_cuts(cells):
+    cells = np.ascontiguousarray(cells, dtype=np.int64)
+    out = np.zeros(len(cells) + 2, dtype=np.int64)
+    n = ctypes.c_int64(0)
+    p = ctypes.POINTER(ctypes.c_int64)
+    rc = native.lib().ghmm_debug_pipeline_cuts(cells.ctypes.data_as(p), len(cells), out.ctypes.data_as(p), len(out),
+                                               ctypes.byref(n))
+    assert rc == 0
+    return out[: n.value].tolist()
+
+
+def test_pipeline_cuts_of_a_pipelined_call():
+    # three chunks at 1/8 and 1/2 of the cells below 5e11; growing chunks above; no cut with fewer than 8 regions after
+    assert _library_cuts([10**8] * 1000) == [0, 125, 500, 1000]
+    assert _library_cuts([10**8] * 12) == [0, 2, 12]  # the 1/2 cut would leave 6 regions
+    assert _library_cuts([10**8] * 10000) == [0, 625, 2188, 5522, 8856, 10000]
+    assert _library_cuts([10**8] * 5) == [0, 5]
+    wl_cells = W.generate(1, regions=1000).cells_per_region()
+    cuts = _library_cuts(wl_cells)
+    assert len(cuts) == 4 and wl_cells[: cuts[1]].sum() >= wl_cells.sum() // 8
+    rng = np.random.default_rng(5)
+    for _ in range(200):
+        G = int(rng.integers(1, 3000))
+        scale = 10 ** int(rng.integers(6, 11))
+        cells = rng.integers(0, 4, size=G) * rng.integers(1, 1000, size=G) * scale
+        got = _library_cuts(cells)
+        assert got == _pipeline_cuts(cells)
+        assert got[0] == 0 and got[-1] == G and all(a < b for a, b in zip(got, got[1:]))
+        assert all(G - c >= 8 for c in got[1:-1])
+
+
+def test_pipeline_cuts_arguments():
+    p = ctypes.POINTER(ctypes.c_int64)
+    cells = np.array([5, -1, 7], dtype=np.int64)
+    out = np.zeros(8, dtype=np.int64)
+    n = ctypes.c_int64(0)
+    L = native.lib()
+    assert L.ghmm_debug_pipeline_cuts(cells.ctypes.data_as(p), 3, out.ctypes.data_as(p), 8, ctypes.byref(n)) != 0
+    cells = np.full(1000, 10**8, dtype=np.int64)
+    assert L.ghmm_debug_pipeline_cuts(cells.ctypes.data_as(p), 1000, out.ctypes.data_as(p), 2, ctypes.byref(n)) == 0
+    assert n.value == 4 and out[:2].tolist() == [0, 125] and out[2] == 0  # the count of all, the first cap written
